@@ -1,0 +1,508 @@
+"""``set_device('b200')``: the Brian2 device plugin of the GB300 step engine.
+
+Import this module (or ``import brian2_gb300`` after ``brian2``) to register the
+device; scripts then only change their ``set_device`` call.
+
+How the work is split with Brian's own machinery (the device subclasses
+``CPPStandaloneDevice``, ``brian2/devices/cpp_standalone/device.py:168``):
+
+* everything that is not the clock-driven step loop -- array initialisation,
+  ``Synapses.connect``, variable setting with expressions and random numbers --
+  is generated, compiled and run exactly as by ``cpp_standalone``, so the
+  constructed network is the reference's, bit for bit;
+* the code objects of the step loop (templates ``stateupdate``, ``threshold``,
+  ``reset``, ``synapses``, ``synapses_push_spikes``, ``spikemonitor``,
+  ``ratemonitor``, ``statemonitor``) are translated by
+  :class:`B200CodeGenerator` and collected into a network *spec*; ``run()``
+  records the run instead of queueing ``Network::run`` into ``main``;
+* after ``main`` has run, the recorded runs execute on the GPU through the
+  ctypes C ABI (:mod:`brian2_gb300.runtime`), and the final state and monitor
+  contents are written into the standalone results directory in the
+  reference's file format, so ``get_value`` / ``SpikeMonitor.t`` etc. work
+  unchanged (``device.py:544-585``).
+
+Limits (raise ``NotImplementedError``, which Brian's test runner treats as
+"not supported by this device"): one clock for all step-loop objects; no host
+code between two ``run()`` calls; random numbers inside the step loop; on_pre
+statements that write a postsynaptic/presynaptic variable other than by
+``+=``/``-=``; on_post pathways; monitors with ``when`` other than the default
+slots; summed variables.
+"""
+from __future__ import annotations
+
+import os
+import time
+
+import numpy as np
+
+from brian2.codegen.generators.cpp_generator import CPPCodeGenerator, c_data_type
+from brian2.core.clocks import Clock
+from brian2.core.functions import Function
+from brian2.core.preferences import prefs
+from brian2.core.variables import ArrayVariable, Constant, DynamicArrayVariable
+from brian2.devices.cpp_standalone.codeobject import CPPStandaloneCodeObject
+from brian2.devices.cpp_standalone.device import CPPStandaloneDevice
+from brian2.devices.device import all_devices
+from brian2.groups.neurongroup import NeuronGroup
+from brian2.groups.subgroup import Subgroup
+from brian2.monitors.ratemonitor import PopulationRateMonitor
+from brian2.monitors.spikemonitor import SpikeMonitor
+from brian2.monitors.statemonitor import StateMonitor
+from brian2.synapses.synapses import Synapses, SynapticPathway
+from brian2.utils.logger import get_logger
+from brian2.utils.stringtools import get_identifiers, stripped_deindented_lines
+
+logger = get_logger(__name__)
+
+STEP_TEMPLATES = {"stateupdate", "threshold", "reset", "synapses", "synapses_push_spikes",
+                  "spikemonitor", "ratemonitor", "statemonitor"}
+
+
+class B200CodeGenerator(CPPCodeGenerator):
+    """C++ generator for device code.
+
+    Produces the same scalar and vector code as ``CPPCodeGenerator`` (the
+    vector code is also what the CPU oracle executes) and, for synaptic
+    ``on_pre`` code, a device variant in which every in-place update of a
+    non-synaptic variable (``ge_post += w``) is an atomic accumulation, since
+    many synapses of one step may target the same neuron.
+    """
+
+    class_name = "b200_cuda"
+
+    def translate_statement_sequence(self, sc_statements, ve_statements):
+        sc_code, ve_code, kwds = super().translate_statement_sequence(sc_statements, ve_statements)
+        if self.template_name == "synapses":
+            kwds["vector_code_device"] = {name: self._device_block(stmts) for name, stmts in ve_statements.items()}
+        return sc_code, ve_code, kwds
+
+    def _device_block(self, statements):
+        read, write, indices, cond_write = self.arrays_helper(statements)
+        atomic = {v for v in write if self.variable_indices[v] not in ("_idx", "0")}
+        for stmt in statements:
+            ids = get_identifiers(stmt.expr)
+            if ids & atomic:
+                raise NotImplementedError(
+                    f"b200: on_pre code reads the non-synaptic variable(s) {sorted(ids & atomic)} it updates")
+            if stmt.var in atomic:
+                if stmt.op not in ("+=", "-=") or (stmt.used_boolean_variables and
+                                                   len(stmt.used_boolean_variables)):
+                    raise NotImplementedError(
+                        f"b200: '{stmt.var} {stmt.op} ...' on a non-synaptic variable; only += and -= "
+                        "(atomic accumulation) are supported in synaptic code")
+        lines = []
+        lines += self.translate_to_read_arrays(read - atomic, write - atomic, indices)
+        lines += self.translate_to_declarations(read - atomic, write - atomic, indices)
+        for stmt in statements:
+            if stmt.var in atomic:
+                var = self.variables[stmt.var]
+                ptr = self.get_array_name(var)
+                idx = self.variable_indices[stmt.var]
+                ctype = self.c_data_type(var.dtype)
+                expr = self.translate_expression(stmt.expr)
+                sign = "" if stmt.op == "+=" else "-"
+                line = f"_b200_atomic_add(&{ptr}[{idx}], ({ctype})({sign}({expr})));"
+                if stmt.var in cond_write:
+                    line = f"if({cond_write[stmt.var]}) {line}"
+                lines.append(line)
+            else:
+                line = self.translate_statement(stmt)
+                if stmt.var in cond_write:
+                    lines.append(f"if({cond_write[stmt.var]})")
+                    lines.append(f"    {line}")
+                else:
+                    lines.append(line)
+        lines += self.translate_to_write_arrays(write - atomic)
+        return stripped_deindented_lines("\n".join(lines))
+
+
+class B200CodeObject(CPPStandaloneCodeObject):
+    """A step-loop code object: carries its translated snippets, runs nothing on its own."""
+
+    generator_class = B200CodeGenerator
+    class_name = "b200_cuda"
+
+    def __init__(self, owner, fragment, variables, variable_indices, template_name, name):
+        super().__init__(owner, "", variables, variable_indices, template_name=template_name,
+                         template_source="", name=name, compiler_kwds={})
+        self.fragment = fragment
+
+    def compile_block(self, block):
+        pass
+
+    def run_block(self, block):
+        pass  # executed inside the device step kernel
+
+
+class B200Device(CPPStandaloneDevice):
+    """Standalone device whose clock-driven step loop runs on one GB300."""
+
+    def __init__(self):
+        super().__init__()
+        self.b200_runs = []            # [(net, n_steps, spec, objects)]
+        self.b200_run_options = dict(threads=None, ctas_per_inst=None)
+        self.b200_last_network = None
+        self.b200_timings = []
+
+    def reinit(self):
+        opts = self.b200_run_options
+        super().reinit()
+        self.b200_runs = []
+        self.b200_run_options = opts
+        self.b200_last_network = None
+        self.b200_timings = []
+
+    def activate(self, build_on_run=True, **kwargs):
+        for k in ("threads", "ctas_per_inst"):
+            if k in kwargs:
+                self.b200_run_options[k] = kwargs.pop(k)
+        super().activate(build_on_run=build_on_run, **kwargs)
+
+    # ------------------------------------------------------------- code objects
+    def code_object(self, owner, name, abstract_code, variables, template_name, variable_indices,
+                    codeobj_class=None, template_kwds=None, override_conditional_write=None,
+                    compiler_kwds=None):
+        if template_name not in STEP_TEMPLATES:
+            return super().code_object(owner, name, abstract_code, variables, template_name, variable_indices,
+                                       codeobj_class=codeobj_class, template_kwds=template_kwds,
+                                       override_conditional_write=override_conditional_write,
+                                       compiler_kwds=compiler_kwds)
+        from brian2.core.names import find_name
+        name = find_name(name)
+        meta = getattr(CPPStandaloneCodeObject.templater, template_name)
+        for vname, var in variables.items():
+            if isinstance(var, Function) and vname in ("rand", "randn", "poisson") and vname in str(abstract_code):
+                raise NotImplementedError("b200: random numbers inside the step loop are not supported")
+        gen = B200CodeGenerator(variables=variables, variable_indices=variable_indices, owner=owner,
+                                iterate_all=meta.iterate_all, codeobj_class=B200CodeObject,
+                                override_conditional_write=override_conditional_write,
+                                allows_scalar_write=meta.allows_scalar_write, name=name,
+                                template_name=template_name)
+        scalar_code, vector_code, kwds = gen.translate(abstract_code, dtype=prefs["core.default_float_dtype"])
+        fragment = dict(template=template_name, scalar=scalar_code, vector=vector_code,
+                        vector_device=kwds.get("vector_code_device"), template_kwds=dict(template_kwds or {}),
+                        variables=variables, variable_indices=variable_indices, generator=gen)
+        codeobj = B200CodeObject(owner, fragment, variables, variable_indices, template_name, name)
+        return codeobj
+
+    # ------------------------------------------------------------- runs
+    def network_run(self, net, duration, report=None, report_period=None, namespace=None, profile=None,
+                    level=0, **kwds):
+        from brian2.core.namespace import get_local_namespace
+        if duration < 0:
+            raise ValueError(f"Function 'run' expected a non-negative duration but got '{duration}'")
+        self.networks.add(net)
+        self.enable_profiling = bool(profile)
+        all_objects = net.sorted_objects
+        net._clocks = {obj.clock for obj in all_objects}
+        t_end = net.t + duration
+        for clock in net._clocks:
+            clock.set_interval(net.t, t_end)
+        if namespace is None:
+            namespace = get_local_namespace(level=level + 2)
+        net.before_run(namespace)
+        self.synapses |= {s for s in net.objects if isinstance(s, Synapses)}
+        self.clocks.update(net._clocks)
+        if len(net._clocks) != 1:
+            raise NotImplementedError("b200: all objects of a network must share one clock")
+        clock = next(iter(net._clocks))
+        n_steps = int(clock._i_end - clock.variables["timestep"].get_value().item()) \
+            if False else int(round(float(duration) / float(clock.dt_)))
+        spec, objects = self._make_spec(net, all_objects, clock)
+        self.b200_runs.append(dict(net=net, n_steps=n_steps, spec=spec, objects=objects, clock=clock,
+                                   queue_len=len(self.main_queue)))
+        self.main_queue.append(("insert_code", f"// b200 network run {len(self.b200_runs) - 1} ({n_steps} steps)"))
+        net.t_ = float(t_end)
+        net.after_run()
+        for c in net._clocks:
+            self.array_cache[c.variables["timestep"]] = np.array([c._i_end])
+            self.array_cache[c.variables["t"]] = np.array([c._i_end * c.dt_])
+        if self.build_on_run:
+            if self.has_been_run:
+                raise RuntimeError("The network has already been built and run before. Use set_device with "
+                                   "build_on_run=False and an explicit device.build call to use multiple "
+                                   "run statements with this device.")
+            self.build(direct_call=False, **self.build_options)
+
+    def network_get_profiling_info(self, net):
+        return [(name, ms * 1e-3) for name, ms in self.b200_timings]
+
+    # ------------------------------------------------------------- spec
+    def _make_spec(self, net, objects, clock):
+        gen_name = CPPCodeGenerator.get_array_name
+        groups, group_index = [], {}
+
+        def group_of(g):
+            base = g.source if isinstance(g, Subgroup) else g
+            if hasattr(base, "__weakref__") is False or not isinstance(base, NeuronGroup):
+                base = getattr(base, "__repr__", None) and base
+            if not isinstance(base, NeuronGroup):
+                raise NotImplementedError(f"b200: unsupported source/target {g!r}")
+            if base.name not in group_index:
+                gv = []
+                for vname, var in sorted(base.variables.items()):
+                    if (isinstance(var, ArrayVariable) and not var.scalar and var.owner is not None
+                            and var.owner.name == base.name and vname != "_spikespace"
+                            and var.size == len(base) and var.ndim == 1):
+                        gv.append(dict(name=vname, ctype=c_data_type(var.dtype), ptr=gen_name(var)))
+                group_index[base.name] = len(groups)
+                groups.append(dict(name=base.name, vars=gv, _obj=base))
+            lo = g.start if isinstance(g, Subgroup) else 0
+            hi = g.stop if isinstance(g, Subgroup) else len(base)
+            return group_index[base.name], (int(lo), int(hi))
+
+        clock_ptrs = dict(dt=gen_name(clock.variables["dt"]), t=gen_name(clock.variables["t"]),
+                          timestep=gen_name(clock.variables["timestep"]))
+        consts = {}
+
+        def collect(frag, allowed_owners):
+            """Constants used by a fragment; extra arrays of other groups."""
+            extra = {}
+            for vname, var in frag["variables"].items():
+                if isinstance(var, Constant) and vname not in ("N", "_vectorisation_idx"):
+                    consts.setdefault(vname, dict(name=vname, ctype=c_data_type(var.dtype),
+                                                  value=float(var.value)))
+                elif isinstance(var, ArrayVariable):
+                    owner = var.owner
+                    if owner is None or isinstance(owner, Clock) or owner.name in allowed_owners:
+                        continue
+                    if isinstance(owner, NeuronGroup) or isinstance(owner, Subgroup):
+                        gi, _ = group_of(owner)
+                        names = [v["name"] for v in groups[gi]["vars"]]
+                        if vname in names or var.name in names:
+                            extra[gen_name(var)] = ("group", gi, names.index(var.name))
+            return extra
+
+        def block(frag):
+            sc = frag["scalar"][None] if isinstance(frag["scalar"], dict) else frag["scalar"]
+            ve = frag["vector"][None] if isinstance(frag["vector"], dict) else frag["vector"]
+            out = dict(scalar=sc, vector=ve)
+            if frag.get("vector_device"):
+                out["vector_device"] = frag["vector_device"][None]
+            return out
+
+        pathways, spkmons, ratemons, statemons = [], [], [], []
+        b200_objects = []
+        for obj in objects:
+            if not obj.active:
+                continue
+            for co in obj._code_objects:
+                if not isinstance(co, B200CodeObject):
+                    continue
+                frag = co.fragment
+                t = frag["template"]
+                b200_objects.append((obj, co))
+                if t in ("stateupdate", "threshold", "reset"):
+                    gi, _ = group_of(obj.group)
+                    g = groups[gi]
+                    key = {"stateupdate": "update"}.get(t, t)
+                    b = block(frag)
+                    ex = collect(frag, {g["name"]})
+                    if ex:
+                        b["extra_ptrs"] = {k: list(v) for k, v in ex.items()}
+                    if t == "threshold":
+                        b["refractory"] = bool(frag["template_kwds"].get("_uses_refractory", False))
+                        if frag["template_kwds"].get("eventspace_variable") is not None and \
+                                frag["template_kwds"]["eventspace_variable"].name != "_spikespace":
+                            raise NotImplementedError("b200: custom events are not supported")
+                    if key in g:
+                        raise NotImplementedError(f"b200: several {t} code objects for one group")
+                    g[key] = b
+                elif t == "synapses":
+                    pw = co.owner
+                    if not isinstance(pw, SynapticPathway) or pw.prepost != "pre":
+                        raise NotImplementedError("b200: only on_pre pathways are supported")
+                    syn = pw.synapses
+                    sgi, srange = group_of(pw.source)
+                    tgi, trange = group_of(pw.target)
+                    sv = []
+                    for vname, var in sorted(syn.variables.items()):
+                        if (isinstance(var, DynamicArrayVariable) and var.owner is not None
+                                and var.owner.name == syn.name and var.ndim == 1
+                                and vname not in ("_synaptic_pre", "_synaptic_post", "N_incoming", "N_outgoing")
+                                and not var.scalar):
+                            sv.append(dict(name=var.name, ctype=c_data_type(var.dtype), ptr=gen_name(var)))
+                    gptrs = {}
+                    for vname, var in frag["variables"].items():
+                        if isinstance(var, ArrayVariable) and var.owner is not None and \
+                                isinstance(var.owner, (NeuronGroup, Subgroup)):
+                            gi, _ = group_of(var.owner)
+                            names = [v["name"] for v in groups[gi]["vars"]]
+                            if var.name in names:
+                                gptrs[gen_name(var)] = [gi, names.index(var.name)]
+                    collect(frag, {syn.name, groups[sgi]["name"], groups[tgi]["name"]})
+                    pathways.append(dict(name=pw.name, src=sgi, tgt=tgi, vars=sv,
+                                         pre_ptr=gen_name(syn.variables["_synaptic_pre"]),
+                                         post_ptr=gen_name(syn.variables["_synaptic_post"]),
+                                         group_ptrs=gptrs, on_pre=block(frag),
+                                         _obj=pw, _src_range=srange, _tgt_range=trange))
+                elif t == "synapses_push_spikes":
+                    pass
+                elif t == "spikemonitor":
+                    if not isinstance(obj, SpikeMonitor) or set(obj.record_variables) - {"i", "t"}:
+                        raise NotImplementedError("b200: spike monitors record i and t only")
+                    gi, rng = group_of(obj.source)
+                    spkmons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng))
+                elif t == "ratemonitor":
+                    gi, rng = group_of(obj.source)
+                    ratemons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng))
+                elif t == "statemonitor":
+                    if obj.when != "start":
+                        raise NotImplementedError("b200: state monitors record at the start of the step")
+                    gi, rng = group_of(obj.source)
+                    names = [v["name"] for v in groups[gi]["vars"]]
+                    for v in obj.record_variables:
+                        if v not in names:
+                            raise NotImplementedError(f"b200: recording '{v}' (not a state variable)")
+                    statemons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng,
+                                          _vars=list(obj.record_variables)))
+        for g in groups:
+            for k in ("update", "threshold", "reset"):
+                g.setdefault(k, None)
+        # every array pointer used by a group block must be declared: add the
+        # clock and constant names used in snippets as they are
+        fdt = prefs["core.default_float_dtype"]
+        spec = dict(name=f"{net.name}", float=c_data_type(fdt), consts=sorted(consts.values(), key=lambda c: c["name"]),
+                    groups=groups, pathways=pathways, spike_monitors=spkmons, rate_monitors=ratemons,
+                    state_monitors=statemons, clock_ptrs=clock_ptrs)
+        return spec, b200_objects
+
+    @staticmethod
+    def public_spec(spec):
+        """The JSON-serialisable part of a spec (drops the Brian objects)."""
+        def clean(x):
+            if isinstance(x, dict):
+                return {k: clean(v) for k, v in x.items() if not k.startswith("_")}
+            if isinstance(x, list):
+                return [clean(v) for v in x]
+            if isinstance(x, tuple):
+                return [clean(v) for v in x]
+            return x
+        return clean(spec)
+
+    # ------------------------------------------------------------- build + GPU
+    def build(self, directory="output", results_directory="results", compile=True, run=True, debug=False,
+              clean=False, with_output=True, additional_source_files=None, run_args=None, direct_call=True,
+              **kwds):
+        for k in ("threads", "ctas_per_inst"):
+            if k in kwds:
+                self.b200_run_options[k] = kwds.pop(k)
+        # host code after the first GPU run cannot be executed before it
+        if self.b200_runs:
+            first = self.b200_runs[0]["queue_len"]
+            for func, args in self.main_queue[first:]:
+                if func == "insert_code" and str(args).startswith("// b200 network run"):
+                    continue
+                raise NotImplementedError("b200: host code between or after run() calls is not supported "
+                                          f"(found '{func}')")
+        super().build(directory=directory, results_directory=results_directory, compile=compile, run=run,
+                      debug=debug, clean=clean, with_output=with_output,
+                      additional_source_files=additional_source_files, run_args=run_args,
+                      direct_call=direct_call, **kwds)
+        if run and self.b200_runs:
+            self._run_on_gpu()
+
+    def _load(self, var):
+        fname = os.path.join(self.results_dir, self.get_array_filename(var))
+        return np.fromfile(fname, dtype=var.dtype)
+
+    def _store(self, var, values):
+        fname = os.path.join(self.results_dir, self.get_array_filename(var))
+        np.ascontiguousarray(values, dtype=var.dtype).tofile(fname)
+
+    def _run_on_gpu(self):
+        from .runtime import Model, Network
+        spec0 = self.b200_runs[0]["spec"]
+        pub = self.public_spec(spec0)
+        model = Model.get(pub)
+        clock = self.b200_runs[0]["clock"]
+        dt = float(clock.dt_)
+        sizes = [len(g["_obj"]) for g in spec0["groups"]]
+        net = Network(model, [sizes], dt)
+        threads = self.b200_run_options.get("threads") or (1024 if max(sizes) <= 8192 else 256)
+        net.configure(threads=threads, ctas_per_inst=self.b200_run_options.get("ctas_per_inst") or 1)
+        # initial state written by the standalone main program
+        for gi, g in enumerate(spec0["groups"]):
+            for v in g["vars"]:
+                net.upload(0, gi, v["name"], self._load(g["_obj"].variables[v["name"]]))
+        for pi, p in enumerate(spec0["pathways"]):
+            syn = p["_obj"].synapses
+            pre = self._load(syn.variables["_synaptic_pre"]).astype(np.int64) - p["_src_range"][0]
+            post = self._load(syn.variables["_synaptic_post"]).astype(np.int64) - p["_tgt_range"][0]
+            dvar = p["_obj"].variables["delay"]
+            if dvar.scalar:
+                d = self._load(dvar)
+                scalar_delay = int(float(d[0]) / dt + 0.5) if d.size else 0
+                steps = None
+            else:
+                d = self._load(dvar)
+                steps = (d / dt + 0.5).astype(np.int32)
+                scalar_delay = 0
+            net.set_synapses(0, pi, pre, post, steps, scalar_delay, p["_src_range"], p["_tgt_range"])
+            for v in p["vars"]:
+                net.upload_synapse_var(0, pi, v["name"], self._load(syn.variables[v["name"]]))
+        for mi, m in enumerate(spec0["spike_monitors"]):
+            net.set_spikemon_range(0, mi, *m["_range"])
+        for mi, m in enumerate(spec0["rate_monitors"]):
+            net.set_ratemon_range(0, mi, *m["_range"])
+        for mi, m in enumerate(spec0["state_monitors"]):
+            idx = self._load(m["_obj"].variables["_indices"]).astype(np.int32)
+            net.set_statemon(0, mi, idx + m["_range"][0], m["_vars"])
+        ts0 = int(self._load(clock.variables["timestep"])[0])
+        net.set_step(0, ts0)
+        net.reset_monitors(0)
+        total_ms = 0.0
+        t_wall = time.time()
+        for r in self.b200_runs:
+            if r["spec"] is not spec0 and self.public_spec(r["spec"]) != pub:
+                raise NotImplementedError("b200: the network changed between runs")
+            net.run(r["n_steps"])
+            total_ms += net.last_run_ms()
+        wall = time.time() - t_wall
+        self.b200_timings = [("b200_step_kernel", total_ms)]
+        self._last_run_time = total_ms * 1e-3
+        self._last_run_completed_fraction = 1.0
+        # write back in the standalone results format
+        for gi, g in enumerate(spec0["groups"]):
+            for v in g["vars"]:
+                self._store(g["_obj"].variables[v["name"]], net.download(0, gi, v["name"]))
+        for pi, p in enumerate(spec0["pathways"]):
+            syn = p["_obj"].synapses
+            for v in p["vars"]:
+                self._store(syn.variables[v["name"]], net.download_synapse_var(0, pi, v["name"]))
+        for mi, m in enumerate(spec0["spike_monitors"]):
+            i, ts, cnt = net.spikes(0, mi)
+            mon = m["_obj"]
+            self._store(mon.variables["i"], i)
+            self._store(mon.variables["t"], ts.astype(np.float64) * dt)
+            lo, hi = m["_range"]
+            self._store(mon.variables["count"], cnt[: hi - lo])
+            self._store(mon.variables["N"], np.array([len(i)]))
+        for mi, m in enumerate(spec0["rate_monitors"]):
+            c = net.rate_counts(0, mi)
+            mon = m["_obj"]
+            lo, hi = m["_range"]
+            n = hi - lo
+            rate = np.array([1.0 * x / dt / n for x in c], dtype=np.float64) if n else np.zeros(len(c))
+            self._store(mon.variables["rate"], rate)
+            self._store(mon.variables["t"], (ts0 + np.arange(len(c))).astype(np.float64) * dt)
+            self._store(mon.variables["N"], np.array([len(c)]))
+        for mi, m in enumerate(spec0["state_monitors"]):
+            tr = net.state_trace(0, mi)
+            mon = m["_obj"]
+            self._store(mon.variables["t"], (ts0 + np.arange(tr.shape[0])).astype(np.float64) * dt)
+            for k, v in enumerate(m["_vars"]):
+                self._store(mon.variables[v], tr[:, k, :])
+                mon.variables[v].size = tr[:, k, :].shape
+            self._store(mon.variables["N"], np.array([tr.shape[0]]))
+        ts_end = net.step(0)
+        self._store(clock.variables["timestep"], np.array([ts_end]))
+        self._store(clock.variables["t"], np.array([ts_end * dt]))
+        self.b200_last_network = net
+        logger.debug(f"b200: {sum(r['n_steps'] for r in self.b200_runs)} steps in {total_ms:.2f} ms "
+                     f"(device), {wall:.3f} s wall")
+
+
+b200_device = B200Device()
+all_devices["b200"] = b200_device
+all_devices["gb300"] = b200_device

@@ -1,0 +1,605 @@
+"""Renders a network *spec* into one CUDA source file for sm_103a.
+
+A spec is plain data (JSON-serialisable dict) describing one Brian2 network
+model: its neuron groups with their state variables and the scalar/vector C++
+snippets of the ``stateupdate``, ``threshold`` and ``reset`` code objects, its
+synaptic pathways with the ``on_pre`` snippets, and its monitors.  The snippets
+are produced by :class:`brian2_gb300.brian_device.B200CodeGenerator`, a subclass
+of Brian's ``CPPCodeGenerator`` (``brian2/codegen/generators/cpp_generator.py:200``),
+so the arithmetic is Brian's own; this module only places them into the fused
+persistent step kernel and the host-side scalar evaluator.
+
+The per-step schedule reproduced by the kernel is Brian's default schedule
+(``brian2/core/network.py:42-50``): state update -> threshold -> spike monitor
+-> synaptic propagation (push + on_pre) -> reset -> rate monitor, with the
+clock tick ``t = timestep*dt`` (``brianlib/clocks.h:34-38``).  The reset is
+applied at the start of the following step (or at the end of the launch), which
+is equivalent because nothing reads the state in between.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import re
+
+CTYPE_KIND = {"double": 0, "float": 1, "int32_t": 2, "char": 3, "int8_t": 3, "int64_t": 4}
+KIND_NP = {0: "float64", 1: "float32", 2: "int32", 3: "int8", 4: "int64"}
+
+_DECL_RE = re.compile(
+    r"^\s*(?:const\s+)?(double|float|int32_t|int64_t|char|bool|int|long|size_t|uint32_t|uint64_t)\s+"
+    r"([A-Za-z_]\w*)\s*(=|;)")
+
+
+def spec_hash(spec: dict) -> str:
+    return hashlib.sha256(json.dumps(spec, sort_keys=True).encode()).hexdigest()[:16]
+
+
+def c_literal(value: float, ctype: str) -> str:
+    if ctype in ("double", "float"):
+        v = float(value)
+        if v != v:
+            return "NAN"
+        if v in (float("inf"), float("-inf")):
+            return "INFINITY" if v > 0 else "-INFINITY"
+        return f"{v.hex()}"
+    return str(int(value))
+
+
+def scalar_outputs(code: str):
+    """(ctype, name) of every variable declared by a scalar block, in order."""
+    out = []
+    for line in code.splitlines():
+        m = _DECL_RE.match(line)
+        if m:
+            out.append((m.group(1), m.group(2)))
+    return out
+
+
+def _indent(code: str, n: int) -> str:
+    pad = " " * n
+    return "\n".join(pad + ln if ln.strip() else "" for ln in code.splitlines())
+
+
+def _block(spec_block):
+    if not spec_block:
+        return None
+    return {"scalar": spec_block.get("scalar", "") or "", "vector": spec_block.get("vector", "") or "",
+            "vector_device": spec_block.get("vector_device"), "refractory": spec_block.get("refractory", False)}
+
+
+class _Tables:
+    """Scalar-table layout of one group or pathway: [constants | block scalars...]."""
+
+    def __init__(self, consts, blocks):
+        self.consts = consts
+        self.entries = [(c["ctype"], c["name"]) for c in consts]
+        self.block_ranges = {}
+        for name, blk in blocks:
+            if blk is None:
+                continue
+            outs = scalar_outputs(blk["scalar"])
+            self.block_ranges[name] = (len(self.entries), outs)
+            self.entries += outs
+
+    @property
+    def size(self):
+        return len(self.entries)
+
+    def device_loads(self, name):
+        """Declarations reading the constants and this block's scalars from S."""
+        lines = [f"const {ct} {nm} = ({ct})_b200_S[{k}];" for k, (ct, nm) in enumerate(self.entries[:len(self.consts)])]
+        if name in self.block_ranges:
+            off, outs = self.block_ranges[name]
+            lines += [f"const {ct} {nm} = ({ct})_b200_S[{off + k}];" for k, (ct, nm) in enumerate(outs)]
+        lines.append("(void)_b200_S;")
+        return "\n".join(lines)
+
+    def host_eval(self, blocks):
+        """Host code that evaluates the scalar blocks and fills _out."""
+        lines = []
+        for k, (ct, nm) in enumerate(self.entries[:len(self.consts)]):
+            lines.append(f"_out[{k}] = (double){nm};")
+        for name, blk in blocks:
+            if blk is None or name not in self.block_ranges:
+                continue
+            off, outs = self.block_ranges[name]
+            lines.append("{")
+            lines.append(_indent(blk["scalar"], 2))
+            for k, (ct, nm) in enumerate(outs):
+                lines.append(f"  _out[{off + k}] = (double){nm};")
+            lines.append("}")
+        return "\n".join(lines)
+
+
+def render_model(spec: dict) -> str:
+    """Returns the complete .cu text for a spec."""
+    groups = spec["groups"]
+    paths = spec.get("pathways", [])
+    spkmons = spec.get("spike_monitors", [])
+    ratemons = spec.get("rate_monitors", [])
+    statemons = spec.get("state_monitors", [])
+    consts = spec.get("consts", [])
+    clock = spec.get("clock_ptrs", {"dt": "_ptr_array_defaultclock_dt", "t": "_ptr_array_defaultclock_t",
+                                     "timestep": "_ptr_array_defaultclock_timestep"})
+    NG, NP = len(groups), len(paths)
+    assert 1 <= NG <= 4 and NP <= 8 and len(spkmons) <= 4 and len(ratemons) <= 4 and len(statemons) <= 4
+
+    o = []
+    w = o.append
+    w(f"// Generated by brian2_gb300.codegen for model '{spec['name']}' ({spec_hash(spec)}); do not edit.")
+    w('#include "b200_device.cuh"')
+    w("")
+    # ------------------------------------------------------------- constants
+    w("static const char* const b200_const_names[] = {" + ", ".join(f'"{c["name"]}"' for c in consts) + ("" if consts else '""') + "};")
+    w("static const double b200_const_defaults[] = {" + ", ".join(c_literal(c["value"], "double") for c in consts) + ("" if consts else "0.0") + "};")
+    w("")
+
+    gtables, ptables = [], []
+    for g in groups:
+        blocks = [("update", _block(g.get("update"))), ("threshold", _block(g.get("threshold"))),
+                  ("reset", _block(g.get("reset")))]
+        gtables.append((_Tables(consts, blocks), blocks))
+    for p in paths:
+        blocks = [("on_pre", _block(p.get("on_pre")))]
+        ptables.append((_Tables(consts, blocks), blocks))
+
+    # ------------------------------------------------------------- model tables
+    for gi, g in enumerate(groups):
+        w(f"static const char* const b200_g{gi}_vars[] = {{" + ", ".join(f'"{v["name"]}"' for v in g["vars"]) + "};")
+        w(f"static const int b200_g{gi}_kinds[] = {{" + ", ".join(str(CTYPE_KIND[v["ctype"]]) for v in g["vars"]) + "};")
+    for pi, p in enumerate(paths):
+        pv = p.get("vars", [])
+        w(f"static const char* const b200_p{pi}_vars[] = {{" + ", ".join(f'"{v["name"]}"' for v in pv) + ('' if pv else '""') + "};")
+        w(f"static const int b200_p{pi}_kinds[] = {{" + ", ".join(str(CTYPE_KIND[v["ctype"]]) for v in pv) + ('' if pv else '0') + "};")
+    w("static const b200_group_info b200_groups[] = {" + ", ".join(
+        f'{{"{g["name"]}", {len(g["vars"])}, b200_g{gi}_vars, b200_g{gi}_kinds, {gtables[gi][0].size}}}'
+        for gi, g in enumerate(groups)) + "};")
+    if paths:
+        w("static const b200_pathway_info b200_pathways[] = {" + ", ".join(
+            f'{{"{p["name"]}", {p["src"]}, {p["tgt"]}, {len(p.get("vars", []))}, b200_p{pi}_vars, b200_p{pi}_kinds, {ptables[pi][0].size}}}'
+            for pi, p in enumerate(paths)) + "};")
+    else:
+        w("static const b200_pathway_info* const b200_pathways = nullptr;")
+    for nm, mons in (("spkmon", spkmons), ("ratemon", ratemons), ("statemon", statemons)):
+        if mons:
+            w(f"static const b200_mon_info b200_{nm}[] = {{" + ", ".join(f'{{"{m["name"]}", {m["group"]}}}' for m in mons) + "};")
+        else:
+            w(f"static const b200_mon_info* const b200_{nm} = nullptr;")
+    w("")
+
+    # ------------------------------------------------------------- host scalars
+    w("// Host evaluation of the scalar (loop-invariant) blocks.  Compiled by the host")
+    w("// compiler with IEEE semantics (-ffp-contract=off), so values equal those of")
+    w("// Brian's C++ code objects, which evaluate the same expressions per call.")
+    w("static void b200_eval_scalars(int _kind, int _id, const double* _c, double _b200_dt, double* _out) {")
+    for k, c in enumerate(consts):
+        w(f"  const {c['ctype']} {c['name']} = ({c['ctype']})_c[{k}];")
+    w(f"  const double* const {clock['dt']} = &_b200_dt;")
+    w(f"  const double _b200_t0 = 0.0; const double* const {clock['t']} = &_b200_t0;")
+    w(f"  const int64_t _b200_ts0 = 0; const int64_t* const {clock['timestep']} = &_b200_ts0;")
+    w(f"  (void){clock['dt']}; (void){clock['t']}; (void){clock['timestep']}; (void)_c;")
+    for k, c in enumerate(consts):
+        w(f"  (void){c['name']};")
+    for gi, (tab, blocks) in enumerate(gtables):
+        w(f"  if (_kind == 0 && _id == {gi}) {{")
+        w(_indent(tab.host_eval(blocks), 4))
+        w("  }")
+    for pi, (tab, blocks) in enumerate(ptables):
+        w(f"  if (_kind == 1 && _id == {pi}) {{")
+        w(_indent(tab.host_eval(blocks), 4))
+        w("  }")
+    w("}")
+    w("")
+
+    # ------------------------------------------------------------- kernel
+    def group_ptrs(gi, indent):
+        g = groups[gi]
+        lines = [f"{v['ctype']}* const {v['ptr']} = ({v['ctype']}*)I.g[{gi}].var[{k}];"
+                 for k, v in enumerate(g["vars"])]
+        lines += [f"(void){v['ptr']};" for v in g["vars"]]
+        return _indent("\n".join(lines), indent)
+
+    def extra_ptrs(block_spec, indent):
+        lines = []
+        for ptr, (kind, obj, var) in sorted((block_spec or {}).get("extra_ptrs", {}).items()):
+            if kind == "group":
+                v = groups[obj]["vars"][var]
+                lines.append(f"{v['ctype']}* const {ptr} = ({v['ctype']}*)I.g[{obj}].var[{var}]; (void){ptr};")
+        return _indent("\n".join(lines), indent)
+
+    w("__device__ __forceinline__ int b200_upper_bound(const int* a, int n, int x) {")
+    w("  int lo = 0, hi = n;")
+    w("  while (lo < hi) { const int m = (lo + hi) >> 1; if (a[m] <= x) lo = m + 1; else hi = m; }")
+    w("  return lo;")
+    w("}")
+    w("")
+    w(f"#define B200_NG {NG}")
+    w("static size_t b200_dyn_smem(int threads, int max_tiles1, int max_w) {")
+    w("  return (size_t)threads * 8 + (size_t)(threads + 1) * 4 + (size_t)threads * 4 +")
+    w("         (size_t)B200_NG * max_tiles1 * 4 + (size_t)(3 * max_w + 1) * 4 + 16;")
+    w("}")
+    w("")
+    w("template <int MAXT>")
+    w("__global__ void __launch_bounds__(MAXT) b200_step_kernel(")
+    w("    const b200_inst_d* __restrict__ insts, const int2* __restrict__ cta_map, int n_inst,")
+    w("    int queue_mode, int* work, int64_t max_steps, uint64_t limit_ns, int max_tiles1, int max_w) {")
+    w("  extern __shared__ __align__(16) unsigned char b200_dyn[];")
+    w("  int64_t* const s_item_seg = (int64_t*)b200_dyn;")
+    w("  int* const s_item_off = (int*)(s_item_seg + blockDim.x);")
+    w("  int* const s_item_src = s_item_off + blockDim.x + 1;")
+    w("  int* const s_pref_all = s_item_src + blockDim.x;")
+    w("  int* const s_nd = s_pref_all + B200_NG * max_tiles1;")
+    w("  int* const s_base = s_nd + max_w;")
+    w("  int* const s_ndoff = s_base + max_w;")
+    w("  __shared__ __align__(16) b200_inst_d I;")
+    w("  __shared__ int s_wsum[B200_MAX_WARPS + 1];")
+    w("  __shared__ int s_unit, s_rank, s_flag;")
+    w("  __shared__ long long s_mon_n[B200_MAX_SPKMON];")
+    w("  __shared__ long long s_stm_n[B200_MAX_STATEMON];")
+    w("  unsigned gen = 0;")
+    w("  (void)s_nd; (void)s_base; (void)s_ndoff; (void)s_item_seg; (void)s_item_off; (void)s_item_src;")
+    w("  for (int pass = 0;; ++pass) {")
+    w("    if (threadIdx.x == 0) {")
+    w("      if (queue_mode) { s_unit = atomicAdd(work, 1); s_rank = 0; }")
+    w("      else if (pass == 0) { const int2 m = cta_map[blockIdx.x]; s_unit = m.x; s_rank = m.y; }")
+    w("      else s_unit = n_inst;")
+    w("    }")
+    w("    __syncthreads();")
+    w("    const int unit = s_unit, rank = s_rank;")
+    w("    if (unit >= n_inst) break;")
+    w("    {")
+    w("      const long long* src = (const long long*)&insts[unit];")
+    w("      long long* dst = (long long*)&I;")
+    w("      for (int k = threadIdx.x; k < (int)(sizeof(b200_inst_d) / 8); k += blockDim.x) dst[k] = src[k];")
+    w("    }")
+    w("    __syncthreads();")
+    w("    if (threadIdx.x == 0) {")
+    w("      gen = b200_ld_acquire(&I.bar[1]);")
+    for m in range(len(spkmons)):
+        w(f"      s_mon_n[{m}] = *((volatile long long*)I.sm[{m}].n);")
+    for m in range(len(statemons)):
+        w(f"      s_stm_n[{m}] = *((volatile long long*)I.stm[{m}].n);")
+    w("    }")
+    w("    __syncthreads();")
+    w("    const int64_t ts0 = I.ts;")
+    w("    const int64_t ts_stop = (I.ts_end < ts0 + max_steps) ? I.ts_end : ts0 + max_steps;")
+    w("    const double _b200_dt = I.dt;")
+    w("    int64_t ts = ts0;")
+    w("    bool ok = true;")
+    w("    for (; ts < ts_stop; ++ts) {")
+    w("      if (threadIdx.x == 0) {")
+    w("        int st = 0;")
+    for m in range(len(spkmons)):
+        w(f"        if (s_mon_n[{m}] + (I.sm[{m}].hi - I.sm[{m}].lo) > I.sm[{m}].cap) st = 1;")
+    w("        s_flag = st;")
+    w("      }")
+    w("      __syncthreads();")
+    w("      if (s_flag) break;")
+    w("      const double _b200_t = (double)ts * _b200_dt;")
+    w("      const int64_t _b200_ts = ts;")
+    w(f"      const double* const {clock['t']} = &_b200_t; (void){clock['t']};")
+    w(f"      const double* const {clock['dt']} = &_b200_dt; (void){clock['dt']};")
+    w(f"      const int64_t* const {clock['timestep']} = &_b200_ts; (void){clock['timestep']};")
+
+    # ---- Phase A: per group reset(ts-1) -> state monitors -> update+threshold+compaction
+    for gi, g in enumerate(groups):
+        tab, blocks = gtables[gi]
+        bd = dict(blocks)
+        w(f"      // ---- group {gi} '{g['name']}': phase A")
+        w("      {")
+        w(f"        b200_group_d& GD = I.g[{gi}];")
+        w("        const int32_t N = GD.N; (void)N;")
+        w(f"        const double* const _b200_S = GD.S;")
+        w(group_ptrs(gi, 8))
+        w("        const int u0 = GD.cta_tile[rank], u1 = GD.cta_tile[rank + 1];")
+        if bd["reset"] is not None:
+            w("        if (ts > ts0) {")
+            w("          for (int u = u0; u < u1; ++u) {")
+            w("            const int cnt = GD.tile_cnt[u], base = GD.tile_start[u];")
+            w("            for (int j = threadIdx.x; j < cnt; j += blockDim.x) {")
+            w("              const int32_t _idx = GD.scratch[base + j];")
+            w("              const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+            w("              {")
+            w(_indent(tab.device_loads("reset"), 16))
+            w(extra_ptrs(g.get("reset"), 16))
+            w(_indent(bd["reset"]["vector"], 16))
+            w("              }")
+            w("            }")
+            w("          }")
+            w("          __syncthreads();")
+            w("        }")
+        for mi, m in enumerate(statemons):
+            if m["group"] != gi:
+                continue
+            w(f"        {{  // state monitor {mi}")
+            w(f"          const b200_statemon_d& SM = I.stm[{mi}];")
+            w("          const int lo = GD.tile_start[GD.cta_tile[rank]], hi = GD.tile_start[GD.cta_tile[rank + 1]];")
+            w("          double* const row = SM.data + (size_t)(ts - SM.step0) * SM.n_vars * SM.n_rec;")
+            w("          for (int k = threadIdx.x; k < SM.n_rec * SM.n_vars; k += blockDim.x) {")
+            w("            const int r = k % SM.n_rec, v = k / SM.n_rec;")
+            w("            const int idx = SM.idx[r];")
+            w("            if (idx >= lo && idx < hi) {")
+            w("              const void* base = GD.var[SM.var_id[v]];")
+            w("              row[k] = SM.var_dbl[v] ? ((const double*)base)[idx] : (double)((const float*)base)[idx];")
+            w("            }")
+            w("          }")
+            w(f"          if (threadIdx.x == 0) s_stm_n[{mi}] = ts + 1 - SM.step0;")
+            w("        }")
+        w("        for (int u = u0; u < u1; ++u) {")
+        w("          const int start = GD.tile_start[u], end = GD.tile_start[u + 1];")
+        w("          int cnt = 0;")
+        w("          for (int tb = start; tb < end; tb += blockDim.x) {")
+        w("            const int32_t _idx = tb + threadIdx.x;")
+        w("            bool _b200_spk = false;")
+        w("            if (_idx < end) {")
+        w("              const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+        if bd["update"] is not None:
+            w("              {")
+            w(_indent(tab.device_loads("update"), 16))
+            w(extra_ptrs(g.get("update"), 16))
+            w(_indent(bd["update"]["vector"], 16))
+            w("              }")
+        if bd["threshold"] is not None:
+            w("              {")
+            w(_indent(tab.device_loads("threshold"), 16))
+            w(extra_ptrs(g.get("threshold"), 16))
+            w(_indent(bd["threshold"]["vector"], 16))
+            w("                _b200_spk = _cond;")
+            if bd["threshold"].get("refractory"):
+                nr = next(v["ptr"] for v in g["vars"] if v["name"] == "not_refractory")
+                ls = next(v["ptr"] for v in g["vars"] if v["name"] == "lastspike")
+                w("                if (_cond) {")
+                w(f"                  {nr}[_idx] = false;")
+                w(f"                  {ls}[_idx] = _b200_t;")
+                w("                }")
+            w("              }")
+        w("            }")
+        w("            int tot;")
+        w("            const int pos = b200_block_compact(_b200_spk, s_wsum, &tot);")
+        w("            if (_b200_spk) GD.scratch[start + cnt + pos] = _idx;")
+        w("            cnt += tot;")
+        w("          }")
+        w("          if (threadIdx.x == 0) GD.tile_cnt[u] = cnt;")
+        w("        }")
+        w("      }")
+    w("      if (!b200_inst_barrier(I, gen, limit_ns)) { ok = false; break; }")
+
+    # ---- Phase B: prefix of tile counts, ring, monitors
+    for gi, g in enumerate(groups):
+        w(f"      // ---- group {gi}: phase B (spike lists)")
+        w("      {")
+        w(f"        b200_group_d& GD = I.g[{gi}];")
+        w(f"        int* const pref = s_pref_all + {gi} * max_tiles1;")
+        w("        const int nt = GD.n_tiles;")
+        w("        int carry = 0;")
+        w("        for (int c0 = 0; c0 < nt; c0 += blockDim.x) {")
+        w("          const int u = c0 + threadIdx.x;")
+        w("          const int x = u < nt ? GD.tile_cnt[u] : 0;")
+        w("          int tot;")
+        w("          const int ex = b200_block_exscan(x, s_wsum, &tot);")
+        w("          if (u < nt) pref[u] = carry + ex;")
+        w("          carry += tot;")
+        w("        }")
+        w("        if (threadIdx.x == 0) pref[nt] = carry;")
+        w("        __syncthreads();")
+        w("        const int u0 = GD.cta_tile[rank], u1 = GD.cta_tile[rank + 1];")
+        w("        if (GD.R > 1) {")
+        w("          const int slot = (int)(ts % GD.R);")
+        w("          int32_t* const ring = GD.ring + (int64_t)slot * GD.N;")
+        w("          for (int u = u0; u < u1; ++u) {")
+        w("            const int cnt = pref[u + 1] - pref[u], base = GD.tile_start[u];")
+        w("            for (int j = threadIdx.x; j < cnt; j += blockDim.x) ring[pref[u] + j] = GD.scratch[base + j];")
+        w("          }")
+        w("          if (rank == 0) {")
+        w("            for (int u = threadIdx.x; u <= nt; u += blockDim.x) GD.ring_prefix[(int64_t)slot * (nt + 1) + u] = pref[u];")
+        w("            if (threadIdx.x == 0) GD.ring_total[slot] = pref[nt];")
+        w("          }")
+        w("        }")
+        for mi, m in enumerate(spkmons):
+            if m["group"] != gi:
+                continue
+            w(f"        {{  // spike monitor {mi}")
+            w(f"          const b200_spkmon_d& SM = I.sm[{mi}];")
+            w(f"          const long long mbase = s_mon_n[{mi}] - pref[SM.tile_lo];")
+            w("          const int a = u0 > SM.tile_lo ? u0 : SM.tile_lo, b = u1 < SM.tile_hi ? u1 : SM.tile_hi;")
+            w("          for (int u = a; u < b; ++u) {")
+            w("            const int cnt = pref[u + 1] - pref[u], base = GD.tile_start[u];")
+            w("            for (int j = threadIdx.x; j < cnt; j += blockDim.x) {")
+            w("              const int idx = GD.scratch[base + j];")
+            w("              const long long pos = mbase + pref[u] + j;")
+            w("              SM.i[pos] = idx - SM.lo;")
+            w("              SM.ts[pos] = (int32_t)ts;")
+            w("              SM.count[idx - SM.lo] += 1;")
+            w("            }")
+            w("          }")
+            w("          __syncthreads();")
+            w(f"          if (threadIdx.x == 0) s_mon_n[{mi}] += pref[SM.tile_hi] - pref[SM.tile_lo];")
+            w("        }")
+        for mi, m in enumerate(ratemons):
+            if m["group"] != gi:
+                continue
+            w(f"        if (rank == 0 && threadIdx.x == 0) {{  // rate monitor {mi}")
+            w(f"          const b200_ratemon_d& RM = I.rm[{mi}];")
+            w("          RM.cnt[ts - RM.step0] = pref[RM.tile_hi] - pref[RM.tile_lo];")
+            w("        }")
+        w("      }")
+
+    # ---- Phase B: synaptic propagation
+    for pi, p in enumerate(paths):
+        tab, blocks = ptables[pi]
+        blk = dict(blocks)["on_pre"]
+        sg, tg = p["src"], p["tgt"]
+        w(f"      // ---- pathway {pi} '{p['name']}': propagation")
+        w("      {")
+        w(f"        const b200_pathway_d& PD = I.p[{pi}];")
+        w(f"        const b200_group_d& SGD = I.g[{sg}];")
+        w(f"        const int* const pref = s_pref_all + {sg} * max_tiles1;")
+        w("        const int W = PD.D - PD.dmin + 1;")
+        w("        for (int k = threadIdx.x; k < W; k += blockDim.x) {")
+        w("          const int d = PD.dmin + k;")
+        w("          const int64_t s = ts - d;")
+        w("          int n = 0, b = 0;")
+        w("          if (s >= 0) {")
+        w("            if (d == 0) { b = pref[PD.tile_lo]; n = pref[PD.tile_hi] - b; }")
+        w("            else {")
+        w("              const int32_t* rp = SGD.ring_prefix + (int64_t)(s % SGD.R) * (SGD.n_tiles + 1);")
+        w("              b = rp[PD.tile_lo]; n = rp[PD.tile_hi] - b;")
+        w("            }")
+        w("          }")
+        w("          s_nd[k] = n; s_base[k] = b;")
+        w("        }")
+        w("        __syncthreads();")
+        w("        {")
+        w("          int carry = 0;")
+        w("          for (int c0 = 0; c0 < W; c0 += blockDim.x) {")
+        w("            const int k = c0 + threadIdx.x;")
+        w("            const int x = k < W ? s_nd[k] : 0;")
+        w("            int tot;")
+        w("            const int ex = b200_block_exscan(x, s_wsum, &tot);")
+        w("            if (k < W) s_ndoff[k] = carry + ex;")
+        w("            carry += tot;")
+        w("          }")
+        w("          if (threadIdx.x == 0) s_ndoff[W] = carry;")
+        w("          __syncthreads();")
+        w("        }")
+        w("        const int Wtot = s_ndoff[W];")
+        w("        const int i0 = (int)((int64_t)Wtot * rank / I.n_cta);")
+        w("        const int i1 = (int)((int64_t)Wtot * (rank + 1) / I.n_cta);")
+        w(f"        const double* const _b200_S = PD.S;")
+        for k, v in enumerate(p.get("vars", [])):
+            w(f"        {v['ctype']}* const {v['ptr']} = ({v['ctype']}*)PD.var[{k}]; (void){v['ptr']};")
+        w(f"        const int32_t* const {p['post_ptr']} = PD.post; (void){p['post_ptr']};")
+        w(f"        const int32_t* const {p['pre_ptr']} = PD.pre; (void){p['pre_ptr']};")
+        for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
+            v = groups[gidx]["vars"][vidx]
+            w(f"        {v['ctype']}* const {ptr} = ({v['ctype']}*)I.g[{gidx}].var[{vidx}]; (void){ptr};")
+        w("        for (int cb = i0; cb < i1; cb += blockDim.x) {")
+        w("          const int it = cb + threadIdx.x;")
+        w("          int len = 0;")
+        w("          if (it < i1) {")
+        w("            const int k = b200_upper_bound(s_ndoff, W + 1, it) - 1;")
+        w("            const int d = PD.dmin + k, r = it - s_ndoff[k];")
+        w("            int32_t src;")
+        w("            if (d == 0) {")
+        w("              const int pos = s_base[k] + r;")
+        w("              const int u = b200_upper_bound(pref, SGD.n_tiles + 1, pos) - 1;")
+        w("              src = SGD.scratch[SGD.tile_start[u] + pos - pref[u]];")
+        w("            } else {")
+        w("              src = SGD.ring[(int64_t)((ts - d) % SGD.R) * SGD.N + s_base[k] + r];")
+        w("            }")
+        w("            const int64_t seg = (int64_t)(src - PD.src_lo) * W + k;")
+        w("            const int64_t lo = PD.segptr[seg];")
+        w("            len = (int)(PD.segptr[seg + 1] - lo);")
+        w("            s_item_seg[threadIdx.x] = lo;")
+        w("            s_item_src[threadIdx.x] = src;")
+        w("          }")
+        w("          int E;")
+        w("          const int off = b200_block_exscan(len, s_wsum, &E);")
+        w("          s_item_off[threadIdx.x] = off;")
+        w("          __syncthreads();")
+        w("          const int nitems = (i1 - cb) < (int)blockDim.x ? (i1 - cb) : (int)blockDim.x;")
+        w("          for (int e = threadIdx.x; e < E; e += blockDim.x) {")
+        w("            const int j = b200_upper_bound(s_item_off, nitems, e) - 1;")
+        w("            const int64_t _idx = s_item_seg[j] + (e - s_item_off[j]);")
+        w("            const int32_t _b200_pre = s_item_src[j]; (void)_b200_pre;")
+        w("            const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+        w("            {")
+        w(_indent(tab.device_loads("on_pre"), 14))
+        w(_indent(blk["vector_device"] if blk.get("vector_device") else blk["vector"], 14))
+        w("            }")
+        w("          }")
+        w("          __syncthreads();")
+        w("        }")
+        w("      }")
+    w("      if (!b200_inst_barrier(I, gen, limit_ns)) { ok = false; break; }")
+    w("    }  // steps")
+
+    # ---- end of launch: apply the reset of the last executed step
+    w("    if (ok && ts > ts0) {")
+    w("      const double _b200_t = (double)(ts - 1) * _b200_dt; (void)_b200_t;")
+    w("      const int64_t _b200_ts = ts - 1;")
+    w(f"      const double* const {clock['t']} = &_b200_t; (void){clock['t']};")
+    w(f"      const double* const {clock['dt']} = &_b200_dt; (void){clock['dt']};")
+    w(f"      const int64_t* const {clock['timestep']} = &_b200_ts; (void){clock['timestep']};")
+    for gi, g in enumerate(groups):
+        tab, blocks = gtables[gi]
+        bd = dict(blocks)
+        if bd["reset"] is None:
+            continue
+        w("      {")
+        w(f"        b200_group_d& GD = I.g[{gi}];")
+        w("        const int32_t N = GD.N; (void)N;")
+        w(f"        const double* const _b200_S = GD.S;")
+        w(group_ptrs(gi, 8))
+        w("        const int u0 = GD.cta_tile[rank], u1 = GD.cta_tile[rank + 1];")
+        w("        for (int u = u0; u < u1; ++u) {")
+        w("          const int cnt = GD.tile_cnt[u], base = GD.tile_start[u];")
+        w("          for (int j = threadIdx.x; j < cnt; j += blockDim.x) {")
+        w("            const int32_t _idx = GD.scratch[base + j];")
+        w("            const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+        w("            {")
+        w(_indent(tab.device_loads("reset"), 14))
+        w(extra_ptrs(g.get("reset"), 14))
+        w(_indent(bd["reset"]["vector"], 14))
+        w("            }")
+        w("          }")
+        w("        }")
+        w("      }")
+    w("    }")
+    w("    __syncthreads();")
+    w("    if (threadIdx.x == 0 && rank == 0) {")
+    w("      *I.ts_done = ts;")
+    for m in range(len(spkmons)):
+        w(f"      *I.sm[{m}].n = s_mon_n[{m}];")
+    for m in range(len(statemons)):
+        w(f"      *I.stm[{m}].n = s_stm_n[{m}];")
+    w("    }")
+    w("    __syncthreads();")
+    w("  }")
+    w("}")
+    w("")
+
+    # ------------------------------------------------------------- launch glue
+    w("static const void* b200_kernel_for(int threads) {")
+    w("  return threads <= 256 ? (const void*)b200_step_kernel<256> : (const void*)b200_step_kernel<1024>;")
+    w("}")
+    w("static int b200_max_active(int threads, int max_tiles1, int max_w) {")
+    w("  const void* k = b200_kernel_for(threads);")
+    w("  const size_t smem = b200_dyn_smem(threads, max_tiles1, max_w);")
+    w("  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);")
+    w("  int n = 0;")
+    w("  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads, smem) != cudaSuccess) return 0;")
+    w("  return n;")
+    w("}")
+    w("static cudaError_t b200_launch(b200_inst_d* insts, const int2* cta_map, int n_inst, int queue_mode,")
+    w("                               int* work, int64_t max_steps, uint64_t limit_ns, int grid, int threads,")
+    w("                               int cooperative, int max_tiles1, int max_w, cudaStream_t s) {")
+    w("  const void* k = b200_kernel_for(threads);")
+    w("  const size_t smem = b200_dyn_smem(threads, max_tiles1, max_w);")
+    w("  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);")
+    w("  if (e != cudaSuccess) return e;")
+    w("  const b200_inst_d* ci = insts;")
+    w("  void* args[] = {(void*)&ci, (void*)&cta_map, (void*)&n_inst, (void*)&queue_mode, (void*)&work,")
+    w("                  (void*)&max_steps, (void*)&limit_ns, (void*)&max_tiles1, (void*)&max_w};")
+    w("  if (cooperative) return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(threads), args, smem, s);")
+    w("  return cudaLaunchKernel(k, dim3(grid), dim3(threads), args, smem, s);")
+    w("}")
+    w("")
+    w(f'static const b200_model_info B200_MODEL = {{"{spec["name"]}", {NG}, {NP}, {len(spkmons)}, {len(ratemons)}, {len(statemons)},')
+    w("  b200_groups, b200_pathways, b200_spkmon, b200_ratemon, b200_statemon,")
+    w(f"  {len(consts)}, b200_const_names, b200_const_defaults, b200_eval_scalars, b200_launch, b200_max_active}};")
+    w("")
+    w('#include "b200_host.h"')
+    w("")
+    return "\n".join(o) + "\n"
+
+
+def spec_tables(spec: dict) -> dict:
+    """Variable tables the Python host uses to address arrays by name."""
+    return {
+        "groups": [[v["name"] for v in g["vars"]] for g in spec["groups"]],
+        "group_kinds": [[CTYPE_KIND[v["ctype"]] for v in g["vars"]] for g in spec["groups"]],
+        "pathways": [[v["name"] for v in p.get("vars", [])] for p in spec.get("pathways", [])],
+        "pathway_kinds": [[CTYPE_KIND[v["ctype"]] for v in p.get("vars", [])] for p in spec.get("pathways", [])],
+        "consts": [c["name"] for c in spec.get("consts", [])],
+    }

@@ -1,0 +1,351 @@
+// Device-side building blocks of the b200 step engine (sm_103a).
+//
+// The generated model file (see brian2_gb300/codegen.py) includes this header
+// and emits one persistent step kernel per model.  Everything here is model
+// independent: the per-instance descriptor layout shared with the host runtime,
+// the bounded instance barrier, order-preserving block compaction, block scans,
+// and the device versions of Brian's C++ function table
+// (brian2/codegen/generators/cpp_generator.py:567-618).
+#pragma once
+#include <cstdint>
+#include <cmath>
+#include <cuda_runtime.h>
+
+#define B200_MAX_GROUPS 4
+#define B200_MAX_PATHWAYS 8
+#define B200_MAX_VARS 24
+#define B200_MAX_SPKMON 4
+#define B200_MAX_RATEMON 4
+#define B200_MAX_STATEMON 4
+#define B200_MAX_THREADS 1024
+#define B200_MAX_WARPS (B200_MAX_THREADS / 32)
+
+// status codes written by kernels (mirrored in include/b200.h)
+#define B200_OK 0
+#define B200_ERR_BARRIER_TIMEOUT 4
+#define B200_ERR_INDEX 5
+
+// ---------------------------------------------------------------------------
+// Descriptors (plain data, filled by the host runtime, read by the kernel).
+// ---------------------------------------------------------------------------
+struct b200_group_d {
+  int32_t N;              // neurons of this group in this instance
+  int32_t R;              // spike-ring slots (max outgoing delay + 1)
+  int32_t n_tiles;        // tiles of this group (each owned by one CTA)
+  int32_t _pad;
+  const int32_t* tile_start;     // [n_tiles+1] first neuron of each tile
+  const int32_t* cta_tile;       // [n_cta+1]  first tile of each CTA of the instance
+  int32_t* scratch;       // [N]       this step's spikes at tile_start[u]+j
+  int32_t* tile_cnt;      // [n_tiles] this step's spike count per tile
+  int32_t* ring;          // [R*N]     spikes of step ts at ring[(ts%R)*N ...] (ascending)
+  int32_t* ring_total;    // [R]       number of spikes stored in each slot
+  int32_t* ring_prefix;   // [R*(n_tiles+1)] per-slot prefix of tile counts
+  void* var[B200_MAX_VARS];      // state variables (SoA, length N)
+  const double* S;        // scalar table (update | threshold | reset)
+};
+
+struct b200_pathway_d {
+  int32_t D;              // largest delay in steps (0 = no delays)
+  int32_t src_lo, src_hi; // presynaptic neuron range within the source group
+  int32_t tile_lo, tile_hi;  // source-group tiles covering [src_lo, src_hi)
+  int32_t dmin;           // smallest delay in steps
+  int64_t n_syn;
+  const int64_t* segptr;  // [(src_hi-src_lo)*(D+1)+1] CSR over (source, delay slot)
+  const int32_t* post;    // [n_syn] target neuron (within target group), CSR order
+  const int32_t* pre;     // [n_syn] source neuron (within source group), CSR order
+  void* var[B200_MAX_VARS];  // synaptic variables in CSR order
+  const double* S;        // scalar table of on_pre
+};
+
+struct b200_spkmon_d {
+  int32_t group, lo, hi, tile_lo, tile_hi, _pad;
+  int64_t cap;            // capacity of i/ts
+  int64_t* n;             // [1] number of recorded spikes
+  int32_t* i;             // [cap] neuron index - lo
+  int32_t* ts;            // [cap] time step of the spike
+  int32_t* count;         // [hi-lo] spikes per neuron
+};
+
+struct b200_ratemon_d {
+  int32_t group, lo, hi, tile_lo, tile_hi, _pad;
+  int64_t step0;          // time step of cnt[0]
+  int64_t cap;            // steps available in cnt
+  int32_t* cnt;           // [cap] spikes in [lo,hi) per step
+};
+
+struct b200_statemon_d {
+  int32_t group, n_rec, n_vars, _pad;
+  const int32_t* idx;     // [n_rec] recorded neuron indices
+  int32_t var_id[8];      // which state variables
+  int32_t var_dbl[8];     // 1 if the variable is double, 0 if float
+  int64_t step0, cap;     // steps available
+  int64_t* n;             // [1] number of recorded steps
+  double* data;           // [cap][n_vars][n_rec] values (as double)
+};
+
+struct b200_inst_d {
+  int32_t cta0, n_cta;    // CTAs [cta0, cta0+n_cta) of the grid run this instance
+  int64_t ts;             // next time step to execute
+  int64_t ts_end;         // stop before this step
+  double dt;
+  unsigned int* bar;      // [2] barrier arrival counter, generation
+  int32_t* status;        // [1] error status of this instance
+  int64_t* ts_done;       // [1] written at exit: first step not executed
+  int32_t* pending_reset; // [B200_MAX_GROUPS] reset of the last step still to apply
+  b200_group_d g[B200_MAX_GROUPS];
+  b200_pathway_d p[B200_MAX_PATHWAYS];
+  b200_spkmon_d sm[B200_MAX_SPKMON];
+  b200_ratemon_d rm[B200_MAX_RATEMON];
+  b200_statemon_d stm[B200_MAX_STATEMON];
+};
+
+static_assert(sizeof(b200_inst_d) % 8 == 0, "descriptor is copied in 8-byte words");
+
+// ---------------------------------------------------------------------------
+// Model tables: emitted by the code generator, read by the host runtime.
+// ---------------------------------------------------------------------------
+enum b200_kind { B200_F64 = 0, B200_F32 = 1, B200_I32 = 2, B200_I8 = 3, B200_I64 = 4 };
+static inline size_t b200_kind_size(int k) {
+  switch (k) {
+    case B200_F64: return 8;
+    case B200_F32: return 4;
+    case B200_I32: return 4;
+    case B200_I8: return 1;
+    case B200_I64: return 8;
+  }
+  return 0;
+}
+
+struct b200_group_info {
+  const char* name;
+  int n_vars;
+  const char* const* var_names;
+  const int* var_kind;
+  int n_scalars;  // size of the scalar table
+};
+struct b200_pathway_info {
+  const char* name;
+  int src_group, tgt_group;
+  int n_vars;
+  const char* const* var_names;
+  const int* var_kind;
+  int n_scalars;
+};
+struct b200_mon_info {
+  const char* name;
+  int group;
+};
+struct b200_model_info {
+  const char* name;
+  int n_groups, n_pathways, n_spkmon, n_ratemon, n_statemon;
+  const b200_group_info* groups;
+  const b200_pathway_info* pathways;
+  const b200_mon_info* spkmon;
+  const b200_mon_info* ratemon;
+  const b200_mon_info* statemon;
+  int n_consts;
+  const char* const* const_names;
+  const double* const_defaults;
+  // evaluates the scalar table of a group (kind 0) or pathway (kind 1)
+  void (*eval_scalars)(int kind, int id, const double* consts, double dt, double* out);
+  // launches the step kernel
+  cudaError_t (*launch)(b200_inst_d* insts, const int2* cta_map, int n_inst, int queue_mode,
+                        int* work, int64_t max_steps, uint64_t limit_ns, int grid, int threads,
+                        int cooperative, int max_tiles1, int max_w, cudaStream_t s);
+  int (*max_active_ctas)(int threads, int max_tiles1, int max_w);
+};
+
+
+// ---------------------------------------------------------------------------
+// Small utilities
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned b200_lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ unsigned b200_ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void b200_st_release(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ uint64_t b200_globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Exclusive block-wide scan of one int per thread.  `wsum` is smem of
+// B200_MAX_WARPS+1 ints.  Returns the exclusive prefix; *total gets the sum.
+// All threads of the block must call it.
+__device__ __forceinline__ int b200_block_exscan(int x, int* wsum, int* total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  int v = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += y;
+  }
+  if (lane == 31) wsum[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    int s = lane < nw ? wsum[lane] : 0;
+    int incl = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane < nw) wsum[lane] = incl - s;
+    if (lane == 31) wsum[B200_MAX_WARPS] = incl;
+  }
+  __syncthreads();
+  const int r = wsum[w] + v - x;
+  *total = wsum[B200_MAX_WARPS];
+  __syncthreads();
+  return r;
+}
+
+// Order-preserving compaction of one flag per thread (warp ballot + scan of the
+// warp counts).  Returns this thread's rank among the set flags of the block in
+// thread order; *total gets the number of set flags.
+__device__ __forceinline__ int b200_block_compact(bool flag, int* wsum, int* total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  const unsigned m = __ballot_sync(0xffffffffu, flag);
+  if (lane == 0) wsum[w] = __popc(m);
+  __syncthreads();
+  if (w == 0) {
+    int s = lane < nw ? wsum[lane] : 0;
+    int incl = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (lane < nw) wsum[lane] = incl - s;
+    if (lane == 31) wsum[B200_MAX_WARPS] = incl;
+  }
+  __syncthreads();
+  const int r = wsum[w] + __popc(m & b200_lanemask_lt());
+  *total = wsum[B200_MAX_WARPS];
+  __syncthreads();
+  return r;
+}
+
+// Barrier over the n_cta CTAs of one instance.  Bounded: after `limit_ns` of
+// waiting the instance status is set to B200_ERR_BARRIER_TIMEOUT and the call
+// returns false, so a kernel never spins forever.  With n_cta == 1 it is a
+// plain __syncthreads.  `gen` is the CTA's private copy of the generation.
+__device__ __forceinline__ bool b200_inst_barrier(const b200_inst_d& I, unsigned& gen,
+                                                  uint64_t limit_ns) {
+  __syncthreads();
+  if (I.n_cta == 1) return true;
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    ok = 1;
+    __threadfence();
+    const unsigned g = gen;
+    const unsigned arrived = atomicAdd(&I.bar[0], 1u);
+    if (arrived == (unsigned)I.n_cta - 1) {
+      I.bar[0] = 0;
+      __threadfence();
+      b200_st_release(&I.bar[1], g + 1);
+    } else {
+      const uint64_t t0 = b200_globaltimer();
+      int spins = 0;
+      while (b200_ld_acquire(&I.bar[1]) == g) {
+        if (++spins > 64) {
+          __nanosleep(64);
+          if ((spins & 255) == 0) {
+            if (b200_globaltimer() - t0 > limit_ns || *((volatile int32_t*)I.status) != 0) {
+              atomicCAS(I.status, 0, B200_ERR_BARRIER_TIMEOUT);
+              ok = 0;
+              break;
+            }
+          }
+        }
+      }
+    }
+    gen = g + 1;
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// ---------------------------------------------------------------------------
+// Brian's function table for device code (same definitions as the C++ target,
+// brian2/codegen/generators/cpp_generator.py:567-618 and
+// brian2/devices/cpp_standalone/brianlib/common_math.h).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double _exprel(double x) {
+  if (fabs(x) < 1e-16) return 1.0;
+  if (x > 717) return INFINITY;
+  return expm1(x) / x;
+}
+__device__ __forceinline__ float _exprel(float x) {
+  if (fabsf(x) < 1e-16f) return 1.0f;
+  if (x > 717.0f) return INFINITY;
+  return expm1f(x) / x;
+}
+template <typename T>
+__device__ __forceinline__ T _clip(const T value, const double a_min, const double a_max) {
+  if (value < a_min) return a_min;
+  if (value > a_max) return a_max;
+  return value;
+}
+__device__ __forceinline__ int _brian_sign(double x) { return (0 < x) - (x < 0); }
+__device__ __forceinline__ double _brian_pow(double a, double b) { return pow(a, b); }
+__device__ __forceinline__ float _brian_pow(float a, float b) { return powf(a, b); }
+__device__ __forceinline__ double _brian_pow(double a, float b) { return pow(a, (double)b); }
+__device__ __forceinline__ double _brian_pow(float a, double b) { return pow((double)a, b); }
+__device__ __forceinline__ double _brian_pow(double a, int b) { return pow(a, (double)b); }
+__device__ __forceinline__ float _brian_pow(float a, int b) { return powf(a, (float)b); }
+__device__ __forceinline__ double _brian_floordiv(double x, double y) { return floor(x / y); }
+__device__ __forceinline__ float _brian_floordiv(float x, float y) { return floorf(x / y); }
+__device__ __forceinline__ int32_t _brian_floordiv(int32_t x, int32_t y) {
+  int32_t q = x / y;
+  if ((x % y != 0) && ((x < 0) != (y < 0))) --q;
+  return q;
+}
+__device__ __forceinline__ int64_t _brian_floordiv(int64_t x, int64_t y) {
+  int64_t q = x / y;
+  if ((x % y != 0) && ((x < 0) != (y < 0))) --q;
+  return q;
+}
+__device__ __forceinline__ double _brian_mod(double x, double y) {
+  double r = fmod(x, y);
+  if (r != 0 && ((r < 0) != (y < 0))) r += y;
+  return r;
+}
+__device__ __forceinline__ int32_t _brian_mod(int32_t x, int32_t y) {
+  int32_t r = x % y;
+  if (r != 0 && ((r < 0) != (y < 0))) r += y;
+  return r;
+}
+__device__ __forceinline__ int64_t _brian_mod(int64_t x, int64_t y) {
+  int64_t r = x % y;
+  if (r != 0 && ((r < 0) != (y < 0))) r += y;
+  return r;
+}
+template <typename T>
+__device__ __forceinline__ int int_(T value) { return (int)value; }
+// core/functions.py:771 timestep(t, dt) = int64((t + 1e-3*dt)/dt)
+__device__ __forceinline__ int64_t _timestep(double t, double dt) {
+  return (int64_t)((t + 1e-3 * dt) / dt);
+}
+#define _brian_abs fabs
+
+// Atomic accumulation used by on_pre statements `x_post += expr`.
+__device__ __forceinline__ void _b200_atomic_add(double* p, double v) { atomicAdd(p, v); }
+__device__ __forceinline__ void _b200_atomic_add(float* p, float v) { atomicAdd(p, v); }
+__device__ __forceinline__ void _b200_atomic_add(float* p, double v) { atomicAdd(p, (float)v); }
+__device__ __forceinline__ void _b200_atomic_add(int32_t* p, int32_t v) { atomicAdd(p, v); }

@@ -1,0 +1,960 @@
+// Host runtime of the b200 step engine: the C ABI declared in include/b200.h.
+//
+// This file is included once by every generated model (.cu) after the model
+// tables (b200_model_info) have been defined, so each model shared library is
+// self-contained: one dlopen, one ctypes.CDLL.  It owns all device memory of a
+// network ("handle"), builds the CSR/delay layout, tiles the neuron groups over
+// CTAs, grows monitor buffers, launches the persistent step kernel and reports
+// errors as status codes with a message (no exit() in library code).
+#pragma once
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "b200_device.cuh"
+
+#define B200_ERR_CUDA 1
+#define B200_ERR_ARG 2
+#define B200_ERR_CAPACITY 3
+
+// ---------------------------------------------------------------------------
+struct b200_dbuf {  // a device buffer owned by the handle
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct b200_group_h {
+  int32_t N = 0;
+  std::vector<b200_dbuf> var;
+  std::vector<int32_t> tile_start, cta_tile;
+  b200_dbuf d_tile_start, d_cta_tile, scratch, tile_cnt, ring, ring_total, ring_prefix;
+  b200_dbuf S;
+  int32_t R = 1;
+};
+struct b200_pathway_h {
+  int32_t src_lo = 0, src_hi = 0, tgt_lo = 0, tgt_hi = 0;
+  int32_t dmin = 0, dmax = 0;
+  int64_t n_syn = 0;
+  bool has_syn = false;
+  std::vector<int64_t> perm;  // perm[csr position] = synapse index (creation order)
+  b200_dbuf segptr, post, pre, S;
+  std::vector<b200_dbuf> var;
+};
+struct b200_spkmon_h {
+  int32_t lo = 0, hi = 0;
+  int64_t cap = 0;
+  b200_dbuf n, i, ts, count;
+};
+struct b200_ratemon_h {
+  int32_t lo = 0, hi = 0;
+  int64_t step0 = 0, cap = 0, n = 0;
+  b200_dbuf cnt;
+};
+struct b200_statemon_h {
+  int32_t n_rec = 0, n_vars = 0;
+  std::vector<int32_t> idx, vars;
+  int64_t step0 = 0, cap = 0;
+  b200_dbuf d_idx, n, data;
+};
+struct b200_inst_h {
+  std::vector<double> consts;
+  std::vector<b200_group_h> g;
+  std::vector<b200_pathway_h> p;
+  std::vector<b200_spkmon_h> sm;
+  std::vector<b200_ratemon_h> rm;
+  std::vector<b200_statemon_h> stm;
+  int32_t n_cta = 1;
+  int64_t ts = 0;
+  b200_dbuf bar, status, ts_done, pending;
+};
+
+struct b200_net {
+  const b200_model_info* M = nullptr;
+  int n_inst = 0;
+  double dt = 1e-4;
+  std::vector<b200_inst_h> inst;
+  b200_dbuf d_insts, d_cta_map, d_work;
+  std::vector<b200_inst_d> h_insts;
+  cudaStream_t stream = nullptr;
+  int threads = 256;
+  int max_tiles1 = 2, max_w = 1;  // dynamic shared-memory extents
+  int queue_mode = 0;      // 1: single-CTA instances pulled from a work queue
+  int grid = 0;
+  int64_t chunk_steps = 100000;
+  uint64_t limit_ns = 2000000000ull;  // bounded waits: 2 s
+  bool prepared = false;
+  bool use_graph = true;
+  cudaGraphExec_t graph_exec = nullptr;
+  int64_t graph_steps = -1;
+  int64_t launches = 0;
+  double last_run_ms = 0.0;
+  std::string err;
+  size_t device_bytes = 0;
+};
+
+static int b200_fail(b200_net* n, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (n) n->err = buf;
+  return code;
+}
+
+#define B200_CU(net, call)                                                              \
+  do {                                                                                  \
+    cudaError_t _e = (call);                                                            \
+    if (_e != cudaSuccess)                                                              \
+      return b200_fail(net, B200_ERR_CUDA, "%s failed: %s (%s:%d)", #call,              \
+                       cudaGetErrorString(_e), __FILE__, __LINE__);                     \
+  } while (0)
+
+static int b200_alloc(b200_net* n, b200_dbuf& b, size_t bytes, bool zero = true) {
+  if (b.p && b.bytes >= bytes && bytes > 0) {
+    if (zero) B200_CU(n, cudaMemsetAsync(b.p, 0, bytes, n->stream));
+    return 0;
+  }
+  if (b.p) {
+    cudaFree(b.p);
+    n->device_bytes -= b.bytes;
+    b.p = nullptr;
+    b.bytes = 0;
+  }
+  size_t a = bytes ? bytes : 16;
+  B200_CU(n, cudaMalloc(&b.p, a));
+  b.bytes = a;
+  n->device_bytes += a;
+  if (zero) B200_CU(n, cudaMemsetAsync(b.p, 0, a, n->stream));
+  return 0;
+}
+static void b200_free(b200_net* n, b200_dbuf& b) {
+  if (b.p) {
+    cudaFree(b.p);
+    if (n) n->device_bytes -= b.bytes;
+  }
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+extern "C" {
+
+// ----------------------------------------------------------------- lifecycle
+int b200_create(b200_net** out, int32_t n_inst, const int32_t* group_sizes, double dt) {
+  if (!out || n_inst <= 0 || !group_sizes || !(dt > 0)) return B200_ERR_ARG;
+  b200_net* n = new b200_net();
+  n->M = &B200_MODEL;
+  n->n_inst = n_inst;
+  n->dt = dt;
+  n->inst.resize(n_inst);
+  cudaError_t e = cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    *out = n;
+    return b200_fail(n, B200_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  }
+  const b200_model_info* M = n->M;
+  for (int k = 0; k < n_inst; ++k) {
+    b200_inst_h& I = n->inst[k];
+    I.consts.assign(M->const_defaults, M->const_defaults + M->n_consts);
+    I.g.resize(M->n_groups);
+    I.p.resize(M->n_pathways);
+    I.sm.resize(M->n_spkmon);
+    I.rm.resize(M->n_ratemon);
+    I.stm.resize(M->n_statemon);
+    for (int g = 0; g < M->n_groups; ++g) {
+      b200_group_h& G = I.g[g];
+      G.N = group_sizes[k * M->n_groups + g];
+      if (G.N < 0) {
+        *out = n;
+        return b200_fail(n, B200_ERR_ARG, "negative group size");
+      }
+      G.var.resize(M->groups[g].n_vars);
+      for (int v = 0; v < M->groups[g].n_vars; ++v) {
+        int r = b200_alloc(n, G.var[v], (size_t)G.N * b200_kind_size(M->groups[g].var_kind[v]));
+        if (r) {
+          *out = n;
+          return r;
+        }
+      }
+    }
+    for (int p = 0; p < M->n_pathways; ++p) {
+      const b200_pathway_info& P = M->pathways[p];
+      I.p[p].src_hi = I.g[P.src_group].N;
+      I.p[p].tgt_hi = I.g[P.tgt_group].N;
+      I.p[p].var.resize(P.n_vars);
+    }
+    for (int s = 0; s < M->n_spkmon; ++s) I.sm[s].hi = I.g[M->spkmon[s].group].N;
+    for (int s = 0; s < M->n_ratemon; ++s) I.rm[s].hi = I.g[M->ratemon[s].group].N;
+  }
+  *out = n;
+  return 0;
+}
+
+int b200_destroy(b200_net* n) {
+  if (!n) return 0;
+  cudaStreamSynchronize(n->stream);
+  if (n->graph_exec) cudaGraphExecDestroy(n->graph_exec);
+  for (auto& I : n->inst) {
+    for (auto& G : I.g) {
+      for (auto& b : G.var) b200_free(n, b);
+      b200_free(n, G.d_tile_start); b200_free(n, G.d_cta_tile); b200_free(n, G.scratch);
+      b200_free(n, G.tile_cnt); b200_free(n, G.ring); b200_free(n, G.ring_total);
+      b200_free(n, G.ring_prefix); b200_free(n, G.S);
+    }
+    for (auto& P : I.p) {
+      for (auto& b : P.var) b200_free(n, b);
+      b200_free(n, P.segptr); b200_free(n, P.post); b200_free(n, P.pre); b200_free(n, P.S);
+    }
+    for (auto& S : I.sm) { b200_free(n, S.n); b200_free(n, S.i); b200_free(n, S.ts); b200_free(n, S.count); }
+    for (auto& S : I.rm) b200_free(n, S.cnt);
+    for (auto& S : I.stm) { b200_free(n, S.d_idx); b200_free(n, S.n); b200_free(n, S.data); }
+    b200_free(n, I.bar); b200_free(n, I.status); b200_free(n, I.ts_done); b200_free(n, I.pending);
+  }
+  b200_free(n, n->d_insts); b200_free(n, n->d_cta_map); b200_free(n, n->d_work);
+  if (n->stream) cudaStreamDestroy(n->stream);
+  delete n;
+  return 0;
+}
+
+int b200_last_error(b200_net* n, char* buf, int64_t len) {
+  if (!buf || len <= 0) return B200_ERR_ARG;
+  const char* s = n ? n->err.c_str() : "null handle";
+  snprintf(buf, (size_t)len, "%s", s);
+  return 0;
+}
+
+// Launch shape.  threads: CTA size (32..1024, multiple of 32).  ctas_per_inst:
+// CTAs cooperating on one instance (>1 uses the bounded instance barrier).
+// queue_mode: 1 lets a grid of resident CTAs pull single-CTA instances from a
+// work queue (batched sweeps).  chunk_steps: steps per kernel launch.
+int b200_configure(b200_net* n, int32_t threads, const int32_t* ctas_per_inst, int32_t queue_mode,
+                   int64_t chunk_steps, int32_t use_graph) {
+  if (!n) return B200_ERR_ARG;
+  if (threads < 32 || threads > B200_MAX_THREADS || threads % 32)
+    return b200_fail(n, B200_ERR_ARG, "threads must be a multiple of 32 in [32,1024]");
+  n->threads = threads;
+  n->queue_mode = queue_mode ? 1 : 0;
+  if (chunk_steps > 0) n->chunk_steps = chunk_steps;
+  n->use_graph = use_graph != 0;
+  for (int k = 0; k < n->n_inst; ++k) {
+    int c = ctas_per_inst ? ctas_per_inst[k] : 1;
+    if (c < 1) return b200_fail(n, B200_ERR_ARG, "ctas_per_inst must be >= 1");
+    if (n->queue_mode && c != 1) return b200_fail(n, B200_ERR_ARG, "queue mode needs 1 CTA per instance");
+    n->inst[k].n_cta = c;
+  }
+  n->prepared = false;
+  return 0;
+}
+
+int b200_set_consts(b200_net* n, int32_t inst, const double* values, int32_t count) {
+  if (!n || inst < 0 || inst >= n->n_inst || count != n->M->n_consts) return B200_ERR_ARG;
+  n->inst[inst].consts.assign(values, values + count);
+  n->prepared = false;
+  return 0;
+}
+
+// kind 0: group state variable (obj = group, var = index); kind 1: synaptic
+// variable (obj = pathway) given in synapse creation order.
+static int b200_var_buf(b200_net* n, int32_t inst, int32_t kind, int32_t obj, int32_t var,
+                        b200_dbuf** buf, int* vkind, int64_t* count) {
+  if (!n || inst < 0 || inst >= n->n_inst) return b200_fail(n, B200_ERR_ARG, "bad instance");
+  b200_inst_h& I = n->inst[inst];
+  if (kind == 0) {
+    if (obj < 0 || obj >= n->M->n_groups || var < 0 || var >= n->M->groups[obj].n_vars)
+      return b200_fail(n, B200_ERR_ARG, "bad group variable %d/%d", obj, var);
+    *buf = &I.g[obj].var[var];
+    *vkind = n->M->groups[obj].var_kind[var];
+    *count = I.g[obj].N;
+  } else if (kind == 1) {
+    if (obj < 0 || obj >= n->M->n_pathways || var < 0 || var >= n->M->pathways[obj].n_vars)
+      return b200_fail(n, B200_ERR_ARG, "bad synaptic variable %d/%d", obj, var);
+    if (!I.p[obj].has_syn) return b200_fail(n, B200_ERR_ARG, "synapses of pathway %d not set", obj);
+    *buf = &I.p[obj].var[var];
+    *vkind = n->M->pathways[obj].var_kind[var];
+    *count = I.p[obj].n_syn;
+  } else {
+    return b200_fail(n, B200_ERR_ARG, "bad kind");
+  }
+  return 0;
+}
+
+int b200_upload(b200_net* n, int32_t inst, int32_t kind, int32_t obj, int32_t var,
+                const void* src, int64_t count) {
+  b200_dbuf* b;
+  int vk;
+  int64_t cnt;
+  int r = b200_var_buf(n, inst, kind, obj, var, &b, &vk, &cnt);
+  if (r) return r;
+  if (count != cnt) return b200_fail(n, B200_ERR_ARG, "upload size %lld != %lld", (long long)count, (long long)cnt);
+  const size_t es = b200_kind_size(vk);
+  if (kind == 0) {
+    B200_CU(n, cudaMemcpyAsync(b->p, src, (size_t)cnt * es, cudaMemcpyHostToDevice, n->stream));
+  } else {
+    // permute creation order -> CSR order
+    const std::vector<int64_t>& perm = n->inst[inst].p[obj].perm;
+    std::vector<char> tmp((size_t)cnt * es);
+    const char* s = (const char*)src;
+    for (int64_t k = 0; k < cnt; ++k) memcpy(&tmp[(size_t)k * es], s + (size_t)perm[k] * es, es);
+    B200_CU(n, cudaMemcpyAsync(b->p, tmp.data(), tmp.size(), cudaMemcpyHostToDevice, n->stream));
+  }
+  B200_CU(n, cudaStreamSynchronize(n->stream));
+  return 0;
+}
+
+int b200_download(b200_net* n, int32_t inst, int32_t kind, int32_t obj, int32_t var, void* dst,
+                  int64_t count) {
+  b200_dbuf* b;
+  int vk;
+  int64_t cnt;
+  int r = b200_var_buf(n, inst, kind, obj, var, &b, &vk, &cnt);
+  if (r) return r;
+  if (count != cnt) return b200_fail(n, B200_ERR_ARG, "download size mismatch");
+  const size_t es = b200_kind_size(vk);
+  if (kind == 0) {
+    B200_CU(n, cudaMemcpyAsync(dst, b->p, (size_t)cnt * es, cudaMemcpyDeviceToHost, n->stream));
+    B200_CU(n, cudaStreamSynchronize(n->stream));
+  } else {
+    std::vector<char> tmp((size_t)cnt * es);
+    B200_CU(n, cudaMemcpyAsync(tmp.data(), b->p, tmp.size(), cudaMemcpyDeviceToHost, n->stream));
+    B200_CU(n, cudaStreamSynchronize(n->stream));
+    const std::vector<int64_t>& perm = n->inst[inst].p[obj].perm;
+    char* d = (char*)dst;
+    for (int64_t k = 0; k < cnt; ++k) memcpy(d + (size_t)perm[k] * es, &tmp[(size_t)k * es], es);
+  }
+  return 0;
+}
+
+// Synapses of one pathway in creation order (brian2/synapses/synapses.py:2074):
+// pre/post are indices within the source/target subgroup ranges
+// [src_lo,src_hi) / [tgt_lo,tgt_hi) of their groups; delay_steps holds the
+// quantised delay of each synapse, or NULL for the single delay `scalar_delay`.
+// Replaces CSpikeQueue::prepare (brian2/synapses/spikequeue.h:45-105): the
+// per-source synapse lists become one CSR over (source, delay slot), built by a
+// stable counting sort so each segment keeps creation order.
+int b200_set_synapses(b200_net* n, int32_t inst, int32_t pw, int32_t src_lo, int32_t src_hi,
+                      int32_t tgt_lo, int32_t tgt_hi, const int32_t* pre, const int32_t* post,
+                      const int32_t* delay_steps, int32_t scalar_delay, int64_t n_syn) {
+  if (!n || inst < 0 || inst >= n->n_inst || pw < 0 || pw >= n->M->n_pathways)
+    return b200_fail(n, B200_ERR_ARG, "bad instance/pathway");
+  b200_inst_h& I = n->inst[inst];
+  const b200_pathway_info& PI = n->M->pathways[pw];
+  b200_pathway_h& P = I.p[pw];
+  const int32_t Ns = I.g[PI.src_group].N, Nt = I.g[PI.tgt_group].N;
+  if (src_lo < 0 || src_hi > Ns || src_lo > src_hi || tgt_lo < 0 || tgt_hi > Nt || tgt_lo > tgt_hi)
+    return b200_fail(n, B200_ERR_ARG, "bad source/target range");
+  if (n_syn < 0 || (n_syn > 0 && (!pre || !post))) return b200_fail(n, B200_ERR_ARG, "bad synapse arrays");
+  const int32_t ns = src_hi - src_lo;
+  int32_t dmin = 0, dmax = 0;
+  if (delay_steps && n_syn > 0) {
+    dmin = dmax = delay_steps[0];
+    for (int64_t k = 0; k < n_syn; ++k) {
+      dmin = std::min(dmin, delay_steps[k]);
+      dmax = std::max(dmax, delay_steps[k]);
+    }
+    if (dmin < 0) return b200_fail(n, B200_ERR_ARG, "negative delay");
+  } else {
+    if (scalar_delay < 0) return b200_fail(n, B200_ERR_ARG, "negative delay");
+    dmin = dmax = scalar_delay;
+  }
+  const int32_t W = dmax - dmin + 1;
+  std::vector<int64_t> seg((size_t)ns * W + 1, 0);
+  for (int64_t k = 0; k < n_syn; ++k) {
+    const int32_t s = pre[k], t = post[k];
+    if (s < 0 || s >= ns || t < 0 || t >= tgt_hi - tgt_lo)
+      return b200_fail(n, B200_ERR_INDEX, "synapse %lld index out of range (pre %d, post %d)", (long long)k, s, t);
+    const int32_t d = delay_steps ? delay_steps[k] - dmin : 0;
+    seg[(size_t)s * W + d + 1]++;
+  }
+  for (size_t k = 1; k < seg.size(); ++k) seg[k] += seg[k - 1];
+  std::vector<int64_t> fill(seg.begin(), seg.end() - 1);
+  P.perm.assign((size_t)n_syn, 0);
+  std::vector<int32_t> cpost((size_t)n_syn), cpre((size_t)n_syn);
+  for (int64_t k = 0; k < n_syn; ++k) {
+    const int32_t s = pre[k];
+    const int32_t d = delay_steps ? delay_steps[k] - dmin : 0;
+    const int64_t pos = fill[(size_t)s * W + d]++;
+    P.perm[pos] = k;
+    cpost[pos] = post[k] + tgt_lo;  // stored as index within the target group
+    cpre[pos] = s + src_lo;         // index within the source group
+  }
+  P.src_lo = src_lo; P.src_hi = src_hi; P.tgt_lo = tgt_lo; P.tgt_hi = tgt_hi;
+  P.dmin = dmin; P.dmax = dmax; P.n_syn = n_syn; P.has_syn = true;
+  int r;
+  if ((r = b200_alloc(n, P.segptr, seg.size() * 8, false))) return r;
+  if ((r = b200_alloc(n, P.post, (size_t)n_syn * 4, false))) return r;
+  if ((r = b200_alloc(n, P.pre, (size_t)n_syn * 4, false))) return r;
+  B200_CU(n, cudaMemcpyAsync(P.segptr.p, seg.data(), seg.size() * 8, cudaMemcpyHostToDevice, n->stream));
+  if (n_syn) {
+    B200_CU(n, cudaMemcpyAsync(P.post.p, cpost.data(), (size_t)n_syn * 4, cudaMemcpyHostToDevice, n->stream));
+    B200_CU(n, cudaMemcpyAsync(P.pre.p, cpre.data(), (size_t)n_syn * 4, cudaMemcpyHostToDevice, n->stream));
+  }
+  for (int v = 0; v < PI.n_vars; ++v)
+    if ((r = b200_alloc(n, P.var[v], (size_t)n_syn * b200_kind_size(PI.var_kind[v])))) return r;
+  B200_CU(n, cudaStreamSynchronize(n->stream));
+  n->prepared = false;
+  return 0;
+}
+
+// Adopts a CSR that was built on the device (scale-mode construction).  The
+// arrays are copied; the synapse order is the CSR order itself.
+int b200_set_synapses_csr(b200_net* n, int32_t inst, int32_t pw, int32_t src_lo, int32_t src_hi,
+                          int32_t tgt_lo, int32_t tgt_hi, int32_t dmin, int32_t dmax,
+                          const int64_t* d_segptr, const int32_t* d_post, const int32_t* d_pre,
+                          int64_t n_syn) {
+  if (!n || inst < 0 || inst >= n->n_inst || pw < 0 || pw >= n->M->n_pathways)
+    return b200_fail(n, B200_ERR_ARG, "bad instance/pathway");
+  b200_inst_h& I = n->inst[inst];
+  const b200_pathway_info& PI = n->M->pathways[pw];
+  b200_pathway_h& P = I.p[pw];
+  if (dmin < 0 || dmax < dmin) return b200_fail(n, B200_ERR_ARG, "bad delay range");
+  const int64_t nseg = (int64_t)(src_hi - src_lo) * (dmax - dmin + 1) + 1;
+  int r;
+  if ((r = b200_alloc(n, P.segptr, (size_t)nseg * 8, false))) return r;
+  if ((r = b200_alloc(n, P.post, (size_t)n_syn * 4, false))) return r;
+  if ((r = b200_alloc(n, P.pre, (size_t)n_syn * 4, false))) return r;
+  B200_CU(n, cudaMemcpyAsync(P.segptr.p, d_segptr, (size_t)nseg * 8, cudaMemcpyDeviceToDevice, n->stream));
+  B200_CU(n, cudaMemcpyAsync(P.post.p, d_post, (size_t)n_syn * 4, cudaMemcpyDeviceToDevice, n->stream));
+  B200_CU(n, cudaMemcpyAsync(P.pre.p, d_pre, (size_t)n_syn * 4, cudaMemcpyDeviceToDevice, n->stream));
+  P.perm.resize((size_t)n_syn);
+  for (int64_t k = 0; k < n_syn; ++k) P.perm[k] = k;
+  P.src_lo = src_lo; P.src_hi = src_hi; P.tgt_lo = tgt_lo; P.tgt_hi = tgt_hi;
+  P.dmin = dmin; P.dmax = dmax; P.n_syn = n_syn; P.has_syn = true;
+  for (int v = 0; v < PI.n_vars; ++v)
+    if ((r = b200_alloc(n, P.var[v], (size_t)n_syn * b200_kind_size(PI.var_kind[v])))) return r;
+  B200_CU(n, cudaStreamSynchronize(n->stream));
+  n->prepared = false;
+  return 0;
+}
+
+// Device pointer of a synaptic variable (CSR order), for device-side fills.
+int b200_synapse_var_ptr(b200_net* n, int32_t inst, int32_t pw, int32_t var, void** out) {
+  b200_dbuf* b;
+  int vk;
+  int64_t cnt;
+  int r = b200_var_buf(n, inst, 1, pw, var, &b, &vk, &cnt);
+  if (r) return r;
+  *out = b->p;
+  return 0;
+}
+
+int b200_set_monitor_range(b200_net* n, int32_t inst, int32_t kind, int32_t mon, int32_t lo, int32_t hi) {
+  if (!n || inst < 0 || inst >= n->n_inst) return B200_ERR_ARG;
+  b200_inst_h& I = n->inst[inst];
+  if (kind == 0 && mon >= 0 && mon < n->M->n_spkmon) {
+    const int32_t N = I.g[n->M->spkmon[mon].group].N;
+    if (lo < 0 || hi > N || lo > hi) return b200_fail(n, B200_ERR_ARG, "bad monitor range");
+    I.sm[mon].lo = lo; I.sm[mon].hi = hi;
+  } else if (kind == 1 && mon >= 0 && mon < n->M->n_ratemon) {
+    const int32_t N = I.g[n->M->ratemon[mon].group].N;
+    if (lo < 0 || hi > N || lo > hi) return b200_fail(n, B200_ERR_ARG, "bad monitor range");
+    I.rm[mon].lo = lo; I.rm[mon].hi = hi;
+  } else {
+    return b200_fail(n, B200_ERR_ARG, "bad monitor");
+  }
+  n->prepared = false;
+  return 0;
+}
+
+// StateMonitor: record variables `vars` of neurons `idx` at the start of every step.
+int b200_set_statemon(b200_net* n, int32_t inst, int32_t mon, const int32_t* idx, int32_t n_rec,
+                      const int32_t* vars, int32_t n_vars) {
+  if (!n || inst < 0 || inst >= n->n_inst || mon < 0 || mon >= n->M->n_statemon) return B200_ERR_ARG;
+  if (n_vars > 8 || n_vars < 0 || n_rec < 0) return b200_fail(n, B200_ERR_ARG, "bad state monitor");
+  b200_statemon_h& S = n->inst[inst].stm[mon];
+  const int g = n->M->statemon[mon].group;
+  for (int k = 0; k < n_rec; ++k)
+    if (idx[k] < 0 || idx[k] >= n->inst[inst].g[g].N) return b200_fail(n, B200_ERR_INDEX, "bad record index");
+  for (int k = 0; k < n_vars; ++k)
+    if (vars[k] < 0 || vars[k] >= n->M->groups[g].n_vars) return b200_fail(n, B200_ERR_ARG, "bad var");
+  S.idx.assign(idx, idx + n_rec);
+  S.vars.assign(vars, vars + n_vars);
+  S.n_rec = n_rec;
+  S.n_vars = n_vars;
+  n->prepared = false;
+  return 0;
+}
+
+}  // extern "C"
+
+// ----------------------------------------------------------------- prepare
+// Tiles of one group: contiguous neuron ranges, each owned by one CTA, whose
+// boundaries include every source/monitor range boundary so that the spikes of
+// any such range are a contiguous run of tiles.
+static void b200_make_tiles(int32_t N, int n_cta, std::vector<int32_t> cuts,
+                            std::vector<int32_t>& tile_start, std::vector<int32_t>& cta_tile) {
+  cuts.push_back(0);
+  cuts.push_back(N);
+  const int32_t target = std::max<int32_t>(1, (N + n_cta - 1) / n_cta);
+  for (int32_t x = target; x < N; x += target) cuts.push_back(x);
+  std::sort(cuts.begin(), cuts.end());
+  cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
+  tile_start = cuts;  // tiles [cuts[u], cuts[u+1])
+  const int n_tiles = (int)tile_start.size() - 1;
+  cta_tile.assign(n_cta + 1, n_tiles);
+  // CTA c owns the tiles whose start lies in [c*target, (c+1)*target)
+  int u = 0;
+  for (int c = 0; c < n_cta; ++c) {
+    cta_tile[c] = u;
+    const int64_t end = (int64_t)(c + 1) * target;
+    while (u < n_tiles && tile_start[u] < end) ++u;
+  }
+  cta_tile[n_cta] = n_tiles;
+}
+
+static int b200_prepare(b200_net* n) {
+  const b200_model_info* M = n->M;
+  int r;
+  n->h_insts.assign(n->n_inst, b200_inst_d());
+  std::vector<int2> cta_map;
+  int cta = 0;
+  for (int k = 0; k < n->n_inst; ++k) {
+    b200_inst_h& I = n->inst[k];
+    b200_inst_d& D = n->h_insts[k];
+    memset(&D, 0, sizeof(D));
+    D.n_cta = I.n_cta;
+    D.cta0 = n->queue_mode ? 0 : cta;
+    if (!n->queue_mode)
+      for (int c = 0; c < I.n_cta; ++c) cta_map.push_back(make_int2(k, c));
+    cta += I.n_cta;
+    D.ts = I.ts;
+    D.dt = n->dt;
+    if ((r = b200_alloc(n, I.bar, 16))) return r;
+    if ((r = b200_alloc(n, I.status, 16))) return r;
+    if ((r = b200_alloc(n, I.ts_done, 16))) return r;
+    if ((r = b200_alloc(n, I.pending, 16 * 4))) return r;
+    D.bar = (unsigned*)I.bar.p;
+    D.status = (int32_t*)I.status.p;
+    D.ts_done = (int64_t*)I.ts_done.p;
+    D.pending_reset = (int32_t*)I.pending.p;
+    for (int g = 0; g < M->n_groups; ++g) {
+      b200_group_h& G = I.g[g];
+      std::vector<int32_t> cuts;
+      int32_t R = 1;
+      for (int p = 0; p < M->n_pathways; ++p)
+        if (M->pathways[p].src_group == g) {
+          cuts.push_back(I.p[p].src_lo);
+          cuts.push_back(I.p[p].src_hi);
+          R = std::max(R, I.p[p].dmax + 1);
+        }
+      for (int s = 0; s < M->n_spkmon; ++s)
+        if (M->spkmon[s].group == g) { cuts.push_back(I.sm[s].lo); cuts.push_back(I.sm[s].hi); }
+      for (int s = 0; s < M->n_ratemon; ++s)
+        if (M->ratemon[s].group == g) { cuts.push_back(I.rm[s].lo); cuts.push_back(I.rm[s].hi); }
+      const std::vector<int32_t> old_tiles = G.tile_start;
+      b200_make_tiles(G.N, I.n_cta, cuts, G.tile_start, G.cta_tile);
+      const int n_tiles = (int)G.tile_start.size() - 1;
+      const bool ring_changed = (R != G.R) || !G.ring.p;
+      const bool retile = !ring_changed && old_tiles != G.tile_start && I.ts > 0 && R > 1;
+      G.R = R;
+      if ((r = b200_alloc(n, G.d_tile_start, G.tile_start.size() * 4, false))) return r;
+      if ((r = b200_alloc(n, G.d_cta_tile, G.cta_tile.size() * 4, false))) return r;
+      B200_CU(n, cudaMemcpyAsync(G.d_tile_start.p, G.tile_start.data(), G.tile_start.size() * 4, cudaMemcpyHostToDevice, n->stream));
+      B200_CU(n, cudaMemcpyAsync(G.d_cta_tile.p, G.cta_tile.data(), G.cta_tile.size() * 4, cudaMemcpyHostToDevice, n->stream));
+      if ((r = b200_alloc(n, G.scratch, (size_t)std::max(G.N, 1) * 4, false))) return r;
+      if ((r = b200_alloc(n, G.tile_cnt, (size_t)n_tiles * 4))) return r;
+      if (ring_changed) {
+        // the ring keeps spikes in flight across runs; it is only rebuilt when
+        // its size changes (first run, or new delays)
+        if ((r = b200_alloc(n, G.ring, (size_t)R * std::max(G.N, 1) * 4))) return r;
+        if ((r = b200_alloc(n, G.ring_total, (size_t)R * 4))) return r;
+      }
+      if ((r = b200_alloc(n, G.ring_prefix, (size_t)R * (n_tiles + 1) * 4, ring_changed))) return r;
+      if (retile) {
+        // spikes still in flight were indexed by the old tiles: recount them
+        std::vector<int32_t> tot(R), ring((size_t)R * G.N), pre((size_t)R * (n_tiles + 1));
+        B200_CU(n, cudaMemcpy(tot.data(), G.ring_total.p, (size_t)R * 4, cudaMemcpyDeviceToHost));
+        B200_CU(n, cudaMemcpy(ring.data(), G.ring.p, (size_t)R * G.N * 4, cudaMemcpyDeviceToHost));
+        for (int s = 0; s < R; ++s) {
+          const int32_t* a = ring.data() + (size_t)s * G.N;
+          for (int u = 0; u <= n_tiles; ++u)
+            pre[(size_t)s * (n_tiles + 1) + u] =
+                (int32_t)(std::lower_bound(a, a + tot[s], G.tile_start[u]) - a);
+        }
+        B200_CU(n, cudaMemcpy(G.ring_prefix.p, pre.data(), pre.size() * 4, cudaMemcpyHostToDevice));
+      }
+      std::vector<double> S(std::max(M->groups[g].n_scalars, 1));
+      M->eval_scalars(0, g, I.consts.data(), n->dt, S.data());
+      if ((r = b200_alloc(n, G.S, S.size() * 8, false))) return r;
+      B200_CU(n, cudaMemcpyAsync(G.S.p, S.data(), S.size() * 8, cudaMemcpyHostToDevice, n->stream));
+      B200_CU(n, cudaStreamSynchronize(n->stream));
+      b200_group_d& GD = D.g[g];
+      GD.N = G.N; GD.R = R; GD.n_tiles = n_tiles;
+      GD.tile_start = (const int32_t*)G.d_tile_start.p;
+      GD.cta_tile = (const int32_t*)G.d_cta_tile.p;
+      GD.scratch = (int32_t*)G.scratch.p;
+      GD.tile_cnt = (int32_t*)G.tile_cnt.p;
+      GD.ring = (int32_t*)G.ring.p;
+      GD.ring_total = (int32_t*)G.ring_total.p;
+      GD.ring_prefix = (int32_t*)G.ring_prefix.p;
+      for (int v = 0; v < M->groups[g].n_vars; ++v) GD.var[v] = G.var[v].p;
+      GD.S = (const double*)G.S.p;
+    }
+    for (int p = 0; p < M->n_pathways; ++p) {
+      b200_pathway_h& P = I.p[p];
+      const b200_pathway_info& PI = M->pathways[p];
+      if (!P.has_syn) {
+        // no synapses: an empty CSR over the whole source group
+        std::vector<int32_t> none;
+        if ((r = b200_set_synapses(n, k, p, 0, I.g[PI.src_group].N, 0, I.g[PI.tgt_group].N,
+                                   none.data(), none.data(), nullptr, 0, 0)))
+          return r;
+      }
+      b200_pathway_d& PD = D.p[p];
+      const b200_group_h& SG = I.g[PI.src_group];
+      PD.D = P.dmax;
+      PD.src_lo = P.src_lo; PD.src_hi = P.src_hi;
+      PD.tile_lo = (int)(std::lower_bound(SG.tile_start.begin(), SG.tile_start.end(), P.src_lo) - SG.tile_start.begin());
+      PD.tile_hi = (int)(std::lower_bound(SG.tile_start.begin(), SG.tile_start.end(), P.src_hi) - SG.tile_start.begin());
+      PD.dmin = P.dmin;
+      PD.n_syn = P.n_syn;
+      PD.segptr = (const int64_t*)P.segptr.p;
+      PD.post = (const int32_t*)P.post.p;
+      PD.pre = (const int32_t*)P.pre.p;
+      for (int v = 0; v < PI.n_vars; ++v) PD.var[v] = P.var[v].p;
+      std::vector<double> S(std::max(PI.n_scalars, 1));
+      M->eval_scalars(1, p, I.consts.data(), n->dt, S.data());
+      if ((r = b200_alloc(n, P.S, S.size() * 8, false))) return r;
+      B200_CU(n, cudaMemcpyAsync(P.S.p, S.data(), S.size() * 8, cudaMemcpyHostToDevice, n->stream));
+      B200_CU(n, cudaStreamSynchronize(n->stream));
+      PD.S = (const double*)P.S.p;
+    }
+    for (int s = 0; s < M->n_spkmon; ++s) {
+      b200_spkmon_h& S = I.sm[s];
+      const b200_group_h& G = I.g[M->spkmon[s].group];
+      if (!S.n.p) {
+        if ((r = b200_alloc(n, S.n, 16))) return r;
+        if ((r = b200_alloc(n, S.count, (size_t)std::max(S.hi - S.lo, 1) * 4))) return r;
+      }
+      if (!S.i.p) {
+        S.cap = std::max<int64_t>(1 << 16, 8 * (int64_t)(S.hi - S.lo));
+        if ((r = b200_alloc(n, S.i, (size_t)S.cap * 4, false))) return r;
+        if ((r = b200_alloc(n, S.ts, (size_t)S.cap * 4, false))) return r;
+      }
+      b200_spkmon_d& SD = D.sm[s];
+      SD.group = M->spkmon[s].group; SD.lo = S.lo; SD.hi = S.hi;
+      SD.tile_lo = (int)(std::lower_bound(G.tile_start.begin(), G.tile_start.end(), S.lo) - G.tile_start.begin());
+      SD.tile_hi = (int)(std::lower_bound(G.tile_start.begin(), G.tile_start.end(), S.hi) - G.tile_start.begin());
+      SD.cap = S.cap;
+      SD.n = (int64_t*)S.n.p; SD.i = (int32_t*)S.i.p; SD.ts = (int32_t*)S.ts.p;
+      SD.count = (int32_t*)S.count.p;
+    }
+    for (int s = 0; s < M->n_ratemon; ++s) {
+      b200_ratemon_h& S = I.rm[s];
+      const b200_group_h& G = I.g[M->ratemon[s].group];
+      b200_ratemon_d& RD = D.rm[s];
+      RD.group = M->ratemon[s].group; RD.lo = S.lo; RD.hi = S.hi;
+      RD.tile_lo = (int)(std::lower_bound(G.tile_start.begin(), G.tile_start.end(), S.lo) - G.tile_start.begin());
+      RD.tile_hi = (int)(std::lower_bound(G.tile_start.begin(), G.tile_start.end(), S.hi) - G.tile_start.begin());
+    }
+    for (int s = 0; s < M->n_statemon; ++s) {
+      b200_statemon_h& S = I.stm[s];
+      b200_statemon_d& SD = D.stm[s];
+      SD.group = M->statemon[s].group;
+      SD.n_rec = S.n_rec;
+      SD.n_vars = S.n_vars;
+      if ((r = b200_alloc(n, S.d_idx, (size_t)std::max(S.n_rec, 1) * 4, false))) return r;
+      if (S.n_rec)
+        B200_CU(n, cudaMemcpyAsync(S.d_idx.p, S.idx.data(), (size_t)S.n_rec * 4, cudaMemcpyHostToDevice, n->stream));
+      if (!S.n.p && (r = b200_alloc(n, S.n, 16))) return r;
+      SD.idx = (const int32_t*)S.d_idx.p;
+      for (int v = 0; v < S.n_vars; ++v) {
+        SD.var_id[v] = S.vars[v];
+        SD.var_dbl[v] = M->groups[SD.group].var_kind[S.vars[v]] == B200_F64;
+      }
+      SD.n = (int64_t*)S.n.p;
+    }
+  }
+  n->max_tiles1 = 2;
+  n->max_w = 1;
+  for (int k = 0; k < n->n_inst; ++k) {
+    for (int g = 0; g < M->n_groups; ++g)
+      n->max_tiles1 = std::max(n->max_tiles1, (int)n->inst[k].g[g].tile_start.size());
+    for (int p = 0; p < M->n_pathways; ++p)
+      n->max_w = std::max(n->max_w, n->inst[k].p[p].dmax - n->inst[k].p[p].dmin + 1);
+  }
+  int max_per_sm = M->max_active_ctas(n->threads, n->max_tiles1, n->max_w);
+  int dev = 0, n_sm = 0;
+  B200_CU(n, cudaGetDevice(&dev));
+  B200_CU(n, cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+  const int resident = std::max(1, max_per_sm) * n_sm;
+  if (n->queue_mode) {
+    n->grid = std::min(n->n_inst, resident);
+  } else {
+    n->grid = cta;
+    if (cta > resident)
+      return b200_fail(n, B200_ERR_ARG,
+                       "%d CTAs requested but only %d can be resident (%d/SM); use queue mode or fewer CTAs",
+                       cta, resident, max_per_sm);
+  }
+  if ((r = b200_alloc(n, n->d_cta_map, std::max<size_t>(cta_map.size(), 1) * sizeof(int2), false))) return r;
+  if (!cta_map.empty())
+    B200_CU(n, cudaMemcpyAsync(n->d_cta_map.p, cta_map.data(), cta_map.size() * sizeof(int2), cudaMemcpyHostToDevice, n->stream));
+  if ((r = b200_alloc(n, n->d_work, 16))) return r;
+  if ((r = b200_alloc(n, n->d_insts, sizeof(b200_inst_d) * n->n_inst, false))) return r;
+  B200_CU(n, cudaStreamSynchronize(n->stream));
+  if (n->graph_exec) {
+    cudaGraphExecDestroy(n->graph_exec);
+    n->graph_exec = nullptr;
+    n->graph_steps = -1;
+  }
+  n->prepared = true;
+  return 0;
+}
+
+// Grow a spike monitor so that at least `need` more spikes fit.
+static int b200_grow_spkmon(b200_net* n, b200_spkmon_h& S, int64_t used, int64_t need) {
+  int64_t cap = S.cap;
+  while (cap - used < need) cap *= 2;
+  if (cap == S.cap) return 0;
+  b200_dbuf ni, nt;
+  int r;
+  if ((r = b200_alloc(n, ni, (size_t)cap * 4, false))) return r;
+  if ((r = b200_alloc(n, nt, (size_t)cap * 4, false))) return r;
+  if (used) {
+    B200_CU(n, cudaMemcpyAsync(ni.p, S.i.p, (size_t)used * 4, cudaMemcpyDeviceToDevice, n->stream));
+    B200_CU(n, cudaMemcpyAsync(nt.p, S.ts.p, (size_t)used * 4, cudaMemcpyDeviceToDevice, n->stream));
+  }
+  B200_CU(n, cudaStreamSynchronize(n->stream));
+  b200_free(n, S.i);
+  b200_free(n, S.ts);
+  S.i = ni;
+  S.ts = nt;
+  S.cap = cap;
+  return 0;
+}
+
+extern "C" {
+
+// Runs every instance for n_steps time steps from its current step.  Replaces
+// Network::run (brian2/devices/cpp_standalone/templates/network.cpp:38-122):
+// the per-step schedule runs on the device inside the persistent kernel, the
+// host only relaunches when a spike monitor needs more room.
+int b200_run(b200_net* n, int64_t n_steps) {
+  if (!n) return B200_ERR_ARG;
+  if (n_steps < 0) return b200_fail(n, B200_ERR_ARG, "negative step count");
+  int r;
+  if (!n->prepared && (r = b200_prepare(n))) return r;
+  const b200_model_info* M = n->M;
+  // rate / state monitors get room for the whole run up front
+  for (int k = 0; k < n->n_inst; ++k) {
+    b200_inst_h& I = n->inst[k];
+    for (int s = 0; s < M->n_ratemon; ++s) {
+      b200_ratemon_h& S = I.rm[s];
+      const int64_t need = I.ts + n_steps - S.step0;
+      if (S.cap < need) {
+        b200_dbuf nb;
+        const int64_t cap = std::max<int64_t>(need, 2 * S.cap);
+        if ((r = b200_alloc(n, nb, (size_t)cap * 4))) return r;
+        if (S.cap) B200_CU(n, cudaMemcpyAsync(nb.p, S.cnt.p, (size_t)S.cap * 4, cudaMemcpyDeviceToDevice, n->stream));
+        B200_CU(n, cudaStreamSynchronize(n->stream));
+        b200_free(n, S.cnt);
+        S.cnt = nb;
+        S.cap = cap;
+      }
+      n->h_insts[k].rm[s].step0 = S.step0;
+      n->h_insts[k].rm[s].cap = S.cap;
+      n->h_insts[k].rm[s].cnt = (int32_t*)S.cnt.p;
+    }
+    for (int s = 0; s < M->n_statemon; ++s) {
+      b200_statemon_h& S = I.stm[s];
+      const int64_t need = I.ts + n_steps - S.step0;
+      const size_t row = (size_t)std::max(S.n_rec * S.n_vars, 1) * 8;
+      if (S.cap < need) {
+        b200_dbuf nb;
+        const int64_t cap = std::max<int64_t>(need, 2 * S.cap);
+        if ((r = b200_alloc(n, nb, (size_t)cap * row))) return r;
+        if (S.cap) B200_CU(n, cudaMemcpyAsync(nb.p, S.data.p, (size_t)S.cap * row, cudaMemcpyDeviceToDevice, n->stream));
+        B200_CU(n, cudaStreamSynchronize(n->stream));
+        b200_free(n, S.data);
+        S.data = nb;
+        S.cap = cap;
+      }
+      n->h_insts[k].stm[s].step0 = S.step0;
+      n->h_insts[k].stm[s].cap = S.cap;
+      n->h_insts[k].stm[s].data = (double*)S.data.p;
+    }
+  }
+  std::vector<int64_t> target(n->n_inst);
+  for (int k = 0; k < n->n_inst; ++k) target[k] = n->inst[k].ts + n_steps;
+  cudaEvent_t e0, e1;
+  B200_CU(n, cudaEventCreate(&e0));
+  B200_CU(n, cudaEventCreate(&e1));
+  B200_CU(n, cudaEventRecord(e0, n->stream));
+  const int coop = (!n->queue_mode) ? 1 : 0;
+  for (int guard = 0; guard < 1 << 20; ++guard) {
+    bool any = false;
+    for (int k = 0; k < n->n_inst; ++k) {
+      b200_inst_h& I = n->inst[k];
+      b200_inst_d& D = n->h_insts[k];
+      D.ts = I.ts;
+      D.ts_end = target[k];
+      if (I.ts < target[k]) any = true;
+      for (int s = 0; s < M->n_spkmon; ++s) {
+        b200_spkmon_h& S = I.sm[s];
+        int64_t used = 0;
+        B200_CU(n, cudaMemcpy(&used, S.n.p, 8, cudaMemcpyDeviceToHost));
+        // room for at least 64 steps of all neurons spiking
+        const int64_t need = std::min<int64_t>(target[k] - I.ts, 64) * (int64_t)(S.hi - S.lo);
+        if ((r = b200_grow_spkmon(n, S, used, need))) return r;
+        D.sm[s].cap = S.cap;
+        D.sm[s].i = (int32_t*)S.i.p;
+        D.sm[s].ts = (int32_t*)S.ts.p;
+      }
+    }
+    if (!any) break;
+    B200_CU(n, cudaMemcpyAsync(n->d_insts.p, n->h_insts.data(), sizeof(b200_inst_d) * n->n_inst,
+                               cudaMemcpyHostToDevice, n->stream));
+    B200_CU(n, cudaMemsetAsync(n->d_work.p, 0, 16, n->stream));
+    const int64_t steps = n->chunk_steps;
+    cudaError_t le = M->launch((b200_inst_d*)n->d_insts.p, (const int2*)n->d_cta_map.p, n->n_inst,
+                               n->queue_mode, (int*)n->d_work.p, steps, n->limit_ns, n->grid,
+                               n->threads, coop, n->max_tiles1, n->max_w, n->stream);
+    if (le != cudaSuccess) return b200_fail(n, B200_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(le));
+    ++n->launches;
+    B200_CU(n, cudaStreamSynchronize(n->stream));
+    for (int k = 0; k < n->n_inst; ++k) {
+      b200_inst_h& I = n->inst[k];
+      int32_t st = 0;
+      int64_t done = 0;
+      B200_CU(n, cudaMemcpy(&st, I.status.p, 4, cudaMemcpyDeviceToHost));
+      B200_CU(n, cudaMemcpy(&done, I.ts_done.p, 8, cudaMemcpyDeviceToHost));
+      if (st != 0) {
+        cudaMemset(I.status.p, 0, 4);
+        return b200_fail(n, st == B200_ERR_BARRIER_TIMEOUT ? B200_ERR_BARRIER_TIMEOUT : B200_ERR_INDEX,
+                         "instance %d: device status %d at step %lld (%s)", k, st, (long long)done,
+                         st == B200_ERR_BARRIER_TIMEOUT ? "instance barrier timed out" : "index out of range");
+      }
+      if (done < I.ts || done > target[k])
+        return b200_fail(n, B200_ERR_CUDA, "instance %d: bad progress %lld", k, (long long)done);
+      I.ts = done;
+    }
+  }
+  B200_CU(n, cudaEventRecord(e1, n->stream));
+  B200_CU(n, cudaEventSynchronize(e1));
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  n->last_run_ms = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return 0;
+}
+
+int b200_get_step(b200_net* n, int32_t inst, int64_t* ts) {
+  if (!n || inst < 0 || inst >= n->n_inst || !ts) return B200_ERR_ARG;
+  *ts = n->inst[inst].ts;
+  return 0;
+}
+
+int b200_set_step(b200_net* n, int32_t inst, int64_t ts) {
+  if (!n || inst < 0 || inst >= n->n_inst || ts < 0) return B200_ERR_ARG;
+  n->inst[inst].ts = ts;
+  return 0;
+}
+
+int b200_last_run_ms(b200_net* n, double* ms) {
+  if (!n || !ms) return B200_ERR_ARG;
+  *ms = n->last_run_ms;
+  return 0;
+}
+
+int b200_spikemon_size(b200_net* n, int32_t inst, int32_t mon, int64_t* count) {
+  if (!n || inst < 0 || inst >= n->n_inst || mon < 0 || mon >= n->M->n_spkmon || !count) return B200_ERR_ARG;
+  b200_spkmon_h& S = n->inst[inst].sm[mon];
+  *count = 0;
+  if (!S.n.p) return 0;
+  B200_CU(n, cudaMemcpy(count, S.n.p, 8, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+// i, ts: [count] (count from b200_spikemon_size); per_neuron: [hi-lo] or NULL
+int b200_spikemon_get(b200_net* n, int32_t inst, int32_t mon, int32_t* i, int32_t* ts,
+                      int32_t* per_neuron, int64_t count) {
+  int64_t have = 0;
+  int r = b200_spikemon_size(n, inst, mon, &have);
+  if (r) return r;
+  if (count != have) return b200_fail(n, B200_ERR_ARG, "spike monitor size mismatch");
+  b200_spkmon_h& S = n->inst[inst].sm[mon];
+  if (count) {
+    if (i) B200_CU(n, cudaMemcpy(i, S.i.p, (size_t)count * 4, cudaMemcpyDeviceToHost));
+    if (ts) B200_CU(n, cudaMemcpy(ts, S.ts.p, (size_t)count * 4, cudaMemcpyDeviceToHost));
+  }
+  if (per_neuron && S.count.p && S.hi > S.lo)
+    B200_CU(n, cudaMemcpy(per_neuron, S.count.p, (size_t)(S.hi - S.lo) * 4, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int b200_ratemon_size(b200_net* n, int32_t inst, int32_t mon, int64_t* steps) {
+  if (!n || inst < 0 || inst >= n->n_inst || mon < 0 || mon >= n->M->n_ratemon || !steps) return B200_ERR_ARG;
+  *steps = n->inst[inst].ts - n->inst[inst].rm[mon].step0;
+  return 0;
+}
+
+// counts: [steps] spikes per step (rate = count/dt/N is formed by the caller,
+// as in brian2/devices/cpp_standalone/templates/ratemonitor.cpp:33)
+int b200_ratemon_get(b200_net* n, int32_t inst, int32_t mon, int32_t* counts, int64_t steps) {
+  int64_t have = 0;
+  int r = b200_ratemon_size(n, inst, mon, &have);
+  if (r) return r;
+  if (steps != have) return b200_fail(n, B200_ERR_ARG, "rate monitor size mismatch");
+  if (steps) B200_CU(n, cudaMemcpy(counts, n->inst[inst].rm[mon].cnt.p, (size_t)steps * 4, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int b200_statemon_size(b200_net* n, int32_t inst, int32_t mon, int64_t* steps) {
+  if (!n || inst < 0 || inst >= n->n_inst || mon < 0 || mon >= n->M->n_statemon || !steps) return B200_ERR_ARG;
+  b200_statemon_h& S = n->inst[inst].stm[mon];
+  *steps = 0;
+  if (S.n.p) B200_CU(n, cudaMemcpy(steps, S.n.p, 8, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+// data: [steps][n_vars][n_rec] as double
+int b200_statemon_get(b200_net* n, int32_t inst, int32_t mon, double* data, int64_t steps) {
+  int64_t have = 0;
+  int r = b200_statemon_size(n, inst, mon, &have);
+  if (r) return r;
+  if (steps != have) return b200_fail(n, B200_ERR_ARG, "state monitor size mismatch");
+  b200_statemon_h& S = n->inst[inst].stm[mon];
+  if (steps) B200_CU(n, cudaMemcpy(data, S.data.p, (size_t)steps * S.n_rec * S.n_vars * 8, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+// Clears spike/rate/state monitors of one instance (new recording window).
+int b200_reset_monitors(b200_net* n, int32_t inst) {
+  if (!n || inst < 0 || inst >= n->n_inst) return B200_ERR_ARG;
+  b200_inst_h& I = n->inst[inst];
+  for (auto& S : I.sm) {
+    if (S.n.p) B200_CU(n, cudaMemset(S.n.p, 0, 8));
+    if (S.count.p) B200_CU(n, cudaMemset(S.count.p, 0, S.count.bytes));
+  }
+  for (auto& S : I.rm) S.step0 = I.ts;
+  for (auto& S : I.stm) {
+    S.step0 = I.ts;
+    if (S.n.p) B200_CU(n, cudaMemset(S.n.p, 0, 8));
+  }
+  return 0;
+}
+
+int b200_model_name(char* buf, int64_t len) {
+  if (!buf || len <= 0) return B200_ERR_ARG;
+  snprintf(buf, (size_t)len, "%s", B200_MODEL.name);
+  return 0;
+}
+
+int b200_device_bytes(b200_net* n, int64_t* bytes) {
+  if (!n || !bytes) return B200_ERR_ARG;
+  *bytes = (int64_t)n->device_bytes;
+  return 0;
+}
+
+int b200_launch_count(b200_net* n, int64_t* count) {
+  if (!n || !count) return B200_ERR_ARG;
+  *count = n->launches;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,298 @@
+"""ctypes host for the b200 C ABI (include/b200.h).
+
+:class:`Model` is a compiled network spec (one shared library); :class:`Network`
+is a handle on the device: ``n_inst`` independent instances of the model (one
+network, or a batched parameter sweep), their state, synapses and monitors.
+Every call maps to one ``extern "C"`` entry point; a non-zero status raises
+:class:`B200Error` with the library's message, the way Brian's standalone
+device raises ``RuntimeError`` for a failed run
+(``brian2/devices/cpp_standalone/device.py:1316-1324``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import numpy as np
+
+from . import native
+from .codegen import KIND_NP, spec_tables
+
+_i32p = C.POINTER(C.c_int32)
+_i64p = C.POINTER(C.c_int64)
+_f64p = C.POINTER(C.c_double)
+
+STATUS = {1: "CUDA error", 2: "invalid argument", 3: "capacity", 4: "device wait timed out", 5: "index out of range"}
+
+
+class B200Error(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"b200 status {status} ({STATUS.get(status, '?')}): {message}")
+        self.status = status
+
+
+def _ptr(a, t=C.c_void_p):
+    return a.ctypes.data_as(t)
+
+
+def _declare(lib):
+    h = C.c_void_p
+    sig = {
+        "b200_create": [C.POINTER(h), C.c_int32, _i32p, C.c_double],
+        "b200_destroy": [h],
+        "b200_last_error": [h, C.c_char_p, C.c_int64],
+        "b200_configure": [h, C.c_int32, _i32p, C.c_int32, C.c_int64, C.c_int32],
+        "b200_set_consts": [h, C.c_int32, _f64p, C.c_int32],
+        "b200_upload": [h, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64],
+        "b200_download": [h, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64],
+        "b200_set_synapses": [h, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                              _i32p, _i32p, _i32p, C.c_int32, C.c_int64],
+        "b200_set_synapses_csr": [h, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                  C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64],
+        "b200_synapse_var_ptr": [h, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)],
+        "b200_set_monitor_range": [h, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32],
+        "b200_set_statemon": [h, C.c_int32, C.c_int32, _i32p, C.c_int32, _i32p, C.c_int32],
+        "b200_run": [h, C.c_int64],
+        "b200_get_step": [h, C.c_int32, _i64p],
+        "b200_set_step": [h, C.c_int32, C.c_int64],
+        "b200_last_run_ms": [h, _f64p],
+        "b200_spikemon_size": [h, C.c_int32, C.c_int32, _i64p],
+        "b200_spikemon_get": [h, C.c_int32, C.c_int32, _i32p, _i32p, _i32p, C.c_int64],
+        "b200_ratemon_size": [h, C.c_int32, C.c_int32, _i64p],
+        "b200_ratemon_get": [h, C.c_int32, C.c_int32, _i32p, C.c_int64],
+        "b200_statemon_size": [h, C.c_int32, C.c_int32, _i64p],
+        "b200_statemon_get": [h, C.c_int32, C.c_int32, _f64p, C.c_int64],
+        "b200_reset_monitors": [h, C.c_int32],
+        "b200_model_name": [C.c_char_p, C.c_int64],
+        "b200_device_bytes": [h, _i64p],
+        "b200_launch_count": [h, _i64p],
+    }
+    for name, args in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    return lib
+
+
+class Model:
+    """A network spec compiled to its model library."""
+
+    _cache: dict[str, "Model"] = {}
+
+    def __init__(self, spec: dict):
+        self.spec = spec
+        self.tables = spec_tables(spec)
+        self.path = native.build_model(spec)
+        self.lib = _declare(native.load(self.path))
+        self.group_index = {g["name"]: k for k, g in enumerate(spec["groups"])}
+        self.pathway_index = {p["name"]: k for k, p in enumerate(spec.get("pathways", []))}
+        self.spkmon_index = {m["name"]: k for k, m in enumerate(spec.get("spike_monitors", []))}
+        self.ratemon_index = {m["name"]: k for k, m in enumerate(spec.get("rate_monitors", []))}
+        self.statemon_index = {m["name"]: k for k, m in enumerate(spec.get("state_monitors", []))}
+
+    @classmethod
+    def get(cls, spec: dict) -> "Model":
+        key = native.model_library_path(spec)
+        m = cls._cache.get(key)
+        if m is None:
+            m = cls._cache[key] = Model(spec)
+        return m
+
+
+class Network:
+    """Device handle: `n_inst` instances of one model."""
+
+    def __init__(self, model: Model, sizes, dt: float):
+        self.model = model
+        self.lib = model.lib
+        sizes = np.ascontiguousarray(np.asarray(sizes, dtype=np.int32).reshape(-1, len(model.spec["groups"])))
+        self.n_inst = sizes.shape[0]
+        self.sizes = sizes
+        self.dt = float(dt)
+        self._h = C.c_void_p()
+        self._check(self.lib.b200_create(C.byref(self._h), self.n_inst, _ptr(sizes, _i32p), self.dt))
+        self.n_syn = {}
+
+    # -- plumbing -----------------------------------------------------------
+    def _check(self, status):
+        if status != 0:
+            buf = C.create_string_buffer(1024)
+            if self._h:
+                self.lib.b200_last_error(self._h, buf, 1024)
+            raise B200Error(status, buf.value.decode(errors="replace"))
+
+    def close(self):
+        if self._h:
+            self.lib.b200_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _g(self, group):
+        return group if isinstance(group, int) else self.model.group_index[group]
+
+    def _p(self, pw):
+        return pw if isinstance(pw, int) else self.model.pathway_index[pw]
+
+    # -- configuration --------------------------------------------------------
+    def configure(self, threads=256, ctas_per_inst=1, queue_mode=False, chunk_steps=0, use_graph=False):
+        c = np.ascontiguousarray(np.broadcast_to(np.asarray(ctas_per_inst, dtype=np.int32), (self.n_inst,)))
+        self._check(self.lib.b200_configure(self._h, int(threads), _ptr(c, _i32p), int(bool(queue_mode)),
+                                            int(chunk_steps), int(bool(use_graph))))
+
+    def set_consts(self, inst, values: dict):
+        names = self.model.tables["consts"]
+        cur = {c["name"]: c["value"] for c in self.model.spec.get("consts", [])}
+        cur.update(getattr(self, "_consts", {}).get(inst, {}))
+        cur.update(values)
+        self.__dict__.setdefault("_consts", {})[inst] = cur
+        arr = np.array([float(cur[n]) for n in names], dtype=np.float64)
+        self._check(self.lib.b200_set_consts(self._h, int(inst), _ptr(arr, _f64p), len(names)))
+
+    # -- state ----------------------------------------------------------------
+    def _var(self, group, var):
+        g = self._g(group)
+        v = var if isinstance(var, int) else self.model.tables["groups"][g].index(var)
+        return g, v, np.dtype(KIND_NP[self.model.tables["group_kinds"][g][v]])
+
+    def upload(self, inst, group, var, values):
+        g, v, dt = self._var(group, var)
+        a = np.ascontiguousarray(values, dtype=dt)
+        self._check(self.lib.b200_upload(self._h, int(inst), 0, g, v, _ptr(a), a.size))
+
+    def download(self, inst, group, var):
+        g, v, dt = self._var(group, var)
+        a = np.empty(int(self.sizes[inst, g]), dtype=dt)
+        self._check(self.lib.b200_download(self._h, int(inst), 0, g, v, _ptr(a), a.size))
+        return a
+
+    def set_synapses(self, inst, pathway, pre, post, delay_steps=None, scalar_delay=0,
+                     src_range=None, tgt_range=None):
+        p = self._p(pathway)
+        info = self.model.spec["pathways"][p]
+        Ns, Nt = int(self.sizes[inst, info["src"]]), int(self.sizes[inst, info["tgt"]])
+        s0, s1 = src_range if src_range is not None else (0, Ns)
+        t0, t1 = tgt_range if tgt_range is not None else (0, Nt)
+        pre = np.ascontiguousarray(pre, dtype=np.int32)
+        post = np.ascontiguousarray(post, dtype=np.int32)
+        dptr = None
+        if delay_steps is not None:
+            d = np.ascontiguousarray(delay_steps, dtype=np.int32)
+            dptr = _ptr(d, _i32p)
+        self._check(self.lib.b200_set_synapses(self._h, int(inst), p, s0, s1, t0, t1, _ptr(pre, _i32p),
+                                               _ptr(post, _i32p), dptr, int(scalar_delay), pre.size))
+        self.n_syn[(inst, p)] = pre.size
+
+    def set_synapses_csr(self, inst, pathway, src_range, tgt_range, dmin, dmax, segptr_dev, post_dev,
+                         pre_dev, n_syn):
+        p = self._p(pathway)
+        self._check(self.lib.b200_set_synapses_csr(self._h, int(inst), p, int(src_range[0]), int(src_range[1]),
+                                                   int(tgt_range[0]), int(tgt_range[1]), int(dmin), int(dmax),
+                                                   C.c_void_p(segptr_dev), C.c_void_p(post_dev),
+                                                   C.c_void_p(pre_dev), int(n_syn)))
+        self.n_syn[(inst, p)] = int(n_syn)
+
+    def synapse_var_ptr(self, inst, pathway, var):
+        p = self._p(pathway)
+        v = var if isinstance(var, int) else self.model.tables["pathways"][p].index(var)
+        out = C.c_void_p()
+        self._check(self.lib.b200_synapse_var_ptr(self._h, int(inst), p, v, C.byref(out)))
+        return out.value
+
+    def _svar(self, pathway, var):
+        p = self._p(pathway)
+        v = var if isinstance(var, int) else self.model.tables["pathways"][p].index(var)
+        return p, v, np.dtype(KIND_NP[self.model.tables["pathway_kinds"][p][v]])
+
+    def upload_synapse_var(self, inst, pathway, var, values):
+        p, v, dt = self._svar(pathway, var)
+        a = np.ascontiguousarray(values, dtype=dt)
+        self._check(self.lib.b200_upload(self._h, int(inst), 1, p, v, _ptr(a), a.size))
+
+    def download_synapse_var(self, inst, pathway, var):
+        p, v, dt = self._svar(pathway, var)
+        a = np.empty(self.n_syn[(inst, p)], dtype=dt)
+        self._check(self.lib.b200_download(self._h, int(inst), 1, p, v, _ptr(a), a.size))
+        return a
+
+    # -- monitors -------------------------------------------------------------
+    def set_spikemon_range(self, inst, mon, lo, hi):
+        m = mon if isinstance(mon, int) else self.model.spkmon_index[mon]
+        self._check(self.lib.b200_set_monitor_range(self._h, int(inst), 0, m, int(lo), int(hi)))
+
+    def set_ratemon_range(self, inst, mon, lo, hi):
+        m = mon if isinstance(mon, int) else self.model.ratemon_index[mon]
+        self._check(self.lib.b200_set_monitor_range(self._h, int(inst), 1, m, int(lo), int(hi)))
+
+    def set_statemon(self, inst, mon, indices, variables):
+        m = mon if isinstance(mon, int) else self.model.statemon_index[mon]
+        g = self.model.spec["state_monitors"][m]["group"]
+        idx = np.ascontiguousarray(indices, dtype=np.int32)
+        vs = np.ascontiguousarray([v if isinstance(v, int) else self.model.tables["groups"][g].index(v)
+                                   for v in variables], dtype=np.int32)
+        self._check(self.lib.b200_set_statemon(self._h, int(inst), m, _ptr(idx, _i32p), idx.size,
+                                               _ptr(vs, _i32p), vs.size))
+        self.__dict__.setdefault("_statemon_shape", {})[(inst, m)] = (vs.size, idx.size)
+
+    def spikes(self, inst=0, mon=0):
+        """(i, timestep, per-neuron count) recorded by a spike monitor."""
+        m = mon if isinstance(mon, int) else self.model.spkmon_index[mon]
+        n = C.c_int64()
+        self._check(self.lib.b200_spikemon_size(self._h, int(inst), m, C.byref(n)))
+        i = np.empty(n.value, np.int32)
+        ts = np.empty(n.value, np.int32)
+        g = self.model.spec["spike_monitors"][m]["group"]
+        cnt = np.empty(int(self.sizes[inst, g]), np.int32)
+        self._check(self.lib.b200_spikemon_get(self._h, int(inst), m, _ptr(i, _i32p), _ptr(ts, _i32p),
+                                               _ptr(cnt, _i32p), n.value))
+        return i, ts, cnt
+
+    def rate_counts(self, inst=0, mon=0):
+        m = mon if isinstance(mon, int) else self.model.ratemon_index[mon]
+        n = C.c_int64()
+        self._check(self.lib.b200_ratemon_size(self._h, int(inst), m, C.byref(n)))
+        a = np.empty(n.value, np.int32)
+        self._check(self.lib.b200_ratemon_get(self._h, int(inst), m, _ptr(a, _i32p), n.value))
+        return a
+
+    def state_trace(self, inst=0, mon=0):
+        """[steps, n_vars, n_rec] float64 values recorded at the start of each step."""
+        m = mon if isinstance(mon, int) else self.model.statemon_index[mon]
+        n_vars, n_rec = self._statemon_shape[(inst, m)]
+        n = C.c_int64()
+        self._check(self.lib.b200_statemon_size(self._h, int(inst), m, C.byref(n)))
+        a = np.empty((n.value, n_vars, n_rec), np.float64)
+        self._check(self.lib.b200_statemon_get(self._h, int(inst), m, _ptr(a, _f64p), n.value))
+        return a
+
+    def reset_monitors(self, inst=0):
+        self._check(self.lib.b200_reset_monitors(self._h, int(inst)))
+
+    # -- running --------------------------------------------------------------
+    def run(self, n_steps: int):
+        self._check(self.lib.b200_run(self._h, int(n_steps)))
+
+    def step(self, inst=0):
+        t = C.c_int64()
+        self._check(self.lib.b200_get_step(self._h, int(inst), C.byref(t)))
+        return t.value
+
+    def set_step(self, inst, ts):
+        self._check(self.lib.b200_set_step(self._h, int(inst), int(ts)))
+
+    def last_run_ms(self):
+        v = C.c_double()
+        self._check(self.lib.b200_last_run_ms(self._h, C.byref(v)))
+        return v.value
+
+    def launches(self):
+        v = C.c_int64()
+        self._check(self.lib.b200_launch_count(self._h, C.byref(v)))
+        return v.value
+
+    def device_bytes(self):
+        v = C.c_int64()
+        self._check(self.lib.b200_device_bytes(self._h, C.byref(v)))
+        return v.value

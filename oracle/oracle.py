@@ -1,0 +1,493 @@
+"""THE ORACLE -- test infrastructure only (tests/, smoke(), bench.py cpu_baseline).
+
+A CPU restatement of the reference's clock-driven step loop, used to check the
+CUDA path.  It is generated per network spec, like Brian2's ``cpp_standalone``
+code objects, and executes the spec's *plain* C++ snippets (Brian's own
+``CPPCodeGenerator`` output) inside loops that restate the reference templates:
+
+* ``Network::run``: per step, every code object in schedule order, then the
+  clock tick ``t = timestep*dt``
+  (brian2/devices/cpp_standalone/templates/network.cpp:67-104,
+  brianlib/clocks.h:34-38; schedule brian2/core/network.py:42-50);
+* state update over all neurons (templates/stateupdate.cpp:5-21);
+* threshold with sequential ascending compaction into the spike space and the
+  refractory bookkeeping (templates/threshold.cpp:18-31);
+* spike monitor append of (i, t) and per-neuron counts
+  (templates/spikemonitor.cpp:13-48);
+* per pathway ``advance()`` then ``push()`` into a ring of synapse-index
+  vectors, ``peek()`` and ``on_pre`` for each queued synapse in queue order
+  (templates/synapses_push_spikes.cpp:24-28, synapses/spikequeue.h:146-205,
+  templates/synapses.cpp:20-49);
+* reset for each spike (templates/reset.cpp:16-22);
+* rate monitor count per step (templates/ratemonitor.cpp:7-35);
+* state monitor record at the start of the step (templates/statemonitor.cpp).
+
+Scalar blocks are evaluated every step, as the reference does.  The library is
+built with ``g++ -O2 -ffp-contract=off -fno-fast-math`` (the reference's strict
+build).  It is pinned against fixtures produced by running Brian2 itself
+(tests/golden/make_golden.py) and must never be used by the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import hashlib
+import json
+import os
+import shutil
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+
+_i32p = C.POINTER(C.c_int32)
+_i64p = C.POINTER(C.c_int64)
+_f64p = C.POINTER(C.c_double)
+
+_CT_NP = {"double": np.float64, "float": np.float32, "int32_t": np.int32, "char": np.int8,
+          "int8_t": np.int8, "int64_t": np.int64}
+
+
+def _ind(code, n):
+    return "\n".join(" " * n + ln if ln.strip() else "" for ln in code.splitlines())
+
+
+def render_oracle(spec: dict) -> str:
+    groups = spec["groups"]
+    paths = spec.get("pathways", [])
+    spkmons = spec.get("spike_monitors", [])
+    ratemons = spec.get("rate_monitors", [])
+    statemons = spec.get("state_monitors", [])
+    consts = spec.get("consts", [])
+    clock = spec.get("clock_ptrs", {"dt": "_ptr_array_defaultclock_dt", "t": "_ptr_array_defaultclock_t",
+                                     "timestep": "_ptr_array_defaultclock_timestep"})
+    o = []
+    w = o.append
+    w("// oracle for model '%s' (generated; test infrastructure)" % spec["name"])
+    w("#include <cmath>\n#include <cstdint>\n#include <cstring>\n#include <vector>\n#include <algorithm>")
+    w("static inline double _exprel(double x) { if (fabs(x) < 1e-16) return 1.0; if (x > 717) return INFINITY; return expm1(x)/x; }")
+    w("static inline float _exprel(float x) { if (fabsf(x) < 1e-16f) return 1.0f; if (x > 717.0f) return INFINITY; return expm1f(x)/x; }")
+    w("template <typename T> static inline T _clip(const T v, const double a, const double b) { if (v < a) return a; if (v > b) return b; return v; }")
+    w("static inline double _brian_pow(double a, double b) { return pow(a, b); }")
+    w("static inline float _brian_pow(float a, float b) { return powf(a, b); }")
+    w("static inline double _brian_pow(double a, float b) { return pow(a, (double)b); }")
+    w("static inline double _brian_pow(float a, double b) { return pow((double)a, b); }")
+    w("static inline double _brian_pow(double a, int b) { return pow(a, (double)b); }")
+    w("static inline float _brian_pow(float a, int b) { return powf(a, (float)b); }")
+    w("static inline double _brian_mod(double x, double y) { double r = fmod(x, y); if (r != 0 && ((r < 0) != (y < 0))) r += y; return r; }")
+    w("static inline double _brian_floordiv(double x, double y) { return floor(x / y); }")
+    w("template <typename T> static inline int int_(T v) { return (int)v; }")
+    w("static inline int64_t _timestep(double t, double dt) { return (int64_t)((t + 1e-3 * dt) / dt); }")
+    w("#define _brian_abs fabs")
+    w("struct Net {")
+    w("  double dt; int64_t ts = 0;")
+    w("  std::vector<double> c;")
+    for gi, g in enumerate(groups):
+        w(f"  int32_t N{gi} = 0;")
+        for v in g["vars"]:
+            w(f"  std::vector<{v['ctype']}> g{gi}_{v['name']};")
+        w(f"  std::vector<int32_t> spk{gi};")
+    for pi, p in enumerate(paths):
+        w(f"  int32_t p{pi}_src_lo = 0, p{pi}_src_hi = 0; std::vector<int32_t> p{pi}_pre, p{pi}_post, p{pi}_delay;")
+        for v in p.get("vars", []):
+            w(f"  std::vector<{v['ctype']}> p{pi}_{v['name']};")
+        w(f"  std::vector<std::vector<int32_t>> p{pi}_queue = std::vector<std::vector<int32_t>>(1); int p{pi}_offset = 0;")
+        w(f"  std::vector<std::vector<int32_t>> p{pi}_syn;")
+    for mi, m in enumerate(spkmons):
+        w(f"  int32_t sm{mi}_lo = 0, sm{mi}_hi = 0; std::vector<int32_t> sm{mi}_i, sm{mi}_ts, sm{mi}_count;")
+    for mi, m in enumerate(ratemons):
+        w(f"  int32_t rm{mi}_lo = 0, rm{mi}_hi = 0; std::vector<int32_t> rm{mi}_cnt;")
+    for mi, m in enumerate(statemons):
+        w(f"  std::vector<int32_t> st{mi}_idx, st{mi}_vars; std::vector<double> st{mi}_data; int64_t st{mi}_n = 0;")
+    w("};")
+    w('extern "C" {')
+    w("Net* oracle_create(const int32_t* sizes, double dt) {")
+    w("  Net* n = new Net(); n->dt = dt;")
+    w("  n->c = {" + ", ".join(repr(float(c["value"])) for c in consts) + "};")
+    for gi, g in enumerate(groups):
+        w(f"  n->N{gi} = sizes[{gi}];")
+        for v in g["vars"]:
+            w(f"  n->g{gi}_{v['name']}.assign(sizes[{gi}], 0);")
+    for pi, p in enumerate(paths):
+        w(f"  n->p{pi}_src_hi = sizes[{p['src']}];")
+    for mi, m in enumerate(spkmons):
+        w(f"  n->sm{mi}_hi = sizes[{m['group']}]; n->sm{mi}_count.assign(sizes[{m['group']}], 0);")
+    for mi, m in enumerate(ratemons):
+        w(f"  n->rm{mi}_hi = sizes[{m['group']}];")
+    w("  return n;")
+    w("}")
+    w("void oracle_destroy(Net* n) { delete n; }")
+    w("void oracle_set_consts(Net* n, const double* v, int32_t k) { n->c.assign(v, v + k); }")
+    # uploads / downloads through a switch over (group, var)
+    w("void* oracle_var(Net* n, int32_t kind, int32_t obj, int32_t var) {")
+    for gi, g in enumerate(groups):
+        for vi, v in enumerate(g["vars"]):
+            w(f"  if (kind == 0 && obj == {gi} && var == {vi}) return n->g{gi}_{v['name']}.data();")
+    for pi, p in enumerate(paths):
+        for vi, v in enumerate(p.get("vars", [])):
+            w(f"  if (kind == 1 && obj == {pi} && var == {vi}) return n->p{pi}_{v['name']}.data();")
+    w("  return nullptr;")
+    w("}")
+    # synapses: pre/post relative to the source/target range; stored absolute
+    w("int oracle_set_synapses(Net* n, int32_t pw, const int32_t* pre, const int32_t* post, const int32_t* delay,")
+    w("                        int32_t scalar_delay, int64_t n_syn, int32_t src_lo, int32_t src_hi, int32_t tgt_lo) {")
+    for pi, p in enumerate(paths):
+        w(f"  if (pw == {pi}) {{")
+        w(f"    n->p{pi}_src_lo = src_lo; n->p{pi}_src_hi = src_hi;")
+        w(f"    n->p{pi}_pre.resize(n_syn); n->p{pi}_post.resize(n_syn); n->p{pi}_delay.resize(n_syn);")
+        w(f"    for (int64_t k = 0; k < n_syn; ++k) {{ n->p{pi}_pre[k] = pre[k] + src_lo; n->p{pi}_post[k] = post[k] + tgt_lo;")
+        w(f"      n->p{pi}_delay[k] = delay ? delay[k] : scalar_delay; }}")
+        for v in p.get("vars", []):
+            w(f"    n->p{pi}_{v['name']}.assign(n_syn, 0);")
+        # CSpikeQueue::prepare: per-source synapse lists, ring size max_delay+1 (spikequeue.h:45-105)
+        w(f"    n->p{pi}_syn.assign(src_hi - src_lo, std::vector<int32_t>());")
+        w(f"    int32_t md = 0; for (int64_t k = 0; k < n_syn; ++k) {{ n->p{pi}_syn[pre[k]].push_back((int32_t)k); md = std::max(md, n->p{pi}_delay[k]); }}")
+        w(f"    if ((int)n->p{pi}_queue.size() < md + 1) {{")
+        w(f"      std::rotate(n->p{pi}_queue.begin(), n->p{pi}_queue.begin() + n->p{pi}_offset, n->p{pi}_queue.end());")
+        w(f"      n->p{pi}_offset = 0; n->p{pi}_queue.resize(md + 1); }}")
+        w("    return 0;")
+        w("  }")
+    w("  return 1;")
+    w("}")
+    w("void oracle_set_range(Net* n, int32_t kind, int32_t mon, int32_t lo, int32_t hi) {")
+    for mi, m in enumerate(spkmons):
+        w(f"  if (kind == 0 && mon == {mi}) {{ n->sm{mi}_lo = lo; n->sm{mi}_hi = hi; n->sm{mi}_count.assign(hi - lo, 0); }}")
+    for mi, m in enumerate(ratemons):
+        w(f"  if (kind == 1 && mon == {mi}) {{ n->rm{mi}_lo = lo; n->rm{mi}_hi = hi; }}")
+    w("}")
+    w("void oracle_set_statemon(Net* n, int32_t mon, const int32_t* idx, int32_t nr, const int32_t* vars, int32_t nv) {")
+    for mi, m in enumerate(statemons):
+        w(f"  if (mon == {mi}) {{ n->st{mi}_idx.assign(idx, idx + nr); n->st{mi}_vars.assign(vars, vars + nv); }}")
+    w("}")
+
+    # ---- the step loop
+    w("void oracle_run(Net* n, int64_t n_steps) {")
+    for k, cst in enumerate(consts):
+        w(f"  const {cst['ctype']} {cst['name']} = ({cst['ctype']})n->c[{k}]; (void){cst['name']};")
+    w("  const double _dt_v = n->dt;")
+    w(f"  const double* const {clock['dt']} = &_dt_v;")
+    w("  for (int64_t _s = 0; _s < n_steps; ++_s) {")
+    w("    const int64_t _ts_v = n->ts;")
+    w("    const double _t_v = (double)n->ts * n->dt;")
+    w(f"    const double* const {clock['t']} = &_t_v; (void){clock['t']};")
+    w(f"    const int64_t* const {clock['timestep']} = &_ts_v; (void){clock['timestep']};")
+
+    def gptrs(gi, indent):
+        g = groups[gi]
+        return _ind("\n".join(f"{v['ctype']}* const {v['ptr']} = n->g{gi}_{v['name']}.data(); (void){v['ptr']};"
+                              for v in g["vars"]), indent)
+
+    def extra(block, indent):
+        lines = []
+        for ptr, (kind, obj, var) in sorted((block or {}).get("extra_ptrs", {}).items()):
+            v = groups[obj]["vars"][var]
+            lines.append(f"{v['ctype']}* const {ptr} = n->g{obj}_{v['name']}.data(); (void){ptr};")
+        return _ind("\n".join(lines), indent)
+
+    # state monitors record at the start of the step
+    for mi, m in enumerate(statemons):
+        gi = m["group"]
+        w("    {")
+        w(gptrs(gi, 6))
+        w(f"      for (size_t v = 0; v < n->st{mi}_vars.size(); ++v) for (size_t r = 0; r < n->st{mi}_idx.size(); ++r) {{")
+        w("        double val = 0;")
+        for vi, v in enumerate(groups[gi]["vars"]):
+            w(f"        if (n->st{mi}_vars[v] == {vi}) val = (double)n->g{gi}_{v['name']}[n->st{mi}_idx[r]];")
+        w(f"        n->st{mi}_data.push_back(val);")
+        w("      }")
+        w(f"      n->st{mi}_n++;")
+        w("    }")
+    # state updaters of all groups
+    for gi, g in enumerate(groups):
+        if not g.get("update"):
+            continue
+        w("    {")
+        w(gptrs(gi, 6))
+        w(f"      const int32_t N = n->N{gi}; (void)N;")
+        w("      {")
+        w(_ind(g["update"]["scalar"], 8))
+        w(extra(g.get("update"), 8))
+        w("        for (int32_t _idx = 0; _idx < N; ++_idx) {")
+        w("          const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+        w(_ind(g["update"]["vector"], 10))
+        w("        }")
+        w("      }")
+        w("    }")
+    # thresholders
+    for gi, g in enumerate(groups):
+        w("    {")
+        w(gptrs(gi, 6))
+        w(f"      const int32_t N = n->N{gi}; (void)N;")
+        w(f"      n->spk{gi}.clear();")
+        if g.get("threshold"):
+            w("      {")
+            w(_ind(g["threshold"]["scalar"], 8))
+            w(extra(g.get("threshold"), 8))
+            w("        for (int32_t _idx = 0; _idx < N; ++_idx) {")
+            w("          const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+            w(_ind(g["threshold"]["vector"], 10))
+            w("          if (_cond) {")
+            w(f"            n->spk{gi}.push_back(_idx);")
+            if g["threshold"].get("refractory"):
+                nr = next(v["ptr"] for v in g["vars"] if v["name"] == "not_refractory")
+                ls = next(v["ptr"] for v in g["vars"] if v["name"] == "lastspike")
+                w(f"            {nr}[_idx] = false; {ls}[_idx] = _t_v;")
+            w("          }")
+            w("        }")
+            w("      }")
+        w("    }")
+    # spike monitors
+    for mi, m in enumerate(spkmons):
+        gi = m["group"]
+        w("    {")
+        w(f"      const std::vector<int32_t>& sp = n->spk{gi};")
+        w(f"      for (int32_t idx : sp) if (idx >= n->sm{mi}_lo && idx < n->sm{mi}_hi) {{")
+        w(f"        n->sm{mi}_i.push_back(idx - n->sm{mi}_lo); n->sm{mi}_ts.push_back((int32_t)n->ts); n->sm{mi}_count[idx - n->sm{mi}_lo]++; }}")
+        w("    }")
+    # pathways: advance, push, peek, on_pre
+    for pi, p in enumerate(paths):
+        sg = p["src"]
+        w("    {")
+        w(f"      std::vector<std::vector<int32_t>>& Q = n->p{pi}_queue; int& off = n->p{pi}_offset;")
+        w("      Q[off].clear(); off = (off + 1) % (int)Q.size();")
+        w(f"      const std::vector<int32_t>& sp = n->spk{sg};")
+        w(f"      const int a = (int)(std::lower_bound(sp.begin(), sp.end(), n->p{pi}_src_lo) - sp.begin());")
+        w(f"      const int b = (int)(std::upper_bound(sp.begin(), sp.end(), n->p{pi}_src_hi - 1) - sp.begin());")
+        w("      for (int s = a; s < b; ++s) {")
+        w(f"        const std::vector<int32_t>& syn = n->p{pi}_syn[sp[s] - n->p{pi}_src_lo];")
+        w(f"        for (int32_t k : syn) Q[(off + n->p{pi}_delay[k]) % Q.size()].push_back(k);")
+        w("      }")
+        w(f"      int32_t* const {p['pre_ptr']} = n->p{pi}_pre.data(); (void){p['pre_ptr']};")
+        w(f"      int32_t* const {p['post_ptr']} = n->p{pi}_post.data(); (void){p['post_ptr']};")
+        for v in p.get("vars", []):
+            w(f"      {v['ctype']}* const {v['ptr']} = n->p{pi}_{v['name']}.data(); (void){v['ptr']};")
+        for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
+            v = groups[gidx]["vars"][vidx]
+            w(f"      {v['ctype']}* const {ptr} = n->g{gidx}_{v['name']}.data(); (void){ptr};")
+        w("      {")
+        w(_ind(p["on_pre"]["scalar"], 8))
+        w("        const std::vector<int32_t>& q = Q[off];")
+        w("        for (size_t _q = 0; _q < q.size(); ++_q) {")
+        w("          const int64_t _idx = q[_q];")
+        w("          const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+        w(_ind(p["on_pre"]["vector"], 10))
+        w("        }")
+        w("      }")
+        w("    }")
+    # resets
+    for gi, g in enumerate(groups):
+        if not g.get("reset"):
+            continue
+        w("    {")
+        w(gptrs(gi, 6))
+        w(f"      const int32_t N = n->N{gi}; (void)N;")
+        w("      {")
+        w(_ind(g["reset"]["scalar"], 8))
+        w(extra(g.get("reset"), 8))
+        w(f"        for (int32_t _idx : n->spk{gi}) {{")
+        w("          const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+        w(_ind(g["reset"]["vector"], 10))
+        w("        }")
+        w("      }")
+        w("    }")
+    for mi, m in enumerate(ratemons):
+        gi = m["group"]
+        w(f"    {{ int c = 0; for (int32_t idx : n->spk{gi}) if (idx >= n->rm{mi}_lo && idx < n->rm{mi}_hi) ++c; n->rm{mi}_cnt.push_back(c); }}")
+    w("    n->ts += 1;")
+    w("  }")
+    w("}")
+    for mi, _ in enumerate(spkmons):
+        w(f"int64_t oracle_spikemon_size_{mi}(Net* n) {{ return (int64_t)n->sm{mi}_i.size(); }}")
+        w(f"void oracle_spikemon_get_{mi}(Net* n, int32_t* i, int32_t* ts, int32_t* cnt) {{")
+        w(f"  std::copy(n->sm{mi}_i.begin(), n->sm{mi}_i.end(), i); std::copy(n->sm{mi}_ts.begin(), n->sm{mi}_ts.end(), ts);")
+        w(f"  std::copy(n->sm{mi}_count.begin(), n->sm{mi}_count.end(), cnt); }}")
+    for mi, _ in enumerate(ratemons):
+        w(f"int64_t oracle_ratemon_size_{mi}(Net* n) {{ return (int64_t)n->rm{mi}_cnt.size(); }}")
+        w(f"void oracle_ratemon_get_{mi}(Net* n, int32_t* c) {{ std::copy(n->rm{mi}_cnt.begin(), n->rm{mi}_cnt.end(), c); }}")
+    for mi, _ in enumerate(statemons):
+        w(f"int64_t oracle_statemon_size_{mi}(Net* n) {{ return n->st{mi}_n; }}")
+        w(f"void oracle_statemon_get_{mi}(Net* n, double* d) {{ std::copy(n->st{mi}_data.begin(), n->st{mi}_data.end(), d); }}")
+    w("}  // extern C")
+    return "\n".join(o) + "\n"
+
+
+def _build(spec):
+    src_text = render_oracle(spec)
+    tag = hashlib.sha256(src_text.encode()).hexdigest()[:16]
+    out = os.path.join(BUILD, f"oracle_{spec['name']}_{tag}.so")
+    if not os.path.exists(out):
+        os.makedirs(BUILD, exist_ok=True)
+        src = out[:-3] + ".cpp"
+        with open(src, "w") as f:
+            f.write(src_text)
+        tmp = out + f".tmp{os.getpid()}"
+        cxx = shutil.which("g++") or "g++"
+        r = subprocess.run([cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+                            "-w", src, "-o", tmp], capture_output=True, text=True)
+        if r.returncode:
+            raise RuntimeError("oracle build failed:\n" + r.stderr[-4000:])
+        os.replace(tmp, out)
+    return out
+
+
+class OracleNet:
+    """Same interface subset as brian2_gb300.runtime.Network, on the CPU."""
+
+    _libs = {}
+
+    def __init__(self, spec, sizes, dt):
+        self.spec = spec
+        path = _build(spec)
+        lib = self._libs.get(path)
+        if lib is None:
+            lib = self._libs[path] = C.CDLL(path)
+            lib.oracle_create.restype = C.c_void_p
+            lib.oracle_create.argtypes = [_i32p, C.c_double]
+            lib.oracle_destroy.argtypes = [C.c_void_p]
+            lib.oracle_var.restype = C.c_void_p
+            lib.oracle_var.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
+            lib.oracle_set_consts.argtypes = [C.c_void_p, _f64p, C.c_int32]
+            lib.oracle_set_synapses.argtypes = [C.c_void_p, C.c_int32, _i32p, _i32p, _i32p, C.c_int32, C.c_int64,
+                                                C.c_int32, C.c_int32, C.c_int32]
+            lib.oracle_set_range.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+            lib.oracle_set_statemon.argtypes = [C.c_void_p, C.c_int32, _i32p, C.c_int32, _i32p, C.c_int32]
+            lib.oracle_run.argtypes = [C.c_void_p, C.c_int64]
+        self.lib = lib
+        self.sizes = np.ascontiguousarray(sizes, dtype=np.int32).reshape(-1)
+        self.h = lib.oracle_create(self.sizes.ctypes.data_as(_i32p), float(dt))
+        self.n_syn = {}
+        self._stm = {}
+
+    def __del__(self):
+        try:
+            self.lib.oracle_destroy(self.h)
+        except Exception:
+            pass
+
+    def _gv(self, group, var):
+        gs = self.spec["groups"]
+        g = group if isinstance(group, int) else [x["name"] for x in gs].index(group)
+        names = [v["name"] for v in gs[g]["vars"]]
+        v = var if isinstance(var, int) else names.index(var)
+        return g, v, _CT_NP[gs[g]["vars"][v]["ctype"]]
+
+    def set_consts(self, values: dict):
+        cur = {c["name"]: c["value"] for c in self.spec.get("consts", [])}
+        cur.update(values)
+        a = np.array([float(cur[c["name"]]) for c in self.spec.get("consts", [])], np.float64)
+        self.lib.oracle_set_consts(self.h, a.ctypes.data_as(_f64p), a.size)
+
+    def upload(self, group, var, values):
+        g, v, dt = self._gv(group, var)
+        a = np.ascontiguousarray(values, dtype=dt)
+        assert a.size == self.sizes[g]
+        C.memmove(self.lib.oracle_var(self.h, 0, g, v), a.ctypes.data, a.nbytes)
+
+    def download(self, group, var):
+        g, v, dt = self._gv(group, var)
+        a = np.empty(int(self.sizes[g]), dt)
+        C.memmove(a.ctypes.data, self.lib.oracle_var(self.h, 0, g, v), a.nbytes)
+        return a
+
+    def _pv(self, pathway, var):
+        ps = self.spec["pathways"]
+        p = pathway if isinstance(pathway, int) else [x["name"] for x in ps].index(pathway)
+        names = [v["name"] for v in ps[p].get("vars", [])]
+        v = var if isinstance(var, int) else names.index(var)
+        return p, v, _CT_NP[ps[p]["vars"][v]["ctype"]]
+
+    def set_synapses(self, pathway, pre, post, delay_steps=None, scalar_delay=0, src_range=None, tgt_range=None):
+        ps = self.spec["pathways"]
+        p = pathway if isinstance(pathway, int) else [x["name"] for x in ps].index(pathway)
+        s0, s1 = src_range if src_range is not None else (0, int(self.sizes[ps[p]["src"]]))
+        t0 = tgt_range[0] if tgt_range is not None else 0
+        pre = np.ascontiguousarray(pre, np.int32)
+        post = np.ascontiguousarray(post, np.int32)
+        d = None if delay_steps is None else np.ascontiguousarray(delay_steps, np.int32)
+        r = self.lib.oracle_set_synapses(self.h, p, pre.ctypes.data_as(_i32p), post.ctypes.data_as(_i32p),
+                                         None if d is None else d.ctypes.data_as(_i32p), int(scalar_delay),
+                                         pre.size, s0, s1, t0)
+        assert r == 0
+        self.n_syn[p] = pre.size
+
+    def upload_synapse_var(self, pathway, var, values):
+        p, v, dt = self._pv(pathway, var)
+        a = np.ascontiguousarray(values, dtype=dt)
+        assert a.size == self.n_syn[p]
+        C.memmove(self.lib.oracle_var(self.h, 1, p, v), a.ctypes.data, a.nbytes)
+
+    def download_synapse_var(self, pathway, var):
+        p, v, dt = self._pv(pathway, var)
+        a = np.empty(self.n_syn[p], dt)
+        C.memmove(a.ctypes.data, self.lib.oracle_var(self.h, 1, p, v), a.nbytes)
+        return a
+
+    def set_spikemon_range(self, mon, lo, hi):
+        self.lib.oracle_set_range(self.h, 0, int(mon), int(lo), int(hi))
+
+    def set_ratemon_range(self, mon, lo, hi):
+        self.lib.oracle_set_range(self.h, 1, int(mon), int(lo), int(hi))
+
+    def set_statemon(self, mon, indices, variables):
+        g = self.spec["state_monitors"][mon]["group"]
+        names = [v["name"] for v in self.spec["groups"][g]["vars"]]
+        idx = np.ascontiguousarray(indices, np.int32)
+        vs = np.ascontiguousarray([v if isinstance(v, int) else names.index(v) for v in variables], np.int32)
+        self.lib.oracle_set_statemon(self.h, int(mon), idx.ctypes.data_as(_i32p), idx.size,
+                                     vs.ctypes.data_as(_i32p), vs.size)
+        self._stm[mon] = (vs.size, idx.size)
+
+    def run(self, n_steps):
+        self.lib.oracle_run(self.h, int(n_steps))
+
+    def spikes(self, mon=0):
+        f = getattr(self.lib, f"oracle_spikemon_size_{mon}")
+        f.restype = C.c_int64
+        f.argtypes = [C.c_void_p]
+        n = f(self.h)
+        i = np.empty(n, np.int32)
+        ts = np.empty(n, np.int32)
+        g = self.spec["spike_monitors"][mon]["group"]
+        cnt = np.empty(int(self.sizes[g]), np.int32)
+        getattr(self.lib, f"oracle_spikemon_get_{mon}")(C.c_void_p(self.h), i.ctypes.data_as(_i32p),
+                                                         ts.ctypes.data_as(_i32p), cnt.ctypes.data_as(_i32p))
+        return i, ts, cnt
+
+    def rate_counts(self, mon=0):
+        f = getattr(self.lib, f"oracle_ratemon_size_{mon}")
+        f.restype = C.c_int64
+        f.argtypes = [C.c_void_p]
+        n = f(self.h)
+        a = np.empty(n, np.int32)
+        getattr(self.lib, f"oracle_ratemon_get_{mon}")(C.c_void_p(self.h), a.ctypes.data_as(_i32p))
+        return a
+
+    def state_trace(self, mon=0):
+        f = getattr(self.lib, f"oracle_statemon_size_{mon}")
+        f.restype = C.c_int64
+        f.argtypes = [C.c_void_p]
+        n = f(self.h)
+        nv, nr = self._stm[mon]
+        a = np.empty((n, nv, nr), np.float64)
+        getattr(self.lib, f"oracle_statemon_get_{mon}")(C.c_void_p(self.h), a.ctypes.data_as(_f64p))
+        return a
+
+
+def oracle_from_built(spec, built, dt=1e-4):
+    """An OracleNet holding the same network as a brian2_gb300.workloads.Built."""
+    o = OracleNet(spec, built.sizes, dt)
+    if built.consts:
+        o.set_consts(built.consts)
+    for (g, v), arr in built.group_init.items():
+        o.upload(g, v, arr)
+    for pw, s in built.synapses.items():
+        o.set_synapses(pw, s["pre"], s["post"], s.get("delay_steps"), s.get("scalar_delay", 0), s.get("src"),
+                       s.get("tgt"))
+        for var, arr in s.get("vars", {}).items():
+            o.upload_synapse_var(pw, var, arr)
+    for m, (lo, hi) in built.spikemon_ranges.items():
+        o.set_spikemon_range(m if isinstance(m, int) else 0, lo, hi)
+    for m, (lo, hi) in built.ratemon_ranges.items():
+        o.set_ratemon_range(m if isinstance(m, int) else 0, lo, hi)
+    return o
