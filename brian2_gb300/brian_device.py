@@ -243,7 +243,7 @@ class B200Device(CPPStandaloneDevice):
                 for vname, var in sorted(base.variables.items()):
                     if (isinstance(var, ArrayVariable) and not var.scalar and var.owner is not None
                             and var.owner.name == base.name and vname != "_spikespace"
-                            and var.size == len(base) and var.ndim == 1):
+                            and var.size == len(base) and getattr(var, "ndim", 1) == 1):
                         gv.append(dict(name=vname, ctype=c_data_type(var.dtype), ptr=gen_name(var)))
                 group_index[base.name] = len(groups)
                 groups.append(dict(name=base.name, vars=gv, _obj=base))
@@ -273,12 +273,17 @@ class B200Device(CPPStandaloneDevice):
                             extra[gen_name(var)] = ("group", gi, names.index(var.name))
             return extra
 
+        def text(code):
+            if isinstance(code, dict):
+                code = code[None]
+            if not isinstance(code, str):
+                code = "\n".join(code)
+            return code.strip("\n")
+
         def block(frag):
-            sc = frag["scalar"][None] if isinstance(frag["scalar"], dict) else frag["scalar"]
-            ve = frag["vector"][None] if isinstance(frag["vector"], dict) else frag["vector"]
-            out = dict(scalar=sc, vector=ve)
+            out = dict(scalar=text(frag["scalar"]), vector=text(frag["vector"]))
             if frag.get("vector_device"):
-                out["vector_device"] = frag["vector_device"][None]
+                out["vector_device"] = text(frag["vector_device"])
             return out
 
         pathways, spkmons, ratemons, statemons = [], [], [], []
@@ -309,18 +314,20 @@ class B200Device(CPPStandaloneDevice):
                         raise NotImplementedError(f"b200: several {t} code objects for one group")
                     g[key] = b
                 elif t == "synapses":
-                    pw = co.owner
+                    pw = obj
                     if not isinstance(pw, SynapticPathway) or pw.prepost != "pre":
                         raise NotImplementedError("b200: only on_pre pathways are supported")
                     syn = pw.synapses
                     sgi, srange = group_of(pw.source)
                     tgi, trange = group_of(pw.target)
-                    sv = []
+                    sv, seen = [], set()
+                    used = {id(v) for v in frag["variables"].values()}
                     for vname, var in sorted(syn.variables.items()):
                         if (isinstance(var, DynamicArrayVariable) and var.owner is not None
-                                and var.owner.name == syn.name and var.ndim == 1
-                                and vname not in ("_synaptic_pre", "_synaptic_post", "N_incoming", "N_outgoing")
-                                and not var.scalar):
+                                and var.owner.name == syn.name and getattr(var, "ndim", 1) == 1
+                                and var.name not in ("_synaptic_pre", "_synaptic_post", "N_incoming", "N_outgoing")
+                                and not var.scalar and id(var) in used and var.name not in seen):
+                            seen.add(var.name)
                             sv.append(dict(name=var.name, ctype=c_data_type(var.dtype), ptr=gen_name(var)))
                     gptrs = {}
                     for vname, var in frag["variables"].items():
@@ -367,12 +374,14 @@ class B200Device(CPPStandaloneDevice):
                     state_monitors=statemons, clock_ptrs=clock_ptrs)
         return spec, b200_objects
 
+    PRIVATE_KEYS = {"_obj", "_range", "_src_range", "_tgt_range", "_vars"}
+
     @staticmethod
     def public_spec(spec):
         """The JSON-serialisable part of a spec (drops the Brian objects)."""
         def clean(x):
             if isinstance(x, dict):
-                return {k: clean(v) for k, v in x.items() if not k.startswith("_")}
+                return {k: clean(v) for k, v in x.items() if k not in B200Device.PRIVATE_KEYS}
             if isinstance(x, list):
                 return [clean(v) for v in x]
             if isinstance(x, tuple):

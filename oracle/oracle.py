@@ -66,17 +66,16 @@ def render_oracle(spec: dict) -> str:
     w = o.append
     w("// oracle for model '%s' (generated; test infrastructure)" % spec["name"])
     w("#include <cmath>\n#include <cstdint>\n#include <cstring>\n#include <vector>\n#include <algorithm>")
+    # Brian's code objects see ``using namespace std`` (brian2/synapses/spikequeue.h:10,
+    # included through objects.h), so exp(float) is std::exp(float); _exprel and
+    # _brian_pow keep the reference's definitions (double-only _exprel, pow macro)
+    # (brian2/codegen/generators/cpp_generator.py:90-197, 567-618)
+    w("using namespace std;")
     w("static inline double _exprel(double x) { if (fabs(x) < 1e-16) return 1.0; if (x > 717) return INFINITY; return expm1(x)/x; }")
-    w("static inline float _exprel(float x) { if (fabsf(x) < 1e-16f) return 1.0f; if (x > 717.0f) return INFINITY; return expm1f(x)/x; }")
     w("template <typename T> static inline T _clip(const T v, const double a, const double b) { if (v < a) return a; if (v > b) return b; return v; }")
-    w("static inline double _brian_pow(double a, double b) { return pow(a, b); }")
-    w("static inline float _brian_pow(float a, float b) { return powf(a, b); }")
-    w("static inline double _brian_pow(double a, float b) { return pow(a, (double)b); }")
-    w("static inline double _brian_pow(float a, double b) { return pow((double)a, b); }")
-    w("static inline double _brian_pow(double a, int b) { return pow(a, (double)b); }")
-    w("static inline float _brian_pow(float a, int b) { return powf(a, (float)b); }")
-    w("static inline double _brian_mod(double x, double y) { double r = fmod(x, y); if (r != 0 && ((r < 0) != (y < 0))) r += y; return r; }")
-    w("static inline double _brian_floordiv(double x, double y) { return floor(x / y); }")
+    w("#define _brian_pow(x, y) (pow((x), (y)))")
+    w("template <typename T1, typename T2> static inline double _brian_mod(T1 x, T2 y) { return x - y * floor(1.0 * x / y); }")
+    w("template <typename T1, typename T2> static inline double _brian_floordiv(T1 x, T2 y) { return floor(1.0 * x / y); }")
     w("template <typename T> static inline int int_(T v) { return (int)v; }")
     w("static inline int64_t _timestep(double t, double dt) { return (int64_t)((t + 1e-3 * dt) / dt); }")
     w("#define _brian_abs fabs")
