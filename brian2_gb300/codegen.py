@@ -222,7 +222,8 @@ def render_model(spec: dict) -> str:
     w("template <int MAXT>")
     w("__global__ void __launch_bounds__(MAXT) b200_step_kernel(")
     w("    const b200_inst_d* __restrict__ insts, const int2* __restrict__ cta_map, int n_inst,")
-    w("    int queue_mode, int* work, int64_t max_steps, uint64_t limit_ns, int max_tiles1, int max_w) {")
+    w("    int queue_mode, int* work, int64_t max_steps, uint64_t limit_ns, int max_tiles1, int max_w,")
+    w("    int fault_rank) {")
     w("  extern __shared__ __align__(16) unsigned char b200_dyn[];")
     w("  int64_t* const s_item_seg = (int64_t*)b200_dyn;")
     w("  int* const s_item_off = (int*)(s_item_seg + blockDim.x);")
@@ -362,6 +363,8 @@ def render_model(spec: dict) -> str:
         w("          if (threadIdx.x == 0) GD.tile_cnt[u] = cnt;")
         w("        }")
         w("      }")
+    w("      // test hook: CTA `fault_rank` leaves without arriving, the others must time out")
+    w("      if (rank == fault_rank && ts == ts0) { ok = false; break; }")
     w("      if (!b200_inst_barrier(I, gen, limit_ns)) { ok = false; break; }")
 
     # ---- Phase B: prefix of tile counts, ring, monitors
@@ -573,14 +576,14 @@ def render_model(spec: dict) -> str:
     w("}")
     w("static cudaError_t b200_launch(b200_inst_d* insts, const int2* cta_map, int n_inst, int queue_mode,")
     w("                               int* work, int64_t max_steps, uint64_t limit_ns, int grid, int threads,")
-    w("                               int cooperative, int max_tiles1, int max_w, cudaStream_t s) {")
+    w("                               int cooperative, int max_tiles1, int max_w, int fault_rank, cudaStream_t s) {")
     w("  const void* k = b200_kernel_for(threads);")
     w("  const size_t smem = b200_dyn_smem(threads, max_tiles1, max_w);")
     w("  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);")
     w("  if (e != cudaSuccess) return e;")
     w("  const b200_inst_d* ci = insts;")
     w("  void* args[] = {(void*)&ci, (void*)&cta_map, (void*)&n_inst, (void*)&queue_mode, (void*)&work,")
-    w("                  (void*)&max_steps, (void*)&limit_ns, (void*)&max_tiles1, (void*)&max_w};")
+    w("                  (void*)&max_steps, (void*)&limit_ns, (void*)&max_tiles1, (void*)&max_w, (void*)&fault_rank};")
     w("  if (cooperative) return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(threads), args, smem, s);")
     w("  return cudaLaunchKernel(k, dim3(grid), dim3(threads), args, smem, s);")
     w("}")

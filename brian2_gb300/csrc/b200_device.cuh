@@ -151,7 +151,7 @@ struct b200_model_info {
   // launches the step kernel
   cudaError_t (*launch)(b200_inst_d* insts, const int2* cta_map, int n_inst, int queue_mode,
                         int* work, int64_t max_steps, uint64_t limit_ns, int grid, int threads,
-                        int cooperative, int max_tiles1, int max_w, cudaStream_t s);
+                        int cooperative, int max_tiles1, int max_w, int fault_rank, cudaStream_t s);
   int (*max_active_ctas)(int threads, int max_tiles1, int max_w);
 };
 
@@ -282,64 +282,67 @@ __device__ __forceinline__ bool b200_inst_barrier(const b200_inst_d& I, unsigned
 }
 
 // ---------------------------------------------------------------------------
-// Brian's function table for device code (same definitions as the C++ target,
-// brian2/codegen/generators/cpp_generator.py:567-618 and
-// brian2/devices/cpp_standalone/brianlib/common_math.h).
+// Brian's function table (brian2/codegen/generators/cpp_generator.py:90-197,
+// 567-618; brian2/devices/cpp_standalone/brianlib/common_math.h).  Host and
+// device: the scalar blocks are evaluated on the host, where the semantics are
+// the reference's (double-only _exprel, `pow` resolved through namespace std);
+// on the device float arguments stay in float.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double _exprel(double x) {
+__host__ __device__ __forceinline__ double _exprel(double x) {
   if (fabs(x) < 1e-16) return 1.0;
   if (x > 717) return INFINITY;
   return expm1(x) / x;
 }
+#ifdef __CUDA_ARCH__
 __device__ __forceinline__ float _exprel(float x) {
   if (fabsf(x) < 1e-16f) return 1.0f;
   if (x > 717.0f) return INFINITY;
   return expm1f(x) / x;
 }
+#else
+static inline double _exprel(float x) { return _exprel((double)x); }
+#endif
 template <typename T>
-__device__ __forceinline__ T _clip(const T value, const double a_min, const double a_max) {
+__host__ __device__ __forceinline__ T _clip(const T value, const double a_min, const double a_max) {
   if (value < a_min) return a_min;
   if (value > a_max) return a_max;
   return value;
 }
-__device__ __forceinline__ int _brian_sign(double x) { return (0 < x) - (x < 0); }
-__device__ __forceinline__ double _brian_pow(double a, double b) { return pow(a, b); }
-__device__ __forceinline__ float _brian_pow(float a, float b) { return powf(a, b); }
-__device__ __forceinline__ double _brian_pow(double a, float b) { return pow(a, (double)b); }
-__device__ __forceinline__ double _brian_pow(float a, double b) { return pow((double)a, b); }
-__device__ __forceinline__ double _brian_pow(double a, int b) { return pow(a, (double)b); }
-__device__ __forceinline__ float _brian_pow(float a, int b) { return powf(a, (float)b); }
-__device__ __forceinline__ double _brian_floordiv(double x, double y) { return floor(x / y); }
-__device__ __forceinline__ float _brian_floordiv(float x, float y) { return floorf(x / y); }
-__device__ __forceinline__ int32_t _brian_floordiv(int32_t x, int32_t y) {
-  int32_t q = x / y;
-  if ((x % y != 0) && ((x < 0) != (y < 0))) --q;
+template <typename T1, typename T2>
+__host__ __device__ __forceinline__ auto _brian_pow(T1 a, T2 b) -> decltype(pow(a, b)) {
+  using std::pow;
+  return pow(a, b);
+}
+template <typename T1, typename T2>
+__host__ __device__ __forceinline__ double _brian_floordiv(T1 x, T2 y) { return floor(1.0 * x / y); }
+__host__ __device__ __forceinline__ int32_t _brian_floordiv(int32_t a, int32_t b) {
+  int32_t q = a / b;
+  int32_t r = a - q * b;
+  q -= ((r != 0) & ((r ^ b) < 0));
   return q;
 }
-__device__ __forceinline__ int64_t _brian_floordiv(int64_t x, int64_t y) {
-  int64_t q = x / y;
-  if ((x % y != 0) && ((x < 0) != (y < 0))) --q;
+__host__ __device__ __forceinline__ int64_t _brian_floordiv(int64_t a, int64_t b) {
+  int64_t q = a / b;
+  int64_t r = a - q * b;
+  q -= ((r != 0) & ((r ^ b) < 0));
   return q;
 }
-__device__ __forceinline__ double _brian_mod(double x, double y) {
-  double r = fmod(x, y);
-  if (r != 0 && ((r < 0) != (y < 0))) r += y;
-  return r;
-}
-__device__ __forceinline__ int32_t _brian_mod(int32_t x, int32_t y) {
+template <typename T1, typename T2>
+__host__ __device__ __forceinline__ double _brian_mod(T1 x, T2 y) { return x - y * floor(1.0 * x / y); }
+__host__ __device__ __forceinline__ int32_t _brian_mod(int32_t x, int32_t y) {
   int32_t r = x % y;
-  if (r != 0 && ((r < 0) != (y < 0))) r += y;
+  r += ((r != 0) & ((r ^ y) < 0)) * y;
   return r;
 }
-__device__ __forceinline__ int64_t _brian_mod(int64_t x, int64_t y) {
+__host__ __device__ __forceinline__ int64_t _brian_mod(int64_t x, int64_t y) {
   int64_t r = x % y;
-  if (r != 0 && ((r < 0) != (y < 0))) r += y;
+  r += ((r != 0) & ((r ^ y) < 0)) * y;
   return r;
 }
 template <typename T>
-__device__ __forceinline__ int int_(T value) { return (int)value; }
+__host__ __device__ __forceinline__ int int_(T value) { return (int)value; }
 // core/functions.py:771 timestep(t, dt) = int64((t + 1e-3*dt)/dt)
-__device__ __forceinline__ int64_t _timestep(double t, double dt) {
+__host__ __device__ __forceinline__ int64_t _timestep(double t, double dt) {
   return (int64_t)((t + 1e-3 * dt) / dt);
 }
 #define _brian_abs fabs

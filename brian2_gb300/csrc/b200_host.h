@@ -86,6 +86,7 @@ struct b200_net {
   int grid = 0;
   int64_t chunk_steps = 100000;
   uint64_t limit_ns = 2000000000ull;  // bounded waits: 2 s
+  int fault_rank = -1;                 // test hook: CTA that skips its first barrier
   bool prepared = false;
   bool use_graph = true;
   cudaGraphExec_t graph_exec = nullptr;
@@ -812,7 +813,8 @@ int b200_run(b200_net* n, int64_t n_steps) {
     const int64_t steps = n->chunk_steps;
     cudaError_t le = M->launch((b200_inst_d*)n->d_insts.p, (const int2*)n->d_cta_map.p, n->n_inst,
                                n->queue_mode, (int*)n->d_work.p, steps, n->limit_ns, n->grid,
-                               n->threads, coop, n->max_tiles1, n->max_w, n->stream);
+                               n->threads, coop, n->max_tiles1, n->max_w, n->fault_rank, n->stream);
+    n->fault_rank = -1;  // one-shot
     if (le != cudaSuccess) return b200_fail(n, B200_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(le));
     ++n->launches;
     B200_CU(n, cudaStreamSynchronize(n->stream));
@@ -823,7 +825,9 @@ int b200_run(b200_net* n, int64_t n_steps) {
       B200_CU(n, cudaMemcpy(&st, I.status.p, 4, cudaMemcpyDeviceToHost));
       B200_CU(n, cudaMemcpy(&done, I.ts_done.p, 8, cudaMemcpyDeviceToHost));
       if (st != 0) {
+        // leave the handle usable: clear the status and the barrier state
         cudaMemset(I.status.p, 0, 4);
+        cudaMemset(I.bar.p, 0, 16);
         return b200_fail(n, st == B200_ERR_BARRIER_TIMEOUT ? B200_ERR_BARRIER_TIMEOUT : B200_ERR_INDEX,
                          "instance %d: device status %d at step %lld (%s)", k, st, (long long)done,
                          st == B200_ERR_BARRIER_TIMEOUT ? "instance barrier timed out" : "index out of range");
@@ -840,6 +844,15 @@ int b200_run(b200_net* n, int64_t n_steps) {
   n->last_run_ms = ms;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  return 0;
+}
+
+// Test hook: bounded-wait limit, and a CTA rank that leaves before its first
+// barrier of the next launch (so the instance barrier must time out).
+int b200_set_wait_limit(b200_net* n, int64_t limit_ns, int32_t fault_rank) {
+  if (!n || limit_ns <= 0) return B200_ERR_ARG;
+  n->limit_ns = (uint64_t)limit_ns;
+  n->fault_rank = fault_rank;
   return 0;
 }
 

@@ -64,6 +64,7 @@ def _declare(lib):
         "b200_model_name": [C.c_char_p, C.c_int64],
         "b200_device_bytes": [h, _i64p],
         "b200_launch_count": [h, _i64p],
+        "b200_set_wait_limit": [h, C.c_int64, C.c_int32],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -291,6 +292,9 @@ class Network:
         v = C.c_int64()
         self._check(self.lib.b200_launch_count(self._h, C.byref(v)))
         return v.value
+
+    def set_wait_limit(self, limit_ns, fault_rank=-1):
+        self._check(self.lib.b200_set_wait_limit(self._h, int(limit_ns), int(fault_rank)))
 
     def device_bytes(self):
         v = C.c_int64()

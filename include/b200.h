@@ -1,0 +1,128 @@
+/*
+ * b200.h -- C ABI of the GB300 clock-driven step engine for Brian2.
+ *
+ * Every model library (one per network spec, built by brian2_gb300.native from
+ * the code generator's output) exports exactly these symbols.  Plain C types
+ * only; the handle owns all device memory; every entry point returns a status
+ * (0 = ok, see B200_STATUS_*) and b200_last_error() gives the message.  No entry
+ * point calls exit(): the reference's generated code exits on bad sizes or
+ * indices (brian2/devices/cpp_standalone/templates/synapses_create_generator.cpp:105,113,196,218),
+ * here those are B200_STATUS_INDEX / B200_STATUS_ARG.
+ *
+ * The reference has no C ABI for this path: its boundary is "generate a C++
+ * project and run ./main" (brian2/devices/cpp_standalone/device.py:1207-1351).
+ * Each function below names the piece of that project it replaces.
+ */
+#ifndef B200_H
+#define B200_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct b200_net b200_net;
+
+#define B200_STATUS_OK 0
+#define B200_STATUS_CUDA 1     /* a CUDA runtime call failed */
+#define B200_STATUS_ARG 2      /* invalid argument (sizes, ranges, ids) */
+#define B200_STATUS_CAPACITY 3 /* a buffer limit was exceeded */
+#define B200_STATUS_TIMEOUT 4  /* a bounded device-side wait gave up */
+#define B200_STATUS_INDEX 5    /* an index (synapse, neuron) out of range */
+
+/* Kinds of variables addressed by b200_upload / b200_download. */
+#define B200_VAR_GROUP 0   /* neuron-group state variable */
+#define B200_VAR_SYNAPSE 1 /* synaptic variable, given in synapse creation order */
+
+/* Creates n_inst independent instances of the model (one network, or a batched
+ * sweep).  group_sizes[k*n_groups+g] = neurons of group g in instance k.
+ * Replaces _init_arrays (brian2/devices/cpp_standalone/templates/objects.cpp:185-248). */
+int b200_create(b200_net** out, int32_t n_inst, const int32_t* group_sizes, double dt);
+/* Frees every device buffer of the handle. Replaces _dealloc_arrays (objects.cpp:372-400). */
+int b200_destroy(b200_net* net);
+/* Copies the message of the last failing call into buf. */
+int b200_last_error(b200_net* net, char* buf, int64_t len);
+
+/* Launch shape: threads per CTA, CTAs per instance (>1: instance barrier), queue
+ * mode (resident CTAs pull single-CTA instances), steps per kernel launch, and
+ * whether launches are replayed from a captured CUDA graph.  Replaces the OpenMP
+ * thread preference (brian2/devices/cpp_standalone/device.py:60-67). */
+int b200_configure(b200_net* net, int32_t threads, const int32_t* ctas_per_inst, int32_t queue_mode,
+                   int64_t chunk_steps, int32_t use_graph);
+/* Per-instance values of the model's namespace constants (the %CONSTANTS% of the
+ * generated code objects, device.py:936-940); scalar blocks are re-evaluated. */
+int b200_set_consts(b200_net* net, int32_t inst, const double* values, int32_t count);
+
+/* Host <-> device copies of state and synaptic variables.
+ * Replace _load_arrays / _write_arrays (objects.cpp:249-370). */
+int b200_upload(b200_net* net, int32_t inst, int32_t kind, int32_t obj, int32_t var, const void* src,
+                int64_t count);
+int b200_download(b200_net* net, int32_t inst, int32_t kind, int32_t obj, int32_t var, void* dst,
+                  int64_t count);
+
+/* Synapses of one pathway in creation order.  pre/post are relative to the source
+ * range [src_lo,src_hi) and target range [tgt_lo,tgt_hi); delay_steps[k] is the
+ * quantised delay (int)(delay/dt+0.5), or NULL for the single scalar_delay.
+ * Replaces CSpikeQueue::prepare (brian2/synapses/spikequeue.h:45-105) and the
+ * before_run block of templates/synapses_push_spikes.cpp:5-17. */
+int b200_set_synapses(b200_net* net, int32_t inst, int32_t pathway, int32_t src_lo, int32_t src_hi,
+                      int32_t tgt_lo, int32_t tgt_hi, const int32_t* pre, const int32_t* post,
+                      const int32_t* delay_steps, int32_t scalar_delay, int64_t n_syn);
+/* Same, from a CSR over (source, delay slot) that is already in device memory
+ * (device-side construction of very large networks). */
+int b200_set_synapses_csr(b200_net* net, int32_t inst, int32_t pathway, int32_t src_lo, int32_t src_hi,
+                          int32_t tgt_lo, int32_t tgt_hi, int32_t dmin, int32_t dmax,
+                          const int64_t* d_segptr, const int32_t* d_post, const int32_t* d_pre,
+                          int64_t n_syn);
+/* Device address of a synaptic variable (CSR order) for device-side fills. */
+int b200_synapse_var_ptr(b200_net* net, int32_t inst, int32_t pathway, int32_t var, void** out);
+
+/* Monitor ranges (subgroup sources) and StateMonitor selection.  Replace the
+ * _source_start/_source_stop handling of templates/spikemonitor.cpp:17-33,
+ * templates/ratemonitor.cpp:8-31 and the record indices of templates/statemonitor.cpp. */
+int b200_set_monitor_range(b200_net* net, int32_t inst, int32_t kind, int32_t mon, int32_t lo, int32_t hi);
+int b200_set_statemon(b200_net* net, int32_t inst, int32_t mon, const int32_t* idx, int32_t n_rec,
+                      const int32_t* vars, int32_t n_vars);
+
+/* Runs every instance n_steps clock steps from its current step: state update,
+ * threshold, spike monitor, propagation (advance/push/on_pre), reset, rate and
+ * state monitors, clock tick -- all on the device.  Replaces Network::run
+ * (templates/network.cpp:38-122) with the code objects of stateupdate.cpp,
+ * threshold.cpp, spikemonitor.cpp, synapses_push_spikes.cpp, synapses.cpp,
+ * reset.cpp, ratemonitor.cpp and statemonitor.cpp. */
+int b200_run(b200_net* net, int64_t n_steps);
+/* Current clock step of an instance (Clock::timestep, brianlib/clocks.h:34-38). */
+int b200_get_step(b200_net* net, int32_t inst, int64_t* ts);
+int b200_set_step(b200_net* net, int32_t inst, int64_t ts);
+/* Device time of the last b200_run in ms (CUDA events); the reference's
+ * _last_run_time (device.py:1326-1332). */
+int b200_last_run_ms(b200_net* net, double* ms);
+
+/* Monitor contents, copied back on request (device-resident until then).
+ * Replace the dynamic arrays written by spikemonitor.cpp:37-47, ratemonitor.cpp:33-35,
+ * statemonitor.cpp. */
+int b200_spikemon_size(b200_net* net, int32_t inst, int32_t mon, int64_t* count);
+int b200_spikemon_get(b200_net* net, int32_t inst, int32_t mon, int32_t* i, int32_t* ts,
+                      int32_t* per_neuron, int64_t count);
+int b200_ratemon_size(b200_net* net, int32_t inst, int32_t mon, int64_t* steps);
+int b200_ratemon_get(b200_net* net, int32_t inst, int32_t mon, int32_t* counts, int64_t steps);
+int b200_statemon_size(b200_net* net, int32_t inst, int32_t mon, int64_t* steps);
+int b200_statemon_get(b200_net* net, int32_t inst, int32_t mon, double* data, int64_t steps);
+int b200_reset_monitors(b200_net* net, int32_t inst);
+
+/* Bounded device-side waits: limit in ns for the instance barrier, and a test
+ * hook (fault_rank >= 0) that makes that CTA leave before its first barrier of
+ * the next launch, so the others time out and b200_run returns
+ * B200_STATUS_TIMEOUT with the handle still usable.  The reference's analogue
+ * is the wall-clock limit of Network::run (templates/network.cpp:59-82). */
+int b200_set_wait_limit(b200_net* net, int64_t limit_ns, int32_t fault_rank);
+
+/* Introspection. */
+int b200_model_name(char* buf, int64_t len);
+int b200_device_bytes(b200_net* net, int64_t* bytes);
+int b200_launch_count(b200_net* net, int64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* B200_H */

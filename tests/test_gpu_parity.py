@@ -1,0 +1,136 @@
+"""CUDA path against the reference's outputs and the oracle (GPU only).
+
+Bar: float64 CUBA and delay networks are bit-exact with Brian2 cpp_standalone
+(spike raster and final state) for every launch shape, because their per-step
+arithmetic is mul/add with host-computed loop invariants and their synaptic
+increments are equal per target variable (so atomic order cannot change a
+sum).  COBAHH evaluates exp/expm1/pow on the device, whose libm differs from
+glibc in the last ulp; its rasters are compared up to the first divergence,
+which must come later than a stated time, and are reported.
+"""
+import numpy as np
+import pytest
+
+from brian2_gb300 import workloads as W
+from cases import CASES
+from oracle import oracle_from_built
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [dict(threads=256), dict(threads=1024), dict(threads=256, ctas_per_inst=3), dict(threads=128, ctas_per_inst=8)]
+
+
+def first_divergence(i1, t1, i2, t2):
+    """Time step of the first difference between two rasters (or None)."""
+    n = min(len(i1), len(i2))
+    d = np.flatnonzero((i1[:n] != i2[:n]) | (t1[:n] != t2[:n]))
+    if len(d):
+        return int(min(t1[d[0]], t2[d[0]]))
+    if len(i1) != len(i2):
+        return int((t1 if len(t1) > n else t2)[n])
+    return None
+
+
+@pytest.mark.parametrize("case", ["cuba_small_f64", "cuba_f64", "delays_small_f64", "delays_f64"])
+@pytest.mark.parametrize("shape", range(len(SHAPES)))
+def test_bit_exact_with_reference(case, shape, golden):
+    spec_name, build, steps = CASES[case]
+    spec = W.load_spec(spec_name)
+    meta, z = golden(case)
+    net = W.instantiate(spec, [build(spec)], **SHAPES[shape])
+    net.run(steps)
+    i, ts, cnt = net.spikes(0, 0)
+    assert len(i) == meta["n_spikes"]
+    np.testing.assert_array_equal(i, z["spk_i"])
+    np.testing.assert_array_equal(ts, z["spk_ts"])
+    for var in ("v", "ge", "gi"):
+        np.testing.assert_array_equal(net.download(0, "neurongroup", var), z[var], err_msg=var)
+    np.testing.assert_array_equal(net.rate_counts(0, 0), np.bincount(z["spk_ts"], minlength=steps))
+    np.testing.assert_array_equal(cnt, np.bincount(z["spk_i"], minlength=len(cnt)))
+
+
+def test_split_runs_equal_one_run(golden):
+    """run(a); run(b) == run(a+b): spikes in flight in the delay ring and the
+    pending reset survive the boundary (Network.run continuation)."""
+    spec_name, build, steps = CASES["delays_small_f64"]
+    spec = W.load_spec(spec_name)
+    meta, z = golden("delays_small_f64")
+    net = W.instantiate(spec, [build(spec)], threads=256, ctas_per_inst=2)
+    for chunk in (1, 7, 500, 1000, steps - 1508):
+        net.run(chunk)
+    i, ts, _ = net.spikes(0, 0)
+    np.testing.assert_array_equal(i, z["spk_i"])
+    np.testing.assert_array_equal(ts, z["spk_ts"])
+    np.testing.assert_array_equal(net.download(0, "neurongroup", "v"), z["v"])
+
+
+@pytest.mark.parametrize("case", ["cobahh_small_f64", "cobahh_f64", "cobahh_f32"])
+def test_cobahh_until_first_divergence(case, golden):
+    spec_name, build, steps = CASES[case]
+    spec = W.load_spec(spec_name)
+    meta, z = golden(case)
+    net = W.instantiate(spec, [build(spec)], threads=256)
+    net.run(steps)
+    i, ts, _ = net.spikes(0, 0)
+    div = first_divergence(i, ts, z["spk_i"], z["spk_ts"])
+    v = net.download(0, "neurongroup", "v").astype(np.float64)
+    rel = np.abs(v - z["v"]) / np.maximum(np.abs(z["v"]), 1e-12)
+    print(f"\n{case}: spikes gpu={len(i)} ref={len(z['spk_i'])} first divergent step={div} "
+          f"v max rel err={rel.max():.3e} median={np.median(rel):.3e}")
+    assert abs(len(i) - len(z["spk_i"])) <= 0.05 * len(z["spk_i"]) + 5
+    # no divergence in the first 20 ms (200 steps) of the run
+    assert div is None or div >= 200
+
+
+def test_multi_cta_matches_single_cta():
+    spec = W.load_spec("cuba_f64")
+    b = W.build_cuba(spec, N=3000, seed=21)
+    outs = []
+    for shape in (dict(threads=512), dict(threads=64, ctas_per_inst=16)):
+        net = W.instantiate(spec, [b], **shape)
+        net.run(2000)
+        outs.append((net.spikes(0, 0), net.download(0, "neurongroup", "v")))
+    (i0, t0, c0), v0 = outs[0]
+    (i1, t1, c1), v1 = outs[1]
+    np.testing.assert_array_equal(i0, i1)
+    np.testing.assert_array_equal(t0, t1)
+    np.testing.assert_array_equal(v0, v1)
+
+
+def test_batched_instances_equal_separate_oracles():
+    """Queue mode: independent instances of different sizes and constants in
+    one launch, each identical to its own oracle run."""
+    spec = W.load_spec("cuba_f64")
+    rng = np.random.default_rng(0)
+    builts = []
+    for k in range(7):
+        N = int(rng.integers(200, 1500))
+        b = W.build_cuba(spec, N=N, seed=100 + k, consts=dict(taum=float(rng.uniform(0.01, 0.03))))
+        builts.append(b)
+    net = W.instantiate(spec, builts, threads=256, queue_mode=True)
+    net.run(1500)
+    for k, b in enumerate(builts):
+        o = oracle_from_built(spec, b)
+        o.run(1500)
+        oi, ots, _ = o.spikes(0)
+        i, ts, _ = net.spikes(k, 0)
+        np.testing.assert_array_equal(i, oi)
+        np.testing.assert_array_equal(ts, ots)
+        np.testing.assert_array_equal(net.download(k, "neurongroup", "v"), o.download(0, "v"))
+
+
+def test_barrier_timeout_reports_status_and_handle_stays_usable():
+    from brian2_gb300.runtime import B200Error
+    spec = W.load_spec("cuba_f64")
+    b = W.build_cuba(spec, N=2000, seed=3)
+    net = W.instantiate(spec, [b], threads=128, ctas_per_inst=4)
+    net.set_wait_limit(50_000_000, fault_rank=1)   # 50 ms; CTA 1 skips its first barrier
+    with pytest.raises(B200Error) as e:
+        net.run(10)
+    assert e.value.status == 4
+    # the context is intact: a new network on the same device runs normally
+    net2 = W.instantiate(spec, [b], threads=128, ctas_per_inst=4)
+    net2.run(100)
+    o = oracle_from_built(spec, b)
+    o.run(100)
+    np.testing.assert_array_equal(net2.spikes(0, 0)[0], o.spikes(0)[0])
