@@ -1,0 +1,303 @@
+"""Benchmark of the clock-driven step loop on one GB300 (or N replicas).
+
+Workload (default): the large CUBA network with delays -- 1,000,000 LIF neurons
+(80/20 E/I), fixed in-degree 1000 (800 E + 200 I sources, 1e9 synapses),
+per-synapse float32 weights, per-synapse delays uniform in 0.1-5.0 ms quantised
+to dt = 0.1 ms, float32 state, exact-linear integration.  Synthetic data: the
+network is constructed on the device from a seed.  One bench step = 1000 clock
+steps (100 ms simulated), continuing the same simulation.
+
+Printed (rank 0, one JSON line): synaptic events/s over the timed steps
+(events = sum over emitted spikes of the source's out-degree), simulated
+seconds per wall second, an end-to-end figure through the public API with host
+buffers (state uploaded from pinned memory and the step's spikes read back every
+step), the step kernel's roofline, and the oracle timed on the host cores as a
+CPU baseline.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_NEURONS = 1_000_000
+K_IN = 1000
+STEPS_PER_BENCH_STEP = 1000  # 100 ms simulated
+WORKLOAD = "cuba_delays_1e6_k1000_f32"
+METRIC = "synaptic_events_per_s"
+UNIT = "events/s"
+
+
+def rank_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(s[0]) for s in self.samples if s and s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if len(s) > 1 and s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if len(s) > 3 + k and s[3 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def ncu_traffic_per_neuron_step():
+    """DRAM bytes per (neuron-step) of the step kernel from the committed ncu
+    summary (profiles/step_kernel_cuba_delays.json), or None."""
+    p = os.path.join(ROOT, "profiles", "step_kernel_cuba_delays.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d["dram_bytes_per_launch"] / (d["neurons"] * d["steps_per_launch"]), d
+    except Exception:
+        return None, None
+
+
+def cpu_baseline(max_seconds=20.0):
+    """The oracle (single-threaded CPU restatement of the reference's step loop)
+    on a bounded sample of the same workload: the 10,000-neuron network of
+    identical construction (in-degree 1000, delays 0.1-5 ms), float64."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import oracle_from_built
+    from brian2_gb300 import workloads as W
+    spec = W.load_spec("delays_f64")
+    b = W.build_delays(spec, N=10_000, K=K_IN, seed=1234)
+    outdeg = np.zeros(10_000, np.int64)
+    for s in b.synapses.values():
+        outdeg += np.bincount(s["pre"] + s["src"][0], minlength=10_000)
+    o = oracle_from_built(spec, b)
+    o.run(500)  # warm-up: fill the delay ring
+    i0 = len(o.spikes(0)[0])
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < 20000 and time.perf_counter() - t0 < max_seconds:
+        o.run(500)
+        steps += 500
+        if time.perf_counter() - t0 > max_seconds / 2 and steps >= 2000:
+            break
+    dt = time.perf_counter() - t0
+    i, ts, _ = o.spikes(0)
+    ev = int(outdeg[i[i0:]].sum())
+    return {"value": ev / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"oracle (C++ restatement, float64) on the 10,000-neuron subnetwork of identical "
+                      f"construction, {steps} clock steps ({steps * 1e-4:.2f} s simulated) in {dt:.2f} s wall",
+            "sim_s_per_wall_s": steps * 1e-4 / dt}
+
+
+def run_reference(args, rank, world):
+    """--impl reference: the reference's CPU path for this workload (the oracle
+    port, single-threaded) on the same metric and config."""
+    if rank != 0:
+        return
+    vals = []
+    for _ in range(args.warmup):
+        cpu_baseline(max_seconds=5.0)
+    for _ in range(args.steps):
+        vals.append(cpu_baseline(max_seconds=10.0))
+    v = float(np.median([x["value"] for x in vals]))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded construction)",
+            "config": {"workload": WORKLOAD, "sample": "10,000-neuron subnetwork, same construction"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--neurons", type=int, default=N_NEURONS)
+    ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--ctas", type=int, default=0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = rank_info()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist = dist_mod
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        if dist:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local)) if world > 1 else None
+    from brian2_gb300 import workloads as W
+    from brian2_gb300.scale import build_delays_scale
+    spec = W.load_spec("delays_f32")
+    N = args.neurons
+    seed = 1234 + rank  # weak scaling: every rank simulates its own network
+    t_build = time.perf_counter()
+    threads = args.threads or 1024
+    ctas = args.ctas or 152
+    net, _ = build_delays_scale(spec, N=N, K=K_IN, seed=seed, threads=threads, ctas_per_inst=ctas)
+    t_build = time.perf_counter() - t_build
+    outdeg = net.outdegree
+    plan = net.launch_plan()
+
+    def bench_step():
+        net.run(STEPS_PER_BENCH_STEP)
+        return net.last_kernel_ms()
+
+    for _ in range(args.warmup):
+        bench_step()
+    n_before = int(net.spikes(0, 0)[0].size)
+    launches0 = net.launches()
+    if dist:
+        dist.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    kernel_ms = []
+    for _ in range(args.steps):
+        kernel_ms.append(bench_step())
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    launches = net.launches() - launches0
+    i, ts, _ = net.spikes(0, 0)
+    i = i[n_before:]
+    events = int(outdeg[i].sum())
+    sim_s = args.steps * STEPS_PER_BENCH_STEP * 1e-4
+    if dist:
+        import torch
+        t = torch.tensor([wall], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        wall = float(t.item())
+        e = torch.tensor([events], dtype=torch.float64)
+        dist.all_reduce(e, op=dist.ReduceOp.SUM)
+        events_all = float(e.item())
+    else:
+        events_all = float(events)
+    value = events_all / wall
+
+    # roofline of the step kernel: algorithmic bytes per launch (one launch = one
+    # bench step of 1000 clock steps): 24 B per neuron-step (v, ge, gi read and
+    # written, float32) + 8 B per synaptic event (target index + weight)
+    launch_ms = float(np.mean(kernel_ms))
+    alg_bytes = 24.0 * N * STEPS_PER_BENCH_STEP + 8.0 * events / args.steps
+    achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
+    peaks, peak_kind = measured_peaks()
+    tr_per_ns, tr_src = ncu_traffic_per_neuron_step()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "peak_kind": peak_kind,
+                "traffic": (tr_per_ns * N * STEPS_PER_BENCH_STEP) if tr_per_ns else None,
+                "kernel": "b200_step_kernel", "ms_per_launch": launch_ms,
+                "algorithmic_bytes_per_launch": alg_bytes}
+
+    # end to end through the public API: every step uploads the state from
+    # pinned host memory, runs, and reads the step's spikes back
+    import torch
+    host = {v: torch.empty(N, dtype=torch.float32).pin_memory() for v in ("v", "ge", "gi")}
+    for v in host:
+        host[v].numpy()[:] = net.download(0, "neurongroup", v)
+    e2e_events, h2d, d2h = 0, 0, 0
+    if dist:
+        dist.barrier()
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        for v, buf in host.items():
+            net.upload(0, "neurongroup", v, buf.numpy())
+            h2d += buf.numel() * 4
+        net.reset_monitors(0)
+        net.run(STEPS_PER_BENCH_STEP)
+        si, sts, _ = net.spikes(0, 0)
+        d2h += si.nbytes + sts.nbytes
+        e2e_events += int(outdeg[si].sum())
+    e2e_wall = time.perf_counter() - t1
+    if dist:
+        t = torch.tensor([e2e_wall], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_wall = float(t.item())
+        e = torch.tensor([e2e_events], dtype=torch.float64)
+        dist.all_reduce(e, op=dist.ReduceOp.SUM)
+        e2e_events = float(e.item())
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: network constructed on the device from a seed",
+            "config": {"workload": WORKLOAD, "neurons": N, "in_degree": K_IN, "synapses": N * K_IN,
+                       "delays_ms": [0.1, 5.0], "dt_ms": 0.1, "clock_steps_per_step": STEPS_PER_BENCH_STEP,
+                       "l2": "inputs larger than L2 (synapse arrays 8 GB per GPU)",
+                       "threads": threads, "ctas": ctas, "launch_plan": plan, "build_s": round(t_build, 2)},
+            "sim_s_per_wall_s": sim_s / wall,
+            "spikes_per_step": float(len(i)) / args.steps,
+            "e2e": {"value": e2e_events / e2e_wall, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
+                    "d2h_bytes_per_step": d2h // args.steps},
+            "roofline": roofline,
+            "gpu_launches": int(launches),
+            "clocks": clk,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -55,6 +55,25 @@ def scalar_outputs(code: str):
     return out
 
 
+_FLOAT_LIT = re.compile(r"(?<![\w.])((?:\d+\.\d*|\.\d+)(?:[eE][+-]?\d+)?|\d+[eE][+-]?\d+)(?![\w.])")
+
+
+def _single_precision(code: str) -> str:
+    """Device code of a float32 network stays in single precision.
+
+    Brian's float32 code objects keep namespace constants and literals in
+    double (``const double Vt``, ``1.0f*(- 4.0)/ms``), which on the host costs
+    nothing but on GB300 puts every such operation on the FP64 pipe (about
+    1/64 of the FP32 rate).  Here double literals become float literals;
+    constants and loop-invariant scalars are loaded as float (see
+    ``_Tables.device_loads``).  The clock time and ``lastspike`` stay double.
+    This is a deliberate difference from the reference's float32 mode, whose
+    results the float32 device path matches within the stated tolerance, not
+    bit for bit.
+    """
+    return _FLOAT_LIT.sub(lambda m: m.group(1) + "f", code)
+
+
 def _indent(code: str, n: int) -> str:
     pad = " " * n
     return "\n".join(pad + ln if ln.strip() else "" for ln in code.splitlines())
@@ -85,13 +104,20 @@ class _Tables:
     def size(self):
         return len(self.entries)
 
-    def device_loads(self, name):
-        """Declarations reading the constants and this block's scalars from S."""
-        lines = [f"const {ct} {nm} = ({ct})_b200_S[{k}];" for k, (ct, nm) in enumerate(self.entries[:len(self.consts)])]
+    def device_loads(self, name, single=False):
+        """Declarations reading the constants and this block's scalars from the
+        typed shared copies of S (_b200_S double, _b200_Sf float, _b200_Si
+        integer), so no conversion runs per use (float instead of double when
+        `single`)."""
+        def load(ct, nm, k):
+            et = "float" if (single and ct == "double") else ct
+            src = {"double": "_b200_S", "float": "_b200_Sf"}.get(et, "_b200_Si")
+            return f"const {et} {nm} = ({et}){src}[{k}];"
+        lines = [load(ct, nm, k) for k, (ct, nm) in enumerate(self.entries[:len(self.consts)])]
         if name in self.block_ranges:
             off, outs = self.block_ranges[name]
-            lines += [f"const {ct} {nm} = ({ct})_b200_S[{off + k}];" for k, (ct, nm) in enumerate(outs)]
-        lines.append("(void)_b200_S;")
+            lines += [load(ct, nm, off + k) for k, (ct, nm) in enumerate(outs)]
+        lines.append("(void)_b200_S; (void)_b200_Sf; (void)_b200_Si;")
         return "\n".join(lines)
 
     def host_eval(self, blocks):
@@ -122,6 +148,26 @@ def render_model(spec: dict) -> str:
     clock = spec.get("clock_ptrs", {"dt": "_ptr_array_defaultclock_dt", "t": "_ptr_array_defaultclock_t",
                                      "timestep": "_ptr_array_defaultclock_timestep"})
     NG, NP = len(groups), len(paths)
+    # device code reads the clock from registers, not through pointers to locals
+    def _clockless(code):
+        if not code:
+            return code
+        for key, var in (("t", "_b200_t"), ("dt", "_b200_dt"), ("timestep", "_b200_ts")):
+            code = re.sub(re.escape(clock[key]) + r"\s*\[\s*0\s*\]", var, code)
+        return code
+    f32 = spec.get("float", "double") == "float"
+
+    def _device(code):
+        code = _clockless(code)
+        return _single_precision(code) if (f32 and code) else code
+    groups = [dict(g) for g in groups]
+    for g in groups:
+        for blk in ("update", "threshold", "reset"):
+            if g.get(blk):
+                g[blk] = dict(g[blk], vector=_device(g[blk].get("vector")))
+    paths = [dict(p, on_pre=dict(p["on_pre"], vector=_device(p["on_pre"].get("vector")),
+                                 vector_device=_device(p["on_pre"].get("vector_device"))))
+             for p in paths]
     assert 1 <= NG <= 4 and NP <= 8 and len(spkmons) <= 4 and len(ratemons) <= 4 and len(statemons) <= 4
 
     o = []
@@ -143,16 +189,44 @@ def render_model(spec: dict) -> str:
         blocks = [("on_pre", _block(p.get("on_pre")))]
         ptables.append((_Tables(consts, blocks), blocks))
 
+    SIZE = {"double": 8, "int64_t": 8, "float": 4, "int32_t": 4, "char": 1, "int8_t": 1}
+
+    def used_vars(gi):
+        """Variables of group gi that the step code touches (cached in smem)."""
+        g = groups[gi]
+        text = ""
+        for blk in ("update", "threshold", "reset"):
+            if g.get(blk):
+                text += g[blk].get("vector", "") + "\n" + json.dumps(g[blk].get("extra_ptrs", {}))
+        for p in paths:
+            text += (p["on_pre"].get("vector_device") or p["on_pre"].get("vector", "")) + json.dumps(p.get("group_ptrs", {}))
+            for gg in groups:
+                for blk in ("update", "threshold", "reset"):
+                    if gg.get(blk):
+                        text += json.dumps(gg[blk].get("extra_ptrs", {}))
+        used = []
+        for k, v in enumerate(g["vars"]):
+            if re.search(r"\b%s\b" % re.escape(v["ptr"]), text):
+                used.append(k)
+            elif v["name"] in ("not_refractory", "lastspike") and g.get("threshold") and g["threshold"].get("refractory"):
+                used.append(k)
+        # pack 8-byte variables first so every cached array stays aligned
+        return sorted(used, key=lambda k: -SIZE[g["vars"][k]["ctype"]])
+
+    USED = [used_vars(gi) for gi in range(NG)]
+    MAXV = max(len(g["vars"]) for g in groups)
+
     # ------------------------------------------------------------- model tables
     for gi, g in enumerate(groups):
         w(f"static const char* const b200_g{gi}_vars[] = {{" + ", ".join(f'"{v["name"]}"' for v in g["vars"]) + "};")
         w(f"static const int b200_g{gi}_kinds[] = {{" + ", ".join(str(CTYPE_KIND[v["ctype"]]) for v in g["vars"]) + "};")
+        w(f"static const int b200_g{gi}_used[] = {{" + ", ".join("1" if k in USED[gi] else "0" for k in range(len(g["vars"]))) + "};")
     for pi, p in enumerate(paths):
         pv = p.get("vars", [])
         w(f"static const char* const b200_p{pi}_vars[] = {{" + ", ".join(f'"{v["name"]}"' for v in pv) + ('' if pv else '""') + "};")
         w(f"static const int b200_p{pi}_kinds[] = {{" + ", ".join(str(CTYPE_KIND[v["ctype"]]) for v in pv) + ('' if pv else '0') + "};")
     w("static const b200_group_info b200_groups[] = {" + ", ".join(
-        f'{{"{g["name"]}", {len(g["vars"])}, b200_g{gi}_vars, b200_g{gi}_kinds, {gtables[gi][0].size}}}'
+        f'{{"{g["name"]}", {len(g["vars"])}, b200_g{gi}_vars, b200_g{gi}_kinds, {gtables[gi][0].size}, b200_g{gi}_used}}'
         for gi, g in enumerate(groups)) + "};")
     if paths:
         w("static const b200_pathway_info b200_pathways[] = {" + ", ".join(
@@ -192,11 +266,11 @@ def render_model(spec: dict) -> str:
     w("")
 
     # ------------------------------------------------------------- kernel
-    def group_ptrs(gi, indent):
+    def gptr_decls(gi, indent, restrict):
         g = groups[gi]
-        lines = [f"{v['ctype']}* const {v['ptr']} = ({v['ctype']}*)I.g[{gi}].var[{k}];"
+        r = " __restrict__" if restrict else ""
+        lines = [f"{v['ctype']}*{r} const {v['ptr']} = ({v['ctype']}*)s_gv[{gi}][{k}]; (void){v['ptr']};"
                  for k, v in enumerate(g["vars"])]
-        lines += [f"(void){v['ptr']};" for v in g["vars"]]
         return _indent("\n".join(lines), indent)
 
     def extra_ptrs(block_spec, indent):
@@ -204,8 +278,36 @@ def render_model(spec: dict) -> str:
         for ptr, (kind, obj, var) in sorted((block_spec or {}).get("extra_ptrs", {}).items()):
             if kind == "group":
                 v = groups[obj]["vars"][var]
-                lines.append(f"{v['ctype']}* const {ptr} = ({v['ctype']}*)I.g[{obj}].var[{var}]; (void){ptr};")
+                lines.append(f"{v['ctype']}* const {ptr} = ({v['ctype']}*)s_gv[{obj}][{var}]; (void){ptr};")
         return _indent("\n".join(lines), indent)
+
+    def reset_block(gi, indent, tsexpr):
+        """Reset of the spikes of step `tsexpr` in this CTA's tiles."""
+        tab, blocks = gtables[gi]
+        bd = dict(blocks)
+        if bd["reset"] is None:
+            return ""
+        g = groups[gi]
+        L = ["{",
+             f"  const int32_t* const scr = s_scr[{gi}]; const int32_t* const tcnt = s_tc[{gi}];",
+             f"  const int* const tst = s_tst + {gi} * max_tiles1;",
+             f"  const int32_t N = I.g[{gi}].N; (void)N;",
+             f"  const double* const _b200_S = s_Sg{gi}; const float* const _b200_Sf = s_Sg{gi}f; const long long* const _b200_Si = s_Sg{gi}i;",
+             gptr_decls(gi, 2, False),
+             f"  for (int u = s_ut[{gi}][0]; u < s_ut[{gi}][1]; ++u) {{",
+             "    const int cnt = tcnt[u], base = tst[u];",
+             "    for (int j = threadIdx.x; j < cnt; j += blockDim.x) {",
+             "      const int32_t _idx = scr[base + j];",
+             "      const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;",
+             "      {",
+             _indent(tab.device_loads("reset", f32), 8),
+             extra_ptrs(g.get("reset"), 8),
+             _indent(bd["reset"]["vector"], 8),
+             "      }",
+             "    }",
+             "  }",
+             "}"]
+        return _indent("\n".join(L), indent)
 
     w("__device__ __forceinline__ int b200_upper_bound(const int* a, int n, int x) {")
     w("  int lo = 0, hi = n;")
@@ -214,31 +316,46 @@ def render_model(spec: dict) -> str:
     w("}")
     w("")
     w(f"#define B200_NG {NG}")
-    w("static size_t b200_dyn_smem(int threads, int max_tiles1, int max_w) {")
-    w("  return (size_t)threads * 8 + (size_t)(threads + 1) * 4 + (size_t)threads * 4 +")
-    w("         (size_t)B200_NG * max_tiles1 * 4 + (size_t)(3 * max_w + 1) * 4 + 16;")
+    w(f"#define B200_MAXV {MAXV}")
+    w("// dynamic shared memory: [state cache | item seg | item off | item src | prefix | tile starts | delays]")
+    w("static size_t b200_dyn_smem(int threads, int max_tiles1, int max_w, int state_bytes) {")
+    w("  return (size_t)state_bytes + (size_t)threads * 8 + (size_t)(threads + 1) * 4 + (size_t)threads * 4 +")
+    w("         (size_t)2 * B200_NG * max_tiles1 * 4 + (size_t)(3 * max_w + 1) * 4 + 16;")
     w("}")
     w("")
     w("template <int MAXT>")
-    w("__global__ void __launch_bounds__(MAXT) b200_step_kernel(")
+    w("__global__ void __launch_bounds__(MAXT, 1) b200_step_kernel(")
     w("    const b200_inst_d* __restrict__ insts, const int2* __restrict__ cta_map, int n_inst,")
     w("    int queue_mode, int* work, int64_t max_steps, uint64_t limit_ns, int max_tiles1, int max_w,")
-    w("    int fault_rank) {")
+    w("    int fault_rank, int state_bytes, unsigned long long* __restrict__ prof, int cluster) {")
     w("  extern __shared__ __align__(16) unsigned char b200_dyn[];")
-    w("  int64_t* const s_item_seg = (int64_t*)b200_dyn;")
+    w("  unsigned char* const s_state = b200_dyn;")
+    w("  int64_t* const s_item_seg = (int64_t*)(b200_dyn + state_bytes);")
     w("  int* const s_item_off = (int*)(s_item_seg + blockDim.x);")
     w("  int* const s_item_src = s_item_off + blockDim.x + 1;")
     w("  int* const s_pref_all = s_item_src + blockDim.x;")
-    w("  int* const s_nd = s_pref_all + B200_NG * max_tiles1;")
+    w("  int* const s_tst = s_pref_all + B200_NG * max_tiles1;")
+    w("  int* const s_nd = s_tst + B200_NG * max_tiles1;")
     w("  int* const s_base = s_nd + max_w;")
     w("  int* const s_ndoff = s_base + max_w;")
     w("  __shared__ __align__(16) b200_inst_d I;")
     w("  __shared__ int s_wsum[B200_MAX_WARPS + 1];")
-    w("  __shared__ int s_unit, s_rank, s_flag;")
+    w("  __shared__ int s_cnt[B200_MAX_THREADS];")
+    w("  __shared__ int s_unit, s_rank, s_flag, s_cache;")
     w("  __shared__ long long s_mon_n[B200_MAX_SPKMON];")
     w("  __shared__ long long s_stm_n[B200_MAX_STATEMON];")
+    w("  __shared__ void* s_gv[B200_NG][B200_MAXV];")
+    w("  __shared__ int32_t* s_scr[B200_NG];")
+    w("  __shared__ int32_t* s_tc[B200_NG];")
+    w("  __shared__ int s_ut[B200_NG][2];")
+    for gi in range(NG):
+        n_ = max(gtables[gi][0].size, 1)
+        w(f"  __shared__ double s_Sg{gi}[{n_}]; __shared__ float s_Sg{gi}f[{n_}]; __shared__ long long s_Sg{gi}i[{n_}];")
+    for pi in range(NP):
+        n_ = max(ptables[pi][0].size, 1)
+        w(f"  __shared__ double s_Sp{pi}[{n_}]; __shared__ float s_Sp{pi}f[{n_}]; __shared__ long long s_Sp{pi}i[{n_}];")
     w("  unsigned gen = 0;")
-    w("  (void)s_nd; (void)s_base; (void)s_ndoff; (void)s_item_seg; (void)s_item_off; (void)s_item_src;")
+    w("  (void)s_nd; (void)s_base; (void)s_ndoff; (void)s_item_seg; (void)s_item_off; (void)s_item_src; (void)s_state;")
     w("  for (int pass = 0;; ++pass) {")
     w("    if (threadIdx.x == 0) {")
     w("      if (queue_mode) { s_unit = atomicAdd(work, 1); s_rank = 0; }")
@@ -254,12 +371,46 @@ def render_model(spec: dict) -> str:
     w("      for (int k = threadIdx.x; k < (int)(sizeof(b200_inst_d) / 8); k += blockDim.x) dst[k] = src[k];")
     w("    }")
     w("    __syncthreads();")
+    # pointer table and smem cache
     w("    if (threadIdx.x == 0) {")
     w("      gen = b200_ld_acquire(&I.bar[1]);")
     for m in range(len(spkmons)):
         w(f"      s_mon_n[{m}] = *((volatile long long*)I.sm[{m}].n);")
     for m in range(len(statemons)):
         w(f"      s_stm_n[{m}] = *((volatile long long*)I.stm[{m}].n);")
+    w("      const int cache = (I.n_cta == 1 && I.cache_bytes > 0 && I.cache_bytes <= state_bytes) ? 1 : 0;")
+    w("      s_cache = cache;")
+    w("      size_t off = 0;")
+    for gi, g in enumerate(groups):
+        for k in range(len(g["vars"])):
+            w(f"      s_gv[{gi}][{k}] = I.g[{gi}].var[{k}];")
+        w(f"      s_scr[{gi}] = I.g[{gi}].scratch; s_tc[{gi}] = I.g[{gi}].tile_cnt;")
+        w("      if (cache) {")
+        for k in USED[gi]:
+            sz = SIZE[g["vars"][k]["ctype"]]
+            w(f"        s_gv[{gi}][{k}] = s_state + off; off += ((size_t)I.g[{gi}].N * {sz} + 15) & ~(size_t)15;")
+        w(f"        s_scr[{gi}] = (int32_t*)(s_state + off); off += ((size_t)I.g[{gi}].N * 4 + 15) & ~(size_t)15;")
+        w(f"        s_tc[{gi}] = (int32_t*)(s_state + off); off += ((size_t)I.g[{gi}].n_tiles * 4 + 15) & ~(size_t)15;")
+        w("      }")
+        w(f"      s_ut[{gi}][0] = I.g[{gi}].cta_tile[rank]; s_ut[{gi}][1] = I.g[{gi}].cta_tile[rank + 1];")
+    w("    }")
+    w("    __syncthreads();")
+    for gi, g in enumerate(groups):
+        w(f"    for (int u = threadIdx.x; u <= I.g[{gi}].n_tiles; u += blockDim.x) s_tst[{gi} * max_tiles1 + u] = I.g[{gi}].tile_start[u];")
+    # loop-invariant scalars: one shared copy per CTA (all threads read the same words)
+    for gi in range(NG):
+        w(f"    for (int k = threadIdx.x; k < {gtables[gi][0].size}; k += blockDim.x) {{")
+        w(f"      const double x = I.g[{gi}].S[k]; s_Sg{gi}[k] = x; s_Sg{gi}f[k] = (float)x; s_Sg{gi}i[k] = (long long)x;")
+        w("    }")
+    for pi in range(NP):
+        w(f"    for (int k = threadIdx.x; k < {ptables[pi][0].size}; k += blockDim.x) {{")
+        w(f"      const double x = I.p[{pi}].S[k]; s_Sp{pi}[k] = x; s_Sp{pi}f[k] = (float)x; s_Sp{pi}i[k] = (long long)x;")
+        w("    }")
+    w("    if (s_cache) {  // state of a single-CTA instance lives in shared memory for the launch")
+    for gi, g in enumerate(groups):
+        for k in USED[gi]:
+            sz = SIZE[g["vars"][k]["ctype"]]
+            w(f"      b200_copy_bytes(s_gv[{gi}][{k}], I.g[{gi}].var[{k}], (size_t)I.g[{gi}].N * {sz});")
     w("    }")
     w("    __syncthreads();")
     w("    const int64_t ts0 = I.ts;")
@@ -267,6 +418,12 @@ def render_model(spec: dict) -> str:
     w("    const double _b200_dt = I.dt;")
     w("    int64_t ts = ts0;")
     w("    bool ok = true;")
+    w("    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, NW = blockDim.x >> 5;")
+    w(f"    // per-phase device profile (thread 0 of each CTA; phases: A, barrier A, spike lists,")
+    w(f"    // {NP} pathway(s), barrier B)")
+    w(f"    unsigned long long _pt = 0, _pacc[{4 + NP}];")
+    w(f"    for (int q = 0; q < {4 + NP}; ++q) _pacc[q] = 0;")
+    w("#define B200_PHASE(q) do { if (prof && threadIdx.x == 0) { const unsigned long long _c = clock64(); _pacc[q] += _c - _pt; _pt = _c; } } while (0)")
     w("    for (; ts < ts_stop; ++ts) {")
     w("      if (threadIdx.x == 0) {")
     w("        int st = 0;")
@@ -278,94 +435,106 @@ def render_model(spec: dict) -> str:
     w("      if (s_flag) break;")
     w("      const double _b200_t = (double)ts * _b200_dt;")
     w("      const int64_t _b200_ts = ts;")
-    w(f"      const double* const {clock['t']} = &_b200_t; (void){clock['t']};")
-    w(f"      const double* const {clock['dt']} = &_b200_dt; (void){clock['dt']};")
-    w(f"      const int64_t* const {clock['timestep']} = &_b200_ts; (void){clock['timestep']};")
+    w("      if (prof && threadIdx.x == 0) _pt = clock64();")
 
-    # ---- Phase A: per group reset(ts-1) -> state monitors -> update+threshold+compaction
+    # ---- Phase A
     for gi, g in enumerate(groups):
         tab, blocks = gtables[gi]
         bd = dict(blocks)
-        w(f"      // ---- group {gi} '{g['name']}': phase A")
-        w("      {")
-        w(f"        b200_group_d& GD = I.g[{gi}];")
-        w("        const int32_t N = GD.N; (void)N;")
-        w(f"        const double* const _b200_S = GD.S;")
-        w(group_ptrs(gi, 8))
-        w("        const int u0 = GD.cta_tile[rank], u1 = GD.cta_tile[rank + 1];")
+        w(f"      // ---- group {gi} '{g['name']}': phase A (reset of step ts-1, monitors, update + threshold)")
         if bd["reset"] is not None:
-            w("        if (ts > ts0) {")
-            w("          for (int u = u0; u < u1; ++u) {")
-            w("            const int cnt = GD.tile_cnt[u], base = GD.tile_start[u];")
-            w("            for (int j = threadIdx.x; j < cnt; j += blockDim.x) {")
-            w("              const int32_t _idx = GD.scratch[base + j];")
-            w("              const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
-            w("              {")
-            w(_indent(tab.device_loads("reset"), 16))
-            w(extra_ptrs(g.get("reset"), 16))
-            w(_indent(bd["reset"]["vector"], 16))
-            w("              }")
-            w("            }")
-            w("          }")
-            w("          __syncthreads();")
-            w("        }")
+            w("      if (ts > ts0) {")
+            w(reset_block(gi, 8, "ts - 1"))
+            w("        __syncthreads();")
+            w("      }")
+        w("      {")
+        w(f"        const int32_t N = I.g[{gi}].N; (void)N;")
+        w(f"        const double* const _b200_S = s_Sg{gi}; const float* const _b200_Sf = s_Sg{gi}f; const long long* const _b200_Si = s_Sg{gi}i;")
+        w(gptr_decls(gi, 8, True))
+        w(f"        int32_t* const scr = s_scr[{gi}]; int32_t* const tcnt = s_tc[{gi}];")
+        w(f"        const int* const tst = s_tst + {gi} * max_tiles1;")
         for mi, m in enumerate(statemons):
             if m["group"] != gi:
                 continue
-            w(f"        {{  // state monitor {mi}")
+            w(f"        {{  // state monitor {mi}: values at the start of the step")
             w(f"          const b200_statemon_d& SM = I.stm[{mi}];")
-            w("          const int lo = GD.tile_start[GD.cta_tile[rank]], hi = GD.tile_start[GD.cta_tile[rank + 1]];")
+            w(f"          const int lo = tst[s_ut[{gi}][0]], hi = tst[s_ut[{gi}][1]];")
             w("          double* const row = SM.data + (size_t)(ts - SM.step0) * SM.n_vars * SM.n_rec;")
             w("          for (int k = threadIdx.x; k < SM.n_rec * SM.n_vars; k += blockDim.x) {")
             w("            const int r = k % SM.n_rec, v = k / SM.n_rec;")
             w("            const int idx = SM.idx[r];")
             w("            if (idx >= lo && idx < hi) {")
-            w("              const void* base = GD.var[SM.var_id[v]];")
-            w("              row[k] = SM.var_dbl[v] ? ((const double*)base)[idx] : (double)((const float*)base)[idx];")
+            w("              double val = 0.0;")
+            w("              switch (SM.var_id[v]) {")
+            for k, v in enumerate(g["vars"]):
+                w(f"                case {k}: val = (double)(({v['ctype']}*)s_gv[{gi}][{k}])[idx]; break;")
+            w("              }")
+            w("              row[k] = val;")
             w("            }")
             w("          }")
             w(f"          if (threadIdx.x == 0) s_stm_n[{mi}] = ts + 1 - SM.step0;")
             w("        }")
-        w("        for (int u = u0; u < u1; ++u) {")
-        w("          const int start = GD.tile_start[u], end = GD.tile_start[u + 1];")
+        w(f"        for (int u = s_ut[{gi}][0]; u < s_ut[{gi}][1]; ++u) {{")
+        w("          const int start = tst[u], end = tst[u + 1];")
         w("          int cnt = 0;")
-        w("          for (int tb = start; tb < end; tb += blockDim.x) {")
-        w("            const int32_t _idx = tb + threadIdx.x;")
-        w("            bool _b200_spk = false;")
-        w("            if (_idx < end) {")
-        w("              const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+        w("          for (int pb = start; pb < end; pb += 32 * (int)blockDim.x) {")
+        w("            const int pe = (end - pb < 32 * (int)blockDim.x) ? end : pb + 32 * (int)blockDim.x;")
+        w("            const int E = (pe - pb + blockDim.x - 1) / blockDim.x;")
+        w("            unsigned flags = 0u;")
+        w("#pragma unroll 4")
+        w("            for (int k = 0; k < E; ++k) {")
+        w("              const int32_t _idx = pb + k * (int)blockDim.x + threadIdx.x;")
+        w("              if (_idx < pe) {")
+        w("                const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
         if bd["update"] is not None:
-            w("              {")
-            w(_indent(tab.device_loads("update"), 16))
-            w(extra_ptrs(g.get("update"), 16))
-            w(_indent(bd["update"]["vector"], 16))
-            w("              }")
+            w("                {")
+            w(_indent(tab.device_loads("update", f32), 18))
+            w(extra_ptrs(g.get("update"), 18))
+            w(_indent(bd["update"]["vector"], 18))
+            w("                }")
         if bd["threshold"] is not None:
-            w("              {")
-            w(_indent(tab.device_loads("threshold"), 16))
-            w(extra_ptrs(g.get("threshold"), 16))
-            w(_indent(bd["threshold"]["vector"], 16))
-            w("                _b200_spk = _cond;")
+            w("                {")
+            w(_indent(tab.device_loads("threshold", f32), 18))
+            w(extra_ptrs(g.get("threshold"), 18))
+            w(_indent(bd["threshold"]["vector"], 18))
+            w("                  if (_cond) flags |= 1u << k;")
             if bd["threshold"].get("refractory"):
                 nr = next(v["ptr"] for v in g["vars"] if v["name"] == "not_refractory")
                 ls = next(v["ptr"] for v in g["vars"] if v["name"] == "lastspike")
-                w("                if (_cond) {")
-                w(f"                  {nr}[_idx] = false;")
-                w(f"                  {ls}[_idx] = _b200_t;")
-                w("                }")
-            w("              }")
+                w("                  if (_cond) {")
+                w(f"                    {nr}[_idx] = false;")
+                w(f"                    {ls}[_idx] = _b200_t;")
+                w("                  }")
+            w("                }")
+        w("              }")
         w("            }")
+        w("            // order-preserving compaction: counts per (slice k, warp), one block scan")
+        w("            for (int k = 0; k < E; ++k) {")
+        w("              const unsigned m = __ballot_sync(0xffffffffu, (flags >> k) & 1u);")
+        w("              if (lane == 0) s_cnt[k * NW + wid] = __popc(m);")
+        w("            }")
+        w("            __syncthreads();")
         w("            int tot;")
-        w("            const int pos = b200_block_compact(_b200_spk, s_wsum, &tot);")
-        w("            if (_b200_spk) GD.scratch[start + cnt + pos] = _idx;")
+        w("            const int x = (int)threadIdx.x < E * NW ? s_cnt[threadIdx.x] : 0;")
+        w("            const int ex = b200_block_exscan(x, s_wsum, &tot);")
+        w("            if ((int)threadIdx.x < E * NW) s_cnt[threadIdx.x] = ex;")
+        w("            __syncthreads();")
+        w("            for (int k = 0; k < E; ++k) {")
+        w("              const unsigned m = __ballot_sync(0xffffffffu, (flags >> k) & 1u);")
+        w("              if ((flags >> k) & 1u)")
+        w("                scr[start + cnt + s_cnt[k * NW + wid] + __popc(m & b200_lanemask_lt())] = pb + k * (int)blockDim.x + threadIdx.x;")
+        w("            }")
         w("            cnt += tot;")
+        w("            __syncthreads();")
         w("          }")
-        w("          if (threadIdx.x == 0) GD.tile_cnt[u] = cnt;")
+        w("          if (threadIdx.x == 0) tcnt[u] = cnt;")
         w("        }")
         w("      }")
+    w("      B200_PHASE(0);")
     w("      // test hook: CTA `fault_rank` leaves without arriving, the others must time out")
     w("      if (rank == fault_rank && ts == ts0) { ok = false; break; }")
-    w("      if (!b200_inst_barrier(I, gen, limit_ns)) { ok = false; break; }")
+    w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster)) { ok = false; break; }")
+    w("      B200_PHASE(1);")
 
     # ---- Phase B: prefix of tile counts, ring, monitors
     for gi, g in enumerate(groups):
@@ -373,11 +542,13 @@ def render_model(spec: dict) -> str:
         w("      {")
         w(f"        b200_group_d& GD = I.g[{gi}];")
         w(f"        int* const pref = s_pref_all + {gi} * max_tiles1;")
+        w(f"        const int* const tst = s_tst + {gi} * max_tiles1;")
+        w(f"        const int32_t* const scr = s_scr[{gi}]; const int32_t* const tcnt = s_tc[{gi}];")
         w("        const int nt = GD.n_tiles;")
         w("        int carry = 0;")
         w("        for (int c0 = 0; c0 < nt; c0 += blockDim.x) {")
         w("          const int u = c0 + threadIdx.x;")
-        w("          const int x = u < nt ? GD.tile_cnt[u] : 0;")
+        w("          const int x = u < nt ? tcnt[u] : 0;")
         w("          int tot;")
         w("          const int ex = b200_block_exscan(x, s_wsum, &tot);")
         w("          if (u < nt) pref[u] = carry + ex;")
@@ -385,13 +556,13 @@ def render_model(spec: dict) -> str:
         w("        }")
         w("        if (threadIdx.x == 0) pref[nt] = carry;")
         w("        __syncthreads();")
-        w("        const int u0 = GD.cta_tile[rank], u1 = GD.cta_tile[rank + 1];")
+        w(f"        const int u0 = s_ut[{gi}][0], u1 = s_ut[{gi}][1];")
         w("        if (GD.R > 1) {")
         w("          const int slot = (int)(ts % GD.R);")
         w("          int32_t* const ring = GD.ring + (int64_t)slot * GD.N;")
         w("          for (int u = u0; u < u1; ++u) {")
-        w("            const int cnt = pref[u + 1] - pref[u], base = GD.tile_start[u];")
-        w("            for (int j = threadIdx.x; j < cnt; j += blockDim.x) ring[pref[u] + j] = GD.scratch[base + j];")
+        w("            const int cnt = pref[u + 1] - pref[u], base = tst[u];")
+        w("            for (int j = threadIdx.x; j < cnt; j += blockDim.x) ring[pref[u] + j] = scr[base + j];")
         w("          }")
         w("          if (rank == 0) {")
         w("            for (int u = threadIdx.x; u <= nt; u += blockDim.x) GD.ring_prefix[(int64_t)slot * (nt + 1) + u] = pref[u];")
@@ -406,9 +577,9 @@ def render_model(spec: dict) -> str:
             w(f"          const long long mbase = s_mon_n[{mi}] - pref[SM.tile_lo];")
             w("          const int a = u0 > SM.tile_lo ? u0 : SM.tile_lo, b = u1 < SM.tile_hi ? u1 : SM.tile_hi;")
             w("          for (int u = a; u < b; ++u) {")
-            w("            const int cnt = pref[u + 1] - pref[u], base = GD.tile_start[u];")
+            w("            const int cnt = pref[u + 1] - pref[u], base = tst[u];")
             w("            for (int j = threadIdx.x; j < cnt; j += blockDim.x) {")
-            w("              const int idx = GD.scratch[base + j];")
+            w("              const int idx = scr[base + j];")
             w("              const long long pos = mbase + pref[u] + j;")
             w("              SM.i[pos] = idx - SM.lo;")
             w("              SM.ts[pos] = (int32_t)ts;")
@@ -427,6 +598,7 @@ def render_model(spec: dict) -> str:
             w("        }")
         w("      }")
 
+    w("      B200_PHASE(2);")
     # ---- Phase B: synaptic propagation
     for pi, p in enumerate(paths):
         tab, blocks = ptables[pi]
@@ -437,6 +609,8 @@ def render_model(spec: dict) -> str:
         w(f"        const b200_pathway_d& PD = I.p[{pi}];")
         w(f"        const b200_group_d& SGD = I.g[{sg}];")
         w(f"        const int* const pref = s_pref_all + {sg} * max_tiles1;")
+        w(f"        const int* const tst = s_tst + {sg} * max_tiles1;")
+        w(f"        const int32_t* const scr = s_scr[{sg}];")
         w("        const int W = PD.D - PD.dmin + 1;")
         w("        for (int k = threadIdx.x; k < W; k += blockDim.x) {")
         w("          const int d = PD.dmin + k;")
@@ -468,14 +642,14 @@ def render_model(spec: dict) -> str:
         w("        const int Wtot = s_ndoff[W];")
         w("        const int i0 = (int)((int64_t)Wtot * rank / I.n_cta);")
         w("        const int i1 = (int)((int64_t)Wtot * (rank + 1) / I.n_cta);")
-        w(f"        const double* const _b200_S = PD.S;")
+        w(f"        const double* const _b200_S = s_Sp{pi}; const float* const _b200_Sf = s_Sp{pi}f; const long long* const _b200_Si = s_Sp{pi}i;")
         for k, v in enumerate(p.get("vars", [])):
-            w(f"        {v['ctype']}* const {v['ptr']} = ({v['ctype']}*)PD.var[{k}]; (void){v['ptr']};")
-        w(f"        const int32_t* const {p['post_ptr']} = PD.post; (void){p['post_ptr']};")
-        w(f"        const int32_t* const {p['pre_ptr']} = PD.pre; (void){p['pre_ptr']};")
+            w(f"        {v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)PD.var[{k}]; (void){v['ptr']};")
+        w(f"        const int32_t* __restrict__ const {p['post_ptr']} = PD.post; (void){p['post_ptr']};")
+        w(f"        const int32_t* __restrict__ const {p['pre_ptr']} = PD.pre; (void){p['pre_ptr']};")
         for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
             v = groups[gidx]["vars"][vidx]
-            w(f"        {v['ctype']}* const {ptr} = ({v['ctype']}*)I.g[{gidx}].var[{vidx}]; (void){ptr};")
+            w(f"        {v['ctype']}* __restrict__ const {ptr} = ({v['ctype']}*)s_gv[{gidx}][{vidx}]; (void){ptr};")
         w("        for (int cb = i0; cb < i1; cb += blockDim.x) {")
         w("          const int it = cb + threadIdx.x;")
         w("          int len = 0;")
@@ -486,7 +660,7 @@ def render_model(spec: dict) -> str:
         w("            if (d == 0) {")
         w("              const int pos = s_base[k] + r;")
         w("              const int u = b200_upper_bound(pref, SGD.n_tiles + 1, pos) - 1;")
-        w("              src = SGD.scratch[SGD.tile_start[u] + pos - pref[u]];")
+        w("              src = scr[tst[u] + pos - pref[u]];")
         w("            } else {")
         w("              src = SGD.ring[(int64_t)((ts - d) % SGD.R) * SGD.N + s_base[k] + r];")
         w("            }")
@@ -501,55 +675,49 @@ def render_model(spec: dict) -> str:
         w("          s_item_off[threadIdx.x] = off;")
         w("          __syncthreads();")
         w("          const int nitems = (i1 - cb) < (int)blockDim.x ? (i1 - cb) : (int)blockDim.x;")
-        w("          for (int e = threadIdx.x; e < E; e += blockDim.x) {")
-        w("            const int j = b200_upper_bound(s_item_off, nitems, e) - 1;")
-        w("            const int64_t _idx = s_item_seg[j] + (e - s_item_off[j]);")
-        w("            const int32_t _b200_pre = s_item_src[j]; (void)_b200_pre;")
-        w("            const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
-        w("            {")
-        w(_indent(tab.device_loads("on_pre"), 14))
-        w(_indent(blk["vector_device"] if blk.get("vector_device") else blk["vector"], 14))
+        w("          for (int e0 = threadIdx.x; e0 < E; e0 += 4 * (int)blockDim.x) {")
+        w("#pragma unroll")
+        w("            for (int q = 0; q < 4; ++q) {")
+        w("              const int e = e0 + q * (int)blockDim.x;")
+        w("              if (e < E) {")
+        w("                const int j = b200_upper_bound(s_item_off, nitems, e) - 1;")
+        w("                const int64_t _idx = s_item_seg[j] + (e - s_item_off[j]);")
+        w("                const int32_t _b200_pre = s_item_src[j]; (void)_b200_pre;")
+        w("                const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+        w("                {")
+        w(_indent(tab.device_loads("on_pre", f32), 18))
+        w(_indent(blk["vector_device"] if blk.get("vector_device") else blk["vector"], 18))
+        w("                }")
+        w("              }")
         w("            }")
         w("          }")
         w("          __syncthreads();")
         w("        }")
         w("      }")
-    w("      if (!b200_inst_barrier(I, gen, limit_ns)) { ok = false; break; }")
+        w(f"      B200_PHASE({3 + pi});")
+    w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster)) { ok = false; break; }")
+    w(f"      B200_PHASE({3 + NP});")
     w("    }  // steps")
+    w(f"    if (prof && threadIdx.x == 0)")
+    w(f"      for (int q = 0; q < {4 + NP}; ++q) atomicAdd(&prof[(size_t)unit * {4 + NP} + q], _pacc[q]);")
+    w("#undef B200_PHASE")
 
-    # ---- end of launch: apply the reset of the last executed step
+    # ---- end of launch: apply the reset of the last executed step, write back the cache
     w("    if (ok && ts > ts0) {")
     w("      const double _b200_t = (double)(ts - 1) * _b200_dt; (void)_b200_t;")
     w("      const int64_t _b200_ts = ts - 1;")
-    w(f"      const double* const {clock['t']} = &_b200_t; (void){clock['t']};")
-    w(f"      const double* const {clock['dt']} = &_b200_dt; (void){clock['dt']};")
-    w(f"      const int64_t* const {clock['timestep']} = &_b200_ts; (void){clock['timestep']};")
-    for gi, g in enumerate(groups):
-        tab, blocks = gtables[gi]
-        bd = dict(blocks)
-        if bd["reset"] is None:
-            continue
-        w("      {")
-        w(f"        b200_group_d& GD = I.g[{gi}];")
-        w("        const int32_t N = GD.N; (void)N;")
-        w(f"        const double* const _b200_S = GD.S;")
-        w(group_ptrs(gi, 8))
-        w("        const int u0 = GD.cta_tile[rank], u1 = GD.cta_tile[rank + 1];")
-        w("        for (int u = u0; u < u1; ++u) {")
-        w("          const int cnt = GD.tile_cnt[u], base = GD.tile_start[u];")
-        w("          for (int j = threadIdx.x; j < cnt; j += blockDim.x) {")
-        w("            const int32_t _idx = GD.scratch[base + j];")
-        w("            const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
-        w("            {")
-        w(_indent(tab.device_loads("reset"), 14))
-        w(extra_ptrs(g.get("reset"), 14))
-        w(_indent(bd["reset"]["vector"], 14))
-        w("            }")
-        w("          }")
-        w("        }")
-        w("      }")
+    for gi in range(NG):
+        rb = reset_block(gi, 6, "ts - 1")
+        if rb:
+            w(rb)
     w("    }")
     w("    __syncthreads();")
+    w("    if (s_cache) {")
+    for gi, g in enumerate(groups):
+        for k in USED[gi]:
+            sz = SIZE[g["vars"][k]["ctype"]]
+            w(f"      b200_copy_bytes(I.g[{gi}].var[{k}], s_gv[{gi}][{k}], (size_t)I.g[{gi}].N * {sz});")
+    w("    }")
     w("    if (threadIdx.x == 0 && rank == 0) {")
     w("      *I.ts_done = ts;")
     for m in range(len(spkmons)):
@@ -564,33 +732,71 @@ def render_model(spec: dict) -> str:
 
     # ------------------------------------------------------------- launch glue
     w("static const void* b200_kernel_for(int threads) {")
-    w("  return threads <= 256 ? (const void*)b200_step_kernel<256> : (const void*)b200_step_kernel<1024>;")
+    w("  if (threads <= 256) return (const void*)b200_step_kernel<256>;")
+    w("  if (threads <= 512) return (const void*)b200_step_kernel<512>;")
+    w("  return (const void*)b200_step_kernel<1024>;")
     w("}")
-    w("static int b200_max_active(int threads, int max_tiles1, int max_w) {")
+    w("static int b200_max_active(int threads, int max_tiles1, int max_w, int state_bytes) {")
     w("  const void* k = b200_kernel_for(threads);")
-    w("  const size_t smem = b200_dyn_smem(threads, max_tiles1, max_w);")
-    w("  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);")
+    w("  const size_t smem = b200_dyn_smem(threads, max_tiles1, max_w, state_bytes);")
+    w("  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;")
     w("  int n = 0;")
     w("  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads, smem) != cudaSuccess) return 0;")
     w("  return n;")
     w("}")
+    w("static int b200_static_smem(int threads) {")
+    w("  cudaFuncAttributes a;")
+    w("  if (cudaFuncGetAttributes(&a, b200_kernel_for(threads)) != cudaSuccess) return 64 * 1024;")
+    w("  return (int)a.sharedSizeBytes;")
+    w("}")
     w("static cudaError_t b200_launch(b200_inst_d* insts, const int2* cta_map, int n_inst, int queue_mode,")
     w("                               int* work, int64_t max_steps, uint64_t limit_ns, int grid, int threads,")
-    w("                               int cooperative, int max_tiles1, int max_w, int fault_rank, cudaStream_t s) {")
+    w("                               int cooperative, int max_tiles1, int max_w, int fault_rank, int state_bytes,")
+    w("                               unsigned long long* prof, int cluster, cudaStream_t s) {")
     w("  const void* k = b200_kernel_for(threads);")
-    w("  const size_t smem = b200_dyn_smem(threads, max_tiles1, max_w);")
+    w("  const size_t smem = b200_dyn_smem(threads, max_tiles1, max_w, state_bytes);")
     w("  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);")
     w("  if (e != cudaSuccess) return e;")
     w("  const b200_inst_d* ci = insts;")
     w("  void* args[] = {(void*)&ci, (void*)&cta_map, (void*)&n_inst, (void*)&queue_mode, (void*)&work,")
-    w("                  (void*)&max_steps, (void*)&limit_ns, (void*)&max_tiles1, (void*)&max_w, (void*)&fault_rank};")
+    w("                  (void*)&max_steps, (void*)&limit_ns, (void*)&max_tiles1, (void*)&max_w, (void*)&fault_rank,")
+    w("                  (void*)&state_bytes, (void*)&prof, (void*)&cluster};")
+    w("  if (cluster > 1) {  // one thread-block cluster per instance")
+    w("    if (cluster > 8) {")
+    w("      e = cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);")
+    w("      if (e != cudaSuccess) return e;")
+    w("    }")
+    w("    cudaLaunchConfig_t cfg = {};")
+    w("    cfg.gridDim = dim3(grid); cfg.blockDim = dim3(threads); cfg.dynamicSmemBytes = smem; cfg.stream = s;")
+    w("    cudaLaunchAttribute at[1];")
+    w("    at[0].id = cudaLaunchAttributeClusterDimension;")
+    w("    at[0].val.clusterDim.x = cluster; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;")
+    w("    cfg.attrs = at; cfg.numAttrs = 1;")
+    w("    return cudaLaunchKernelExC(&cfg, k, args);")
+    w("  }")
     w("  if (cooperative) return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(threads), args, smem, s);")
     w("  return cudaLaunchKernel(k, dim3(grid), dim3(threads), args, smem, s);")
+    w("}")
+    w("static int b200_max_cluster(int threads, int max_tiles1, int max_w, int state_bytes, int cluster) {")
+    w("  const void* k = b200_kernel_for(threads);")
+    w("  const size_t smem = b200_dyn_smem(threads, max_tiles1, max_w, state_bytes);")
+    w("  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;")
+    w("  if (cluster > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return 0;")
+    w("  cudaLaunchConfig_t cfg = {};")
+    w("  cfg.gridDim = dim3(cluster); cfg.blockDim = dim3(threads); cfg.dynamicSmemBytes = smem;")
+    w("  cudaLaunchAttribute at[1];")
+    w("  at[0].id = cudaLaunchAttributeClusterDimension;")
+    w("  at[0].val.clusterDim.x = cluster; at[0].val.clusterDim.y = 1; at[0].val.clusterDim.z = 1;")
+    w("  cfg.attrs = at; cfg.numAttrs = 1;")
+    w("  int n = 0;")
+    w("  if (cudaOccupancyMaxPotentialClusterSize(&n, k, &cfg) != cudaSuccess) return 0;")
+    w("  return n;")
     w("}")
     w("")
     w(f'static const b200_model_info B200_MODEL = {{"{spec["name"]}", {NG}, {NP}, {len(spkmons)}, {len(ratemons)}, {len(statemons)},')
     w("  b200_groups, b200_pathways, b200_spkmon, b200_ratemon, b200_statemon,")
-    w(f"  {len(consts)}, b200_const_names, b200_const_defaults, b200_eval_scalars, b200_launch, b200_max_active}};")
+    w(f"  {len(consts)}, b200_const_names, b200_const_defaults, b200_eval_scalars, b200_launch, b200_max_active,")
+    w(f"  b200_static_smem, b200_max_cluster, {4 + NP}}};")
     w("")
     w('#include "b200_host.h"')
     w("")

@@ -85,6 +85,8 @@ struct b200_statemon_d {
 
 struct b200_inst_d {
   int32_t cta0, n_cta;    // CTAs [cta0, cta0+n_cta) of the grid run this instance
+  int32_t cache_bytes;    // >0: single-CTA instance whose state is cached in shared memory
+  int32_t _pad0;
   int64_t ts;             // next time step to execute
   int64_t ts_end;         // stop before this step
   double dt;
@@ -122,6 +124,7 @@ struct b200_group_info {
   const char* const* var_names;
   const int* var_kind;
   int n_scalars;  // size of the scalar table
+  const int* var_used;  // 1 if the step code touches the variable
 };
 struct b200_pathway_info {
   const char* name;
@@ -151,8 +154,12 @@ struct b200_model_info {
   // launches the step kernel
   cudaError_t (*launch)(b200_inst_d* insts, const int2* cta_map, int n_inst, int queue_mode,
                         int* work, int64_t max_steps, uint64_t limit_ns, int grid, int threads,
-                        int cooperative, int max_tiles1, int max_w, int fault_rank, cudaStream_t s);
-  int (*max_active_ctas)(int threads, int max_tiles1, int max_w);
+                        int cooperative, int max_tiles1, int max_w, int fault_rank, int state_bytes,
+                        unsigned long long* prof, int cluster, cudaStream_t s);
+  int (*max_active_ctas)(int threads, int max_tiles1, int max_w, int state_bytes);
+  int (*static_smem)(int threads);
+  int (*max_cluster)(int threads, int max_tiles1, int max_w, int state_bytes, int cluster);
+  int n_phases;  // device profile: A, barrier A, spike lists, one per pathway, barrier B
 };
 
 
@@ -240,12 +247,38 @@ __device__ __forceinline__ int b200_block_compact(bool flag, int* wsum, int* tot
   return r;
 }
 
+// Block-cooperative copy of `bytes` (the arrays are 16-byte aligned in shared
+// memory and at least 4-byte aligned in global memory).
+__device__ __forceinline__ void b200_copy_bytes(void* dst, const void* src, size_t bytes) {
+  const size_t nw = bytes / 4;
+  uint32_t* d = (uint32_t*)dst;
+  const uint32_t* s = (const uint32_t*)src;
+  for (size_t k = threadIdx.x; k < nw; k += blockDim.x) d[k] = s[k];
+  unsigned char* db = (unsigned char*)dst;
+  const unsigned char* sb = (const unsigned char*)src;
+  for (size_t k = nw * 4 + threadIdx.x; k < bytes; k += blockDim.x) db[k] = sb[k];
+}
+
+// Hardware barrier over the CTAs of a thread-block cluster (one instance per
+// cluster).  Release/acquire at cluster scope also orders the global-memory
+// accesses made before it.  Every CTA of the cluster executes the same
+// sequence of these barriers (the step loop's control flow is uniform).
+__device__ __forceinline__ void b200_cluster_sync() {
+  asm volatile(
+      "barrier.cluster.arrive.release.aligned;\n"
+      "barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
 // Barrier over the n_cta CTAs of one instance.  Bounded: after `limit_ns` of
 // waiting the instance status is set to B200_ERR_BARRIER_TIMEOUT and the call
 // returns false, so a kernel never spins forever.  With n_cta == 1 it is a
 // plain __syncthreads.  `gen` is the CTA's private copy of the generation.
 __device__ __forceinline__ bool b200_inst_barrier(const b200_inst_d& I, unsigned& gen,
-                                                  uint64_t limit_ns) {
+                                                  uint64_t limit_ns, int cluster) {
+  if (cluster) {
+    b200_cluster_sync();
+    return true;
+  }
   __syncthreads();
   if (I.n_cta == 1) return true;
   __shared__ int ok;

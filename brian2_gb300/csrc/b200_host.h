@@ -82,6 +82,12 @@ struct b200_net {
   cudaStream_t stream = nullptr;
   int threads = 256;
   int max_tiles1 = 2, max_w = 1;  // dynamic shared-memory extents
+  int state_bytes = 0;            // shared-memory state cache per CTA (0: none)
+  bool smem_cache = true;         // cache the state of single-CTA instances
+  bool profiling = false;         // per-phase clock64 profile of the step kernel
+  bool use_clusters = true;       // instances of 2..16 CTAs run as thread-block clusters
+  int cluster = 0;                // cluster size of the current launch plan (0: none)
+  b200_dbuf prof;
   int queue_mode = 0;      // 1: single-CTA instances pulled from a work queue
   int grid = 0;
   int64_t chunk_steps = 100000;
@@ -93,6 +99,7 @@ struct b200_net {
   int64_t graph_steps = -1;
   int64_t launches = 0;
   double last_run_ms = 0.0;
+  double last_kernel_ms = 0.0;  // kernel launches only (CUDA events around them)
   std::string err;
   size_t device_bytes = 0;
 };
@@ -215,7 +222,7 @@ int b200_destroy(b200_net* n) {
     for (auto& S : I.stm) { b200_free(n, S.d_idx); b200_free(n, S.n); b200_free(n, S.data); }
     b200_free(n, I.bar); b200_free(n, I.status); b200_free(n, I.ts_done); b200_free(n, I.pending);
   }
-  b200_free(n, n->d_insts); b200_free(n, n->d_cta_map); b200_free(n, n->d_work);
+  b200_free(n, n->d_insts); b200_free(n, n->d_cta_map); b200_free(n, n->d_work); b200_free(n, n->prof);
   if (n->stream) cudaStreamDestroy(n->stream);
   delete n;
   return 0;
@@ -677,13 +684,52 @@ static int b200_prepare(b200_net* n) {
     for (int p = 0; p < M->n_pathways; ++p)
       n->max_w = std::max(n->max_w, n->inst[k].p[p].dmax - n->inst[k].p[p].dmin + 1);
   }
-  int max_per_sm = M->max_active_ctas(n->threads, n->max_tiles1, n->max_w);
+  // shared-memory state cache of single-CTA instances: the used state
+  // variables, the step's spike list and the tile counts
+  {
+    int dev = 0, optin = 0;
+    B200_CU(n, cudaGetDevice(&dev));
+    B200_CU(n, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const long other = (long)M->static_smem(n->threads) +
+                       (long)(n->threads * 16 + 2 * M->n_groups * n->max_tiles1 * 4 + (3 * n->max_w + 1) * 4 + 64);
+    const long budget = (long)optin - other - 1024;
+    n->state_bytes = 0;
+    for (int k = 0; k < n->n_inst; ++k) {
+      b200_inst_h& I = n->inst[k];
+      long bytes = 0;
+      if (n->smem_cache && I.n_cta == 1) {
+        for (int g = 0; g < M->n_groups; ++g) {
+          const long Ng = I.g[g].N;
+          for (int v = 0; v < M->groups[g].n_vars; ++v)
+            if (M->groups[g].var_used[v]) bytes += (Ng * (long)b200_kind_size(M->groups[g].var_kind[v]) + 15) & ~15L;
+          bytes += (Ng * 4 + 15) & ~15L;
+          bytes += ((long)(I.g[g].tile_start.size() - 1) * 4 + 15) & ~15L;
+        }
+        if (bytes > budget) bytes = 0;
+      }
+      n->h_insts[k].cache_bytes = (int32_t)bytes;
+      n->state_bytes = std::max<long>(n->state_bytes, bytes);
+    }
+  }
+  int max_per_sm = M->max_active_ctas(n->threads, n->max_tiles1, n->max_w, n->state_bytes);
   int dev = 0, n_sm = 0;
   B200_CU(n, cudaGetDevice(&dev));
   B200_CU(n, cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
   const int resident = std::max(1, max_per_sm) * n_sm;
+  // thread-block clusters: every instance has the same CTA count C in 2..16
+  n->cluster = 0;
+  if (!n->queue_mode && n->use_clusters && n->fault_rank < 0) {
+    int C = n->inst[0].n_cta;
+    bool same = true;
+    for (int k = 1; k < n->n_inst; ++k) same = same && n->inst[k].n_cta == C;
+    if (same && C >= 2 && C <= 16 &&
+        M->max_cluster(n->threads, n->max_tiles1, n->max_w, n->state_bytes, C) >= C)
+      n->cluster = C;
+  }
   if (n->queue_mode) {
     n->grid = std::min(n->n_inst, resident);
+  } else if (n->cluster) {
+    n->grid = cta;  // independent clusters: no co-residency of the whole grid needed
   } else {
     n->grid = cta;
     if (cta > resident)
@@ -785,7 +831,11 @@ int b200_run(b200_net* n, int64_t n_steps) {
   B200_CU(n, cudaEventCreate(&e0));
   B200_CU(n, cudaEventCreate(&e1));
   B200_CU(n, cudaEventRecord(e0, n->stream));
-  const int coop = (!n->queue_mode) ? 1 : 0;
+  const int coop = (!n->queue_mode && !n->cluster) ? 1 : 0;
+  cudaEvent_t k0, k1;
+  B200_CU(n, cudaEventCreate(&k0));
+  B200_CU(n, cudaEventCreate(&k1));
+  double kernel_ms = 0.0;
   for (int guard = 0; guard < 1 << 20; ++guard) {
     bool any = false;
     for (int k = 0; k < n->n_inst; ++k) {
@@ -811,13 +861,26 @@ int b200_run(b200_net* n, int64_t n_steps) {
                                cudaMemcpyHostToDevice, n->stream));
     B200_CU(n, cudaMemsetAsync(n->d_work.p, 0, 16, n->stream));
     const int64_t steps = n->chunk_steps;
+
+    B200_CU(n, cudaEventRecord(k0, n->stream));
     cudaError_t le = M->launch((b200_inst_d*)n->d_insts.p, (const int2*)n->d_cta_map.p, n->n_inst,
                                n->queue_mode, (int*)n->d_work.p, steps, n->limit_ns, n->grid,
-                               n->threads, coop, n->max_tiles1, n->max_w, n->fault_rank, n->stream);
-    n->fault_rank = -1;  // one-shot
+                               n->threads, coop, n->max_tiles1, n->max_w, n->fault_rank, n->state_bytes,
+                               n->profiling ? (unsigned long long*)n->prof.p : nullptr,
+                               n->cluster, n->stream);
+    if (n->fault_rank >= 0) {  // one-shot; the next launch may use clusters again
+      n->fault_rank = -1;
+      n->prepared = false;
+    }
     if (le != cudaSuccess) return b200_fail(n, B200_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(le));
     ++n->launches;
+    B200_CU(n, cudaEventRecord(k1, n->stream));
     B200_CU(n, cudaStreamSynchronize(n->stream));
+    {
+      float kms = 0.f;
+      cudaEventElapsedTime(&kms, k0, k1);
+      kernel_ms += kms;
+    }
     for (int k = 0; k < n->n_inst; ++k) {
       b200_inst_h& I = n->inst[k];
       int32_t st = 0;
@@ -842,8 +905,67 @@ int b200_run(b200_net* n, int64_t n_steps) {
   float ms = 0;
   cudaEventElapsedTime(&ms, e0, e1);
   n->last_run_ms = ms;
+  n->last_kernel_ms = kernel_ms;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  cudaEventDestroy(k0);
+  cudaEventDestroy(k1);
+  return 0;
+}
+
+// Device profile of the step kernel: per instance and phase, SM clock cycles
+// summed over the instance's CTAs and steps (phases: 0 update/threshold/reset,
+// 1 barrier after it, 2 spike lists and monitors, 3.. one per pathway, last the
+// barrier after propagation).  The reference's analogue is run(profile=True)
+// (templates/common_group.cpp:72-90).
+int b200_set_profiling(b200_net* n, int32_t enable) {
+  if (!n) return B200_ERR_ARG;
+  n->profiling = enable != 0;
+  if (n->profiling) {
+    int r = b200_alloc(n, n->prof, (size_t)n->n_inst * n->M->n_phases * 8);
+    if (r) return r;
+    B200_CU(n, cudaStreamSynchronize(n->stream));
+  }
+  return 0;
+}
+
+int b200_get_profile(b200_net* n, int32_t inst, uint64_t* cycles, int32_t n_phases) {
+  if (!n || inst < 0 || inst >= n->n_inst || n_phases != n->M->n_phases || !n->prof.p) return B200_ERR_ARG;
+  B200_CU(n, cudaMemcpy(cycles, (char*)n->prof.p + (size_t)inst * n_phases * 8, (size_t)n_phases * 8,
+                        cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int b200_profile_phases(b200_net* n, int32_t* count) {
+  if (!n || !count) return B200_ERR_ARG;
+  *count = n->M->n_phases;
+  return 0;
+}
+
+// Thread-block clusters for instances of 2..16 CTAs (hardware barrier) on
+// (default) or off (bounded atomic barrier, cooperative launch).
+int b200_set_clusters(b200_net* n, int32_t enable) {
+  if (!n) return B200_ERR_ARG;
+  n->use_clusters = enable != 0;
+  n->prepared = false;
+  return 0;
+}
+
+int b200_launch_plan(b200_net* n, int32_t* grid, int32_t* cluster, int32_t* state_bytes) {
+  if (!n) return B200_ERR_ARG;
+  int r;
+  if (!n->prepared && (r = b200_prepare(n))) return r;
+  if (grid) *grid = n->grid;
+  if (cluster) *cluster = n->cluster;
+  if (state_bytes) *state_bytes = n->state_bytes;
+  return 0;
+}
+
+// Shared-memory state cache of single-CTA instances on (default) or off.
+int b200_set_smem_cache(b200_net* n, int32_t enable) {
+  if (!n) return B200_ERR_ARG;
+  n->smem_cache = enable != 0;
+  n->prepared = false;
   return 0;
 }
 
@@ -853,6 +975,7 @@ int b200_set_wait_limit(b200_net* n, int64_t limit_ns, int32_t fault_rank) {
   if (!n || limit_ns <= 0) return B200_ERR_ARG;
   n->limit_ns = (uint64_t)limit_ns;
   n->fault_rank = fault_rank;
+  if (fault_rank >= 0) n->prepared = false;  // the fault hook needs the bounded barrier
   return 0;
 }
 
@@ -871,6 +994,12 @@ int b200_set_step(b200_net* n, int32_t inst, int64_t ts) {
 int b200_last_run_ms(b200_net* n, double* ms) {
   if (!n || !ms) return B200_ERR_ARG;
   *ms = n->last_run_ms;
+  return 0;
+}
+
+int b200_last_kernel_ms(b200_net* n, double* ms) {
+  if (!n || !ms) return B200_ERR_ARG;
+  *ms = n->last_kernel_ms;
   return 0;
 }
 

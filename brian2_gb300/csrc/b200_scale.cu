@@ -227,6 +227,11 @@ __global__ void b200s_sort_segments(const int64_t* __restrict__ seg, int64_t n_s
   }
 }
 
+__global__ void b200s_outdeg_kernel(const int64_t* __restrict__ seg, int n_src, int W, int32_t* __restrict__ out) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n_src; s += gridDim.x * blockDim.x)
+    out[s] = (int32_t)(seg[(int64_t)(s + 1) * W] - seg[(int64_t)s * W]);
+}
+
 template <typename T>
 __global__ void b200s_fill_kernel(T* p, T v, int64_t n) {
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n; e += (int64_t)gridDim.x * blockDim.x)
@@ -360,6 +365,17 @@ int b200s_fill_f64(double* p, double v, int64_t n) {
   b200s_fill_kernel<double><<<4096, 256>>>(p, v, n);
   S_CU(cudaGetLastError());
   S_CU(cudaDeviceSynchronize());
+  return 0;
+}
+
+// Out-degree of every source of a CSR over (source, delay slot), to the host.
+int b200s_outdegree(const int64_t* d_segptr, int32_t n_src, int32_t W, int32_t* host_out) {
+  int32_t* d = nullptr;
+  S_CU(cudaMalloc(&d, (size_t)n_src * 4 + 16));
+  b200s_outdeg_kernel<<<1024, 256>>>(d_segptr, n_src, W, d);
+  S_CU(cudaGetLastError());
+  S_CU(cudaMemcpy(host_out, d, (size_t)n_src * 4, cudaMemcpyDeviceToHost));
+  cudaFree(d);
   return 0;
 }
 

@@ -54,6 +54,7 @@ def _declare(lib):
         "b200_get_step": [h, C.c_int32, _i64p],
         "b200_set_step": [h, C.c_int32, C.c_int64],
         "b200_last_run_ms": [h, _f64p],
+        "b200_last_kernel_ms": [h, _f64p],
         "b200_spikemon_size": [h, C.c_int32, C.c_int32, _i64p],
         "b200_spikemon_get": [h, C.c_int32, C.c_int32, _i32p, _i32p, _i32p, C.c_int64],
         "b200_ratemon_size": [h, C.c_int32, C.c_int32, _i64p],
@@ -65,6 +66,12 @@ def _declare(lib):
         "b200_device_bytes": [h, _i64p],
         "b200_launch_count": [h, _i64p],
         "b200_set_wait_limit": [h, C.c_int64, C.c_int32],
+        "b200_set_smem_cache": [h, C.c_int32],
+        "b200_set_profiling": [h, C.c_int32],
+        "b200_set_clusters": [h, C.c_int32],
+        "b200_launch_plan": [h, _i32p, _i32p, _i32p],
+        "b200_profile_phases": [h, _i32p],
+        "b200_get_profile": [h, C.c_int32, C.POINTER(C.c_uint64), C.c_int32],
     }
     for name, args in sig.items():
         f = getattr(lib, name)
@@ -288,10 +295,39 @@ class Network:
         self._check(self.lib.b200_last_run_ms(self._h, C.byref(v)))
         return v.value
 
+    def last_kernel_ms(self):
+        v = C.c_double()
+        self._check(self.lib.b200_last_kernel_ms(self._h, C.byref(v)))
+        return v.value
+
     def launches(self):
         v = C.c_int64()
         self._check(self.lib.b200_launch_count(self._h, C.byref(v)))
         return v.value
+
+    def set_clusters(self, enable=True):
+        self._check(self.lib.b200_set_clusters(self._h, int(bool(enable))))
+
+    def launch_plan(self):
+        g, c, sb = C.c_int32(), C.c_int32(), C.c_int32()
+        self._check(self.lib.b200_launch_plan(self._h, C.byref(g), C.byref(c), C.byref(sb)))
+        return dict(grid=g.value, cluster=c.value, state_bytes=sb.value)
+
+    def set_profiling(self, enable=True):
+        self._check(self.lib.b200_set_profiling(self._h, int(bool(enable))))
+
+    def profile(self, inst=0):
+        """{phase: SM cycles summed over the instance's CTAs and steps}."""
+        n = C.c_int32()
+        self._check(self.lib.b200_profile_phases(self._h, C.byref(n)))
+        a = np.zeros(n.value, np.uint64)
+        self._check(self.lib.b200_get_profile(self._h, int(inst), a.ctypes.data_as(C.POINTER(C.c_uint64)), n.value))
+        names = ["update_threshold_reset", "barrier_a", "spike_lists_monitors"] + \
+                [f"propagate:{p['name']}" for p in self.model.spec.get("pathways", [])] + ["barrier_b"]
+        return dict(zip(names, (int(x) for x in a)))
+
+    def set_smem_cache(self, enable=True):
+        self._check(self.lib.b200_set_smem_cache(self._h, int(bool(enable))))
 
     def set_wait_limit(self, limit_ns, fault_rank=-1):
         self._check(self.lib.b200_set_wait_limit(self._h, int(limit_ns), int(fault_rank)))

@@ -35,6 +35,7 @@ def lib():
         L.b200s_to_host.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
         L.b200s_host_draw.argtypes = [C.c_uint32] * 4 + [C.c_uint64, C.c_uint32]
         L.b200s_host_draw.restype = C.c_uint32
+        L.b200s_outdegree.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]
         _lib = L
     return _lib
 
@@ -69,6 +70,12 @@ class DeviceCSR:
                 raise RuntimeError(L.b200s_last_error().decode())
         return seg, post, pre
 
+    def outdegree(self):
+        out = np.empty(self.n_src, np.int32)
+        if lib().b200s_outdegree(self.seg, self.n_src, self.W, out.ctypes.data):
+            raise RuntimeError(lib().b200s_last_error().decode())
+        return out
+
     def free(self):
         L = lib()
         for p in (self.seg, self.post, self.pre):
@@ -98,10 +105,12 @@ def build_delays_scale(spec, N=1_000_000, K=1000, seed=1234, ne_frac=0.8, wscale
     if "i" in model.tables["groups"][0]:
         net.upload(0, "neurongroup", "i", np.arange(N, dtype=np.int32))
     csrs = []
+    outdeg = np.zeros(N, np.int64)
     for pw, (lo, hi, k, w) in (("synapses_pre", (0, Ne, Ke, we)), ("synapses_1_pre", (Ne, N, Ki, wi))):
         pid = model.pathway_index[pw]
         d = DeviceCSR(seed, pid, hi - lo, lo, N, k, dmin, dspan, DT)
         net.set_synapses_csr(0, pw, (lo, hi), (0, N), d.slot_min, d.slot_max, d.seg, d.post, d.pre, d.n_syn)
+        outdeg[lo:hi] += d.outdegree()
         wp = net.synapse_var_ptr(0, pw, "w")
         fill = lib().b200s_fill_f32 if ft == np.float32 else lib().b200s_fill_f64
         if fill(wp, w, d.n_syn):
@@ -110,4 +119,5 @@ def build_delays_scale(spec, N=1_000_000, K=1000, seed=1234, ne_frac=0.8, wscale
             csrs.append(d)
         else:
             d.free()
+    net.outdegree = outdeg  # synapses per source neuron (for counting synaptic events)
     return net, csrs

@@ -49,6 +49,13 @@ int b200_last_error(b200_net* net, char* buf, int64_t len);
  * thread preference (brian2/devices/cpp_standalone/device.py:60-67). */
 int b200_configure(b200_net* net, int32_t threads, const int32_t* ctas_per_inst, int32_t queue_mode,
                    int64_t chunk_steps, int32_t use_graph);
+/* Keep the state of single-CTA instances in shared memory for the duration of a
+ * launch (default on; off is for comparison and tuning). */
+int b200_set_smem_cache(b200_net* net, int32_t enable);
+/* Run instances of 2..16 CTAs as thread-block clusters with the hardware cluster
+ * barrier (default on), and report the launch plan that b200_run will use. */
+int b200_set_clusters(b200_net* net, int32_t enable);
+int b200_launch_plan(b200_net* net, int32_t* grid, int32_t* cluster, int32_t* state_bytes);
 /* Per-instance values of the model's namespace constants (the %CONSTANTS% of the
  * generated code objects, device.py:936-940); scalar blocks are re-evaluated. */
 int b200_set_consts(b200_net* net, int32_t inst, const double* values, int32_t count);
@@ -97,6 +104,8 @@ int b200_set_step(b200_net* net, int32_t inst, int64_t ts);
 /* Device time of the last b200_run in ms (CUDA events); the reference's
  * _last_run_time (device.py:1326-1332). */
 int b200_last_run_ms(b200_net* net, double* ms);
+/* Device time of the step-kernel launches of the last b200_run only, in ms. */
+int b200_last_kernel_ms(b200_net* net, double* ms);
 
 /* Monitor contents, copied back on request (device-resident until then).
  * Replace the dynamic arrays written by spikemonitor.cpp:37-47, ratemonitor.cpp:33-35,
@@ -116,6 +125,14 @@ int b200_reset_monitors(b200_net* net, int32_t inst);
  * B200_STATUS_TIMEOUT with the handle still usable.  The reference's analogue
  * is the wall-clock limit of Network::run (templates/network.cpp:59-82). */
 int b200_set_wait_limit(b200_net* net, int64_t limit_ns, int32_t fault_rank);
+
+/* Per-phase device profile of the step kernel (SM cycles summed over CTAs and
+ * steps; phases: update/threshold/reset, barrier, spike lists and monitors, one
+ * per pathway, barrier).  Replaces run(profile=True) timing
+ * (templates/common_group.cpp:72-90, objects.cpp:351-358). */
+int b200_set_profiling(b200_net* net, int32_t enable);
+int b200_profile_phases(b200_net* net, int32_t* count);
+int b200_get_profile(b200_net* net, int32_t inst, uint64_t* cycles, int32_t n_phases);
 
 /* Introspection. */
 int b200_model_name(char* buf, int64_t len);

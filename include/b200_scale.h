@@ -23,6 +23,7 @@ int b200s_free(void* p);
 int b200s_fill_f32(float* p, float v, int64_t n);
 int b200s_fill_f64(double* p, double v, int64_t n);
 int b200s_to_host(void* dst, const void* src, int64_t bytes);
+int b200s_outdegree(const int64_t* d_segptr, int32_t n_src, int32_t W, int32_t* host_out);
 uint32_t b200s_host_draw(uint32_t k, uint32_t j, uint32_t p, uint32_t r, uint64_t seed, uint32_t M);
 #ifdef __cplusplus
 }
