@@ -23,6 +23,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <cuda_runtime.h>
 
 namespace {
@@ -383,6 +384,150 @@ int b200s_to_host(void* dst, const void* src, int64_t bytes) {
   S_CU(cudaMemcpy(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost));
   return 0;
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of b200s_fixed_indegree_csr.
+//
+// For callers that may not call cudaMalloc/cudaFree while they run: a host
+// program whose device memory is owned by another framework's pool allocator
+// (a cudaMalloc/cudaFree pair in the middle of its work would synchronise the
+// whole device and bypass that pool), or a long-running loop with a fixed
+// device-memory budget that rebuilds small networks between runs.  The caller
+// passes the output buffers; the temporary arrays come from one fixed device
+// array that every GPU loading this library holds until the process exits.
+// ---------------------------------------------------------------------------
+#define B200S_NOALLOC_SCRATCH_BYTES ((size_t)16 << 20)  // 16 MiB per device
+
+static __device__ __align__(256) unsigned char b200s_noalloc_scratch[B200S_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_scratch_mu;
+void* g_scratch_addr[256] = {nullptr};  // device address of the array, per device ordinal
+
+// Device address of the scratch array on the current device.  Host code may
+// not use the symbol itself (it names a host-side stand-in), so the address is
+// looked up once per device with that device current, and cached.
+int scratch_on_current_device(unsigned char** out) {
+  int dev = 0;
+  S_CU(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 256) {
+    snprintf(g_err, sizeof(g_err), "device ordinal %d out of range", dev);
+    return 2;
+  }
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void* p = nullptr;
+    S_CU(cudaGetSymbolAddress(&p, b200s_noalloc_scratch));
+    g_scratch_addr[dev] = p;
+  }
+  *out = (unsigned char*)g_scratch_addr[dev];
+  return 0;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+}  // namespace
+
+extern "C" {
+
+// Scratch bytes the allocation-free entry point needs for a pathway, or 0 if
+// the sizes are invalid.  Larger requests are rejected by the entry point.
+int64_t b200s_noalloc_scratch_bytes(int32_t n_src, int32_t n_post, int32_t K, double dmin, double dspan,
+                                    double dt) {
+  if (K < 0 || K > 1024 || K > n_src || n_post < 0 || n_src <= 0) return 0;
+  const int s0 = (int)(dmin / dt + 0.5), s1 = (int)((dmin + dspan) / dt + 0.5);
+  if (s0 < 0 || s1 > 255) return 0;
+  const int64_t n = (int64_t)n_post * K, nb = (int64_t)n_src * (s1 - s0 + 1);
+  const int64_t nblk = (nb + 1023) / 1024;
+  return (int64_t)(align256((size_t)n * 4) + align256((size_t)n) + align256((size_t)nb * 4 + 16) +
+                   align256((size_t)(nblk + 1) * 8) + 256);
+}
+
+// Same network as b200s_fixed_indegree_csr, written into caller-allocated
+// device buffers: d_segptr with n_src*(slot_max-slot_min+1)+1 entries
+// (cap_seg), d_post and d_pre with n_post*K entries (cap_syn).  Allocates
+// nothing.  Its first call on a device looks up the scratch array's device
+// address (and so loads this library onto that device); make that first call
+// before any stream capture.  All calls share the one scratch array and leave
+// their temporaries in it: calls that overlap on the GPU (several host threads,
+// or several streams) race on it and must be serialised by the caller.  Runs on
+// the legacy default stream and returns after the work has completed.
+int b200s_fixed_indegree_csr_noalloc(uint64_t seed, int32_t path_id, int32_t n_src, int32_t src_off,
+                                     int32_t n_post, int32_t K, double dmin, double dspan, double dt,
+                                     int32_t* slot_min, int32_t* slot_max, int64_t* d_segptr, int64_t cap_seg,
+                                     int32_t* d_post, int32_t* d_pre, int64_t cap_syn) {
+  g_err[0] = 0;
+  const int64_t need = b200s_noalloc_scratch_bytes(n_src, n_post, K, dmin, dspan, dt);
+  if (need == 0) {
+    snprintf(g_err, sizeof(g_err), "invalid sizes (K=%d, n_src=%d, n_post=%d) or delays", K, n_src, n_post);
+    return 2;
+  }
+  if ((size_t)need > B200S_NOALLOC_SCRATCH_BYTES) {
+    snprintf(g_err, sizeof(g_err),
+             "network too large for the allocation-free path: needs %lld scratch bytes, the limit is %zu "
+             "(use b200s_fixed_indegree_csr)", (long long)need, B200S_NOALLOC_SCRATCH_BYTES);
+    return 3;
+  }
+  const int s0 = (int)(dmin / dt + 0.5), s1 = (int)((dmin + dspan) / dt + 0.5);
+  const int W = s1 - s0 + 1;
+  const int64_t n = (int64_t)n_post * K, nb = (int64_t)n_src * W, nblk = (nb + 1023) / 1024;
+  if (cap_seg < nb + 1 || cap_syn < n || !d_segptr || (n > 0 && (!d_post || !d_pre))) {
+    snprintf(g_err, sizeof(g_err), "output buffers too small: need %lld segment and %lld synapse entries",
+             (long long)(nb + 1), (long long)n);
+    return 2;
+  }
+  unsigned char* base = nullptr;
+  int r = scratch_on_current_device(&base);
+  if (r) return r;
+  int32_t* pre = (int32_t*)base;
+  size_t off = align256((size_t)n * 4);
+  uint8_t* slot = base + off;
+  off += align256((size_t)n);
+  int* cnt = (int*)(base + off);
+  off += align256((size_t)nb * 4 + 16);
+  int64_t* bsum = (int64_t*)(base + off);
+  off += align256((size_t)(nblk + 1) * 8);
+  int* err = (int*)(base + off);
+  // the scratch keeps the previous call's contents: clear what must start at zero
+  S_CU(cudaMemset(err, 0, 16));
+  if (n_post > 0)
+    b200s_sample_kernel<<<n_post, 256>>>(seed, (uint32_t)path_id, (uint32_t)n_src, K, n_post, dmin, dspan, dt,
+                                         pre, slot, err);
+  S_CU(cudaGetLastError());
+  int h_err = 0;
+  S_CU(cudaMemcpy(&h_err, err, 4, cudaMemcpyDeviceToHost));
+  if (h_err) {
+    snprintf(g_err, sizeof(g_err), "sampling did not converge");
+    return 3;
+  }
+  S_CU(cudaMemset(cnt, 0, (size_t)nb * 4 + 16));
+  b200s_count_kernel<<<4096, 256>>>(pre, slot, n, W, s0, n_src, cnt, err);
+  S_CU(cudaGetLastError());
+  S_CU(cudaMemcpy(&h_err, err, 4, cudaMemcpyDeviceToHost));
+  if (h_err) {
+    snprintf(g_err, sizeof(g_err), "construction produced an out-of-range index");
+    return 5;
+  }
+  b200s_scan_block<<<(unsigned)nblk, 1024>>>(cnt, nb, d_segptr, bsum);
+  b200s_scan_sums<<<1, 32>>>(bsum, nblk);
+  b200s_scan_add<<<(unsigned)nblk, 1024>>>(d_segptr, nb, bsum);
+  S_CU(cudaMemcpy(d_segptr + nb, bsum + nblk, 8, cudaMemcpyDeviceToDevice));
+  S_CU(cudaGetLastError());
+  S_CU(cudaMemset(cnt, 0, (size_t)nb * 4 + 16));
+  b200s_scatter_kernel<<<4096, 256>>>(pre, slot, n, K, W, s0, d_segptr, cnt, d_post);
+  S_CU(cudaGetLastError());
+  b200s_sort_segments<<<4096, 256>>>(d_segptr, nb, W, src_off, d_post, d_pre);
+  S_CU(cudaGetLastError());
+  S_CU(cudaDeviceSynchronize());
+  *slot_min = s0;
+  *slot_max = s1;
+  return 0;
+}
+
+}  // extern "C"
+
+extern "C" {
 
 // Host evaluation of one draw, for tests of the generator itself.
 uint32_t b200s_host_draw(uint32_t k, uint32_t j, uint32_t p, uint32_t r, uint64_t seed, uint32_t M) {

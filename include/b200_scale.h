@@ -24,6 +24,22 @@ int b200s_fill_f32(float* p, float v, int64_t n);
 int b200s_fill_f64(double* p, double v, int64_t n);
 int b200s_to_host(void* dst, const void* src, int64_t bytes);
 int b200s_outdegree(const int64_t* d_segptr, int32_t n_src, int32_t W, int32_t* host_out);
+
+/* No counterpart in the reference.  Allocation-free variant of
+ * b200s_fixed_indegree_csr for callers that may not call cudaMalloc/cudaFree
+ * while they run (device memory owned by another framework's pool, or a fixed
+ * device-memory budget): outputs are caller-allocated device buffers, the
+ * temporaries live in one 16 MiB device array per GPU (held until exit);
+ * larger networks are rejected with status 3.  The first call on a device sets
+ * up the array's address (make it before any stream capture).  Calls share the
+ * array: calls that overlap on the GPU race and must be serialised.
+ * b200s_noalloc_scratch_bytes() gives the scratch a network needs. */
+int64_t b200s_noalloc_scratch_bytes(int32_t n_src, int32_t n_post, int32_t K, double dmin, double dspan,
+                                    double dt);
+int b200s_fixed_indegree_csr_noalloc(uint64_t seed, int32_t path_id, int32_t n_src, int32_t src_off,
+                                     int32_t n_post, int32_t K, double dmin, double dspan, double dt,
+                                     int32_t* slot_min, int32_t* slot_max, int64_t* d_segptr, int64_t cap_seg,
+                                     int32_t* d_post, int32_t* d_pre, int64_t cap_syn);
 uint32_t b200s_host_draw(uint32_t k, uint32_t j, uint32_t p, uint32_t r, uint64_t seed, uint32_t M);
 #ifdef __cplusplus
 }
