@@ -1,0 +1,94 @@
+"""Batched parameter sweeps: many independent networks in one persistent launch.
+
+Each network of the sweep is one *instance* of the same compiled model with its
+own size, its own namespace constants (here ``taum`` and the excitatory weight
+``we``) and its own synapses.  All instances run in one launch of the step
+kernel in queue mode: resident CTAs take instances from a work queue (largest
+first, so the long ones start early), each instance on one CTA with its state
+in shared memory, every launch replayed from a captured CUDA graph.  The plain
+path for comparison runs the same networks one after another, each with its
+own best launch shape.
+
+Sweep of the benchmark (configuration "batched parameter sweep"): 256 CUBA
+networks, N uniform in 500..8000 (80/20 E/I), taum uniform in 10..30 ms,
+excitatory weight scale uniform in 0.5..2.0, Bernoulli p=0.02 from seed s+k,
+float32, dt = 0.1 ms, 500 ms.
+"""
+from __future__ import annotations
+
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+from . import workloads as W
+
+
+def sweep_parameters(n=256, seed=2024, n_lo=500, n_hi=8000):
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(n_lo, n_hi + 1, size=n)
+    taum = rng.uniform(0.010, 0.030, size=n)
+    wscale = rng.uniform(0.5, 2.0, size=n)
+    return [dict(N=int(sizes[k]), taum=float(taum[k]), wscale=float(wscale[k]), seed=int(seed) + k)
+            for k in range(n)]
+
+
+def build_sweep(spec, params, workers=16):
+    """Constructs every instance (host construction releases the GIL, so a
+    thread pool builds them in parallel)."""
+    we0 = W.const(spec, "we")
+
+    def one(p):
+        return W.build_cuba(spec, N=p["N"], seed=p["seed"],
+                            consts=dict(taum=p["taum"], we=we0 * p["wscale"]))
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        return list(ex.map(one, params))
+
+
+class Sweep:
+    """All instances of a sweep on the device, in one network handle."""
+
+    def __init__(self, spec, builts, threads=512, use_graph=True, chunk_steps=0):
+        order = sorted(range(len(builts)), key=lambda k: -sum(builts[k].sizes))
+        self.order = order                  # instance slot -> sweep index (largest first)
+        self.builts = [builts[k] for k in order]
+        self.net = W.instantiate(spec, self.builts, threads=threads, queue_mode=True, chunk_steps=chunk_steps)
+        if use_graph:
+            self.net.configure(threads=threads, ctas_per_inst=1, queue_mode=True, chunk_steps=chunk_steps,
+                               use_graph=True)
+
+    def run(self, steps):
+        self.net.run(steps)
+        return self.net.last_kernel_ms()
+
+    def spikes(self, k):
+        """Spike raster of sweep index k."""
+        slot = self.order.index(k)
+        return self.net.spikes(slot, 0)
+
+
+def run_sequential(spec, builts, steps, shape=None):
+    """The plain GPU path: every network alone, one after another; returns the
+    summed device time (ms) and the per-network spike counts."""
+    total_ms = 0.0
+    counts = []
+    for b in builts:
+        s = shape or dict(threads=512, ctas_per_inst=1)
+        net = W.instantiate(spec, [b], threads=s["threads"], ctas_per_inst=s.get("ctas_per_inst", 1))
+        net.run(steps)
+        total_ms += net.last_kernel_ms()
+        counts.append(len(net.spikes(0, 0)[0]))
+        net.close()
+    return total_ms, counts
+
+
+def compare(spec, builts, steps, threads=512, seq_shape=None):
+    """Batched vs sequential: device ms of each and the speed-up."""
+    t0 = time.perf_counter()
+    sw = Sweep(spec, builts, threads=threads)
+    batched_ms = sw.run(steps)
+    b_counts = [len(sw.spikes(k)[0]) for k in range(len(builts))]
+    sw.net.close()
+    seq_ms, s_counts = run_sequential(spec, builts, steps, seq_shape)
+    return dict(batched_ms=batched_ms, sequential_ms=seq_ms, speedup=seq_ms / batched_ms,
+                same_spike_counts=b_counts == s_counts, wall_s=time.perf_counter() - t0)

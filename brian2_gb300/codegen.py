@@ -323,8 +323,8 @@ def render_model(spec: dict) -> str:
     w("         (size_t)2 * B200_NG * max_tiles1 * 4 + (size_t)(3 * max_w + 1) * 4 + 16;")
     w("}")
     w("")
-    w("template <int MAXT>")
-    w("__global__ void __launch_bounds__(MAXT, 1) b200_step_kernel(")
+    w("template <int MAXT, int MINB>")
+    w("__global__ void __launch_bounds__(MAXT, MINB) b200_step_kernel(")
     w("    const b200_inst_d* __restrict__ insts, const int2* __restrict__ cta_map, int n_inst,")
     w("    int queue_mode, int* work, int64_t max_steps, uint64_t limit_ns, int max_tiles1, int max_w,")
     w("    int fault_rank, int state_bytes, unsigned long long* __restrict__ prof, int cluster) {")
@@ -389,8 +389,10 @@ def render_model(spec: dict) -> str:
         for k in USED[gi]:
             sz = SIZE[g["vars"][k]["ctype"]]
             w(f"        s_gv[{gi}][{k}] = s_state + off; off += ((size_t)I.g[{gi}].N * {sz} + 15) & ~(size_t)15;")
-        w(f"        s_scr[{gi}] = (int32_t*)(s_state + off); off += ((size_t)I.g[{gi}].N * 4 + 15) & ~(size_t)15;")
-        w(f"        s_tc[{gi}] = (int32_t*)(s_state + off); off += ((size_t)I.g[{gi}].n_tiles * 4 + 15) & ~(size_t)15;")
+        w("        if (I.cache_lists) {")
+        w(f"          s_scr[{gi}] = (int32_t*)(s_state + off); off += ((size_t)I.g[{gi}].N * 4 + 15) & ~(size_t)15;")
+        w(f"          s_tc[{gi}] = (int32_t*)(s_state + off); off += ((size_t)I.g[{gi}].n_tiles * 4 + 15) & ~(size_t)15;")
+        w("        }")
         w("      }")
         w(f"      s_ut[{gi}][0] = I.g[{gi}].cta_tile[rank]; s_ut[{gi}][1] = I.g[{gi}].cta_tile[rank + 1];")
     w("    }")
@@ -731,29 +733,34 @@ def render_model(spec: dict) -> str:
     w("")
 
     # ------------------------------------------------------------- launch glue
-    w("static const void* b200_kernel_for(int threads) {")
-    w("  if (threads <= 256) return (const void*)b200_step_kernel<256>;")
-    w("  if (threads <= 512) return (const void*)b200_step_kernel<512>;")
-    w("  return (const void*)b200_step_kernel<1024>;")
+    w("// `tcode` = threads | (min CTAs per SM - 1) << 16: the (512, 2) variant caps")
+    w("// registers so that two CTAs fit on an SM (sweeps with more instances than SMs)")
+    w("static const void* b200_kernel_for(int tcode) {")
+    w("  const int threads = tcode & 0xffff, minb = (tcode >> 16) + 1;")
+    w("  if (threads <= 256) return (const void*)b200_step_kernel<256, 1>;")
+    w("  if (threads <= 512) return minb >= 2 ? (const void*)b200_step_kernel<512, 2> : (const void*)b200_step_kernel<512, 1>;")
+    w("  return (const void*)b200_step_kernel<1024, 1>;")
     w("}")
-    w("static int b200_max_active(int threads, int max_tiles1, int max_w, int state_bytes) {")
-    w("  const void* k = b200_kernel_for(threads);")
+    w("static int b200_max_active(int tcode, int max_tiles1, int max_w, int state_bytes) {")
+    w("  const void* k = b200_kernel_for(tcode);")
+    w("  const int threads = tcode & 0xffff;")
     w("  const size_t smem = b200_dyn_smem(threads, max_tiles1, max_w, state_bytes);")
     w("  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;")
     w("  int n = 0;")
     w("  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads, smem) != cudaSuccess) return 0;")
     w("  return n;")
     w("}")
-    w("static int b200_static_smem(int threads) {")
+    w("static int b200_static_smem(int tcode) {")
     w("  cudaFuncAttributes a;")
-    w("  if (cudaFuncGetAttributes(&a, b200_kernel_for(threads)) != cudaSuccess) return 64 * 1024;")
+    w("  if (cudaFuncGetAttributes(&a, b200_kernel_for(tcode)) != cudaSuccess) return 64 * 1024;")
     w("  return (int)a.sharedSizeBytes;")
     w("}")
     w("static cudaError_t b200_launch(b200_inst_d* insts, const int2* cta_map, int n_inst, int queue_mode,")
-    w("                               int* work, int64_t max_steps, uint64_t limit_ns, int grid, int threads,")
+    w("                               int* work, int64_t max_steps, uint64_t limit_ns, int grid, int tcode,")
     w("                               int cooperative, int max_tiles1, int max_w, int fault_rank, int state_bytes,")
     w("                               unsigned long long* prof, int cluster, cudaStream_t s) {")
-    w("  const void* k = b200_kernel_for(threads);")
+    w("  const void* k = b200_kernel_for(tcode);")
+    w("  const int threads = tcode & 0xffff;")
     w("  const size_t smem = b200_dyn_smem(threads, max_tiles1, max_w, state_bytes);")
     w("  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);")
     w("  if (e != cudaSuccess) return e;")
@@ -777,8 +784,9 @@ def render_model(spec: dict) -> str:
     w("  if (cooperative) return cudaLaunchCooperativeKernel(k, dim3(grid), dim3(threads), args, smem, s);")
     w("  return cudaLaunchKernel(k, dim3(grid), dim3(threads), args, smem, s);")
     w("}")
-    w("static int b200_max_cluster(int threads, int max_tiles1, int max_w, int state_bytes, int cluster) {")
-    w("  const void* k = b200_kernel_for(threads);")
+    w("static int b200_max_cluster(int tcode, int max_tiles1, int max_w, int state_bytes, int cluster) {")
+    w("  const void* k = b200_kernel_for(tcode);")
+    w("  const int threads = tcode & 0xffff;")
     w("  const size_t smem = b200_dyn_smem(threads, max_tiles1, max_w, state_bytes);")
     w("  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;")
     w("  if (cluster > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return 0;")

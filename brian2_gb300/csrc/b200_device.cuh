@@ -86,7 +86,7 @@ struct b200_statemon_d {
 struct b200_inst_d {
   int32_t cta0, n_cta;    // CTAs [cta0, cta0+n_cta) of the grid run this instance
   int32_t cache_bytes;    // >0: single-CTA instance whose state is cached in shared memory
-  int32_t _pad0;
+  int32_t cache_lists;    // 1: the step's spike list and tile counts are cached too
   int64_t ts;             // next time step to execute
   int64_t ts_end;         // stop before this step
   double dt;

@@ -81,6 +81,7 @@ struct b200_net {
   std::vector<b200_inst_d> h_insts;
   cudaStream_t stream = nullptr;
   int threads = 256;
+  int min_blocks = 1;             // 2: register-capped variant, two CTAs per SM
   int max_tiles1 = 2, max_w = 1;  // dynamic shared-memory extents
   int state_bytes = 0;            // shared-memory state cache per CTA (0: none)
   bool smem_cache = true;         // cache the state of single-CTA instances
@@ -102,6 +103,7 @@ struct b200_net {
   double last_kernel_ms = 0.0;  // kernel launches only (CUDA events around them)
   std::string err;
   size_t device_bytes = 0;
+  int tcode() const { return threads | ((min_blocks - 1) << 16); }
 };
 
 static int b200_fail(b200_net* n, int code, const char* fmt, ...) {
@@ -690,28 +692,52 @@ static int b200_prepare(b200_net* n) {
     int dev = 0, optin = 0;
     B200_CU(n, cudaGetDevice(&dev));
     B200_CU(n, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    const long other = (long)M->static_smem(n->threads) +
+    // sweeps with more instances than SMs use the two-CTAs-per-SM variant
+    int n_sm_ = 0, dev_ = 0;
+    B200_CU(n, cudaGetDevice(&dev_));
+    B200_CU(n, cudaDeviceGetAttribute(&n_sm_, cudaDevAttrMultiProcessorCount, dev_));
+    n->min_blocks = (n->queue_mode && n->threads == 512 && n->n_inst > n_sm_) ? 2 : 1;
+    const long other = (long)M->static_smem(n->tcode()) +
                        (long)(n->threads * 16 + 2 * M->n_groups * n->max_tiles1 * 4 + (3 * n->max_w + 1) * 4 + 64);
     const long budget = (long)optin - other - 1024;
-    n->state_bytes = 0;
-    for (int k = 0; k < n->n_inst; ++k) {
+    // bytes of the cache of instance k: state variables, plus (lists) the step's
+    // spike list and tile counts
+    auto cache_bytes = [&](int k, bool lists) -> long {
       b200_inst_h& I = n->inst[k];
+      if (!n->smem_cache || I.n_cta != 1) return 0;
       long bytes = 0;
-      if (n->smem_cache && I.n_cta == 1) {
-        for (int g = 0; g < M->n_groups; ++g) {
-          const long Ng = I.g[g].N;
-          for (int v = 0; v < M->groups[g].n_vars; ++v)
-            if (M->groups[g].var_used[v]) bytes += (Ng * (long)b200_kind_size(M->groups[g].var_kind[v]) + 15) & ~15L;
+      for (int g = 0; g < M->n_groups; ++g) {
+        const long Ng = I.g[g].N;
+        for (int v = 0; v < M->groups[g].n_vars; ++v)
+          if (M->groups[g].var_used[v]) bytes += (Ng * (long)b200_kind_size(M->groups[g].var_kind[v]) + 15) & ~15L;
+        if (lists) {
           bytes += (Ng * 4 + 15) & ~15L;
           bytes += ((long)(I.g[g].tile_start.size() - 1) * 4 + 15) & ~15L;
         }
-        if (bytes > budget) bytes = 0;
       }
+      return bytes > budget ? 0 : bytes;
+    };
+    long with_lists = 0, state_only = 0;
+    for (int k = 0; k < n->n_inst; ++k) {
+      with_lists = std::max(with_lists, cache_bytes(k, true));
+      state_only = std::max(state_only, cache_bytes(k, false));
+    }
+    // a sweep of many instances wants two resident CTAs per SM: drop the lists
+    // from the cache when that is what it takes
+    bool lists = true;
+    if (n->queue_mode && n->n_inst > 1) {
+      const long half = (long)optin / 2 - other - 1024;
+      if (with_lists > half && state_only <= half) lists = false;
+    }
+    n->state_bytes = 0;
+    for (int k = 0; k < n->n_inst; ++k) {
+      const long bytes = cache_bytes(k, lists);
       n->h_insts[k].cache_bytes = (int32_t)bytes;
+      n->h_insts[k].cache_lists = lists ? 1 : 0;
       n->state_bytes = std::max<long>(n->state_bytes, bytes);
     }
   }
-  int max_per_sm = M->max_active_ctas(n->threads, n->max_tiles1, n->max_w, n->state_bytes);
+  int max_per_sm = M->max_active_ctas(n->tcode(), n->max_tiles1, n->max_w, n->state_bytes);
   int dev = 0, n_sm = 0;
   B200_CU(n, cudaGetDevice(&dev));
   B200_CU(n, cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
@@ -723,7 +749,7 @@ static int b200_prepare(b200_net* n) {
     bool same = true;
     for (int k = 1; k < n->n_inst; ++k) same = same && n->inst[k].n_cta == C;
     if (same && C >= 2 && C <= 16 &&
-        M->max_cluster(n->threads, n->max_tiles1, n->max_w, n->state_bytes, C) >= C)
+        M->max_cluster(n->tcode(), n->max_tiles1, n->max_w, n->state_bytes, C) >= C)
       n->cluster = C;
   }
   if (n->queue_mode) {
@@ -863,11 +889,43 @@ int b200_run(b200_net* n, int64_t n_steps) {
     const int64_t steps = n->chunk_steps;
 
     B200_CU(n, cudaEventRecord(k0, n->stream));
-    cudaError_t le = M->launch((b200_inst_d*)n->d_insts.p, (const int2*)n->d_cta_map.p, n->n_inst,
-                               n->queue_mode, (int*)n->d_work.p, steps, n->limit_ns, n->grid,
-                               n->threads, coop, n->max_tiles1, n->max_w, n->fault_rank, n->state_bytes,
-                               n->profiling ? (unsigned long long*)n->prof.p : nullptr,
-                               n->cluster, n->stream);
+    cudaError_t le = cudaSuccess;
+    const bool graph = n->use_graph && n->fault_rank < 0;
+    if (graph && (!n->graph_exec || n->graph_steps != steps)) {
+      // capture the launch (work-queue reset + persistent kernel) once; every
+      // later chunk is one graph replay
+      if (n->graph_exec) {
+        cudaGraphExecDestroy(n->graph_exec);
+        n->graph_exec = nullptr;
+      }
+      cudaGraph_t g = nullptr;
+      B200_CU(n, cudaStreamBeginCapture(n->stream, cudaStreamCaptureModeThreadLocal));
+      cudaMemsetAsync(n->d_work.p, 0, 16, n->stream);
+      le = M->launch((b200_inst_d*)n->d_insts.p, (const int2*)n->d_cta_map.p, n->n_inst, n->queue_mode,
+                     (int*)n->d_work.p, steps, n->limit_ns, n->grid, n->tcode(), coop, n->max_tiles1,
+                     n->max_w, n->fault_rank, n->state_bytes,
+                     n->profiling ? (unsigned long long*)n->prof.p : nullptr, n->cluster, n->stream);
+      cudaError_t ce = cudaStreamEndCapture(n->stream, &g);
+      if (le != cudaSuccess || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return b200_fail(n, B200_ERR_CUDA, "graph capture of the step launch: %s",
+                         cudaGetErrorString(le != cudaSuccess ? le : ce));
+      }
+      le = cudaGraphInstantiate(&n->graph_exec, g, 0);
+      cudaGraphDestroy(g);
+      if (le != cudaSuccess) return b200_fail(n, B200_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(le));
+      n->graph_steps = steps;
+    }
+    if (graph) {
+      le = cudaGraphLaunch(n->graph_exec, n->stream);
+    } else {
+      le = M->launch((b200_inst_d*)n->d_insts.p, (const int2*)n->d_cta_map.p, n->n_inst,
+                     n->queue_mode, (int*)n->d_work.p, steps, n->limit_ns, n->grid,
+                     n->tcode(), coop, n->max_tiles1, n->max_w, n->fault_rank, n->state_bytes,
+                     n->profiling ? (unsigned long long*)n->prof.p : nullptr,
+                     n->cluster, n->stream);
+    }
     if (n->fault_rank >= 0) {  // one-shot; the next launch may use clusters again
       n->fault_rank = -1;
       n->prepared = false;
@@ -921,6 +979,7 @@ int b200_run(b200_net* n, int64_t n_steps) {
 int b200_set_profiling(b200_net* n, int32_t enable) {
   if (!n) return B200_ERR_ARG;
   n->profiling = enable != 0;
+  n->graph_steps = -1;
   if (n->profiling) {
     int r = b200_alloc(n, n->prof, (size_t)n->n_inst * n->M->n_phases * 8);
     if (r) return r;

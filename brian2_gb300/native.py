@@ -115,6 +115,13 @@ def build_scale() -> str:
         [nvcc_path()] + nvcc_flags(True) + [src, "-o", tmp], "libb200_scale"))
 
 
+def build_adjoint() -> str:
+    src = os.path.join(CSRC, "b200_adjoint.cu")
+    out = os.path.join(BUILD, f"libb200_adjoint_{_sources_digest([src])}.so")
+    return _locked_build(out, lambda tmp: _run(
+        [nvcc_path()] + nvcc_flags(True) + [src, "-o", tmp], "libb200_adjoint"))
+
+
 def load(path: str) -> ctypes.CDLL:
     with _lock:
         lib = _loaded.get(path)
