@@ -32,10 +32,10 @@ def lib():
     if _lib is None:
         L = native.load(native.build_adjoint())
         for name in ("b200a_forward_f32", "b200a_forward_f64"):
-            getattr(L, name).argtypes = [C.c_void_p] * 10 + [C.c_void_p]
+            getattr(L, name).argtypes = [C.c_void_p] * 11 + [C.c_void_p]
             getattr(L, name).restype = C.c_int
         for name in ("b200a_backward_f32", "b200a_backward_f64"):
-            getattr(L, name).argtypes = [C.c_void_p] * 12 + [C.c_void_p]
+            getattr(L, name).argtypes = [C.c_void_p] * 15 + [C.c_void_p]
             getattr(L, name).restype = C.c_int
         L.b200a_last_error.restype = C.c_char_p
         _lib = L
@@ -114,14 +114,14 @@ def _suffix(dtype):
     return "f64" if dtype == torch.float64 else "f32"
 
 
-def forward_trace(ctx: _Ctx, W, W_out, taum, ckpt=None, spike_count=None):
+def forward_trace(ctx: _Ctx, W, W_out, taum, ckpt=None, spike_count=None, io=None):
     import torch
     cfg = ctx.cfg
     vo = torch.empty((cfg.steps, cfg.n_o), dtype=ctx.dtype, device="cuda")
     fp = cfg.fparams(taum)
     f = getattr(lib(), "b200a_forward_" + _suffix(ctx.dtype))
     r = f(ctx.ip.numpy().ctypes.data, fp.ctypes.data, _ptr(W), _ptr(W_out), _ptr(ctx.in_ptr), _ptr(ctx.in_ids),
-          _ptr(ctx.state0), _ptr(vo), _ptr(spike_count), _ptr(ckpt), _stream())
+          _ptr(ctx.state0), _ptr(vo), _ptr(spike_count), _ptr(ckpt), _ptr(io), _stream())
     if r:
         raise RuntimeError("adjoint forward: " + lib().b200a_last_error().decode())
     return vo
@@ -137,15 +137,16 @@ def _make_function():
         @staticmethod
         def forward(fctx, W, W_out, taum, ctx):
             ckpt = torch.empty((ctx.nseg, ctx.S), dtype=ctx.dtype, device="cuda")
-            vo = forward_trace(ctx, W.contiguous(), W_out.contiguous(), float(taum), ckpt=ckpt)
-            fctx.save_for_backward(W, W_out, ckpt)
+            io = torch.empty((ctx.cfg.steps, ctx.cfg.n_o), dtype=ctx.dtype, device="cuda")
+            vo = forward_trace(ctx, W.contiguous(), W_out.contiguous(), float(taum), ckpt=ckpt, io=io)
+            fctx.save_for_backward(W, W_out, ckpt, vo, io)
             fctx.taum = float(taum)
             fctx.ctx = ctx
             return vo
 
         @staticmethod
         def backward(fctx, grad_vo):
-            W, W_out, ckpt = fctx.saved_tensors
+            W, W_out, ckpt, vo, io = fctx.saved_tensors
             ctx = fctx.ctx
             cfg = ctx.cfg
             dW = torch.zeros_like(W)
@@ -156,7 +157,7 @@ def _make_function():
             f = getattr(lib(), "b200a_backward_" + _suffix(ctx.dtype))
             r = f(ctx.ip.numpy().ctypes.data, fp.ctypes.data, _ptr(W.contiguous()), _ptr(W_out.contiguous()),
                   _ptr(ctx.in_ptr), _ptr(ctx.in_ids), _ptr(ckpt), _ptr(grad_vo.contiguous()), _ptr(seg), _ptr(dW),
-                  _ptr(dWo), _ptr(dt), _stream())
+                  _ptr(dWo), _ptr(dt), _ptr(vo), _ptr(io), _ptr(ctx.state0), _stream())
             if r:
                 raise RuntimeError("adjoint backward: " + lib().b200a_last_error().decode())
             return dW, dWo, dt.reshape(()), None

@@ -72,16 +72,19 @@ template <typename T>
 __device__ void step_forward(const AdjP<T>& P, const Coef<T>& C, int n, T* s_v, T* s_I, T* s_vo, T* s_Io,
                              int* s_spk, T* s_r, int* s_nspk, const T* __restrict__ W,
                              const T* __restrict__ Wout, const int* __restrict__ in_ptr,
-                             const int* __restrict__ in_ids, T* vo_trace, int* spike_count) {
+                             const int* __restrict__ in_ids, T* vo_trace, int* spike_count,
+                             T* io_trace = nullptr, bool readout = true) {
   // hidden neurons: update, threshold, crossing fraction, reset
   for (int h = threadIdx.x; h < P.n_h; h += blockDim.x) {
     const T v = s_v[h], I = s_I[h];
     const T vm = P.El + C.a_m * (v - P.El) + C.c * I;
     if (vm > P.Vt) {
-      const int k = atomicAdd(s_nspk, 1);
-      if (k < MAXSPK) {
-        s_spk[k] = h;
-        s_r[k] = (T)1 - (P.Vt - v) / (vm - v);
+      if (readout) {
+        const int k = atomicAdd(s_nspk, 1);
+        if (k < MAXSPK) {
+          s_spk[k] = h;
+          s_r[k] = (T)1 - (P.Vt - v) / (vm - v);
+        }
       }
       s_v[h] = P.Vr;
       if (spike_count) spike_count[h] += 1;
@@ -99,7 +102,7 @@ __device__ void step_forward(const AdjP<T>& P, const Coef<T>& C, int n, T* s_v, 
   }
   // readout: spikes of this step in ascending neuron order (deterministic sums)
   const int ns = min(*s_nspk, MAXSPK);
-  if (threadIdx.x < P.n_o) {
+  if (readout && threadIdx.x < P.n_o) {
     const int o = threadIdx.x;
     T av = 0, ai = 0;
     int last = -1;
@@ -119,10 +122,21 @@ __device__ void step_forward(const AdjP<T>& P, const Coef<T>& C, int n, T* s_v, 
     s_vo[o] = von;
     s_Io[o] = C.a_s * Io + ai;
     if (vo_trace) vo_trace[(size_t)n * P.n_o + o] = von;
+    if (io_trace) io_trace[(size_t)n * P.n_o + o] = s_Io[o];
   }
   __syncthreads();
-  if (threadIdx.x == 0) *s_nspk = 0;
-  __syncthreads();
+  if (readout) {
+    if (threadIdx.x == 0) *s_nspk = 0;
+    __syncthreads();
+  }
+}
+
+// W_out in shared memory when it fits (every spike of every step reads a row)
+template <typename T>
+__device__ const T* stage_wout(const AdjP<T>& P, const T* Wout, T* s_wout, bool fits) {
+  if (!fits) return Wout;
+  for (int k = threadIdx.x; k < P.n_h * P.n_o; k += blockDim.x) s_wout[k] = Wout[k];
+  return s_wout;
 }
 
 template <typename T>
@@ -154,7 +168,8 @@ __global__ void __launch_bounds__(1024, 1) forward_kernel(AdjP<T> P, const T* __
                                                           const T* __restrict__ Wout,
                                                           const int* __restrict__ in_ptr,
                                                           const int* __restrict__ in_ids, const T* __restrict__ state0,
-                                                          T* vo_trace, int* spike_count, T* ckpt) {
+                                                          T* vo_trace, int* spike_count, T* ckpt, T* io_trace,
+                                                          int wout_smem) {
   extern __shared__ __align__(16) unsigned char smem[];
   T* s_v = (T*)smem;
   T* s_I = s_v + P.n_h;
@@ -162,15 +177,18 @@ __global__ void __launch_bounds__(1024, 1) forward_kernel(AdjP<T> P, const T* __
   T* s_Io = s_vo + MAXO;
   T* s_r = s_Io + MAXO;
   int* s_spk = (int*)(s_r + MAXSPK);
+  T* s_wout = (T*)(s_spk + MAXSPK);
   __shared__ int s_nspk;
   if (threadIdx.x == 0) s_nspk = 0;
   const Coef<T> C(P);
   load_state(P, state0, s_v, s_I, s_vo, s_Io);
+  const T* Wo = stage_wout(P, Wout, s_wout, wout_smem != 0);
   __syncthreads();
   const int S = 2 * P.n_h + 2 * P.n_o;
   for (int n = 0; n < P.steps; ++n) {
     if (ckpt && n % P.K == 0) save_state(P, ckpt + (size_t)(n / P.K) * S, s_v, s_I, s_vo, s_Io);
-    step_forward(P, C, n, s_v, s_I, s_vo, s_Io, s_spk, s_r, &s_nspk, W, Wout, in_ptr, in_ids, vo_trace, spike_count);
+    step_forward(P, C, n, s_v, s_I, s_vo, s_Io, s_spk, s_r, &s_nspk, W, Wo, in_ptr, in_ids, vo_trace, spike_count,
+                 io_trace);
   }
 }
 
@@ -195,7 +213,9 @@ __global__ void __launch_bounds__(1024, 1) backward_kernel(AdjP<T> P, const T* _
                                                            const int* __restrict__ in_ids,
                                                            const T* __restrict__ ckpt,
                                                            const T* __restrict__ grad_vo, T* segbuf, T* dW,
-                                                           T* dWout, T* dtaum) {
+                                                           T* dWout, T* dtaum, const T* __restrict__ vo_trace,
+                                                           const T* __restrict__ io_trace,
+                                                           const T* __restrict__ state0, int wout_smem) {
   extern __shared__ __align__(16) unsigned char smem[];
   T* s_v = (T*)smem;
   T* s_I = s_v + P.n_h;
@@ -221,6 +241,8 @@ __global__ void __launch_bounds__(1024, 1) backward_kernel(AdjP<T> P, const T* _
   T* s_ro = s_g + (size_t)P.K * P.n_o;           // [K * 2 n_o]: vo_n, Io_n
   int* s_ip = (int*)(s_ro + (size_t)P.K * 2 * P.n_o);  // [K + 1] input offsets
   int* s_ids = s_ip + P.K + 1;                   // [MAXIDS] input indices
+  T* s_wout = (T*)(((uintptr_t)(s_ids + MAXIDS) + 15) & ~(uintptr_t)15);
+  const T* Wo = stage_wout(P, Wout, s_wout, wout_smem != 0);
   const int h0 = threadIdx.x;
   const bool own = h0 < P.n_h;
   for (int seg = nseg - 1; seg >= 0; --seg) {
@@ -228,14 +250,18 @@ __global__ void __launch_bounds__(1024, 1) backward_kernel(AdjP<T> P, const T* _
     // recompute the segment from its checkpoint, keeping the state at each step
     load_state(P, ckpt + (size_t)seg * S, s_v, s_I, s_vo, s_Io);
     __syncthreads();
-    for (int n = s0; n < s1; ++n) {
+    // the readout state of every step comes from the forward traces
+    for (int k = threadIdx.x; k < (s1 - s0) * P.n_o; k += blockDim.x) {
+      const int n = s0 + k / P.n_o, o = k % P.n_o;
+      s_ro[(size_t)(n - s0) * 2 * P.n_o + o] =
+          n == 0 ? state0[2 * P.n_h + o] : vo_trace[(size_t)(n - 1) * P.n_o + o];
+      s_ro[(size_t)(n - s0) * 2 * P.n_o + P.n_o + o] =
+          n == 0 ? state0[2 * P.n_h + P.n_o + o] : io_trace[(size_t)(n - 1) * P.n_o + o];
+    }
+    for (int n = s0; n < s1; ++n) {  // hidden layer only
       save_state(P, segbuf + (size_t)(n - s0) * S, s_v, s_I, s_vo, s_Io);
-      if (threadIdx.x < P.n_o) {
-        s_ro[(size_t)(n - s0) * 2 * P.n_o + threadIdx.x] = s_vo[threadIdx.x];
-        s_ro[(size_t)(n - s0) * 2 * P.n_o + P.n_o + threadIdx.x] = s_Io[threadIdx.x];
-      }
-      step_forward(P, C, n, s_v, s_I, s_vo, s_Io, s_spk, s_r, &s_nspk, W, Wout, in_ptr, in_ids, (T*)nullptr,
-                   (int*)nullptr);
+      step_forward(P, C, n, s_v, s_I, s_vo, s_Io, s_spk, s_r, &s_nspk, W, Wo, in_ptr, in_ids, (T*)nullptr,
+                   (int*)nullptr, (T*)nullptr, false);
     }
     const int ib = in_ptr[s0], nin = in_ptr[s1] - ib;
     const bool ids_smem = nin <= MAXIDS;
@@ -295,7 +321,7 @@ __global__ void __launch_bounds__(1024, 1) backward_kernel(AdjP<T> P, const T* _
           readout_kernel_fn(P, r, f, e, df_dr, de_dr, df_dt);
           T dLdr = 0;
           for (int o = 0; o < P.n_o; ++o) {
-            const T w = Wout[(size_t)h * P.n_o + o];
+            const T w = Wo[(size_t)h * P.n_o + o];
             atomicAdd(&dWout[(size_t)h * P.n_o + o], s_Lvo[o] * f + s_lIo1[o] * e);
             dLdr += w * (s_Lvo[o] * df_dr + s_lIo1[o] * de_dr);
             p_ft += w * s_Lvo[o] * df_dt;
@@ -326,26 +352,31 @@ __global__ void __launch_bounds__(1024, 1) backward_kernel(AdjP<T> P, const T* _
 }
 
 template <typename T>
-size_t smem_bytes(const AdjP<T>& P, bool backward) {
+size_t smem_bytes(const AdjP<T>& P, bool backward, bool wout) {
   size_t b = (size_t)(2 * P.n_h + 2 * MAXO + MAXSPK) * sizeof(T) + MAXSPK * sizeof(int);
   if (backward)
     b += (size_t)2 * P.n_h * sizeof(T) + (size_t)P.K * 3 * P.n_o * sizeof(T) + (size_t)(P.K + 1 + MAXIDS) * sizeof(int) + 16;
+  if (wout) b += (size_t)P.n_h * P.n_o * sizeof(T) + 16;
   return b + 64;
 }
+
+constexpr size_t SMEM_LIMIT = 220 * 1024;
 
 thread_local char g_err[256];
 
 template <typename T>
 int run_forward(const AdjP<T>& P, const T* W, const T* Wout, const int* in_ptr, const int* in_ids, const T* state0,
-                T* vo_trace, int* spike_count, T* ckpt, cudaStream_t s) {
+                T* vo_trace, int* spike_count, T* ckpt, T* io_trace, cudaStream_t s) {
   if (P.n_o > MAXO || P.n_h <= 0 || P.n_h > MAXSPK || P.steps < 0 || P.K <= 0) {
     snprintf(g_err, sizeof(g_err), "invalid sizes (n_h <= %d, n_o <= %d)", MAXSPK, MAXO);
     return 2;
   }
-  const size_t sm = smem_bytes(P, false);
+  const int wout = smem_bytes(P, false, true) <= SMEM_LIMIT ? 1 : 0;
+  const size_t sm = smem_bytes(P, false, wout != 0);
   cudaError_t e = cudaFuncSetAttribute(forward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e == cudaSuccess) {
-    forward_kernel<T><<<1, 1024, sm, s>>>(P, W, Wout, in_ptr, in_ids, state0, vo_trace, spike_count, ckpt);
+    forward_kernel<T><<<1, 1024, sm, s>>>(P, W, Wout, in_ptr, in_ids, state0, vo_trace, spike_count, ckpt, io_trace,
+                                          wout);
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) {
@@ -357,19 +388,22 @@ int run_forward(const AdjP<T>& P, const T* W, const T* Wout, const int* in_ptr, 
 
 template <typename T>
 int run_backward(const AdjP<T>& P, const T* W, const T* Wout, const int* in_ptr, const int* in_ids, const T* ckpt,
-                 const T* grad_vo, T* segbuf, T* dW, T* dWout, T* dtaum, cudaStream_t s) {
+                 const T* grad_vo, T* segbuf, T* dW, T* dWout, T* dtaum, const T* vo_trace, const T* io_trace,
+                 const T* state0, cudaStream_t s) {
   if (P.n_o > MAXO || P.n_h <= 0 || P.n_h > MAXSPK || P.steps < 0 || P.K <= 0) {
     snprintf(g_err, sizeof(g_err), "invalid sizes (n_h <= %d, n_o <= %d)", MAXSPK, MAXO);
     return 2;
   }
-  const size_t sm = smem_bytes(P, true);
-  if (sm > 227 * 1024) {
+  const int wout = smem_bytes(P, true, true) <= SMEM_LIMIT ? 1 : 0;
+  const size_t sm = smem_bytes(P, true, wout != 0);
+  if (sm > SMEM_LIMIT) {
     snprintf(g_err, sizeof(g_err), "network too large for one CTA (%zu bytes of shared memory)", sm);
     return 2;
   }
   cudaError_t e = cudaFuncSetAttribute(backward_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e == cudaSuccess) {
-    backward_kernel<T><<<1, 1024, sm, s>>>(P, W, Wout, in_ptr, in_ids, ckpt, grad_vo, segbuf, dW, dWout, dtaum);
+    backward_kernel<T><<<1, 1024, sm, s>>>(P, W, Wout, in_ptr, in_ids, ckpt, grad_vo, segbuf, dW, dWout, dtaum,
+                                           vo_trace, io_trace, state0, wout);
     e = cudaGetLastError();
   }
   if (e != cudaSuccess) {
@@ -390,31 +424,38 @@ const char* b200a_last_error() { return g_err; }
 // entries or NULL; spike_count: n_h or NULL; stream: a cudaStream_t or 0.
 int b200a_forward_f32(const int32_t* ip, const double* fp, const float* W, const float* Wout, const int32_t* in_ptr,
                       const int32_t* in_ids, const float* state0, float* vo_trace, int32_t* spike_count,
-                      float* ckpt, void* stream) {
+                      float* ckpt, float* io_trace, void* stream) {
   AdjP<float> P{ip[0], ip[1], ip[2], ip[3], ip[4], (float)fp[0], (float)fp[1], (float)fp[2], (float)fp[3],
                 (float)fp[4], (float)fp[5]};
-  return run_forward(P, W, Wout, in_ptr, in_ids, state0, vo_trace, spike_count, ckpt, (cudaStream_t)stream);
+  return run_forward(P, W, Wout, in_ptr, in_ids, state0, vo_trace, spike_count, ckpt, io_trace,
+                     (cudaStream_t)stream);
 }
 int b200a_forward_f64(const int32_t* ip, const double* fp, const double* W, const double* Wout, const int32_t* in_ptr,
                       const int32_t* in_ids, const double* state0, double* vo_trace, int32_t* spike_count,
-                      double* ckpt, void* stream) {
+                      double* ckpt, double* io_trace, void* stream) {
   AdjP<double> P{ip[0], ip[1], ip[2], ip[3], ip[4], fp[0], fp[1], fp[2], fp[3], fp[4], fp[5]};
-  return run_forward(P, W, Wout, in_ptr, in_ids, state0, vo_trace, spike_count, ckpt, (cudaStream_t)stream);
+  return run_forward(P, W, Wout, in_ptr, in_ids, state0, vo_trace, spike_count, ckpt, io_trace,
+                     (cudaStream_t)stream);
 }
 // segbuf: K*(2 n_h + 2 n_o) entries; dW (n_in*n_h), dWout (n_h*n_o) are
-// accumulated into (zero them first); dtaum: one entry, written.
+// accumulated into (zero them first); dtaum: one entry, written; vo_trace and
+// io_trace are the forward pass's traces, state0 its initial state.
 int b200a_backward_f32(const int32_t* ip, const double* fp, const float* W, const float* Wout, const int32_t* in_ptr,
                        const int32_t* in_ids, const float* ckpt, const float* grad_vo, float* segbuf, float* dW,
-                       float* dWout, float* dtaum, void* stream) {
+                       float* dWout, float* dtaum, const float* vo_trace, const float* io_trace, const float* state0,
+                       void* stream) {
   AdjP<float> P{ip[0], ip[1], ip[2], ip[3], ip[4], (float)fp[0], (float)fp[1], (float)fp[2], (float)fp[3],
                 (float)fp[4], (float)fp[5]};
-  return run_backward(P, W, Wout, in_ptr, in_ids, ckpt, grad_vo, segbuf, dW, dWout, dtaum, (cudaStream_t)stream);
+  return run_backward(P, W, Wout, in_ptr, in_ids, ckpt, grad_vo, segbuf, dW, dWout, dtaum, vo_trace, io_trace, state0,
+                      (cudaStream_t)stream);
 }
 int b200a_backward_f64(const int32_t* ip, const double* fp, const double* W, const double* Wout,
                        const int32_t* in_ptr, const int32_t* in_ids, const double* ckpt, const double* grad_vo,
-                       double* segbuf, double* dW, double* dWout, double* dtaum, void* stream) {
+                       double* segbuf, double* dW, double* dWout, double* dtaum, const double* vo_trace,
+                       const double* io_trace, const double* state0, void* stream) {
   AdjP<double> P{ip[0], ip[1], ip[2], ip[3], ip[4], fp[0], fp[1], fp[2], fp[3], fp[4], fp[5]};
-  return run_backward(P, W, Wout, in_ptr, in_ids, ckpt, grad_vo, segbuf, dW, dWout, dtaum, (cudaStream_t)stream);
+  return run_backward(P, W, Wout, in_ptr, in_ids, ckpt, grad_vo, segbuf, dW, dWout, dtaum, vo_trace, io_trace, state0,
+                      (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -14,7 +14,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared(header):
     text = open(os.path.join(ROOT, "include", header)).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(b200s?_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(b200[sa]?_\w+)\s*\(", text)))
 
 
 def exported(path):
@@ -40,6 +40,14 @@ def test_construct_library_exports_abi():
 def test_scale_library_exports_abi():
     lib = exported(native.build_scale())
     missing = [n for n in declared("b200_scale.h") if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_adjoint_library_exports_abi():
+    lib = exported(native.build_adjoint())
+    names = declared("b200_adjoint.h")
+    assert len(names) == 5
+    missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
 
 
