@@ -11,8 +11,15 @@ Printed (rank 0, one JSON line): synaptic events/s over the timed steps
 (events = sum over emitted spikes of the source's out-degree), simulated
 seconds per wall second, an end-to-end figure through the public API with host
 buffers (state uploaded from pinned memory and the step's spikes read back every
-step), the step kernel's roofline, and the oracle timed on the host cores as a
-CPU baseline.
+step), the step kernel's roofline, and the reference's own CPU step loop timed
+on the host cores as a CPU baseline: the cpp_standalone project the reference
+generates for the 10,000-neuron subnetwork of identical construction, OpenMP
+(oracle/ref_standalone.py); where that project was not generated, the oracle
+(single-threaded C++ restatement) instead.  On one GPU the line also carries
+the other workloads, each measured in this run: CUBA 4000 (float64), COBAHH
+4000 (float64 and float32), the 256-network batched sweep against the same
+networks run one after another, and the adjoint's forward+adjoint / forward
+cost ratio.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -106,9 +113,39 @@ def ncu_traffic_per_neuron_step():
 
 
 def cpu_baseline(max_seconds=20.0):
+    """The reference's CPU step loop on a bounded sample of the same workload:
+    the 10,000-neuron network of identical construction (in-degree 1000, delays
+    0.1-5 ms), float64, 1 s simulated.  The reference's own generated
+    cpp_standalone project (OpenMP) where it is present, else the oracle."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_standalone
+    if ref_standalone.available():
+        T = ref_standalone.all_threads()
+        ref_standalone.build(T)
+        r = ref_standalone.run(T)
+        return {"value": r["events"] / r["run_time_s"], "unit": UNIT, "cores": r["threads"], "kind": "reference",
+                "sample": f"reference cpp_standalone project (generated by the reference, g++ -O3 -ffast-math "
+                          f"-fopenmp, {r['threads']} OpenMP threads) on the 10,000-neuron subnetwork of identical "
+                          f"construction: {r['steps']} clock steps ({r['sim_s']:.2f} s simulated), "
+                          f"{r['spikes']} spikes, {r['events']} events, step loop {r['run_time_s']:.2f} s",
+                "sim_s_per_wall_s": r["sim_s"] / r["run_time_s"], "host_cpus": os.cpu_count(),
+                "single_thread": _reference_single_thread(ref_standalone, T)}
+    return cpu_baseline_port(max_seconds)
+
+
+def _reference_single_thread(ref_standalone, T):
+    """The same reference project without OpenMP parallelism (1 thread)."""
+    if T == 1 or 1 not in ref_standalone.variants():
+        return None
+    ref_standalone.build(1)
+    r = ref_standalone.run(1)
+    return {"value": r["events"] / r["run_time_s"], "cores": 1, "step_loop_s": r["run_time_s"],
+            "sim_s_per_wall_s": r["sim_s"] / r["run_time_s"]}
+
+
+def cpu_baseline_port(max_seconds=20.0):
     """The oracle (single-threaded CPU restatement of the reference's step loop)
-    on a bounded sample of the same workload: the 10,000-neuron network of
-    identical construction (in-degree 1000, delays 0.1-5 ms), float64."""
+    on the same sample."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from oracle import oracle_from_built
     from brian2_gb300 import workloads as W
@@ -136,22 +173,109 @@ def cpu_baseline(max_seconds=20.0):
             "sim_s_per_wall_s": steps * 1e-4 / dt}
 
 
+def _outdegree(b, n):
+    out = np.zeros(n, np.int64)
+    for syn in b.synapses.values():
+        out += np.bincount(syn["pre"] + syn["src"][0], minlength=n)
+    return out
+
+
+def extra_plain(name, builder, steps=10_000):
+    """One plain network (1 s simulated) with the autotuned launch shape."""
+    from brian2_gb300 import autotune, workloads as W
+    spec = W.load_spec(name)
+    b = builder(spec)
+    n = sum(b.sizes)
+    shape = autotune.tune(spec, [b])
+    net = W.instantiate(spec, [b], threads=shape["threads"], ctas_per_inst=shape["ctas_per_inst"])
+    net.run(steps)
+    ms = net.last_kernel_ms()
+    i, _, _ = net.spikes(0, 0)
+    ev = int(_outdegree(b, n)[i].sum())
+    net.close()
+    return {"neurons": n, "clock_steps": steps, "device_ms": ms, "sim_s_per_wall_s": steps * 1e-4 / (ms * 1e-3),
+            "events_per_s": ev / (ms * 1e-3), "spikes": int(len(i)), "us_per_clock_step": ms * 1e3 / steps,
+            "launch_shape": {k: shape[k] for k in ("threads", "ctas_per_inst")}}
+
+
+def extra_batched(steps=5000):
+    """256 CUBA networks of uneven size (float32, 500 ms): one persistent
+    graph-replayed launch (autotuned block size) against the same networks run
+    one after another on the plain path (each with its own tuned shape)."""
+    from brian2_gb300 import autotune, batched, workloads as W
+    spec = W.load_spec("cuba_f32")
+    t0 = time.perf_counter()
+    builts = batched.build_sweep(spec, batched.sweep_parameters(256))
+    t_build = time.perf_counter() - t0
+    shape = autotune.tune(spec, builts)
+    r = batched.compare(spec, builts, steps, threads=shape["threads"])
+    r.update(instances=len(builts), neurons=int(sum(sum(b.sizes) for b in builts)), clock_steps=steps,
+             threads=shape["threads"], host_build_s=round(t_build, 2))
+    return r
+
+
+def extra_adjoint(reps=5):
+    """Adjoint workload (float32): forward alone vs forward+adjoint (the loss's
+    forward through the autograd function and its backward), median of reps."""
+    import torch
+    from brian2_gb300.adjoint import AdjointConfig, AdjointProblem, forward_trace
+    P = AdjointProblem(AdjointConfig(), dtype=torch.float32)
+    Wt, Wo, tm = P.params()
+    fw, fb = [], []
+    for rep in range(reps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with torch.no_grad():
+            forward_trace(P.ctx, Wt.detach(), Wo.detach(), float(tm.detach()))
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        P.loss(Wt, Wo, tm).backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        Wt.grad = Wo.grad = tm.grad = None
+        if rep:
+            fw.append(t1 - t0)
+            fb.append(t2 - t1)
+    f, b = float(np.median(fw)), float(np.median(fb))
+    return {"forward_ms": f * 1e3, "forward_adjoint_ms": b * 1e3, "ratio": b / f, "dtype": "f32",
+            "clock_steps": P.cfg.steps, "hidden": P.cfg.n_h, "inputs": P.cfg.n_in, "readout": P.cfg.n_o}
+
+
+def extras():
+    from brian2_gb300 import workloads as W
+    out = {}
+    jobs = [("cuba_4000_f64", lambda: extra_plain("cuba_f64", lambda s: W.build_cuba(s, N=4000, seed=1234))),
+            ("cobahh_4000_f64", lambda: extra_plain("cobahh_f64", lambda s: W.build_cobahh(s, N=4000, seed=1234))),
+            ("cobahh_4000_f32", lambda: extra_plain("cobahh_f32", lambda s: W.build_cobahh(s, N=4000, seed=1234))),
+            ("batched_sweep_256_f32", extra_batched),
+            ("adjoint_f32", extra_adjoint)]
+    for name, fn in jobs:
+        try:
+            out[name] = fn()
+        except Exception as e:  # reported, not fatal: the headline line still prints
+            out[name] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    return out
+
+
 def run_reference(args, rank, world):
-    """--impl reference: the reference's CPU path for this workload (the oracle
-    port, single-threaded) on the same metric and config."""
+    """--impl reference: the reference's CPU path for this workload (its
+    generated cpp_standalone project with OpenMP, else the oracle port) on the
+    same metric and config; every step is one bounded sample."""
     if rank != 0:
         return
     vals = []
-    for _ in range(args.warmup):
+    for _ in range(min(args.warmup, 1)):
         cpu_baseline(max_seconds=5.0)
     for _ in range(args.steps):
         vals.append(cpu_baseline(max_seconds=10.0))
     v = float(np.median([x["value"] for x in vals]))
+    base = vals[0]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded construction)",
             "config": {"workload": WORKLOAD, "sample": "10,000-neuron subnetwork, same construction"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port", "sample": vals[0]["sample"]},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": base["cores"], "kind": base["kind"],
+                             "sample": base["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -166,6 +290,7 @@ def main():
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--ctas", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
     args = ap.parse_args()
     rank, world, local = rank_info()
     dist = None
@@ -271,6 +396,10 @@ def main():
         dist.all_reduce(e, op=dist.ReduceOp.SUM)
         e2e_events = float(e.item())
 
+    other = None
+    if rank == 0 and world == 1 and not args.no_extras:
+        net.close()  # frees the 1e9-synapse network before the other workloads
+        other = extras()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline()
@@ -292,6 +421,7 @@ def main():
             "gpu_launches": int(launches),
             "clocks": clk,
             "cpu_baseline": cpu,
+            "other_workloads": other,
         }
         print(json.dumps(line), flush=True)
     if dist:

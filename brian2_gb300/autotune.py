@@ -33,21 +33,23 @@ def _save_cache(c):
     os.replace(tmp, _CACHE_FILE)
 
 
-def candidates(total_neurons: int, n_inst: int, f64: bool):
+def candidates(total_neurons: int, n_inst: int):
     """Shapes worth trying: (threads, ctas_per_inst, queue_mode)."""
     if n_inst > 1:
         return [(t, 1, True) for t in (256, 512, 1024)]
     out = [(512, 1, False), (1024, 1, False)]
     for c in (2, 4, 8, 16):
-        if total_neurons >= 256 * c:
+        if total_neurons >= 128 * c:
             out.append((256, c, False))
-    if f64 or total_neurons > 50_000:
+    # one CTA per SM: FP64-bound or arithmetic-heavy models (e.g. Hodgkin-Huxley
+    # in either precision) and large networks
+    if total_neurons >= 2000:
         out.append((256, 152, False))
         out.append((1024, 152, False))
     return out
 
 
-def tune(spec, builts, steps=300, make_network=None, verbose=False):
+def tune(spec, builts, steps=None, make_network=None, verbose=False):
     """Returns the fastest {threads, ctas_per_inst, queue_mode} for these
     instances; `make_network(threads, ctas, queue)` builds a fresh network."""
     from .codegen import spec_hash
@@ -58,9 +60,10 @@ def tune(spec, builts, steps=300, make_network=None, verbose=False):
     if key in cache:
         return cache[key]
     total = max(sum(s) for s in sizes)
-    f64 = spec.get("float", "double") == "double"
+    if steps is None:  # sweeps: long enough that the state load at launch start does not decide
+        steps = 1000 if len(builts) > 1 else 300
     best = None
-    for threads, ctas, queue in candidates(total, len(builts), f64):
+    for threads, ctas, queue in candidates(total, len(builts)):
         try:
             net = (make_network(threads, ctas, queue) if make_network else
                    instantiate(spec, builts, threads=threads, ctas_per_inst=ctas, queue_mode=queue))

@@ -1,0 +1,56 @@
+"""float32 mode against the float64 reference, per configuration (GPU only).
+
+For each network the float32 device path runs on the same construction as a
+float64 fixture of the reference.  Measured and printed: the first time step
+at which the spike raster differs from the float64 reference's, and the
+largest relative error of v against the float64 oracle at checkpoints before
+that step.  Bar: v within 1e-4 relative at every checkpoint before the first
+divergent spike (after it, the networks are different trajectories).
+"""
+import numpy as np
+import pytest
+
+from brian2_gb300 import workloads as W
+from cases import CASES
+from oracle import oracle_from_built
+from test_gpu_parity import first_divergence
+
+pytestmark = pytest.mark.gpu
+
+# float32 spec, float64 fixture, float32 builder (same construction as the fixture's)
+F32 = {
+    "cuba": ("cuba_f32", "cuba_f64", lambda s: W.build_cuba(s, N=4000, seed=1234)),
+    "cobahh": ("cobahh_f32", "cobahh_f64", lambda s: W.build_cobahh(s, N=4000, seed=1234)),
+    "delays": ("delays_f32", "delays_f64", lambda s: W.build_delays(s, N=10000, K=1000, seed=1234)),
+}
+CHECKPOINTS = (1, 10, 50, 100, 200, 500, 1000, 2000, 5000, 10000)
+
+
+@pytest.mark.parametrize("name", sorted(F32))
+def test_fp32_state_error_and_first_divergence(name, golden):
+    spec32_name, case, build32 = F32[name]
+    spec64_name, build64, steps = CASES[case]
+    meta, z = golden(case)
+    spec32, spec64 = W.load_spec(spec32_name), W.load_spec(spec64_name)
+    net = W.instantiate(spec32, [build32(spec32)], threads=256, ctas_per_inst=4)
+    net.run(steps)
+    i, ts, _ = net.spikes(0, 0)
+    div = first_divergence(i, ts, z["spk_i"], z["spk_ts"])
+    net.close()
+    # state error before the first divergent spike, against the float64 oracle
+    net = W.instantiate(spec32, [build32(spec32)], threads=256, ctas_per_inst=4)
+    orc = oracle_from_built(spec64, build64(spec64))
+    done, errs = 0, {}
+    for c in CHECKPOINTS:
+        if c > steps or (div is not None and c >= div):
+            break
+        net.run(c - done)
+        orc.run(c - done)
+        done = c
+        v32 = net.download(0, "neurongroup", "v").astype(np.float64)
+        v64 = orc.download(0, "v")
+        errs[c] = float((np.abs(v32 - v64) / np.maximum(np.abs(v64), 1e-12)).max())
+    print(f"\n{name} float32 vs float64 reference: spikes {len(i)} vs {len(z['spk_i'])}, "
+          f"first divergent step {div} (of {steps}), max rel v error at checkpoints {errs}")
+    assert errs, "no checkpoint before the first divergence"
+    assert max(errs.values()) < 1e-4, errs
