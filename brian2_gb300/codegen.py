@@ -137,6 +137,32 @@ class _Tables:
         return "\n".join(lines)
 
 
+_LOAD_RE = re.compile(r"^\s*(?:const\s+)?(\w+)\s+(\w+)\s*=\s*(_ptr_array_\w+)\[_idx\];\s*$")
+
+
+def split_loads(code: str):
+    """Brian's vector code starts with one load per variable it reads
+    (``T x = _ptr_array_...[_idx];``).  Returns [(ctype, name, ptr)] of those
+    leading loads and the code that follows them."""
+    lines = (code or "").split("\n")
+    loads, k = [], 0
+    while k < len(lines):
+        ln = lines[k]
+        if not ln.strip():
+            k += 1
+            continue
+        m = _LOAD_RE.match(ln)
+        if not m:
+            break
+        loads.append((m.group(1), m.group(2), m.group(3)))
+        k += 1
+    return loads, "\n".join(lines[k:])
+
+
+def stored_ptrs(code: str):
+    return set(re.findall(r"(_ptr_array_\w+)\[_idx\]\s*=[^=]", code or ""))
+
+
 def render_model(spec: dict) -> str:
     """Returns the complete .cu text for a spec."""
     groups = spec["groups"]
@@ -317,9 +343,10 @@ def render_model(spec: dict) -> str:
     w("")
     w(f"#define B200_NG {NG}")
     w(f"#define B200_MAXV {MAXV}")
-    w("// dynamic shared memory: [state cache | item seg | item off | item src | prefix | tile starts | delays]")
+    w("// dynamic shared memory: [state cache | item seg | item off | item src | item pathway | prefix |")
+    w("//                         tile starts | delays]")
     w("static size_t b200_dyn_smem(int threads, int max_tiles1, int max_w, int state_bytes) {")
-    w("  return (size_t)state_bytes + (size_t)threads * 8 + (size_t)(threads + 1) * 4 + (size_t)threads * 4 +")
+    w("  return (size_t)state_bytes + (size_t)threads * 8 + (size_t)(threads + 1) * 4 + (size_t)threads * 8 +")
     w("         (size_t)2 * B200_NG * max_tiles1 * 4 + (size_t)(3 * max_w + 1) * 4 + 16;")
     w("}")
     w("")
@@ -333,7 +360,8 @@ def render_model(spec: dict) -> str:
     w("  int64_t* const s_item_seg = (int64_t*)(b200_dyn + state_bytes);")
     w("  int* const s_item_off = (int*)(s_item_seg + blockDim.x);")
     w("  int* const s_item_src = s_item_off + blockDim.x + 1;")
-    w("  int* const s_pref_all = s_item_src + blockDim.x;")
+    w("  int* const s_item_q = s_item_src + blockDim.x;")
+    w("  int* const s_pref_all = s_item_q + blockDim.x;")
     w("  int* const s_tst = s_pref_all + B200_NG * max_tiles1;")
     w("  int* const s_nd = s_tst + B200_NG * max_tiles1;")
     w("  int* const s_base = s_nd + max_w;")
@@ -355,7 +383,8 @@ def render_model(spec: dict) -> str:
         n_ = max(ptables[pi][0].size, 1)
         w(f"  __shared__ double s_Sp{pi}[{n_}]; __shared__ float s_Sp{pi}f[{n_}]; __shared__ long long s_Sp{pi}i[{n_}];")
     w("  unsigned gen = 0;")
-    w("  (void)s_nd; (void)s_base; (void)s_ndoff; (void)s_item_seg; (void)s_item_off; (void)s_item_src; (void)s_state;")
+    w("  (void)s_nd; (void)s_base; (void)s_ndoff; (void)s_item_seg; (void)s_item_off; (void)s_item_src; (void)s_item_q;")
+    w("  (void)s_state;")
     w("  for (int pass = 0;; ++pass) {")
     w("    if (threadIdx.x == 0) {")
     w("      if (queue_mode) { s_unit = atomicAdd(work, 1); s_rank = 0; }")
@@ -482,23 +511,52 @@ def render_model(spec: dict) -> str:
         w("          for (int pb = start; pb < end; pb += 32 * (int)blockDim.x) {")
         w("            const int pe = (end - pb < 32 * (int)blockDim.x) ? end : pb + 32 * (int)blockDim.x;")
         w("            const int E = (pe - pb + blockDim.x - 1) / blockDim.x;")
+        # the state loads of up to PF slices are issued before any of them is
+        # computed (each slice is one L2 round trip otherwise)
+        upd_v = bd["update"]["vector"] if bd["update"] is not None else ""
+        thr_v = bd["threshold"]["vector"] if bd["threshold"] is not None else ""
+        upd_loads, upd_rest = split_loads(upd_v)
+        thr_loads, thr_rest = split_loads(thr_v)
+        upd_st = stored_ptrs(upd_v)
+        pf = {}
+        for ct, nm, ptr in upd_loads + [x for x in thr_loads if x[2] not in upd_st]:
+            pf.setdefault(ptr, ct)
+        pfi = {ptr: j for j, ptr in enumerate(pf)}
+        words = sum(max(1, SIZE.get(ct, 8) // 4) for ct in pf.values())
+        PF = max(1, min(4, 16 // max(words, 1)))
         w("            unsigned flags = 0u;")
-        w("#pragma unroll 4")
-        w("            for (int k = 0; k < E; ++k) {")
+        w(f"            for (int k0 = 0; k0 < E; k0 += {PF}) {{")
+        for ptr, j in pfi.items():
+            w(f"              {pf[ptr]} _pf{j}[{PF}];")
+        w("#pragma unroll")
+        w(f"              for (int kq = 0; kq < {PF}; ++kq) {{")
+        w("                const int32_t _idx = pb + (k0 + kq) * (int)blockDim.x + threadIdx.x;")
+        w("                if (k0 + kq < E && _idx < pe) {")
+        for ptr, j in pfi.items():
+            w(f"                  _pf{j}[kq] = {ptr}[_idx];")
+        w("                }")
+        w("              }")
+        w("#pragma unroll")
+        w(f"              for (int kq = 0; kq < {PF}; ++kq) {{")
+        w("              const int k = k0 + kq;")
         w("              const int32_t _idx = pb + k * (int)blockDim.x + threadIdx.x;")
-        w("              if (_idx < pe) {")
+        w("              if (k < E && _idx < pe) {")
         w("                const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
         if bd["update"] is not None:
             w("                {")
             w(_indent(tab.device_loads("update", f32), 18))
             w(extra_ptrs(g.get("update"), 18))
-            w(_indent(bd["update"]["vector"], 18))
+            for ct, nm, ptr in upd_loads:
+                w(f"                  {ct} {nm} = _pf{pfi[ptr]}[kq];")
+            w(_indent(upd_rest, 18))
             w("                }")
         if bd["threshold"] is not None:
             w("                {")
             w(_indent(tab.device_loads("threshold", f32), 18))
             w(extra_ptrs(g.get("threshold"), 18))
-            w(_indent(bd["threshold"]["vector"], 18))
+            for ct, nm, ptr in thr_loads:
+                w(f"                  {ct} {nm} = " + (f"_pf{pfi[ptr]}[kq];" if ptr not in upd_st else f"{ptr}[_idx];"))
+            w(_indent(thr_rest, 18))
             w("                  if (_cond) flags |= 1u << k;")
             if bd["threshold"].get("refractory"):
                 nr = next(v["ptr"] for v in g["vars"] if v["name"] == "not_refractory")
@@ -508,6 +566,7 @@ def render_model(spec: dict) -> str:
                 w(f"                    {ls}[_idx] = _b200_t;")
                 w("                  }")
             w("                }")
+        w("              }")
         w("              }")
         w("            }")
         w("            // order-preserving compaction: counts per (slice k, warp), one block scan")
@@ -601,21 +660,47 @@ def render_model(spec: dict) -> str:
         w("      }")
 
     w("      B200_PHASE(2);")
-    # ---- Phase B: synaptic propagation
+    # ---- Phase B: synaptic propagation, one pass per source group: the items
+    # (delay slot, spike) of all its pathways form one list, so the dependent
+    # loads (ring -> segment bounds -> synapses) of the pathways overlap
+    # consecutive pathways from the same source whose on_pre code touches
+    # disjoint neuron variables: running them interleaved cannot change what
+    # any of them reads, so the reference's pathway-by-pathway order is kept
+    merged = []
     for pi, p in enumerate(paths):
-        tab, blocks = ptables[pi]
-        blk = dict(blocks)["on_pre"]
-        sg, tg = p["src"], p["tgt"]
-        w(f"      // ---- pathway {pi} '{p['name']}': propagation")
+        touched = set(p.get("group_ptrs", {}))
+        last = merged[-1] if merged else None
+        if last and last[0] == p["src"] and not (last[2] & touched):
+            last[1].append(pi)
+            last[2].update(touched)
+        else:
+            merged.append((p["src"], [pi], set(touched)))
+    for sg, pis, _ in merged:
+        L = len(pis)
+
+        def which(kexpr, ind):
+            """q (index into pis) and the local window index kk of item window k."""
+            out = [f"int q = 0, kk = {kexpr};"]
+            for q in range(1, L):
+                out.append(f"if (q == {q - 1} && kk >= W{q - 1}) {{ kk -= W{q - 1}; q = {q}; }}")
+            pexpr = "0"
+            for q in reversed(range(L)):
+                pexpr = f"{pis[q]}" if q == L - 1 else f"(q == {q} ? {pis[q]} : {pexpr})"
+            out.append(f"const b200_pathway_d& PD = I.p[{pexpr}];")
+            return _indent("\n".join(out), ind)
+
+        w(f"      // ---- pathways {', '.join(paths[q]['name'] for q in pis)}: propagation")
         w("      {")
-        w(f"        const b200_pathway_d& PD = I.p[{pi}];")
         w(f"        const b200_group_d& SGD = I.g[{sg}];")
         w(f"        const int* const pref = s_pref_all + {sg} * max_tiles1;")
         w(f"        const int* const tst = s_tst + {sg} * max_tiles1;")
         w(f"        const int32_t* const scr = s_scr[{sg}];")
-        w("        const int W = PD.D - PD.dmin + 1;")
-        w("        for (int k = threadIdx.x; k < W; k += blockDim.x) {")
-        w("          const int d = PD.dmin + k;")
+        for q, pi in enumerate(pis):
+            w(f"        const int W{q} = I.p[{pi}].D - I.p[{pi}].dmin + 1; (void)W{q};")
+        w(f"        const int WT = {' + '.join(f'W{q}' for q in range(L))};")
+        w("        for (int k = threadIdx.x; k < WT; k += blockDim.x) {")
+        w(which("k", 10))
+        w("          const int d = PD.dmin + kk;")
         w("          const int64_t s = ts - d;")
         w("          int n = 0, b = 0;")
         w("          if (s >= 0) {")
@@ -630,34 +715,28 @@ def render_model(spec: dict) -> str:
         w("        __syncthreads();")
         w("        {")
         w("          int carry = 0;")
-        w("          for (int c0 = 0; c0 < W; c0 += blockDim.x) {")
+        w("          for (int c0 = 0; c0 < WT; c0 += blockDim.x) {")
         w("            const int k = c0 + threadIdx.x;")
-        w("            const int x = k < W ? s_nd[k] : 0;")
+        w("            const int x = k < WT ? s_nd[k] : 0;")
         w("            int tot;")
         w("            const int ex = b200_block_exscan(x, s_wsum, &tot);")
-        w("            if (k < W) s_ndoff[k] = carry + ex;")
+        w("            if (k < WT) s_ndoff[k] = carry + ex;")
         w("            carry += tot;")
         w("          }")
-        w("          if (threadIdx.x == 0) s_ndoff[W] = carry;")
+        w("          if (threadIdx.x == 0) s_ndoff[WT] = carry;")
         w("          __syncthreads();")
         w("        }")
-        w("        const int Wtot = s_ndoff[W];")
+        w("        const int Wtot = s_ndoff[WT];")
         w("        const int i0 = (int)((int64_t)Wtot * rank / I.n_cta);")
         w("        const int i1 = (int)((int64_t)Wtot * (rank + 1) / I.n_cta);")
-        w(f"        const double* const _b200_S = s_Sp{pi}; const float* const _b200_Sf = s_Sp{pi}f; const long long* const _b200_Si = s_Sp{pi}i;")
-        for k, v in enumerate(p.get("vars", [])):
-            w(f"        {v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)PD.var[{k}]; (void){v['ptr']};")
-        w(f"        const int32_t* __restrict__ const {p['post_ptr']} = PD.post; (void){p['post_ptr']};")
-        w(f"        const int32_t* __restrict__ const {p['pre_ptr']} = PD.pre; (void){p['pre_ptr']};")
-        for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
-            v = groups[gidx]["vars"][vidx]
-            w(f"        {v['ctype']}* __restrict__ const {ptr} = ({v['ctype']}*)s_gv[{gidx}][{vidx}]; (void){ptr};")
         w("        for (int cb = i0; cb < i1; cb += blockDim.x) {")
         w("          const int it = cb + threadIdx.x;")
         w("          int len = 0;")
         w("          if (it < i1) {")
-        w("            const int k = b200_upper_bound(s_ndoff, W + 1, it) - 1;")
-        w("            const int d = PD.dmin + k, r = it - s_ndoff[k];")
+        w("            const int k = b200_upper_bound(s_ndoff, WT + 1, it) - 1;")
+        w(which("k - 0", 12))
+        w("            const int W = PD.D - PD.dmin + 1;")
+        w("            const int d = PD.dmin + kk, r = it - s_ndoff[k];")
         w("            int32_t src;")
         w("            if (d == 0) {")
         w("              const int pos = s_base[k] + r;")
@@ -666,11 +745,12 @@ def render_model(spec: dict) -> str:
         w("            } else {")
         w("              src = SGD.ring[(int64_t)((ts - d) % SGD.R) * SGD.N + s_base[k] + r];")
         w("            }")
-        w("            const int64_t seg = (int64_t)(src - PD.src_lo) * W + k;")
+        w("            const int64_t seg = (int64_t)(src - PD.src_lo) * W + kk;")
         w("            const int64_t lo = PD.segptr[seg];")
         w("            len = (int)(PD.segptr[seg + 1] - lo);")
         w("            s_item_seg[threadIdx.x] = lo;")
         w("            s_item_src[threadIdx.x] = src;")
+        w("            s_item_q[threadIdx.x] = q;")
         w("          }")
         w("          int E;")
         w("          const int off = b200_block_exscan(len, s_wsum, &E);")
@@ -679,24 +759,38 @@ def render_model(spec: dict) -> str:
         w("          const int nitems = (i1 - cb) < (int)blockDim.x ? (i1 - cb) : (int)blockDim.x;")
         w("          for (int e0 = threadIdx.x; e0 < E; e0 += 4 * (int)blockDim.x) {")
         w("#pragma unroll")
-        w("            for (int q = 0; q < 4; ++q) {")
-        w("              const int e = e0 + q * (int)blockDim.x;")
+        w("            for (int qq = 0; qq < 4; ++qq) {")
+        w("              const int e = e0 + qq * (int)blockDim.x;")
         w("              if (e < E) {")
         w("                const int j = b200_upper_bound(s_item_off, nitems, e) - 1;")
         w("                const int64_t _idx = s_item_seg[j] + (e - s_item_off[j]);")
         w("                const int32_t _b200_pre = s_item_src[j]; (void)_b200_pre;")
         w("                const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
-        w("                {")
-        w(_indent(tab.device_loads("on_pre", f32), 18))
-        w(_indent(blk["vector_device"] if blk.get("vector_device") else blk["vector"], 18))
-        w("                }")
+        w("                const int q = s_item_q[j]; (void)q;")
+        for q, pi in enumerate(pis):
+            p = paths[pi]
+            tab, blocks = ptables[pi]
+            blk = dict(blocks)["on_pre"]
+            w(("                if" if q == 0 else "                else if") + f" (q == {q}) {{  // {p['name']}")
+            w(f"                  const b200_pathway_d& PQ = I.p[{pi}]; (void)PQ;")
+            w(f"                  const double* const _b200_S = s_Sp{pi}; const float* const _b200_Sf = s_Sp{pi}f; const long long* const _b200_Si = s_Sp{pi}i;")
+            for k, v in enumerate(p.get("vars", [])):
+                w(f"                  {v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)PQ.var[{k}]; (void){v['ptr']};")
+            w(f"                  const int32_t* __restrict__ const {p['post_ptr']} = PQ.post; (void){p['post_ptr']};")
+            w(f"                  const int32_t* __restrict__ const {p['pre_ptr']} = PQ.pre; (void){p['pre_ptr']};")
+            for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
+                v = groups[gidx]["vars"][vidx]
+                w(f"                  {v['ctype']}* __restrict__ const {ptr} = ({v['ctype']}*)s_gv[{gidx}][{vidx}]; (void){ptr};")
+            w(_indent(tab.device_loads("on_pre", f32), 18))
+            w(_indent(blk["vector_device"] if blk.get("vector_device") else blk["vector"], 18))
+            w("                }")
         w("              }")
         w("            }")
         w("          }")
         w("          __syncthreads();")
         w("        }")
         w("      }")
-        w(f"      B200_PHASE({3 + pi});")
+        w(f"      B200_PHASE({3 + pis[0]});")
     w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster)) { ok = false; break; }")
     w(f"      B200_PHASE({3 + NP});")
     w("    }  // steps")

@@ -683,8 +683,10 @@ static int b200_prepare(b200_net* n) {
   for (int k = 0; k < n->n_inst; ++k) {
     for (int g = 0; g < M->n_groups; ++g)
       n->max_tiles1 = std::max(n->max_tiles1, (int)n->inst[k].g[g].tile_start.size());
-    for (int p = 0; p < M->n_pathways; ++p)
-      n->max_w = std::max(n->max_w, n->inst[k].p[p].dmax - n->inst[k].p[p].dmin + 1);
+    // pathways of one source may share a delivery pass: their delay windows add up
+    int wsum = 0;
+    for (int p = 0; p < M->n_pathways; ++p) wsum += n->inst[k].p[p].dmax - n->inst[k].p[p].dmin + 1;
+    n->max_w = std::max(n->max_w, wsum);
   }
   // shared-memory state cache of single-CTA instances: the used state
   // variables, the step's spike list and the tile counts
