@@ -104,6 +104,25 @@ class _Tables:
     def size(self):
         return len(self.entries)
 
+    def _load(self, ct, nm, k, single):
+        et = "float" if (single and ct == "double") else ct
+        src = {"double": "_b200_S", "float": "_b200_Sf"}.get(et, "_b200_Si")
+        return f"const {et} {nm} = ({et}){src}[{k}];"
+
+    def const_loads(self, single=False):
+        """The namespace constants (the same values in every table of a model)."""
+        return "\n".join(self._load(ct, nm, k, single) for k, (ct, nm) in enumerate(self.entries[:len(self.consts)]))
+
+    def scalar_loads(self, name, single=False):
+        """The loop-invariant scalars of one block (no constants)."""
+        if name not in self.block_ranges:
+            return ""
+        off, outs = self.block_ranges[name]
+        return "\n".join(self._load(ct, nm, off + k, single) for k, (ct, nm) in enumerate(outs))
+
+    def scalar_names(self, name):
+        return [nm for _, nm in self.block_ranges.get(name, (0, []))[1]]
+
     def device_loads(self, name, single=False):
         """Declarations reading the constants and this block's scalars from the
         typed shared copies of S (_b200_S double, _b200_Sf float, _b200_Si
@@ -240,6 +259,50 @@ def render_model(spec: dict) -> str:
         return sorted(used, key=lambda k: -SIZE[g["vars"][k]["ctype"]])
 
     USED = [used_vars(gi) for gi in range(NG)]
+
+    def owner_payloads():
+        """Owner mode applies when every on_pre only adds, into variables of its
+        target neuron, values computed from synaptic variables and constants.
+        Returns, per pathway, the synaptic variables an event carries (indices
+        into the pathway's variables), or None for the whole model."""
+        if not paths:
+            return None
+        for g in groups:
+            for blk in ("update", "threshold", "reset"):
+                if g.get(blk) and g[blk].get("extra_ptrs"):
+                    return None
+        out = []
+        for p in paths:
+            code = p["on_pre"].get("vector_device") or p["on_pre"].get("vector") or ""
+            loads, rest = split_loads(code)
+            varptr = {v["ptr"]: k for k, v in enumerate(p.get("vars", []))}
+            pay, has_post = [], False
+            for ct, nm, ptr in loads:
+                if ptr == p["post_ptr"] and nm == "_postsynaptic_idx":
+                    has_post = True
+                elif ptr in varptr and SIZE.get(ct) in (4, 8):
+                    pay.append(varptr[ptr])
+                else:
+                    return None
+            if not has_post or len(pay) > 4:
+                return None
+            tgt_ptrs = {ptr for ptr, (gi, vi) in p.get("group_ptrs", {}).items() if gi == p["tgt"]}
+            for ln in rest.split("\n"):
+                ln = ln.strip()
+                if not ln:
+                    continue
+                m = re.match(r"^_b200_atomic_add\(&(\w+)\[_postsynaptic_idx\],\s*(.*)\);$", ln)
+                if not m or m.group(1) not in tgt_ptrs or "_ptr_array" in m.group(2) or "[" in m.group(2):
+                    return None
+            out.append(pay)
+        return out
+
+    PAYLOAD = owner_payloads()
+    OWNER = PAYLOAD is not None
+    # device profile slots: classic kernel A, barrier A, lists, one per pathway,
+    # barrier B; owner kernel update, barrier, lists, push pass 1, batch table +
+    # pass 2, delivery
+    NPH = max(4 + NP, 6)
     MAXV = max(len(g["vars"]) for g in groups)
 
     # ------------------------------------------------------------- model tables
@@ -254,9 +317,13 @@ def render_model(spec: dict) -> str:
     w("static const b200_group_info b200_groups[] = {" + ", ".join(
         f'{{"{g["name"]}", {len(g["vars"])}, b200_g{gi}_vars, b200_g{gi}_kinds, {gtables[gi][0].size}, b200_g{gi}_used}}'
         for gi, g in enumerate(groups)) + "};")
+    for pi, p in enumerate(paths):
+        pay = PAYLOAD[pi] if OWNER else []
+        w(f"static const int b200_p{pi}_payload[] = {{" + (", ".join(str(k) for k in pay) if pay else "0") + "};")
     if paths:
         w("static const b200_pathway_info b200_pathways[] = {" + ", ".join(
-            f'{{"{p["name"]}", {p["src"]}, {p["tgt"]}, {len(p.get("vars", []))}, b200_p{pi}_vars, b200_p{pi}_kinds, {ptables[pi][0].size}}}'
+            f'{{"{p["name"]}", {p["src"]}, {p["tgt"]}, {len(p.get("vars", []))}, b200_p{pi}_vars, b200_p{pi}_kinds, '
+            f'{ptables[pi][0].size}, {len(PAYLOAD[pi]) if OWNER else 0}, b200_p{pi}_payload}}'
             for pi, p in enumerate(paths)) + "};")
     else:
         w("static const b200_pathway_info* const b200_pathways = nullptr;")
@@ -307,15 +374,21 @@ def render_model(spec: dict) -> str:
                 lines.append(f"{v['ctype']}* const {ptr} = ({v['ctype']}*)s_gv[{obj}][{var}]; (void){ptr};")
         return _indent("\n".join(lines), indent)
 
-    def reset_block(gi, indent, tsexpr):
+    def owner_list(gi, tsexpr):
+        """Owner mode: spike list and tile counts of step `tsexpr` in the ring."""
+        return (f"I.g[{gi}].ring + (int64_t)(({tsexpr}) % B200_OWNER_RING) * I.g[{gi}].N",
+                f"I.g[{gi}].ring_prefix + (int64_t)(({tsexpr}) % B200_OWNER_RING) * (I.g[{gi}].n_tiles + 1)")
+
+    def reset_block(gi, indent, tsexpr, owner=False):
         """Reset of the spikes of step `tsexpr` in this CTA's tiles."""
         tab, blocks = gtables[gi]
         bd = dict(blocks)
         if bd["reset"] is None:
             return ""
         g = groups[gi]
+        scr_e, tc_e = owner_list(gi, tsexpr) if owner else (f"s_scr[{gi}]", f"s_tc[{gi}]")
         L = ["{",
-             f"  const int32_t* const scr = s_scr[{gi}]; const int32_t* const tcnt = s_tc[{gi}];",
+             f"  const int32_t* const scr = {scr_e}; const int32_t* const tcnt = {tc_e};",
              f"  const int* const tst = s_tst + {gi} * max_tiles1;",
              f"  const int32_t N = I.g[{gi}].N; (void)N;",
              f"  const double* const _b200_S = s_Sg{gi}; const float* const _b200_Sf = s_Sg{gi}f; const long long* const _b200_Si = s_Sg{gi}i;",
@@ -334,6 +407,149 @@ def render_model(spec: dict) -> str:
              "  }",
              "}"]
         return _indent("\n".join(L), indent)
+
+    def emit_phase_a(owner):
+        """Reset of the previous step, state monitors, update + threshold with
+        ordered compaction of this CTA's tiles."""
+        # ---- Phase A
+        for gi, g in enumerate(groups):
+            tab, blocks = gtables[gi]
+            bd = dict(blocks)
+            w(f"      // ---- group {gi} '{g['name']}': phase A (reset of step ts-1, monitors, update + threshold)")
+            if bd["reset"] is not None:
+                w("      if (ts > ts0) {")
+                w(reset_block(gi, 8, "ts - 1", owner))
+                w("        __syncthreads();")
+                w("      }")
+            w("      {")
+            w(f"        const int32_t N = I.g[{gi}].N; (void)N;")
+            w(f"        const double* const _b200_S = s_Sg{gi}; const float* const _b200_Sf = s_Sg{gi}f; const long long* const _b200_Si = s_Sg{gi}i;")
+            w(gptr_decls(gi, 8, True))
+            if owner:
+                scr_e, tc_e = owner_list(gi, "ts")
+                w(f"        int32_t* const scr = {scr_e}; int32_t* const tcnt = {tc_e};")
+            else:
+                w(f"        int32_t* const scr = s_scr[{gi}]; int32_t* const tcnt = s_tc[{gi}];")
+            w(f"        const int* const tst = s_tst + {gi} * max_tiles1;")
+            for mi, m in enumerate(statemons):
+                if m["group"] != gi:
+                    continue
+                w(f"        {{  // state monitor {mi}: values at the start of the step")
+                w(f"          const b200_statemon_d& SM = I.stm[{mi}];")
+                w(f"          const int lo = tst[s_ut[{gi}][0]], hi = tst[s_ut[{gi}][1]];")
+                w("          double* const row = SM.data + (size_t)(ts - SM.step0) * SM.n_vars * SM.n_rec;")
+                w("          for (int k = threadIdx.x; k < SM.n_rec * SM.n_vars; k += blockDim.x) {")
+                w("            const int r = k % SM.n_rec, v = k / SM.n_rec;")
+                w("            const int idx = SM.idx[r];")
+                w("            if (idx >= lo && idx < hi) {")
+                w("              double val = 0.0;")
+                w("              switch (SM.var_id[v]) {")
+                for k, v in enumerate(g["vars"]):
+                    w(f"                case {k}: val = (double)(({v['ctype']}*)s_gv[{gi}][{k}])[idx]; break;")
+                w("              }")
+                w("              row[k] = val;")
+                w("            }")
+                w("          }")
+                w(f"          if (threadIdx.x == 0) s_stm_n[{mi}] = ts + 1 - SM.step0;")
+                w("        }")
+            # constants and block scalars are loaded once per step, not per neuron
+            upd_sc = set(tab.scalar_names("update")) if bd["update"] is not None else set()
+            thr_sc = set(tab.scalar_names("threshold")) if bd["threshold"] is not None else set()
+            hoist_sc = not (upd_sc & thr_sc)
+            w(_indent(tab.const_loads(f32), 8))
+            if hoist_sc:
+                if bd["update"] is not None:
+                    w(_indent(tab.scalar_loads("update", f32), 8))
+                if bd["threshold"] is not None:
+                    w(_indent(tab.scalar_loads("threshold", f32), 8))
+            w(f"        for (int u = s_ut[{gi}][0]; u < s_ut[{gi}][1]; ++u) {{")
+            w("          const int start = tst[u], end = tst[u + 1];")
+            w("          int cnt = 0;")
+            w("          for (int pb = start; pb < end; pb += 32 * (int)blockDim.x) {")
+            w("            const int pe = (end - pb < 32 * (int)blockDim.x) ? end : pb + 32 * (int)blockDim.x;")
+            w("            const int E = (pe - pb + blockDim.x - 1) / blockDim.x;")
+            # the state loads of up to PF slices are issued before any of them is
+            # computed (each slice is one L2 round trip otherwise)
+            upd_v = bd["update"]["vector"] if bd["update"] is not None else ""
+            thr_v = bd["threshold"]["vector"] if bd["threshold"] is not None else ""
+            upd_loads, upd_rest = split_loads(upd_v)
+            thr_loads, thr_rest = split_loads(thr_v)
+            upd_st = stored_ptrs(upd_v)
+            pf = {}
+            for ct, nm, ptr in upd_loads + [x for x in thr_loads if x[2] not in upd_st]:
+                pf.setdefault(ptr, ct)
+            pfi = {ptr: j for j, ptr in enumerate(pf)}
+            words = sum(max(1, SIZE.get(ct, 8) // 4) for ct in pf.values())
+            PF = max(1, min(4, 16 // max(words, 1)))
+            w("            unsigned flags = 0u;")
+            w(f"            for (int k0 = 0; k0 < E; k0 += {PF}) {{")
+            for ptr, j in pfi.items():
+                w(f"              {pf[ptr]} _pf{j}[{PF}];")
+            w("#pragma unroll")
+            w(f"              for (int kq = 0; kq < {PF}; ++kq) {{")
+            w("                const int32_t _idx = pb + (k0 + kq) * (int)blockDim.x + threadIdx.x;")
+            w("                if (k0 + kq < E && _idx < pe) {")
+            for ptr, j in pfi.items():
+                w(f"                  _pf{j}[kq] = {ptr}[_idx];")
+            w("                }")
+            w("              }")
+            w("#pragma unroll")
+            w(f"              for (int kq = 0; kq < {PF}; ++kq) {{")
+            w("              const int k = k0 + kq;")
+            w("              const int32_t _idx = pb + k * (int)blockDim.x + threadIdx.x;")
+            w("              if (k < E && _idx < pe) {")
+            w("                const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+            if bd["update"] is not None:
+                w("                {")
+                if not hoist_sc:
+                    w(_indent(tab.scalar_loads("update", f32), 18))
+                w(extra_ptrs(g.get("update"), 18))
+                for ct, nm, ptr in upd_loads:
+                    w(f"                  {ct} {nm} = _pf{pfi[ptr]}[kq];")
+                w(_indent(upd_rest, 18))
+                w("                }")
+            if bd["threshold"] is not None:
+                w("                {")
+                if not hoist_sc:
+                    w(_indent(tab.scalar_loads("threshold", f32), 18))
+                w(extra_ptrs(g.get("threshold"), 18))
+                for ct, nm, ptr in thr_loads:
+                    w(f"                  {ct} {nm} = " + (f"_pf{pfi[ptr]}[kq];" if ptr not in upd_st else f"{ptr}[_idx];"))
+                w(_indent(thr_rest, 18))
+                w("                  if (_cond) flags |= 1u << k;")
+                if bd["threshold"].get("refractory"):
+                    nr = next(v["ptr"] for v in g["vars"] if v["name"] == "not_refractory")
+                    ls = next(v["ptr"] for v in g["vars"] if v["name"] == "lastspike")
+                    w("                  if (_cond) {")
+                    w(f"                    {nr}[_idx] = false;")
+                    w(f"                    {ls}[_idx] = _b200_t;")
+                    w("                  }")
+                w("                }")
+            w("              }")
+            w("              }")
+            w("            }")
+            w("            // order-preserving compaction: counts per (slice k, warp), one block scan")
+            w("            for (int k = 0; k < E; ++k) {")
+            w("              const unsigned m = __ballot_sync(0xffffffffu, (flags >> k) & 1u);")
+            w("              if (lane == 0) s_cnt[k * NW + wid] = __popc(m);")
+            w("            }")
+            w("            __syncthreads();")
+            w("            int tot;")
+            w("            const int x = (int)threadIdx.x < E * NW ? s_cnt[threadIdx.x] : 0;")
+            w("            const int ex = b200_block_exscan(x, s_wsum, &tot);")
+            w("            if ((int)threadIdx.x < E * NW) s_cnt[threadIdx.x] = ex;")
+            w("            __syncthreads();")
+            w("            for (int k = 0; k < E; ++k) {")
+            w("              const unsigned m = __ballot_sync(0xffffffffu, (flags >> k) & 1u);")
+            w("              if ((flags >> k) & 1u)")
+            w("                scr[start + cnt + s_cnt[k * NW + wid] + __popc(m & b200_lanemask_lt())] = pb + k * (int)blockDim.x + threadIdx.x;")
+            w("            }")
+            w("            cnt += tot;")
+            w("            __syncthreads();")
+            w("          }")
+            w("          if (threadIdx.x == 0) tcnt[u] = cnt;")
+            w("        }")
+            w("      }")
 
     w("__device__ __forceinline__ int b200_upper_bound(const int* a, int n, int x) {")
     w("  int lo = 0, hi = n;")
@@ -468,129 +684,7 @@ def render_model(spec: dict) -> str:
     w("      const int64_t _b200_ts = ts;")
     w("      if (prof && threadIdx.x == 0) _pt = clock64();")
 
-    # ---- Phase A
-    for gi, g in enumerate(groups):
-        tab, blocks = gtables[gi]
-        bd = dict(blocks)
-        w(f"      // ---- group {gi} '{g['name']}': phase A (reset of step ts-1, monitors, update + threshold)")
-        if bd["reset"] is not None:
-            w("      if (ts > ts0) {")
-            w(reset_block(gi, 8, "ts - 1"))
-            w("        __syncthreads();")
-            w("      }")
-        w("      {")
-        w(f"        const int32_t N = I.g[{gi}].N; (void)N;")
-        w(f"        const double* const _b200_S = s_Sg{gi}; const float* const _b200_Sf = s_Sg{gi}f; const long long* const _b200_Si = s_Sg{gi}i;")
-        w(gptr_decls(gi, 8, True))
-        w(f"        int32_t* const scr = s_scr[{gi}]; int32_t* const tcnt = s_tc[{gi}];")
-        w(f"        const int* const tst = s_tst + {gi} * max_tiles1;")
-        for mi, m in enumerate(statemons):
-            if m["group"] != gi:
-                continue
-            w(f"        {{  // state monitor {mi}: values at the start of the step")
-            w(f"          const b200_statemon_d& SM = I.stm[{mi}];")
-            w(f"          const int lo = tst[s_ut[{gi}][0]], hi = tst[s_ut[{gi}][1]];")
-            w("          double* const row = SM.data + (size_t)(ts - SM.step0) * SM.n_vars * SM.n_rec;")
-            w("          for (int k = threadIdx.x; k < SM.n_rec * SM.n_vars; k += blockDim.x) {")
-            w("            const int r = k % SM.n_rec, v = k / SM.n_rec;")
-            w("            const int idx = SM.idx[r];")
-            w("            if (idx >= lo && idx < hi) {")
-            w("              double val = 0.0;")
-            w("              switch (SM.var_id[v]) {")
-            for k, v in enumerate(g["vars"]):
-                w(f"                case {k}: val = (double)(({v['ctype']}*)s_gv[{gi}][{k}])[idx]; break;")
-            w("              }")
-            w("              row[k] = val;")
-            w("            }")
-            w("          }")
-            w(f"          if (threadIdx.x == 0) s_stm_n[{mi}] = ts + 1 - SM.step0;")
-            w("        }")
-        w(f"        for (int u = s_ut[{gi}][0]; u < s_ut[{gi}][1]; ++u) {{")
-        w("          const int start = tst[u], end = tst[u + 1];")
-        w("          int cnt = 0;")
-        w("          for (int pb = start; pb < end; pb += 32 * (int)blockDim.x) {")
-        w("            const int pe = (end - pb < 32 * (int)blockDim.x) ? end : pb + 32 * (int)blockDim.x;")
-        w("            const int E = (pe - pb + blockDim.x - 1) / blockDim.x;")
-        # the state loads of up to PF slices are issued before any of them is
-        # computed (each slice is one L2 round trip otherwise)
-        upd_v = bd["update"]["vector"] if bd["update"] is not None else ""
-        thr_v = bd["threshold"]["vector"] if bd["threshold"] is not None else ""
-        upd_loads, upd_rest = split_loads(upd_v)
-        thr_loads, thr_rest = split_loads(thr_v)
-        upd_st = stored_ptrs(upd_v)
-        pf = {}
-        for ct, nm, ptr in upd_loads + [x for x in thr_loads if x[2] not in upd_st]:
-            pf.setdefault(ptr, ct)
-        pfi = {ptr: j for j, ptr in enumerate(pf)}
-        words = sum(max(1, SIZE.get(ct, 8) // 4) for ct in pf.values())
-        PF = max(1, min(4, 16 // max(words, 1)))
-        w("            unsigned flags = 0u;")
-        w(f"            for (int k0 = 0; k0 < E; k0 += {PF}) {{")
-        for ptr, j in pfi.items():
-            w(f"              {pf[ptr]} _pf{j}[{PF}];")
-        w("#pragma unroll")
-        w(f"              for (int kq = 0; kq < {PF}; ++kq) {{")
-        w("                const int32_t _idx = pb + (k0 + kq) * (int)blockDim.x + threadIdx.x;")
-        w("                if (k0 + kq < E && _idx < pe) {")
-        for ptr, j in pfi.items():
-            w(f"                  _pf{j}[kq] = {ptr}[_idx];")
-        w("                }")
-        w("              }")
-        w("#pragma unroll")
-        w(f"              for (int kq = 0; kq < {PF}; ++kq) {{")
-        w("              const int k = k0 + kq;")
-        w("              const int32_t _idx = pb + k * (int)blockDim.x + threadIdx.x;")
-        w("              if (k < E && _idx < pe) {")
-        w("                const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
-        if bd["update"] is not None:
-            w("                {")
-            w(_indent(tab.device_loads("update", f32), 18))
-            w(extra_ptrs(g.get("update"), 18))
-            for ct, nm, ptr in upd_loads:
-                w(f"                  {ct} {nm} = _pf{pfi[ptr]}[kq];")
-            w(_indent(upd_rest, 18))
-            w("                }")
-        if bd["threshold"] is not None:
-            w("                {")
-            w(_indent(tab.device_loads("threshold", f32), 18))
-            w(extra_ptrs(g.get("threshold"), 18))
-            for ct, nm, ptr in thr_loads:
-                w(f"                  {ct} {nm} = " + (f"_pf{pfi[ptr]}[kq];" if ptr not in upd_st else f"{ptr}[_idx];"))
-            w(_indent(thr_rest, 18))
-            w("                  if (_cond) flags |= 1u << k;")
-            if bd["threshold"].get("refractory"):
-                nr = next(v["ptr"] for v in g["vars"] if v["name"] == "not_refractory")
-                ls = next(v["ptr"] for v in g["vars"] if v["name"] == "lastspike")
-                w("                  if (_cond) {")
-                w(f"                    {nr}[_idx] = false;")
-                w(f"                    {ls}[_idx] = _b200_t;")
-                w("                  }")
-            w("                }")
-        w("              }")
-        w("              }")
-        w("            }")
-        w("            // order-preserving compaction: counts per (slice k, warp), one block scan")
-        w("            for (int k = 0; k < E; ++k) {")
-        w("              const unsigned m = __ballot_sync(0xffffffffu, (flags >> k) & 1u);")
-        w("              if (lane == 0) s_cnt[k * NW + wid] = __popc(m);")
-        w("            }")
-        w("            __syncthreads();")
-        w("            int tot;")
-        w("            const int x = (int)threadIdx.x < E * NW ? s_cnt[threadIdx.x] : 0;")
-        w("            const int ex = b200_block_exscan(x, s_wsum, &tot);")
-        w("            if ((int)threadIdx.x < E * NW) s_cnt[threadIdx.x] = ex;")
-        w("            __syncthreads();")
-        w("            for (int k = 0; k < E; ++k) {")
-        w("              const unsigned m = __ballot_sync(0xffffffffu, (flags >> k) & 1u);")
-        w("              if ((flags >> k) & 1u)")
-        w("                scr[start + cnt + s_cnt[k * NW + wid] + __popc(m & b200_lanemask_lt())] = pb + k * (int)blockDim.x + threadIdx.x;")
-        w("            }")
-        w("            cnt += tot;")
-        w("            __syncthreads();")
-        w("          }")
-        w("          if (threadIdx.x == 0) tcnt[u] = cnt;")
-        w("        }")
-        w("      }")
+    emit_phase_a(False)
     w("      B200_PHASE(0);")
     w("      // test hook: CTA `fault_rank` leaves without arriving, the others must time out")
     w("      if (rank == fault_rank && ts == ts0) { ok = false; break; }")
@@ -691,6 +785,9 @@ def render_model(spec: dict) -> str:
 
         w(f"      // ---- pathways {', '.join(paths[q]['name'] for q in pis)}: propagation")
         w("      {")
+        w(f"        const double* const _b200_S = s_Sp{pis[0]}; const float* const _b200_Sf = s_Sp{pis[0]}f; const long long* const _b200_Si = s_Sp{pis[0]}i;")
+        w("        (void)_b200_S; (void)_b200_Sf; (void)_b200_Si;")
+        w(_indent(ptables[pis[0]][0].const_loads(f32), 8))
         w(f"        const b200_group_d& SGD = I.g[{sg}];")
         w(f"        const int* const pref = s_pref_all + {sg} * max_tiles1;")
         w(f"        const int* const tst = s_tst + {sg} * max_tiles1;")
@@ -781,7 +878,7 @@ def render_model(spec: dict) -> str:
             for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
                 v = groups[gidx]["vars"][vidx]
                 w(f"                  {v['ctype']}* __restrict__ const {ptr} = ({v['ctype']}*)s_gv[{gidx}][{vidx}]; (void){ptr};")
-            w(_indent(tab.device_loads("on_pre", f32), 18))
+            w(_indent(tab.scalar_loads("on_pre", f32), 18))
             w(_indent(blk["vector_device"] if blk.get("vector_device") else blk["vector"], 18))
             w("                }")
         w("              }")
@@ -795,7 +892,7 @@ def render_model(spec: dict) -> str:
     w(f"      B200_PHASE({3 + NP});")
     w("    }  // steps")
     w(f"    if (prof && threadIdx.x == 0)")
-    w(f"      for (int q = 0; q < {4 + NP}; ++q) atomicAdd(&prof[(size_t)unit * {4 + NP} + q], _pacc[q]);")
+    w(f"      for (int q = 0; q < {4 + NP}; ++q) atomicAdd(&prof[(size_t)unit * {NPH} + q], _pacc[q]);")
     w("#undef B200_PHASE")
 
     # ---- end of launch: apply the reset of the last executed step, write back the cache
@@ -826,19 +923,558 @@ def render_model(spec: dict) -> str:
     w("}")
     w("")
 
+    # ------------------------------------------------------------- owner-mode kernel
+    def emit_owner_kernel():
+        """Owner mode: each CTA of an instance owns the target neurons of its
+        tiles and is the only one to deliver into them.  A step is
+        update+threshold (own tiles, spike list published in the ring) -> split
+        barrier -> push of the spikes of step ts-lag into per-CTA event FIFOs
+        (delay 0: applied at once) -> delivery of the events due at ts."""
+        merged = []
+        for pi, p in enumerate(paths):
+            touched = set(p.get("group_ptrs", {}))
+            last = merged[-1] if merged else None
+            if last and last[0] == p["src"] and not (last[2] & touched):
+                last[1].append(pi)
+                last[2].update(touched)
+            else:
+                merged.append((p["src"], [pi], set(touched)))
+
+        def body_decls(pi, ind):
+            """Declarations the on_pre body of pathway pi needs (owner arrays)."""
+            p = paths[pi]
+            L = [f"const b200_pathway_d& PQ = I.p[{pi}]; (void)PQ;",
+                 f"const double* const _b200_S = s_Sp{pi}; const float* const _b200_Sf = s_Sp{pi}f; const long long* const _b200_Si = s_Sp{pi}i;"]
+            for k, v in enumerate(p.get("vars", [])):
+                L.append(f"{v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)PQ.var[{k}]; (void){v['ptr']};")
+            L.append(f"const int32_t* __restrict__ const {p['post_ptr']} = PQ.post; (void){p['post_ptr']};")
+            for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
+                v = groups[gidx]["vars"][vidx]
+                L.append(f"{v['ctype']}* const {ptr} = ({v['ctype']}*)s_gv[{gidx}][{vidx}]; (void){ptr};")
+            tab, blocks = ptables[pi]
+            L.append(tab.scalar_loads("on_pre", f32))
+            L.append("(void)_b200_S; (void)_b200_Sf; (void)_b200_Si;")
+            return _indent("\n".join(L), ind)
+
+        def body_code(pi):
+            p = paths[pi]
+            blk = dict(ptables[pi][1])["on_pre"]
+            return blk["vector_device"] if blk.get("vector_device") else blk["vector"]
+
+        def fifo_body(pi, ind):
+            """on_pre applied to the FIFO record `rec` (loads bound to the record)."""
+            p = paths[pi]
+            loads, rest = split_loads(body_code(pi))
+            varptr = {v["ptr"]: k for k, v in enumerate(p.get("vars", []))}
+            L = []
+            for ct, nm, ptr in loads:
+                if ptr == p["post_ptr"]:
+                    L.append(f"const {ct} {nm} = ({ct})PQ.ev.tgt[rbase + rec];")
+                else:
+                    m = PAYLOAD[pi].index(varptr[ptr])
+                    L.append(f"const {ct} {nm} = (({ct}*)PQ.ev.pay[{m}])[rbase + rec];")
+            L.append(rest)
+            return _indent("\n".join(L), ind)
+
+        def fifo_store(pi, ind):
+            """pass 2: the record of synapse `syn` at FIFO position `rec`."""
+            p = paths[pi]
+            L = ["PQ.ev.tgt[rbase + rec] = PQ.post[syn];"]
+            for m, k in enumerate(PAYLOAD[pi]):
+                ct = p["vars"][k]["ctype"]
+                L.append(f"(({ct}*)PQ.ev.pay[{m}])[rbase + rec] = (({ct}*)PQ.var[{k}])[syn];")
+            return _indent("\n".join(L), ind)
+
+        def qdispatch(pis, ind, fn):
+            """if (q == 0) { fn(pi0) } else if ... over the pathways of a group."""
+            L = []
+            for q, pi in enumerate(pis):
+                L.append(("if" if q == 0 else "else if") + f" (q == {q}) {{  // {paths[pi]['name']}")
+                L.append(fn(pi))
+                L.append("}")
+            return _indent("\n".join(L), ind)
+
+        w("static size_t b200_dyn_smem_owner(int threads, int max_tiles1, int max_w, int state_bytes) {")
+        w("  return b200_dyn_smem(threads, max_tiles1, max_w, state_bytes) + (size_t)max_w * 8 + (size_t)(max_w + 1) * 4;")
+        w("}")
+        w("")
+        w("template <int MAXT, int MINB>")
+        w("__global__ void __launch_bounds__(MAXT, MINB) b200_owner_kernel(")
+        w("    const b200_inst_d* __restrict__ insts, const int2* __restrict__ cta_map, int n_inst,")
+        w("    int queue_mode, int* work, int64_t max_steps, uint64_t limit_ns, int max_tiles1, int max_w,")
+        w("    int fault_rank, int state_bytes, unsigned long long* __restrict__ prof, int cluster) {")
+        w("  (void)queue_mode; (void)work;")
+        w("  extern __shared__ __align__(16) unsigned char b200_dyn[];")
+        w("  unsigned char* const s_state = b200_dyn;")
+        w("  int64_t* const s_item_seg = (int64_t*)(b200_dyn + state_bytes);  // [threads]")
+        w("  int64_t* const s_wbase = s_item_seg + blockDim.x;                   // [max_w] first record of each window")
+        w("  int* const s_item_off = (int*)(s_wbase + max_w);                    // [threads + 1]")
+        w("  int* const s_item_src = s_item_off + blockDim.x + 1;                // [threads]")
+        w("  int* const s_item_q = s_item_src + blockDim.x;                      // [threads]")
+        w("  int* const s_pref_all = s_item_q + blockDim.x;                      // [NG * max_tiles1]")
+        w("  int* const s_tst = s_pref_all + B200_NG * max_tiles1;               // [NG * max_tiles1]")
+        w("  int* const s_nd = s_tst + B200_NG * max_tiles1;                     // [max_w] per-delay counts")
+        w("  int* const s_base = s_nd + max_w;                                   // [max_w + 1] batch offsets")
+        w("  int* const s_ndoff = s_base + max_w + 1;                            // [max_w + 1] window offsets")
+        w("  __shared__ __align__(16) b200_inst_d I;")
+        w("  __shared__ int s_wsum[B200_MAX_WARPS + 1];")
+        w("  __shared__ int s_cnt[B200_MAX_THREADS];")
+        w("  __shared__ int s_unit, s_rank, s_flag, s_cache;")
+        w("  __shared__ long long s_mon_n[B200_MAX_SPKMON];")
+        w("  __shared__ long long s_stm_n[B200_MAX_STATEMON];")
+        w("  __shared__ void* s_gv[B200_NG][B200_MAXV];")
+        w("  __shared__ int s_ut[B200_NG][2];")
+        w("  __shared__ int s_own[B200_NG][2];")
+        w(f"  __shared__ long long s_head[{max(NP, 1)}], s_tail[{max(NP, 1)}];")
+        w(f"  __shared__ int s_qoff[{max(NP, 1) + 1}], s_skip[{max(NP, 1)}];")
+        for gi in range(NG):
+            n_ = max(gtables[gi][0].size, 1)
+            w(f"  __shared__ double s_Sg{gi}[{n_}]; __shared__ float s_Sg{gi}f[{n_}]; __shared__ long long s_Sg{gi}i[{n_}];")
+        for pi in range(NP):
+            n_ = max(ptables[pi][0].size, 1)
+            w(f"  __shared__ double s_Sp{pi}[{n_}]; __shared__ float s_Sp{pi}f[{n_}]; __shared__ long long s_Sp{pi}i[{n_}];")
+        w("  (void)s_item_src; (void)s_state;")
+        w("  for (int pass = 0;; ++pass) {")
+        w("    if (threadIdx.x == 0) {")
+        w("      if (pass == 0) { const int2 m = cta_map[blockIdx.x]; s_unit = m.x; s_rank = m.y; }")
+        w("      else s_unit = n_inst;")
+        w("    }")
+        w("    __syncthreads();")
+        w("    const int unit = s_unit, rank = s_rank;")
+        w("    if (unit >= n_inst) break;")
+        w("    {")
+        w("      const long long* src = (const long long*)&insts[unit];")
+        w("      long long* dst = (long long*)&I;")
+        w("      for (int k = threadIdx.x; k < (int)(sizeof(b200_inst_d) / 8); k += blockDim.x) dst[k] = src[k];")
+        w("    }")
+        w("    __syncthreads();")
+        w("    if (threadIdx.x == 0) {")
+        for m in range(len(spkmons)):
+            w(f"      s_mon_n[{m}] = *((volatile long long*)I.sm[{m}].n);")
+        for m in range(len(statemons)):
+            w(f"      s_stm_n[{m}] = *((volatile long long*)I.stm[{m}].n);")
+        w("      const int cache = (I.cache_bytes > 0 && I.cache_bytes <= state_bytes) ? 1 : 0;")
+        w("      s_cache = cache;")
+        w("      size_t off = 0;")
+        for gi, g in enumerate(groups):
+            w(f"      s_ut[{gi}][0] = I.g[{gi}].cta_tile[rank]; s_ut[{gi}][1] = I.g[{gi}].cta_tile[rank + 1];")
+            w(f"      s_own[{gi}][0] = I.g[{gi}].tile_start[s_ut[{gi}][0]]; s_own[{gi}][1] = I.g[{gi}].tile_start[s_ut[{gi}][1]];")
+            for k in range(len(g["vars"])):
+                w(f"      s_gv[{gi}][{k}] = I.g[{gi}].var[{k}];")
+            w("      if (cache) {  // own neurons only: pointers offset so that global indices address them")
+            for k in USED[gi]:
+                sz = SIZE[g["vars"][k]["ctype"]]
+                w(f"        s_gv[{gi}][{k}] = (void*)(s_state + off - (size_t)s_own[{gi}][0] * {sz});")
+                w(f"        off += ((size_t)(s_own[{gi}][1] - s_own[{gi}][0]) * {sz} + 15) & ~(size_t)15;")
+            w("      }")
+        for pi in range(NP):
+            w(f"      if (I.p[{pi}].D > 0) {{ s_head[{pi}] = I.p[{pi}].ev.state[2 * rank]; s_tail[{pi}] = I.p[{pi}].ev.state[2 * rank + 1]; }}")
+        w("    }")
+        w("    __syncthreads();")
+        for gi in range(NG):
+            w(f"    for (int u = threadIdx.x; u <= I.g[{gi}].n_tiles; u += blockDim.x) s_tst[{gi} * max_tiles1 + u] = I.g[{gi}].tile_start[u];")
+        for gi in range(NG):
+            w(f"    for (int k = threadIdx.x; k < {gtables[gi][0].size}; k += blockDim.x) {{")
+            w(f"      const double x = I.g[{gi}].S[k]; s_Sg{gi}[k] = x; s_Sg{gi}f[k] = (float)x; s_Sg{gi}i[k] = (long long)x;")
+            w("    }")
+        for pi in range(NP):
+            w(f"    for (int k = threadIdx.x; k < {ptables[pi][0].size}; k += blockDim.x) {{")
+            w(f"      const double x = I.p[{pi}].S[k]; s_Sp{pi}[k] = x; s_Sp{pi}f[k] = (float)x; s_Sp{pi}i[k] = (long long)x;")
+            w("    }")
+        w("    if (s_cache) {  // the owned neurons' state lives in shared memory for the launch")
+        for gi, g in enumerate(groups):
+            for k in USED[gi]:
+                sz = SIZE[g["vars"][k]["ctype"]]
+                w(f"      b200_copy_bytes((char*)s_gv[{gi}][{k}] + (size_t)s_own[{gi}][0] * {sz}, (const char*)I.g[{gi}].var[{k}] + (size_t)s_own[{gi}][0] * {sz},")
+                w(f"                      (size_t)(s_own[{gi}][1] - s_own[{gi}][0]) * {sz});")
+        w("    }")
+        w("    __syncthreads();")
+        w("    const int64_t ts0 = I.ts;")
+        w("    const int64_t ts_stop = (I.ts_end < ts0 + max_steps) ? I.ts_end : ts0 + max_steps;")
+        w("    const double _b200_dt = I.dt;")
+        w("    int64_t ts = ts0;")
+        w("    bool ok = true, pend = false;")
+        w("    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, NW = blockDim.x >> 5;")
+        w("    (void)lane; (void)wid; (void)NW;")
+        w(f"    unsigned long long _pt = 0, _pacc[{NPH}];")
+        w(f"    for (int q = 0; q < {NPH}; ++q) _pacc[q] = 0;")
+        w("#define B200_PHASE(q) do { if (prof && threadIdx.x == 0) { const unsigned long long _c = clock64(); _pacc[q] += _c - _pt; _pt = _c; } } while (0)")
+
+        def emit_lists(tsexpr, record_mon, ind):
+            """Tile prefix of the spikes of step `tsexpr` for every group, and
+            (if `record_mon`) the spike and rate monitors of that step."""
+            sp = " " * ind
+            for gi, g in enumerate(groups):
+                scr_e, tc_e = owner_list(gi, tsexpr)
+                w(sp + "{")
+                w(sp + f"  const int32_t* const lst = {scr_e}; const int32_t* const tcnt = {tc_e};")
+                w(sp + f"  int* const pref = s_pref_all + {gi} * max_tiles1;")
+                w(sp + f"  const int* const tst = s_tst + {gi} * max_tiles1;")
+                w(sp + f"  const int nt = I.g[{gi}].n_tiles;")
+                w(sp + "  int carry = 0;")
+                w(sp + "  for (int c0 = 0; c0 < nt; c0 += blockDim.x) {")
+                w(sp + "    const int u = c0 + threadIdx.x;")
+                w(sp + "    const int x = u < nt ? tcnt[u] : 0;")
+                w(sp + "    int tot;")
+                w(sp + "    const int ex = b200_block_exscan(x, s_wsum, &tot);")
+                w(sp + "    if (u < nt) pref[u] = carry + ex;")
+                w(sp + "    carry += tot;")
+                w(sp + "  }")
+                w(sp + "  if (threadIdx.x == 0) pref[nt] = carry;")
+                w(sp + "  __syncthreads();")
+                w(sp + "  (void)lst; (void)tst;")
+                for mi, m in enumerate(spkmons):
+                    if m["group"] != gi:
+                        continue
+                    w(sp + f"  if ({record_mon}) {{  // spike monitor {mi}")
+                    w(sp + f"    const b200_spkmon_d& SM = I.sm[{mi}];")
+                    w(sp + f"    const long long mbase = s_mon_n[{mi}] - pref[SM.tile_lo];")
+                    w(sp + f"    const int a = s_ut[{gi}][0] > SM.tile_lo ? s_ut[{gi}][0] : SM.tile_lo;")
+                    w(sp + f"    const int b = s_ut[{gi}][1] < SM.tile_hi ? s_ut[{gi}][1] : SM.tile_hi;")
+                    w(sp + "    for (int u = a; u < b; ++u) {")
+                    w(sp + "      const int cnt = pref[u + 1] - pref[u], base = tst[u];")
+                    w(sp + "      for (int j = threadIdx.x; j < cnt; j += blockDim.x) {")
+                    w(sp + "        const int idx = lst[base + j];")
+                    w(sp + "        const long long pos = mbase + pref[u] + j;")
+                    w(sp + "        SM.i[pos] = idx - SM.lo;")
+                    w(sp + f"        SM.ts[pos] = (int32_t)({tsexpr});")
+                    w(sp + "        SM.count[idx - SM.lo] += 1;")
+                    w(sp + "      }")
+                    w(sp + "    }")
+                    w(sp + "    __syncthreads();")
+                    w(sp + f"    if (threadIdx.x == 0) s_mon_n[{mi}] += pref[SM.tile_hi] - pref[SM.tile_lo];")
+                    w(sp + "  }")
+                for mi, m in enumerate(ratemons):
+                    if m["group"] != gi:
+                        continue
+                    w(sp + f"  if (({record_mon}) && rank == 0 && threadIdx.x == 0) {{  // rate monitor {mi}")
+                    w(sp + f"    const b200_ratemon_d& RM = I.rm[{mi}];")
+                    w(sp + f"    RM.cnt[({tsexpr}) - RM.step0] = pref[RM.tile_hi] - pref[RM.tile_lo];")
+                    w(sp + "  }")
+                w(sp + "}")
+            w(sp + "__syncthreads();")
+
+        w("    for (; ts < ts_stop; ++ts) {")
+        w("      if (threadIdx.x == 0) {")
+        w("        int st = 0;")
+        for m in range(len(spkmons)):
+            w(f"        if (s_mon_n[{m}] + 2 * (long long)(I.sm[{m}].hi - I.sm[{m}].lo) > I.sm[{m}].cap) st = 1;")
+        w("        s_flag = st;")
+        w("      }")
+        w("      __syncthreads();")
+        w("      if (s_flag) break;")
+        w("      const double _b200_t = (double)ts * _b200_dt;")
+        w("      const int64_t _b200_ts = ts;")
+        w("      if (prof && threadIdx.x == 0) _pt = clock64();")
+        emit_phase_a(True)
+        w("      B200_PHASE(0);")
+        w("      // test hook: CTA `fault_rank` leaves without arriving, the others must time out")
+        w("      if (rank == fault_rank && ts == ts0) { ok = false; pend = false; break; }")
+        w("      // split barrier: lag 1 waits for the previous step's spikes (arrived long ago)")
+        w("      if (I.lag) {")
+        w("        if (pend && !b200_owner_wait(I, ts - 1, limit_ns, cluster)) { ok = false; pend = false; break; }")
+        w("        b200_owner_arrive(I, cluster);")
+        w("        pend = true;")
+        w("      } else {")
+        w("        b200_owner_arrive(I, cluster);")
+        w("        if (!b200_owner_wait(I, ts, limit_ns, cluster)) { ok = false; break; }")
+        w("      }")
+        w("      B200_PHASE(1);")
+        w("      const int64_t s_step = ts - I.lag;  // the step whose spikes are pushed now")
+        w("      if (s_step >= 0) {")
+        emit_lists("s_step", "s_step >= ts0", 8)
+        w("      }")
+        w("      B200_PHASE(2);")
+        for sg, pis, _ in merged:
+            L = len(pis)
+            w(f"      // ---- pathways {', '.join(paths[q]['name'] for q in pis)}: push and delivery")
+            w("      {")
+            w(f"        const double* const _b200_S = s_Sp{pis[0]}; const float* const _b200_Sf = s_Sp{pis[0]}f; const long long* const _b200_Si = s_Sp{pis[0]}i;")
+            w("        (void)_b200_S; (void)_b200_Sf; (void)_b200_Si;")
+            w(_indent(ptables[pis[0]][0].const_loads(f32), 8))
+            w(f"        const b200_group_d& SGD = I.g[{sg}];")
+            w(f"        const int* const pref = s_pref_all + {sg} * max_tiles1;")
+            w(f"        const int* const tst = s_tst + {sg} * max_tiles1;")
+            w(f"        const int32_t* const lst = SGD.ring + (int64_t)((s_step >= 0 ? s_step : 0) % B200_OWNER_RING) * SGD.N;")
+            for q, pi in enumerate(pis):
+                w(f"        const int W{q} = I.p[{pi}].D > 0 ? I.p[{pi}].D - I.p[{pi}].dmin + 1 : 0;")
+            w(f"        const int WT = {' + '.join(f'W{q}' for q in range(L))};")
+            w("        if (threadIdx.x == 0) {")
+            w("          int acc = 0;")
+            for q, pi in enumerate(pis):
+                w(f"          s_qoff[{q}] = acc;")
+                w(f"          if (s_step >= 0) acc += pref[I.p[{pi}].tile_hi] - pref[I.p[{pi}].tile_lo];")
+            w(f"          s_qoff[{L}] = acc;")
+            w("        }")
+            w("        for (int k = threadIdx.x; k < WT; k += blockDim.x) s_nd[k] = 0;")
+            w("        __syncthreads();")
+            w(f"        const int NI = s_qoff[{L}];")
+
+            def window_of(kexpr, ind):
+                """q and kk (delay index) of FIFO window k (pathways with D > 0)."""
+                out = [f"int q = 0, kk = {kexpr};"]
+                for q in range(1, L):
+                    out.append(f"if (q == {q - 1} && kk >= W{q - 1}) {{ kk -= W{q - 1}; q = {q}; }}")
+                return _indent("\n".join(out), ind)
+
+            koff = " + ".join(["0"] + [f"W{q}" for q in range(L)])
+
+            def koff_of(q):
+                return "(" + " + ".join(["0"] + [f"W{x}" for x in range(q)]) + ")"
+
+            def traverse(pass_no):
+                """Items (spike of step s_step, pathway) -> owner segments -> events."""
+                w("        for (int cb = 0; cb < NI; cb += blockDim.x) {")
+                w("          const int it = cb + threadIdx.x;")
+                w("          int len = 0;")
+                w("          if (it < NI) {")
+                w("            int q = 0;")
+                for q in range(1, L):
+                    w(f"            if (it >= s_qoff[{q}]) q = {q};")
+                pexpr = f"{pis[L - 1]}"
+                for q in reversed(range(L - 1)):
+                    pexpr = f"(q == {q} ? {pis[q]} : {pexpr})"
+                w(f"            const b200_pathway_d& PD = I.p[{pexpr}];")
+                w("            const int pos = it - s_qoff[q] + pref[PD.tile_lo];")
+                w(f"            const int u = b200_upper_bound(pref, I.g[{sg}].n_tiles + 1, pos) - 1;")
+                w("            const int32_t src = lst[tst[u] + pos - pref[u]];")
+                w("            const int64_t sg_ = (int64_t)(src - PD.src_lo) * I.n_cta + rank;")
+                w("            const int64_t lo = PD.segptr[sg_];")
+                w("            len = (int)(PD.segptr[sg_ + 1] - lo);")
+                w("            s_item_seg[threadIdx.x] = lo;")
+                w("            s_item_q[threadIdx.x] = q;")
+                w("          }")
+                w("          int E;")
+                w("          const int eoff = b200_block_exscan(len, s_wsum, &E);")
+                w("          s_item_off[threadIdx.x] = eoff;")
+                w("          __syncthreads();")
+                w("          const int nitems = (NI - cb) < (int)blockDim.x ? (NI - cb) : (int)blockDim.x;")
+                w("          for (int e0 = threadIdx.x; e0 < E; e0 += 4 * (int)blockDim.x) {")
+                w("#pragma unroll")
+                w("            for (int qq = 0; qq < 4; ++qq) {")
+                w("              const int e = e0 + qq * (int)blockDim.x;")
+                w("              if (e < E) {")
+                w("                const int j = b200_upper_bound(s_item_off, nitems, e) - 1;")
+                w("                const int64_t syn = s_item_seg[j] + (e - s_item_off[j]);")
+                w("                const int q = s_item_q[j];")
+                for q, pi in enumerate(pis):
+                    w(("                if" if q == 0 else "                else if") + f" (q == {q}) {{  // {paths[pi]['name']}")
+                    if pass_no == 1:
+                        w(f"                  if (I.p[{pi}].D == 0) {{  // no delay: applied now")
+                        w("                    const int64_t _idx = syn; const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+                        w(body_decls(pi, 20))
+                        w(_indent(body_code(pi), 20))
+                        w("                  } else {")
+                        w(f"                    atomicAdd(&s_nd[{koff_of(q)} + (int)I.p[{pi}].odelay[syn] - I.p[{pi}].dmin], 1);")
+                        w("                  }")
+                    else:
+                        w(f"                  if (I.p[{pi}].D > 0 && !s_skip[{pi}]) {{")
+                        w(f"                    const b200_pathway_d& PQ = I.p[{pi}];")
+                        w(f"                    const int k = {koff_of(q)} + (int)PQ.odelay[syn] - PQ.dmin;")
+                        w(f"                    const int64_t p_ = (int64_t)(s_base[k] - s_base[{koff_of(q)}]) + atomicAdd(&s_nd[k], 1);")
+                        w("                    const int64_t rec = (s_head[" + str(pi) + "] + p_) & (PQ.ev.cap - 1);")
+                        w("                    const int64_t rbase = (int64_t)rank * PQ.ev.cap;")
+                        w(fifo_store(pi, 20))
+                        w("                  }")
+                    w("                }")
+                w("              }")
+                w("            }")
+                w("          }")
+                w("          __syncthreads();")
+                w("        }")
+
+            w("        // pass 1: events without delay are applied, the others counted per delay")
+            traverse(1)
+            w("        B200_PHASE(3);")
+            w("        if (WT > 0) {")
+            w("          // batch offsets (exclusive, per pathway) and the FIFO capacity check")
+            w("          int carry = 0;")
+            w("          for (int c0 = 0; c0 < WT; c0 += blockDim.x) {")
+            w("            const int k = c0 + threadIdx.x;")
+            w("            const int x = k < WT ? s_nd[k] : 0;")
+            w("            int tot;")
+            w("            const int ex = b200_block_exscan(x, s_wsum, &tot);")
+            w("            if (k < WT) s_base[k] = carry + ex;")
+            w("            carry += tot;")
+            w("          }")
+            w("          if (threadIdx.x == 0) s_base[WT] = carry;")
+            w("          __syncthreads();")
+            w("          // a batch that does not fit is dropped and the instance status set: every")
+            w("          // CTA keeps the same barrier sequence, the host reports the error")
+            w("          if (threadIdx.x == 0) {")
+            for q, pi in enumerate(pis):
+                w(f"            if (I.p[{pi}].D > 0) {{")
+                w(f"              const long long nq = s_base[{koff_of(q)} + W{q}] - s_base[{koff_of(q)}];")
+                w(f"              s_skip[{pi}] = s_step < 0 ? 1 : 0;")
+                w(f"              if (s_step >= 0 && s_head[{pi}] + nq - s_tail[{pi}] > I.p[{pi}].ev.cap) {{")
+                w(f"                atomicCAS(I.status, 0, B200_ERR_EVENT_OVERFLOW); s_skip[{pi}] = 1;")
+                w("              }")
+                w("            }")
+            w("          }")
+            w("          __syncthreads();")
+            w("          if (s_step >= 0) {")
+            for q, pi in enumerate(pis):
+                w(f"            if (I.p[{pi}].D > 0) {{  // batch table entry of step s_step")
+                w(f"              const b200_fifo_d& F = I.p[{pi}].ev;")
+                w("              const int b = (int)(s_step % F.RB);")
+                w("              const int64_t row = (int64_t)rank * F.RB + b;")
+                w(f"              for (int kk = threadIdx.x; kk <= W{q}; kk += blockDim.x)")
+                w(f"                F.off[row * (F.W + 1) + kk] = s_skip[{pi}] ? 0 : s_base[{koff_of(q)} + kk] - s_base[{koff_of(q)}];")
+                w(f"              if (threadIdx.x == 0) {{ F.base[row] = s_head[{pi}]; F.tag[row] = s_step; }}")
+                w("            }")
+            w("          }")
+            w("          for (int k = threadIdx.x; k < WT; k += blockDim.x) s_nd[k] = 0;")
+            w("          __syncthreads();")
+            w("          // pass 2: the records, in delay order, at the FIFO head")
+            traverse(2)
+            w("          if (threadIdx.x == 0 && s_step >= 0) {")
+            for q, pi in enumerate(pis):
+                w(f"            if (I.p[{pi}].D > 0 && !s_skip[{pi}]) s_head[{pi}] += s_base[{koff_of(q)} + W{q}] - s_base[{koff_of(q)}];")
+            w("          }")
+            w("          B200_PHASE(4);")
+            w("          // delivery of the events due at ts: window (pathway, delay d) is the")
+            w("          // part of the batch of step ts - d with that delay")
+            w("          for (int k = threadIdx.x; k < WT; k += blockDim.x) {")
+            w(window_of("k", 12))
+            pexpr = f"{pis[L - 1]}"
+            for q in reversed(range(L - 1)):
+                pexpr = f"(q == {q} ? {pis[q]} : {pexpr})"
+            w(f"            const b200_pathway_d& PD = I.p[{pexpr}];")
+            w("            const int64_t sb = ts - (PD.dmin + kk);")
+            w("            int n = 0;")
+            w("            int64_t lo = 0;")
+            w("            if (sb >= 0) {")
+            w("              const int64_t row = (int64_t)rank * PD.ev.RB + (int)(sb % PD.ev.RB);")
+            w("              if (PD.ev.tag[row] == sb) {")
+            w("                const int32_t* o = PD.ev.off + row * (PD.ev.W + 1);")
+            w("                lo = PD.ev.base[row] + o[kk];")
+            w("                n = o[kk + 1] - o[kk];")
+            w("              }")
+            w("            }")
+            w("            s_nd[k] = n; s_wbase[k] = lo;")
+            w("          }")
+            w("          __syncthreads();")
+            w("          {")
+            w("            int carry2 = 0;")
+            w("            for (int c0 = 0; c0 < WT; c0 += blockDim.x) {")
+            w("              const int k = c0 + threadIdx.x;")
+            w("              const int x = k < WT ? s_nd[k] : 0;")
+            w("              int tot;")
+            w("              const int ex = b200_block_exscan(x, s_wsum, &tot);")
+            w("              if (k < WT) s_ndoff[k] = carry2 + ex;")
+            w("              carry2 += tot;")
+            w("            }")
+            w("            if (threadIdx.x == 0) s_ndoff[WT] = carry2;")
+            w("            __syncthreads();")
+            w("          }")
+            w("          const int ED = s_ndoff[WT];")
+            w("          for (int e0 = threadIdx.x; e0 < ED; e0 += 4 * (int)blockDim.x) {")
+            w("#pragma unroll")
+            w("            for (int qq = 0; qq < 4; ++qq) {")
+            w("              const int e = e0 + qq * (int)blockDim.x;")
+            w("              if (e < ED) {")
+            w("                const int k = b200_upper_bound(s_ndoff, WT + 1, e) - 1;")
+            w(window_of("k", 16))
+            w("                (void)kk;")
+            for q, pi in enumerate(pis):
+                w(("                if" if q == 0 else "                else if") + f" (q == {q}) {{  // {paths[pi]['name']}")
+                w(body_decls(pi, 18))
+                w("                  const int64_t rbase = (int64_t)rank * PQ.ev.cap;")
+                w("                  const int64_t rec = (s_wbase[k] + (e - s_ndoff[k])) & (PQ.ev.cap - 1);")
+                w(fifo_body(pi, 18))
+                w("                }")
+            w("              }")
+            w("            }")
+            w("          }")
+            w("          __syncthreads();")
+            w("          // retire the batches whose largest delay was due now")
+            w("          if (threadIdx.x == 0) {")
+            for q, pi in enumerate(pis):
+                w(f"            if (I.p[{pi}].D > 0) {{")
+                w(f"              const b200_fifo_d& F = I.p[{pi}].ev;")
+                w(f"              const int64_t sb = ts - I.p[{pi}].D;")
+                w("              if (sb >= 0) {")
+                w("                const int64_t row = (int64_t)rank * F.RB + (int)(sb % F.RB);")
+                w(f"                if (F.tag[row] == sb) s_tail[{pi}] = F.base[row] + F.off[row * (F.W + 1) + F.W];")
+                w("              }")
+                w("            }")
+            w("          }")
+            w("          __syncthreads();")
+            w("        }")
+            w("      }")
+            w("      B200_PHASE(5);")
+        w("    }  // steps")
+        w(f"    if (prof && threadIdx.x == 0)")
+        w(f"      for (int q = 0; q < {NPH}; ++q) atomicAdd(&prof[(size_t)unit * {NPH} + q], _pacc[q]);")
+        w("#undef B200_PHASE")
+        w("    // the last step's arrival: wait for it, then record its spikes in the monitors")
+        w("    if (pend) {")
+        w("      if (!b200_owner_wait(I, ts - 1, limit_ns, cluster)) ok = false;")
+        w("      else {")
+        w("        const int64_t s_step = ts - 1;")
+        emit_lists("s_step", "true", 8)
+        w("      }")
+        w("    }")
+        w("    if (ok && ts > ts0) {")
+        w("      const double _b200_t = (double)(ts - 1) * _b200_dt; (void)_b200_t;")
+        w("      const int64_t _b200_ts = ts - 1;")
+        for gi in range(NG):
+            rb = reset_block(gi, 6, "ts - 1", True)
+            if rb:
+                w(rb)
+        w("    }")
+        w("    __syncthreads();")
+        w("    if (s_cache) {")
+        for gi, g in enumerate(groups):
+            for k in USED[gi]:
+                sz = SIZE[g["vars"][k]["ctype"]]
+                w(f"      b200_copy_bytes((char*)I.g[{gi}].var[{k}] + (size_t)s_own[{gi}][0] * {sz}, (const char*)s_gv[{gi}][{k}] + (size_t)s_own[{gi}][0] * {sz},")
+                w(f"                      (size_t)(s_own[{gi}][1] - s_own[{gi}][0]) * {sz});")
+        w("    }")
+        w("    if (threadIdx.x == 0) {")
+        for pi in range(NP):
+            w(f"      if (I.p[{pi}].D > 0) {{ I.p[{pi}].ev.state[2 * rank] = s_head[{pi}]; I.p[{pi}].ev.state[2 * rank + 1] = s_tail[{pi}]; }}")
+        w("      if (rank == 0) {")
+        w("        *I.ts_done = ts;")
+        for m in range(len(spkmons)):
+            w(f"        *I.sm[{m}].n = s_mon_n[{m}];")
+        for m in range(len(statemons)):
+            w(f"        *I.stm[{m}].n = s_stm_n[{m}];")
+        w("      }")
+        w("    }")
+        w("    __syncthreads();")
+        w("  }")
+        w("}")
+        w("")
+
+    if OWNER:
+        emit_owner_kernel()
+
     # ------------------------------------------------------------- launch glue
     w("// `tcode` = threads | (min CTAs per SM - 1) << 16: the (512, 2) variant caps")
     w("// registers so that two CTAs fit on an SM (sweeps with more instances than SMs)")
     w("static const void* b200_kernel_for(int tcode) {")
-    w("  const int threads = tcode & 0xffff, minb = (tcode >> 16) + 1;")
+    w("  const int threads = tcode & 0xffff, minb = ((tcode >> 16) & 0xf) + 1;")
+    if OWNER:
+        w("  if (tcode & B200_TCODE_OWNER) {  // owner mode: one CTA per SM")
+        w("    if (threads <= 256) return (const void*)b200_owner_kernel<256, 1>;")
+        w("    if (threads <= 512) return (const void*)b200_owner_kernel<512, 1>;")
+        w("    return (const void*)b200_owner_kernel<1024, 1>;")
+        w("  }")
     w("  if (threads <= 256) return (const void*)b200_step_kernel<256, 1>;")
     w("  if (threads <= 512) return minb >= 2 ? (const void*)b200_step_kernel<512, 2> : (const void*)b200_step_kernel<512, 1>;")
     w("  return (const void*)b200_step_kernel<1024, 1>;")
     w("}")
+    w("static size_t b200_smem_for(int tcode, int max_tiles1, int max_w, int state_bytes) {")
+    w("  const int threads = tcode & 0xffff;")
+    if OWNER:
+        w("  if (tcode & B200_TCODE_OWNER) return b200_dyn_smem_owner(threads, max_tiles1, max_w, state_bytes);")
+    w("  return b200_dyn_smem(threads, max_tiles1, max_w, state_bytes);")
+    w("}")
     w("static int b200_max_active(int tcode, int max_tiles1, int max_w, int state_bytes) {")
     w("  const void* k = b200_kernel_for(tcode);")
     w("  const int threads = tcode & 0xffff;")
-    w("  const size_t smem = b200_dyn_smem(threads, max_tiles1, max_w, state_bytes);")
+    w("  const size_t smem = b200_smem_for(tcode, max_tiles1, max_w, state_bytes);")
     w("  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;")
     w("  int n = 0;")
     w("  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, threads, smem) != cudaSuccess) return 0;")
@@ -855,7 +1491,7 @@ def render_model(spec: dict) -> str:
     w("                               unsigned long long* prof, int cluster, cudaStream_t s) {")
     w("  const void* k = b200_kernel_for(tcode);")
     w("  const int threads = tcode & 0xffff;")
-    w("  const size_t smem = b200_dyn_smem(threads, max_tiles1, max_w, state_bytes);")
+    w("  const size_t smem = b200_smem_for(tcode, max_tiles1, max_w, state_bytes);")
     w("  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);")
     w("  if (e != cudaSuccess) return e;")
     w("  const b200_inst_d* ci = insts;")
@@ -881,7 +1517,7 @@ def render_model(spec: dict) -> str:
     w("static int b200_max_cluster(int tcode, int max_tiles1, int max_w, int state_bytes, int cluster) {")
     w("  const void* k = b200_kernel_for(tcode);")
     w("  const int threads = tcode & 0xffff;")
-    w("  const size_t smem = b200_dyn_smem(threads, max_tiles1, max_w, state_bytes);")
+    w("  const size_t smem = b200_smem_for(tcode, max_tiles1, max_w, state_bytes);")
     w("  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;")
     w("  if (cluster > 8 && cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return 0;")
     w("  cudaLaunchConfig_t cfg = {};")
@@ -898,7 +1534,7 @@ def render_model(spec: dict) -> str:
     w(f'static const b200_model_info B200_MODEL = {{"{spec["name"]}", {NG}, {NP}, {len(spkmons)}, {len(ratemons)}, {len(statemons)},')
     w("  b200_groups, b200_pathways, b200_spkmon, b200_ratemon, b200_statemon,")
     w(f"  {len(consts)}, b200_const_names, b200_const_defaults, b200_eval_scalars, b200_launch, b200_max_active,")
-    w(f"  b200_static_smem, b200_max_cluster, {4 + NP}}};")
+    w(f"  b200_static_smem, b200_max_cluster, {NPH}, {1 if OWNER else 0}}};")
     w("")
     w('#include "b200_host.h"')
     w("")

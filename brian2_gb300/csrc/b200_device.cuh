@@ -24,6 +24,9 @@
 #define B200_OK 0
 #define B200_ERR_BARRIER_TIMEOUT 4
 #define B200_ERR_INDEX 5
+#define B200_ERR_EVENT_OVERFLOW 6
+#define B200_MAX_PAYLOAD 4
+#define B200_OWNER_RING 4   // spike-list slots in owner mode (see the kernel's ordering argument)
 
 // ---------------------------------------------------------------------------
 // Descriptors (plain data, filled by the host runtime, read by the kernel).
@@ -44,6 +47,24 @@ struct b200_group_d {
   const double* S;        // scalar table (update | threshold | reset)
 };
 
+// Owner mode: per (pathway, CTA) FIFO of delivery events.  Every step the CTA
+// appends one *batch* (the events of that step's spikes, sorted by delay) at
+// `head`; a batch is retired once its largest delay is due, so the records
+// form a circular FIFO of `cap` (a power of two) entries.  Arrays are per CTA:
+// element [rank * cap + i], state [rank * 2 + {0: head, 1: tail}], batch
+// table [rank * RB + b] (absolute base, step tag) and [rank * RB + b][W + 1]
+// (exclusive per-delay offsets within the batch).
+struct b200_fifo_d {
+  int64_t cap;            // records per CTA (power of two)
+  int32_t RB, W;          // batch-table slots, delays per batch
+  int32_t* tgt;           // [n_cta * cap] target neuron (within the target group)
+  void* pay[B200_MAX_PAYLOAD];  // [n_cta * cap] payload values (synaptic variables)
+  int64_t* state;         // [n_cta * 2] head, tail (absolute record positions)
+  int64_t* base;          // [n_cta * RB] first record of each batch
+  int64_t* tag;           // [n_cta * RB] step of the spikes of each batch (-1: none)
+  int32_t* off;           // [n_cta * RB * (W + 1)] per-delay offsets in each batch
+};
+
 struct b200_pathway_d {
   int32_t D;              // largest delay in steps (0 = no delays)
   int32_t src_lo, src_hi; // presynaptic neuron range within the source group
@@ -53,8 +74,12 @@ struct b200_pathway_d {
   const int64_t* segptr;  // [(src_hi-src_lo)*(D+1)+1] CSR over (source, delay slot)
   const int32_t* post;    // [n_syn] target neuron (within target group), CSR order
   const int32_t* pre;     // [n_syn] source neuron (within source group), CSR order
-  void* var[B200_MAX_VARS];  // synaptic variables in CSR order
+  void* var[B200_MAX_VARS];  // synaptic variables in CSR order (owner mode: owner order)
   const double* S;        // scalar table of on_pre
+  // owner mode: segptr is over (source, owning CTA) with n_cta entries per
+  // source, post/var are in that order, odelay is each synapse's delay slot
+  const uint16_t* odelay;
+  b200_fifo_d ev;
 };
 
 struct b200_spkmon_d {
@@ -94,6 +119,11 @@ struct b200_inst_d {
   int32_t* status;        // [1] error status of this instance
   int64_t* ts_done;       // [1] written at exit: first step not executed
   int32_t* pending_reset; // [B200_MAX_GROUPS] reset of the last step still to apply
+  // owner mode (b200_owner_kernel): each CTA delivers into the neurons it owns
+  int32_t owner;          // 1: this instance runs in owner mode
+  int32_t lag;            // 1: every delay >= 1 step, a step pushes the previous step's spikes
+  int64_t ts_base;        // step whose arrival count starts at 0 in bar64
+  unsigned long long* bar64;  // [1] arrivals of the split barrier
   b200_group_d g[B200_MAX_GROUPS];
   b200_pathway_d p[B200_MAX_PATHWAYS];
   b200_spkmon_d sm[B200_MAX_SPKMON];
@@ -133,6 +163,9 @@ struct b200_pathway_info {
   const char* const* var_names;
   const int* var_kind;
   int n_scalars;
+  // owner mode: the synaptic variables on_pre reads (carried by each event)
+  int n_payload;
+  const int* payload_var;
 };
 struct b200_mon_info {
   const char* name;
@@ -160,7 +193,12 @@ struct b200_model_info {
   int (*static_smem)(int threads);
   int (*max_cluster)(int threads, int max_tiles1, int max_w, int state_bytes, int cluster);
   int n_phases;  // device profile: A, barrier A, spike lists, one per pathway, barrier B
+  // 1: every pathway's on_pre only adds to variables of its target neuron from
+  // synaptic values and constants, so owner-mode delivery applies
+  int owner_ok;
 };
+// `tcode` bit selecting the owner-mode kernel
+#define B200_TCODE_OWNER (1 << 20)
 
 
 // ---------------------------------------------------------------------------
@@ -180,6 +218,16 @@ __device__ __forceinline__ unsigned b200_ld_acquire(const unsigned* p) {
 
 __device__ __forceinline__ void b200_st_release(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long b200_ld_acquire64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void b200_red_release_add64(unsigned long long* p, unsigned long long v) {
+  asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 __device__ __forceinline__ uint64_t b200_globaltimer() {
@@ -247,9 +295,15 @@ __device__ __forceinline__ int b200_block_compact(bool flag, int* wsum, int* tot
   return r;
 }
 
-// Block-cooperative copy of `bytes` (the arrays are 16-byte aligned in shared
-// memory and at least 4-byte aligned in global memory).
+// Block-cooperative copy of `bytes`: 4-byte words when both ends are 4-byte
+// aligned, single bytes otherwise (a 1-byte variable from a tile boundary).
 __device__ __forceinline__ void b200_copy_bytes(void* dst, const void* src, size_t bytes) {
+  if ((((uintptr_t)dst) | ((uintptr_t)src)) & 3) {
+    unsigned char* db = (unsigned char*)dst;
+    const unsigned char* sb = (const unsigned char*)src;
+    for (size_t k = threadIdx.x; k < bytes; k += blockDim.x) db[k] = sb[k];
+    return;
+  }
   const size_t nw = bytes / 4;
   uint32_t* d = (uint32_t*)dst;
   const uint32_t* s = (const uint32_t*)src;
@@ -385,3 +439,153 @@ __device__ __forceinline__ void _b200_atomic_add(double* p, double v) { atomicAd
 __device__ __forceinline__ void _b200_atomic_add(float* p, float v) { atomicAdd(p, v); }
 __device__ __forceinline__ void _b200_atomic_add(float* p, double v) { atomicAdd(p, (float)v); }
 __device__ __forceinline__ void _b200_atomic_add(int32_t* p, int32_t v) { atomicAdd(p, v); }
+
+// ---------------------------------------------------------------------------
+// Owner mode: split-phase instance barrier.  Every CTA of an instance arrives
+// once per step (release), and waits (acquire) until all have arrived for a
+// given step; the arrival count of step t is (t + 1 - ts_base) * n_cta.  In
+// cluster mode the hardware cluster barrier is used in the same arrive / wait
+// order (each arrive is followed by exactly one wait).  Waits are bounded.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void b200_owner_arrive(const b200_inst_d& I, int cluster) {
+  __syncthreads();
+  if (cluster) {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+    return;
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    b200_red_release_add64(I.bar64, 1ull);
+  }
+}
+
+__device__ __forceinline__ bool b200_owner_wait(const b200_inst_d& I, int64_t t, uint64_t limit_ns,
+                                                int cluster) {
+  if (cluster) {
+    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+    return true;
+  }
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    ok = 1;
+    const unsigned long long target = (unsigned long long)(t + 1 - I.ts_base) * (unsigned long long)I.n_cta;
+    if (b200_ld_acquire64(I.bar64) < target) {
+      const uint64_t t0 = b200_globaltimer();
+      int spins = 0;
+      while (b200_ld_acquire64(I.bar64) < target) {
+        if (++spins > 32) __nanosleep(32);
+        if ((spins & 255) == 0 &&
+            (b200_globaltimer() - t0 > limit_ns || *((volatile int32_t*)I.status) != 0)) {
+          atomicCAS(I.status, 0, B200_ERR_BARRIER_TIMEOUT);
+          ok = 0;
+          break;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// ---------------------------------------------------------------------------
+// Owner mode: relayout of one pathway's CSR over (source, delay slot) into
+// segments over (source, owning CTA), stable (within a segment the synapses
+// keep their (delay, CSR) order).  One warp per source; `own_lo` [n_own + 1]
+// are the first target neurons owned by each CTA.  Every source's synapses
+// stay in the source's range of the CSR, so oseg[s * n_own + r] starts at
+// segptr[s * W] plus the counts of the owners before r.  `cnt` is n_own ints of
+// shared memory per warp.
+// ---------------------------------------------------------------------------
+struct b200_relayout_args {
+  const int64_t* segptr;   // [n_src * W + 1]
+  const int32_t* post;     // [n_syn]
+  const void* var[B200_MAX_PAYLOAD];
+  int32_t var_size[B200_MAX_PAYLOAD];
+  int32_t n_var;
+  int32_t n_src, W, dmin, n_own;
+  const int32_t* own_lo;   // [n_own + 1]
+  int64_t* oseg;           // [n_src * n_own + 1]
+  int32_t* opost;          // [n_syn]
+  uint16_t* odelay;        // [n_syn]
+  void* ovar[B200_MAX_PAYLOAD];
+  int32_t* status;         // set to B200_ERR_INDEX on an out-of-range target
+};
+
+__device__ __forceinline__ int b200_owner_of(const int32_t* own_lo, int n_own, int32_t t) {
+  int lo = 0, hi = n_own;  // last r with own_lo[r] <= t
+  while (hi - lo > 1) {
+    const int m = (lo + hi) >> 1;
+    if (own_lo[m] <= t) lo = m; else hi = m;
+  }
+  return lo;
+}
+
+__global__ void b200_owner_relayout_kernel(b200_relayout_args A) {
+  extern __shared__ int b200_rl_smem[];
+  int* s_own = b200_rl_smem;                                     // [n_own + 1]
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  int* cnt = b200_rl_smem + A.n_own + 1 + wid * A.n_own;        // [n_own] per warp
+  for (int k = threadIdx.x; k <= A.n_own; k += blockDim.x) s_own[k] = A.own_lo[k];
+  __syncthreads();
+  const int32_t t_lo = s_own[0], t_hi = s_own[A.n_own];
+  for (int64_t s = (int64_t)blockIdx.x * nwarp + wid; s < A.n_src; s += (int64_t)gridDim.x * nwarp) {
+    const int64_t* sp = A.segptr + s * A.W;
+    const int64_t base = sp[0], end = sp[A.W];
+    for (int r = lane; r < A.n_own; r += 32) cnt[r] = 0;
+    __syncwarp();
+    // pass 1: synapses per owner
+    for (int64_t j0 = base; j0 < end; j0 += 32) {
+      const int64_t j = j0 + lane;
+      if (j < end) {
+        const int32_t t = A.post[j];
+        if (t < t_lo || t >= t_hi) atomicCAS(A.status, 0, B200_ERR_INDEX);
+        else atomicAdd(&cnt[b200_owner_of(s_own, A.n_own, t)], 1);
+      }
+    }
+    __syncwarp();
+    // exclusive prefix over owners (serial per warp lane 0: n_own is small)
+    if (lane == 0) {
+      int64_t acc = 0;
+      for (int r = 0; r < A.n_own; ++r) {
+        const int c = cnt[r];
+        A.oseg[s * A.n_own + r] = base + acc;
+        cnt[r] = (int)acc;
+        acc += c;
+      }
+    }
+    __syncwarp();
+    // pass 2: stable scatter, delay slot by delay slot
+    for (int k = 0; k < A.W; ++k) {
+      const int64_t a = sp[k], b = sp[k + 1];
+      for (int64_t j0 = a; j0 < b; j0 += 32) {
+        const int64_t j = j0 + lane;
+        const bool act = j < b;
+        int32_t t = 0;
+        int r = -1;
+        if (act) {
+          t = A.post[j];
+          if (t >= t_lo && t < t_hi) r = b200_owner_of(s_own, A.n_own, t);
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, r);
+        const int rank = __popc(peers & b200_lanemask_lt());
+        const int c0 = r >= 0 ? cnt[r] : 0;
+        __syncwarp();
+        if (r >= 0) {
+          const int64_t pos = base + c0 + rank;
+          A.opost[pos] = t;
+          A.odelay[pos] = (uint16_t)(A.dmin + k);
+          for (int v = 0; v < A.n_var; ++v) {
+            if (A.var_size[v] == 8)
+              ((int64_t*)A.ovar[v])[pos] = ((const int64_t*)A.var[v])[j];
+            else
+              ((int32_t*)A.ovar[v])[pos] = ((const int32_t*)A.var[v])[j];
+          }
+          if (rank == 0) cnt[r] = c0 + __popc(peers);
+        }
+        __syncwarp();
+      }
+    }
+    __syncwarp();
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) A.oseg[(int64_t)A.n_src * A.n_own] = A.segptr[(int64_t)A.n_src * A.W];
+}

@@ -43,6 +43,16 @@ struct b200_pathway_h {
   std::vector<int64_t> perm;  // perm[csr position] = synapse index (creation order)
   b200_dbuf segptr, post, pre, S;
   std::vector<b200_dbuf> var;
+  // owner mode: synapses over (source, owning CTA), the payload variables in
+  // that order, and the per-CTA event FIFOs
+  b200_dbuf oseg, opost, odelay;
+  std::vector<b200_dbuf> ovar;
+  std::vector<int32_t> own_lo;  // ownership the layout was built for (empty: none)
+  bool own_stale = true;
+  b200_dbuf ev_tgt, ev_state, ev_base, ev_tag, ev_off;
+  std::vector<b200_dbuf> ev_pay;
+  int64_t ev_cap = 0;
+  int32_t ev_RB = 0, ev_W = 0, ev_ncta = 0;
 };
 struct b200_spkmon_h {
   int32_t lo = 0, hi = 0;
@@ -69,7 +79,8 @@ struct b200_inst_h {
   std::vector<b200_statemon_h> stm;
   int32_t n_cta = 1;
   int64_t ts = 0;
-  b200_dbuf bar, status, ts_done, pending;
+  b200_dbuf bar, status, ts_done, pending, bar64;
+  int32_t ran_owner = -1;  // mode of the runs so far with spikes in flight: -1 none, 0 classic, 1 owner
 };
 
 struct b200_net {
@@ -87,6 +98,9 @@ struct b200_net {
   bool smem_cache = true;         // cache the state of single-CTA instances
   bool profiling = false;         // per-phase clock64 profile of the step kernel
   bool use_clusters = true;       // instances of 2..16 CTAs run as thread-block clusters
+  int allow_owner = 2;            // owner-mode delivery: 0 off, 1 on where possible, 2 auto
+  int owner = 0;                  // 1: the current plan runs b200_owner_kernel
+  double ev_factor = 1.0;         // event FIFO records per CTA, in units of its incoming synapses
   int cluster = 0;                // cluster size of the current launch plan (0: none)
   b200_dbuf prof;
   int queue_mode = 0;      // 1: single-CTA instances pulled from a work queue
@@ -103,7 +117,7 @@ struct b200_net {
   double last_kernel_ms = 0.0;  // kernel launches only (CUDA events around them)
   std::string err;
   size_t device_bytes = 0;
-  int tcode() const { return threads | ((min_blocks - 1) << 16); }
+  int tcode() const { return threads | ((min_blocks - 1) << 16) | (owner ? B200_TCODE_OWNER : 0); }
 };
 
 static int b200_fail(b200_net* n, int code, const char* fmt, ...) {
@@ -218,11 +232,17 @@ int b200_destroy(b200_net* n) {
     for (auto& P : I.p) {
       for (auto& b : P.var) b200_free(n, b);
       b200_free(n, P.segptr); b200_free(n, P.post); b200_free(n, P.pre); b200_free(n, P.S);
+      for (auto& b : P.ovar) b200_free(n, b);
+      for (auto& b : P.ev_pay) b200_free(n, b);
+      b200_free(n, P.oseg); b200_free(n, P.opost); b200_free(n, P.odelay);
+      b200_free(n, P.ev_tgt); b200_free(n, P.ev_state); b200_free(n, P.ev_base); b200_free(n, P.ev_tag);
+      b200_free(n, P.ev_off);
     }
     for (auto& S : I.sm) { b200_free(n, S.n); b200_free(n, S.i); b200_free(n, S.ts); b200_free(n, S.count); }
     for (auto& S : I.rm) b200_free(n, S.cnt);
     for (auto& S : I.stm) { b200_free(n, S.d_idx); b200_free(n, S.n); b200_free(n, S.data); }
     b200_free(n, I.bar); b200_free(n, I.status); b200_free(n, I.ts_done); b200_free(n, I.pending);
+    b200_free(n, I.bar64);
   }
   b200_free(n, n->d_insts); b200_free(n, n->d_cta_map); b200_free(n, n->d_work); b200_free(n, n->prof);
   if (n->stream) cudaStreamDestroy(n->stream);
@@ -310,6 +330,8 @@ int b200_upload(b200_net* n, int32_t inst, int32_t kind, int32_t obj, int32_t va
     const char* s = (const char*)src;
     for (int64_t k = 0; k < cnt; ++k) memcpy(&tmp[(size_t)k * es], s + (size_t)perm[k] * es, es);
     B200_CU(n, cudaMemcpyAsync(b->p, tmp.data(), tmp.size(), cudaMemcpyHostToDevice, n->stream));
+    n->inst[inst].p[obj].own_stale = true;
+    n->prepared = false;
   }
   B200_CU(n, cudaStreamSynchronize(n->stream));
   return 0;
@@ -393,6 +415,7 @@ int b200_set_synapses(b200_net* n, int32_t inst, int32_t pw, int32_t src_lo, int
   }
   P.src_lo = src_lo; P.src_hi = src_hi; P.tgt_lo = tgt_lo; P.tgt_hi = tgt_hi;
   P.dmin = dmin; P.dmax = dmax; P.n_syn = n_syn; P.has_syn = true;
+  P.own_stale = true;
   int r;
   if ((r = b200_alloc(n, P.segptr, seg.size() * 8, false))) return r;
   if ((r = b200_alloc(n, P.post, (size_t)n_syn * 4, false))) return r;
@@ -433,6 +456,7 @@ int b200_set_synapses_csr(b200_net* n, int32_t inst, int32_t pw, int32_t src_lo,
   for (int64_t k = 0; k < n_syn; ++k) P.perm[k] = k;
   P.src_lo = src_lo; P.src_hi = src_hi; P.tgt_lo = tgt_lo; P.tgt_hi = tgt_hi;
   P.dmin = dmin; P.dmax = dmax; P.n_syn = n_syn; P.has_syn = true;
+  P.own_stale = true;
   for (int v = 0; v < PI.n_vars; ++v)
     if ((r = b200_alloc(n, P.var[v], (size_t)n_syn * b200_kind_size(PI.var_kind[v])))) return r;
   B200_CU(n, cudaStreamSynchronize(n->stream));
@@ -448,6 +472,8 @@ int b200_synapse_var_ptr(b200_net* n, int32_t inst, int32_t pw, int32_t var, voi
   int r = b200_var_buf(n, inst, 1, pw, var, &b, &vk, &cnt);
   if (r) return r;
   *out = b->p;
+  n->inst[inst].p[pw].own_stale = true;  // the caller may write it: owner copies are rebuilt
+  n->prepared = false;
   return 0;
 }
 
@@ -515,9 +541,153 @@ static void b200_make_tiles(int32_t N, int n_cta, std::vector<int32_t> cuts,
   cta_tile[n_cta] = n_tiles;
 }
 
+static int64_t b200_pow2ceil(int64_t x) {
+  int64_t p = 1;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+// Owner mode, one pathway of instance k: the synapses regrouped over (source,
+// owning CTA) (rebuilt when the synapses or the ownership changed), the per-CTA
+// event FIFOs, and the descriptor pointing at them.
+static int b200_owner_pathway(b200_net* n, int k, int p, b200_pathway_d& PD) {
+  const b200_model_info* M = n->M;
+  b200_inst_h& I = n->inst[k];
+  b200_pathway_h& P = I.p[p];
+  const b200_pathway_info& PI = M->pathways[p];
+  const b200_group_h& TG = I.g[PI.tgt_group];
+  const int C = I.n_cta;
+  std::vector<int32_t> own_lo(C + 1);
+  for (int r = 0; r <= C; ++r) own_lo[r] = TG.tile_start[TG.cta_tile[r]];
+  const bool delays = P.dmax >= 1 && P.n_syn > 0;
+  if (!P.own_lo.empty() && P.own_lo != own_lo && I.ts > 0 && delays)
+    return b200_fail(n, B200_ERR_ARG,
+                     "pathway %s: the CTA count of a network with delays cannot change once it has run in "
+                     "owner mode (events in flight belong to their CTA)", PI.name);
+  int r;
+  const int64_t n_src = P.src_hi - P.src_lo;
+  if (P.own_stale || P.own_lo != own_lo) {
+    if ((r = b200_alloc(n, P.oseg, (size_t)(n_src * C + 1) * 8, false))) return r;
+    if ((r = b200_alloc(n, P.opost, (size_t)std::max<int64_t>(P.n_syn, 1) * 4, false))) return r;
+    if ((r = b200_alloc(n, P.odelay, (size_t)std::max<int64_t>(P.n_syn, 1) * 2, false))) return r;
+    P.ovar.resize(PI.n_payload);
+    b200_relayout_args A;
+    memset(&A, 0, sizeof(A));
+    A.segptr = (const int64_t*)P.segptr.p;
+    A.post = (const int32_t*)P.post.p;
+    A.n_var = PI.n_payload;
+    for (int m = 0; m < PI.n_payload; ++m) {
+      const int v = PI.payload_var[m];
+      const size_t es = b200_kind_size(PI.var_kind[v]);
+      if (es != 4 && es != 8) return b200_fail(n, B200_ERR_ARG, "owner mode: unsupported synaptic variable size");
+      if ((r = b200_alloc(n, P.ovar[m], (size_t)std::max<int64_t>(P.n_syn, 1) * es, false))) return r;
+      A.var[m] = P.var[v].p;
+      A.var_size[m] = (int32_t)es;
+      A.ovar[m] = P.ovar[m].p;
+    }
+    A.n_src = (int32_t)n_src;
+    A.W = P.dmax - P.dmin + 1;
+    A.dmin = P.dmin;
+    A.n_own = C;
+    b200_dbuf d_own;
+    if ((r = b200_alloc(n, d_own, (size_t)(C + 1) * 4, false))) return r;
+    B200_CU(n, cudaMemcpyAsync(d_own.p, own_lo.data(), (size_t)(C + 1) * 4, cudaMemcpyHostToDevice, n->stream));
+    A.own_lo = (const int32_t*)d_own.p;
+    A.oseg = (int64_t*)P.oseg.p;
+    A.opost = (int32_t*)P.opost.p;
+    A.odelay = (uint16_t*)P.odelay.p;
+    A.status = (int32_t*)I.status.p;
+    B200_CU(n, cudaMemsetAsync(I.status.p, 0, 4, n->stream));
+    const int threads = 256, warps = threads / 32;
+    const size_t smem = (size_t)(C + 1 + warps * C) * 4;
+    if (smem > 48 * 1024)
+      B200_CU(n, cudaFuncSetAttribute(b200_owner_relayout_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int n_sm = 0, dev = 0;
+    B200_CU(n, cudaGetDevice(&dev));
+    B200_CU(n, cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t want = (n_src + warps - 1) / warps;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)n_sm * 8));
+    b200_owner_relayout_kernel<<<grid, threads, smem, n->stream>>>(A);
+    B200_CU(n, cudaGetLastError());
+    B200_CU(n, cudaStreamSynchronize(n->stream));
+    b200_free(n, d_own);
+    int32_t st = 0;
+    B200_CU(n, cudaMemcpy(&st, I.status.p, 4, cudaMemcpyDeviceToHost));
+    if (st) {
+      cudaMemset(I.status.p, 0, 4);
+      return b200_fail(n, B200_ERR_INDEX, "pathway %s: a target lies outside the target group's tiles", PI.name);
+    }
+    P.own_lo = own_lo;
+    P.own_stale = false;
+  }
+  // event FIFOs (pathways with delays): room for `ev_factor` x the largest
+  // CTA's incoming synapses (estimated from the synapses per target neuron)
+  if (delays) {
+    int32_t widest = 0;
+    for (int c = 0; c < C; ++c) widest = std::max(widest, own_lo[c + 1] - own_lo[c]);
+    const double per_target = (double)P.n_syn / std::max(1, P.tgt_hi - P.tgt_lo);
+    const int64_t est = (int64_t)(1.25 * per_target * widest * n->ev_factor) + 1;
+    const int64_t cap = b200_pow2ceil(std::max<int64_t>(est, (int64_t)1 << 10));
+    const int32_t W = P.dmax - P.dmin + 1, RB = P.dmax + 2;
+    if (cap != P.ev_cap || W != P.ev_W || RB != P.ev_RB || C != P.ev_ncta) {
+      if (I.ts > 0 && I.ran_owner == 1 && P.ev_cap > 0)
+        return b200_fail(n, B200_ERR_ARG, "pathway %s: the event FIFO cannot be resized once the network has run", PI.name);
+      if ((r = b200_alloc(n, P.ev_tgt, (size_t)C * cap * 4, false))) return r;
+      P.ev_pay.resize(PI.n_payload);
+      for (int m = 0; m < PI.n_payload; ++m)
+        if ((r = b200_alloc(n, P.ev_pay[m], (size_t)C * cap * b200_kind_size(PI.var_kind[PI.payload_var[m]]), false)))
+          return r;
+      if ((r = b200_alloc(n, P.ev_state, (size_t)C * 2 * 8))) return r;
+      if ((r = b200_alloc(n, P.ev_base, (size_t)C * RB * 8))) return r;
+      if ((r = b200_alloc(n, P.ev_tag, (size_t)C * RB * 8, false))) return r;
+      B200_CU(n, cudaMemsetAsync(P.ev_tag.p, 0xff, (size_t)C * RB * 8, n->stream));  // -1: no batch
+      if ((r = b200_alloc(n, P.ev_off, (size_t)C * RB * (W + 1) * 4))) return r;
+      B200_CU(n, cudaStreamSynchronize(n->stream));
+      P.ev_cap = cap; P.ev_W = W; P.ev_RB = RB; P.ev_ncta = C;
+    }
+  }
+  PD.segptr = (const int64_t*)P.oseg.p;
+  PD.post = (const int32_t*)P.opost.p;
+  PD.pre = nullptr;
+  for (int v = 0; v < B200_MAX_VARS; ++v) PD.var[v] = nullptr;
+  for (int m = 0; m < PI.n_payload; ++m) PD.var[PI.payload_var[m]] = P.ovar[m].p;
+  PD.odelay = (const uint16_t*)P.odelay.p;
+  memset(&PD.ev, 0, sizeof(PD.ev));
+  if (delays) {
+    PD.ev.cap = P.ev_cap; PD.ev.RB = P.ev_RB; PD.ev.W = P.ev_W;
+    PD.ev.tgt = (int32_t*)P.ev_tgt.p;
+    for (int m = 0; m < PI.n_payload; ++m) PD.ev.pay[m] = P.ev_pay[m].p;
+    PD.ev.state = (int64_t*)P.ev_state.p;
+    PD.ev.base = (int64_t*)P.ev_base.p;
+    PD.ev.tag = (int64_t*)P.ev_tag.p;
+    PD.ev.off = (int32_t*)P.ev_off.p;
+  }
+  return 0;
+}
+
 static int b200_prepare(b200_net* n) {
   const b200_model_info* M = n->M;
   int r;
+  // owner mode: a model whose on_pre code allows it, every instance on 2+ CTAs
+  {
+    bool want = n->allow_owner != 0 && M->owner_ok && !n->queue_mode;
+    for (int k = 0; k < n->n_inst && want; ++k) want = n->inst[k].n_cta >= 2;
+    // auto: owner mode where it is measured faster (no synaptic delays)
+    for (int k = 0; k < n->n_inst && want && n->allow_owner == 2; ++k)
+      for (int p = 0; p < M->n_pathways; ++p)
+        if (n->inst[k].p[p].n_syn > 0 && n->inst[k].p[p].dmax > 0) want = false;
+    n->owner = want ? 1 : 0;
+    for (int k = 0; k < n->n_inst; ++k) {
+      const b200_inst_h& I = n->inst[k];
+      bool inflight = false;
+      for (int p = 0; p < M->n_pathways; ++p) inflight = inflight || (I.p[p].dmax >= 1 && I.p[p].n_syn > 0);
+      if (I.ts > 0 && inflight && I.ran_owner >= 0 && I.ran_owner != n->owner)
+        return b200_fail(n, B200_ERR_ARG,
+                         "instance %d: switching between owner and classic delivery after the first run of a "
+                         "network with delays would lose the spikes in flight; choose the mode (b200_set_owner) "
+                         "and the CTA count before the first run", k);
+    }
+  }
   n->h_insts.assign(n->n_inst, b200_inst_d());
   std::vector<int2> cta_map;
   int cta = 0;
@@ -554,11 +724,12 @@ static int b200_prepare(b200_net* n) {
         if (M->spkmon[s].group == g) { cuts.push_back(I.sm[s].lo); cuts.push_back(I.sm[s].hi); }
       for (int s = 0; s < M->n_ratemon; ++s)
         if (M->ratemon[s].group == g) { cuts.push_back(I.rm[s].lo); cuts.push_back(I.rm[s].hi); }
+      if (n->owner) R = B200_OWNER_RING;  // lists of the last steps only: events wait in the FIFOs
       const std::vector<int32_t> old_tiles = G.tile_start;
       b200_make_tiles(G.N, I.n_cta, cuts, G.tile_start, G.cta_tile);
       const int n_tiles = (int)G.tile_start.size() - 1;
       const bool ring_changed = (R != G.R) || !G.ring.p;
-      const bool retile = !ring_changed && old_tiles != G.tile_start && I.ts > 0 && R > 1;
+      const bool retile = !n->owner && !ring_changed && old_tiles != G.tile_start && I.ts > 0 && R > 1;
       G.R = R;
       if ((r = b200_alloc(n, G.d_tile_start, G.tile_start.size() * 4, false))) return r;
       if ((r = b200_alloc(n, G.d_cta_tile, G.cta_tile.size() * 4, false))) return r;
@@ -631,6 +802,15 @@ static int b200_prepare(b200_net* n) {
       B200_CU(n, cudaMemcpyAsync(P.S.p, S.data(), S.size() * 8, cudaMemcpyHostToDevice, n->stream));
       B200_CU(n, cudaStreamSynchronize(n->stream));
       PD.S = (const double*)P.S.p;
+      if (n->owner && (r = b200_owner_pathway(n, k, p, PD))) return r;
+    }
+    if (n->owner) {
+      D.owner = 1;
+      D.lag = 1;  // every pathway with synapses has delays >= 1 step
+      for (int p = 0; p < M->n_pathways; ++p)
+        if (I.p[p].n_syn > 0 && I.p[p].dmin == 0) D.lag = 0;
+      if ((r = b200_alloc(n, I.bar64, 16))) return r;
+      D.bar64 = (unsigned long long*)I.bar64.p;
     }
     for (int s = 0; s < M->n_spkmon; ++s) {
       b200_spkmon_h& S = I.sm[s];
@@ -700,13 +880,29 @@ static int b200_prepare(b200_net* n) {
     B200_CU(n, cudaDeviceGetAttribute(&n_sm_, cudaDevAttrMultiProcessorCount, dev_));
     n->min_blocks = (n->queue_mode && n->threads == 512 && n->n_inst > n_sm_) ? 2 : 1;
     const long other = (long)M->static_smem(n->tcode()) +
-                       (long)(n->threads * 16 + 2 * M->n_groups * n->max_tiles1 * 4 + (3 * n->max_w + 1) * 4 + 64);
+                       (long)(n->threads * 20 + 4 + 2 * M->n_groups * n->max_tiles1 * 4 + (3 * n->max_w + 1) * 4 + 64) +
+                       (n->owner ? (long)n->max_w * 8 + (long)(n->max_w + 1) * 4 : 0L);
     const long budget = (long)optin - other - 1024;
     // bytes of the cache of instance k: state variables, plus (lists) the step's
     // spike list and tile counts
     auto cache_bytes = [&](int k, bool lists) -> long {
       b200_inst_h& I = n->inst[k];
-      if (!n->smem_cache || I.n_cta != 1) return 0;
+      if (!n->smem_cache) return 0;
+      if (n->owner) {  // each CTA caches the neurons it owns
+        long worst = 0;
+        for (int c = 0; c < I.n_cta; ++c) {
+          long bytes = 0;
+          for (int g = 0; g < M->n_groups; ++g) {
+            const b200_group_h& G = I.g[g];
+            const long Ng = G.tile_start[G.cta_tile[c + 1]] - G.tile_start[G.cta_tile[c]];
+            for (int v = 0; v < M->groups[g].n_vars; ++v)
+              if (M->groups[g].var_used[v]) bytes += (Ng * (long)b200_kind_size(M->groups[g].var_kind[v]) + 15) & ~15L;
+          }
+          worst = std::max(worst, bytes);
+        }
+        return worst > budget ? 0 : worst;
+      }
+      if (I.n_cta != 1) return 0;
       long bytes = 0;
       for (int g = 0; g < M->n_groups; ++g) {
         const long Ng = I.g[g].N;
@@ -877,7 +1073,8 @@ int b200_run(b200_net* n, int64_t n_steps) {
         int64_t used = 0;
         B200_CU(n, cudaMemcpy(&used, S.n.p, 8, cudaMemcpyDeviceToHost));
         // room for at least 64 steps of all neurons spiking
-        const int64_t need = std::min<int64_t>(target[k] - I.ts, 64) * (int64_t)(S.hi - S.lo);
+        // (owner mode records a step's spikes one step later: one more step of room)
+        const int64_t need = (std::min<int64_t>(target[k] - I.ts, 64) + (n->owner ? 1 : 0)) * (int64_t)(S.hi - S.lo);
         if ((r = b200_grow_spkmon(n, S, used, need))) return r;
         D.sm[s].cap = S.cap;
         D.sm[s].i = (int32_t*)S.i.p;
@@ -885,6 +1082,12 @@ int b200_run(b200_net* n, int64_t n_steps) {
       }
     }
     if (!any) break;
+    if (n->owner) {  // the split barrier counts the arrivals of this launch from 0
+      for (int k = 0; k < n->n_inst; ++k) {
+        n->h_insts[k].ts_base = n->inst[k].ts;
+        B200_CU(n, cudaMemsetAsync(n->inst[k].bar64.p, 0, 8, n->stream));
+      }
+    }
     B200_CU(n, cudaMemcpyAsync(n->d_insts.p, n->h_insts.data(), sizeof(b200_inst_d) * n->n_inst,
                                cudaMemcpyHostToDevice, n->stream));
     B200_CU(n, cudaMemsetAsync(n->d_work.p, 0, 16, n->stream));
@@ -951,12 +1154,20 @@ int b200_run(b200_net* n, int64_t n_steps) {
         // leave the handle usable: clear the status and the barrier state
         cudaMemset(I.status.p, 0, 4);
         cudaMemset(I.bar.p, 0, 16);
+        if (st == B200_ERR_EVENT_OVERFLOW) {
+          I.ts = done;
+          return b200_fail(n, B200_ERR_CAPACITY,
+                           "instance %d: an owner-mode event FIFO overflowed before step %lld (events were dropped; "
+                           "raise its size with b200_set_event_capacity and run again from the start)",
+                           k, (long long)done);
+        }
         return b200_fail(n, st == B200_ERR_BARRIER_TIMEOUT ? B200_ERR_BARRIER_TIMEOUT : B200_ERR_INDEX,
                          "instance %d: device status %d at step %lld (%s)", k, st, (long long)done,
                          st == B200_ERR_BARRIER_TIMEOUT ? "instance barrier timed out" : "index out of range");
       }
       if (done < I.ts || done > target[k])
         return b200_fail(n, B200_ERR_CUDA, "instance %d: bad progress %lld", k, (long long)done);
+      if (done > I.ts) I.ran_owner = n->owner;
       I.ts = done;
     }
   }
@@ -1000,6 +1211,40 @@ int b200_get_profile(b200_net* n, int32_t inst, uint64_t* cycles, int32_t n_phas
 int b200_profile_phases(b200_net* n, int32_t* count) {
   if (!n || !count) return B200_ERR_ARG;
   *count = n->M->n_phases;
+  return 0;
+}
+
+// Owner-mode delivery on (default) or off.  In owner mode each CTA of a
+// multi-CTA instance owns the target neurons of its tiles: it keeps their
+// state in shared memory for the launch, takes every spike of the step from
+// the spike lists and delivers only into its own neurons, through per-CTA
+// event FIFOs ordered by due step (delays >= 1) or at once (no delay).  It
+// applies when every on_pre only adds synaptic values or constants into
+// variables of its target (the model library says so).  The reference has one
+// delivery path (CSpikeQueue, brian2/synapses/spikequeue.h:14-206); both modes
+// reproduce it.
+int b200_set_owner(b200_net* n, int32_t enable) {
+  if (!n || enable < 0 || enable > 2) return B200_ERR_ARG;
+  n->allow_owner = enable;
+  n->prepared = false;
+  return 0;
+}
+
+// 1 if the current launch plan uses owner-mode delivery.
+int b200_owner_active(b200_net* n, int32_t* active) {
+  if (!n || !active) return B200_ERR_ARG;
+  int r;
+  if (!n->prepared && (r = b200_prepare(n))) return r;
+  *active = n->owner;
+  return 0;
+}
+
+// Owner-mode event FIFO size per CTA, in units of the CTA's incoming synapses
+// (default 1: every synapse may carry one event in flight).
+int b200_set_event_capacity(b200_net* n, double factor) {
+  if (!n || !(factor > 0.0)) return B200_ERR_ARG;
+  n->ev_factor = factor;
+  n->prepared = false;
   return 0;
 }
 

@@ -69,6 +69,9 @@ def _declare(lib):
         "b200_set_smem_cache": [h, C.c_int32],
         "b200_set_profiling": [h, C.c_int32],
         "b200_set_clusters": [h, C.c_int32],
+        "b200_set_owner": [h, C.c_int32],
+        "b200_owner_active": [h, _i32p],
+        "b200_set_event_capacity": [h, C.c_double],
         "b200_launch_plan": [h, _i32p, _i32p, _i32p],
         "b200_profile_phases": [h, _i32p],
         "b200_get_profile": [h, C.c_int32, C.POINTER(C.c_uint64), C.c_int32],
@@ -308,6 +311,19 @@ class Network:
     def set_clusters(self, enable=True):
         self._check(self.lib.b200_set_clusters(self._h, int(bool(enable))))
 
+    def set_owner(self, enable=True):
+        """Owner-mode delivery: True (where the model allows it), False, or
+        "auto" (the default: on for networks without synaptic delays)."""
+        self._check(self.lib.b200_set_owner(self._h, 2 if enable == "auto" else int(bool(enable))))
+
+    def owner_active(self):
+        a = C.c_int32()
+        self._check(self.lib.b200_owner_active(self._h, C.byref(a)))
+        return bool(a.value)
+
+    def set_event_capacity(self, factor):
+        self._check(self.lib.b200_set_event_capacity(self._h, float(factor)))
+
     def launch_plan(self):
         g, c, sb = C.c_int32(), C.c_int32(), C.c_int32()
         self._check(self.lib.b200_launch_plan(self._h, C.byref(g), C.byref(c), C.byref(sb)))
@@ -322,8 +338,12 @@ class Network:
         self._check(self.lib.b200_profile_phases(self._h, C.byref(n)))
         a = np.zeros(n.value, np.uint64)
         self._check(self.lib.b200_get_profile(self._h, int(inst), a.ctypes.data_as(C.POINTER(C.c_uint64)), n.value))
-        names = ["update_threshold_reset", "barrier_a", "spike_lists_monitors"] + \
-                [f"propagate:{p['name']}" for p in self.model.spec.get("pathways", [])] + ["barrier_b"]
+        if self.owner_active():
+            names = ["update_threshold_reset", "barrier", "spike_lists_monitors", "push_count",
+                     "push_fifo", "deliver"]
+        else:
+            names = ["update_threshold_reset", "barrier_a", "spike_lists_monitors"] + \
+                    [f"propagate:{p['name']}" for p in self.model.spec.get("pathways", [])] + ["barrier_b"]
         return dict(zip(names, (int(x) for x in a)))
 
     def set_smem_cache(self, enable=True):

@@ -56,6 +56,18 @@ int b200_set_smem_cache(b200_net* net, int32_t enable);
  * barrier (default on), and report the launch plan that b200_run will use. */
 int b200_set_clusters(b200_net* net, int32_t enable);
 int b200_launch_plan(b200_net* net, int32_t* grid, int32_t* cluster, int32_t* state_bytes);
+/* Owner-mode delivery (0 off, 1 on where it applies, 2 auto = default: on for
+ * networks without synaptic delays, where it is measured faster): each CTA of a multi-CTA
+ * instance delivers only into the target neurons it owns, keeping their state
+ * in shared memory, with per-CTA event FIFOs ordered by due step.  A second
+ * implementation of CSpikeQueue + on_pre (brian2/synapses/spikequeue.h:14-206,
+ * templates/synapses.cpp:20-49); b200_owner_active reports whether the current
+ * launch plan uses it.  b200_set_event_capacity sizes the FIFOs in units of a
+ * CTA's incoming synapses (default 1); an overflow fails the run with
+ * B200_STATUS_CAPACITY and a message. */
+int b200_set_owner(b200_net* net, int32_t enable);
+int b200_owner_active(b200_net* net, int32_t* active);
+int b200_set_event_capacity(b200_net* net, double factor);
 /* Per-instance values of the model's namespace constants (the %CONSTANTS% of the
  * generated code objects, device.py:936-940); scalar blocks are re-evaluated. */
 int b200_set_consts(b200_net* net, int32_t inst, const double* values, int32_t count);

@@ -17,7 +17,20 @@ from oracle import oracle_from_built
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [dict(threads=256), dict(threads=1024), dict(threads=256, ctas_per_inst=3), dict(threads=128, ctas_per_inst=8)]
+# multi-CTA shapes run owner-mode delivery by default; owner=False forces the
+# classic delivery (every CTA delivers any spike's synapses, with atomics)
+SHAPES = [dict(threads=256), dict(threads=1024), dict(threads=256, ctas_per_inst=3), dict(threads=128, ctas_per_inst=8),
+          dict(threads=256, ctas_per_inst=3, owner=False), dict(threads=128, ctas_per_inst=8, owner=False),
+          dict(threads=512, ctas_per_inst=20)]
+
+
+def make_net(spec, built, shape):
+    shape = dict(shape)
+    owner = shape.pop("owner", True)
+    net = W.instantiate(spec, [built], **shape)
+    net.set_owner(owner)
+    assert net.owner_active() == (owner and shape.get("ctas_per_inst", 1) > 1)
+    return net
 
 
 def first_divergence(i1, t1, i2, t2):
@@ -37,7 +50,7 @@ def test_bit_exact_with_reference(case, shape, golden):
     spec_name, build, steps = CASES[case]
     spec = W.load_spec(spec_name)
     meta, z = golden(case)
-    net = W.instantiate(spec, [build(spec)], **SHAPES[shape])
+    net = make_net(spec, build(spec), SHAPES[shape])
     net.run(steps)
     i, ts, cnt = net.spikes(0, 0)
     assert len(i) == meta["n_spikes"]
@@ -49,13 +62,15 @@ def test_bit_exact_with_reference(case, shape, golden):
     np.testing.assert_array_equal(cnt, np.bincount(z["spk_i"], minlength=len(cnt)))
 
 
-def test_split_runs_equal_one_run(golden):
-    """run(a); run(b) == run(a+b): spikes in flight in the delay ring and the
-    pending reset survive the boundary (Network.run continuation)."""
+@pytest.mark.parametrize("owner", [True, False])
+def test_split_runs_equal_one_run(golden, owner):
+    """run(a); run(b) == run(a+b): spikes in flight (delay ring, owner-mode
+    event FIFOs) and the pending reset survive the boundary (Network.run
+    continuation)."""
     spec_name, build, steps = CASES["delays_small_f64"]
     spec = W.load_spec(spec_name)
     meta, z = golden("delays_small_f64")
-    net = W.instantiate(spec, [build(spec)], threads=256, ctas_per_inst=2)
+    net = make_net(spec, build(spec), dict(threads=256, ctas_per_inst=2, owner=owner))
     for chunk in (1, 7, 500, 1000, steps - 1508):
         net.run(chunk)
     i, ts, _ = net.spikes(0, 0)
@@ -119,11 +134,13 @@ def test_batched_instances_equal_separate_oracles():
         np.testing.assert_array_equal(net.download(k, "neurongroup", "v"), o.download(0, "v"))
 
 
-def test_barrier_timeout_reports_status_and_handle_stays_usable():
+@pytest.mark.parametrize("owner", [True, False])
+def test_barrier_timeout_reports_status_and_handle_stays_usable(owner):
     from brian2_gb300.runtime import B200Error
     spec = W.load_spec("cuba_f64")
     b = W.build_cuba(spec, N=2000, seed=3)
     net = W.instantiate(spec, [b], threads=128, ctas_per_inst=4)
+    net.set_owner(owner)
     net.set_wait_limit(50_000_000, fault_rank=1)   # 50 ms; CTA 1 skips its first barrier
     with pytest.raises(B200Error) as e:
         net.run(10)
@@ -134,3 +151,46 @@ def test_barrier_timeout_reports_status_and_handle_stays_usable():
     o = oracle_from_built(spec, b)
     o.run(100)
     np.testing.assert_array_equal(net2.spikes(0, 0)[0], o.spikes(0)[0])
+
+
+def test_owner_fifo_overflow_is_reported():
+    """An event FIFO too small for the traffic: the run fails with a capacity
+    status and a message (events are dropped, no CTA leaves the barrier
+    sequence), and the device stays usable."""
+    from brian2_gb300.runtime import B200Error
+    spec_name, build, steps = CASES["delays_f64"]
+    spec = W.load_spec(spec_name)
+    b = build(spec)
+    net = W.instantiate(spec, [b], threads=256, ctas_per_inst=8)
+    net.set_owner(True)
+    net.set_event_capacity(1e-6)   # 1024 records per CTA
+    assert net.owner_active()
+    with pytest.raises(B200Error) as e:
+        net.run(300)
+    assert e.value.status == 3 and "FIFO" in str(e.value)
+    net2 = W.instantiate(spec, [b], threads=256, ctas_per_inst=8)
+    net2.run(50)
+
+
+def test_owner_equals_classic_on_device_built_network():
+    """1e5 neurons, in-degree 1000, delays 0.1-5 ms, float32, built on the
+    device: owner-mode and classic delivery give the same raster and state
+    (equal increments per target variable make the atomic order immaterial)."""
+    from brian2_gb300.scale import build_delays_scale
+    spec = W.load_spec("delays_f32")
+    out = []
+    for owner in (True, False):
+        net, _ = build_delays_scale(spec, N=100_000, K=1000, seed=77, threads=512, ctas_per_inst=64)
+        net.set_owner(owner)
+        assert net.owner_active() == owner
+        net.run(300)
+        net.run(200)
+        out.append((net.spikes(0, 0), net.download(0, "neurongroup", "v"), net.download(0, "neurongroup", "ge")))
+        net.close()
+    (i0, t0, c0), v0, g0 = out[0]
+    (i1, t1, c1), v1, g1 = out[1]
+    assert len(i0) > 1000
+    np.testing.assert_array_equal(i0, i1)
+    np.testing.assert_array_equal(t0, t1)
+    np.testing.assert_array_equal(v0, v1)
+    np.testing.assert_array_equal(g0, g1)
