@@ -688,7 +688,7 @@ def render_model(spec: dict) -> str:
     w("      B200_PHASE(0);")
     w("      // test hook: CTA `fault_rank` leaves without arriving, the others must time out")
     w("      if (rank == fault_rank && ts == ts0) { ok = false; break; }")
-    w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster)) { ok = false; break; }")
+    w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster, rank)) { ok = false; break; }")
     w("      B200_PHASE(1);")
 
     # ---- Phase B: prefix of tile counts, ring, monitors
@@ -888,7 +888,7 @@ def render_model(spec: dict) -> str:
         w("        }")
         w("      }")
         w(f"      B200_PHASE({3 + pis[0]});")
-    w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster)) { ok = false; break; }")
+    w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster, rank)) { ok = false; break; }")
     w(f"      B200_PHASE({3 + NP});")
     w("    }  // steps")
     w(f"    if (prof && threadIdx.x == 0)")
@@ -1027,6 +1027,9 @@ def render_model(spec: dict) -> str:
         w("  __shared__ int s_own[B200_NG][2];")
         w(f"  __shared__ long long s_head[{max(NP, 1)}], s_tail[{max(NP, 1)}];")
         w(f"  __shared__ int s_qoff[{max(NP, 1) + 1}], s_skip[{max(NP, 1)}];")
+        w(f"  __shared__ int32_t* s_toff[{max(NP, 1)}];        // this CTA's batch table: per-delay offsets,")
+        w(f"  __shared__ long long* s_tbase[{max(NP, 1)}];     // first record and step of each batch")
+        w(f"  __shared__ long long* s_ttag[{max(NP, 1)}];      // (shared memory or global)")
         for gi in range(NG):
             n_ = max(gtables[gi][0].size, 1)
             w(f"  __shared__ double s_Sg{gi}[{n_}]; __shared__ float s_Sg{gi}f[{n_}]; __shared__ long long s_Sg{gi}i[{n_}];")
@@ -1068,9 +1071,30 @@ def render_model(spec: dict) -> str:
                 w(f"        off += ((size_t)(s_own[{gi}][1] - s_own[{gi}][0]) * {sz} + 15) & ~(size_t)15;")
             w("      }")
         for pi in range(NP):
-            w(f"      if (I.p[{pi}].D > 0) {{ s_head[{pi}] = I.p[{pi}].ev.state[2 * rank]; s_tail[{pi}] = I.p[{pi}].ev.state[2 * rank + 1]; }}")
+            w(f"      if (I.p[{pi}].D > 0) {{")
+            w(f"        const b200_fifo_d& F = I.p[{pi}].ev;")
+            w(f"        s_head[{pi}] = F.state[2 * rank]; s_tail[{pi}] = F.state[2 * rank + 1];")
+            w("        if (I.tab_smem) {")
+            w(f"          s_toff[{pi}] = (int32_t*)(s_state + F.tab_off);")
+            w(f"          s_tbase[{pi}] = (long long*)(s_state + F.tab_off + (((size_t)F.RB * (F.W + 1) * 4 + 15) & ~(size_t)15));")
+            w(f"          s_ttag[{pi}] = s_tbase[{pi}] + F.RB;")
+            w("        } else {")
+            w(f"          s_toff[{pi}] = F.off + (size_t)rank * F.RB * (F.W + 1);")
+            w(f"          s_tbase[{pi}] = (long long*)F.base + (size_t)rank * F.RB;")
+            w(f"          s_ttag[{pi}] = (long long*)F.tag + (size_t)rank * F.RB;")
+            w("        }")
+            w("      }")
         w("    }")
         w("    __syncthreads();")
+        w("    if (I.tab_smem) {  // this CTA's batch tables live in shared memory for the launch")
+        for pi in range(NP):
+            w(f"      if (I.p[{pi}].D > 0) {{")
+            w(f"        const b200_fifo_d& F = I.p[{pi}].ev;")
+            w(f"        b200_copy_bytes(s_toff[{pi}], F.off + (size_t)rank * F.RB * (F.W + 1), (size_t)F.RB * (F.W + 1) * 4);")
+            w(f"        b200_copy_bytes(s_tbase[{pi}], F.base + (size_t)rank * F.RB, (size_t)F.RB * 8);")
+            w(f"        b200_copy_bytes(s_ttag[{pi}], F.tag + (size_t)rank * F.RB, (size_t)F.RB * 8);")
+            w("      }")
+        w("    }")
         for gi in range(NG):
             w(f"    for (int u = threadIdx.x; u <= I.g[{gi}].n_tiles; u += blockDim.x) s_tst[{gi} * max_tiles1 + u] = I.g[{gi}].tile_start[u];")
         for gi in range(NG):
@@ -1283,8 +1307,118 @@ def render_model(spec: dict) -> str:
                 w("          __syncthreads();")
                 w("        }")
 
-            w("        // pass 1: events without delay are applied, the others counted per delay")
+            # ---- staging area (events of this step, in shared memory) for this group
+            cs = []
+            for pi in pis:
+                for m, k in enumerate(PAYLOAD[pi]):
+                    sz = SIZE[paths[pi]["vars"][k]["ctype"]]
+                    if m >= len(cs):
+                        cs.append(sz)
+                    else:
+                        cs[m] = max(cs[m], sz)
+            group_ev_bytes.append(8 + sum(cs))
+            w("        int* const st_k = (int*)(s_state + I.stage_off);          // window of the event (-1: none)")
+            w("        int* const st_tgt = st_k + I.stage_cap;                     // target neuron")
+            for m in range(len(cs)):
+                base = "(unsigned char*)(st_tgt + I.stage_cap)" if m == 0 else f"st_col{m - 1} + (size_t){cs[m - 1]} * I.stage_cap"
+                w(f"        unsigned char* const st_col{m} = {base};  // payload column {m}")
+            w("        (void)st_k; (void)st_tgt;")
+
+            def stage_store(pi, q, ind):
+                p = paths[pi]
+                L = [f"const int k = {koff_of(q)} + (int)PQ.odelay[syn] - PQ.dmin;",
+                     "st_k[e] = k;",
+                     "st_tgt[e] = PQ.post[syn];"]
+                for m, k in enumerate(PAYLOAD[pi]):
+                    ct = p["vars"][k]["ctype"]
+                    L.append(f"*({ct}*)(st_col{m} + (size_t)e * {cs[m]}) = (({ct}*)PQ.var[{k}])[syn];")
+                L.append("atomicAdd(&s_nd[k], 1);")
+                return _indent("\n".join(L), ind)
+
+            def stage_apply(pi, ind):
+                """on_pre applied from staged event e (due now)."""
+                p = paths[pi]
+                loads, rest = split_loads(body_code(pi))
+                varptr = {v["ptr"]: k for k, v in enumerate(p.get("vars", []))}
+                L = []
+                for ct, nm, ptr in loads:
+                    if ptr == p["post_ptr"]:
+                        L.append(f"const {ct} {nm} = ({ct})st_tgt[e];")
+                    else:
+                        m = PAYLOAD[pi].index(varptr[ptr])
+                        L.append(f"const {ct} {nm} = *({ct}*)(st_col{m} + (size_t)e * {cs[m]});")
+                L.append(rest)
+                return _indent("\n".join(L), ind)
+
+            def stage_to_fifo(pi, ind):
+                p = paths[pi]
+                L = ["PQ.ev.tgt[rbase + rec] = st_tgt[e];"]
+                for m, k in enumerate(PAYLOAD[pi]):
+                    ct = p["vars"][k]["ctype"]
+                    L.append(f"(({ct}*)PQ.ev.pay[{m}])[rbase + rec] = *({ct}*)(st_col{m} + (size_t)e * {cs[m]});")
+                return _indent("\n".join(L), ind)
+
+            w("        // one pass when the step's events fit the staging area: every synapse is")
+            w("        // read once, events without delay are applied, the others staged and counted")
+            w("        if (threadIdx.x == 0) s_flag = 0;")
+            w("        __syncthreads();")
+            w("        int E1 = 0;")
+            w("        if (I.stage_cap > 0 && NI > 0 && NI <= (int)blockDim.x) {")
+            w("          const int it = threadIdx.x;")
+            w("          int len = 0;")
+            w("          if (it < NI) {")
+            w("            int q = 0;")
+            for q in range(1, L):
+                w(f"            if (it >= s_qoff[{q}]) q = {q};")
+            pexpr = f"{pis[L - 1]}"
+            for q in reversed(range(L - 1)):
+                pexpr = f"(q == {q} ? {pis[q]} : {pexpr})"
+            w(f"            const b200_pathway_d& PD = I.p[{pexpr}];")
+            w("            const int pos = it - s_qoff[q] + pref[PD.tile_lo];")
+            w(f"            const int u = b200_upper_bound(pref, I.g[{sg}].n_tiles + 1, pos) - 1;")
+            w("            const int32_t src = lst[tst[u] + pos - pref[u]];")
+            w("            const int64_t sg_ = (int64_t)(src - PD.src_lo) * I.n_cta + rank;")
+            w("            const int64_t lo = PD.segptr[sg_];")
+            w("            len = (int)(PD.segptr[sg_ + 1] - lo);")
+            w("            s_item_seg[threadIdx.x] = lo;")
+            w("            s_item_q[threadIdx.x] = q;")
+            w("          }")
+            w("          const int eoff = b200_block_exscan(len, s_wsum, &E1);")
+            w("          s_item_off[threadIdx.x] = eoff;")
+            w("          __syncthreads();")
+            w("          if (E1 <= I.stage_cap) {")
+            w("            for (int e0 = threadIdx.x; e0 < E1; e0 += 4 * (int)blockDim.x) {")
+            w("#pragma unroll")
+            w("              for (int qq = 0; qq < 4; ++qq) {")
+            w("                const int e = e0 + qq * (int)blockDim.x;")
+            w("                if (e < E1) {")
+            w("                  const int j = b200_upper_bound(s_item_off, NI, e) - 1;")
+            w("                  const int64_t syn = s_item_seg[j] + (e - s_item_off[j]);")
+            w("                  const int q = s_item_q[j];")
+            for q, pi in enumerate(pis):
+                w(("                  if" if q == 0 else "                  else if") + f" (q == {q}) {{  // {paths[pi]['name']}")
+                w(f"                    if (I.p[{pi}].D == 0) {{  // no delay: applied now")
+                w("                      st_k[e] = -1;")
+                w("                      const int64_t _idx = syn; const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+                w(body_decls(pi, 22))
+                w(_indent(body_code(pi), 22))
+                w("                    } else {")
+                w(f"                      const b200_pathway_d& PQ = I.p[{pi}];")
+                w(stage_store(pi, q, 22))
+                w("                    }")
+                w("                  }")
+            w("                }")
+            w("              }")
+            w("            }")
+            w("            if (threadIdx.x == 0) s_flag = 1;")
+            w("          }")
+            w("          __syncthreads();")
+            w("        }")
+            w("        const bool staged = s_flag != 0;")
+            w("        if (!staged) {")
+            w("          // pass 1 over global memory: events without delay applied, the others counted")
             traverse(1)
+            w("        }")
             w("        B200_PHASE(3);")
             w("        if (WT > 0) {")
             w("          // batch offsets (exclusive, per pathway) and the FIFO capacity check")
@@ -1315,42 +1449,62 @@ def render_model(spec: dict) -> str:
             w("          if (s_step >= 0) {")
             for q, pi in enumerate(pis):
                 w(f"            if (I.p[{pi}].D > 0) {{  // batch table entry of step s_step")
-                w(f"              const b200_fifo_d& F = I.p[{pi}].ev;")
-                w("              const int b = (int)(s_step % F.RB);")
-                w("              const int64_t row = (int64_t)rank * F.RB + b;")
+                w(f"              const int b = (int)(s_step % I.p[{pi}].ev.RB);")
                 w(f"              for (int kk = threadIdx.x; kk <= W{q}; kk += blockDim.x)")
-                w(f"                F.off[row * (F.W + 1) + kk] = s_skip[{pi}] ? 0 : s_base[{koff_of(q)} + kk] - s_base[{koff_of(q)}];")
-                w(f"              if (threadIdx.x == 0) {{ F.base[row] = s_head[{pi}]; F.tag[row] = s_step; }}")
+                w(f"                s_toff[{pi}][b * (W{q} + 1) + kk] = s_skip[{pi}] ? 0 : s_base[{koff_of(q)} + kk] - s_base[{koff_of(q)}];")
+                w(f"              if (threadIdx.x == 0) {{ s_tbase[{pi}][b] = s_head[{pi}]; s_ttag[{pi}][b] = s_step; }}")
                 w("            }")
             w("          }")
             w("          for (int k = threadIdx.x; k < WT; k += blockDim.x) s_nd[k] = 0;")
             w("          __syncthreads();")
-            w("          // pass 2: the records, in delay order, at the FIFO head")
+            w("          if (staged) {")
+            w("            // records from the staging area; the events due now are applied at once")
+            w("            for (int e = threadIdx.x; e < E1; e += blockDim.x) {")
+            w("              const int k = st_k[e];")
+            w("              if (k >= 0) {")
+            w(window_of("k", 16))
+            for q, pi in enumerate(pis):
+                w(("                if" if q == 0 else "                else if") + f" (q == {q} && !s_skip[{pi}]) {{  // {paths[pi]['name']}")
+                w(body_decls(pi, 18))
+                w("                  if (s_step + PQ.dmin + kk == ts) {")
+                w(stage_apply(pi, 20))
+                w("                  } else {")
+                w(f"                    const int64_t p_ = (int64_t)(s_base[k] - s_base[{koff_of(q)}]) + atomicAdd(&s_nd[k], 1);")
+                w(f"                    const int64_t rec = (s_head[{pi}] + p_) & (PQ.ev.cap - 1);")
+                w("                    const int64_t rbase = (int64_t)rank * PQ.ev.cap;")
+                w(stage_to_fifo(pi, 20))
+                w("                  }")
+                w("                }")
+            w("              }")
+            w("            }")
+            w("            __syncthreads();")
+            w("          } else {")
+            w("            // pass 2 over global memory: the records, in delay order, at the FIFO head")
             traverse(2)
+            w("          }")
             w("          if (threadIdx.x == 0 && s_step >= 0) {")
             for q, pi in enumerate(pis):
                 w(f"            if (I.p[{pi}].D > 0 && !s_skip[{pi}]) s_head[{pi}] += s_base[{koff_of(q)} + W{q}] - s_base[{koff_of(q)}];")
             w("          }")
             w("          B200_PHASE(4);")
-            w("          // delivery of the events due at ts: window (pathway, delay d) is the")
-            w("          // part of the batch of step ts - d with that delay")
+            w("          // delivery of the events due at ts: window (pathway, delay d) is the part")
+            w("          // of the batch of step ts - d with that delay (already applied when staged)")
             w("          for (int k = threadIdx.x; k < WT; k += blockDim.x) {")
             w(window_of("k", 12))
-            pexpr = f"{pis[L - 1]}"
-            for q in reversed(range(L - 1)):
-                pexpr = f"(q == {q} ? {pis[q]} : {pexpr})"
-            w(f"            const b200_pathway_d& PD = I.p[{pexpr}];")
-            w("            const int64_t sb = ts - (PD.dmin + kk);")
             w("            int n = 0;")
             w("            int64_t lo = 0;")
-            w("            if (sb >= 0) {")
-            w("              const int64_t row = (int64_t)rank * PD.ev.RB + (int)(sb % PD.ev.RB);")
-            w("              if (PD.ev.tag[row] == sb) {")
-            w("                const int32_t* o = PD.ev.off + row * (PD.ev.W + 1);")
-            w("                lo = PD.ev.base[row] + o[kk];")
-            w("                n = o[kk + 1] - o[kk];")
-            w("              }")
-            w("            }")
+            for q, pi in enumerate(pis):
+                w(("            if" if q == 0 else "            else if") + f" (q == {q}) {{")
+                w(f"              const int64_t sb = ts - (I.p[{pi}].dmin + kk);")
+                w("              if (sb >= 0 && !(staged && sb == s_step)) {")
+                w(f"                const int b = (int)(sb % I.p[{pi}].ev.RB);")
+                w(f"                if (s_ttag[{pi}][b] == sb) {{")
+                w(f"                  const int32_t* o = s_toff[{pi}] + b * (W{q} + 1);")
+                w(f"                  lo = s_tbase[{pi}][b] + o[kk];")
+                w("                  n = o[kk + 1] - o[kk];")
+                w("                }")
+                w("              }")
+                w("            }")
             w("            s_nd[k] = n; s_wbase[k] = lo;")
             w("          }")
             w("          __syncthreads();")
@@ -1391,11 +1545,10 @@ def render_model(spec: dict) -> str:
             w("          if (threadIdx.x == 0) {")
             for q, pi in enumerate(pis):
                 w(f"            if (I.p[{pi}].D > 0) {{")
-                w(f"              const b200_fifo_d& F = I.p[{pi}].ev;")
                 w(f"              const int64_t sb = ts - I.p[{pi}].D;")
                 w("              if (sb >= 0) {")
-                w("                const int64_t row = (int64_t)rank * F.RB + (int)(sb % F.RB);")
-                w(f"                if (F.tag[row] == sb) s_tail[{pi}] = F.base[row] + F.off[row * (F.W + 1) + F.W];")
+                w(f"                const int b = (int)(sb % I.p[{pi}].ev.RB);")
+                w(f"                if (s_ttag[{pi}][b] == sb) s_tail[{pi}] = s_tbase[{pi}][b] + s_toff[{pi}][b * (W{q} + 1) + W{q}];")
                 w("              }")
                 w("            }")
             w("          }")
@@ -1431,6 +1584,15 @@ def render_model(spec: dict) -> str:
                 w(f"      b200_copy_bytes((char*)I.g[{gi}].var[{k}] + (size_t)s_own[{gi}][0] * {sz}, (const char*)s_gv[{gi}][{k}] + (size_t)s_own[{gi}][0] * {sz},")
                 w(f"                      (size_t)(s_own[{gi}][1] - s_own[{gi}][0]) * {sz});")
         w("    }")
+        w("    if (I.tab_smem) {")
+        for pi in range(NP):
+            w(f"      if (I.p[{pi}].D > 0) {{")
+            w(f"        const b200_fifo_d& F = I.p[{pi}].ev;")
+            w(f"        b200_copy_bytes(F.off + (size_t)rank * F.RB * (F.W + 1), s_toff[{pi}], (size_t)F.RB * (F.W + 1) * 4);")
+            w(f"        b200_copy_bytes(F.base + (size_t)rank * F.RB, s_tbase[{pi}], (size_t)F.RB * 8);")
+            w(f"        b200_copy_bytes(F.tag + (size_t)rank * F.RB, s_ttag[{pi}], (size_t)F.RB * 8);")
+            w("      }")
+        w("    }")
         w("    if (threadIdx.x == 0) {")
         for pi in range(NP):
             w(f"      if (I.p[{pi}].D > 0) {{ I.p[{pi}].ev.state[2 * rank] = s_head[{pi}]; I.p[{pi}].ev.state[2 * rank + 1] = s_tail[{pi}]; }}")
@@ -1447,8 +1609,10 @@ def render_model(spec: dict) -> str:
         w("}")
         w("")
 
+    group_ev_bytes = []
     if OWNER:
         emit_owner_kernel()
+    OWNER_EV_BYTES = max(group_ev_bytes) if group_ev_bytes else 8
 
     # ------------------------------------------------------------- launch glue
     w("// `tcode` = threads | (min CTAs per SM - 1) << 16: the (512, 2) variant caps")
@@ -1534,7 +1698,7 @@ def render_model(spec: dict) -> str:
     w(f'static const b200_model_info B200_MODEL = {{"{spec["name"]}", {NG}, {NP}, {len(spkmons)}, {len(ratemons)}, {len(statemons)},')
     w("  b200_groups, b200_pathways, b200_spkmon, b200_ratemon, b200_statemon,")
     w(f"  {len(consts)}, b200_const_names, b200_const_defaults, b200_eval_scalars, b200_launch, b200_max_active,")
-    w(f"  b200_static_smem, b200_max_cluster, {NPH}, {1 if OWNER else 0}}};")
+    w(f"  b200_static_smem, b200_max_cluster, {NPH}, {1 if OWNER else 0}, {OWNER_EV_BYTES}}};")
     w("")
     w('#include "b200_host.h"')
     w("")

@@ -57,6 +57,7 @@ struct b200_group_d {
 struct b200_fifo_d {
   int64_t cap;            // records per CTA (power of two)
   int32_t RB, W;          // batch-table slots, delays per batch
+  int32_t tab_off, _pad;  // byte offset of this CTA's batch table in shared memory (when cached there)
   int32_t* tgt;           // [n_cta * cap] target neuron (within the target group)
   void* pay[B200_MAX_PAYLOAD];  // [n_cta * cap] payload values (synaptic variables)
   int64_t* state;         // [n_cta * 2] head, tail (absolute record positions)
@@ -124,6 +125,10 @@ struct b200_inst_d {
   int32_t lag;            // 1: every delay >= 1 step, a step pushes the previous step's spikes
   int64_t ts_base;        // step whose arrival count starts at 0 in bar64
   unsigned long long* bar64;  // [1] arrivals of the split barrier
+  int32_t tab_smem;       // 1: the batch tables are kept in shared memory for the launch
+  int32_t stage_off;      // byte offset of the event staging area in shared memory
+  int32_t stage_cap;      // events it holds (0: none; pushes take two passes over global memory)
+  int32_t _pad_o;
   b200_group_d g[B200_MAX_GROUPS];
   b200_pathway_d p[B200_MAX_PATHWAYS];
   b200_spkmon_d sm[B200_MAX_SPKMON];
@@ -196,6 +201,7 @@ struct b200_model_info {
   // 1: every pathway's on_pre only adds to variables of its target neuron from
   // synaptic values and constants, so owner-mode delivery applies
   int owner_ok;
+  int owner_event_bytes;  // shared-memory bytes per staged event
 };
 // `tcode` bit selecting the owner-mode kernel
 #define B200_TCODE_OWNER (1 << 20)
@@ -326,9 +332,10 @@ __device__ __forceinline__ void b200_cluster_sync() {
 // Barrier over the n_cta CTAs of one instance.  Bounded: after `limit_ns` of
 // waiting the instance status is set to B200_ERR_BARRIER_TIMEOUT and the call
 // returns false, so a kernel never spins forever.  With n_cta == 1 it is a
-// plain __syncthreads.  `gen` is the CTA's private copy of the generation.
+// plain __syncthreads.  `gen` counts the barriers this CTA has passed; `rank`
+// is the CTA's rank within the instance.
 __device__ __forceinline__ bool b200_inst_barrier(const b200_inst_d& I, unsigned& gen,
-                                                  uint64_t limit_ns, int cluster) {
+                                                  uint64_t limit_ns, int cluster, int rank) {
   if (cluster) {
     b200_cluster_sync();
     return true;
@@ -337,32 +344,29 @@ __device__ __forceinline__ bool b200_inst_barrier(const b200_inst_d& I, unsigned
   if (I.n_cta == 1) return true;
   __shared__ int ok;
   if (threadIdx.x == 0) {
+    // one arrival word, no reset: rank 0 adds 2^31 - (n_cta - 1), every other
+    // CTA adds 1, so bit 31 flips exactly when the last CTA has arrived (the
+    // scheme of the cooperative-groups grid barrier); waiters poll that bit
     ok = 1;
+    const unsigned nb = rank == 0 ? 0x80000000u - (unsigned)(I.n_cta - 1) : 1u;
     __threadfence();
-    const unsigned g = gen;
-    const unsigned arrived = atomicAdd(&I.bar[0], 1u);
-    if (arrived == (unsigned)I.n_cta - 1) {
-      I.bar[0] = 0;
-      __threadfence();
-      b200_st_release(&I.bar[1], g + 1);
+    const unsigned old = atomicAdd(&I.bar[0], nb);
+    if (((old + nb) ^ old) & 0x80000000u) {
+      __threadfence();  // this CTA completed the barrier: order its reads after the others' writes
     } else {
       const uint64_t t0 = b200_globaltimer();
       int spins = 0;
-      while (b200_ld_acquire(&I.bar[1]) == g) {
-        if (++spins > 64) {
-          __nanosleep(64);
-          if ((spins & 255) == 0) {
-            if (b200_globaltimer() - t0 > limit_ns || *((volatile int32_t*)I.status) != 0) {
-              atomicCAS(I.status, 0, B200_ERR_BARRIER_TIMEOUT);
-              ok = 0;
-              break;
-            }
-          }
+      while (((b200_ld_acquire(&I.bar[0]) ^ old) & 0x80000000u) == 0) {
+        if (++spins > 32) __nanosleep(32);
+        if ((spins & 255) == 0 &&
+            (b200_globaltimer() - t0 > limit_ns || *((volatile int32_t*)I.status) != 0)) {
+          atomicCAS(I.status, 0, B200_ERR_BARRIER_TIMEOUT);
+          ok = 0;
+          break;
         }
       }
     }
-    gen = g + 1;
-    __threadfence();
+    ++gen;
   }
   __syncthreads();
   return ok != 0;

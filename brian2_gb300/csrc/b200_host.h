@@ -653,6 +653,7 @@ static int b200_owner_pathway(b200_net* n, int k, int p, b200_pathway_d& PD) {
   for (int m = 0; m < PI.n_payload; ++m) PD.var[PI.payload_var[m]] = P.ovar[m].p;
   PD.odelay = (const uint16_t*)P.odelay.p;
   memset(&PD.ev, 0, sizeof(PD.ev));
+  if (!delays) { PD.D = 0; PD.dmin = 0; }  // no FIFO: a pathway without synapses has no events
   if (delays) {
     PD.ev.cap = P.ev_cap; PD.ev.RB = P.ev_RB; PD.ev.W = P.ev_W;
     PD.ev.tgt = (int32_t*)P.ev_tgt.p;
@@ -933,6 +934,37 @@ static int b200_prepare(b200_net* n) {
       n->h_insts[k].cache_bytes = (int32_t)bytes;
       n->h_insts[k].cache_lists = lists ? 1 : 0;
       n->state_bytes = std::max<long>(n->state_bytes, bytes);
+    }
+    if (n->owner) {
+      // after the state cache: the batch tables of the event FIFOs, then a
+      // staging area for one step's events (one pass over the synapses)
+      int total_cta = 0, n_sm_o = 0, dev_o = 0;
+      for (int k = 0; k < n->n_inst; ++k) total_cta += n->inst[k].n_cta;
+      B200_CU(n, cudaGetDevice(&dev_o));
+      B200_CU(n, cudaDeviceGetAttribute(&n_sm_o, cudaDevAttrMultiProcessorCount, dev_o));
+      const long room = total_cta > n_sm_o ? std::min(budget, (long)optin / 2 - other - 1024) : budget;
+      for (int k = 0; k < n->n_inst; ++k) {
+        b200_inst_d& D = n->h_insts[k];
+        long off = ((long)D.cache_bytes + 15) & ~15L;
+        long tab = 0;
+        for (int p = 0; p < M->n_pathways; ++p)
+          if (D.p[p].ev.cap > 0)
+            tab += (((long)D.p[p].ev.RB * (D.p[p].ev.W + 1) * 4 + 15) & ~15L) + (long)D.p[p].ev.RB * 16;
+        D.tab_smem = (tab > 0 && off + tab <= room) ? 1 : 0;
+        if (D.tab_smem)
+          for (int p = 0; p < M->n_pathways; ++p)
+            if (D.p[p].ev.cap > 0) {
+              D.p[p].ev.tab_off = (int32_t)off;
+              off += (((long)D.p[p].ev.RB * (D.p[p].ev.W + 1) * 4 + 15) & ~15L) + (long)D.p[p].ev.RB * 16;
+            }
+        const long ev = std::max(8, M->owner_event_bytes);
+        long cap = off < room ? std::min<long>(16384, (room - off) / ev) : 0;
+        cap &= ~3L;
+        D.stage_off = (int32_t)off;
+        D.stage_cap = (int32_t)cap;
+        off += cap * ev;
+        n->state_bytes = std::max<long>(n->state_bytes, off);
+      }
     }
   }
   int max_per_sm = M->max_active_ctas(n->tcode(), n->max_tiles1, n->max_w, n->state_bytes);
