@@ -143,6 +143,7 @@ class B200Device(CPPStandaloneDevice):
         self.b200_run_options = dict(threads=None, ctas_per_inst=None)
         self.b200_last_network = None
         self.b200_timings = []
+        self.b200_job_dir = None
 
     def reinit(self):
         opts = self.b200_run_options
@@ -396,6 +397,8 @@ class B200Device(CPPStandaloneDevice):
         for k in ("threads", "ctas_per_inst"):
             if k in kwds:
                 self.b200_run_options[k] = kwds.pop(k)
+        if "b200_defer" in kwds:
+            self.b200_run_options["defer"] = bool(kwds.pop("b200_defer"))
         # host code after the first GPU run cannot be executed before it
         if self.b200_runs:
             first = self.b200_runs[0]["queue_len"]
@@ -419,68 +422,74 @@ class B200Device(CPPStandaloneDevice):
         fname = os.path.join(self.results_dir, self.get_array_filename(var))
         np.ascontiguousarray(values, dtype=var.dtype).tofile(fname)
 
-    def _run_on_gpu(self):
-        from .runtime import Model, Network
+    def b200_export_job(self, directory):
+        """Writes the recorded runs as a job directory (:mod:`brian2_gb300.job`):
+        the spec and the initial state that the standalone ``main`` wrote."""
+        from .job import write_job
         spec0 = self.b200_runs[0]["spec"]
         pub = self.public_spec(spec0)
-        model = Model.get(pub)
-        clock = self.b200_runs[0]["clock"]
-        dt = float(clock.dt_)
-        sizes = [len(g["_obj"]) for g in spec0["groups"]]
-        net = Network(model, [sizes], dt)
-        threads = self.b200_run_options.get("threads") or (1024 if max(sizes) <= 8192 else 256)
-        net.configure(threads=threads, ctas_per_inst=self.b200_run_options.get("ctas_per_inst") or 1)
-        # initial state written by the standalone main program
-        for gi, g in enumerate(spec0["groups"]):
-            for v in g["vars"]:
-                net.upload(0, gi, v["name"], self._load(g["_obj"].variables[v["name"]]))
-        for pi, p in enumerate(spec0["pathways"]):
-            syn = p["_obj"].synapses
-            pre = self._load(syn.variables["_synaptic_pre"]).astype(np.int64) - p["_src_range"][0]
-            post = self._load(syn.variables["_synaptic_post"]).astype(np.int64) - p["_tgt_range"][0]
-            dvar = p["_obj"].variables["delay"]
-            if dvar.scalar:
-                d = self._load(dvar)
-                scalar_delay = int(float(d[0]) / dt + 0.5) if d.size else 0
-                steps = None
-            else:
-                d = self._load(dvar)
-                steps = (d / dt + 0.5).astype(np.int32)
-                scalar_delay = 0
-            net.set_synapses(0, pi, pre, post, steps, scalar_delay, p["_src_range"], p["_tgt_range"])
-            for v in p["vars"]:
-                net.upload_synapse_var(0, pi, v["name"], self._load(syn.variables[v["name"]]))
-        for mi, m in enumerate(spec0["spike_monitors"]):
-            net.set_spikemon_range(0, mi, *m["_range"])
-        for mi, m in enumerate(spec0["rate_monitors"]):
-            net.set_ratemon_range(0, mi, *m["_range"])
-        for mi, m in enumerate(spec0["state_monitors"]):
-            idx = self._load(m["_obj"].variables["_indices"]).astype(np.int32)
-            net.set_statemon(0, mi, idx + m["_range"][0], m["_vars"])
-        ts0 = int(self._load(clock.variables["timestep"])[0])
-        net.set_step(0, ts0)
-        net.reset_monitors(0)
-        total_ms = 0.0
-        t_wall = time.time()
-        for r in self.b200_runs:
+        for r in self.b200_runs[1:]:
             if r["spec"] is not spec0 and self.public_spec(r["spec"]) != pub:
                 raise NotImplementedError("b200: the network changed between runs")
-            net.run(r["n_steps"])
-            total_ms += net.last_run_ms()
-        wall = time.time() - t_wall
-        self.b200_timings = [("b200_step_kernel", total_ms)]
-        self._last_run_time = total_ms * 1e-3
+        clock = self.b200_runs[0]["clock"]
+        dt = float(clock.dt_)
+        init = {}
+        for gi, g in enumerate(spec0["groups"]):
+            init[f"g{gi}_N"] = np.int64(len(g["_obj"]))
+            for v in g["vars"]:
+                init[f"g{gi}_{v['name']}"] = self._load(g["_obj"].variables[v["name"]])
+        for pi, p in enumerate(spec0["pathways"]):
+            syn = p["_obj"].synapses
+            init[f"p{pi}_pre"] = (self._load(syn.variables["_synaptic_pre"]).astype(np.int64)
+                                  - p["_src_range"][0]).astype(np.int32)
+            init[f"p{pi}_post"] = (self._load(syn.variables["_synaptic_post"]).astype(np.int64)
+                                   - p["_tgt_range"][0]).astype(np.int32)
+            dvar = p["_obj"].variables["delay"]
+            d = self._load(dvar)
+            if dvar.scalar:
+                init[f"p{pi}_scalar_delay"] = np.int64(int(float(d[0]) / dt + 0.5) if d.size else 0)
+            else:
+                init[f"p{pi}_scalar_delay"] = np.int64(0)
+                init[f"p{pi}_delay_steps"] = (d / dt + 0.5).astype(np.int32)
+            init[f"p{pi}_src_range"] = np.asarray(p["_src_range"], np.int64)
+            init[f"p{pi}_tgt_range"] = np.asarray(p["_tgt_range"], np.int64)
+            for v in p["vars"]:
+                init[f"p{pi}_{v['name']}"] = self._load(syn.variables[v["name"]])
+        for mi, m in enumerate(spec0["spike_monitors"]):
+            init[f"sm{mi}_range"] = np.asarray(m["_range"], np.int64)
+        for mi, m in enumerate(spec0["rate_monitors"]):
+            init[f"rm{mi}_range"] = np.asarray(m["_range"], np.int64)
+        for mi, m in enumerate(spec0["state_monitors"]):
+            idx = self._load(m["_obj"].variables["_indices"]).astype(np.int32)
+            init[f"stm{mi}_idx"] = idx + m["_range"][0]
+            init[f"stm{mi}_vars"] = np.asarray(m["_vars"])
+        init["ts0"] = np.int64(int(self._load(clock.variables["timestep"])[0]))
+        write_job(directory, pub, init, [r["n_steps"] for r in self.b200_runs], dt, self.b200_run_options)
+        self.b200_job_dir = directory
+        return directory
+
+    def b200_import_results(self, directory=None):
+        """Writes the outputs of a job run (``out.npz``) into the standalone
+        results files, where ``get_value`` and the monitors read them."""
+        directory = directory or self.b200_job_dir
+        spec0 = self.b200_runs[0]["spec"]
+        clock = self.b200_runs[0]["clock"]
+        dt = float(clock.dt_)
+        with np.load(os.path.join(directory, "out.npz")) as z:
+            out = {k: z[k] for k in z.files}
+        ts0 = int(out["ts0"])
+        self.b200_timings = [("b200_step_kernel", float(out["device_ms"]))]
+        self._last_run_time = float(out["device_ms"]) * 1e-3
         self._last_run_completed_fraction = 1.0
-        # write back in the standalone results format
         for gi, g in enumerate(spec0["groups"]):
             for v in g["vars"]:
-                self._store(g["_obj"].variables[v["name"]], net.download(0, gi, v["name"]))
+                self._store(g["_obj"].variables[v["name"]], out[f"g{gi}_{v['name']}"])
         for pi, p in enumerate(spec0["pathways"]):
             syn = p["_obj"].synapses
             for v in p["vars"]:
-                self._store(syn.variables[v["name"]], net.download_synapse_var(0, pi, v["name"]))
+                self._store(syn.variables[v["name"]], out[f"p{pi}_{v['name']}"])
         for mi, m in enumerate(spec0["spike_monitors"]):
-            i, ts, cnt = net.spikes(0, mi)
+            i, ts, cnt = out[f"sm{mi}_i"], out[f"sm{mi}_ts"], out[f"sm{mi}_count"]
             mon = m["_obj"]
             self._store(mon.variables["i"], i)
             self._store(mon.variables["t"], ts.astype(np.float64) * dt)
@@ -488,7 +497,7 @@ class B200Device(CPPStandaloneDevice):
             self._store(mon.variables["count"], cnt[: hi - lo])
             self._store(mon.variables["N"], np.array([len(i)]))
         for mi, m in enumerate(spec0["rate_monitors"]):
-            c = net.rate_counts(0, mi)
+            c = out[f"rm{mi}_counts"]
             mon = m["_obj"]
             lo, hi = m["_range"]
             n = hi - lo
@@ -497,19 +506,31 @@ class B200Device(CPPStandaloneDevice):
             self._store(mon.variables["t"], (ts0 + np.arange(len(c))).astype(np.float64) * dt)
             self._store(mon.variables["N"], np.array([len(c)]))
         for mi, m in enumerate(spec0["state_monitors"]):
-            tr = net.state_trace(0, mi)
+            tr = out[f"stm{mi}_trace"]
             mon = m["_obj"]
             self._store(mon.variables["t"], (ts0 + np.arange(tr.shape[0])).astype(np.float64) * dt)
             for k, v in enumerate(m["_vars"]):
                 self._store(mon.variables[v], tr[:, k, :])
                 mon.variables[v].size = tr[:, k, :].shape
             self._store(mon.variables["N"], np.array([tr.shape[0]]))
-        ts_end = net.step(0)
+        ts_end = int(out["ts_end"])
         self._store(clock.variables["timestep"], np.array([ts_end]))
         self._store(clock.variables["t"], np.array([ts_end * dt]))
-        self.b200_last_network = net
-        logger.debug(f"b200: {sum(r['n_steps'] for r in self.b200_runs)} steps in {total_ms:.2f} ms "
-                     f"(device), {wall:.3f} s wall")
+        logger.debug(f"b200: {sum(r['n_steps'] for r in self.b200_runs)} steps in "
+                     f"{float(out['device_ms']):.2f} ms (device)")
+
+    def _run_on_gpu(self):
+        """Export the runs as a job, run it on this host's GPU, import the
+        results.  With ``build(..., b200_defer=True)`` only the job is written
+        (to be run where the GPU is, then ``b200_import_results``)."""
+        from .job import run_job
+        directory = self.b200_export_job(os.path.join(self.project_dir, "b200_job"))
+        if self.b200_run_options.get("defer"):
+            logger.info(f"b200: job written to {directory}; run it with `python -m brian2_gb300.job "
+                        f"{directory}` and import the results with device.b200_import_results()")
+            return
+        run_job(directory)
+        self.b200_import_results(directory)
 
 
 b200_device = B200Device()

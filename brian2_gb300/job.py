@@ -1,0 +1,121 @@
+"""A network run as a self-contained job directory (no Brian2 needed).
+
+``set_device('b200')`` (:mod:`brian2_gb300.brian_device`) writes, after
+Brian's standalone ``main`` has built the network, a job directory:
+
+* ``spec.json``: the network spec (groups, variables, Brian's generated code
+  snippets, pathways, monitors, namespace constants);
+* ``init.npz``: the initial state written by ``main`` (group variables,
+  synapse indices, quantised delays and synaptic variables, monitor ranges and
+  recorded indices, the clock's time step);
+* ``job.json``: dt, the step counts of the recorded ``run()`` calls and the
+  launch options.
+
+:func:`run_job` executes it on the GPU through the C ABI and writes ``out.npz``
+(final state, synaptic variables, monitor contents, device time); the plugin
+turns that into the standalone results files.  The split is the reference's
+own: ``device.build`` writes a project, the project runs where it is compiled,
+and results come back as files (``brian2/devices/cpp_standalone/device.py:
+1184-1351``).  So a network built where Brian2 is installed can run on a GPU
+host that only has this package::
+
+    python -m brian2_gb300.job <job directory> [--threads T] [--ctas C]
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+
+def write_job(directory, spec, init, runs, dt, options=None):
+    os.makedirs(directory, exist_ok=True)
+    with open(os.path.join(directory, "spec.json"), "w") as f:
+        json.dump(spec, f, indent=1, sort_keys=True)
+    np.savez_compressed(os.path.join(directory, "init.npz"), **init)
+    with open(os.path.join(directory, "job.json"), "w") as f:
+        json.dump(dict(dt=float(dt), runs=[int(r) for r in runs], options=dict(options or {})), f, indent=1)
+
+
+def load_job(directory):
+    with open(os.path.join(directory, "spec.json")) as f:
+        spec = json.load(f)
+    with open(os.path.join(directory, "job.json")) as f:
+        job = json.load(f)
+    with np.load(os.path.join(directory, "init.npz")) as z:
+        init = {k: z[k] for k in z.files}
+    return spec, init, job
+
+
+def run_job(directory, threads=None, ctas_per_inst=None, write=True):
+    """Runs a job on the GPU; returns (and writes as out.npz) its outputs."""
+    from .runtime import Model, Network
+    spec, init, job = load_job(directory)
+    opts = dict(job.get("options", {}))
+    dt = job["dt"]
+    model = Model.get(spec)
+    sizes = [int(init[f"g{gi}_N"]) for gi in range(len(spec["groups"]))]
+    net = Network(model, [sizes], dt)
+    threads = threads or opts.get("threads") or (1024 if max(sizes) <= 8192 else 256)
+    ctas = ctas_per_inst or opts.get("ctas_per_inst") or 1
+    net.configure(threads=threads, ctas_per_inst=ctas)
+    for gi, g in enumerate(spec["groups"]):
+        for v in g["vars"]:
+            net.upload(0, gi, v["name"], init[f"g{gi}_{v['name']}"])
+    for pi, p in enumerate(spec.get("pathways", [])):
+        steps = init[f"p{pi}_delay_steps"] if f"p{pi}_delay_steps" in init else None
+        net.set_synapses(0, pi, init[f"p{pi}_pre"], init[f"p{pi}_post"], steps, int(init[f"p{pi}_scalar_delay"]),
+                         tuple(int(x) for x in init[f"p{pi}_src_range"]),
+                         tuple(int(x) for x in init[f"p{pi}_tgt_range"]))
+        for v in p.get("vars", []):
+            net.upload_synapse_var(0, pi, v["name"], init[f"p{pi}_{v['name']}"])
+    for mi in range(len(spec.get("spike_monitors", []))):
+        net.set_spikemon_range(0, mi, *(int(x) for x in init[f"sm{mi}_range"]))
+    for mi in range(len(spec.get("rate_monitors", []))):
+        net.set_ratemon_range(0, mi, *(int(x) for x in init[f"rm{mi}_range"]))
+    for mi, m in enumerate(spec.get("state_monitors", [])):
+        net.set_statemon(0, mi, init[f"stm{mi}_idx"], list(init[f"stm{mi}_vars"]))
+    ts0 = int(init["ts0"])
+    net.set_step(0, ts0)
+    net.reset_monitors(0)
+    total_ms, t0 = 0.0, time.time()
+    for n in job["runs"]:
+        net.run(int(n))
+        total_ms += net.last_run_ms()
+    out = dict(device_ms=np.float64(total_ms), wall_s=np.float64(time.time() - t0), ts_end=np.int64(net.step(0)),
+               ts0=np.int64(ts0))
+    for gi, g in enumerate(spec["groups"]):
+        for v in g["vars"]:
+            out[f"g{gi}_{v['name']}"] = net.download(0, gi, v["name"])
+    for pi, p in enumerate(spec.get("pathways", [])):
+        for v in p.get("vars", []):
+            out[f"p{pi}_{v['name']}"] = net.download_synapse_var(0, pi, v["name"])
+    for mi in range(len(spec.get("spike_monitors", []))):
+        i, ts, cnt = net.spikes(0, mi)
+        out[f"sm{mi}_i"], out[f"sm{mi}_ts"], out[f"sm{mi}_count"] = i, ts, cnt
+    for mi in range(len(spec.get("rate_monitors", []))):
+        out[f"rm{mi}_counts"] = net.rate_counts(0, mi)
+    for mi in range(len(spec.get("state_monitors", []))):
+        out[f"stm{mi}_trace"] = net.state_trace(0, mi)
+    net.close()
+    if write:
+        np.savez(os.path.join(directory, "out.npz"), **out)
+    return out
+
+
+def main(argv=None):
+    import argparse
+    ap = argparse.ArgumentParser(description="run a b200 job directory on the GPU")
+    ap.add_argument("directory")
+    ap.add_argument("--threads", type=int, default=None)
+    ap.add_argument("--ctas", type=int, default=None)
+    a = ap.parse_args(argv)
+    out = run_job(a.directory, a.threads, a.ctas)
+    print(f"{a.directory}: steps {int(out['ts0'])}..{int(out['ts_end'])}, {float(out['device_ms']):.2f} ms on the device")
+
+
+if __name__ == "__main__":
+    sys.exit(main())

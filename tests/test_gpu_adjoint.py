@@ -32,7 +32,7 @@ def test_adjoint_equals_autograd_reference_f64():
     loss = P.loss(W, Wo, tm)
     loss.backward()
     rl, gW, gWo, gT, _ = adjoint_ref.loss_and_grads(P.prob, cfg)
-    assert abs(float(loss) - rl) <= 1e-12 * abs(rl)
+    assert abs(loss.item() - rl) <= 1e-12 * abs(rl)
     for g, r in ((W.grad.cpu().numpy(), gW), (Wo.grad.cpu().numpy(), gWo)):
         assert np.abs(r).max() > 0
         np.testing.assert_allclose(g, r, rtol=1e-8, atol=1e-9 * np.abs(r).max())

@@ -1,0 +1,28 @@
+"""The drop-in path end to end: a job that set_device('b200') wrote from the
+reference's own script (tests/golden/jobs) runs on the GPU through
+brian2_gb300.job and reproduces the reference's fixture of the same case."""
+import os
+
+import numpy as np
+import pytest
+
+from brian2_gb300.job import run_job
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.mark.parametrize("case,ctas", [("cuba_small_f64", 1), ("delays_small_f64", 1), ("cobahh_small_f64", 1),
+                                       ("cuba_small_f64", 4), ("delays_small_f64", 4)])
+def test_plugin_job_reproduces_reference(case, ctas, golden):
+    meta, z = golden(case)
+    out = run_job(os.path.join(HERE, "golden", "jobs", case), ctas_per_inst=ctas, write=False)
+    np.testing.assert_array_equal(out["sm0_i"], z["spk_i"])
+    np.testing.assert_array_equal(out["sm0_ts"], z["spk_ts"])
+    assert int(out["ts_end"]) == meta["n_steps"]
+    if case.startswith("cobahh"):   # device exp/expm1: last-ulp differences in the state
+        np.testing.assert_allclose(out["g0_v"], z["v"], rtol=1e-9, atol=0)
+    else:
+        np.testing.assert_array_equal(out["g0_v"], z["v"])
+        np.testing.assert_array_equal(out["g0_ge"], z["ge"])
+    np.testing.assert_array_equal(out["rm0_counts"], np.bincount(z["spk_ts"], minlength=meta["n_steps"]))

@@ -1,0 +1,33 @@
+"""Jobs written by the set_device('b200') plugin from the reference's own
+scripts (tests/golden/make_jobs.py): the network they carry is the
+reference's construction, array for array (no GPU)."""
+import os
+
+import numpy as np
+import pytest
+
+from brian2_gb300.job import load_job
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CASES = ["cuba_small_f64", "delays_small_f64", "cobahh_small_f64"]
+# Brian names the first Synapses object "synapses", the second "synapses_1"
+FIXTURE_KEY = {"synapses_pre": "Ce", "synapses_1_pre": "Ci"}
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_job_carries_the_reference_network(case, golden):
+    spec, init, job = load_job(os.path.join(HERE, "golden", "jobs", case))
+    meta, z = golden(case)
+    assert int(init["g0_N"]) == meta["N"]
+    np.testing.assert_array_equal(init["g0_v"], z["v0"])
+    assert sum(job["runs"]) == meta["n_steps"] and job["dt"] == pytest.approx(1e-4)
+    assert len(spec["pathways"]) == 2
+    for pi, p in enumerate(spec["pathways"]):
+        k = FIXTURE_KEY[p["name"]]
+        np.testing.assert_array_equal(init[f"p{pi}_pre"], z[f"{k}_pre"])
+        np.testing.assert_array_equal(init[f"p{pi}_post"], z[f"{k}_post"])
+        d = z[f"{k}_delay"]
+        if d.size > 1:
+            np.testing.assert_array_equal(init[f"p{pi}_delay_steps"], (d / 1e-4 + 0.5).astype(np.int32))
+        if f"{k}_w" in z:
+            np.testing.assert_array_equal(init[f"p{pi}_w"], z[f"{k}_w"])
