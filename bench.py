@@ -291,6 +291,10 @@ def main():
     ap.add_argument("--ctas", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--chunk-steps", type=int, default=0,
+                    help="clock steps per kernel launch (default: one launch per bench step)")
+    ap.add_argument("--owner", default="auto", choices=["auto", "on", "off"],
+                    help="owner-mode delivery (auto: the library's choice)")
     args = ap.parse_args()
     rank, world, local = rank_info()
     dist = None
@@ -312,12 +316,18 @@ def main():
     N = args.neurons
     seed = 1234 + rank  # weak scaling: every rank simulates its own network
     t_build = time.perf_counter()
-    threads = args.threads or 1024
-    ctas = args.ctas or 152
+    # two 512-thread CTAs per SM: one CTA's barrier waits overlap the other's work
+    threads = args.threads or 512
+    ctas = args.ctas or 304
     net, _ = build_delays_scale(spec, N=N, K=K_IN, seed=seed, threads=threads, ctas_per_inst=ctas)
+    if args.chunk_steps:
+        net.configure(threads=threads, ctas_per_inst=ctas, queue_mode=False, chunk_steps=args.chunk_steps,
+                      use_graph=False)
+    net.set_owner({"auto": "auto", "on": True, "off": False}[args.owner])
     t_build = time.perf_counter() - t_build
     outdeg = net.outdegree
     plan = net.launch_plan()
+    net_owner = net.owner_active()
 
     def bench_step():
         net.run(STEPS_PER_BENCH_STEP)
@@ -412,7 +422,8 @@ def main():
             "config": {"workload": WORKLOAD, "neurons": N, "in_degree": K_IN, "synapses": N * K_IN,
                        "delays_ms": [0.1, 5.0], "dt_ms": 0.1, "clock_steps_per_step": STEPS_PER_BENCH_STEP,
                        "l2": "inputs larger than L2 (synapse arrays 8 GB per GPU)",
-                       "threads": threads, "ctas": ctas, "launch_plan": plan, "build_s": round(t_build, 2)},
+                       "threads": threads, "ctas": ctas, "launch_plan": plan, "build_s": round(t_build, 2),
+                       "owner_mode": net_owner},
             "sim_s_per_wall_s": sim_s / wall,
             "spikes_per_step": float(len(i)) / args.steps,
             "e2e": {"value": e2e_events / e2e_wall, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,

@@ -46,6 +46,8 @@ def candidates(total_neurons: int, n_inst: int):
     if total_neurons >= 2000:
         out.append((256, 152, False))
         out.append((1024, 152, False))
+    if total_neurons >= 100_000:  # two CTAs per SM
+        out.append((512, 304, False))
     return out
 
 

@@ -879,7 +879,12 @@ static int b200_prepare(b200_net* n) {
     int n_sm_ = 0, dev_ = 0;
     B200_CU(n, cudaGetDevice(&dev_));
     B200_CU(n, cudaDeviceGetAttribute(&n_sm_, cudaDevAttrMultiProcessorCount, dev_));
-    n->min_blocks = (n->queue_mode && n->threads == 512 && n->n_inst > n_sm_) ? 2 : 1;
+    // instances on more CTAs than SMs (two per SM, so one CTA's barrier waits overlap
+    // the other's work) use it too
+    int max_cta = 0;
+    for (int k = 0; k < n->n_inst; ++k) max_cta = std::max(max_cta, n->inst[k].n_cta);
+    n->min_blocks = (n->threads == 512 && !n->owner &&
+                     ((n->queue_mode && n->n_inst > n_sm_) || (!n->queue_mode && max_cta > n_sm_))) ? 2 : 1;
     const long other = (long)M->static_smem(n->tcode()) +
                        (long)(n->threads * 20 + 4 + 2 * M->n_groups * n->max_tiles1 * 4 + (3 * n->max_w + 1) * 4 + 64) +
                        (n->owner ? (long)n->max_w * 8 + (long)(n->max_w + 1) * 4 : 0L);
@@ -958,7 +963,8 @@ static int b200_prepare(b200_net* n) {
               off += (((long)D.p[p].ev.RB * (D.p[p].ev.W + 1) * 4 + 15) & ~15L) + (long)D.p[p].ev.RB * 16;
             }
         const long ev = std::max(8, M->owner_event_bytes);
-        long cap = off < room ? std::min<long>(16384, (room - off) / ev) : 0;
+        // staging only serves pathways with delays (the others deliver at once)
+        long cap = (tab > 0 && off < room) ? std::min<long>(16384, (room - off) / ev) : 0;
         cap &= ~3L;
         D.stage_off = (int32_t)off;
         D.stage_cap = (int32_t)cap;
