@@ -86,17 +86,40 @@ def _block(spec_block):
             "vector_device": spec_block.get("vector_device"), "refractory": spec_block.get("refractory", False)}
 
 
-class _Tables:
-    """Scalar-table layout of one group or pathway: [constants | block scalars...]."""
+def split_time_dependent(code: str, clock_ptrs):
+    """Brian's scalar blocks hold what is invariant over neurons, not over
+    steps: a declaration that reads the clock's t or timestep (or a name
+    declared from them) changes every step.  Returns (step-invariant lines,
+    time-dependent lines)."""
+    fixed, moving, names = [], [], set()
+    for line in (code or "").splitlines():
+        dep = any(p in line for p in clock_ptrs) or any(re.search(r"\b%s\b" % re.escape(n), line) for n in names)
+        if dep:
+            moving.append(line)
+            m = _DECL_RE.match(line)
+            if m:
+                names.add(m.group(2))
+        else:
+            fixed.append(line)
+    return "\n".join(fixed), "\n".join(moving)
 
-    def __init__(self, consts, blocks):
+
+class _Tables:
+    """Scalar-table layout of one group or pathway: [constants | block scalars...].
+    Block scalars that depend on the clock's time are not in the table: they
+    are evaluated on the device every step (``time_code``)."""
+
+    def __init__(self, consts, blocks, clock_ptrs=()):
         self.consts = consts
         self.entries = [(c["ctype"], c["name"]) for c in consts]
         self.block_ranges = {}
+        self.fixed_code, self.moving_code = {}, {}
         for name, blk in blocks:
             if blk is None:
                 continue
-            outs = scalar_outputs(blk["scalar"])
+            fixed, moving = split_time_dependent(blk["scalar"], clock_ptrs)
+            self.fixed_code[name], self.moving_code[name] = fixed, moving
+            outs = scalar_outputs(fixed)
             self.block_ranges[name] = (len(self.entries), outs)
             self.entries += outs
 
@@ -119,6 +142,11 @@ class _Tables:
             return ""
         off, outs = self.block_ranges[name]
         return "\n".join(self._load(ct, nm, off + k, single) for k, (ct, nm) in enumerate(outs))
+
+    def time_code(self, name):
+        """Device lines of the block's time-dependent scalars (clock reads as in
+        the block: the caller maps them to the step's registers)."""
+        return self.moving_code.get(name, "")
 
     def scalar_names(self, name):
         return [nm for _, nm in self.block_ranges.get(name, (0, []))[1]]
@@ -149,7 +177,7 @@ class _Tables:
                 continue
             off, outs = self.block_ranges[name]
             lines.append("{")
-            lines.append(_indent(blk["scalar"], 2))
+            lines.append(_indent(self.fixed_code[name], 2))
             for k, (ct, nm) in enumerate(outs):
                 lines.append(f"  _out[{off + k}] = (double){nm};")
             lines.append("}")
@@ -229,10 +257,10 @@ def render_model(spec: dict) -> str:
     for g in groups:
         blocks = [("update", _block(g.get("update"))), ("threshold", _block(g.get("threshold"))),
                   ("reset", _block(g.get("reset")))]
-        gtables.append((_Tables(consts, blocks), blocks))
+        gtables.append((_Tables(consts, blocks, (clock["t"], clock["timestep"])), blocks))
     for p in paths:
         blocks = [("on_pre", _block(p.get("on_pre")))]
-        ptables.append((_Tables(consts, blocks), blocks))
+        ptables.append((_Tables(consts, blocks, (clock["t"], clock["timestep"])), blocks))
 
     SIZE = {"double": 8, "int64_t": 8, "float": 4, "int32_t": 4, "char": 1, "int8_t": 1}
 
@@ -388,6 +416,8 @@ def render_model(spec: dict) -> str:
         g = groups[gi]
         scr_e, tc_e = owner_list(gi, tsexpr) if owner else (f"s_scr[{gi}]", f"s_tc[{gi}]")
         L = ["{",
+             f"  const double _b200_t = (double)({tsexpr}) * _b200_dt; (void)_b200_t;  // the step of the reset",
+             f"  const int64_t _b200_ts = {tsexpr}; (void)_b200_ts;",
              f"  const int32_t* const scr = {scr_e}; const int32_t* const tcnt = {tc_e};",
              f"  const int* const tst = s_tst + {gi} * max_tiles1;",
              f"  const int32_t N = I.g[{gi}].N; (void)N;",
@@ -400,6 +430,7 @@ def render_model(spec: dict) -> str:
              "      const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;",
              "      {",
              _indent(tab.device_loads("reset", f32), 8),
+             _indent(_device(tab.time_code("reset")), 8),
              extra_ptrs(g.get("reset"), 8),
              _indent(bd["reset"]["vector"], 8),
              "      }",
@@ -453,15 +484,15 @@ def render_model(spec: dict) -> str:
                 w(f"          if (threadIdx.x == 0) s_stm_n[{mi}] = ts + 1 - SM.step0;")
                 w("        }")
             # constants and block scalars are loaded once per step, not per neuron
-            upd_sc = set(tab.scalar_names("update")) if bd["update"] is not None else set()
-            thr_sc = set(tab.scalar_names("threshold")) if bd["threshold"] is not None else set()
+            upd_sc = {nm for _, nm in scalar_outputs(bd["update"]["scalar"])} if bd["update"] is not None else set()
+            thr_sc = {nm for _, nm in scalar_outputs(bd["threshold"]["scalar"])} if bd["threshold"] is not None else set()
             hoist_sc = not (upd_sc & thr_sc)
             w(_indent(tab.const_loads(f32), 8))
             if hoist_sc:
-                if bd["update"] is not None:
-                    w(_indent(tab.scalar_loads("update", f32), 8))
-                if bd["threshold"] is not None:
-                    w(_indent(tab.scalar_loads("threshold", f32), 8))
+                for blk_name in ("update", "threshold"):
+                    if bd[blk_name] is not None:
+                        w(_indent(tab.scalar_loads(blk_name, f32), 8))
+                        w(_indent(_device(tab.time_code(blk_name)), 8))
             w(f"        for (int u = s_ut[{gi}][0]; u < s_ut[{gi}][1]; ++u) {{")
             w("          const int start = tst[u], end = tst[u + 1];")
             w("          int cnt = 0;")
@@ -503,6 +534,7 @@ def render_model(spec: dict) -> str:
                 w("                {")
                 if not hoist_sc:
                     w(_indent(tab.scalar_loads("update", f32), 18))
+                    w(_indent(_device(tab.time_code("update")), 18))
                 w(extra_ptrs(g.get("update"), 18))
                 for ct, nm, ptr in upd_loads:
                     w(f"                  {ct} {nm} = _pf{pfi[ptr]}[kq];")
@@ -512,6 +544,7 @@ def render_model(spec: dict) -> str:
                 w("                {")
                 if not hoist_sc:
                     w(_indent(tab.scalar_loads("threshold", f32), 18))
+                    w(_indent(_device(tab.time_code("threshold")), 18))
                 w(extra_ptrs(g.get("threshold"), 18))
                 for ct, nm, ptr in thr_loads:
                     w(f"                  {ct} {nm} = " + (f"_pf{pfi[ptr]}[kq];" if ptr not in upd_st else f"{ptr}[_idx];"))
@@ -879,6 +912,7 @@ def render_model(spec: dict) -> str:
                 v = groups[gidx]["vars"][vidx]
                 w(f"                  {v['ctype']}* __restrict__ const {ptr} = ({v['ctype']}*)s_gv[{gidx}][{vidx}]; (void){ptr};")
             w(_indent(tab.scalar_loads("on_pre", f32), 18))
+            w(_indent(_device(tab.time_code("on_pre")), 18))
             w(_indent(blk["vector_device"] if blk.get("vector_device") else blk["vector"], 18))
             w("                }")
         w("              }")
@@ -953,6 +987,7 @@ def render_model(spec: dict) -> str:
                 L.append(f"{v['ctype']}* const {ptr} = ({v['ctype']}*)s_gv[{gidx}][{vidx}]; (void){ptr};")
             tab, blocks = ptables[pi]
             L.append(tab.scalar_loads("on_pre", f32))
+            L.append(_device(tab.time_code("on_pre")))
             L.append("(void)_b200_S; (void)_b200_Sf; (void)_b200_Si;")
             return _indent("\n".join(L), ind)
 

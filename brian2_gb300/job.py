@@ -50,8 +50,9 @@ def load_job(directory):
     return spec, init, job
 
 
-def run_job(directory, threads=None, ctas_per_inst=None, write=True):
-    """Runs a job on the GPU; returns (and writes as out.npz) its outputs."""
+def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None):
+    """Runs a job on the GPU; returns (and writes as out.npz) its outputs.
+    `owner`: delivery mode (True, False, "auto"; None keeps the default)."""
     from .runtime import Model, Network
     spec, init, job = load_job(directory)
     opts = dict(job.get("options", {}))
@@ -62,6 +63,8 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True):
     threads = threads or opts.get("threads") or (1024 if max(sizes) <= 8192 else 256)
     ctas = ctas_per_inst or opts.get("ctas_per_inst") or 1
     net.configure(threads=threads, ctas_per_inst=ctas)
+    if owner is not None:
+        net.set_owner(owner)
     for gi, g in enumerate(spec["groups"]):
         for v in g["vars"]:
             net.upload(0, gi, v["name"], init[f"g{gi}_{v['name']}"])
@@ -86,7 +89,7 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True):
         net.run(int(n))
         total_ms += net.last_run_ms()
     out = dict(device_ms=np.float64(total_ms), wall_s=np.float64(time.time() - t0), ts_end=np.int64(net.step(0)),
-               ts0=np.int64(ts0))
+               ts0=np.int64(ts0), owner=np.int64(net.owner_active()))
     for gi, g in enumerate(spec["groups"]):
         for v in g["vars"]:
             out[f"g{gi}_{v['name']}"] = net.download(0, gi, v["name"])

@@ -122,3 +122,130 @@ def cuba_delays(N=10000, K=1000, duration_ms=1000.0, seed_value=1234, ne_frac=0.
     r_mon = PopulationRateMonitor(P)
     run(duration_ms * ms)
     return dict(P=P, Ce=Ce, Ci=Ci, spikes=s_mon, rate=r_mon)
+
+
+# ---------------------------------------------------------------------------
+# Scenarios beyond the benchmark networks (parity of less common step-loop
+# features: timed refractoriness, heterogeneous weights and delays, monitors
+# on subgroups, a state monitor, a separate input group, on_pre reading a
+# presynaptic variable).  Each returns its monitors.
+# ---------------------------------------------------------------------------
+def lif_refractory(N=300, duration_ms=200.0, seed_value=11):
+    """LIF driven by a per-neuron constant input, 2 ms refractory period
+    (``v`` clamped while refractory), recurrent excitation p=0.05."""
+    from brian2 import NeuronGroup, Synapses, SpikeMonitor, PopulationRateMonitor, ms, mV, seed, run
+    seed(seed_value)
+    ns = dict(tau=10 * ms, Vt=-50 * mV, Vr=-65 * mV, El=-65 * mV, w=0.4 * mV)
+    P = NeuronGroup(N, '''dv/dt = (El - v + I)/tau : volt (unless refractory)
+                          I : volt (constant)''',
+                    threshold='v > Vt', reset='v = Vr', refractory=2 * ms, method='exact', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    P.I = '12*mV + rand() * 8*mV'
+    S = Synapses(P, P, on_pre='v += w', namespace=ns)
+    S.connect('i != j', p=0.05)
+    # monitors must be locals of the frame that calls run() (Brian collects them there)
+    s_mon = SpikeMonitor(P)
+    r_mon = PopulationRateMonitor(P)
+    run(duration_ms * ms)
+    return dict(P=P, S=S, spikes=s_mon, rate=r_mon)
+
+
+def hetero_delays(N=400, duration_ms=150.0, seed_value=21):
+    """CUBA dynamics with per-synapse random weights and delays (0-3 ms)."""
+    from brian2 import NeuronGroup, Synapses, SpikeMonitor, PopulationRateMonitor, ms, mV, seed, run
+    seed(seed_value)
+    ns = dict(taum=20 * ms, taue=5 * ms, Vt=-50 * mV, Vr=-60 * mV, El=-49 * mV)
+    P = NeuronGroup(N, '''dv/dt  = (ge-(v-El))/taum : volt
+                          dge/dt = -ge/taue : volt''',
+                    threshold='v>Vt', reset='v = Vr', method='exact', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    S = Synapses(P, P, model='w : volt', on_pre='ge += w', namespace=ns)
+    S.connect('i != j', p=0.05)
+    S.w = '(rand() - 0.3) * 1.5*mV'
+    S.delay = 'rand() * 3*ms'
+    # monitors must be locals of the frame that calls run() (Brian collects them there)
+    s_mon = SpikeMonitor(P)
+    r_mon = PopulationRateMonitor(P)
+    run(duration_ms * ms)
+    return dict(P=P, S=S, spikes=s_mon, rate=r_mon)
+
+
+def subgroup_monitors(N=500, duration_ms=200.0, seed_value=31):
+    """CUBA with monitors on parts of the group and a state monitor."""
+    from brian2 import (NeuronGroup, Synapses, SpikeMonitor, PopulationRateMonitor, StateMonitor,
+                        ms, mV, seed, run)
+    seed(seed_value)
+    ns = dict(taum=20 * ms, taue=5 * ms, taui=10 * ms, Vt=-50 * mV, Vr=-60 * mV, El=-49 * mV,
+              we=1.62 * mV, wi=-9 * mV)
+    P = NeuronGroup(N, '''dv/dt  = (ge+gi-(v-El))/taum : volt
+                          dge/dt = -ge/taue : volt
+                          dgi/dt = -gi/taui : volt''',
+                    threshold='v>Vt', reset='v = Vr', method='exact', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    Ne = int(0.8 * N)
+    Ce = Synapses(P[:Ne], P, on_pre='ge += we', namespace=ns)
+    Ci = Synapses(P[Ne:], P, on_pre='gi += wi', namespace=ns)
+    Ce.connect(p=0.02)
+    Ci.connect(p=0.02)
+    s_mon = SpikeMonitor(P[100:300])
+    r_mon = PopulationRateMonitor(P[:50])
+    st_mon = StateMonitor(P, 'v', record=[0, 10, 250, 499])
+    run(duration_ms * ms)
+    return dict(P=P, Ce=Ce, Ci=Ci, spikes=s_mon, rate=r_mon, state=st_mon)
+
+
+def input_group(N_in=200, N=300, duration_ms=200.0, seed_value=41):
+    """A separate group of driven input neurons projecting with delays onto a
+    recurrent CUBA population."""
+    from brian2 import NeuronGroup, Synapses, SpikeMonitor, PopulationRateMonitor, ms, mV, seed, run
+    seed(seed_value)
+    ns = dict(taum=20 * ms, taue=5 * ms, Vt=-50 * mV, Vr=-60 * mV, El=-60 * mV, w_in=2 * mV, w=0.5 * mV,
+              tau_in=5 * ms)
+    inp = NeuronGroup(N_in, '''dv/dt = (-60*mV - v + I)/tau_in : volt
+                               I : volt (constant)''',
+                      threshold='v > -50*mV', reset='v = -60*mV', method='exact', namespace=ns)
+    inp.v = '-60*mV + rand() * 10*mV'
+    inp.I = '8*mV + rand() * 6*mV'
+    P = NeuronGroup(N, '''dv/dt  = (ge-(v-El))/taum : volt
+                          dge/dt = -ge/taue : volt''',
+                    threshold='v>Vt', reset='v = Vr', method='exact', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    Sin = Synapses(inp, P, on_pre='ge += w_in', namespace=ns)
+    Sin.connect(p=0.1)
+    Sin.delay = '1*ms + rand() * 2*ms'
+    S = Synapses(P, P, on_pre='ge += w', namespace=ns)
+    S.connect('i != j', p=0.05)
+    s_mon = SpikeMonitor(P)
+    r_mon = PopulationRateMonitor(P)
+    run(duration_ms * ms)
+    return dict(P=P, inp=inp, Sin=Sin, S=S, spikes=s_mon, rate=r_mon)
+
+
+def presynaptic_read(N=300, duration_ms=150.0, seed_value=51):
+    """on_pre uses a variable of the presynaptic neuron (its adaptation
+    current at delivery time)."""
+    from brian2 import NeuronGroup, Synapses, SpikeMonitor, PopulationRateMonitor, ms, mV, seed, run
+    seed(seed_value)
+    ns = dict(taum=15 * ms, taue=5 * ms, taua=50 * ms, Vt=-50 * mV, Vr=-60 * mV, El=-48 * mV)
+    P = NeuronGroup(N, '''dv/dt  = (ge-(v-El))/taum : volt
+                          dge/dt = -ge/taue : volt
+                          da/dt = -a/taua : 1''',
+                    threshold='v>Vt', reset='v = Vr; a += 0.2', method='exact', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    S = Synapses(P, P, on_pre='ge_post += 1.2*mV * (1 - a_pre)', namespace=ns)
+    S.connect('i != j', p=0.05)
+    S.delay = '0.5*ms'
+    # monitors must be locals of the frame that calls run() (Brian collects them there)
+    s_mon = SpikeMonitor(P)
+    r_mon = PopulationRateMonitor(P)
+    run(duration_ms * ms)
+    return dict(P=P, S=S, spikes=s_mon, rate=r_mon)
+
+
+SCENARIOS = {
+    "lif_refractory": lif_refractory,
+    "hetero_delays": hetero_delays,
+    "subgroup_monitors": subgroup_monitors,
+    "input_group": input_group,
+    "presynaptic_read": presynaptic_read,
+}

@@ -1,0 +1,96 @@
+"""Reference fixtures and b200 jobs of the parity scenarios.
+
+For each scenario of ``oracle/brian_configs.py:SCENARIOS`` this runs the same
+Brian2 script twice, each in its own process (a standalone device builds once
+per process):
+
+* with the reference's ``cpp_standalone`` device (one thread, strict IEEE
+  flags, float64) -> ``tests/golden/scenarios/<name>.npz``: the spike monitor's
+  indices and time steps, the rate monitor's per-step counts, the state
+  monitor's trace, the final state of the monitored group;
+* with the ``b200`` plugin in deferred mode -> ``tests/golden/jobs/<name>/``:
+  the job the plugin writes from the script (spec, initial state, synapses).
+
+Run where the reference is importable::
+
+    bash oracle/make_ref_env.sh
+    PYTHONPATH=oracle/_ref/pyenv python tests/golden/make_scenarios.py [name ...]
+"""
+import json
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+BUILD = os.path.join(ROOT, "oracle", "_ref", "scenario_build")
+STRICT = ['-w', '-O3', '-std=c++17', '-ffp-contract=off', '-fno-fast-math']
+
+
+def setup(device_name, directory, **kw):
+    import numpy as np
+    from brian2 import set_device, prefs, defaultclock, ms
+    set_device(device_name, directory=directory, build_on_run=True, **kw)
+    prefs.devices.cpp_standalone.openmp_threads = 0
+    prefs.codegen.cpp.extra_compile_args_gcc = STRICT
+    prefs.core.default_float_dtype = np.float64
+    defaultclock.dt = 0.1 * ms
+
+
+def run_ref(name):
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import brian_configs as bc
+    d = os.path.join(BUILD, name + "_ref")
+    shutil.rmtree(d, ignore_errors=True)
+    setup("cpp_standalone", d)
+    r = bc.SCENARIOS[name]()
+    P, spk, rate = r["P"], r["spikes"], r["rate"]
+    out = {}
+    t = np.asarray(spk.t_[:])
+    out["spk_i"] = np.asarray(spk.i[:], dtype=np.int32)
+    out["spk_ts"] = np.round(t / 1e-4).astype(np.int32)
+    n_rate = len(rate.source)
+    out["rate_counts"] = np.round(np.asarray(rate.rate_[:]) * 1e-4 * n_rate).astype(np.int32)
+    if "state" in r:
+        out["state_v"] = np.asarray(r["state"].v_[:]).copy()        # [n_rec, steps]
+        out["state_idx"] = np.asarray(r["state"].record, dtype=np.int32)
+    for var in ("v", "ge", "gi", "a"):
+        if var in P.variables:
+            out[var] = np.asarray(getattr(P, var + "_")[:]).copy()
+    np.savez_compressed(os.path.join(HERE, "scenarios", name + ".npz"), **out)
+    with open(os.path.join(HERE, "scenarios", name + ".json"), "w") as f:
+        json.dump(dict(group=P.name, n_spikes=int(len(t)), n_steps=int(len(out["rate_counts"]))), f, indent=1)
+    print(name, "reference:", len(t), "spikes")
+
+
+def run_job(name):
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import brian2_gb300.brian_device  # noqa: F401  (registers the device)
+    from brian2 import device
+    import brian_configs as bc
+    d = os.path.join(BUILD, name + "_job")
+    shutil.rmtree(d, ignore_errors=True)
+    setup("b200", d, b200_defer=True)
+    bc.SCENARIOS[name]()
+    out = os.path.join(HERE, "jobs", name)
+    shutil.rmtree(out, ignore_errors=True)
+    shutil.copytree(device.b200_job_dir, out)
+    print(name, "job ->", out)
+
+
+if __name__ == "__main__":
+    if sys.argv[1:2] == ["--ref"]:
+        run_ref(sys.argv[2])
+        sys.exit(0)
+    if sys.argv[1:2] == ["--job"]:
+        run_job(sys.argv[2])
+        sys.exit(0)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import brian_configs as bc
+    os.makedirs(os.path.join(HERE, "scenarios"), exist_ok=True)
+    for n in sys.argv[1:] or list(bc.SCENARIOS):
+        for phase in ("--ref", "--job"):
+            subprocess.run([sys.executable, os.path.abspath(__file__), phase, n], check=True)

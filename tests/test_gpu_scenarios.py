@@ -1,0 +1,48 @@
+"""Parity scenarios through the drop-in path (GPU only): for each script of
+oracle/brian_configs.py:SCENARIOS, the job the set_device('b200') plugin
+wrote runs on the GPU and is compared with the reference's own run of the
+same script (tests/golden/make_scenarios.py).
+
+Bit-exact where every per-target increment of a pathway is equal (timed
+refractoriness, subgroup monitors and a state monitor, a separate input
+group); where increments differ (random weights, a presynaptic factor) the
+order of the float64 sums into a target differs from the reference's queue
+order, so the raster must match and the state agree to 1e-12 relative."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from brian2_gb300.job import load_job, run_job
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+EXACT = {"lif_refractory": True, "hetero_delays": False, "subgroup_monitors": True, "input_group": True,
+         "presynaptic_read": False}
+
+
+@pytest.mark.parametrize("name", sorted(EXACT))
+@pytest.mark.parametrize("ctas,owner", [(1, "auto"), (4, True), (4, False), (20, "auto")])
+def test_scenario_matches_reference(name, ctas, owner):
+    jobdir = os.path.join(HERE, "golden", "jobs", name)
+    spec, _, job = load_job(jobdir)
+    with np.load(os.path.join(HERE, "golden", "scenarios", name + ".npz")) as z:
+        ref = {k: z[k] for k in z.files}
+    with open(os.path.join(HERE, "golden", "scenarios", name + ".json")) as f:
+        meta = json.load(f)
+    out = run_job(jobdir, threads=128, ctas_per_inst=ctas, write=False, owner=owner)
+    assert len(out["sm0_i"]) == meta["n_spikes"]
+    np.testing.assert_array_equal(out["sm0_i"], ref["spk_i"])
+    np.testing.assert_array_equal(out["sm0_ts"], ref["spk_ts"])
+    np.testing.assert_array_equal(out["rm0_counts"], ref["rate_counts"])
+    gi = [g["name"] for g in spec["groups"]].index(meta["group"])
+    for var in ("v", "ge", "gi", "a"):
+        if var in ref:
+            if EXACT[name]:
+                np.testing.assert_array_equal(out[f"g{gi}_{var}"], ref[var], err_msg=var)
+            else:
+                np.testing.assert_allclose(out[f"g{gi}_{var}"], ref[var], rtol=1e-12, atol=1e-18, err_msg=var)
+    if "state_v" in ref:
+        tr = out["stm0_trace"][:, 0, :].T            # [n_rec, steps]
+        np.testing.assert_array_equal(tr, ref["state_v"])

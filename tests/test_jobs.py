@@ -31,3 +31,25 @@ def test_job_carries_the_reference_network(case, golden):
             np.testing.assert_array_equal(init[f"p{pi}_delay_steps"], (d / 1e-4 + 0.5).astype(np.int32))
         if f"{k}_w" in z:
             np.testing.assert_array_equal(init[f"p{pi}_w"], z[f"{k}_w"])
+
+
+SCENARIOS = ["lif_refractory", "hetero_delays", "subgroup_monitors", "input_group", "presynaptic_read"]
+
+
+@pytest.mark.parametrize("name", SCENARIOS)
+def test_scenario_jobs_describe_their_features(name):
+    """The plugin's spec of each scenario carries the feature it exercises."""
+    spec, init, job = load_job(os.path.join(HERE, "golden", "jobs", name))
+    names = {v["name"] for g in spec["groups"] for v in g["vars"]}
+    if name == "lif_refractory":
+        assert {"not_refractory", "lastspike"} <= names
+    if name == "hetero_delays":
+        assert "p0_delay_steps" in init and init["p0_delay_steps"].max() > 0 and "p0_w" in init
+    if name == "subgroup_monitors":
+        assert tuple(init["sm0_range"]) == (100, 300) and tuple(init["rm0_range"]) == (0, 50)
+        assert list(init["stm0_idx"]) == [0, 10, 250, 499]
+    if name == "input_group":
+        assert len(spec["groups"]) == 2 and {p["src"] for p in spec["pathways"]} == {0, 1}
+    if name == "presynaptic_read":
+        assert any("_presynaptic_idx" in (p["on_pre"].get("vector_device") or p["on_pre"]["vector"])
+                   for p in spec["pathways"])
