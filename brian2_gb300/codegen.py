@@ -414,7 +414,7 @@ def render_model(spec: dict) -> str:
         if bd["reset"] is None:
             return ""
         g = groups[gi]
-        scr_e, tc_e = owner_list(gi, tsexpr) if owner else (f"s_scr[{gi}]", f"s_tc[{gi}]")
+        scr_e, tc_e = owner_list(gi, tsexpr) if owner else (f"s_oscr[{gi}]", f"s_otc[{gi}]")
         L = ["{",
              f"  const double _b200_t = (double)({tsexpr}) * _b200_dt; (void)_b200_t;  // the step of the reset",
              f"  const int64_t _b200_ts = {tsexpr}; (void)_b200_ts;",
@@ -461,6 +461,7 @@ def render_model(spec: dict) -> str:
                 w(f"        int32_t* const scr = {scr_e}; int32_t* const tcnt = {tc_e};")
             else:
                 w(f"        int32_t* const scr = s_scr[{gi}]; int32_t* const tcnt = s_tc[{gi}];")
+                w(f"        int32_t* const oscr = s_oscr[{gi}]; int32_t* const otc = s_otc[{gi}];")
             w(f"        const int* const tst = s_tst + {gi} * max_tiles1;")
             for mi, m in enumerate(statemons):
                 if m["group"] != gi:
@@ -575,12 +576,19 @@ def render_model(spec: dict) -> str:
             w("            for (int k = 0; k < E; ++k) {")
             w("              const unsigned m = __ballot_sync(0xffffffffu, (flags >> k) & 1u);")
             w("              if ((flags >> k) & 1u)")
-            w("                scr[start + cnt + s_cnt[k * NW + wid] + __popc(m & b200_lanemask_lt())] = pb + k * (int)blockDim.x + threadIdx.x;")
+            if owner:
+                w("                scr[start + cnt + s_cnt[k * NW + wid] + __popc(m & b200_lanemask_lt())] = pb + k * (int)blockDim.x + threadIdx.x;")
+            else:
+                w("                {")
+                w("                  const int _p = start + cnt + s_cnt[k * NW + wid] + __popc(m & b200_lanemask_lt());")
+                w("                  scr[_p] = pb + k * (int)blockDim.x + threadIdx.x;")
+                w("                  oscr[_p] = pb + k * (int)blockDim.x + threadIdx.x;  // this CTA's copy")
+                w("                }")
             w("            }")
             w("            cnt += tot;")
             w("            __syncthreads();")
             w("          }")
-            w("          if (threadIdx.x == 0) tcnt[u] = cnt;")
+            w("          if (threadIdx.x == 0) tcnt[u] = cnt;" if owner else "          if (threadIdx.x == 0) { tcnt[u] = cnt; otc[u] = cnt; }")
             w("        }")
             w("      }")
 
@@ -624,6 +632,8 @@ def render_model(spec: dict) -> str:
     w("  __shared__ void* s_gv[B200_NG][B200_MAXV];")
     w("  __shared__ int32_t* s_scr[B200_NG];")
     w("  __shared__ int32_t* s_tc[B200_NG];")
+    w("  __shared__ int32_t* s_oscr[B200_NG];  // this CTA's own spike lists / tile counts (shared copy")
+    w("  __shared__ int32_t* s_otc[B200_NG];   //  when there is room, else the global lists)")
     w("  __shared__ int s_ut[B200_NG][2];")
     for gi in range(NG):
         n_ = max(gtables[gi][0].size, 1)
@@ -673,6 +683,11 @@ def render_model(spec: dict) -> str:
         w("        }")
         w("      }")
         w(f"      s_ut[{gi}][0] = I.g[{gi}].cta_tile[rank]; s_ut[{gi}][1] = I.g[{gi}].cta_tile[rank + 1];")
+        w(f"      s_oscr[{gi}] = s_scr[{gi}]; s_otc[{gi}] = s_tc[{gi}];")
+        w(f"      if (!cache && I.g[{gi}].own_off >= 0) {{  // offset so that global positions address them")
+        w(f"        s_oscr[{gi}] = (int32_t*)(s_state + I.g[{gi}].own_off) - I.g[{gi}].tile_start[s_ut[{gi}][0]];")
+        w(f"        s_otc[{gi}] = (int32_t*)(s_state + I.g[{gi}].own_off + (((size_t)I.g[{gi}].own_cap * 4 + 15) & ~(size_t)15)) - s_ut[{gi}][0];")
+        w("      }")
     w("    }")
     w("    __syncthreads();")
     for gi, g in enumerate(groups):
@@ -731,7 +746,8 @@ def render_model(spec: dict) -> str:
         w(f"        b200_group_d& GD = I.g[{gi}];")
         w(f"        int* const pref = s_pref_all + {gi} * max_tiles1;")
         w(f"        const int* const tst = s_tst + {gi} * max_tiles1;")
-        w(f"        const int32_t* const scr = s_scr[{gi}]; const int32_t* const tcnt = s_tc[{gi}];")
+        w(f"        const int32_t* const tcnt = s_tc[{gi}];")
+        w(f"        const int32_t* const oscr = s_oscr[{gi}];  // this CTA's own lists")
         w("        const int nt = GD.n_tiles;")
         w("        int carry = 0;")
         w("        for (int c0 = 0; c0 < nt; c0 += blockDim.x) {")
@@ -750,7 +766,7 @@ def render_model(spec: dict) -> str:
         w("          int32_t* const ring = GD.ring + (int64_t)slot * GD.N;")
         w("          for (int u = u0; u < u1; ++u) {")
         w("            const int cnt = pref[u + 1] - pref[u], base = tst[u];")
-        w("            for (int j = threadIdx.x; j < cnt; j += blockDim.x) ring[pref[u] + j] = scr[base + j];")
+        w("            for (int j = threadIdx.x; j < cnt; j += blockDim.x) ring[pref[u] + j] = oscr[base + j];")
         w("          }")
         w("          if (rank == 0) {")
         w("            for (int u = threadIdx.x; u <= nt; u += blockDim.x) GD.ring_prefix[(int64_t)slot * (nt + 1) + u] = pref[u];")
@@ -767,7 +783,7 @@ def render_model(spec: dict) -> str:
             w("          for (int u = a; u < b; ++u) {")
             w("            const int cnt = pref[u + 1] - pref[u], base = tst[u];")
             w("            for (int j = threadIdx.x; j < cnt; j += blockDim.x) {")
-            w("              const int idx = scr[base + j];")
+            w("              const int idx = oscr[base + j];")
             w("              const long long pos = mbase + pref[u] + j;")
             w("              SM.i[pos] = idx - SM.lo;")
             w("              SM.ts[pos] = (int32_t)ts;")

@@ -35,7 +35,9 @@ struct b200_group_d {
   int32_t N;              // neurons of this group in this instance
   int32_t R;              // spike-ring slots (max outgoing delay + 1)
   int32_t n_tiles;        // tiles of this group (each owned by one CTA)
-  int32_t _pad;
+  int32_t own_off;        // >= 0: byte offset in shared memory of this CTA's copy of its own
+                          // spike lists (own_cap entries) and tile counts (own_tiles entries)
+  int32_t own_cap, own_tiles;
   const int32_t* tile_start;     // [n_tiles+1] first neuron of each tile
   const int32_t* cta_tile;       // [n_cta+1]  first tile of each CTA of the instance
   int32_t* scratch;       // [N]       this step's spikes at tile_start[u]+j

@@ -765,6 +765,7 @@ static int b200_prepare(b200_net* n) {
       B200_CU(n, cudaStreamSynchronize(n->stream));
       b200_group_d& GD = D.g[g];
       GD.N = G.N; GD.R = R; GD.n_tiles = n_tiles;
+      GD.own_off = -1;  // no shared copy of the CTA's own spike lists unless placed below
       GD.tile_start = (const int32_t*)G.d_tile_start.p;
       GD.cta_tile = (const int32_t*)G.d_cta_tile.p;
       GD.scratch = (int32_t*)G.scratch.p;
@@ -939,6 +940,33 @@ static int b200_prepare(b200_net* n) {
       n->h_insts[k].cache_bytes = (int32_t)bytes;
       n->h_insts[k].cache_lists = lists ? 1 : 0;
       n->state_bytes = std::max<long>(n->state_bytes, bytes);
+    }
+    if (!n->owner && !n->queue_mode) {
+      // classic multi-CTA instances: a shared-memory copy of each CTA's own spike
+      // lists and tile counts (the reset and the ring copy read them there)
+      for (int k = 0; k < n->n_inst; ++k) {
+        b200_inst_d& D = n->h_insts[k];
+        if (D.cache_bytes > 0) continue;
+        const b200_inst_h& I = n->inst[k];
+        long off = 0;
+        std::vector<long> offs(M->n_groups);
+        for (int g = 0; g < M->n_groups; ++g) {
+          const b200_group_h& G = I.g[g];
+          int cap = 0, tiles = 0;
+          for (int c = 0; c < I.n_cta; ++c) {
+            cap = std::max(cap, G.tile_start[G.cta_tile[c + 1]] - G.tile_start[G.cta_tile[c]]);
+            tiles = std::max(tiles, G.cta_tile[c + 1] - G.cta_tile[c]);
+          }
+          D.g[g].own_cap = std::max(cap, 1);
+          D.g[g].own_tiles = std::max(tiles, 1);
+          offs[g] = off;
+          off += (((long)D.g[g].own_cap * 4 + 15) & ~15L) + (((long)D.g[g].own_tiles * 4 + 15) & ~15L);
+        }
+        if (off <= budget) {
+          for (int g = 0; g < M->n_groups; ++g) D.g[g].own_off = (int32_t)offs[g];
+          n->state_bytes = std::max<long>(n->state_bytes, off);
+        }
+      }
     }
     if (n->owner) {
       // after the state cache: the batch tables of the event FIFOs, then a
