@@ -342,8 +342,9 @@ def main():
     N = args.neurons
     seed = 1234 + rank  # weak scaling: every rank simulates its own network
     t_build = time.perf_counter()
-    # two 512-thread CTAs per SM: one CTA's barrier waits overlap the other's work
-    threads = args.threads or 512
+    # two 256-thread CTAs per SM (128 registers each): one CTA's barrier waits
+    # overlap the other's work, and each thread keeps four events' loads in flight
+    threads = args.threads or 256
     ctas = args.ctas or 304
     net, _ = build_delays_scale(spec, N=N, K=K_IN, seed=seed, threads=threads, ctas_per_inst=ctas)
     if args.chunk_steps:

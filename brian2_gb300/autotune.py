@@ -48,6 +48,7 @@ def candidates(total_neurons: int, n_inst: int):
         out.append((1024, 152, False))
     if total_neurons >= 100_000:  # two CTAs per SM
         out.append((512, 304, False))
+        out.append((256, 304, False))
     return out
 
 

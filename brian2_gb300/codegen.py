@@ -903,37 +903,116 @@ def render_model(spec: dict) -> str:
         w("          s_item_off[threadIdx.x] = off;")
         w("          __syncthreads();")
         w("          const int nitems = (i1 - cb) < (int)blockDim.x ? (i1 - cb) : (int)blockDim.x;")
-        w("          for (int e0 = threadIdx.x; e0 < E; e0 += 4 * (int)blockDim.x) {")
-        w("#pragma unroll")
-        w("            for (int qq = 0; qq < 4; ++qq) {")
-        w("              const int e = e0 + qq * (int)blockDim.x;")
-        w("              if (e < E) {")
-        w("                const int j = b200_upper_bound(s_item_off, nitems, e) - 1;")
-        w("                const int64_t _idx = s_item_seg[j] + (e - s_item_off[j]);")
-        w("                const int32_t _b200_pre = s_item_src[j]; (void)_b200_pre;")
-        w("                const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
-        w("                const int q = s_item_q[j]; (void)q;")
-        for q, pi in enumerate(pis):
-            p = paths[pi]
-            tab, blocks = ptables[pi]
-            blk = dict(blocks)["on_pre"]
-            w(("                if" if q == 0 else "                else if") + f" (q == {q}) {{  // {p['name']}")
-            w(f"                  const b200_pathway_d& PQ = I.p[{pi}]; (void)PQ;")
-            w(f"                  const double* const _b200_S = s_Sp{pi}; const float* const _b200_Sf = s_Sp{pi}f; const long long* const _b200_Si = s_Sp{pi}i;")
-            for k, v in enumerate(p.get("vars", [])):
-                w(f"                  {v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)PQ.var[{k}]; (void){v['ptr']};")
-            w(f"                  const int32_t* __restrict__ const {p['post_ptr']} = PQ.post; (void){p['post_ptr']};")
-            w(f"                  const int32_t* __restrict__ const {p['pre_ptr']} = PQ.pre; (void){p['pre_ptr']};")
-            for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
-                v = groups[gidx]["vars"][vidx]
-                w(f"                  {v['ctype']}* __restrict__ const {ptr} = ({v['ctype']}*)s_gv[{gidx}][{vidx}]; (void){ptr};")
-            w(_indent(tab.scalar_loads("on_pre", f32), 18))
-            w(_indent(_device(tab.time_code("on_pre")), 18))
-            w(_indent(blk["vector_device"] if blk.get("vector_device") else blk["vector"], 18))
-            w("                }")
-        w("              }")
-        w("            }")
+        # events: when every pathway of the group starts its on_pre with loads of
+        # the same types, a thread first issues the loads of its four events,
+        # then applies them (the loads no longer wait behind the atomics)
+        sigs = []
+        for pi in pis:
+            lds, _ = split_loads(dict(ptables[pi][1])["on_pre"]["vector_device"] or
+                                 dict(ptables[pi][1])["on_pre"]["vector"])
+            sigs.append([ct for ct, _, _ in lds])
+        two_phase = all(sg_ == sigs[0] for sg_ in sigs) and len(sigs[0]) > 0
+        if two_phase:
+            # (the variants capped at 64 registers keep the one-phase loop: the
+            # loads of four events in flight would spill there)
+            w("          if constexpr (MAXT * MINB < 1024) {")
+            NL = len(sigs[0])
+
+            def load_expr(pi, ptr, ct):
+                p = paths[pi]
+                if ptr == p["post_ptr"]:
+                    return f"I.p[{pi}].post[_idx]"
+                if ptr == p["pre_ptr"]:
+                    return f"I.p[{pi}].pre[_idx]"
+                k = next(k for k, v in enumerate(p.get("vars", [])) if v["ptr"] == ptr)
+                return f"(({ct}*)I.p[{pi}].var[{k}])[_idx]"
+
+            w("          for (int e0 = threadIdx.x; e0 < E; e0 += 4 * (int)blockDim.x) {")
+            w("            int _q4[4]; int32_t _pre4[4]; int64_t _ix4[4];")
+            for li, ct in enumerate(sigs[0]):
+                w(f"            {ct} _ld{li}[4];")
+            w("#pragma unroll")
+            w("            for (int qq = 0; qq < 4; ++qq) {")
+            w("              const int e = e0 + qq * (int)blockDim.x;")
+            w("              _q4[qq] = -1;")
+            w("              if (e < E) {")
+            w("                const int j = b200_upper_bound(s_item_off, nitems, e) - 1;")
+            w("                const int64_t _idx = s_item_seg[j] + (e - s_item_off[j]);")
+            w("                const int q = s_item_q[j];")
+            w("                _q4[qq] = q; _pre4[qq] = s_item_src[j]; _ix4[qq] = _idx;")
+            for q, pi in enumerate(pis):
+                lds, _ = split_loads(dict(ptables[pi][1])["on_pre"]["vector_device"] or
+                                     dict(ptables[pi][1])["on_pre"]["vector"])
+                w(("                if" if q == 0 else "                else if") + f" (q == {q}) {{")
+                for li, (ct, nm, ptr) in enumerate(lds):
+                    w(f"                  _ld{li}[qq] = {load_expr(pi, ptr, ct)};")
+                w("                }")
+            w("              }")
+            w("            }")
+            w("#pragma unroll")
+            w("            for (int qq = 0; qq < 4; ++qq) {")
+            w("              if (_q4[qq] >= 0) {")
+            w("                const int q = _q4[qq];")
+            w("                const int64_t _idx = _ix4[qq]; (void)_idx;")
+            w("                const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+            w("                const int32_t _b200_pre = _pre4[qq]; (void)_b200_pre;")
+            for q, pi in enumerate(pis):
+                p = paths[pi]
+                tab, blocks = ptables[pi]
+                blk = dict(blocks)["on_pre"]
+                lds, rest = split_loads(blk["vector_device"] or blk["vector"])
+                w(("                if" if q == 0 else "                else if") + f" (q == {q}) {{  // {p['name']}")
+                w(f"                  const b200_pathway_d& PQ = I.p[{pi}]; (void)PQ;")
+                w(f"                  const double* const _b200_S = s_Sp{pi}; const float* const _b200_Sf = s_Sp{pi}f; const long long* const _b200_Si = s_Sp{pi}i;")
+                for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
+                    v = groups[gidx]["vars"][vidx]
+                    w(f"                  {v['ctype']}* __restrict__ const {ptr} = ({v['ctype']}*)s_gv[{gidx}][{vidx}]; (void){ptr};")
+                for k, v in enumerate(p.get("vars", [])):
+                    w(f"                  {v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)PQ.var[{k}]; (void){v['ptr']};")
+                w(_indent(tab.scalar_loads("on_pre", f32), 18))
+                w(_indent(_device(tab.time_code("on_pre")), 18))
+                for li, (ct, nm, ptr) in enumerate(lds):
+                    w(f"                  {ct} {nm} = _ld{li}[qq];")
+                w(_indent(rest, 18))
+                w("                }")
+            w("              }")
+            w("            }")
+            w("          }")
+            w("          } else {")
+        if True:  # the one-phase loop (always emitted; the only one without a common load signature)
+            w("          for (int e0 = threadIdx.x; e0 < E; e0 += 4 * (int)blockDim.x) {")
+            w("#pragma unroll")
+            w("            for (int qq = 0; qq < 4; ++qq) {")
+            w("              const int e = e0 + qq * (int)blockDim.x;")
+            w("              if (e < E) {")
+            w("                const int j = b200_upper_bound(s_item_off, nitems, e) - 1;")
+            w("                const int64_t _idx = s_item_seg[j] + (e - s_item_off[j]);")
+            w("                const int32_t _b200_pre = s_item_src[j]; (void)_b200_pre;")
+            w("                const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+            w("                const int q = s_item_q[j]; (void)q;")
+            for q, pi in enumerate(pis):
+                p = paths[pi]
+                tab, blocks = ptables[pi]
+                blk = dict(blocks)["on_pre"]
+                w(("                if" if q == 0 else "                else if") + f" (q == {q}) {{  // {p['name']}")
+                w(f"                  const b200_pathway_d& PQ = I.p[{pi}]; (void)PQ;")
+                w(f"                  const double* const _b200_S = s_Sp{pi}; const float* const _b200_Sf = s_Sp{pi}f; const long long* const _b200_Si = s_Sp{pi}i;")
+                for k, v in enumerate(p.get("vars", [])):
+                    w(f"                  {v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)PQ.var[{k}]; (void){v['ptr']};")
+                w(f"                  const int32_t* __restrict__ const {p['post_ptr']} = PQ.post; (void){p['post_ptr']};")
+                w(f"                  const int32_t* __restrict__ const {p['pre_ptr']} = PQ.pre; (void){p['pre_ptr']};")
+                for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
+                    v = groups[gidx]["vars"][vidx]
+                    w(f"                  {v['ctype']}* __restrict__ const {ptr} = ({v['ctype']}*)s_gv[{gidx}][{vidx}]; (void){ptr};")
+                w(_indent(tab.scalar_loads("on_pre", f32), 18))
+                w(_indent(_device(tab.time_code("on_pre")), 18))
+                w(_indent(blk["vector_device"] if blk.get("vector_device") else blk["vector"], 18))
+                w("                }")
+            w("              }")
+            w("            }")
         w("          }")
+        if two_phase:
+            w("          }  // if constexpr")
         w("          __syncthreads();")
         w("        }")
         w("      }")
