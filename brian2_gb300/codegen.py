@@ -1755,7 +1755,7 @@ def render_model(spec: dict) -> str:
         w("    if (threads <= 512) return (const void*)b200_owner_kernel<512, 1>;")
         w("    return (const void*)b200_owner_kernel<1024, 1>;")
         w("  }")
-    w("  if (threads <= 256) return (const void*)b200_step_kernel<256, 1>;")
+    w("  if (threads <= 256) return minb >= 2 ? (const void*)b200_step_kernel<256, 2> : (const void*)b200_step_kernel<256, 1>;")
     w("  if (threads <= 512) return minb >= 2 ? (const void*)b200_step_kernel<512, 2> : (const void*)b200_step_kernel<512, 1>;")
     w("  return (const void*)b200_step_kernel<1024, 1>;")
     w("}")

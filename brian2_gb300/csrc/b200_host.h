@@ -884,8 +884,9 @@ static int b200_prepare(b200_net* n) {
     // the other's work) use it too
     int max_cta = 0;
     for (int k = 0; k < n->n_inst; ++k) max_cta = std::max(max_cta, n->inst[k].n_cta);
-    n->min_blocks = (n->threads == 512 && !n->owner &&
-                     ((n->queue_mode && n->n_inst > n_sm_) || (!n->queue_mode && max_cta > n_sm_))) ? 2 : 1;
+    n->min_blocks = (!n->owner && ((n->threads == 512 && n->queue_mode && n->n_inst > n_sm_) ||
+                                   ((n->threads == 512 || n->threads == 256) && !n->queue_mode && max_cta > n_sm_)))
+                        ? 2 : 1;
     const long other = (long)M->static_smem(n->tcode()) +
                        (long)(n->threads * 20 + 4 + 2 * M->n_groups * n->max_tiles1 * 4 + (3 * n->max_w + 1) * 4 + 64) +
                        (n->owner ? (long)n->max_w * 8 + (long)(n->max_w + 1) * 4 : 0L);
