@@ -45,6 +45,7 @@ from brian2.devices.cpp_standalone.device import CPPStandaloneDevice
 from brian2.devices.device import all_devices
 from brian2.groups.neurongroup import NeuronGroup
 from brian2.groups.subgroup import Subgroup
+from brian2.input.spikegeneratorgroup import SpikeGeneratorGroup
 from brian2.monitors.ratemonitor import PopulationRateMonitor
 from brian2.monitors.spikemonitor import SpikeMonitor
 from brian2.monitors.statemonitor import StateMonitor
@@ -55,7 +56,7 @@ from brian2.utils.stringtools import get_identifiers, stripped_deindented_lines
 logger = get_logger(__name__)
 
 STEP_TEMPLATES = {"stateupdate", "threshold", "reset", "synapses", "synapses_push_spikes",
-                  "spikemonitor", "ratemonitor", "statemonitor"}
+                  "spikemonitor", "ratemonitor", "statemonitor", "spikegenerator"}
 
 
 class B200CodeGenerator(CPPCodeGenerator):
@@ -235,19 +236,21 @@ class B200Device(CPPStandaloneDevice):
 
         def group_of(g):
             base = g.source if isinstance(g, Subgroup) else g
-            if hasattr(base, "__weakref__") is False or not isinstance(base, NeuronGroup):
-                base = getattr(base, "__repr__", None) and base
-            if not isinstance(base, NeuronGroup):
+            if not isinstance(base, (NeuronGroup, SpikeGeneratorGroup)):
                 raise NotImplementedError(f"b200: unsupported source/target {g!r}")
             if base.name not in group_index:
                 gv = []
                 for vname, var in sorted(base.variables.items()):
+                    if isinstance(base, SpikeGeneratorGroup) and vname != "i":
+                        continue  # the spike lists are a generator's own arrays, not per-neuron state
                     if (isinstance(var, ArrayVariable) and not var.scalar and var.owner is not None
                             and var.owner.name == base.name and vname != "_spikespace"
                             and var.size == len(base) and getattr(var, "ndim", 1) == 1):
                         gv.append(dict(name=vname, ctype=c_data_type(var.dtype), ptr=gen_name(var)))
                 group_index[base.name] = len(groups)
                 groups.append(dict(name=base.name, vars=gv, _obj=base))
+                if isinstance(base, SpikeGeneratorGroup):
+                    groups[-1]["generator"] = True
             lo = g.start if isinstance(g, Subgroup) else 0
             hi = g.stop if isinstance(g, Subgroup) else len(base)
             return group_index[base.name], (int(lo), int(hi))
@@ -346,6 +349,8 @@ class B200Device(CPPStandaloneDevice):
                                          _obj=pw, _src_range=srange, _tgt_range=trange))
                 elif t == "synapses_push_spikes":
                     pass
+                elif t == "spikegenerator":
+                    group_of(obj)
                 elif t == "spikemonitor":
                     if not isinstance(obj, SpikeMonitor) or set(obj.record_variables) - {"i", "t"}:
                         raise NotImplementedError("b200: spike monitors record i and t only")
@@ -438,6 +443,12 @@ class B200Device(CPPStandaloneDevice):
             init[f"g{gi}_N"] = np.int64(len(g["_obj"]))
             for v in g["vars"]:
                 init[f"g{gi}_{v['name']}"] = self._load(g["_obj"].variables[v["name"]])
+            if g.get("generator"):
+                gv = g["_obj"].variables
+                init[f"g{gi}_gen_bins"] = self._load(gv["_timebins"]).astype(np.int32)
+                init[f"g{gi}_gen_index"] = self._load(gv["neuron_index"]).astype(np.int32)
+                init[f"g{gi}_gen_period"] = np.int64(self._load(gv["_period_bins"])[0])
+                init[f"g{gi}_gen_last"] = np.int64(self._load(gv["_lastindex"])[0])
         for pi, p in enumerate(spec0["pathways"]):
             syn = p["_obj"].synapses
             init[f"p{pi}_pre"] = (self._load(syn.variables["_synaptic_pre"]).astype(np.int64)
@@ -484,6 +495,8 @@ class B200Device(CPPStandaloneDevice):
         for gi, g in enumerate(spec0["groups"]):
             for v in g["vars"]:
                 self._store(g["_obj"].variables[v["name"]], out[f"g{gi}_{v['name']}"])
+            if g.get("generator"):
+                self._store(g["_obj"].variables["_lastindex"], np.array([int(out[f"g{gi}_gen_last"])]))
         for pi, p in enumerate(spec0["pathways"]):
             syn = p["_obj"].synapses
             for v in p["vars"]:

@@ -343,7 +343,8 @@ def render_model(spec: dict) -> str:
         w(f"static const char* const b200_p{pi}_vars[] = {{" + ", ".join(f'"{v["name"]}"' for v in pv) + ('' if pv else '""') + "};")
         w(f"static const int b200_p{pi}_kinds[] = {{" + ", ".join(str(CTYPE_KIND[v["ctype"]]) for v in pv) + ('' if pv else '0') + "};")
     w("static const b200_group_info b200_groups[] = {" + ", ".join(
-        f'{{"{g["name"]}", {len(g["vars"])}, b200_g{gi}_vars, b200_g{gi}_kinds, {gtables[gi][0].size}, b200_g{gi}_used}}'
+        f'{{"{g["name"]}", {len(g["vars"])}, b200_g{gi}_vars, b200_g{gi}_kinds, {gtables[gi][0].size}, b200_g{gi}_used, '
+        f'{1 if g.get("generator") else 0}}}'
         for gi, g in enumerate(groups)) + "};")
     for pi, p in enumerate(paths):
         pay = PAYLOAD[pi] if OWNER else []
@@ -439,6 +440,55 @@ def render_model(spec: dict) -> str:
              "}"]
         return _indent("\n".join(L), indent)
 
+    def emit_generator(gi, owner):
+        """A spike generator group's step (templates/spikegenerator.cpp:5-31):
+        the entries from the cursor whose time bin is <= the step's (modulo
+        the period), compacted per tile in array order (the entries of a bin
+        are sorted by neuron index, input/spikegeneratorgroup.py:356)."""
+        if owner:
+            scr_e, tc_e = owner_list(gi, "ts")
+        else:
+            scr_e, tc_e = f"s_scr[{gi}]", f"s_tc[{gi}]"
+        w(f"      {{  // ---- group {gi} '{groups[gi]['name']}': spike generator")
+        w(f"        const b200_group_d& GG = I.g[{gi}];")
+        w(f"        int32_t* const scr = {scr_e}; int32_t* const tcnt = {tc_e};")
+        if not owner:
+            w(f"        int32_t* const oscr = s_oscr[{gi}]; int32_t* const otc = s_otc[{gi}];")
+        w(f"        const int* const tst = s_tst + {gi} * max_tiles1;")
+        w("        if (threadIdx.x == 0) {")
+        w(f"          long long tb = ts; int lo = s_glast[{gi}];")
+        w("          if (GG.gen_period > 0) {")
+        w("            tb %= GG.gen_period;")
+        w("            if (lo > 0 && GG.gen_bins[lo - 1] >= tb) lo = 0;")
+        w("          }")
+        w("          int a = lo, b = (int)GG.gen_n;  // first entry after the step's bin")
+        w("          while (a < b) { const int m = (a + b) >> 1; if (GG.gen_bins[m] <= tb) a = m + 1; else b = m; }")
+        w(f"          s_gen_lo = lo; s_gen_hi = a; s_glast[{gi}] = a;")
+        w("        }")
+        w("        __syncthreads();")
+        w("        const int glo = s_gen_lo, ghi = s_gen_hi;")
+        w(f"        for (int u = s_ut[{gi}][0]; u < s_ut[{gi}][1]; ++u) {{")
+        w("          const int t0 = tst[u], t1 = tst[u + 1];")
+        w("          int cnt = 0;")
+        w("          for (int j0 = glo; j0 < ghi; j0 += blockDim.x) {")
+        w("            const int j = j0 + threadIdx.x;")
+        w("            const int idx = j < ghi ? GG.gen_index[j] : -1;")
+        w("            const bool f = idx >= t0 && idx < t1;")
+        w("            int tot;")
+        w("            const int rk = b200_block_compact(f, s_wsum, &tot);")
+        w("            if (f && t0 + cnt + rk < t1) {")
+        w("              scr[t0 + cnt + rk] = idx;")
+        if not owner:
+            w("              oscr[t0 + cnt + rk] = idx;")
+        w("            }")
+        w("            cnt += tot;")
+        w("          }")
+        w("          if (cnt > t1 - t0) cnt = t1 - t0;")
+        w("          if (threadIdx.x == 0) { tcnt[u] = cnt;" + ("" if owner else " otc[u] = cnt;") + " }")
+        w("        }")
+        w("        __syncthreads();")
+        w("      }")
+
     def emit_phase_a(owner):
         """Reset of the previous step, state monitors, update + threshold with
         ordered compaction of this CTA's tiles."""
@@ -446,6 +496,9 @@ def render_model(spec: dict) -> str:
         for gi, g in enumerate(groups):
             tab, blocks = gtables[gi]
             bd = dict(blocks)
+            if g.get("generator"):
+                emit_generator(gi, owner)
+                continue
             w(f"      // ---- group {gi} '{g['name']}': phase A (reset of step ts-1, monitors, update + threshold)")
             if bd["reset"] is not None:
                 w("      if (ts > ts0) {")
@@ -635,6 +688,8 @@ def render_model(spec: dict) -> str:
     w("  __shared__ int32_t* s_oscr[B200_NG];  // this CTA's own spike lists / tile counts (shared copy")
     w("  __shared__ int32_t* s_otc[B200_NG];   //  when there is room, else the global lists)")
     w("  __shared__ int s_ut[B200_NG][2];")
+    w("  __shared__ int s_glast[B200_NG], s_gen_lo, s_gen_hi;  // spike generator cursors")
+    w("  (void)s_glast; (void)s_gen_lo; (void)s_gen_hi;")
     for gi in range(NG):
         n_ = max(gtables[gi][0].size, 1)
         w(f"  __shared__ double s_Sg{gi}[{n_}]; __shared__ float s_Sg{gi}f[{n_}]; __shared__ long long s_Sg{gi}i[{n_}];")
@@ -684,6 +739,8 @@ def render_model(spec: dict) -> str:
         w("      }")
         w(f"      s_ut[{gi}][0] = I.g[{gi}].cta_tile[rank]; s_ut[{gi}][1] = I.g[{gi}].cta_tile[rank + 1];")
         w(f"      s_oscr[{gi}] = s_scr[{gi}]; s_otc[{gi}] = s_tc[{gi}];")
+        if g.get("generator"):
+            w(f"      s_glast[{gi}] = *((volatile int32_t*)I.g[{gi}].gen_last);")
         w(f"      if (!cache && I.g[{gi}].own_off >= 0) {{  // offset so that global positions address them")
         w(f"        s_oscr[{gi}] = (int32_t*)(s_state + I.g[{gi}].own_off) - I.g[{gi}].tile_start[s_ut[{gi}][0]];")
         w(f"        s_otc[{gi}] = (int32_t*)(s_state + I.g[{gi}].own_off + (((size_t)I.g[{gi}].own_cap * 4 + 15) & ~(size_t)15)) - s_ut[{gi}][0];")
@@ -1042,6 +1099,9 @@ def render_model(spec: dict) -> str:
     w("    }")
     w("    if (threadIdx.x == 0 && rank == 0) {")
     w("      *I.ts_done = ts;")
+    for gi, g in enumerate(groups):
+        if g.get("generator"):
+            w(f"      *I.g[{gi}].gen_last = s_glast[{gi}];")
     for m in range(len(spkmons)):
         w(f"      *I.sm[{m}].n = s_mon_n[{m}];")
     for m in range(len(statemons)):
@@ -1155,6 +1215,8 @@ def render_model(spec: dict) -> str:
         w("  __shared__ void* s_gv[B200_NG][B200_MAXV];")
         w("  __shared__ int s_ut[B200_NG][2];")
         w("  __shared__ int s_own[B200_NG][2];")
+        w("  __shared__ int s_glast[B200_NG], s_gen_lo, s_gen_hi;  // spike generator cursors")
+        w("  (void)s_glast; (void)s_gen_lo; (void)s_gen_hi;")
         w(f"  __shared__ long long s_head[{max(NP, 1)}], s_tail[{max(NP, 1)}];")
         w(f"  __shared__ int s_qoff[{max(NP, 1) + 1}], s_skip[{max(NP, 1)}];")
         w(f"  __shared__ int32_t* s_toff[{max(NP, 1)}];        // this CTA's batch table: per-delay offsets,")
@@ -1192,6 +1254,8 @@ def render_model(spec: dict) -> str:
         for gi, g in enumerate(groups):
             w(f"      s_ut[{gi}][0] = I.g[{gi}].cta_tile[rank]; s_ut[{gi}][1] = I.g[{gi}].cta_tile[rank + 1];")
             w(f"      s_own[{gi}][0] = I.g[{gi}].tile_start[s_ut[{gi}][0]]; s_own[{gi}][1] = I.g[{gi}].tile_start[s_ut[{gi}][1]];")
+            if g.get("generator"):
+                w(f"      s_glast[{gi}] = *((volatile int32_t*)I.g[{gi}].gen_last);")
             for k in range(len(g["vars"])):
                 w(f"      s_gv[{gi}][{k}] = I.g[{gi}].var[{k}];")
             w("      if (cache) {  // own neurons only: pointers offset so that global indices address them")
@@ -1728,6 +1792,9 @@ def render_model(spec: dict) -> str:
             w(f"      if (I.p[{pi}].D > 0) {{ I.p[{pi}].ev.state[2 * rank] = s_head[{pi}]; I.p[{pi}].ev.state[2 * rank + 1] = s_tail[{pi}]; }}")
         w("      if (rank == 0) {")
         w("        *I.ts_done = ts;")
+        for gi, g in enumerate(groups):
+            if g.get("generator"):
+                w(f"        *I.g[{gi}].gen_last = s_glast[{gi}];")
         for m in range(len(spkmons)):
             w(f"        *I.sm[{m}].n = s_mon_n[{m}];")
         for m in range(len(statemons)):

@@ -47,6 +47,13 @@ struct b200_group_d {
   int32_t* ring_prefix;   // [R*(n_tiles+1)] per-slot prefix of tile counts
   void* var[B200_MAX_VARS];      // state variables (SoA, length N)
   const double* S;        // scalar table (update | threshold | reset)
+  // spike generator groups (SpikeGeneratorGroup): spikes from sorted lists
+  const int32_t* gen_bins;   // [gen_n] time bin of each spike (non-decreasing)
+  const int32_t* gen_index;  // [gen_n] neuron of each spike
+  int64_t gen_n;
+  int32_t* gen_last;         // [1] next spike to emit (persists across launches)
+  int32_t gen_period;        // period in steps (0: no repetition)
+  int32_t _pad_g;
 };
 
 // Owner mode: per (pathway, CTA) FIFO of delivery events.  Every step the CTA
@@ -162,6 +169,7 @@ struct b200_group_info {
   const int* var_kind;
   int n_scalars;  // size of the scalar table
   const int* var_used;  // 1 if the step code touches the variable
+  int generator;  // 1: a spike generator group (spikes from b200_set_generator lists)
 };
 struct b200_pathway_info {
   const char* name;
@@ -515,6 +523,7 @@ struct b200_relayout_args {
   uint16_t* odelay;        // [n_syn]
   void* ovar[B200_MAX_PAYLOAD];
   int32_t* status;         // set to B200_ERR_INDEX on an out-of-range target
+  unsigned long long* own_in;  // [n_own] incoming synapses per owner (accumulated)
 };
 
 __device__ __forceinline__ int b200_owner_of(const int32_t* own_lo, int n_own, int32_t t) {
@@ -531,7 +540,11 @@ __global__ void b200_owner_relayout_kernel(b200_relayout_args A) {
   int* s_own = b200_rl_smem;                                     // [n_own + 1]
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
   int* cnt = b200_rl_smem + A.n_own + 1 + wid * A.n_own;        // [n_own] per warp
+  // [n_own] per warp: this warp's synapses per owner (8-byte aligned after the int arrays)
+  unsigned long long* tot = (unsigned long long*)(b200_rl_smem + ((A.n_own + 1 + nwarp * A.n_own + 1) & ~1)) +
+                            (size_t)wid * A.n_own;
   for (int k = threadIdx.x; k <= A.n_own; k += blockDim.x) s_own[k] = A.own_lo[k];
+  for (int k = lane; k < A.n_own; k += 32) tot[k] = 0;
   __syncthreads();
   const int32_t t_lo = s_own[0], t_hi = s_own[A.n_own];
   for (int64_t s = (int64_t)blockIdx.x * nwarp + wid; s < A.n_src; s += (int64_t)gridDim.x * nwarp) {
@@ -557,6 +570,7 @@ __global__ void b200_owner_relayout_kernel(b200_relayout_args A) {
         A.oseg[s * A.n_own + r] = base + acc;
         cnt[r] = (int)acc;
         acc += c;
+        tot[r] += (unsigned long long)c;
       }
     }
     __syncwarp();
@@ -593,5 +607,8 @@ __global__ void b200_owner_relayout_kernel(b200_relayout_args A) {
     }
     __syncwarp();
   }
+  __syncwarp();
+  for (int k = lane; k < A.n_own; k += 32)
+    if (tot[k]) atomicAdd(&A.own_in[k], tot[k]);
   if (blockIdx.x == 0 && threadIdx.x == 0) A.oseg[(int64_t)A.n_src * A.n_own] = A.segptr[(int64_t)A.n_src * A.W];
 }

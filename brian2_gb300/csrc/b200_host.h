@@ -30,6 +30,9 @@ struct b200_dbuf {  // a device buffer owned by the handle
 struct b200_group_h {
   int32_t N = 0;
   std::vector<b200_dbuf> var;
+  b200_dbuf gen_bins, gen_index, gen_last;  // spike generator lists and cursor
+  int64_t gen_n = 0;
+  int32_t gen_period = 0;
   std::vector<int32_t> tile_start, cta_tile;
   b200_dbuf d_tile_start, d_cta_tile, scratch, tile_cnt, ring, ring_total, ring_prefix;
   b200_dbuf S;
@@ -48,6 +51,7 @@ struct b200_pathway_h {
   b200_dbuf oseg, opost, odelay;
   std::vector<b200_dbuf> ovar;
   std::vector<int32_t> own_lo;  // ownership the layout was built for (empty: none)
+  std::vector<int64_t> own_in;  // incoming synapses of each owning CTA
   bool own_stale = true;
   b200_dbuf ev_tgt, ev_state, ev_base, ev_tag, ev_off;
   std::vector<b200_dbuf> ev_pay;
@@ -100,7 +104,7 @@ struct b200_net {
   bool use_clusters = true;       // instances of 2..16 CTAs run as thread-block clusters
   int allow_owner = 2;            // owner-mode delivery: 0 off, 1 on where possible, 2 auto
   int owner = 0;                  // 1: the current plan runs b200_owner_kernel
-  double ev_factor = 1.0;         // event FIFO records per CTA, in units of its incoming synapses
+  double ev_factor = 0.0;         // event FIFO records per CTA, in units of its incoming synapses (0: worst case)
   int cluster = 0;                // cluster size of the current launch plan (0: none)
   b200_dbuf prof;
   int queue_mode = 0;      // 1: single-CTA instances pulled from a work queue
@@ -225,6 +229,7 @@ int b200_destroy(b200_net* n) {
   for (auto& I : n->inst) {
     for (auto& G : I.g) {
       for (auto& b : G.var) b200_free(n, b);
+      b200_free(n, G.gen_bins); b200_free(n, G.gen_index); b200_free(n, G.gen_last);
       b200_free(n, G.d_tile_start); b200_free(n, G.d_cta_tile); b200_free(n, G.scratch);
       b200_free(n, G.tile_cnt); b200_free(n, G.ring); b200_free(n, G.ring_total);
       b200_free(n, G.ring_prefix); b200_free(n, G.S);
@@ -589,17 +594,19 @@ static int b200_owner_pathway(b200_net* n, int k, int p, b200_pathway_d& PD) {
     A.W = P.dmax - P.dmin + 1;
     A.dmin = P.dmin;
     A.n_own = C;
-    b200_dbuf d_own;
+    b200_dbuf d_own, d_in;
     if ((r = b200_alloc(n, d_own, (size_t)(C + 1) * 4, false))) return r;
+    if ((r = b200_alloc(n, d_in, (size_t)C * 8))) return r;
     B200_CU(n, cudaMemcpyAsync(d_own.p, own_lo.data(), (size_t)(C + 1) * 4, cudaMemcpyHostToDevice, n->stream));
     A.own_lo = (const int32_t*)d_own.p;
+    A.own_in = (unsigned long long*)d_in.p;
     A.oseg = (int64_t*)P.oseg.p;
     A.opost = (int32_t*)P.opost.p;
     A.odelay = (uint16_t*)P.odelay.p;
     A.status = (int32_t*)I.status.p;
     B200_CU(n, cudaMemsetAsync(I.status.p, 0, 4, n->stream));
     const int threads = 256, warps = threads / 32;
-    const size_t smem = (size_t)(C + 1 + warps * C) * 4;
+    const size_t smem = (size_t)((C + 1 + warps * C + 1) & ~1) * 4 + (size_t)warps * C * 8;
     if (smem > 48 * 1024)
       B200_CU(n, cudaFuncSetAttribute(b200_owner_relayout_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int n_sm = 0, dev = 0;
@@ -611,6 +618,9 @@ static int b200_owner_pathway(b200_net* n, int k, int p, b200_pathway_d& PD) {
     B200_CU(n, cudaGetLastError());
     B200_CU(n, cudaStreamSynchronize(n->stream));
     b200_free(n, d_own);
+    P.own_in.assign(C, 0);
+    B200_CU(n, cudaMemcpy(P.own_in.data(), d_in.p, (size_t)C * 8, cudaMemcpyDeviceToHost));
+    b200_free(n, d_in);
     int32_t st = 0;
     B200_CU(n, cudaMemcpy(&st, I.status.p, 4, cudaMemcpyDeviceToHost));
     if (st) {
@@ -620,15 +630,28 @@ static int b200_owner_pathway(b200_net* n, int k, int p, b200_pathway_d& PD) {
     P.own_lo = own_lo;
     P.own_stale = false;
   }
-  // event FIFOs (pathways with delays): room for `ev_factor` x the largest
-  // CTA's incoming synapses (estimated from the synapses per target neuron)
+  // event FIFOs (pathways with delays), in records per CTA.  A synapse carries
+  // at most one event per step and a batch is freed when its longest delay is
+  // delivered, so dmax + 2 batches of the largest CTA's incoming synapses never
+  // overflow: the default where that fits in an eighth of the device's memory,
+  // else the largest power of two that does (at least one batch).  An explicit
+  // b200_set_event_capacity factor sizes them in units of the incoming synapses.
   if (delays) {
-    int32_t widest = 0;
-    for (int c = 0; c < C; ++c) widest = std::max(widest, own_lo[c + 1] - own_lo[c]);
-    const double per_target = (double)P.n_syn / std::max(1, P.tgt_hi - P.tgt_lo);
-    const int64_t est = (int64_t)(1.25 * per_target * widest * n->ev_factor) + 1;
-    const int64_t cap = b200_pow2ceil(std::max<int64_t>(est, (int64_t)1 << 10));
+    int64_t max_in = 1;
+    for (int c = 0; c < C; ++c) max_in = std::max(max_in, P.own_in[c]);
     const int32_t W = P.dmax - P.dmin + 1, RB = P.dmax + 2;
+    size_t rec = 4;
+    for (int m = 0; m < PI.n_payload; ++m) rec += b200_kind_size(PI.var_kind[PI.payload_var[m]]);
+    int64_t cap;
+    if (n->ev_factor > 0) {
+      cap = b200_pow2ceil(std::max<int64_t>((int64_t)(n->ev_factor * (double)max_in) + 1, (int64_t)1 << 10));
+    } else {
+      size_t free_b = 0, total_b = 0;
+      B200_CU(n, cudaMemGetInfo(&free_b, &total_b));
+      const int64_t floor_cap = b200_pow2ceil(std::max<int64_t>(max_in + 1, (int64_t)1 << 10));
+      cap = b200_pow2ceil(std::max<int64_t>(max_in * (int64_t)(P.dmax + 2), (int64_t)1 << 10));
+      while (cap > floor_cap && (double)C * (double)cap * (double)rec > (double)total_b / 8) cap >>= 1;
+    }
     if (cap != P.ev_cap || W != P.ev_W || RB != P.ev_RB || C != P.ev_ncta) {
       if (I.ts > 0 && I.ran_owner == 1 && P.ev_cap > 0)
         return b200_fail(n, B200_ERR_ARG, "pathway %s: the event FIFO cannot be resized once the network has run", PI.name);
@@ -727,7 +750,16 @@ static int b200_prepare(b200_net* n) {
         if (M->ratemon[s].group == g) { cuts.push_back(I.rm[s].lo); cuts.push_back(I.rm[s].hi); }
       if (n->owner) R = B200_OWNER_RING;  // lists of the last steps only: events wait in the FIFOs
       const std::vector<int32_t> old_tiles = G.tile_start;
-      b200_make_tiles(G.N, I.n_cta, cuts, G.tile_start, G.cta_tile);
+      if (M->groups[g].generator) {
+        // a spike generator emits in array order (not by neuron): all its tiles
+        // belong to the first CTA, split only at source/monitor range boundaries
+        std::vector<int32_t> one;
+        b200_make_tiles(G.N, 1, cuts, G.tile_start, one);
+        G.cta_tile.assign(I.n_cta + 1, (int32_t)G.tile_start.size() - 1);
+        G.cta_tile[0] = 0;
+      } else {
+        b200_make_tiles(G.N, I.n_cta, cuts, G.tile_start, G.cta_tile);
+      }
       const int n_tiles = (int)G.tile_start.size() - 1;
       const bool ring_changed = (R != G.R) || !G.ring.p;
       const bool retile = !n->owner && !ring_changed && old_tiles != G.tile_start && I.ts > 0 && R > 1;
@@ -775,6 +807,18 @@ static int b200_prepare(b200_net* n) {
       GD.ring_prefix = (int32_t*)G.ring_prefix.p;
       for (int v = 0; v < M->groups[g].n_vars; ++v) GD.var[v] = G.var[v].p;
       GD.S = (const double*)G.S.p;
+      if (M->groups[g].generator) {
+        if (!G.gen_last.p) {  // no lists set: a generator without spikes
+          if ((r = b200_alloc(n, G.gen_last, 16))) return r;
+          if ((r = b200_alloc(n, G.gen_bins, 16))) return r;
+          if ((r = b200_alloc(n, G.gen_index, 16))) return r;
+        }
+        GD.gen_bins = (const int32_t*)G.gen_bins.p;
+        GD.gen_index = (const int32_t*)G.gen_index.p;
+        GD.gen_n = G.gen_n;
+        GD.gen_last = (int32_t*)G.gen_last.p;
+        GD.gen_period = G.gen_period;
+      }
     }
     for (int p = 0; p < M->n_pathways; ++p) {
       b200_pathway_h& P = I.p[p];
@@ -953,6 +997,10 @@ static int b200_prepare(b200_net* n) {
         std::vector<long> offs(M->n_groups);
         for (int g = 0; g < M->n_groups; ++g) {
           const b200_group_h& G = I.g[g];
+          if (M->groups[g].generator) {  // all on the first CTA: global lists
+            D.g[g].own_cap = 1; D.g[g].own_tiles = 1; offs[g] = -1;
+            continue;
+          }
           int cap = 0, tiles = 0;
           for (int c = 0; c < I.n_cta; ++c) {
             cap = std::max(cap, G.tile_start[G.cta_tile[c + 1]] - G.tile_start[G.cta_tile[c]]);
@@ -1312,6 +1360,47 @@ int b200_set_event_capacity(b200_net* n, double factor) {
   if (!n || !(factor > 0.0)) return B200_ERR_ARG;
   n->ev_factor = factor;
   n->prepared = false;
+  return 0;
+}
+
+// Spikes of a spike generator group (SpikeGeneratorGroup,
+// brian2/input/spikegeneratorgroup.py:21; emission as
+// brian2/devices/cpp_standalone/templates/spikegenerator.cpp:5-31): the time
+// bin and neuron of every spike, sorted by time bin; `period_bins` > 0 repeats
+// them with that period; `last` is the first spike still to emit.
+int b200_set_generator(b200_net* n, int32_t inst, int32_t group, const int32_t* bins, const int32_t* index,
+                       int64_t count, int32_t period_bins, int32_t last) {
+  if (!n || inst < 0 || inst >= n->n_inst || group < 0 || group >= n->M->n_groups || count < 0 ||
+      !n->M->groups[group].generator || count > INT32_MAX || last < 0 || last > count ||
+      (count && (!bins || !index)))
+    return b200_fail(n, B200_ERR_ARG, "bad generator group or arguments");
+  b200_group_h& G = n->inst[inst].g[group];
+  for (int64_t k = 0; k < count; ++k) {
+    if (index[k] < 0 || index[k] >= G.N) return b200_fail(n, B200_ERR_INDEX, "generator spike %lld: neuron out of range", (long long)k);
+    if (k && bins[k] < bins[k - 1]) return b200_fail(n, B200_ERR_ARG, "generator spikes not sorted by time bin");
+  }
+  int r;
+  if ((r = b200_alloc(n, G.gen_bins, (size_t)std::max<int64_t>(count, 1) * 4, false))) return r;
+  if ((r = b200_alloc(n, G.gen_index, (size_t)std::max<int64_t>(count, 1) * 4, false))) return r;
+  if ((r = b200_alloc(n, G.gen_last, 16))) return r;
+  if (count) {
+    B200_CU(n, cudaMemcpyAsync(G.gen_bins.p, bins, (size_t)count * 4, cudaMemcpyHostToDevice, n->stream));
+    B200_CU(n, cudaMemcpyAsync(G.gen_index.p, index, (size_t)count * 4, cudaMemcpyHostToDevice, n->stream));
+  }
+  B200_CU(n, cudaMemcpyAsync(G.gen_last.p, &last, 4, cudaMemcpyHostToDevice, n->stream));
+  B200_CU(n, cudaStreamSynchronize(n->stream));
+  G.gen_n = count;
+  G.gen_period = std::max(period_bins, 0);
+  n->prepared = false;
+  return 0;
+}
+
+// The generator's cursor after a run (the `_lastindex` the reference keeps).
+int b200_get_generator(b200_net* n, int32_t inst, int32_t group, int32_t* last) {
+  if (!n || inst < 0 || inst >= n->n_inst || group < 0 || group >= n->M->n_groups || !last ||
+      !n->M->groups[group].generator || !n->inst[inst].g[group].gen_last.p)
+    return b200_fail(n, B200_ERR_ARG, "bad generator group");
+  B200_CU(n, cudaMemcpy(last, n->inst[inst].g[group].gen_last.p, 4, cudaMemcpyDeviceToHost));
   return 0;
 }
 

@@ -6,7 +6,7 @@ Brian's standalone ``main`` has built the network, a job directory:
 * ``spec.json``: the network spec (groups, variables, Brian's generated code
   snippets, pathways, monitors, namespace constants);
 * ``init.npz``: the initial state written by ``main`` (group variables,
-  synapse indices, quantised delays and synaptic variables, monitor ranges and
+  spike generators' time bins, neuron indices, period and cursor, synapse indices, quantised delays and synaptic variables, monitor ranges and
   recorded indices, the clock's time step);
 * ``job.json``: dt, the step counts of the recorded ``run()`` calls and the
   launch options.
@@ -68,6 +68,9 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None)
     for gi, g in enumerate(spec["groups"]):
         for v in g["vars"]:
             net.upload(0, gi, v["name"], init[f"g{gi}_{v['name']}"])
+        if g.get("generator"):
+            net.set_generator(0, gi, init[f"g{gi}_gen_bins"], init[f"g{gi}_gen_index"],
+                              int(init[f"g{gi}_gen_period"]), int(init[f"g{gi}_gen_last"]))
     for pi, p in enumerate(spec.get("pathways", [])):
         steps = init[f"p{pi}_delay_steps"] if f"p{pi}_delay_steps" in init else None
         net.set_synapses(0, pi, init[f"p{pi}_pre"], init[f"p{pi}_post"], steps, int(init[f"p{pi}_scalar_delay"]),
@@ -93,6 +96,8 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None)
     for gi, g in enumerate(spec["groups"]):
         for v in g["vars"]:
             out[f"g{gi}_{v['name']}"] = net.download(0, gi, v["name"])
+        if g.get("generator"):
+            out[f"g{gi}_gen_last"] = np.int64(net.generator_cursor(0, gi))
     for pi, p in enumerate(spec.get("pathways", [])):
         for v in p.get("vars", []):
             out[f"p{pi}_{v['name']}"] = net.download_synapse_var(0, pi, v["name"])

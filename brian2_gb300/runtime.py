@@ -72,6 +72,8 @@ def _declare(lib):
         "b200_set_owner": [h, C.c_int32],
         "b200_owner_active": [h, _i32p],
         "b200_set_event_capacity": [h, C.c_double],
+        "b200_set_generator": [h, C.c_int32, C.c_int32, _i32p, _i32p, C.c_int64, C.c_int32, C.c_int32],
+        "b200_get_generator": [h, C.c_int32, C.c_int32, _i32p],
         "b200_launch_plan": [h, _i32p, _i32p, _i32p],
         "b200_profile_phases": [h, _i32p],
         "b200_get_profile": [h, C.c_int32, C.POINTER(C.c_uint64), C.c_int32],
@@ -229,6 +231,23 @@ class Network:
         return a
 
     # -- monitors -------------------------------------------------------------
+    def set_generator(self, inst, group, timebins, indices, period_bins=0, last=0):
+        """Spikes of a spike generator group: per entry its time bin (sorted)
+        and neuron index; the period in bins (0: none) and the cursor."""
+        g = self._g(group)
+        b = np.ascontiguousarray(timebins, dtype=np.int32)
+        i = np.ascontiguousarray(indices, dtype=np.int32)
+        if b.shape != i.shape:
+            raise ValueError("timebins and indices differ in length")
+        self._check(self.lib.b200_set_generator(self._h, int(inst), g, _ptr(b, _i32p), _ptr(i, _i32p), b.size,
+                                                int(period_bins), int(last)))
+
+    def generator_cursor(self, inst, group):
+        """The generator's cursor (the reference's `_lastindex`)."""
+        a = C.c_int32(0)
+        self._check(self.lib.b200_get_generator(self._h, int(inst), self._g(group), C.byref(a)))
+        return int(a.value)
+
     def set_spikemon_range(self, inst, mon, lo, hi):
         m = mon if isinstance(mon, int) else self.model.spkmon_index[mon]
         self._check(self.lib.b200_set_monitor_range(self._h, int(inst), 0, m, int(lo), int(hi)))

@@ -62,12 +62,22 @@ int b200_launch_plan(b200_net* net, int32_t* grid, int32_t* cluster, int32_t* st
  * in shared memory, with per-CTA event FIFOs ordered by due step.  A second
  * implementation of CSpikeQueue + on_pre (brian2/synapses/spikequeue.h:14-206,
  * templates/synapses.cpp:20-49); b200_owner_active reports whether the current
- * launch plan uses it.  b200_set_event_capacity sizes the FIFOs in units of a
- * CTA's incoming synapses (default 1); an overflow fails the run with
- * B200_STATUS_CAPACITY and a message. */
+ * launch plan uses it.  The FIFOs default to the worst case (dmax + 2 steps of
+ * a CTA's incoming synapses) where that fits in an eighth of the device memory;
+ * b200_set_event_capacity sizes them in units of a CTA's incoming synapses
+ * instead.  An overflow fails the run with B200_STATUS_CAPACITY and a message. */
 int b200_set_owner(b200_net* net, int32_t enable);
 int b200_owner_active(b200_net* net, int32_t* active);
 int b200_set_event_capacity(b200_net* net, double factor);
+/* Spike generator groups (input/spikegeneratorgroup.py:37-372, stepped by
+ * templates/spikegenerator.cpp:5-31): the entries' time bins (sorted, the
+ * group's `_timebins`), their neuron indices (`neuron_index`), the period in
+ * bins (`_period_bins`, 0 = none) and the cursor (`_lastindex`).  Each step
+ * emits the entries from the cursor whose bin is <= the step (modulo the
+ * period), as the group's spikes.  b200_get_generator reads the cursor back. */
+int b200_set_generator(b200_net* net, int32_t inst, int32_t group, const int32_t* bins, const int32_t* index,
+                       int64_t count, int32_t period_bins, int32_t last);
+int b200_get_generator(b200_net* net, int32_t inst, int32_t group, int32_t* last);
 /* Per-instance values of the model's namespace constants (the %CONSTANTS% of the
  * generated code objects, device.py:936-940); scalar blocks are re-evaluated. */
 int b200_set_consts(b200_net* net, int32_t inst, const double* values, int32_t count);

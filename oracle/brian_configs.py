@@ -242,10 +242,46 @@ def presynaptic_read(N=300, duration_ms=150.0, seed_value=51):
     return dict(P=P, S=S, spikes=s_mon, rate=r_mon)
 
 
+def spike_generator(N_in=100, N=300, duration_ms=130.0, period_ms=40.0, seed_value=61):
+    """A SpikeGeneratorGroup (four spikes per input in each 40 ms period,
+    some at exact multiples of dt, repeated three and a quarter times) driving
+    a recurrent CUBA population through synapses with delays."""
+    import numpy as np
+    from brian2 import (NeuronGroup, Synapses, SpikeGeneratorGroup, SpikeMonitor, PopulationRateMonitor,
+                        ms, mV, seed, run)
+    seed(seed_value)
+    rng = np.random.default_rng(seed_value)
+    n_bins = int(round(period_ms / 0.1))
+    idx, times = [], []
+    for k in range(N_in):
+        bins = rng.choice(n_bins, size=4, replace=False)
+        jitter = np.where(rng.random(4) < 0.25, 0.0, rng.random(4) * 0.09)
+        idx.extend([k] * 4)
+        times.extend(list(bins * 0.1 + jitter))
+    G = SpikeGeneratorGroup(N_in, np.array(idx), np.array(times) * ms, period=period_ms * ms)
+    ns = dict(taum=20 * ms, taue=5 * ms, Vt=-50 * mV, Vr=-60 * mV, El=-52 * mV, w_in=3 * mV, w=0.5 * mV)
+    P = NeuronGroup(N, '''dv/dt  = (ge-(v-El))/taum : volt
+                          dge/dt = -ge/taue : volt''',
+                    threshold='v>Vt', reset='v = Vr', method='exact', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    Sin = Synapses(G, P, on_pre='ge += w_in', namespace=ns)
+    Sin.connect(p=0.1)
+    Sin.delay = 'rand() * 2*ms'
+    S = Synapses(P, P, on_pre='ge += w', namespace=ns)
+    S.connect('i != j', p=0.05)
+    # monitors must be locals of the frame that calls run() (Brian collects them there)
+    s_mon = SpikeMonitor(P)
+    r_mon = PopulationRateMonitor(P)
+    g_mon = SpikeMonitor(G)
+    run(duration_ms * ms)
+    return dict(P=P, G=G, Sin=Sin, S=S, spikes=s_mon, rate=r_mon, gen_spikes=g_mon)
+
+
 SCENARIOS = {
     "lif_refractory": lif_refractory,
     "hetero_delays": hetero_delays,
     "subgroup_monitors": subgroup_monitors,
     "input_group": input_group,
     "presynaptic_read": presynaptic_read,
+    "spike_generator": spike_generator,
 }

@@ -12,6 +12,9 @@ code objects, and executes the spec's *plain* C++ snippets (Brian's own
 * state update over all neurons (templates/stateupdate.cpp:5-21);
 * threshold with sequential ascending compaction into the spike space and the
   refractory bookkeeping (templates/threshold.cpp:18-31);
+* spike generators: the entries from the cursor whose time bin is <= the
+  step's (modulo the period, with the cursor reset after a wrap), in array
+  order (templates/spikegenerator.cpp:5-31);
 * spike monitor append of (i, t) and per-neuron counts
   (templates/spikemonitor.cpp:13-48);
 * per pathway ``advance()`` then ``push()`` into a ring of synapse-index
@@ -87,6 +90,8 @@ def render_oracle(spec: dict) -> str:
         for v in g["vars"]:
             w(f"  std::vector<{v['ctype']}> g{gi}_{v['name']};")
         w(f"  std::vector<int32_t> spk{gi};")
+        if g.get("generator"):
+            w(f"  std::vector<int32_t> gen{gi}_bins, gen{gi}_index; int32_t gen{gi}_period = 0, gen{gi}_last = 0;")
     for pi, p in enumerate(paths):
         w(f"  int32_t p{pi}_src_lo = 0, p{pi}_src_hi = 0; std::vector<int32_t> p{pi}_pre, p{pi}_post, p{pi}_delay;")
         for v in p.get("vars", []):
@@ -149,6 +154,20 @@ def render_oracle(spec: dict) -> str:
         w("  }")
     w("  return 1;")
     w("}")
+    w("void oracle_set_generator(Net* n, int32_t g, const int32_t* bins, const int32_t* index, int64_t count,")
+    w("                          int32_t period, int32_t last) {")
+    for gi, g in enumerate(groups):
+        if g.get("generator"):
+            w(f"  if (g == {gi}) {{ n->gen{gi}_bins.assign(bins, bins + count); n->gen{gi}_index.assign(index, index + count);")
+            w(f"    n->gen{gi}_period = period; n->gen{gi}_last = last; }}")
+    w("}")
+    w("int32_t oracle_get_generator(Net* n, int32_t g) {")
+    for gi, g in enumerate(groups):
+        if g.get("generator"):
+            w(f"  if (g == {gi}) return n->gen{gi}_last;")
+    w("  return -1;")
+    w("}")
+    w("void oracle_set_step(Net* n, int64_t ts) { n->ts = ts; }")
     w("void oracle_set_range(Net* n, int32_t kind, int32_t mon, int32_t lo, int32_t hi) {")
     for mi, m in enumerate(spkmons):
         w(f"  if (kind == 0 && mon == {mi}) {{ n->sm{mi}_lo = lo; n->sm{mi}_hi = hi; n->sm{mi}_count.assign(hi - lo, 0); }}")
@@ -219,6 +238,17 @@ def render_oracle(spec: dict) -> str:
         w(gptrs(gi, 6))
         w(f"      const int32_t N = n->N{gi}; (void)N;")
         w(f"      n->spk{gi}.clear();")
+        if g.get("generator"):
+            w(f"      int32_t tb = (int32_t)n->ts; int32_t& last = n->gen{gi}_last;")
+            w(f"      if (n->gen{gi}_period > 0) {{")
+            w(f"        tb %= n->gen{gi}_period;")
+            w(f"        if (last > 0 && n->gen{gi}_bins[last - 1] >= tb) last = 0;")
+            w("      }")
+            w(f"      for (size_t k = last; k < n->gen{gi}_bins.size(); ++k) {{")
+            w(f"        if (n->gen{gi}_bins[k] > tb) break;")
+            w(f"        n->spk{gi}.push_back(n->gen{gi}_index[k]);")
+            w("      }")
+            w(f"      last += (int32_t)n->spk{gi}.size();")
         if g.get("threshold"):
             w("      {")
             w(_ind(g["threshold"]["scalar"], 8))
@@ -352,6 +382,11 @@ class OracleNet:
             lib.oracle_set_range.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
             lib.oracle_set_statemon.argtypes = [C.c_void_p, C.c_int32, _i32p, C.c_int32, _i32p, C.c_int32]
             lib.oracle_run.argtypes = [C.c_void_p, C.c_int64]
+            lib.oracle_set_generator.argtypes = [C.c_void_p, C.c_int32, _i32p, _i32p, C.c_int64, C.c_int32,
+                                                 C.c_int32]
+            lib.oracle_get_generator.argtypes = [C.c_void_p, C.c_int32]
+            lib.oracle_get_generator.restype = C.c_int32
+            lib.oracle_set_step.argtypes = [C.c_void_p, C.c_int64]
         self.lib = lib
         self.sizes = np.ascontiguousarray(sizes, dtype=np.int32).reshape(-1)
         self.h = lib.oracle_create(self.sizes.ctypes.data_as(_i32p), float(dt))
@@ -437,6 +472,18 @@ class OracleNet:
                                      vs.ctypes.data_as(_i32p), vs.size)
         self._stm[mon] = (vs.size, idx.size)
 
+    def set_generator(self, group, timebins, indices, period_bins=0, last=0):
+        b = np.ascontiguousarray(timebins, np.int32)
+        i = np.ascontiguousarray(indices, np.int32)
+        self.lib.oracle_set_generator(self.h, int(group), b.ctypes.data_as(_i32p), i.ctypes.data_as(_i32p), b.size,
+                                      int(period_bins), int(last))
+
+    def generator_cursor(self, group):
+        return int(self.lib.oracle_get_generator(self.h, int(group)))
+
+    def set_step(self, ts):
+        self.lib.oracle_set_step(self.h, int(ts))
+
     def run(self, n_steps):
         self.lib.oracle_run(self.h, int(n_steps))
 
@@ -490,3 +537,54 @@ def oracle_from_built(spec, built, dt=1e-4):
     for m, (lo, hi) in built.ratemon_ranges.items():
         o.set_ratemon_range(m if isinstance(m, int) else 0, lo, hi)
     return o
+
+
+def run_job_on_oracle(directory):
+    """Runs a job directory (brian2_gb300/job.py's format) on the oracle; the
+    returned dict has run_job's keys for state, monitors and generator cursors."""
+    import json as _json
+    with open(os.path.join(directory, "spec.json")) as f:
+        spec = _json.load(f)
+    with open(os.path.join(directory, "job.json")) as f:
+        job = _json.load(f)
+    with np.load(os.path.join(directory, "init.npz")) as z:
+        init = {k: z[k] for k in z.files}
+    sizes = [int(init[f"g{gi}_N"]) for gi in range(len(spec["groups"]))]
+    o = OracleNet(spec, sizes, job["dt"])
+    for gi, g in enumerate(spec["groups"]):
+        for v in g["vars"]:
+            o.upload(gi, v["name"], init[f"g{gi}_{v['name']}"])
+        if g.get("generator"):
+            o.set_generator(gi, init[f"g{gi}_gen_bins"], init[f"g{gi}_gen_index"], int(init[f"g{gi}_gen_period"]),
+                            int(init[f"g{gi}_gen_last"]))
+    for pi, p in enumerate(spec.get("pathways", [])):
+        steps = init.get(f"p{pi}_delay_steps")
+        o.set_synapses(pi, init[f"p{pi}_pre"], init[f"p{pi}_post"], steps, int(init[f"p{pi}_scalar_delay"]),
+                       tuple(int(x) for x in init[f"p{pi}_src_range"]), tuple(int(x) for x in init[f"p{pi}_tgt_range"]))
+        for v in p.get("vars", []):
+            o.upload_synapse_var(pi, v["name"], init[f"p{pi}_{v['name']}"])
+    for mi in range(len(spec.get("spike_monitors", []))):
+        o.set_spikemon_range(mi, *(int(x) for x in init[f"sm{mi}_range"]))
+    for mi in range(len(spec.get("rate_monitors", []))):
+        o.set_ratemon_range(mi, *(int(x) for x in init[f"rm{mi}_range"]))
+    for mi in range(len(spec.get("state_monitors", []))):
+        o.set_statemon(mi, init[f"stm{mi}_idx"], list(init[f"stm{mi}_vars"]))
+    o.set_step(int(init["ts0"]))
+    for n in job["runs"]:
+        o.run(int(n))
+    out = {}
+    for gi, g in enumerate(spec["groups"]):
+        for v in g["vars"]:
+            out[f"g{gi}_{v['name']}"] = o.download(gi, v["name"])
+        if g.get("generator"):
+            out[f"g{gi}_gen_last"] = np.int64(o.generator_cursor(gi))
+    for pi, p in enumerate(spec.get("pathways", [])):
+        for v in p.get("vars", []):
+            out[f"p{pi}_{v['name']}"] = o.download_synapse_var(pi, v["name"])
+    for mi in range(len(spec.get("spike_monitors", []))):
+        out[f"sm{mi}_i"], out[f"sm{mi}_ts"], out[f"sm{mi}_count"] = o.spikes(mi)
+    for mi in range(len(spec.get("rate_monitors", []))):
+        out[f"rm{mi}_counts"] = o.rate_counts(mi)
+    for mi in range(len(spec.get("state_monitors", []))):
+        out[f"stm{mi}_trace"] = o.state_trace(mi)
+    return out

@@ -7,7 +7,8 @@ per process):
 * with the reference's ``cpp_standalone`` device (one thread, strict IEEE
   flags, float64) -> ``tests/golden/scenarios/<name>.npz``: the spike monitor's
   indices and time steps, the rate monitor's per-step counts, the state
-  monitor's trace, the final state of the monitored group;
+  monitor's trace, the final state of the monitored group (and, for a spike
+  generator, its raster and final cursor);
 * with the ``b200`` plugin in deferred mode -> ``tests/golden/jobs/<name>/``:
   the job the plugin writes from the script (spec, initial state, synapses).
 
@@ -59,9 +60,19 @@ def run_ref(name):
     for var in ("v", "ge", "gi", "a"):
         if var in P.variables:
             out[var] = np.asarray(getattr(P, var + "_")[:]).copy()
+    meta = dict(group=P.name, n_spikes=int(len(t)), n_steps=int(len(out["rate_counts"])), spike_monitor=spk.name)
+    if "gen_spikes" in r:                       # a spike generator's own raster and cursor
+        g = r["gen_spikes"]
+        out["gen_i"] = np.asarray(g.i[:], dtype=np.int32)
+        out["gen_ts"] = np.round(np.asarray(g.t_[:]) / 1e-4).astype(np.int32)
+        meta["gen_monitor"] = g.name
+        meta["gen_group"] = r["G"].name
+        from brian2 import device             # the results file (get_value returns the cached initial 0)
+        fn = os.path.join(device.results_dir, device.get_array_filename(r["G"].variables["_lastindex"]))
+        meta["gen_lastindex"] = int(np.fromfile(fn, dtype=np.int32)[0])
     np.savez_compressed(os.path.join(HERE, "scenarios", name + ".npz"), **out)
     with open(os.path.join(HERE, "scenarios", name + ".json"), "w") as f:
-        json.dump(dict(group=P.name, n_spikes=int(len(t)), n_steps=int(len(out["rate_counts"]))), f, indent=1)
+        json.dump(meta, f, indent=1)
     print(name, "reference:", len(t), "spikes")
 
 

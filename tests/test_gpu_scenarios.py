@@ -19,7 +19,7 @@ from brian2_gb300.job import load_job, run_job
 pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 EXACT = {"lif_refractory": True, "hetero_delays": False, "subgroup_monitors": True, "input_group": True,
-         "presynaptic_read": False}
+         "presynaptic_read": False, "spike_generator": True}
 
 
 @pytest.mark.parametrize("name", sorted(EXACT))
@@ -32,9 +32,17 @@ def test_scenario_matches_reference(name, ctas, owner):
     with open(os.path.join(HERE, "golden", "scenarios", name + ".json")) as f:
         meta = json.load(f)
     out = run_job(jobdir, threads=128, ctas_per_inst=ctas, write=False, owner=owner)
-    assert len(out["sm0_i"]) == meta["n_spikes"]
-    np.testing.assert_array_equal(out["sm0_i"], ref["spk_i"])
-    np.testing.assert_array_equal(out["sm0_ts"], ref["spk_ts"])
+    mons = [m["name"] for m in spec["spike_monitors"]]
+    sm = mons.index(meta.get("spike_monitor", mons[0]))
+    assert len(out[f"sm{sm}_i"]) == meta["n_spikes"]
+    np.testing.assert_array_equal(out[f"sm{sm}_i"], ref["spk_i"])
+    np.testing.assert_array_equal(out[f"sm{sm}_ts"], ref["spk_ts"])
+    if "gen_monitor" in meta:                     # the spike generator's raster and final cursor
+        gm = mons.index(meta["gen_monitor"])
+        np.testing.assert_array_equal(out[f"sm{gm}_i"], ref["gen_i"])
+        np.testing.assert_array_equal(out[f"sm{gm}_ts"], ref["gen_ts"])
+        gg = [g["name"] for g in spec["groups"]].index(meta["gen_group"])
+        assert int(out[f"g{gg}_gen_last"]) == meta["gen_lastindex"]
     np.testing.assert_array_equal(out["rm0_counts"], ref["rate_counts"])
     gi = [g["name"] for g in spec["groups"]].index(meta["group"])
     for var in ("v", "ge", "gi", "a"):

@@ -33,7 +33,8 @@ def test_job_carries_the_reference_network(case, golden):
             np.testing.assert_array_equal(init[f"p{pi}_w"], z[f"{k}_w"])
 
 
-SCENARIOS = ["lif_refractory", "hetero_delays", "subgroup_monitors", "input_group", "presynaptic_read"]
+SCENARIOS = ["lif_refractory", "hetero_delays", "subgroup_monitors", "input_group", "presynaptic_read",
+             "spike_generator"]
 
 
 @pytest.mark.parametrize("name", SCENARIOS)
@@ -50,6 +51,13 @@ def test_scenario_jobs_describe_their_features(name):
         assert list(init["stm0_idx"]) == [0, 10, 250, 499]
     if name == "input_group":
         assert len(spec["groups"]) == 2 and {p["src"] for p in spec["pathways"]} == {0, 1}
+    if name == "spike_generator":
+        gi = next(k for k, g in enumerate(spec["groups"]) if g.get("generator"))
+        bins = init[f"g{gi}_gen_bins"]
+        assert int(init[f"g{gi}_gen_period"]) == 400 and int(init[f"g{gi}_gen_last"]) == 0
+        assert bins.size == 400 and np.all(np.diff(bins) >= 0) and bins.max() < 400
+        assert [v["name"] for v in spec["groups"][gi]["vars"]] == ["i"]
+        assert any(p["src"] == gi for p in spec["pathways"])
     if name == "presynaptic_read":
         assert any("_presynaptic_idx" in (p["on_pre"].get("vector_device") or p["on_pre"]["vector"])
                    for p in spec["pathways"])

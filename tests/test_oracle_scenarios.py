@@ -1,0 +1,45 @@
+"""The oracle pinned on the parity scenarios (no GPU): each job that the
+set_device('b200') plugin wrote from a script of
+oracle/brian_configs.py:SCENARIOS runs on the oracle and must reproduce the
+reference's own run of the same script (tests/golden/make_scenarios.py) bit
+for bit -- the oracle keeps the reference's queue order, so even the
+scenarios with unequal increments sum in the same order."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import run_job_on_oracle
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SCENARIOS = sorted(f[:-5] for f in os.listdir(os.path.join(HERE, "golden", "scenarios")) if f.endswith(".json"))
+
+
+@pytest.mark.parametrize("name", SCENARIOS)
+def test_oracle_reproduces_reference_scenario(name):
+    jobdir = os.path.join(HERE, "golden", "jobs", name)
+    with open(os.path.join(jobdir, "spec.json")) as f:
+        spec = json.load(f)
+    with np.load(os.path.join(HERE, "golden", "scenarios", name + ".npz")) as z:
+        ref = {k: z[k] for k in z.files}
+    with open(os.path.join(HERE, "golden", "scenarios", name + ".json")) as f:
+        meta = json.load(f)
+    out = run_job_on_oracle(jobdir)
+    mons = [m["name"] for m in spec["spike_monitors"]]
+    sm = mons.index(meta.get("spike_monitor", mons[0]))
+    np.testing.assert_array_equal(out[f"sm{sm}_i"], ref["spk_i"])
+    np.testing.assert_array_equal(out[f"sm{sm}_ts"], ref["spk_ts"])
+    np.testing.assert_array_equal(out["rm0_counts"], ref["rate_counts"])
+    if "gen_monitor" in meta:
+        gm = mons.index(meta["gen_monitor"])
+        np.testing.assert_array_equal(out[f"sm{gm}_i"], ref["gen_i"])
+        np.testing.assert_array_equal(out[f"sm{gm}_ts"], ref["gen_ts"])
+        gg = [g["name"] for g in spec["groups"]].index(meta["gen_group"])
+        assert int(out[f"g{gg}_gen_last"]) == meta["gen_lastindex"]
+    gi = [g["name"] for g in spec["groups"]].index(meta["group"])
+    for var in ("v", "ge", "gi", "a"):
+        if var in ref:
+            np.testing.assert_array_equal(out[f"g{gi}_{var}"], ref[var], err_msg=var)
+    if "state_v" in ref:
+        np.testing.assert_array_equal(out["stm0_trace"][:, 0, :].T, ref["state_v"])
