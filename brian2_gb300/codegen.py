@@ -184,6 +184,10 @@ class _Tables:
         return "\n".join(lines)
 
 
+# state words (4-byte) a thread keeps in flight in phase A's prefetch, in the
+# kernel variants with more than 64 registers
+PF_WORDS = 12
+
 _LOAD_RE = re.compile(r"^\s*(?:const\s+)?(\w+)\s+(\w+)\s*=\s*(_ptr_array_\w+)\[_idx\];\s*$")
 
 
@@ -288,6 +292,24 @@ def render_model(spec: dict) -> str:
 
     USED = [used_vars(gi) for gi in range(NG)]
 
+    def private_vars(gi):
+        """Used variables of group gi that only the CTA owning a neuron touches:
+        no pathway's on_pre and no other block's pointers name them (so a
+        multi-CTA classic instance may keep them in shared memory)."""
+        g = groups[gi]
+        if g.get("generator"):
+            return []
+        text = ""
+        for p in paths:
+            text += json.dumps(p.get("on_pre", {})) + json.dumps(p.get("group_ptrs", {}))
+        for gg in groups:
+            for blk in ("update", "threshold", "reset"):
+                if gg.get(blk):
+                    text += json.dumps(gg[blk].get("extra_ptrs", {}))
+        return [k for k in USED[gi] if not re.search(r"\b%s\b" % re.escape(g["vars"][k]["ptr"]), text)]
+
+    PRIV = [private_vars(gi) for gi in range(NG)]
+
     def owner_payloads():
         """Owner mode applies when every on_pre only adds, into variables of its
         target neuron, values computed from synaptic variables and constants.
@@ -330,7 +352,7 @@ def render_model(spec: dict) -> str:
     # device profile slots: classic kernel A, barrier A, lists, one per pathway,
     # barrier B; owner kernel update, barrier, lists, push pass 1, batch table +
     # pass 2, delivery
-    NPH = max(4 + NP, 6)
+    NPH = 6 + NP  # classic: A, barrier, lists, NP propagation, barrier, windows, items; owner: 6
     MAXV = max(len(g["vars"]) for g in groups)
 
     # ------------------------------------------------------------- model tables
@@ -338,13 +360,14 @@ def render_model(spec: dict) -> str:
         w(f"static const char* const b200_g{gi}_vars[] = {{" + ", ".join(f'"{v["name"]}"' for v in g["vars"]) + "};")
         w(f"static const int b200_g{gi}_kinds[] = {{" + ", ".join(str(CTYPE_KIND[v["ctype"]]) for v in g["vars"]) + "};")
         w(f"static const int b200_g{gi}_used[] = {{" + ", ".join("1" if k in USED[gi] else "0" for k in range(len(g["vars"]))) + "};")
+        w(f"static const int b200_g{gi}_priv[] = {{" + ", ".join("1" if k in PRIV[gi] else "0" for k in range(len(g["vars"]))) + "};")
     for pi, p in enumerate(paths):
         pv = p.get("vars", [])
         w(f"static const char* const b200_p{pi}_vars[] = {{" + ", ".join(f'"{v["name"]}"' for v in pv) + ('' if pv else '""') + "};")
         w(f"static const int b200_p{pi}_kinds[] = {{" + ", ".join(str(CTYPE_KIND[v["ctype"]]) for v in pv) + ('' if pv else '0') + "};")
     w("static const b200_group_info b200_groups[] = {" + ", ".join(
         f'{{"{g["name"]}", {len(g["vars"])}, b200_g{gi}_vars, b200_g{gi}_kinds, {gtables[gi][0].size}, b200_g{gi}_used, '
-        f'{1 if g.get("generator") else 0}}}'
+        f'{1 if g.get("generator") else 0}, b200_g{gi}_priv}}'
         for gi, g in enumerate(groups)) + "};")
     for pi, p in enumerate(paths):
         pay = PAYLOAD[pi] if OWNER else []
@@ -565,13 +588,17 @@ def render_model(spec: dict) -> str:
                 pf.setdefault(ptr, ct)
             pfi = {ptr: j for j, ptr in enumerate(pf)}
             words = sum(max(1, SIZE.get(ct, 8) // 4) for ct in pf.values())
-            PF = max(1, min(4, 16 // max(words, 1)))
+            # 16 words of loads in flight per thread in the variants capped at 64
+            # registers, PF_WORDS in the others
+            pf_small = max(1, min(4, 16 // max(words, 1)))
+            pf_big = max(1, min(32, PF_WORDS // max(words, 1)))
+            w(f"            constexpr int PF = (MAXT * MINB < 1024) ? {pf_big} : {pf_small};")
             w("            unsigned flags = 0u;")
-            w(f"            for (int k0 = 0; k0 < E; k0 += {PF}) {{")
+            w("            for (int k0 = 0; k0 < E; k0 += PF) {")
             for ptr, j in pfi.items():
-                w(f"              {pf[ptr]} _pf{j}[{PF}];")
+                w(f"              {pf[ptr]} _pf{j}[PF];")
             w("#pragma unroll")
-            w(f"              for (int kq = 0; kq < {PF}; ++kq) {{")
+            w("              for (int kq = 0; kq < PF; ++kq) {")
             w("                const int32_t _idx = pb + (k0 + kq) * (int)blockDim.x + threadIdx.x;")
             w("                if (k0 + kq < E && _idx < pe) {")
             for ptr, j in pfi.items():
@@ -579,7 +606,7 @@ def render_model(spec: dict) -> str:
             w("                }")
             w("              }")
             w("#pragma unroll")
-            w(f"              for (int kq = 0; kq < {PF}; ++kq) {{")
+            w("              for (int kq = 0; kq < PF; ++kq) {")
             w("              const int k = k0 + kq;")
             w("              const int32_t _idx = pb + k * (int)blockDim.x + threadIdx.x;")
             w("              if (k < E && _idx < pe) {")
@@ -690,6 +717,8 @@ def render_model(spec: dict) -> str:
     w("  __shared__ int s_ut[B200_NG][2];")
     w("  __shared__ int s_glast[B200_NG], s_gen_lo, s_gen_hi;  // spike generator cursors")
     w("  (void)s_glast; (void)s_gen_lo; (void)s_gen_hi;")
+    w("  __shared__ int s_pcache, s_pown[B200_NG][2];  // private-variable cache: on, own neuron range")
+    w("  (void)s_pown;")
     for gi in range(NG):
         n_ = max(gtables[gi][0].size, 1)
         w(f"  __shared__ double s_Sg{gi}[{n_}]; __shared__ float s_Sg{gi}f[{n_}]; __shared__ long long s_Sg{gi}i[{n_}];")
@@ -745,8 +774,33 @@ def render_model(spec: dict) -> str:
         w(f"        s_oscr[{gi}] = (int32_t*)(s_state + I.g[{gi}].own_off) - I.g[{gi}].tile_start[s_ut[{gi}][0]];")
         w(f"        s_otc[{gi}] = (int32_t*)(s_state + I.g[{gi}].own_off + (((size_t)I.g[{gi}].own_cap * 4 + 15) & ~(size_t)15)) - s_ut[{gi}][0];")
         w("      }")
+    # private variables of a multi-CTA instance: this CTA's neurons in shared
+    # memory for the launch, addressed by global index
+    w("      const int pcache = (!cache && I.priv_bytes > 0 && I.priv_bytes <= state_bytes) ? 1 : 0;")
+    w("      s_pcache = pcache;")
+    if any(PRIV):
+        w("      if (pcache) {")
+        w("        size_t poff = 0;")
+        for gi, g in enumerate(groups):
+            if not PRIV[gi]:
+                continue
+            w(f"        s_pown[{gi}][0] = I.g[{gi}].tile_start[s_ut[{gi}][0]]; s_pown[{gi}][1] = I.g[{gi}].tile_start[s_ut[{gi}][1]];")
+            for k in PRIV[gi]:
+                sz = SIZE[g["vars"][k]["ctype"]]
+                w(f"        s_gv[{gi}][{k}] = s_state + poff - (size_t)s_pown[{gi}][0] * {sz}; "
+                  f"poff += ((size_t)(s_pown[{gi}][1] - s_pown[{gi}][0]) * {sz} + 15) & ~(size_t)15;")
+        w("      }")
     w("    }")
     w("    __syncthreads();")
+    if any(PRIV):
+        w("    if (s_pcache) {")
+        for gi, g in enumerate(groups):
+            for k in PRIV[gi]:
+                sz = SIZE[g["vars"][k]["ctype"]]
+                w(f"      b200_copy_bytes((char*)s_gv[{gi}][{k}] + (size_t)s_pown[{gi}][0] * {sz}, "
+                  f"(const char*)I.g[{gi}].var[{k}] + (size_t)s_pown[{gi}][0] * {sz}, "
+                  f"(size_t)(s_pown[{gi}][1] - s_pown[{gi}][0]) * {sz});")
+        w("    }")
     for gi, g in enumerate(groups):
         w(f"    for (int u = threadIdx.x; u <= I.g[{gi}].n_tiles; u += blockDim.x) s_tst[{gi} * max_tiles1 + u] = I.g[{gi}].tile_start[u];")
     # loop-invariant scalars: one shared copy per CTA (all threads read the same words)
@@ -773,8 +827,8 @@ def render_model(spec: dict) -> str:
     w("    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, NW = blockDim.x >> 5;")
     w(f"    // per-phase device profile (thread 0 of each CTA; phases: A, barrier A, spike lists,")
     w(f"    // {NP} pathway(s), barrier B)")
-    w(f"    unsigned long long _pt = 0, _pacc[{4 + NP}];")
-    w(f"    for (int q = 0; q < {4 + NP}; ++q) _pacc[q] = 0;")
+    w(f"    unsigned long long _pt = 0, _pacc[{NPH}];")
+    w(f"    for (int q = 0; q < {NPH}; ++q) _pacc[q] = 0;")
     w("#define B200_PHASE(q) do { if (prof && threadIdx.x == 0) { const unsigned long long _c = clock64(); _pacc[q] += _c - _pt; _pt = _c; } } while (0)")
     w("    for (; ts < ts_stop; ++ts) {")
     w("      if (threadIdx.x == 0) {")
@@ -929,6 +983,7 @@ def render_model(spec: dict) -> str:
         w("          if (threadIdx.x == 0) s_ndoff[WT] = carry;")
         w("          __syncthreads();")
         w("        }")
+        w(f"        B200_PHASE({4 + NP});  // windows")
         w("        const int Wtot = s_ndoff[WT];")
         w("        const int i0 = (int)((int64_t)Wtot * rank / I.n_cta);")
         w("        const int i1 = (int)((int64_t)Wtot * (rank + 1) / I.n_cta);")
@@ -959,6 +1014,7 @@ def render_model(spec: dict) -> str:
         w("          const int off = b200_block_exscan(len, s_wsum, &E);")
         w("          s_item_off[threadIdx.x] = off;")
         w("          __syncthreads();")
+        w(f"          B200_PHASE({5 + NP});  // items")
         w("          const int nitems = (i1 - cb) < (int)blockDim.x ? (i1 - cb) : (int)blockDim.x;")
         # events: when every pathway of the group starts its on_pre with loads of
         # the same types, a thread first issues the loads of its four events,
@@ -1071,6 +1127,7 @@ def render_model(spec: dict) -> str:
         if two_phase:
             w("          }  // if constexpr")
         w("          __syncthreads();")
+        w(f"          B200_PHASE({3 + pis[0]});  // events")
         w("        }")
         w("      }")
         w(f"      B200_PHASE({3 + pis[0]});")
@@ -1078,7 +1135,7 @@ def render_model(spec: dict) -> str:
     w(f"      B200_PHASE({3 + NP});")
     w("    }  // steps")
     w(f"    if (prof && threadIdx.x == 0)")
-    w(f"      for (int q = 0; q < {4 + NP}; ++q) atomicAdd(&prof[(size_t)unit * {NPH} + q], _pacc[q]);")
+    w(f"      for (int q = 0; q < {NPH}; ++q) atomicAdd(&prof[(size_t)unit * {NPH} + q], _pacc[q]);")
     w("#undef B200_PHASE")
 
     # ---- end of launch: apply the reset of the last executed step, write back the cache
@@ -1097,6 +1154,15 @@ def render_model(spec: dict) -> str:
             sz = SIZE[g["vars"][k]["ctype"]]
             w(f"      b200_copy_bytes(I.g[{gi}].var[{k}], s_gv[{gi}][{k}], (size_t)I.g[{gi}].N * {sz});")
     w("    }")
+    if any(PRIV):
+        w("    if (s_pcache) {")
+        for gi, g in enumerate(groups):
+            for k in PRIV[gi]:
+                sz = SIZE[g["vars"][k]["ctype"]]
+                w(f"      b200_copy_bytes((char*)I.g[{gi}].var[{k}] + (size_t)s_pown[{gi}][0] * {sz}, "
+                  f"(const char*)s_gv[{gi}][{k}] + (size_t)s_pown[{gi}][0] * {sz}, "
+                  f"(size_t)(s_pown[{gi}][1] - s_pown[{gi}][0]) * {sz});")
+        w("    }")
     w("    if (threadIdx.x == 0 && rank == 0) {")
     w("      *I.ts_done = ts;")
     for gi, g in enumerate(groups):

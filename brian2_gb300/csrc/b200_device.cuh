@@ -137,7 +137,8 @@ struct b200_inst_d {
   int32_t tab_smem;       // 1: the batch tables are kept in shared memory for the launch
   int32_t stage_off;      // byte offset of the event staging area in shared memory
   int32_t stage_cap;      // events it holds (0: none; pushes take two passes over global memory)
-  int32_t _pad_o;
+  int32_t priv_bytes;     // classic multi-CTA instance: bytes of each CTA's shared-memory copy of
+                          // its own neurons' private variables (0: none)
   b200_group_d g[B200_MAX_GROUPS];
   b200_pathway_d p[B200_MAX_PATHWAYS];
   b200_spkmon_d sm[B200_MAX_SPKMON];
@@ -170,6 +171,8 @@ struct b200_group_info {
   int n_scalars;  // size of the scalar table
   const int* var_used;  // 1 if the step code touches the variable
   int generator;  // 1: a spike generator group (spikes from b200_set_generator lists)
+  const int* var_private;  // 1: used, and touched only by the CTA that owns the neuron (no
+                           // pathway or other group reads or writes it)
 };
 struct b200_pathway_info {
   const char* name;

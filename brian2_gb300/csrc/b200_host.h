@@ -987,13 +987,32 @@ static int b200_prepare(b200_net* n) {
       n->state_bytes = std::max<long>(n->state_bytes, bytes);
     }
     if (!n->owner && !n->queue_mode) {
-      // classic multi-CTA instances: a shared-memory copy of each CTA's own spike
-      // lists and tile counts (the reset and the ring copy read them there)
+      // classic multi-CTA instances: each CTA keeps its own neurons' private
+      // variables (touched by no pathway) in shared memory for the launch, then
+      // a copy of its own spike lists and tile counts (the reset and the ring
+      // copy read them there); with two CTAs per SM each gets half the room
+      const long room = n->min_blocks == 2 ? std::min(budget, (long)optin / 2 - other - 1024) : budget;
       for (int k = 0; k < n->n_inst; ++k) {
         b200_inst_d& D = n->h_insts[k];
         if (D.cache_bytes > 0) continue;
         const b200_inst_h& I = n->inst[k];
-        long off = 0;
+        long priv = 0;
+        if (n->smem_cache && I.n_cta > 1) {
+          for (int c = 0; c < I.n_cta; ++c) {
+            long b = 0;
+            for (int g = 0; g < M->n_groups; ++g) {
+              const b200_group_h& G = I.g[g];
+              const long Ng = G.tile_start[G.cta_tile[c + 1]] - G.tile_start[G.cta_tile[c]];
+              for (int v = 0; v < M->groups[g].n_vars; ++v)
+                if (M->groups[g].var_private[v]) b += (Ng * (long)b200_kind_size(M->groups[g].var_kind[v]) + 15) & ~15L;
+            }
+            priv = std::max(priv, b);
+          }
+          if (priv > room) priv = 0;
+        }
+        D.priv_bytes = (int32_t)priv;
+        n->state_bytes = std::max<long>(n->state_bytes, priv);
+        long off = (priv + 15) & ~15L;
         std::vector<long> offs(M->n_groups);
         for (int g = 0; g < M->n_groups; ++g) {
           const b200_group_h& G = I.g[g];
@@ -1011,7 +1030,7 @@ static int b200_prepare(b200_net* n) {
           offs[g] = off;
           off += (((long)D.g[g].own_cap * 4 + 15) & ~15L) + (((long)D.g[g].own_tiles * 4 + 15) & ~15L);
         }
-        if (off <= budget) {
+        if (off <= room) {
           for (int g = 0; g < M->n_groups; ++g) D.g[g].own_off = (int32_t)offs[g];
           n->state_bytes = std::max<long>(n->state_bytes, off);
         }
@@ -1423,7 +1442,9 @@ int b200_launch_plan(b200_net* n, int32_t* grid, int32_t* cluster, int32_t* stat
   return 0;
 }
 
-// Shared-memory state cache of single-CTA instances on (default) or off.
+// Shared-memory state cache (single-CTA instances: all used variables;
+// multi-CTA classic instances: each CTA's own neurons' private variables) on
+// (default) or off.
 int b200_set_smem_cache(b200_net* n, int32_t enable) {
   if (!n) return B200_ERR_ARG;
   n->smem_cache = enable != 0;

@@ -362,7 +362,8 @@ class Network:
                      "push_fifo", "deliver"]
         else:
             names = ["update_threshold_reset", "barrier_a", "spike_lists_monitors"] + \
-                    [f"propagate:{p['name']}" for p in self.model.spec.get("pathways", [])] + ["barrier_b"]
+                    [f"events:{p['name']}" for p in self.model.spec.get("pathways", [])] + \
+                    ["barrier_b", "delay_windows", "items"]
         return dict(zip(names, (int(x) for x in a)))
 
     def set_smem_cache(self, enable=True):

@@ -49,8 +49,9 @@ int b200_last_error(b200_net* net, char* buf, int64_t len);
  * thread preference (brian2/devices/cpp_standalone/device.py:60-67). */
 int b200_configure(b200_net* net, int32_t threads, const int32_t* ctas_per_inst, int32_t queue_mode,
                    int64_t chunk_steps, int32_t use_graph);
-/* Keep the state of single-CTA instances in shared memory for the duration of a
- * launch (default on; off is for comparison and tuning). */
+/* Keep the state of single-CTA instances, and each CTA's own neurons' private
+ * variables (those no pathway touches) in multi-CTA instances, in shared memory
+ * for the duration of a launch (default on; off is for comparison and tuning). */
 int b200_set_smem_cache(b200_net* net, int32_t enable);
 /* Run instances of 2..16 CTAs as thread-block clusters with the hardware cluster
  * barrier (default on), and report the launch plan that b200_run will use. */
