@@ -187,6 +187,9 @@ class _Tables:
 # state words (4-byte) a thread keeps in flight in phase A's prefetch, in the
 # kernel variants with more than 64 registers
 PF_WORDS = 12
+# events per thread whose loads are issued before any is applied (variants
+# with more than 64 registers)
+EVENT_BATCH = 4
 
 _LOAD_RE = re.compile(r"^\s*(?:const\s+)?(\w+)\s+(\w+)\s*=\s*(_ptr_array_\w+)\[_idx\];\s*$")
 
@@ -679,6 +682,9 @@ def render_model(spec: dict) -> str:
     w("}")
     w("")
     w(f"#define B200_NG {NG}")
+    w("#define B200_LIST_RUN 4  // tile counts a thread loads at once in the spike-list prefix")
+    w(f"#define B200_EVENT_BATCH {EVENT_BATCH}  // events whose loads a thread issues before applying them")
+    w(f"#define B200_WR_SLOTS {max(16, min(128, 1024 // max(NP, 1)))}  // ring slots whose spike bounds a CTA keeps in shared memory")
     w(f"#define B200_MAXV {MAXV}")
     w("// dynamic shared memory: [state cache | item seg | item off | item src | item pathway | prefix |")
     w("//                         tile starts | delays]")
@@ -718,6 +724,8 @@ def render_model(spec: dict) -> str:
     w("  __shared__ int s_glast[B200_NG], s_gen_lo, s_gen_hi;  // spike generator cursors")
     w("  (void)s_glast; (void)s_gen_lo; (void)s_gen_hi;")
     w("  __shared__ int s_pcache, s_pown[B200_NG][2];  // private-variable cache: on, own neuron range")
+    w(f"  __shared__ int s_wr[{max(NP, 1)} * B200_WR_SLOTS * 2];  // per pathway and ring slot: bounds of the slot's spikes")
+    w(f"  __shared__ int s_wr_ok[{max(NP, 1)}];                   // 1: the ring fits B200_WR_SLOTS")
     w("  (void)s_pown;")
     for gi in range(NG):
         n_ = max(gtables[gi][0].size, 1)
@@ -812,6 +820,20 @@ def render_model(spec: dict) -> str:
         w(f"    for (int k = threadIdx.x; k < {ptables[pi][0].size}; k += blockDim.x) {{")
         w(f"      const double x = I.p[{pi}].S[k]; s_Sp{pi}[k] = x; s_Sp{pi}f[k] = (float)x; s_Sp{pi}i[k] = (long long)x;")
         w("    }")
+    # the spike bounds of the ring slots written by earlier launches
+    for pi, p in enumerate(paths):
+        sg = p["src"]
+        w("    {")
+        w(f"      const b200_group_d& G = I.g[{sg}];")
+        w(f"      const int okw = G.R > 1 && G.R <= B200_WR_SLOTS;")
+        w(f"      if (threadIdx.x == 0) s_wr_ok[{pi}] = okw;")
+        w("      if (okw)")
+        w("        for (int sl = threadIdx.x; sl < G.R; sl += blockDim.x) {")
+        w("          const int32_t* rp = G.ring_prefix + (int64_t)sl * (G.n_tiles + 1);")
+        w(f"          s_wr[({pi} * B200_WR_SLOTS + sl) * 2] = rp[I.p[{pi}].tile_lo];")
+        w(f"          s_wr[({pi} * B200_WR_SLOTS + sl) * 2 + 1] = rp[I.p[{pi}].tile_hi];")
+        w("        }")
+        w("    }")
     w("    if (s_cache) {  // state of a single-CTA instance lives in shared memory for the launch")
     for gi, g in enumerate(groups):
         for k in USED[gi]:
@@ -860,18 +882,41 @@ def render_model(spec: dict) -> str:
         w(f"        const int32_t* const tcnt = s_tc[{gi}];")
         w(f"        const int32_t* const oscr = s_oscr[{gi}];  // this CTA's own lists")
         w("        const int nt = GD.n_tiles;")
-        w("        int carry = 0;")
-        w("        for (int c0 = 0; c0 < nt; c0 += blockDim.x) {")
-        w("          const int u = c0 + threadIdx.x;")
-        w("          const int x = u < nt ? tcnt[u] : 0;")
+        # every thread loads its run of consecutive tile counts at once (one
+        # round trip), then one block scan of the run totals
+        w("        {")
+        w("          const int per = (nt + (int)blockDim.x - 1) / (int)blockDim.x;")
+        w("          const int u0r = threadIdx.x * per;")
+        w("          int c[B200_LIST_RUN];")
+        w("          int sum = 0;")
+        w("          if (per <= B200_LIST_RUN) {")
+        w("#pragma unroll")
+        w("            for (int r = 0; r < B200_LIST_RUN; ++r) c[r] = (r < per && u0r + r < nt) ? tcnt[u0r + r] : 0;")
+        w("#pragma unroll")
+        w("            for (int r = 0; r < B200_LIST_RUN; ++r) sum += c[r];")
+        w("          } else {")
+        w("            for (int r = 0; r < per; ++r) sum += (u0r + r < nt) ? tcnt[u0r + r] : 0;")
+        w("          }")
         w("          int tot;")
-        w("          const int ex = b200_block_exscan(x, s_wsum, &tot);")
-        w("          if (u < nt) pref[u] = carry + ex;")
-        w("          carry += tot;")
+        w("          int ex = b200_block_exscan(sum, s_wsum, &tot);")
+        w("          if (per <= B200_LIST_RUN) {")
+        w("#pragma unroll")
+        w("            for (int r = 0; r < B200_LIST_RUN; ++r) if (r < per && u0r + r < nt) { pref[u0r + r] = ex; ex += c[r]; }")
+        w("          } else {")
+        w("            for (int r = 0; r < per; ++r) if (u0r + r < nt) { pref[u0r + r] = ex; ex += tcnt[u0r + r]; }")
+        w("          }")
+        w("          if (threadIdx.x == 0) pref[nt] = tot;")
         w("        }")
-        w("        if (threadIdx.x == 0) pref[nt] = carry;")
         w("        __syncthreads();")
         w(f"        const int u0 = s_ut[{gi}][0], u1 = s_ut[{gi}][1];")
+        src_of = [pi for pi, p in enumerate(paths) if p["src"] == gi]
+        if src_of:
+            w("        if (GD.R > 1 && threadIdx.x == 0) {  // the slot's spike bounds per pathway, for later steps")
+            w("          const int slot = (int)(ts % GD.R);")
+            for pi in src_of:
+                w(f"          if (s_wr_ok[{pi}]) {{ s_wr[({pi} * B200_WR_SLOTS + slot) * 2] = pref[I.p[{pi}].tile_lo]; "
+                  f"s_wr[({pi} * B200_WR_SLOTS + slot) * 2 + 1] = pref[I.p[{pi}].tile_hi]; }}")
+            w("        }")
         w("        if (GD.R > 1) {")
         w("          const int slot = (int)(ts % GD.R);")
         w("          int32_t* const ring = GD.ring + (int64_t)slot * GD.N;")
@@ -898,7 +943,7 @@ def render_model(spec: dict) -> str:
             w("              const long long pos = mbase + pref[u] + j;")
             w("              SM.i[pos] = idx - SM.lo;")
             w("              SM.ts[pos] = (int32_t)ts;")
-            w("              SM.count[idx - SM.lo] += 1;")
+            w("              atomicAdd(&SM.count[idx - SM.lo], 1);  // no read round trip (own neurons: uncontended)")
             w("            }")
             w("          }")
             w("          __syncthreads();")
@@ -913,6 +958,8 @@ def render_model(spec: dict) -> str:
             w("        }")
         w("      }")
 
+    if NP:
+        w("      __syncthreads();  // the slot bounds recorded above")
     w("      B200_PHASE(2);")
     # ---- Phase B: synaptic propagation, one pass per source group: the items
     # (delay slot, spike) of all its pathways form one list, so the dependent
@@ -940,7 +987,8 @@ def render_model(spec: dict) -> str:
             pexpr = "0"
             for q in reversed(range(L)):
                 pexpr = f"{pis[q]}" if q == L - 1 else f"(q == {q} ? {pis[q]} : {pexpr})"
-            out.append(f"const b200_pathway_d& PD = I.p[{pexpr}];")
+            out.append(f"const int pw = {pexpr}; (void)pw;")
+            out.append("const b200_pathway_d& PD = I.p[pw];")
             return _indent("\n".join(out), ind)
 
         w(f"      // ---- pathways {', '.join(paths[q]['name'] for q in pis)}: propagation")
@@ -962,7 +1010,10 @@ def render_model(spec: dict) -> str:
         w("          int n = 0, b = 0;")
         w("          if (s >= 0) {")
         w("            if (d == 0) { b = pref[PD.tile_lo]; n = pref[PD.tile_hi] - b; }")
-        w("            else {")
+        w("            else if (s_wr_ok[pw]) {  // this CTA's shared copy of the slot's bounds")
+        w("              const int* wr = s_wr + (pw * B200_WR_SLOTS + (int)(s % SGD.R)) * 2;")
+        w("              b = wr[0]; n = wr[1] - b;")
+        w("            } else {")
         w("              const int32_t* rp = SGD.ring_prefix + (int64_t)(s % SGD.R) * (SGD.n_tiles + 1);")
         w("              b = rp[PD.tile_lo]; n = rp[PD.tile_hi] - b;")
         w("            }")
@@ -1040,12 +1091,12 @@ def render_model(spec: dict) -> str:
                 k = next(k for k, v in enumerate(p.get("vars", [])) if v["ptr"] == ptr)
                 return f"(({ct}*)I.p[{pi}].var[{k}])[_idx]"
 
-            w("          for (int e0 = threadIdx.x; e0 < E; e0 += 4 * (int)blockDim.x) {")
-            w("            int _q4[4]; int32_t _pre4[4]; int64_t _ix4[4];")
+            w("          for (int e0 = threadIdx.x; e0 < E; e0 += B200_EVENT_BATCH * (int)blockDim.x) {")
+            w("            int _q4[B200_EVENT_BATCH]; int32_t _pre4[B200_EVENT_BATCH]; int64_t _ix4[B200_EVENT_BATCH];")
             for li, ct in enumerate(sigs[0]):
-                w(f"            {ct} _ld{li}[4];")
+                w(f"            {ct} _ld{li}[B200_EVENT_BATCH];")
             w("#pragma unroll")
-            w("            for (int qq = 0; qq < 4; ++qq) {")
+            w("            for (int qq = 0; qq < B200_EVENT_BATCH; ++qq) {")
             w("              const int e = e0 + qq * (int)blockDim.x;")
             w("              _q4[qq] = -1;")
             w("              if (e < E) {")
@@ -1063,7 +1114,7 @@ def render_model(spec: dict) -> str:
             w("              }")
             w("            }")
             w("#pragma unroll")
-            w("            for (int qq = 0; qq < 4; ++qq) {")
+            w("            for (int qq = 0; qq < B200_EVENT_BATCH; ++qq) {")
             w("              if (_q4[qq] >= 0) {")
             w("                const int q = _q4[qq];")
             w("                const int64_t _idx = _ix4[qq]; (void)_idx;")
