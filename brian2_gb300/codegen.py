@@ -846,6 +846,7 @@ def render_model(spec: dict) -> str:
     w("    const double _b200_dt = I.dt;")
     w("    int64_t ts = ts0;")
     w("    bool ok = true;")
+    w("    const bool lagm = I.lag && I.n_cta > 1;  // deliveries read no spikes of their own step")
     w("    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, NW = blockDim.x >> 5;")
     w(f"    // per-phase device profile (thread 0 of each CTA; phases: A, barrier A, spike lists,")
     w(f"    // {NP} pathway(s), barrier B)")
@@ -869,98 +870,106 @@ def render_model(spec: dict) -> str:
     w("      B200_PHASE(0);")
     w("      // test hook: CTA `fault_rank` leaves without arriving, the others must time out")
     w("      if (rank == fault_rank && ts == ts0) { ok = false; break; }")
-    w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster, rank)) { ok = false; break; }")
-    w("      B200_PHASE(1);")
-
     # ---- Phase B: prefix of tile counts, ring, monitors
-    for gi, g in enumerate(groups):
-        w(f"      // ---- group {gi}: phase B (spike lists)")
-        w("      {")
-        w(f"        b200_group_d& GD = I.g[{gi}];")
-        w(f"        int* const pref = s_pref_all + {gi} * max_tiles1;")
-        w(f"        const int* const tst = s_tst + {gi} * max_tiles1;")
-        w(f"        const int32_t* const tcnt = s_tc[{gi}];")
-        w(f"        const int32_t* const oscr = s_oscr[{gi}];  // this CTA's own lists")
-        w("        const int nt = GD.n_tiles;")
-        # every thread loads its run of consecutive tile counts at once (one
-        # round trip), then one block scan of the run totals
-        w("        {")
-        w("          const int per = (nt + (int)blockDim.x - 1) / (int)blockDim.x;")
-        w("          const int u0r = threadIdx.x * per;")
-        w("          int c[B200_LIST_RUN];")
-        w("          int sum = 0;")
-        w("          if (per <= B200_LIST_RUN) {")
-        w("#pragma unroll")
-        w("            for (int r = 0; r < B200_LIST_RUN; ++r) c[r] = (r < per && u0r + r < nt) ? tcnt[u0r + r] : 0;")
-        w("#pragma unroll")
-        w("            for (int r = 0; r < B200_LIST_RUN; ++r) sum += c[r];")
-        w("          } else {")
-        w("            for (int r = 0; r < per; ++r) sum += (u0r + r < nt) ? tcnt[u0r + r] : 0;")
-        w("          }")
-        w("          int tot;")
-        w("          int ex = b200_block_exscan(sum, s_wsum, &tot);")
-        w("          if (per <= B200_LIST_RUN) {")
-        w("#pragma unroll")
-        w("            for (int r = 0; r < B200_LIST_RUN; ++r) if (r < per && u0r + r < nt) { pref[u0r + r] = ex; ex += c[r]; }")
-        w("          } else {")
-        w("            for (int r = 0; r < per; ++r) if (u0r + r < nt) { pref[u0r + r] = ex; ex += tcnt[u0r + r]; }")
-        w("          }")
-        w("          if (threadIdx.x == 0) pref[nt] = tot;")
-        w("        }")
-        w("        __syncthreads();")
-        w(f"        const int u0 = s_ut[{gi}][0], u1 = s_ut[{gi}][1];")
-        src_of = [pi for pi, p in enumerate(paths) if p["src"] == gi]
-        if src_of:
-            w("        if (GD.R > 1 && threadIdx.x == 0) {  // the slot's spike bounds per pathway, for later steps")
-            w("          const int slot = (int)(ts % GD.R);")
-            for pi in src_of:
-                w(f"          if (s_wr_ok[{pi}]) {{ s_wr[({pi} * B200_WR_SLOTS + slot) * 2] = pref[I.p[{pi}].tile_lo]; "
-                  f"s_wr[({pi} * B200_WR_SLOTS + slot) * 2 + 1] = pref[I.p[{pi}].tile_hi]; }}")
-            w("        }")
-        w("        if (GD.R > 1) {")
-        w("          const int slot = (int)(ts % GD.R);")
-        w("          int32_t* const ring = GD.ring + (int64_t)slot * GD.N;")
-        w("          for (int u = u0; u < u1; ++u) {")
-        w("            const int cnt = pref[u + 1] - pref[u], base = tst[u];")
-        w("            for (int j = threadIdx.x; j < cnt; j += blockDim.x) ring[pref[u] + j] = oscr[base + j];")
-        w("          }")
-        w("          if (rank == 0) {")
-        w("            for (int u = threadIdx.x; u <= nt; u += blockDim.x) GD.ring_prefix[(int64_t)slot * (nt + 1) + u] = pref[u];")
-        w("            if (threadIdx.x == 0) GD.ring_total[slot] = pref[nt];")
-        w("          }")
-        w("        }")
-        for mi, m in enumerate(spkmons):
-            if m["group"] != gi:
-                continue
-            w(f"        {{  // spike monitor {mi}")
-            w(f"          const b200_spkmon_d& SM = I.sm[{mi}];")
-            w(f"          const long long mbase = s_mon_n[{mi}] - pref[SM.tile_lo];")
-            w("          const int a = u0 > SM.tile_lo ? u0 : SM.tile_lo, b = u1 < SM.tile_hi ? u1 : SM.tile_hi;")
-            w("          for (int u = a; u < b; ++u) {")
-            w("            const int cnt = pref[u + 1] - pref[u], base = tst[u];")
-            w("            for (int j = threadIdx.x; j < cnt; j += blockDim.x) {")
-            w("              const int idx = oscr[base + j];")
-            w("              const long long pos = mbase + pref[u] + j;")
-            w("              SM.i[pos] = idx - SM.lo;")
-            w("              SM.ts[pos] = (int32_t)ts;")
-            w("              atomicAdd(&SM.count[idx - SM.lo], 1);  // no read round trip (own neurons: uncontended)")
-            w("            }")
+    def emit_lists():
+        for gi, g in enumerate(groups):
+            w(f"      // ---- group {gi}: phase B (spike lists)")
+            w("      {")
+            w(f"        b200_group_d& GD = I.g[{gi}];")
+            w(f"        int* const pref = s_pref_all + {gi} * max_tiles1;")
+            w(f"        const int* const tst = s_tst + {gi} * max_tiles1;")
+            w(f"        const int32_t* const tcnt = s_tc[{gi}];")
+            w(f"        const int32_t* const oscr = s_oscr[{gi}];  // this CTA's own lists")
+            w("        const int nt = GD.n_tiles;")
+            # every thread loads its run of consecutive tile counts at once (one
+            # round trip), then one block scan of the run totals
+            w("        {")
+            w("          const int per = (nt + (int)blockDim.x - 1) / (int)blockDim.x;")
+            w("          const int u0r = threadIdx.x * per;")
+            w("          int c[B200_LIST_RUN];")
+            w("          int sum = 0;")
+            w("          if (per <= B200_LIST_RUN) {")
+            w("#pragma unroll")
+            w("            for (int r = 0; r < B200_LIST_RUN; ++r) c[r] = (r < per && u0r + r < nt) ? tcnt[u0r + r] : 0;")
+            w("#pragma unroll")
+            w("            for (int r = 0; r < B200_LIST_RUN; ++r) sum += c[r];")
+            w("          } else {")
+            w("            for (int r = 0; r < per; ++r) sum += (u0r + r < nt) ? tcnt[u0r + r] : 0;")
             w("          }")
-            w("          __syncthreads();")
-            w(f"          if (threadIdx.x == 0) s_mon_n[{mi}] += pref[SM.tile_hi] - pref[SM.tile_lo];")
+            w("          int tot;")
+            w("          int ex = b200_block_exscan(sum, s_wsum, &tot);")
+            w("          if (per <= B200_LIST_RUN) {")
+            w("#pragma unroll")
+            w("            for (int r = 0; r < B200_LIST_RUN; ++r) if (r < per && u0r + r < nt) { pref[u0r + r] = ex; ex += c[r]; }")
+            w("          } else {")
+            w("            for (int r = 0; r < per; ++r) if (u0r + r < nt) { pref[u0r + r] = ex; ex += tcnt[u0r + r]; }")
+            w("          }")
+            w("          if (threadIdx.x == 0) pref[nt] = tot;")
             w("        }")
-        for mi, m in enumerate(ratemons):
-            if m["group"] != gi:
-                continue
-            w(f"        if (rank == 0 && threadIdx.x == 0) {{  // rate monitor {mi}")
-            w(f"          const b200_ratemon_d& RM = I.rm[{mi}];")
-            w("          RM.cnt[ts - RM.step0] = pref[RM.tile_hi] - pref[RM.tile_lo];")
+            w("        __syncthreads();")
+            w(f"        const int u0 = s_ut[{gi}][0], u1 = s_ut[{gi}][1];")
+            src_of = [pi for pi, p in enumerate(paths) if p["src"] == gi]
+            if src_of:
+                w("        if (GD.R > 1 && threadIdx.x == 0) {  // the slot's spike bounds per pathway, for later steps")
+                w("          const int slot = (int)(ts % GD.R);")
+                for pi in src_of:
+                    w(f"          if (s_wr_ok[{pi}]) {{ s_wr[({pi} * B200_WR_SLOTS + slot) * 2] = pref[I.p[{pi}].tile_lo]; "
+                      f"s_wr[({pi} * B200_WR_SLOTS + slot) * 2 + 1] = pref[I.p[{pi}].tile_hi]; }}")
+                w("        }")
+            w("        if (GD.R > 1) {")
+            w("          const int slot = (int)(ts % GD.R);")
+            w("          int32_t* const ring = GD.ring + (int64_t)slot * GD.N;")
+            w("          for (int u = u0; u < u1; ++u) {")
+            w("            const int cnt = pref[u + 1] - pref[u], base = tst[u];")
+            w("            for (int j = threadIdx.x; j < cnt; j += blockDim.x) ring[pref[u] + j] = oscr[base + j];")
+            w("          }")
+            w("          if (rank == 0) {")
+            w("            for (int u = threadIdx.x; u <= nt; u += blockDim.x) GD.ring_prefix[(int64_t)slot * (nt + 1) + u] = pref[u];")
+            w("            if (threadIdx.x == 0) GD.ring_total[slot] = pref[nt];")
+            w("          }")
             w("        }")
-        w("      }")
+            for mi, m in enumerate(spkmons):
+                if m["group"] != gi:
+                    continue
+                w(f"        {{  // spike monitor {mi}")
+                w(f"          const b200_spkmon_d& SM = I.sm[{mi}];")
+                w(f"          const long long mbase = s_mon_n[{mi}] - pref[SM.tile_lo];")
+                w("          const int a = u0 > SM.tile_lo ? u0 : SM.tile_lo, b = u1 < SM.tile_hi ? u1 : SM.tile_hi;")
+                w("          for (int u = a; u < b; ++u) {")
+                w("            const int cnt = pref[u + 1] - pref[u], base = tst[u];")
+                w("            for (int j = threadIdx.x; j < cnt; j += blockDim.x) {")
+                w("              const int idx = oscr[base + j];")
+                w("              const long long pos = mbase + pref[u] + j;")
+                w("              SM.i[pos] = idx - SM.lo;")
+                w("              SM.ts[pos] = (int32_t)ts;")
+                w("              atomicAdd(&SM.count[idx - SM.lo], 1);  // no read round trip (own neurons: uncontended)")
+                w("            }")
+                w("          }")
+                w("          __syncthreads();")
+                w(f"          if (threadIdx.x == 0) s_mon_n[{mi}] += pref[SM.tile_hi] - pref[SM.tile_lo];")
+                w("        }")
+            for mi, m in enumerate(ratemons):
+                if m["group"] != gi:
+                    continue
+                w(f"        if (rank == 0 && threadIdx.x == 0) {{  // rate monitor {mi}")
+                w(f"          const b200_ratemon_d& RM = I.rm[{mi}];")
+                w("          RM.cnt[ts - RM.step0] = pref[RM.tile_hi] - pref[RM.tile_lo];")
+                w("        }")
+            w("      }")
 
-    if NP:
-        w("      __syncthreads();  // the slot bounds recorded above")
-    w("      B200_PHASE(2);")
+        if NP:
+            w("      __syncthreads();  // the slot bounds recorded above")
+        w("      B200_PHASE(2);")
+    w("      unsigned bar_old = 0u;")
+    w("      bool pend = false;  // lag mode: barrier A arrived, not yet waited for")
+    w("      if (lagm) {")
+    w("        b200_inst_arrive(I, cluster, rank, bar_old);")
+    w("        pend = true;")
+    w("      } else {")
+    w("        if (!b200_inst_barrier(I, gen, limit_ns, cluster, rank)) { ok = false; break; }")
+    w("        B200_PHASE(1);")
+    emit_lists()
+    w("      }")
     # ---- Phase B: synaptic propagation, one pass per source group: the items
     # (delay slot, spike) of all its pathways form one list, so the dependent
     # loads (ring -> segment bounds -> synapses) of the pathways overlap
@@ -991,6 +1000,15 @@ def render_model(spec: dict) -> str:
             out.append("const b200_pathway_d& PD = I.p[pw];")
             return _indent("\n".join(out), ind)
 
+        def emit_wait(ind):
+            """Lag mode: wait for barrier A before the first atomic of the step."""
+            sp = " " * ind
+            w(sp + "if (pend) {")
+            w(sp + f"  B200_PHASE({5 + NP});")
+            w(sp + "  if (!b200_inst_wait(I, gen, limit_ns, cluster, rank, bar_old)) ok = false;")
+            w(sp + "  pend = false;")
+            w(sp + "  B200_PHASE(1);")
+            w(sp + "}")
         w(f"      // ---- pathways {', '.join(paths[q]['name'] for q in pis)}: propagation")
         w("      {")
         w(f"        const double* const _b200_S = s_Sp{pis[0]}; const float* const _b200_Sf = s_Sp{pis[0]}f; const long long* const _b200_Si = s_Sp{pis[0]}i;")
@@ -1009,7 +1027,9 @@ def render_model(spec: dict) -> str:
         w("          const int64_t s = ts - d;")
         w("          int n = 0, b = 0;")
         w("          if (s >= 0) {")
-        w("            if (d == 0) { b = pref[PD.tile_lo]; n = pref[PD.tile_hi] - b; }")
+        w("            if (d == 0) {  // (lag mode: only pathways without synapses have delay 0)")
+        w("              if (!lagm) { b = pref[PD.tile_lo]; n = pref[PD.tile_hi] - b; }")
+        w("            }")
         w("            else if (s_wr_ok[pw]) {  // this CTA's shared copy of the slot's bounds")
         w("              const int* wr = s_wr + (pw * B200_WR_SLOTS + (int)(s % SGD.R)) * 2;")
         w("              b = wr[0]; n = wr[1] - b;")
@@ -1091,13 +1111,13 @@ def render_model(spec: dict) -> str:
                 k = next(k for k, v in enumerate(p.get("vars", [])) if v["ptr"] == ptr)
                 return f"(({ct}*)I.p[{pi}].var[{k}])[_idx]"
 
-            w("          for (int e0 = threadIdx.x; e0 < E; e0 += B200_EVENT_BATCH * (int)blockDim.x) {")
+            w("          for (int b0 = 0; b0 < E; b0 += B200_EVENT_BATCH * (int)blockDim.x) {  // block-uniform")
             w("            int _q4[B200_EVENT_BATCH]; int32_t _pre4[B200_EVENT_BATCH]; int64_t _ix4[B200_EVENT_BATCH];")
             for li, ct in enumerate(sigs[0]):
                 w(f"            {ct} _ld{li}[B200_EVENT_BATCH];")
             w("#pragma unroll")
             w("            for (int qq = 0; qq < B200_EVENT_BATCH; ++qq) {")
-            w("              const int e = e0 + qq * (int)blockDim.x;")
+            w("              const int e = b0 + qq * (int)blockDim.x + (int)threadIdx.x;")
             w("              _q4[qq] = -1;")
             w("              if (e < E) {")
             w("                const int j = b200_upper_bound(s_item_off, nitems, e) - 1;")
@@ -1113,6 +1133,7 @@ def render_model(spec: dict) -> str:
                 w("                }")
             w("              }")
             w("            }")
+            emit_wait(12)
             w("#pragma unroll")
             w("            for (int qq = 0; qq < B200_EVENT_BATCH; ++qq) {")
             w("              if (_q4[qq] >= 0) {")
@@ -1144,6 +1165,7 @@ def render_model(spec: dict) -> str:
             w("          }")
             w("          } else {")
         if True:  # the one-phase loop (always emitted; the only one without a common load signature)
+            emit_wait(10)
             w("          for (int e0 = threadIdx.x; e0 < E; e0 += 4 * (int)blockDim.x) {")
             w("#pragma unroll")
             w("            for (int qq = 0; qq < 4; ++qq) {")
@@ -1182,6 +1204,15 @@ def render_model(spec: dict) -> str:
         w("        }")
         w("      }")
         w(f"      B200_PHASE({3 + pis[0]});")
+    w("      if (pend) {  // no events this step")
+    w("        if (!b200_inst_wait(I, gen, limit_ns, cluster, rank, bar_old)) ok = false;")
+    w("        pend = false;")
+    w("        B200_PHASE(1);")
+    w("      }")
+    w("      if (!ok) break;")
+    w("      if (lagm) {")
+    emit_lists()
+    w("      }")
     w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster, rank)) { ok = false; break; }")
     w(f"      B200_PHASE({3 + NP});")
     w("    }  // steps")

@@ -131,7 +131,8 @@ struct b200_inst_d {
   int32_t* pending_reset; // [B200_MAX_GROUPS] reset of the last step still to apply
   // owner mode (b200_owner_kernel): each CTA delivers into the neurons it owns
   int32_t owner;          // 1: this instance runs in owner mode
-  int32_t lag;            // 1: every delay >= 1 step, a step pushes the previous step's spikes
+  int32_t lag;            // 1: every delay >= 1 step (owner: a step pushes the previous step's spikes;
+                          // classic: deliveries are prepared while barrier A completes)
   int64_t ts_base;        // step whose arrival count starts at 0 in bar64
   unsigned long long* bar64;  // [1] arrivals of the split barrier
   int32_t tab_smem;       // 1: the batch tables are kept in shared memory for the launch
@@ -383,6 +384,59 @@ __device__ __forceinline__ bool b200_inst_barrier(const b200_inst_d& I, unsigned
   }
   __syncthreads();
   return ok != 0;
+}
+
+// The same barrier in two halves, so that a CTA can do work that does not
+// depend on the other CTAs between its arrival and its wait: b200_inst_arrive
+// (all threads; thread 0 keeps the arrival word's old value in `old`), then
+// b200_inst_wait (all threads), bounded like b200_inst_barrier.
+__device__ __forceinline__ void b200_inst_arrive(const b200_inst_d& I, int cluster, int rank, unsigned& old) {
+  if (cluster) {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+    return;
+  }
+  __syncthreads();
+  if (I.n_cta == 1) return;
+  if (threadIdx.x == 0) {
+    const unsigned nb = rank == 0 ? 0x80000000u - (unsigned)(I.n_cta - 1) : 1u;
+    __threadfence();
+    old = atomicAdd(&I.bar[0], nb);
+  }
+}
+
+__device__ __forceinline__ bool b200_inst_wait(const b200_inst_d& I, unsigned& gen, uint64_t limit_ns,
+                                               int cluster, int rank, unsigned old) {
+  if (cluster) {
+    asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+    return true;
+  }
+  if (I.n_cta == 1) {
+    __syncthreads();
+    return true;
+  }
+  __shared__ int ok_w;
+  if (threadIdx.x == 0) {
+    ok_w = 1;
+    const unsigned nb = rank == 0 ? 0x80000000u - (unsigned)(I.n_cta - 1) : 1u;
+    if (((old + nb) ^ old) & 0x80000000u) {
+      __threadfence();  // this CTA completed the barrier
+    } else {
+      const uint64_t t0 = b200_globaltimer();
+      int spins = 0;
+      while (((b200_ld_acquire(&I.bar[0]) ^ old) & 0x80000000u) == 0) {
+        if (++spins > 32) __nanosleep(32);
+        if ((spins & 255) == 0 &&
+            (b200_globaltimer() - t0 > limit_ns || *((volatile int32_t*)I.status) != 0)) {
+          atomicCAS(I.status, 0, B200_ERR_BARRIER_TIMEOUT);
+          ok_w = 0;
+          break;
+        }
+      }
+    }
+    ++gen;
+  }
+  __syncthreads();
+  return ok_w != 0;
 }
 
 // ---------------------------------------------------------------------------

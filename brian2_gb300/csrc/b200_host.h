@@ -850,11 +850,14 @@ static int b200_prepare(b200_net* n) {
       PD.S = (const double*)P.S.p;
       if (n->owner && (r = b200_owner_pathway(n, k, p, PD))) return r;
     }
+    // every pathway with synapses has delays >= 1 step: a step's deliveries do
+    // not read that step's spikes (owner mode pushes with a lag of one step,
+    // classic mode prepares its deliveries while its barrier completes)
+    D.lag = 1;
+    for (int p = 0; p < M->n_pathways; ++p)
+      if (I.p[p].n_syn > 0 && I.p[p].dmin == 0) D.lag = 0;
     if (n->owner) {
       D.owner = 1;
-      D.lag = 1;  // every pathway with synapses has delays >= 1 step
-      for (int p = 0; p < M->n_pathways; ++p)
-        if (I.p[p].n_syn > 0 && I.p[p].dmin == 0) D.lag = 0;
       if ((r = b200_alloc(n, I.bar64, 16))) return r;
       D.bar64 = (unsigned long long*)I.bar64.p;
     }
