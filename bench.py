@@ -313,6 +313,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--neurons", type=int, default=N_NEURONS)
+    ap.add_argument("--in-degree", type=int, default=K_IN,
+                    help="synapses per neuron and pathway group (smaller networks for profiling)")
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--ctas", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -346,7 +348,8 @@ def main():
     # overlap the other's work, and each thread keeps four events' loads in flight
     threads = args.threads or 256
     ctas = args.ctas or 304
-    net, _ = build_delays_scale(spec, N=N, K=K_IN, seed=seed, threads=threads, ctas_per_inst=ctas)
+    K = args.in_degree
+    net, _ = build_delays_scale(spec, N=N, K=K, seed=seed, threads=threads, ctas_per_inst=ctas)
     if args.chunk_steps:
         net.configure(threads=threads, ctas_per_inst=ctas, queue_mode=False, chunk_steps=args.chunk_steps,
                       use_graph=False)
@@ -391,7 +394,7 @@ def main():
     alg_bytes = 24.0 * N * STEPS_PER_BENCH_STEP + 8.0 * events / args.steps
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     peaks, peak_kind = measured_peaks()
-    tr_per_ns, tr_src = ncu_traffic_per_neuron_step()
+    tr_per_ns, tr_src = ncu_traffic_per_neuron_step() if K == K_IN else (None, None)  # captured at K_IN
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "peak_kind": peak_kind,
                 "traffic": (tr_per_ns * N * STEPS_PER_BENCH_STEP) if tr_per_ns else None,
@@ -432,7 +435,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": device_s / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: network constructed on the device from a seed",
-            "config": {"workload": WORKLOAD, "neurons": N, "in_degree": K_IN, "synapses": N * K_IN,
+            "config": {"workload": WORKLOAD if (N, K) == (N_NEURONS, K_IN) else f"cuba_delays_n{N}_k{K}_f32",
+                       "neurons": N, "in_degree": K, "synapses": N * K,
                        "delays_ms": [0.1, 5.0], "dt_ms": 0.1, "clock_steps_per_step": STEPS_PER_BENCH_STEP,
                        "l2": "inputs larger than L2 (synapse arrays 8 GB per GPU)",
                        "threads": threads, "ctas": ctas, "launch_plan": plan, "build_s": round(t_build, 2),

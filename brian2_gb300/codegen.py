@@ -515,6 +515,172 @@ def render_model(spec: dict) -> str:
         w("        __syncthreads();")
         w("      }")
 
+    QUADV = {"float": ("float4", 4), "int32_t": ("int4", 4), "char": ("char4", 1), "int8_t": ("char4", 1)}
+
+    def emit_quad(gi, g, bd, tab, hoist_sc):
+        """Update + threshold four neurons per thread with 16-byte (4-byte for
+        1-byte variables) loads and stores, when every variable the update and
+        threshold load or store is one of this group's 4- or 1-byte state
+        variables; the CTA takes this path when its state pointers are aligned
+        for it (s_quad), else the per-neuron path that follows.  Opens the
+        `if (s_quad) { ... } else {` that the caller closes.  Same order of
+        spikes (ascending) and the same arithmetic per neuron."""
+        upd_v = bd["update"]["vector"] if bd["update"] is not None else ""
+        thr_v = bd["threshold"]["vector"] if bd["threshold"] is not None else ""
+        upd_loads, upd_rest = split_loads(upd_v)
+        thr_loads, thr_rest = split_loads(thr_v)
+        upd_st = stored_ptrs(upd_v)
+        own = {v["ptr"]: v for v in g["vars"]}
+        pf = {}
+        for ct, nm, ptr in upd_loads + [x for x in thr_loads if x[2] not in upd_st]:
+            pf.setdefault(ptr, ct)
+        st_lines = {}
+        rest_lines = []
+        for ln in upd_rest.split("\n"):
+            m = re.match(r"^\s*(_ptr_array_\w+)\[_idx\]\s*=\s*([^=;][^;]*);\s*$", ln)
+            if m and m.group(1) in upd_st:
+                st_lines.setdefault(m.group(1), True)
+                rest_lines.append((m.group(1), m.group(2)))
+            else:
+                rest_lines.append((None, ln))
+        ptrs = set(pf) | set(upd_st)
+        if not ptrs or any(p_ not in own or own[p_]["ctype"] not in QUADV for p_ in ptrs):
+            return False
+        if "_idx]" in "\n".join(ln for p_, ln in rest_lines if p_ is None).replace("_idx] =", ""):
+            return False  # other indexed accesses in the update code
+        if bd["threshold"] is not None and re.search(r"_ptr_array_\w+\[", thr_rest):
+            return False
+        nbytes = sum(QUADV[own[p_]["ctype"]][1] for p_ in pf)  # bytes per neuron prefetched
+        pfq_big = max(1, min(8, PF_WORDS // max(nbytes, 1)))  # quads in flight per thread
+        pfi = {ptr: j for j, ptr in enumerate(sorted(pf))}
+        sti = {ptr: j for j, ptr in enumerate(sorted(upd_st))}
+        vt = lambda ptr: QUADV[own[ptr]["ctype"]][0]
+        w(f"        if (s_quad[{gi}]) {{  // four neurons per thread, 16-byte accesses")
+        w(f"          for (int u = s_ut[{gi}][0]; u < s_ut[{gi}][1]; ++u) {{")
+        w("            const int start = tst[u], end = tst[u + 1];")
+        w("            int cnt = 0;")
+        w("            const int q0 = start >> 2, q1 = (end + 3) >> 2;  // quads touching the tile")
+        w("            for (int qb = q0; qb < q1; qb += 8 * (int)blockDim.x) {")
+        w("              const int qe = (q1 - qb < 8 * (int)blockDim.x) ? q1 : qb + 8 * (int)blockDim.x;")
+        w("              const int E = (qe - qb + blockDim.x - 1) / blockDim.x;  // <= 8 slices of quads")
+        w(f"              constexpr int PFQ = (MAXT * MINB < 1024) ? {pfq_big} : 1;")
+        w("              unsigned flags = 0u;  // 4 bits per slice")
+        w("              for (int k0 = 0; k0 < E; k0 += PFQ) {")
+        for ptr, j in pfi.items():
+            w(f"                {vt(ptr)} _qf{j}[PFQ];")
+        w("#pragma unroll")
+        w("                for (int kq = 0; kq < PFQ; ++kq) {")
+        w("                  const int q = qb + (k0 + kq) * (int)blockDim.x + (int)threadIdx.x;")
+        w("                  if (k0 + kq < E && q < qe) {")
+        for ptr, j in pfi.items():
+            w(f"                    _qf{j}[kq] = *(const {vt(ptr)}*)({ptr} + 4 * (size_t)q);")
+        w("                  }")
+        w("                }")
+        w("#pragma unroll")
+        w("                for (int kq = 0; kq < PFQ; ++kq) {")
+        w("                  const int k = k0 + kq;")
+        w("                  const int q = qb + k * (int)blockDim.x + (int)threadIdx.x;")
+        w("                  if (k < E && q < qe) {")
+        for ptr, j in sti.items():
+            w(f"                    {vt(ptr)} _qs{j};")
+        w("#pragma unroll")
+        w("                    for (int e = 0; e < 4; ++e) {")
+        w("                      const int32_t _idx = 4 * q + e;")
+        w("                      if (_idx >= start && _idx < end) {")
+        w("                        const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+        if bd["update"] is not None:
+            w("                        {")
+            if not hoist_sc:
+                w(_indent(tab.scalar_loads("update", f32), 26))
+                w(_indent(_device(tab.time_code("update")), 26))
+            for ct, nm, ptr in upd_loads:
+                w(f"                          {ct} {nm} = (({ct}*)&_qf{pfi[ptr]}[kq])[e];")
+            for p_, ln in rest_lines:
+                if p_ is None:
+                    w(_indent(ln, 26) if ln.strip() else "")
+                else:
+                    ct = own[p_]["ctype"]
+                    w(f"                          (({ct}*)&_qs{sti[p_]})[e] = {ln};")
+            w("                        }")
+        if bd["threshold"] is not None:
+            w("                        {")
+            if not hoist_sc:
+                w(_indent(tab.scalar_loads("threshold", f32), 26))
+                w(_indent(_device(tab.time_code("threshold")), 26))
+            for ct, nm, ptr in thr_loads:
+                if ptr in upd_st:
+                    w(f"                          {ct} {nm} = (({own[ptr]['ctype']}*)&_qs{sti[ptr]})[e];")
+                else:
+                    w(f"                          {ct} {nm} = (({own[ptr]['ctype']}*)&_qf{pfi[ptr]}[kq])[e];")
+            w(_indent(thr_rest, 26))
+            w("                          if (_cond) flags |= 1u << (4 * k + e);")
+            if bd["threshold"].get("refractory"):
+                nr = next(v["ptr"] for v in g["vars"] if v["name"] == "not_refractory")
+                ls = next(v["ptr"] for v in g["vars"] if v["name"] == "lastspike")
+                # a variable the update stores is written back from its register
+                # copy after this loop: the refractory writes go to that copy
+                def ref_store(ptr, val):
+                    if ptr in sti:
+                        return f"(({own[ptr]['ctype']}*)&_qs{sti[ptr]})[e] = {val};"
+                    return f"{ptr}[_idx] = {val};"
+                w("                          if (_cond) {")
+                w("                            " + ref_store(nr, "false"))
+                w("                            " + ref_store(ls, "_b200_t"))
+                w("                          }")
+            w("                        }")
+        w("                      }")
+        w("                    }")
+        if sti:
+            w("                    if (4 * q >= start && 4 * q + 4 <= end) {")
+            for ptr, j in sti.items():
+                w(f"                      *({vt(ptr)}*)({ptr} + 4 * (size_t)q) = _qs{j};")
+            w("                    } else {")
+            w("#pragma unroll")
+            w("                      for (int e = 0; e < 4; ++e)")
+            w("                        if (4 * q + e >= start && 4 * q + e < end) {")
+            for ptr, j in sti.items():
+                ct = own[ptr]["ctype"]
+                w(f"                          {ptr}[4 * q + e] = (({ct}*)&_qs{j})[e];")
+            w("                        }")
+            w("                    }")
+        w("                  }")
+        w("                }")
+        w("              }")
+        w("              // order-preserving compaction: ascending = slice, warp, lane, element")
+        w("              for (int k = 0; k < E; ++k) {")
+        w("                int c = 0;")
+        w("#pragma unroll")
+        w("                for (int e = 0; e < 4; ++e) c += __popc(__ballot_sync(0xffffffffu, (flags >> (4 * k + e)) & 1u));")
+        w("                if (lane == 0) s_cnt[k * NW + wid] = c;")
+        w("              }")
+        w("              __syncthreads();")
+        w("              int tot;")
+        w("              const int x = (int)threadIdx.x < E * NW ? s_cnt[threadIdx.x] : 0;")
+        w("              const int ex = b200_block_exscan(x, s_wsum, &tot);")
+        w("              if ((int)threadIdx.x < E * NW) s_cnt[threadIdx.x] = ex;")
+        w("              __syncthreads();")
+        w("              const unsigned lt = b200_lanemask_lt();")
+        w("              for (int k = 0; k < E; ++k) {")
+        w("                int below = 0;  // set elements of the lower lanes")
+        w("#pragma unroll")
+        w("                for (int e = 0; e < 4; ++e) below += __popc(__ballot_sync(0xffffffffu, (flags >> (4 * k + e)) & 1u) & lt);")
+        w("                const unsigned mine = (flags >> (4 * k)) & 15u;")
+        w("                if (mine) {")
+        w("                  int p = start + cnt + s_cnt[k * NW + wid] + below;")
+        w("                  const int nb = 4 * (qb + k * (int)blockDim.x + (int)threadIdx.x);")
+        w("#pragma unroll")
+        w("                  for (int e = 0; e < 4; ++e)")
+        w("                    if ((mine >> e) & 1u) { scr[p] = nb + e; oscr[p] = nb + e; ++p; }")
+        w("                }")
+        w("              }")
+        w("              cnt += tot;")
+        w("              __syncthreads();")
+        w("            }")
+        w("            if (threadIdx.x == 0) { tcnt[u] = cnt; otc[u] = cnt; }")
+        w("          }")
+        w("        } else {")
+        return True
+
     def emit_phase_a(owner):
         """Reset of the previous step, state monitors, update + threshold with
         ordered compaction of this CTA's tiles."""
@@ -573,6 +739,7 @@ def render_model(spec: dict) -> str:
                     if bd[blk_name] is not None:
                         w(_indent(tab.scalar_loads(blk_name, f32), 8))
                         w(_indent(_device(tab.time_code(blk_name)), 8))
+            quad = (not owner) and emit_quad(gi, g, bd, tab, hoist_sc)
             w(f"        for (int u = s_ut[{gi}][0]; u < s_ut[{gi}][1]; ++u) {{")
             w("          const int start = tst[u], end = tst[u + 1];")
             w("          int cnt = 0;")
@@ -673,6 +840,8 @@ def render_model(spec: dict) -> str:
             w("          }")
             w("          if (threadIdx.x == 0) tcnt[u] = cnt;" if owner else "          if (threadIdx.x == 0) { tcnt[u] = cnt; otc[u] = cnt; }")
             w("        }")
+            if quad:
+                w("        }  // scalar path")
             w("      }")
 
     w("__device__ __forceinline__ int b200_upper_bound(const int* a, int n, int x) {")
@@ -724,6 +893,7 @@ def render_model(spec: dict) -> str:
     w("  __shared__ int s_glast[B200_NG], s_gen_lo, s_gen_hi;  // spike generator cursors")
     w("  (void)s_glast; (void)s_gen_lo; (void)s_gen_hi;")
     w("  __shared__ int s_pcache, s_pown[B200_NG][2];  // private-variable cache: on, own neuron range")
+    w("  __shared__ int s_quad[B200_NG];  // 1: the group's state pointers allow 4-neuron accesses")
     w(f"  __shared__ int s_wr[{max(NP, 1)} * B200_WR_SLOTS * 2];  // per pathway and ring slot: bounds of the slot's spikes")
     w(f"  __shared__ int s_wr_ok[{max(NP, 1)}];                   // 1: the ring fits B200_WR_SLOTS")
     w("  (void)s_pown;")
@@ -799,6 +969,16 @@ def render_model(spec: dict) -> str:
                   f"poff += ((size_t)(s_pown[{gi}][1] - s_pown[{gi}][0]) * {sz} + 15) & ~(size_t)15;")
         w("      }")
     w("    }")
+    # quad accesses need every state pointer aligned to 4 elements (shared
+    # memory copies are offset by the CTA's first neuron)
+    w("    if (threadIdx.x == 0) {")
+    for gi, g in enumerate(groups):
+        conds = []
+        for k, v in enumerate(g["vars"]):
+            if v["ctype"] in QUADV:
+                conds.append(f"(((uintptr_t)s_gv[{gi}][{k}]) % {4 * SIZE[v['ctype']]} == 0)")
+        w(f"      s_quad[{gi}] = {' && '.join(conds) if conds else '0'};")
+    w("    }")
     w("    __syncthreads();")
     if any(PRIV):
         w("    if (s_pcache) {")
@@ -870,6 +1050,22 @@ def render_model(spec: dict) -> str:
     w("      B200_PHASE(0);")
     w("      // test hook: CTA `fault_rank` leaves without arriving, the others must time out")
     w("      if (rank == fault_rank && ts == ts0) { ok = false; break; }")
+    def emit_preload(ind):
+        """Lag mode, right after barrier A: the step's tile counts, loaded now
+        so that their round trip overlaps the deliveries."""
+        sp = " " * ind
+        w(sp + "lc_ok = true;")
+        for gi in range(NG):
+            w(sp + "{")
+            w(sp + f"  const int nt = I.g[{gi}].n_tiles;")
+            w(sp + "  const int per = (nt + (int)blockDim.x - 1) / (int)blockDim.x;")
+            w(sp + "  const int u0r = threadIdx.x * per;")
+            w(sp + f"  const int32_t* const tcnt = s_tc[{gi}];")
+            w(sp + "  if (per > B200_LIST_RUN) lc_ok = false;")
+            w("#pragma unroll")
+            w(sp + f"  for (int r = 0; r < B200_LIST_RUN; ++r) _lc{gi}[r] = (r < per && u0r + r < nt) ? tcnt[u0r + r] : 0;")
+            w(sp + "}")
+
     # ---- Phase B: prefix of tile counts, ring, monitors
     def emit_lists():
         for gi, g in enumerate(groups):
@@ -890,7 +1086,8 @@ def render_model(spec: dict) -> str:
             w("          int sum = 0;")
             w("          if (per <= B200_LIST_RUN) {")
             w("#pragma unroll")
-            w("            for (int r = 0; r < B200_LIST_RUN; ++r) c[r] = (r < per && u0r + r < nt) ? tcnt[u0r + r] : 0;")
+            w(f"            for (int r = 0; r < B200_LIST_RUN; ++r) c[r] = lc_ok ? _lc{gi}[r] : "
+              "((r < per && u0r + r < nt) ? tcnt[u0r + r] : 0);")
             w("#pragma unroll")
             w("            for (int r = 0; r < B200_LIST_RUN; ++r) sum += c[r];")
             w("          } else {")
@@ -962,6 +1159,9 @@ def render_model(spec: dict) -> str:
         w("      B200_PHASE(2);")
     w("      unsigned bar_old = 0u;")
     w("      bool pend = false;  // lag mode: barrier A arrived, not yet waited for")
+    w("      bool lc_ok = false;  // lag mode: the tile counts were loaded right after the wait")
+    for gi in range(NG):
+        w(f"      int _lc{gi}[B200_LIST_RUN]; (void)_lc{gi};")
     w("      if (lagm) {")
     w("        b200_inst_arrive(I, cluster, rank, bar_old);")
     w("        pend = true;")
@@ -1007,6 +1207,7 @@ def render_model(spec: dict) -> str:
             w(sp + f"  B200_PHASE({5 + NP});")
             w(sp + "  if (!b200_inst_wait(I, gen, limit_ns, cluster, rank, bar_old)) ok = false;")
             w(sp + "  pend = false;")
+            emit_preload(ind + 2)
             w(sp + "  B200_PHASE(1);")
             w(sp + "}")
         w(f"      // ---- pathways {', '.join(paths[q]['name'] for q in pis)}: propagation")
@@ -1207,6 +1408,7 @@ def render_model(spec: dict) -> str:
     w("      if (pend) {  // no events this step")
     w("        if (!b200_inst_wait(I, gen, limit_ns, cluster, rank, bar_old)) ok = false;")
     w("        pend = false;")
+    emit_preload(8)
     w("        B200_PHASE(1);")
     w("      }")
     w("      if (!ok) break;")

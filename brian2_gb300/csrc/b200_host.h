@@ -202,7 +202,8 @@ int b200_create(b200_net** out, int32_t n_inst, const int32_t* group_sizes, doub
       }
       G.var.resize(M->groups[g].n_vars);
       for (int v = 0; v < M->groups[g].n_vars; ++v) {
-        int r = b200_alloc(n, G.var[v], (size_t)G.N * b200_kind_size(M->groups[g].var_kind[v]));
+        // rounded up to 16 bytes: the update reads and writes whole groups of four neurons
+        int r = b200_alloc(n, G.var[v], ((size_t)G.N * b200_kind_size(M->groups[g].var_kind[v]) + 15) & ~(size_t)15);
         if (r) {
           *out = n;
           return r;
@@ -529,7 +530,8 @@ static void b200_make_tiles(int32_t N, int n_cta, std::vector<int32_t> cuts,
                             std::vector<int32_t>& tile_start, std::vector<int32_t>& cta_tile) {
   cuts.push_back(0);
   cuts.push_back(N);
-  const int32_t target = std::max<int32_t>(1, (N + n_cta - 1) / n_cta);
+  // CTA ranges start at multiples of 4 neurons (16-byte aligned state accesses)
+  const int32_t target = std::max<int32_t>(4, (((N + n_cta - 1) / n_cta) + 3) & ~3);
   for (int32_t x = target; x < N; x += target) cuts.push_back(x);
   std::sort(cuts.begin(), cuts.end());
   cuts.erase(std::unique(cuts.begin(), cuts.end()), cuts.end());
