@@ -1162,9 +1162,9 @@ def render_model(spec: dict) -> str:
     w("      bool lc_ok = false;  // lag mode: the tile counts were loaded right after the wait")
     for gi in range(NG):
         w(f"      int _lc{gi}[B200_LIST_RUN]; (void)_lc{gi};")
+    w("      bool arrive_due = false;")
     w("      if (lagm) {")
-    w("        b200_inst_arrive(I, cluster, rank, bar_old);")
-    w("        pend = true;")
+    w("        arrive_due = true;  // arrive after the delivery windows (the arrival's fence overlaps the item loads)")
     w("      } else {")
     w("        if (!b200_inst_barrier(I, gen, limit_ns, cluster, rank)) { ok = false; break; }")
     w("        B200_PHASE(1);")
@@ -1256,6 +1256,7 @@ def render_model(spec: dict) -> str:
         w("          __syncthreads();")
         w("        }")
         w(f"        B200_PHASE({4 + NP});  // windows")
+        w("        if (arrive_due) { b200_inst_arrive(I, cluster, rank, bar_old); arrive_due = false; pend = true; }")
         w("        const int Wtot = s_ndoff[WT];")
         w("        const int i0 = (int)((int64_t)Wtot * rank / I.n_cta);")
         w("        const int i1 = (int)((int64_t)Wtot * (rank + 1) / I.n_cta);")
@@ -1405,6 +1406,7 @@ def render_model(spec: dict) -> str:
         w("        }")
         w("      }")
         w(f"      B200_PHASE({3 + pis[0]});")
+    w("      if (arrive_due) { b200_inst_arrive(I, cluster, rank, bar_old); arrive_due = false; pend = true; }")
     w("      if (pend) {  // no events this step")
     w("        if (!b200_inst_wait(I, gen, limit_ns, cluster, rank, bar_old)) ok = false;")
     w("        pend = false;")
