@@ -319,8 +319,8 @@ class B200Device(CPPStandaloneDevice):
                     g[key] = b
                 elif t == "synapses":
                     pw = obj
-                    if not isinstance(pw, SynapticPathway) or pw.prepost != "pre":
-                        raise NotImplementedError("b200: only on_pre pathways are supported")
+                    if not isinstance(pw, SynapticPathway) or pw.prepost not in ("pre", "post"):
+                        raise NotImplementedError("b200: unsupported synaptic pathway")
                     syn = pw.synapses
                     sgi, srange = group_of(pw.source)
                     tgi, trange = group_of(pw.target)
@@ -346,7 +346,7 @@ class B200Device(CPPStandaloneDevice):
                                          pre_ptr=gen_name(syn.variables["_synaptic_pre"]),
                                          post_ptr=gen_name(syn.variables["_synaptic_post"]),
                                          group_ptrs=gptrs, on_pre=block(frag),
-                                         _obj=pw, _src_range=srange, _tgt_range=trange))
+                                         _obj=pw, _src_range=srange, _tgt_range=trange, _syn=syn.name))
                 elif t == "synapses_push_spikes":
                     pass
                 elif t == "spikegenerator":
@@ -369,6 +369,24 @@ class B200Device(CPPStandaloneDevice):
                             raise NotImplementedError(f"b200: recording '{v}' (not a state variable)")
                     statemons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng,
                                           _vars=list(obj.record_variables)))
+        # pathways of one Synapses object (on_pre and on_post) share its synapses and
+        # synaptic variables: the first one in schedule order owns them, the others
+        # alias it; all carry the union of the variables their code uses
+        by_syn = {}
+        for pi, p in enumerate(pathways):
+            by_syn.setdefault(p["_syn"], []).append(pi)
+        for pis in by_syn.values():
+            if len(pis) < 2:
+                continue
+            union = {}
+            for pi in pis:
+                for v in pathways[pi]["vars"]:
+                    union.setdefault(v["name"], v)
+            allv = [union[k] for k in sorted(union)]
+            for pi in pis:
+                pathways[pi]["vars"] = [dict(v) for v in allv]
+            for pi in pis[1:]:
+                pathways[pi]["alias"] = pis[0]
         for g in groups:
             for k in ("update", "threshold", "reset"):
                 g.setdefault(k, None)
@@ -380,7 +398,7 @@ class B200Device(CPPStandaloneDevice):
                     state_monitors=statemons, clock_ptrs=clock_ptrs)
         return spec, b200_objects
 
-    PRIVATE_KEYS = {"_obj", "_range", "_src_range", "_tgt_range", "_vars"}
+    PRIVATE_KEYS = {"_obj", "_range", "_src_range", "_tgt_range", "_vars", "_syn"}
 
     @staticmethod
     def public_spec(spec):
@@ -451,9 +469,11 @@ class B200Device(CPPStandaloneDevice):
                 init[f"g{gi}_gen_last"] = np.int64(self._load(gv["_lastindex"])[0])
         for pi, p in enumerate(spec0["pathways"]):
             syn = p["_obj"].synapses
-            init[f"p{pi}_pre"] = (self._load(syn.variables["_synaptic_pre"]).astype(np.int64)
+            # the spiking side and the other side (for an on_post pathway: the
+            # postsynaptic and the presynaptic neurons)
+            init[f"p{pi}_pre"] = (self._load(p["_obj"].synapse_sources).astype(np.int64)
                                   - p["_src_range"][0]).astype(np.int32)
-            init[f"p{pi}_post"] = (self._load(syn.variables["_synaptic_post"]).astype(np.int64)
+            init[f"p{pi}_post"] = (self._load(p["_obj"].synapse_targets).astype(np.int64)
                                    - p["_tgt_range"][0]).astype(np.int32)
             dvar = p["_obj"].variables["delay"]
             d = self._load(dvar)
@@ -464,7 +484,7 @@ class B200Device(CPPStandaloneDevice):
                 init[f"p{pi}_delay_steps"] = (d / dt + 0.5).astype(np.int32)
             init[f"p{pi}_src_range"] = np.asarray(p["_src_range"], np.int64)
             init[f"p{pi}_tgt_range"] = np.asarray(p["_tgt_range"], np.int64)
-            for v in p["vars"]:
+            for v in p["vars"] if p.get("alias", -1) < 0 else []:  # (an alias shares its owner's)
                 init[f"p{pi}_{v['name']}"] = self._load(syn.variables[v["name"]])
         for mi, m in enumerate(spec0["spike_monitors"]):
             init[f"sm{mi}_range"] = np.asarray(m["_range"], np.int64)
@@ -499,7 +519,7 @@ class B200Device(CPPStandaloneDevice):
                 self._store(g["_obj"].variables["_lastindex"], np.array([int(out[f"g{gi}_gen_last"])]))
         for pi, p in enumerate(spec0["pathways"]):
             syn = p["_obj"].synapses
-            for v in p["vars"]:
+            for v in p["vars"] if p.get("alias", -1) < 0 else []:
                 self._store(syn.variables[v["name"]], out[f"p{pi}_{v['name']}"])
         for mi, m in enumerate(spec0["spike_monitors"]):
             i, ts, cnt = out[f"sm{mi}_i"], out[f"sm{mi}_ts"], out[f"sm{mi}_count"]

@@ -318,7 +318,7 @@ def render_model(spec: dict) -> str:
         target neuron, values computed from synaptic variables and constants.
         Returns, per pathway, the synaptic variables an event carries (indices
         into the pathway's variables), or None for the whole model."""
-        if not paths:
+        if not paths or any(p.get("alias", -1) >= 0 for p in paths):
             return None
         for g in groups:
             for blk in ("update", "threshold", "reset"):
@@ -378,7 +378,7 @@ def render_model(spec: dict) -> str:
     if paths:
         w("static const b200_pathway_info b200_pathways[] = {" + ", ".join(
             f'{{"{p["name"]}", {p["src"]}, {p["tgt"]}, {len(p.get("vars", []))}, b200_p{pi}_vars, b200_p{pi}_kinds, '
-            f'{ptables[pi][0].size}, {len(PAYLOAD[pi]) if OWNER else 0}, b200_p{pi}_payload}}'
+            f'{ptables[pi][0].size}, {len(PAYLOAD[pi]) if OWNER else 0}, b200_p{pi}_payload, {p.get("alias", -1)}}}'
             for pi, p in enumerate(paths)) + "};")
     else:
         w("static const b200_pathway_info* const b200_pathways = nullptr;")
@@ -1178,15 +1178,32 @@ def render_model(spec: dict) -> str:
     # any of them reads, so the reference's pathway-by-pathway order is kept
     merged = []
     for pi, p in enumerate(paths):
-        touched = set(p.get("group_ptrs", {}))
+        # neuron variables and synaptic variables (shared by the pathways of one
+        # Synapses object): pathways touching the same ones are not interleaved
+        touched = set(p.get("group_ptrs", {})) | {v["ptr"] for v in p.get("vars", [])}
         last = merged[-1] if merged else None
         if last and last[0] == p["src"] and not (last[2] & touched):
             last[1].append(pi)
             last[2].update(touched)
         else:
             merged.append((p["src"], [pi], set(touched)))
+    seen_svars = set()
     for sg, pis, _ in merged:
         L = len(pis)
+        svars = {v["ptr"] for q in pis for v in paths[q].get("vars", [])}
+        if svars & seen_svars:
+            # synaptic variables shared with an earlier pathway of this step (the
+            # on_pre and on_post pathways of one Synapses object): all of the
+            # earlier pathway's events come first, as in the reference's schedule
+            w("      if (arrive_due) { b200_inst_arrive(I, cluster, rank, bar_old); arrive_due = false; pend = true; }")
+            w("      if (pend) {")
+            w("        if (!b200_inst_wait(I, gen, limit_ns, cluster, rank, bar_old)) ok = false;")
+            w("        pend = false;")
+            emit_preload(8)
+            w("      }")
+            w("      if (!ok) break;")
+            w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster, rank)) { ok = false; break; }")
+        seen_svars |= svars
 
         def which(kexpr, ind):
             """q (index into pis) and the local window index kk of item window k."""
@@ -1306,10 +1323,11 @@ def render_model(spec: dict) -> str:
 
             def load_expr(pi, ptr, ct):
                 p = paths[pi]
+                own = p.get("alias", -1) if p.get("alias", -1) >= 0 else pi  # shared synapses: the owner's arrays
                 if ptr == p["post_ptr"]:
-                    return f"I.p[{pi}].post[_idx]"
+                    return f"I.p[{own}].post[_idx]"
                 if ptr == p["pre_ptr"]:
-                    return f"I.p[{pi}].pre[_idx]"
+                    return f"I.p[{own}].pre[_idx]"
                 k = next(k for k, v in enumerate(p.get("vars", [])) if v["ptr"] == ptr)
                 return f"(({ct}*)I.p[{pi}].var[{k}])[_idx]"
 
@@ -1330,6 +1348,8 @@ def render_model(spec: dict) -> str:
                 lds, _ = split_loads(dict(ptables[pi][1])["on_pre"]["vector_device"] or
                                      dict(ptables[pi][1])["on_pre"]["vector"])
                 w(("                if" if q == 0 else "                else if") + f" (q == {q}) {{")
+                if paths[pi].get("alias", -1) >= 0:  # the synapse's position in the owning pathway
+                    w(f"                  const int64_t _idx = I.p[{pi}].sidx[_ix4[qq]]; _ix4[qq] = _idx;")
                 for li, (ct, nm, ptr) in enumerate(lds):
                     w(f"                  _ld{li}[qq] = {load_expr(pi, ptr, ct)};")
                 w("                }")
@@ -1356,11 +1376,16 @@ def render_model(spec: dict) -> str:
                     w(f"                  {v['ctype']}* __restrict__ const {ptr} = ({v['ctype']}*)s_gv[{gidx}][{vidx}]; (void){ptr};")
                 for k, v in enumerate(p.get("vars", [])):
                     w(f"                  {v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)PQ.var[{k}]; (void){v['ptr']};")
+                own = p.get("alias", -1) if p.get("alias", -1) >= 0 else pi
+                w(f"                  const int32_t* __restrict__ const {p['post_ptr']} = I.p[{own}].post; (void){p['post_ptr']};")
+                w(f"                  const int32_t* __restrict__ const {p['pre_ptr']} = I.p[{own}].pre; (void){p['pre_ptr']};")
                 w(_indent(tab.scalar_loads("on_pre", f32), 18))
                 w(_indent(_device(tab.time_code("on_pre")), 18))
+                w("                  {  // (Brian's vector code may redeclare the clock's names)")
                 for li, (ct, nm, ptr) in enumerate(lds):
                     w(f"                  {ct} {nm} = _ld{li}[qq];")
                 w(_indent(rest, 18))
+                w("                  }")
                 w("                }")
             w("              }")
             w("            }")
@@ -1387,14 +1412,22 @@ def render_model(spec: dict) -> str:
                 w(f"                  const double* const _b200_S = s_Sp{pi}; const float* const _b200_Sf = s_Sp{pi}f; const long long* const _b200_Si = s_Sp{pi}i;")
                 for k, v in enumerate(p.get("vars", [])):
                     w(f"                  {v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)PQ.var[{k}]; (void){v['ptr']};")
-                w(f"                  const int32_t* __restrict__ const {p['post_ptr']} = PQ.post; (void){p['post_ptr']};")
-                w(f"                  const int32_t* __restrict__ const {p['pre_ptr']} = PQ.pre; (void){p['pre_ptr']};")
+                own = p.get("alias", -1) if p.get("alias", -1) >= 0 else pi
+                w(f"                  const int32_t* __restrict__ const {p['post_ptr']} = I.p[{own}].post; (void){p['post_ptr']};")
+                w(f"                  const int32_t* __restrict__ const {p['pre_ptr']} = I.p[{own}].pre; (void){p['pre_ptr']};")
                 for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
                     v = groups[gidx]["vars"][vidx]
                     w(f"                  {v['ctype']}* __restrict__ const {ptr} = ({v['ctype']}*)s_gv[{gidx}][{vidx}]; (void){ptr};")
                 w(_indent(tab.scalar_loads("on_pre", f32), 18))
                 w(_indent(_device(tab.time_code("on_pre")), 18))
+                if own != pi:  # the synapse's position in the owning pathway
+                    w("                  const int64_t _idx_csr = _idx;")
+                w("                  {  // (Brian's vector code may redeclare the clock's names)")
+                if own != pi:
+                    w(f"                  const int64_t _idx = I.p[{pi}].sidx[_idx_csr];")
+                    w("                  const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
                 w(_indent(blk["vector_device"] if blk.get("vector_device") else blk["vector"], 18))
+                w("                  }")
                 w("                }")
             w("              }")
             w("            }")

@@ -86,6 +86,8 @@ struct b200_pathway_d {
   const int32_t* pre;     // [n_syn] source neuron (within source group), CSR order
   void* var[B200_MAX_VARS];  // synaptic variables in CSR order (owner mode: owner order)
   const double* S;        // scalar table of on_pre
+  const int64_t* sidx;    // shared synapses: [n_syn] the synapse's position in the owning
+                          // pathway's order (post/pre/var then point to that pathway's arrays)
   // owner mode: segptr is over (source, owning CTA) with n_cta entries per
   // source, post/var are in that order, odelay is each synapse's delay slot
   const uint16_t* odelay;
@@ -185,6 +187,9 @@ struct b200_pathway_info {
   // owner mode: the synaptic variables on_pre reads (carried by each event)
   int n_payload;
   const int* payload_var;
+  // >= 0: this pathway (the on_post pathway of a Synapses object) shares the
+  // synapses and synaptic variables of that pathway (its on_pre pathway)
+  int alias;
 };
 struct b200_mon_info {
   const char* name;

@@ -45,6 +45,7 @@ struct b200_pathway_h {
   bool has_syn = false;
   std::vector<int64_t> perm;  // perm[csr position] = synapse index (creation order)
   b200_dbuf segptr, post, pre, S;
+  b200_dbuf sidx;             // shared synapses: position of each entry in the owning pathway
   std::vector<b200_dbuf> var;
   // owner mode: synapses over (source, owning CTA), the payload variables in
   // that order, and the per-CTA event FIFOs
@@ -308,6 +309,7 @@ static int b200_var_buf(b200_net* n, int32_t inst, int32_t kind, int32_t obj, in
   } else if (kind == 1) {
     if (obj < 0 || obj >= n->M->n_pathways || var < 0 || var >= n->M->pathways[obj].n_vars)
       return b200_fail(n, B200_ERR_ARG, "bad synaptic variable %d/%d", obj, var);
+    if (n->M->pathways[obj].alias >= 0) obj = n->M->pathways[obj].alias;  // shared synaptic variables
     if (!I.p[obj].has_syn) return b200_fail(n, B200_ERR_ARG, "synapses of pathway %d not set", obj);
     *buf = &I.p[obj].var[var];
     *vkind = n->M->pathways[obj].var_kind[var];
@@ -325,6 +327,7 @@ int b200_upload(b200_net* n, int32_t inst, int32_t kind, int32_t obj, int32_t va
   int64_t cnt;
   int r = b200_var_buf(n, inst, kind, obj, var, &b, &vk, &cnt);
   if (r) return r;
+  if (kind == 1 && n->M->pathways[obj].alias >= 0) obj = n->M->pathways[obj].alias;
   if (count != cnt) return b200_fail(n, B200_ERR_ARG, "upload size %lld != %lld", (long long)count, (long long)cnt);
   const size_t es = b200_kind_size(vk);
   if (kind == 0) {
@@ -350,6 +353,7 @@ int b200_download(b200_net* n, int32_t inst, int32_t kind, int32_t obj, int32_t 
   int64_t cnt;
   int r = b200_var_buf(n, inst, kind, obj, var, &b, &vk, &cnt);
   if (r) return r;
+  if (kind == 1 && n->M->pathways[obj].alias >= 0) obj = n->M->pathways[obj].alias;
   if (count != cnt) return b200_fail(n, B200_ERR_ARG, "download size mismatch");
   const size_t es = b200_kind_size(vk);
   if (kind == 0) {
@@ -419,10 +423,23 @@ int b200_set_synapses(b200_net* n, int32_t inst, int32_t pw, int32_t src_lo, int
     cpost[pos] = post[k] + tgt_lo;  // stored as index within the target group
     cpre[pos] = s + src_lo;         // index within the source group
   }
+  int r;
+  if (PI.alias >= 0) {
+    // the on_post pathway of a Synapses object: the same synapses (creation
+    // order) as its on_pre pathway, whose arrays hold the synaptic variables
+    const b200_pathway_h& O = I.p[PI.alias];
+    if (!O.has_syn || O.n_syn != n_syn)
+      return b200_fail(n, B200_ERR_ARG, "pathway %s shares the synapses of %s: set those first (same synapses)",
+                       PI.name, n->M->pathways[PI.alias].name);
+    std::vector<int64_t> inv((size_t)n_syn), sx((size_t)n_syn);
+    for (int64_t q = 0; q < n_syn; ++q) inv[(size_t)O.perm[q]] = q;
+    for (int64_t q = 0; q < n_syn; ++q) sx[q] = inv[(size_t)P.perm[q]];
+    if ((r = b200_alloc(n, P.sidx, (size_t)std::max<int64_t>(n_syn, 1) * 8, false))) return r;
+    if (n_syn) B200_CU(n, cudaMemcpyAsync(P.sidx.p, sx.data(), (size_t)n_syn * 8, cudaMemcpyHostToDevice, n->stream));
+  }
   P.src_lo = src_lo; P.src_hi = src_hi; P.tgt_lo = tgt_lo; P.tgt_hi = tgt_hi;
   P.dmin = dmin; P.dmax = dmax; P.n_syn = n_syn; P.has_syn = true;
   P.own_stale = true;
-  int r;
   if ((r = b200_alloc(n, P.segptr, seg.size() * 8, false))) return r;
   if ((r = b200_alloc(n, P.post, (size_t)n_syn * 4, false))) return r;
   if ((r = b200_alloc(n, P.pre, (size_t)n_syn * 4, false))) return r;
@@ -431,8 +448,9 @@ int b200_set_synapses(b200_net* n, int32_t inst, int32_t pw, int32_t src_lo, int
     B200_CU(n, cudaMemcpyAsync(P.post.p, cpost.data(), (size_t)n_syn * 4, cudaMemcpyHostToDevice, n->stream));
     B200_CU(n, cudaMemcpyAsync(P.pre.p, cpre.data(), (size_t)n_syn * 4, cudaMemcpyHostToDevice, n->stream));
   }
-  for (int v = 0; v < PI.n_vars; ++v)
-    if ((r = b200_alloc(n, P.var[v], (size_t)n_syn * b200_kind_size(PI.var_kind[v])))) return r;
+  if (PI.alias < 0)
+    for (int v = 0; v < PI.n_vars; ++v)
+      if ((r = b200_alloc(n, P.var[v], (size_t)n_syn * b200_kind_size(PI.var_kind[v])))) return r;
   B200_CU(n, cudaStreamSynchronize(n->stream));
   n->prepared = false;
   return 0;
@@ -449,6 +467,7 @@ int b200_set_synapses_csr(b200_net* n, int32_t inst, int32_t pw, int32_t src_lo,
   b200_inst_h& I = n->inst[inst];
   const b200_pathway_info& PI = n->M->pathways[pw];
   b200_pathway_h& P = I.p[pw];
+  if (PI.alias >= 0) return b200_fail(n, B200_ERR_ARG, "pathway %s shares synapses: set them with b200_set_synapses", PI.name);
   if (dmin < 0 || dmax < dmin) return b200_fail(n, B200_ERR_ARG, "bad delay range");
   const int64_t nseg = (int64_t)(src_hi - src_lo) * (dmax - dmin + 1) + 1;
   int r;
@@ -477,6 +496,7 @@ int b200_synapse_var_ptr(b200_net* n, int32_t inst, int32_t pw, int32_t var, voi
   int64_t cnt;
   int r = b200_var_buf(n, inst, 1, pw, var, &b, &vk, &cnt);
   if (r) return r;
+  if (n->M->pathways[pw].alias >= 0) pw = n->M->pathways[pw].alias;
   *out = b->p;
   n->inst[inst].p[pw].own_stale = true;  // the caller may write it: owner copies are rebuilt
   n->prepared = false;
@@ -843,7 +863,14 @@ static int b200_prepare(b200_net* n) {
       PD.segptr = (const int64_t*)P.segptr.p;
       PD.post = (const int32_t*)P.post.p;
       PD.pre = (const int32_t*)P.pre.p;
-      for (int v = 0; v < PI.n_vars; ++v) PD.var[v] = P.var[v].p;
+      if (PI.alias >= 0) {  // the shared synapses' variables, pre and post arrays are the owner's
+        const b200_pathway_h& O = I.p[PI.alias];
+        for (int v = 0; v < PI.n_vars; ++v) PD.var[v] = O.var[v].p;
+        PD.sidx = (const int64_t*)P.sidx.p;
+      } else {
+        for (int v = 0; v < PI.n_vars; ++v) PD.var[v] = P.var[v].p;
+        PD.sidx = nullptr;
+      }
       std::vector<double> S(std::max(PI.n_scalars, 1));
       M->eval_scalars(1, p, I.consts.data(), n->dt, S.data());
       if ((r = b200_alloc(n, P.S, S.size() * 8, false))) return r;

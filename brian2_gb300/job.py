@@ -76,7 +76,7 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None)
         net.set_synapses(0, pi, init[f"p{pi}_pre"], init[f"p{pi}_post"], steps, int(init[f"p{pi}_scalar_delay"]),
                          tuple(int(x) for x in init[f"p{pi}_src_range"]),
                          tuple(int(x) for x in init[f"p{pi}_tgt_range"]))
-        for v in p.get("vars", []):
+        for v in p.get("vars", []) if p.get("alias", -1) < 0 else []:  # (an alias shares its owner's)
             net.upload_synapse_var(0, pi, v["name"], init[f"p{pi}_{v['name']}"])
     for mi in range(len(spec.get("spike_monitors", []))):
         net.set_spikemon_range(0, mi, *(int(x) for x in init[f"sm{mi}_range"]))
@@ -99,7 +99,7 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None)
         if g.get("generator"):
             out[f"g{gi}_gen_last"] = np.int64(net.generator_cursor(0, gi))
     for pi, p in enumerate(spec.get("pathways", [])):
-        for v in p.get("vars", []):
+        for v in p.get("vars", []) if p.get("alias", -1) < 0 else []:
             out[f"p{pi}_{v['name']}"] = net.download_synapse_var(0, pi, v["name"])
     for mi in range(len(spec.get("spike_monitors", []))):
         i, ts, cnt = net.spikes(0, mi)

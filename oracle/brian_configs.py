@@ -277,6 +277,49 @@ def spike_generator(N_in=100, N=300, duration_ms=130.0, period_ms=40.0, seed_val
     return dict(P=P, G=G, Sin=Sin, S=S, spikes=s_mon, rate=r_mon, gen_spikes=g_mon)
 
 
+def stdp(N_in=200, N=50, duration_ms=300.0, rate_hz=15.0, seed_value=71):
+    """Event-driven STDP (pair-based traces, additive, clipped) from a spike
+    generator onto a small LIF population.  The on_pre and on_post pathways of
+    the Synapses object share the weight, the traces and their last-update
+    time; the on_pre pathway has random delays (0-2 ms), on_post none."""
+    import numpy as np
+    from brian2 import (NeuronGroup, Synapses, SpikeGeneratorGroup, SpikeMonitor, PopulationRateMonitor,
+                        ms, mV, seed, run)
+    seed(seed_value)
+    rng = np.random.default_rng(seed_value)
+    n_bins = int(round(duration_ms / 0.1))
+    idx, times = [], []
+    for k in range(N_in):  # independent Bernoulli trains at rate_hz, one spike per bin at most
+        bins = np.nonzero(rng.random(n_bins) < rate_hz * 1e-4)[0]
+        idx.extend([k] * len(bins))
+        times.extend(list(bins * 0.1 + 0.05))
+    order = np.argsort(times, kind="stable")
+    G = SpikeGeneratorGroup(N_in, np.array(idx)[order], np.array(times)[order] * ms)
+    ns = dict(taum=10 * ms, taue=5 * ms, Vt=-54 * mV, Vr=-60 * mV, El=-65 * mV, drive=15 * mV,
+              taupre=20 * ms, taupost=20 * ms, wmax=1.0, dApre=0.01, dApost=-0.0105)
+    P = NeuronGroup(N, '''dv/dt = (El - v + ge * drive)/taum : volt
+                          dge/dt = -ge/taue : 1''',
+                    threshold='v>Vt', reset='v = Vr', method='exact', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    S = Synapses(G, P, '''w : 1
+                          dApre/dt = -Apre/taupre : 1 (event-driven)
+                          dApost/dt = -Apost/taupost : 1 (event-driven)''',
+                 on_pre='''ge_post += w
+                           Apre += dApre
+                           w = clip(w + Apost, 0, wmax)''',
+                 on_post='''Apost += dApost
+                            w = clip(w + Apre, 0, wmax)''', namespace=ns)
+    S.connect(p=0.3)
+    S.w = 'rand() * 0.5'
+    S.delay = 'rand() * 2*ms'
+    # monitors must be locals of the frame that calls run() (Brian collects them there)
+    s_mon = SpikeMonitor(P)
+    r_mon = PopulationRateMonitor(P)
+    g_mon = SpikeMonitor(G)
+    run(duration_ms * ms)
+    return dict(P=P, G=G, S=S, spikes=s_mon, rate=r_mon, gen_spikes=g_mon, syn_vars=("w", "Apre", "Apost"))
+
+
 SCENARIOS = {
     "lif_refractory": lif_refractory,
     "hetero_delays": hetero_delays,
@@ -284,4 +327,5 @@ SCENARIOS = {
     "input_group": input_group,
     "presynaptic_read": presynaptic_read,
     "spike_generator": spike_generator,
+    "stdp": stdp,
 }

@@ -287,10 +287,13 @@ def render_oracle(spec: dict) -> str:
         w(f"        const std::vector<int32_t>& syn = n->p{pi}_syn[sp[s] - n->p{pi}_src_lo];")
         w(f"        for (int32_t k : syn) Q[(off + n->p{pi}_delay[k]) % Q.size()].push_back(k);")
         w("      }")
-        w(f"      int32_t* const {p['pre_ptr']} = n->p{pi}_pre.data(); (void){p['pre_ptr']};")
-        w(f"      int32_t* const {p['post_ptr']} = n->p{pi}_post.data(); (void){p['post_ptr']};")
+        # the on_post pathway of a Synapses object shares the synapses (creation
+        # order) and the synaptic variables of its on_pre pathway
+        own = p.get("alias", -1) if p.get("alias", -1) >= 0 else pi
+        w(f"      int32_t* const {p['pre_ptr']} = n->p{own}_pre.data(); (void){p['pre_ptr']};")
+        w(f"      int32_t* const {p['post_ptr']} = n->p{own}_post.data(); (void){p['post_ptr']};")
         for v in p.get("vars", []):
-            w(f"      {v['ctype']}* const {v['ptr']} = n->p{pi}_{v['name']}.data(); (void){v['ptr']};")
+            w(f"      {v['ctype']}* const {v['ptr']} = n->p{own}_{v['name']}.data(); (void){v['ptr']};")
         for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
             v = groups[gidx]["vars"][vidx]
             w(f"      {v['ctype']}* const {ptr} = n->g{gidx}_{v['name']}.data(); (void){ptr};")
@@ -427,6 +430,8 @@ class OracleNet:
     def _pv(self, pathway, var):
         ps = self.spec["pathways"]
         p = pathway if isinstance(pathway, int) else [x["name"] for x in ps].index(pathway)
+        if ps[p].get("alias", -1) >= 0:
+            p = ps[p]["alias"]  # shared synaptic variables
         names = [v["name"] for v in ps[p].get("vars", [])]
         v = var if isinstance(var, int) else names.index(var)
         return p, v, _CT_NP[ps[p]["vars"][v]["ctype"]]
@@ -561,7 +566,7 @@ def run_job_on_oracle(directory):
         steps = init.get(f"p{pi}_delay_steps")
         o.set_synapses(pi, init[f"p{pi}_pre"], init[f"p{pi}_post"], steps, int(init[f"p{pi}_scalar_delay"]),
                        tuple(int(x) for x in init[f"p{pi}_src_range"]), tuple(int(x) for x in init[f"p{pi}_tgt_range"]))
-        for v in p.get("vars", []):
+        for v in p.get("vars", []) if p.get("alias", -1) < 0 else []:
             o.upload_synapse_var(pi, v["name"], init[f"p{pi}_{v['name']}"])
     for mi in range(len(spec.get("spike_monitors", []))):
         o.set_spikemon_range(mi, *(int(x) for x in init[f"sm{mi}_range"]))
@@ -579,7 +584,7 @@ def run_job_on_oracle(directory):
         if g.get("generator"):
             out[f"g{gi}_gen_last"] = np.int64(o.generator_cursor(gi))
     for pi, p in enumerate(spec.get("pathways", [])):
-        for v in p.get("vars", []):
+        for v in p.get("vars", []) if p.get("alias", -1) < 0 else []:
             out[f"p{pi}_{v['name']}"] = o.download_synapse_var(pi, v["name"])
     for mi in range(len(spec.get("spike_monitors", []))):
         out[f"sm{mi}_i"], out[f"sm{mi}_ts"], out[f"sm{mi}_count"] = o.spikes(mi)

@@ -8,7 +8,8 @@ per process):
   flags, float64) -> ``tests/golden/scenarios/<name>.npz``: the spike monitor's
   indices and time steps, the rate monitor's per-step counts, the state
   monitor's trace, the final state of the monitored group (and, for a spike
-  generator, its raster and final cursor);
+  generator, its raster and final cursor; for plastic synapses, their final
+  synaptic variables);
 * with the ``b200`` plugin in deferred mode -> ``tests/golden/jobs/<name>/``:
   the job the plugin writes from the script (spec, initial state, synapses).
 
@@ -70,6 +71,11 @@ def run_ref(name):
         from brian2 import device             # the results file (get_value returns the cached initial 0)
         fn = os.path.join(device.results_dir, device.get_array_filename(r["G"].variables["_lastindex"]))
         meta["gen_lastindex"] = int(np.fromfile(fn, dtype=np.int32)[0])
+    if "syn_vars" in r:                        # synaptic variables (creation order)
+        for var in r["syn_vars"]:
+            out["syn_" + var] = np.asarray(getattr(r["S"], var + "_")[:]).copy()
+        meta["synapses"] = r["S"].name
+        meta["syn_vars"] = list(r["syn_vars"])
     np.savez_compressed(os.path.join(HERE, "scenarios", name + ".npz"), **out)
     with open(os.path.join(HERE, "scenarios", name + ".json"), "w") as f:
         json.dump(meta, f, indent=1)

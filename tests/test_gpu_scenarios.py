@@ -5,9 +5,10 @@ same script (tests/golden/make_scenarios.py).
 
 Bit-exact where every per-target increment of a pathway is equal (timed
 refractoriness, subgroup monitors and a state monitor, a separate input
-group); where increments differ (random weights, a presynaptic factor) the
-order of the float64 sums into a target differs from the reference's queue
-order, so the raster must match and the state agree to 1e-12 relative."""
+group, a spike generator); where increments differ (random weights, a
+presynaptic factor, plastic weights) the order of the float64 sums into a
+target differs from the reference's queue order, so the raster must match and
+the state (and the plastic synapses' variables) agree to 1e-12 relative."""
 import json
 import os
 
@@ -19,7 +20,7 @@ from brian2_gb300.job import load_job, run_job
 pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 EXACT = {"lif_refractory": True, "hetero_delays": False, "subgroup_monitors": True, "input_group": True,
-         "presynaptic_read": False, "spike_generator": True}
+         "presynaptic_read": False, "spike_generator": True, "stdp": False}
 
 
 @pytest.mark.parametrize("name", sorted(EXACT))
@@ -54,3 +55,7 @@ def test_scenario_matches_reference(name, ctas, owner):
     if "state_v" in ref:
         tr = out["stm0_trace"][:, 0, :].T            # [n_rec, steps]
         np.testing.assert_array_equal(tr, ref["state_v"])
+    for var in meta.get("syn_vars", []):           # plastic synapses (on_pre and on_post share them)
+        pi = next(k for k, p in enumerate(spec["pathways"])
+                  if p["name"].startswith(meta["synapses"] + "_") and p.get("alias", -1) < 0)
+        np.testing.assert_allclose(out[f"p{pi}_{var}"], ref["syn_" + var], rtol=1e-12, atol=1e-15, err_msg=var)

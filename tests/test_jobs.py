@@ -34,7 +34,7 @@ def test_job_carries_the_reference_network(case, golden):
 
 
 SCENARIOS = ["lif_refractory", "hetero_delays", "subgroup_monitors", "input_group", "presynaptic_read",
-             "spike_generator"]
+             "spike_generator", "stdp"]
 
 
 @pytest.mark.parametrize("name", SCENARIOS)
@@ -51,6 +51,13 @@ def test_scenario_jobs_describe_their_features(name):
         assert list(init["stm0_idx"]) == [0, 10, 250, 499]
     if name == "input_group":
         assert len(spec["groups"]) == 2 and {p["src"] for p in spec["pathways"]} == {0, 1}
+    if name == "stdp":  # on_pre and on_post pathways of one Synapses object share its variables
+        pre, post = spec["pathways"]
+        assert post.get("alias") == 0 and pre.get("alias", -1) == -1
+        assert [v["name"] for v in pre["vars"]] == [v["name"] for v in post["vars"]] == ["Apost", "Apre", "lastupdate", "w"]
+        assert (pre["src"], pre["tgt"]) == (post["tgt"], post["src"])
+        assert "p1_w" not in init and init["p0_pre"].size == init["p1_pre"].size
+        assert int(init["p1_delay_steps"].max()) == 0 and int(init["p0_delay_steps"].max()) > 0
     if name == "spike_generator":
         gi = next(k for k, g in enumerate(spec["groups"]) if g.get("generator"))
         bins = init[f"g{gi}_gen_bins"]

@@ -43,3 +43,7 @@ def test_oracle_reproduces_reference_scenario(name):
             np.testing.assert_array_equal(out[f"g{gi}_{var}"], ref[var], err_msg=var)
     if "state_v" in ref:
         np.testing.assert_array_equal(out["stm0_trace"][:, 0, :].T, ref["state_v"])
+    for var in meta.get("syn_vars", []):        # plastic synapses: final synaptic variables
+        pi = next(k for k, p in enumerate(spec["pathways"])
+                  if p["name"].startswith(meta["synapses"] + "_") and p.get("alias", -1) < 0)
+        np.testing.assert_array_equal(out[f"p{pi}_{var}"], ref["syn_" + var], err_msg=var)
