@@ -56,7 +56,7 @@ from brian2.utils.stringtools import get_identifiers, stripped_deindented_lines
 logger = get_logger(__name__)
 
 STEP_TEMPLATES = {"stateupdate", "threshold", "reset", "synapses", "synapses_push_spikes",
-                  "spikemonitor", "ratemonitor", "statemonitor", "spikegenerator"}
+                  "spikemonitor", "ratemonitor", "statemonitor", "spikegenerator", "summed_variable"}
 
 
 class B200CodeGenerator(CPPCodeGenerator):
@@ -291,6 +291,7 @@ class B200Device(CPPStandaloneDevice):
             return out
 
         pathways, spkmons, ratemons, statemons = [], [], [], []
+        summed_frags = []
         b200_objects = []
         for obj in objects:
             if not obj.active:
@@ -347,6 +348,8 @@ class B200Device(CPPStandaloneDevice):
                                          post_ptr=gen_name(syn.variables["_synaptic_post"]),
                                          group_ptrs=gptrs, on_pre=block(frag),
                                          _obj=pw, _src_range=srange, _tgt_range=trange, _syn=syn.name))
+                    if pw.prepost == "post":  # spiking side = the postsynaptic neurons
+                        pathways[-1]["prepost"] = "post"
                 elif t == "synapses_push_spikes":
                     pass
                 elif t == "spikegenerator":
@@ -369,6 +372,61 @@ class B200Device(CPPStandaloneDevice):
                             raise NotImplementedError(f"b200: recording '{v}' (not a state variable)")
                     statemons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng,
                                           _vars=list(obj.record_variables)))
+                elif t == "summed_variable":
+                    summed_frags.append((obj, frag))
+
+        def synaptic_vars(syn, frag):
+            used = {id(v) for v in frag["variables"].values()}
+            out = []
+            for vname, var in sorted(syn.variables.items()):
+                if (isinstance(var, DynamicArrayVariable) and var.owner is not None
+                        and var.owner.name == syn.name and getattr(var, "ndim", 1) == 1
+                        and var.name not in ("_synaptic_pre", "_synaptic_post", "N_incoming", "N_outgoing")
+                        and not var.scalar and id(var) in used and var.name not in {v["name"] for v in out}):
+                    out.append(dict(name=var.name, ctype=c_data_type(var.dtype), ptr=gen_name(var)))
+            return out
+
+        def neuron_ptrs(frag):
+            gptrs = {}
+            for vname, var in frag["variables"].items():
+                if isinstance(var, ArrayVariable) and var.owner is not None and \
+                        isinstance(var.owner, (NeuronGroup, Subgroup)):
+                    gi, _ = group_of(var.owner)
+                    names = [v["name"] for v in groups[gi]["vars"]]
+                    if var.name in names:
+                        gptrs[gen_name(var)] = [gi, names.index(var.name)]
+            return gptrs
+
+        # summed variables (templates/summed_variable.cpp): they run over the
+        # synapses of their Synapses object, held by its on_pre pathway or, for a
+        # Synapses object without one, by a pathway that delivers no events
+        summed = []
+        for obj, frag in summed_frags:
+            syn = obj.group
+            tkw = frag["template_kwds"]
+            tgi, _ = group_of(obj.target)
+            tnames = [v["name"] for v in groups[tgi]["vars"]]
+            if tkw["_target_var"].name not in tnames:
+                raise NotImplementedError("b200: summed variable target is not a state variable")
+            pi = next((k for k, p in enumerate(pathways) if p["_syn"] == syn.name), None)
+            if pi is not None and pathways[pi].get("prepost") == "post":
+                raise NotImplementedError("b200: summed variables of a Synapses object with on_post only")
+            if pi is None:
+                sgi, srange = group_of(syn.source)
+                tg2, trange = group_of(syn.target)
+                pathways.append(dict(name=syn.name + "_synapses", src=sgi, tgt=tg2, vars=[],
+                                     pre_ptr=gen_name(syn.variables["_synaptic_pre"]),
+                                     post_ptr=gen_name(syn.variables["_synaptic_post"]),
+                                     group_ptrs={}, on_pre=dict(scalar="", vector=""), events=False,
+                                     _obj=syn, _src_range=srange, _tgt_range=trange, _syn=syn.name))
+                pi = len(pathways) - 1
+            names = {v["name"] for v in pathways[pi]["vars"]}
+            pathways[pi]["vars"] += [v for v in synaptic_vars(syn, frag) if v["name"] not in names]
+            collect(frag, {syn.name} | {g["name"] for g in groups})
+            summed.append(dict(name=obj.name, pathway=pi, tgt_group=tgi,
+                               tgt_var=tnames.index(tkw["_target_var"].name),
+                               index_post=tkw["_index_var"].name == "_synaptic_post",
+                               group_ptrs=neuron_ptrs(frag), code=block(frag)))
         # pathways of one Synapses object (on_pre and on_post) share its synapses and
         # synaptic variables: the first one in schedule order owns them, the others
         # alias it; all carry the union of the variables their code uses
@@ -396,6 +454,8 @@ class B200Device(CPPStandaloneDevice):
         spec = dict(name=f"{net.name}", float=c_data_type(fdt), consts=sorted(consts.values(), key=lambda c: c["name"]),
                     groups=groups, pathways=pathways, spike_monitors=spkmons, rate_monitors=ratemons,
                     state_monitors=statemons, clock_ptrs=clock_ptrs)
+        if summed:
+            spec["summed"] = summed
         return spec, b200_objects
 
     PRIVATE_KEYS = {"_obj", "_range", "_src_range", "_tgt_range", "_vars", "_syn"}
@@ -468,16 +528,17 @@ class B200Device(CPPStandaloneDevice):
                 init[f"g{gi}_gen_period"] = np.int64(self._load(gv["_period_bins"])[0])
                 init[f"g{gi}_gen_last"] = np.int64(self._load(gv["_lastindex"])[0])
         for pi, p in enumerate(spec0["pathways"]):
-            syn = p["_obj"].synapses
+            pseudo = not p.get("events", True)  # (the Synapses object itself: no delivering pathway)
+            syn = p["_obj"] if pseudo else p["_obj"].synapses
             # the spiking side and the other side (for an on_post pathway: the
             # postsynaptic and the presynaptic neurons)
-            init[f"p{pi}_pre"] = (self._load(p["_obj"].synapse_sources).astype(np.int64)
-                                  - p["_src_range"][0]).astype(np.int32)
-            init[f"p{pi}_post"] = (self._load(p["_obj"].synapse_targets).astype(np.int64)
-                                   - p["_tgt_range"][0]).astype(np.int32)
-            dvar = p["_obj"].variables["delay"]
-            d = self._load(dvar)
-            if dvar.scalar:
+            src_arr = syn.variables["_synaptic_pre"] if pseudo else p["_obj"].synapse_sources
+            tgt_arr = syn.variables["_synaptic_post"] if pseudo else p["_obj"].synapse_targets
+            init[f"p{pi}_pre"] = (self._load(src_arr).astype(np.int64) - p["_src_range"][0]).astype(np.int32)
+            init[f"p{pi}_post"] = (self._load(tgt_arr).astype(np.int64) - p["_tgt_range"][0]).astype(np.int32)
+            dvar = None if pseudo else p["_obj"].variables["delay"]
+            d = np.zeros(1) if pseudo else self._load(dvar)
+            if pseudo or dvar.scalar:
                 init[f"p{pi}_scalar_delay"] = np.int64(int(float(d[0]) / dt + 0.5) if d.size else 0)
             else:
                 init[f"p{pi}_scalar_delay"] = np.int64(0)
@@ -518,7 +579,7 @@ class B200Device(CPPStandaloneDevice):
             if g.get("generator"):
                 self._store(g["_obj"].variables["_lastindex"], np.array([int(out[f"g{gi}_gen_last"])]))
         for pi, p in enumerate(spec0["pathways"]):
-            syn = p["_obj"].synapses
+            syn = p["_obj"] if not p.get("events", True) else p["_obj"].synapses
             for v in p["vars"] if p.get("alias", -1) < 0 else []:
                 self._store(syn.variables[v["name"]], out[f"p{pi}_{v['name']}"])
         for mi, m in enumerate(spec0["spike_monitors"]):

@@ -265,8 +265,10 @@ def render_model(spec: dict) -> str:
         blocks = [("update", _block(g.get("update"))), ("threshold", _block(g.get("threshold"))),
                   ("reset", _block(g.get("reset")))]
         gtables.append((_Tables(consts, blocks, (clock["t"], clock["timestep"])), blocks))
-    for p in paths:
+    SUMMED = spec.get("summed", [])
+    for pi, p in enumerate(paths):
         blocks = [("on_pre", _block(p.get("on_pre")))]
+        blocks += [(f"summed{si}", _block(sm["code"])) for si, sm in enumerate(SUMMED) if sm["pathway"] == pi]
         ptables.append((_Tables(consts, blocks, (clock["t"], clock["timestep"])), blocks))
 
     SIZE = {"double": 8, "int64_t": 8, "float": 4, "int32_t": 4, "char": 1, "int8_t": 1}
@@ -280,6 +282,10 @@ def render_model(spec: dict) -> str:
                 text += g[blk].get("vector", "") + "\n" + json.dumps(g[blk].get("extra_ptrs", {}))
         for p in paths:
             text += (p["on_pre"].get("vector_device") or p["on_pre"].get("vector", "")) + json.dumps(p.get("group_ptrs", {}))
+        for sm in SUMMED:
+            text += sm["code"].get("vector", "") + json.dumps(sm["group_ptrs"])
+            if sm["tgt_group"] == gi:
+                text += " " + g["vars"][sm["tgt_var"]]["ptr"] + " "
             for gg in groups:
                 for blk in ("update", "threshold", "reset"):
                     if gg.get(blk):
@@ -305,6 +311,8 @@ def render_model(spec: dict) -> str:
         text = ""
         for p in paths:
             text += json.dumps(p.get("on_pre", {})) + json.dumps(p.get("group_ptrs", {}))
+        for sm in SUMMED:  # (a summed expression reads other neurons' variables)
+            text += json.dumps(sm["code"]) + json.dumps(sm["group_ptrs"])
         for gg in groups:
             for blk in ("update", "threshold", "reset"):
                 if gg.get(blk):
@@ -313,12 +321,20 @@ def render_model(spec: dict) -> str:
 
     PRIV = [private_vars(gi) for gi in range(NG)]
 
+    def syn_arr(pi, which):
+        """Device array holding Brian's _synaptic_pre ('pre') or _synaptic_post
+        ('post') for pathway pi: a pathway stores its spiking side as `pre`, so
+        an on_post pathway that owns its synapses has them swapped."""
+        if paths[pi].get("prepost") == "post":
+            return {"pre": "post", "post": "pre"}[which]
+        return which
+
     def owner_payloads():
         """Owner mode applies when every on_pre only adds, into variables of its
         target neuron, values computed from synaptic variables and constants.
         Returns, per pathway, the synaptic variables an event carries (indices
         into the pathway's variables), or None for the whole model."""
-        if not paths or any(p.get("alias", -1) >= 0 for p in paths):
+        if not paths or SUMMED or any(p.get("alias", -1) >= 0 or not p.get("events", True) for p in paths):
             return None
         for g in groups:
             for blk in ("update", "threshold", "reset"):
@@ -681,6 +697,75 @@ def render_model(spec: dict) -> str:
         w("        } else {")
         return True
 
+    def emit_statemons(gi):
+        """State monitors of group gi: this CTA's recorded neurons, values at
+        the start of the step (templates/statemonitor.cpp)."""
+        g = groups[gi]
+        for mi, m in enumerate(statemons):
+            if m["group"] != gi:
+                continue
+            w(f"        {{  // state monitor {mi}: values at the start of the step")
+            w(f"          const b200_statemon_d& SM = I.stm[{mi}];")
+            w(f"          const int lo = s_tst[{gi} * max_tiles1 + s_ut[{gi}][0]], hi = s_tst[{gi} * max_tiles1 + s_ut[{gi}][1]];")
+            w("          double* const row = SM.data + (size_t)(ts - SM.step0) * SM.n_vars * SM.n_rec;")
+            w("          for (int k = threadIdx.x; k < SM.n_rec * SM.n_vars; k += blockDim.x) {")
+            w("            const int r = k % SM.n_rec, v = k / SM.n_rec;")
+            w("            const int idx = SM.idx[r];")
+            w("            if (idx >= lo && idx < hi) {")
+            w("              double val = 0.0;")
+            w("              switch (SM.var_id[v]) {")
+            for k, v in enumerate(g["vars"]):
+                w(f"                case {k}: val = (double)(({v['ctype']}*)s_gv[{gi}][{k}])[idx]; break;")
+            w("              }")
+            w("              row[k] = val;")
+            w("            }")
+            w("          }")
+            w(f"          if (threadIdx.x == 0) s_stm_n[{mi}] = ts + 1 - SM.step0;")
+            w("        }")
+
+    def emit_summed(si):
+        """Summed variable si (templates/summed_variable.cpp:11-25): each of
+        this CTA's target neurons sums the expression over its synapses in
+        creation order, from zero."""
+        sm = SUMMED[si]
+        pi, gi = sm["pathway"], sm["tgt_group"]
+        p = paths[pi]
+        tab, blocks = ptables[pi]
+        bname = f"summed{si}"
+        tv = groups[gi]["vars"][sm["tgt_var"]]
+        blk = dict(blocks)[bname]
+        w(f"      {{  // summed variable {sm['name']}")
+        w(f"        const b200_pathway_d& PQ = I.p[{pi}]; (void)PQ;")
+        w(f"        const double* const _b200_S = s_Sp{pi}; const float* const _b200_Sf = s_Sp{pi}f; const long long* const _b200_Si = s_Sp{pi}i;")
+        w("        (void)_b200_S; (void)_b200_Sf; (void)_b200_Si;")
+        for k, v in enumerate(p.get("vars", [])):
+            w(f"        {v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)PQ.var[{k}]; (void){v['ptr']};")
+        w(f"        const int32_t* __restrict__ const {p['post_ptr']} = PQ.{syn_arr(pi, 'post')}; (void){p['post_ptr']};")
+        w(f"        const int32_t* __restrict__ const {p['pre_ptr']} = PQ.{syn_arr(pi, 'pre')}; (void){p['pre_ptr']};")
+        for ptr, (gidx, vidx) in sorted(sm.get("group_ptrs", {}).items()):
+            v = groups[gidx]["vars"][vidx]
+            w(f"        {v['ctype']}* __restrict__ const {ptr} = ({v['ctype']}*)s_gv[{gidx}][{vidx}]; (void){ptr};")
+        w(_indent(tab.const_loads(f32), 8))
+        w(_indent(tab.scalar_loads(bname, f32), 8))
+        w(_indent(_device(tab.time_code(bname)), 8))
+        w(f"        {tv['ctype']}* const _b200_tgt = ({tv['ctype']}*)s_gv[{gi}][{sm['tgt_var']}];")
+        w(f"        const b200_summed_d& SD = I.sum[{si}];")
+        w(f"        const int o0 = s_tst[{gi} * max_tiles1 + s_ut[{gi}][0]], o1 = s_tst[{gi} * max_tiles1 + s_ut[{gi}][1]];")
+        w("        for (int j = o0 + (int)threadIdx.x; j < o1; j += blockDim.x) {")
+        w("          if (j < SD.lo || j >= SD.hi) continue;")
+        w(f"          {tv['ctype']} _b200_acc = 0;")
+        w("          for (int64_t k = SD.seg[j - SD.lo]; k < SD.seg[j - SD.lo + 1]; ++k) {")
+        w("            const int64_t _idx = SD.syn[k];")
+        w("            const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+        w("            {")
+        w(_indent(blk["vector"], 14))
+        w("              _b200_acc += _synaptic_var;")
+        w("            }")
+        w("          }")
+        w("          _b200_tgt[j] = _b200_acc;")
+        w("        }")
+        w("      }")
+
     def emit_phase_a(owner):
         """Reset of the previous step, state monitors, update + threshold with
         ordered compaction of this CTA's tiles."""
@@ -692,7 +777,7 @@ def render_model(spec: dict) -> str:
                 emit_generator(gi, owner)
                 continue
             w(f"      // ---- group {gi} '{g['name']}': phase A (reset of step ts-1, monitors, update + threshold)")
-            if bd["reset"] is not None:
+            if bd["reset"] is not None and not SUMMED:  # (with summed variables: before the sums)
                 w("      if (ts > ts0) {")
                 w(reset_block(gi, 8, "ts - 1", owner))
                 w("        __syncthreads();")
@@ -708,27 +793,8 @@ def render_model(spec: dict) -> str:
                 w(f"        int32_t* const scr = s_scr[{gi}]; int32_t* const tcnt = s_tc[{gi}];")
                 w(f"        int32_t* const oscr = s_oscr[{gi}]; int32_t* const otc = s_otc[{gi}];")
             w(f"        const int* const tst = s_tst + {gi} * max_tiles1;")
-            for mi, m in enumerate(statemons):
-                if m["group"] != gi:
-                    continue
-                w(f"        {{  // state monitor {mi}: values at the start of the step")
-                w(f"          const b200_statemon_d& SM = I.stm[{mi}];")
-                w(f"          const int lo = tst[s_ut[{gi}][0]], hi = tst[s_ut[{gi}][1]];")
-                w("          double* const row = SM.data + (size_t)(ts - SM.step0) * SM.n_vars * SM.n_rec;")
-                w("          for (int k = threadIdx.x; k < SM.n_rec * SM.n_vars; k += blockDim.x) {")
-                w("            const int r = k % SM.n_rec, v = k / SM.n_rec;")
-                w("            const int idx = SM.idx[r];")
-                w("            if (idx >= lo && idx < hi) {")
-                w("              double val = 0.0;")
-                w("              switch (SM.var_id[v]) {")
-                for k, v in enumerate(g["vars"]):
-                    w(f"                case {k}: val = (double)(({v['ctype']}*)s_gv[{gi}][{k}])[idx]; break;")
-                w("              }")
-                w("              row[k] = val;")
-                w("            }")
-                w("          }")
-                w(f"          if (threadIdx.x == 0) s_stm_n[{mi}] = ts + 1 - SM.step0;")
-                w("        }")
+            if not SUMMED:  # (with summed variables the monitors record before those are summed)
+                emit_statemons(gi)
             # constants and block scalars are loaded once per step, not per neuron
             upd_sc = {nm for _, nm in scalar_outputs(bd["update"]["scalar"])} if bd["update"] is not None else set()
             thr_sc = {nm for _, nm in scalar_outputs(bd["threshold"]["scalar"])} if bd["threshold"] is not None else set()
@@ -1045,6 +1111,23 @@ def render_model(spec: dict) -> str:
     w("      const double _b200_t = (double)ts * _b200_dt;")
     w("      const int64_t _b200_ts = ts;")
     w("      if (prof && threadIdx.x == 0) _pt = clock64();")
+    if SUMMED:
+        # the reference's schedule: resets of the previous step (after its
+        # deliveries), state monitors (start), then the summed variables (groups
+        # slot, before the groups' updates).  The sums read other CTAs' neurons:
+        # every CTA has applied its resets before any sums, and finishes its sums
+        # before any update
+        for gi in range(NG):
+            if dict(gtables[gi][1])["reset"] is not None:
+                w("      if (ts > ts0) {")
+                w(reset_block(gi, 8, "ts - 1"))
+                w("      }")
+        w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster, rank)) { ok = false; break; }")
+        for gi in range(NG):
+            emit_statemons(gi)
+        for si in range(len(SUMMED)):
+            emit_summed(si)
+        w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster, rank)) { ok = false; break; }")
 
     emit_phase_a(False)
     w("      B200_PHASE(0);")
@@ -1178,6 +1261,8 @@ def render_model(spec: dict) -> str:
     # any of them reads, so the reference's pathway-by-pathway order is kept
     merged = []
     for pi, p in enumerate(paths):
+        if not p.get("events", True):
+            continue  # the synapses of a Synapses object without a delivering pathway
         # neuron variables and synaptic variables (shared by the pathways of one
         # Synapses object): pathways touching the same ones are not interleaved
         touched = set(p.get("group_ptrs", {})) | {v["ptr"] for v in p.get("vars", [])}
@@ -1325,9 +1410,9 @@ def render_model(spec: dict) -> str:
                 p = paths[pi]
                 own = p.get("alias", -1) if p.get("alias", -1) >= 0 else pi  # shared synapses: the owner's arrays
                 if ptr == p["post_ptr"]:
-                    return f"I.p[{own}].post[_idx]"
+                    return f"I.p[{own}].{syn_arr(own, 'post')}[_idx]"
                 if ptr == p["pre_ptr"]:
-                    return f"I.p[{own}].pre[_idx]"
+                    return f"I.p[{own}].{syn_arr(own, 'pre')}[_idx]"
                 k = next(k for k, v in enumerate(p.get("vars", [])) if v["ptr"] == ptr)
                 return f"(({ct}*)I.p[{pi}].var[{k}])[_idx]"
 
@@ -1377,8 +1462,8 @@ def render_model(spec: dict) -> str:
                 for k, v in enumerate(p.get("vars", [])):
                     w(f"                  {v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)PQ.var[{k}]; (void){v['ptr']};")
                 own = p.get("alias", -1) if p.get("alias", -1) >= 0 else pi
-                w(f"                  const int32_t* __restrict__ const {p['post_ptr']} = I.p[{own}].post; (void){p['post_ptr']};")
-                w(f"                  const int32_t* __restrict__ const {p['pre_ptr']} = I.p[{own}].pre; (void){p['pre_ptr']};")
+                w(f"                  const int32_t* __restrict__ const {p['post_ptr']} = I.p[{own}].{syn_arr(own, 'post')}; (void){p['post_ptr']};")
+                w(f"                  const int32_t* __restrict__ const {p['pre_ptr']} = I.p[{own}].{syn_arr(own, 'pre')}; (void){p['pre_ptr']};")
                 w(_indent(tab.scalar_loads("on_pre", f32), 18))
                 w(_indent(_device(tab.time_code("on_pre")), 18))
                 w("                  {  // (Brian's vector code may redeclare the clock's names)")
@@ -1413,8 +1498,8 @@ def render_model(spec: dict) -> str:
                 for k, v in enumerate(p.get("vars", [])):
                     w(f"                  {v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)PQ.var[{k}]; (void){v['ptr']};")
                 own = p.get("alias", -1) if p.get("alias", -1) >= 0 else pi
-                w(f"                  const int32_t* __restrict__ const {p['post_ptr']} = I.p[{own}].post; (void){p['post_ptr']};")
-                w(f"                  const int32_t* __restrict__ const {p['pre_ptr']} = I.p[{own}].pre; (void){p['pre_ptr']};")
+                w(f"                  const int32_t* __restrict__ const {p['post_ptr']} = I.p[{own}].{syn_arr(own, 'post')}; (void){p['post_ptr']};")
+                w(f"                  const int32_t* __restrict__ const {p['pre_ptr']} = I.p[{own}].{syn_arr(own, 'pre')}; (void){p['pre_ptr']};")
                 for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
                     v = groups[gidx]["vars"][vidx]
                     w(f"                  {v['ctype']}* __restrict__ const {ptr} = ({v['ctype']}*)s_gv[{gidx}][{vidx}]; (void){ptr};")
@@ -2277,10 +2362,15 @@ def render_model(spec: dict) -> str:
     w("  return n;")
     w("}")
     w("")
+    if SUMMED:
+        w("static const b200_summed_info b200_summed[] = {" + ", ".join(
+            f'{{"{sm["name"]}", {sm["pathway"]}, {sm["tgt_group"]}, {sm["tgt_var"]}, {1 if sm["index_post"] else 0}}}'
+            for sm in SUMMED) + "};")
     w(f'static const b200_model_info B200_MODEL = {{"{spec["name"]}", {NG}, {NP}, {len(spkmons)}, {len(ratemons)}, {len(statemons)},')
     w("  b200_groups, b200_pathways, b200_spkmon, b200_ratemon, b200_statemon,")
     w(f"  {len(consts)}, b200_const_names, b200_const_defaults, b200_eval_scalars, b200_launch, b200_max_active,")
-    w(f"  b200_static_smem, b200_max_cluster, {NPH}, {1 if OWNER else 0}, {OWNER_EV_BYTES}}};")
+    w(f"  b200_static_smem, b200_max_cluster, {NPH}, {1 if OWNER else 0}, {OWNER_EV_BYTES},")
+    w(f"  {len(SUMMED)}, {'b200_summed' if SUMMED else 'nullptr'}}};")
     w("")
     w('#include "b200_host.h"')
     w("")

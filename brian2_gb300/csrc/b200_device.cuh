@@ -17,6 +17,7 @@
 #define B200_MAX_SPKMON 4
 #define B200_MAX_RATEMON 4
 #define B200_MAX_STATEMON 4
+#define B200_MAX_SUMMED 4
 #define B200_MAX_THREADS 1024
 #define B200_MAX_WARPS (B200_MAX_THREADS / 32)
 
@@ -120,6 +121,15 @@ struct b200_statemon_d {
   double* data;           // [cap][n_vars][n_rec] values (as double)
 };
 
+// A summed variable (SummedVariableUpdater, brian2/synapses/synapses.py:116-175;
+// templates/summed_variable.cpp): each target neuron's value is the sum, in
+// synapse creation order, of an expression over its synapses.
+struct b200_summed_d {
+  int32_t lo, hi;         // target neurons [lo, hi) of the target group
+  const int64_t* seg;     // [hi-lo+1] each target's run in syn
+  const int64_t* syn;     // the synapses' positions in their pathway's arrays, creation order per target
+};
+
 struct b200_inst_d {
   int32_t cta0, n_cta;    // CTAs [cta0, cta0+n_cta) of the grid run this instance
   int32_t cache_bytes;    // >0: single-CTA instance whose state is cached in shared memory
@@ -147,6 +157,7 @@ struct b200_inst_d {
   b200_spkmon_d sm[B200_MAX_SPKMON];
   b200_ratemon_d rm[B200_MAX_RATEMON];
   b200_statemon_d stm[B200_MAX_STATEMON];
+  b200_summed_d sum[B200_MAX_SUMMED];
 };
 
 static_assert(sizeof(b200_inst_d) % 8 == 0, "descriptor is copied in 8-byte words");
@@ -191,6 +202,13 @@ struct b200_pathway_info {
   // synapses and synaptic variables of that pathway (its on_pre pathway)
   int alias;
 };
+struct b200_summed_info {
+  const char* name;
+  int pathway;     // the pathway holding the Synapses object's synapses and variables
+  int tgt_group;   // group of the summed variable
+  int tgt_var;     // its index among the group's variables
+  int index_post;  // 1: summed into the postsynaptic neuron, 0: into the presynaptic one
+};
 struct b200_mon_info {
   const char* name;
   int group;
@@ -221,6 +239,8 @@ struct b200_model_info {
   // synaptic values and constants, so owner-mode delivery applies
   int owner_ok;
   int owner_event_bytes;  // shared-memory bytes per staged event
+  int n_summed;
+  const b200_summed_info* summed;
 };
 // `tcode` bit selecting the owner-mode kernel
 #define B200_TCODE_OWNER (1 << 20)

@@ -59,6 +59,10 @@ struct b200_pathway_h {
   int64_t ev_cap = 0;
   int32_t ev_RB = 0, ev_W = 0, ev_ncta = 0;
 };
+struct b200_summed_h {
+  int32_t lo = 0, hi = 0;
+  b200_dbuf seg, syn;
+};
 struct b200_spkmon_h {
   int32_t lo = 0, hi = 0;
   int64_t cap = 0;
@@ -82,6 +86,7 @@ struct b200_inst_h {
   std::vector<b200_spkmon_h> sm;
   std::vector<b200_ratemon_h> rm;
   std::vector<b200_statemon_h> stm;
+  std::vector<b200_summed_h> sum;
   int32_t n_cta = 1;
   int64_t ts = 0;
   b200_dbuf bar, status, ts_done, pending, bar64;
@@ -194,6 +199,7 @@ int b200_create(b200_net** out, int32_t n_inst, const int32_t* group_sizes, doub
     I.sm.resize(M->n_spkmon);
     I.rm.resize(M->n_ratemon);
     I.stm.resize(M->n_statemon);
+    I.sum.resize(M->n_summed);
     for (int g = 0; g < M->n_groups; ++g) {
       b200_group_h& G = I.g[g];
       G.N = group_sizes[k * M->n_groups + g];
@@ -238,7 +244,7 @@ int b200_destroy(b200_net* n) {
     }
     for (auto& P : I.p) {
       for (auto& b : P.var) b200_free(n, b);
-      b200_free(n, P.segptr); b200_free(n, P.post); b200_free(n, P.pre); b200_free(n, P.S);
+      b200_free(n, P.segptr); b200_free(n, P.post); b200_free(n, P.pre); b200_free(n, P.S); b200_free(n, P.sidx);
       for (auto& b : P.ovar) b200_free(n, b);
       for (auto& b : P.ev_pay) b200_free(n, b);
       b200_free(n, P.oseg); b200_free(n, P.opost); b200_free(n, P.odelay);
@@ -248,6 +254,7 @@ int b200_destroy(b200_net* n) {
     for (auto& S : I.sm) { b200_free(n, S.n); b200_free(n, S.i); b200_free(n, S.ts); b200_free(n, S.count); }
     for (auto& S : I.rm) b200_free(n, S.cnt);
     for (auto& S : I.stm) { b200_free(n, S.d_idx); b200_free(n, S.n); b200_free(n, S.data); }
+    for (auto& S : I.sum) { b200_free(n, S.seg); b200_free(n, S.syn); }
     b200_free(n, I.bar); b200_free(n, I.status); b200_free(n, I.ts_done); b200_free(n, I.pending);
     b200_free(n, I.bar64);
   }
@@ -451,6 +458,27 @@ int b200_set_synapses(b200_net* n, int32_t inst, int32_t pw, int32_t src_lo, int
   if (PI.alias < 0)
     for (int v = 0; v < PI.n_vars; ++v)
       if ((r = b200_alloc(n, P.var[v], (size_t)n_syn * b200_kind_size(PI.var_kind[v])))) return r;
+  // summed variables over these synapses: per target neuron, its synapses'
+  // positions in this pathway's order, in creation order (the order of the
+  // reference's sum, templates/summed_variable.cpp:19-25)
+  for (int sv = 0; sv < n->M->n_summed; ++sv) {
+    const b200_summed_info& SI = n->M->summed[sv];
+    if (SI.pathway != pw) continue;
+    b200_summed_h& S = I.sum[sv];
+    S.lo = SI.index_post ? tgt_lo : src_lo;
+    S.hi = SI.index_post ? tgt_hi : src_hi;
+    const int32_t nt = S.hi - S.lo;
+    std::vector<int64_t> inv((size_t)n_syn), sseg((size_t)nt + 1, 0), ssyn((size_t)n_syn);
+    for (int64_t q = 0; q < n_syn; ++q) inv[(size_t)P.perm[q]] = q;
+    for (int64_t k = 0; k < n_syn; ++k) sseg[(size_t)(SI.index_post ? post[k] : pre[k]) + 1]++;
+    for (size_t t = 1; t < sseg.size(); ++t) sseg[t] += sseg[t - 1];
+    std::vector<int64_t> sfill(sseg.begin(), sseg.end() - 1);
+    for (int64_t k = 0; k < n_syn; ++k) ssyn[(size_t)sfill[(size_t)(SI.index_post ? post[k] : pre[k])]++] = inv[k];
+    if ((r = b200_alloc(n, S.seg, sseg.size() * 8, false))) return r;
+    if ((r = b200_alloc(n, S.syn, (size_t)std::max<int64_t>(n_syn, 1) * 8, false))) return r;
+    B200_CU(n, cudaMemcpyAsync(S.seg.p, sseg.data(), sseg.size() * 8, cudaMemcpyHostToDevice, n->stream));
+    if (n_syn) B200_CU(n, cudaMemcpyAsync(S.syn.p, ssyn.data(), (size_t)n_syn * 8, cudaMemcpyHostToDevice, n->stream));
+  }
   B200_CU(n, cudaStreamSynchronize(n->stream));
   n->prepared = false;
   return 0;
@@ -934,6 +962,12 @@ static int b200_prepare(b200_net* n) {
         SD.var_dbl[v] = M->groups[SD.group].var_kind[S.vars[v]] == B200_F64;
       }
       SD.n = (int64_t*)S.n.p;
+    }
+    for (int sv = 0; sv < M->n_summed; ++sv) {  // (the pathways' synapses are set above)
+      const b200_summed_h& S = I.sum[sv];
+      D.sum[sv].lo = S.lo; D.sum[sv].hi = S.hi;
+      D.sum[sv].seg = (const int64_t*)S.seg.p;
+      D.sum[sv].syn = (const int64_t*)S.syn.p;
     }
   }
   n->max_tiles1 = 2;

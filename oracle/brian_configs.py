@@ -320,6 +320,34 @@ def stdp(N_in=200, N=50, duration_ms=300.0, rate_hz=15.0, seed_value=71):
     return dict(P=P, G=G, S=S, spikes=s_mon, rate=r_mon, gen_spikes=g_mon, syn_vars=("w", "Apre", "Apost"))
 
 
+def gap_junctions(N=200, duration_ms=200.0, seed_value=81):
+    """Electrically coupled LIF neurons: a summed variable (Igap_post = w *
+    (v_pre - v_post), summed over each neuron's gap junctions every step) in a
+    Synapses object without on_pre, plus chemical synapses with delays."""
+    from brian2 import NeuronGroup, Synapses, SpikeMonitor, PopulationRateMonitor, StateMonitor, ms, seed, run
+    seed(seed_value)
+    ns = dict(tau=10 * ms, w_syn=0.05)
+    P = NeuronGroup(N, '''dv/dt = (v0 - v + Igap) / tau : 1
+                          v0 : 1 (constant)
+                          Igap : 1''',
+                    threshold='v > 1', reset='v = 0', method='exact', namespace=ns)
+    P.v = 'rand()'
+    P.v0 = '1.02 + rand() * 0.2'
+    G = Synapses(P, P, '''w : 1 (constant)
+                          Igap_post = w * (v_pre - v_post) : 1 (summed)''', namespace=ns)
+    G.connect('i != j', p=0.05)
+    G.w = 'rand() * 0.02'
+    S = Synapses(P, P, on_pre='v_post += w_syn', namespace=ns)
+    S.connect('i != j', p=0.02)
+    S.delay = '1*ms + rand() * 2*ms'
+    # monitors must be locals of the frame that calls run() (Brian collects them there)
+    s_mon = SpikeMonitor(P)
+    r_mon = PopulationRateMonitor(P)
+    st_mon = StateMonitor(P, ['v', 'Igap'], record=[0, 7, 150])
+    run(duration_ms * ms)
+    return dict(P=P, G=G, S=S, spikes=s_mon, rate=r_mon, state=st_mon, state_extra=("Igap",))
+
+
 SCENARIOS = {
     "lif_refractory": lif_refractory,
     "hetero_delays": hetero_delays,
@@ -328,4 +356,5 @@ SCENARIOS = {
     "presynaptic_read": presynaptic_read,
     "spike_generator": spike_generator,
     "stdp": stdp,
+    "gap_junctions": gap_junctions,
 }

@@ -22,6 +22,9 @@ code objects, and executes the spec's *plain* C++ snippets (Brian's own
   (templates/synapses_push_spikes.cpp:24-28, synapses/spikequeue.h:146-205,
   templates/synapses.cpp:20-49);
 * reset for each spike (templates/reset.cpp:16-22);
+* summed variables: the target range zeroed, then the expression of every
+  synapse in creation order added to its target (templates/summed_variable.cpp:
+  11-25), after the state monitors and before the state updates;
 * rate monitor count per step (templates/ratemonitor.cpp:7-35);
 * state monitor record at the start of the step (templates/statemonitor.cpp).
 
@@ -93,7 +96,7 @@ def render_oracle(spec: dict) -> str:
         if g.get("generator"):
             w(f"  std::vector<int32_t> gen{gi}_bins, gen{gi}_index; int32_t gen{gi}_period = 0, gen{gi}_last = 0;")
     for pi, p in enumerate(paths):
-        w(f"  int32_t p{pi}_src_lo = 0, p{pi}_src_hi = 0; std::vector<int32_t> p{pi}_pre, p{pi}_post, p{pi}_delay;")
+        w(f"  int32_t p{pi}_src_lo = 0, p{pi}_src_hi = 0, p{pi}_tgt_lo = 0, p{pi}_tgt_hi = 0; std::vector<int32_t> p{pi}_pre, p{pi}_post, p{pi}_delay;")
         for v in p.get("vars", []):
             w(f"  std::vector<{v['ctype']}> p{pi}_{v['name']};")
         w(f"  std::vector<std::vector<int32_t>> p{pi}_queue = std::vector<std::vector<int32_t>>(1); int p{pi}_offset = 0;")
@@ -134,11 +137,11 @@ def render_oracle(spec: dict) -> str:
     w("  return nullptr;")
     w("}")
     # synapses: pre/post relative to the source/target range; stored absolute
-    w("int oracle_set_synapses(Net* n, int32_t pw, const int32_t* pre, const int32_t* post, const int32_t* delay,")
+    w("int oracle_set_synapses(Net* n, int32_t pw, const int32_t* pre, const int32_t* post, const int32_t* delay, int32_t tgt_hi,")
     w("                        int32_t scalar_delay, int64_t n_syn, int32_t src_lo, int32_t src_hi, int32_t tgt_lo) {")
     for pi, p in enumerate(paths):
         w(f"  if (pw == {pi}) {{")
-        w(f"    n->p{pi}_src_lo = src_lo; n->p{pi}_src_hi = src_hi;")
+        w(f"    n->p{pi}_src_lo = src_lo; n->p{pi}_src_hi = src_hi; n->p{pi}_tgt_lo = tgt_lo; n->p{pi}_tgt_hi = tgt_hi;")
         w(f"    n->p{pi}_pre.resize(n_syn); n->p{pi}_post.resize(n_syn); n->p{pi}_delay.resize(n_syn);")
         w(f"    for (int64_t k = 0; k < n_syn; ++k) {{ n->p{pi}_pre[k] = pre[k] + src_lo; n->p{pi}_post[k] = post[k] + tgt_lo;")
         w(f"      n->p{pi}_delay[k] = delay ? delay[k] : scalar_delay; }}")
@@ -216,6 +219,32 @@ def render_oracle(spec: dict) -> str:
         w("      }")
         w(f"      n->st{mi}_n++;")
         w("    }")
+    # summed variables (groups slot, before the groups' updates)
+    for si, sm in enumerate(spec.get("summed", [])):
+        pi, gi = sm["pathway"], sm["tgt_group"]
+        p = paths[pi]
+        tv = groups[gi]["vars"][sm["tgt_var"]]
+        w(f"    {{  // summed variable {sm['name']}")
+        w(f"      int32_t* const {p['pre_ptr']} = n->p{pi}_pre.data(); (void){p['pre_ptr']};")
+        w(f"      int32_t* const {p['post_ptr']} = n->p{pi}_post.data(); (void){p['post_ptr']};")
+        for v in p.get("vars", []):
+            w(f"      {v['ctype']}* const {v['ptr']} = n->p{pi}_{v['name']}.data(); (void){v['ptr']};")
+        for ptr, (gidx, vidx) in sorted(sm.get("group_ptrs", {}).items()):
+            v = groups[gidx]["vars"][vidx]
+            w(f"      {v['ctype']}* const {ptr} = n->g{gidx}_{v['name']}.data(); (void){ptr};")
+        w(f"      {tv['ctype']}* const _tgt = n->g{gi}_{tv['name']}.data();")
+        idx = f"n->p{pi}_post" if sm["index_post"] else f"n->p{pi}_pre"
+        lo, hi = (f"n->p{pi}_tgt_lo", f"n->p{pi}_tgt_hi") if sm["index_post"] else (f"n->p{pi}_src_lo", f"n->p{pi}_src_hi")
+        w(f"      for (int32_t _t = {lo}; _t < {hi}; ++_t) _tgt[_t] = 0;")
+        w("      {")
+        w(_ind(sm["code"]["scalar"], 8))
+        w(f"        for (int64_t _idx = 0; _idx < (int64_t){idx}.size(); ++_idx) {{")
+        w("          const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+        w(_ind(sm["code"]["vector"], 10))
+        w(f"          _tgt[{idx}[_idx]] += _synaptic_var;")
+        w("        }")
+        w("      }")
+        w("    }")
     # state updaters of all groups
     for gi, g in enumerate(groups):
         if not g.get("update"):
@@ -290,8 +319,10 @@ def render_oracle(spec: dict) -> str:
         # the on_post pathway of a Synapses object shares the synapses (creation
         # order) and the synaptic variables of its on_pre pathway
         own = p.get("alias", -1) if p.get("alias", -1) >= 0 else pi
-        w(f"      int32_t* const {p['pre_ptr']} = n->p{own}_pre.data(); (void){p['pre_ptr']};")
-        w(f"      int32_t* const {p['post_ptr']} = n->p{own}_post.data(); (void){p['post_ptr']};")
+        # a pathway keeps its spiking side as `pre`: swapped for an on_post pathway
+        sw = paths[own].get("prepost") == "post"
+        w(f"      int32_t* const {p['pre_ptr']} = n->p{own}_{'post' if sw else 'pre'}.data(); (void){p['pre_ptr']};")
+        w(f"      int32_t* const {p['post_ptr']} = n->p{own}_{'pre' if sw else 'post'}.data(); (void){p['post_ptr']};")
         for v in p.get("vars", []):
             w(f"      {v['ctype']}* const {v['ptr']} = n->p{own}_{v['name']}.data(); (void){v['ptr']};")
         for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
@@ -380,7 +411,7 @@ class OracleNet:
             lib.oracle_var.restype = C.c_void_p
             lib.oracle_var.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
             lib.oracle_set_consts.argtypes = [C.c_void_p, _f64p, C.c_int32]
-            lib.oracle_set_synapses.argtypes = [C.c_void_p, C.c_int32, _i32p, _i32p, _i32p, C.c_int32, C.c_int64,
+            lib.oracle_set_synapses.argtypes = [C.c_void_p, C.c_int32, _i32p, _i32p, _i32p, C.c_int32, C.c_int32, C.c_int64,
                                                 C.c_int32, C.c_int32, C.c_int32]
             lib.oracle_set_range.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
             lib.oracle_set_statemon.argtypes = [C.c_void_p, C.c_int32, _i32p, C.c_int32, _i32p, C.c_int32]
@@ -440,12 +471,12 @@ class OracleNet:
         ps = self.spec["pathways"]
         p = pathway if isinstance(pathway, int) else [x["name"] for x in ps].index(pathway)
         s0, s1 = src_range if src_range is not None else (0, int(self.sizes[ps[p]["src"]]))
-        t0 = tgt_range[0] if tgt_range is not None else 0
+        t0, t1 = tgt_range if tgt_range is not None else (0, int(self.sizes[ps[p]["tgt"]]))
         pre = np.ascontiguousarray(pre, np.int32)
         post = np.ascontiguousarray(post, np.int32)
         d = None if delay_steps is None else np.ascontiguousarray(delay_steps, np.int32)
         r = self.lib.oracle_set_synapses(self.h, p, pre.ctypes.data_as(_i32p), post.ctypes.data_as(_i32p),
-                                         None if d is None else d.ctypes.data_as(_i32p), int(scalar_delay),
+                                         None if d is None else d.ctypes.data_as(_i32p), int(t1), int(scalar_delay),
                                          pre.size, s0, s1, t0)
         assert r == 0
         self.n_syn[p] = pre.size

@@ -58,9 +58,11 @@ def run_ref(name):
     if "state" in r:
         out["state_v"] = np.asarray(r["state"].v_[:]).copy()        # [n_rec, steps]
         out["state_idx"] = np.asarray(r["state"].record, dtype=np.int32)
-    for var in ("v", "ge", "gi", "a"):
+    for var in ("v", "ge", "gi", "a", "Igap"):
         if var in P.variables:
             out[var] = np.asarray(getattr(P, var + "_")[:]).copy()
+    for var in r.get("state_extra", ()):        # more recorded variables: [n_rec, steps]
+        out["state_" + var] = np.asarray(getattr(r["state"], var + "_")[:]).copy()
     meta = dict(group=P.name, n_spikes=int(len(t)), n_steps=int(len(out["rate_counts"])), spike_monitor=spk.name)
     if "gen_spikes" in r:                       # a spike generator's own raster and cursor
         g = r["gen_spikes"]

@@ -20,7 +20,8 @@ from brian2_gb300.job import load_job, run_job
 pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 EXACT = {"lif_refractory": True, "hetero_delays": False, "subgroup_monitors": True, "input_group": True,
-         "presynaptic_read": False, "spike_generator": True, "stdp": False}
+         "presynaptic_read": False, "spike_generator": True, "stdp": False,
+         "gap_junctions": True}
 
 
 @pytest.mark.parametrize("name", sorted(EXACT))
@@ -46,7 +47,7 @@ def test_scenario_matches_reference(name, ctas, owner):
         assert int(out[f"g{gg}_gen_last"]) == meta["gen_lastindex"]
     np.testing.assert_array_equal(out["rm0_counts"], ref["rate_counts"])
     gi = [g["name"] for g in spec["groups"]].index(meta["group"])
-    for var in ("v", "ge", "gi", "a"):
+    for var in ("v", "ge", "gi", "a", "Igap"):
         if var in ref:
             if EXACT[name]:
                 np.testing.assert_array_equal(out[f"g{gi}_{var}"], ref[var], err_msg=var)
@@ -55,6 +56,8 @@ def test_scenario_matches_reference(name, ctas, owner):
     if "state_v" in ref:
         tr = out["stm0_trace"][:, 0, :].T            # [n_rec, steps]
         np.testing.assert_array_equal(tr, ref["state_v"])
+    if "state_Igap" in ref:                        # a second recorded variable (a summed one)
+        np.testing.assert_array_equal(out["stm0_trace"][:, 1, :].T, ref["state_Igap"])
     for var in meta.get("syn_vars", []):           # plastic synapses (on_pre and on_post share them)
         pi = next(k for k, p in enumerate(spec["pathways"])
                   if p["name"].startswith(meta["synapses"] + "_") and p.get("alias", -1) < 0)

@@ -34,7 +34,7 @@ def test_job_carries_the_reference_network(case, golden):
 
 
 SCENARIOS = ["lif_refractory", "hetero_delays", "subgroup_monitors", "input_group", "presynaptic_read",
-             "spike_generator", "stdp"]
+             "spike_generator", "stdp", "gap_junctions"]
 
 
 @pytest.mark.parametrize("name", SCENARIOS)
@@ -51,6 +51,11 @@ def test_scenario_jobs_describe_their_features(name):
         assert list(init["stm0_idx"]) == [0, 10, 250, 499]
     if name == "input_group":
         assert len(spec["groups"]) == 2 and {p["src"] for p in spec["pathways"]} == {0, 1}
+    if name == "gap_junctions":  # a summed variable over a Synapses object without on_pre
+        (sm,) = spec["summed"]
+        pw = spec["pathways"][sm["pathway"]]
+        assert pw.get("events") is False and [v["name"] for v in pw["vars"]] == ["w"]
+        assert spec["groups"][sm["tgt_group"]]["vars"][sm["tgt_var"]]["name"] == "Igap" and sm["index_post"]
     if name == "stdp":  # on_pre and on_post pathways of one Synapses object share its variables
         pre, post = spec["pathways"]
         assert post.get("alias") == 0 and pre.get("alias", -1) == -1

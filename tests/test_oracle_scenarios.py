@@ -38,11 +38,13 @@ def test_oracle_reproduces_reference_scenario(name):
         gg = [g["name"] for g in spec["groups"]].index(meta["gen_group"])
         assert int(out[f"g{gg}_gen_last"]) == meta["gen_lastindex"]
     gi = [g["name"] for g in spec["groups"]].index(meta["group"])
-    for var in ("v", "ge", "gi", "a"):
+    for var in ("v", "ge", "gi", "a", "Igap"):
         if var in ref:
             np.testing.assert_array_equal(out[f"g{gi}_{var}"], ref[var], err_msg=var)
     if "state_v" in ref:
         np.testing.assert_array_equal(out["stm0_trace"][:, 0, :].T, ref["state_v"])
+    if "state_Igap" in ref:                      # a second recorded variable (a summed one)
+        np.testing.assert_array_equal(out["stm0_trace"][:, 1, :].T, ref["state_Igap"])
     for var in meta.get("syn_vars", []):        # plastic synapses: final synaptic variables
         pi = next(k for k, p in enumerate(spec["pathways"])
                   if p["name"].startswith(meta["synapses"] + "_") and p.get("alias", -1) < 0)
