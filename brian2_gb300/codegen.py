@@ -571,7 +571,8 @@ def render_model(spec: dict) -> str:
         pfi = {ptr: j for j, ptr in enumerate(sorted(pf))}
         sti = {ptr: j for j, ptr in enumerate(sorted(upd_st))}
         vt = lambda ptr: QUADV[own[ptr]["ctype"]][0]
-        w(f"        if (s_quad[{gi}]) {{  // four neurons per thread, 16-byte accesses")
+        w(f"        if ((MAXT * MINB < 1024) && s_quad[{gi}]) {{  // four neurons per thread, 16-byte accesses")
+        w("          // (not in the variants capped at 64 registers, where it spills)")
         w(f"          for (int u = s_ut[{gi}][0]; u < s_ut[{gi}][1]; ++u) {{")
         w("            const int start = tst[u], end = tst[u + 1];")
         w("            int cnt = 0;")
@@ -1092,12 +1093,15 @@ def render_model(spec: dict) -> str:
     w("    const double _b200_dt = I.dt;")
     w("    int64_t ts = ts0;")
     w("    bool ok = true;")
-    w("    const bool lagm = I.lag && I.n_cta > 1;  // deliveries read no spikes of their own step")
+    # deliveries read no spikes of their own step; not in the variants capped at
+    # 64 registers (their code would spill; they serve single-CTA instances)
+    w("    const bool lagm = (MAXT * MINB < 1024) && I.lag && I.n_cta > 1;")
     w("    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, NW = blockDim.x >> 5;")
     w(f"    // per-phase device profile (thread 0 of each CTA; phases: A, barrier A, spike lists,")
     w(f"    // {NP} pathway(s), barrier B)")
-    w(f"    unsigned long long _pt = 0, _pacc[{NPH}];")
-    w(f"    for (int q = 0; q < {NPH}; ++q) _pacc[q] = 0;")
+    # (in shared memory, written by thread 0 only: no registers held across the steps)
+    w(f"    __shared__ unsigned long long _pt, _pacc[{NPH}];")
+    w(f"    if (threadIdx.x == 0) {{ _pt = 0; for (int q = 0; q < {NPH}; ++q) _pacc[q] = 0; }}")
     w("#define B200_PHASE(q) do { if (prof && threadIdx.x == 0) { const unsigned long long _c = clock64(); _pacc[q] += _c - _pt; _pt = _c; } } while (0)")
     w("    for (; ts < ts_stop; ++ts) {")
     w("      if (threadIdx.x == 0) {")
@@ -1784,8 +1788,8 @@ def render_model(spec: dict) -> str:
         w("    bool ok = true, pend = false;")
         w("    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, NW = blockDim.x >> 5;")
         w("    (void)lane; (void)wid; (void)NW;")
-        w(f"    unsigned long long _pt = 0, _pacc[{NPH}];")
-        w(f"    for (int q = 0; q < {NPH}; ++q) _pacc[q] = 0;")
+        w(f"    __shared__ unsigned long long _pt, _pacc[{NPH}];")
+        w(f"    if (threadIdx.x == 0) {{ _pt = 0; for (int q = 0; q < {NPH}; ++q) _pacc[q] = 0; }}")
         w("#define B200_PHASE(q) do { if (prof && threadIdx.x == 0) { const unsigned long long _c = clock64(); _pacc[q] += _c - _pt; _pt = _c; } } while (0)")
 
         def emit_lists(tsexpr, record_mon, ind):

@@ -348,6 +348,34 @@ def gap_junctions(N=200, duration_ms=200.0, seed_value=81):
     return dict(P=P, G=G, S=S, spikes=s_mon, rate=r_mon, state=st_mon, state_extra=("Igap",))
 
 
+def explicit_methods(N=300, duration_ms=150.0, seed_value=91):
+    """Nonlinear (quadratic integrate-and-fire with adaptation) neurons
+    integrated with the explicit methods: one group with 'euler', one with
+    'rk4' (stateupdaters/explicit.py), coupled by synapses with delays."""
+    from brian2 import NeuronGroup, Synapses, SpikeMonitor, PopulationRateMonitor, ms, mV, seed, run
+    seed(seed_value)
+    ns = dict(tau=10 * ms, tau_w=100 * ms, El=-65 * mV, Vc=-50 * mV, Vr=-70 * mV, Vpeak=-30 * mV,
+              a=0.2, b=2 * mV, kq=15 * mV, w_syn=1.5 * mV)
+    eqs = '''dv/dt = ((v - El) * (v - Vc) / kq - u + I) / tau : volt
+             du/dt = (a * (v - El) - u) / tau_w : volt
+             I : volt (constant)'''
+    P = NeuronGroup(N, eqs, threshold='v > Vpeak', reset='v = Vr; u += b', method='euler', namespace=ns)
+    P.v = 'El + rand() * 5*mV'
+    P.I = '10*mV + rand() * 8*mV'
+    Q = NeuronGroup(N, eqs, threshold='v > Vpeak', reset='v = Vr; u += b', method='rk4', namespace=ns)
+    Q.v = 'El + rand() * 5*mV'
+    Q.I = '10*mV + rand() * 8*mV'
+    S = Synapses(P, Q, on_pre='v_post += w_syn', namespace=ns)
+    S.connect(p=0.05)
+    S.delay = '0.5*ms + rand() * 1*ms'
+    # monitors must be locals of the frame that calls run() (Brian collects them there)
+    s_mon = SpikeMonitor(Q)
+    r_mon = PopulationRateMonitor(Q)
+    p_mon = SpikeMonitor(P)
+    run(duration_ms * ms)
+    return dict(P=Q, G=P, spikes=s_mon, rate=r_mon, other_spikes=p_mon)
+
+
 SCENARIOS = {
     "lif_refractory": lif_refractory,
     "hetero_delays": hetero_delays,
@@ -357,4 +385,5 @@ SCENARIOS = {
     "spike_generator": spike_generator,
     "stdp": stdp,
     "gap_junctions": gap_junctions,
+    "explicit_methods": explicit_methods,
 }

@@ -58,7 +58,7 @@ def run_ref(name):
     if "state" in r:
         out["state_v"] = np.asarray(r["state"].v_[:]).copy()        # [n_rec, steps]
         out["state_idx"] = np.asarray(r["state"].record, dtype=np.int32)
-    for var in ("v", "ge", "gi", "a", "Igap"):
+    for var in ("v", "ge", "gi", "a", "Igap", "u"):
         if var in P.variables:
             out[var] = np.asarray(getattr(P, var + "_")[:]).copy()
     for var in r.get("state_extra", ()):        # more recorded variables: [n_rec, steps]
@@ -73,6 +73,11 @@ def run_ref(name):
         from brian2 import device             # the results file (get_value returns the cached initial 0)
         fn = os.path.join(device.results_dir, device.get_array_filename(r["G"].variables["_lastindex"]))
         meta["gen_lastindex"] = int(np.fromfile(fn, dtype=np.int32)[0])
+    if "other_spikes" in r:                    # a second monitored group (its raster)
+        o = r["other_spikes"]
+        out["other_i"] = np.asarray(o.i[:], dtype=np.int32)
+        out["other_ts"] = np.round(np.asarray(o.t_[:]) / 1e-4).astype(np.int32)
+        meta["other_monitor"] = o.name
     if "syn_vars" in r:                        # synaptic variables (creation order)
         for var in r["syn_vars"]:
             out["syn_" + var] = np.asarray(getattr(r["S"], var + "_")[:]).copy()

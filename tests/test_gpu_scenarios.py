@@ -21,7 +21,7 @@ pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 EXACT = {"lif_refractory": True, "hetero_delays": False, "subgroup_monitors": True, "input_group": True,
          "presynaptic_read": False, "spike_generator": True, "stdp": False,
-         "gap_junctions": True}
+         "gap_junctions": True, "explicit_methods": True}
 
 
 @pytest.mark.parametrize("name", sorted(EXACT))
@@ -39,6 +39,10 @@ def test_scenario_matches_reference(name, ctas, owner):
     assert len(out[f"sm{sm}_i"]) == meta["n_spikes"]
     np.testing.assert_array_equal(out[f"sm{sm}_i"], ref["spk_i"])
     np.testing.assert_array_equal(out[f"sm{sm}_ts"], ref["spk_ts"])
+    if "other_monitor" in meta:                   # a second monitored group
+        om = mons.index(meta["other_monitor"])
+        np.testing.assert_array_equal(out[f"sm{om}_i"], ref["other_i"])
+        np.testing.assert_array_equal(out[f"sm{om}_ts"], ref["other_ts"])
     if "gen_monitor" in meta:                     # the spike generator's raster and final cursor
         gm = mons.index(meta["gen_monitor"])
         np.testing.assert_array_equal(out[f"sm{gm}_i"], ref["gen_i"])
@@ -47,7 +51,7 @@ def test_scenario_matches_reference(name, ctas, owner):
         assert int(out[f"g{gg}_gen_last"]) == meta["gen_lastindex"]
     np.testing.assert_array_equal(out["rm0_counts"], ref["rate_counts"])
     gi = [g["name"] for g in spec["groups"]].index(meta["group"])
-    for var in ("v", "ge", "gi", "a", "Igap"):
+    for var in ("v", "ge", "gi", "a", "Igap", "u"):
         if var in ref:
             if EXACT[name]:
                 np.testing.assert_array_equal(out[f"g{gi}_{var}"], ref[var], err_msg=var)

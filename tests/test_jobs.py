@@ -34,7 +34,7 @@ def test_job_carries_the_reference_network(case, golden):
 
 
 SCENARIOS = ["lif_refractory", "hetero_delays", "subgroup_monitors", "input_group", "presynaptic_read",
-             "spike_generator", "stdp", "gap_junctions"]
+             "spike_generator", "stdp", "gap_junctions", "explicit_methods"]
 
 
 @pytest.mark.parametrize("name", SCENARIOS)

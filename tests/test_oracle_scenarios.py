@@ -31,6 +31,10 @@ def test_oracle_reproduces_reference_scenario(name):
     np.testing.assert_array_equal(out[f"sm{sm}_i"], ref["spk_i"])
     np.testing.assert_array_equal(out[f"sm{sm}_ts"], ref["spk_ts"])
     np.testing.assert_array_equal(out["rm0_counts"], ref["rate_counts"])
+    if "other_monitor" in meta:                   # a second monitored group
+        om = mons.index(meta["other_monitor"])
+        np.testing.assert_array_equal(out[f"sm{om}_i"], ref["other_i"])
+        np.testing.assert_array_equal(out[f"sm{om}_ts"], ref["other_ts"])
     if "gen_monitor" in meta:
         gm = mons.index(meta["gen_monitor"])
         np.testing.assert_array_equal(out[f"sm{gm}_i"], ref["gen_i"])
@@ -38,7 +42,7 @@ def test_oracle_reproduces_reference_scenario(name):
         gg = [g["name"] for g in spec["groups"]].index(meta["gen_group"])
         assert int(out[f"g{gg}_gen_last"]) == meta["gen_lastindex"]
     gi = [g["name"] for g in spec["groups"]].index(meta["group"])
-    for var in ("v", "ge", "gi", "a", "Igap"):
+    for var in ("v", "ge", "gi", "a", "Igap", "u"):
         if var in ref:
             np.testing.assert_array_equal(out[f"g{gi}_{var}"], ref[var], err_msg=var)
     if "state_v" in ref:
