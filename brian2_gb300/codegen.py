@@ -1247,6 +1247,7 @@ def render_model(spec: dict) -> str:
     w("      unsigned bar_old = 0u;")
     w("      bool pend = false;  // lag mode: barrier A arrived, not yet waited for")
     w("      bool lc_ok = false;  // lag mode: the tile counts were loaded right after the wait")
+    w("      bool lists_due = lagm;  // lag mode: the step's spike lists are still to do")
     for gi in range(NG):
         w(f"      int _lc{gi}[B200_LIST_RUN]; (void)_lc{gi};")
     w("      bool arrive_due = false;")
@@ -1478,6 +1479,12 @@ def render_model(spec: dict) -> str:
                 w("                }")
             w("              }")
             w("            }")
+            if (sg, pis) == (merged[0][0], merged[0][1]):
+                # lag mode: this step's spike lists while the first batch's atomics drain
+                w("            if (lists_due) {")
+                w("              lists_due = false;")
+                emit_lists()
+                w("            }")
             w("          }")
             w("          } else {")
         if True:  # the one-phase loop (always emitted; the only one without a common load signature)
@@ -1536,7 +1543,7 @@ def render_model(spec: dict) -> str:
     w("        B200_PHASE(1);")
     w("      }")
     w("      if (!ok) break;")
-    w("      if (lagm) {")
+    w("      if (lagm && lists_due) {")
     emit_lists()
     w("      }")
     w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster, rank)) { ok = false; break; }")
