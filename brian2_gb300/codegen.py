@@ -1307,10 +1307,34 @@ def render_model(spec: dict) -> str:
             out.append("const b200_pathway_d& PD = I.p[pw];")
             return _indent("\n".join(out), ind)
 
-        def emit_wait(ind):
+        def emit_wait(ind, prefetch=False):
             """Lag mode: wait for barrier A before the first atomic of the step."""
             sp = " " * ind
             w(sp + "if (pend) {")
+            if prefetch:
+                # the synapses of the later event batches: into L2 while the barrier completes
+                w(sp + "  for (int jj = threadIdx.x; jj < nitems; jj += blockDim.x) {")
+                w(sp + "    const int o0 = s_item_off[jj], o1 = (jj + 1 < nitems) ? s_item_off[jj + 1] : E;")
+                w(sp + "    if (o1 <= B200_EVENT_BATCH * (int)blockDim.x || o1 <= o0) continue;")
+                w(sp + "    const int64_t sg0 = s_item_seg[jj]; const int ln = o1 - o0; const int q = s_item_q[jj];")
+                for q, pi in enumerate(pis):
+                    lds, _ = split_loads(dict(ptables[pi][1])["on_pre"]["vector_device"] or
+                                         dict(ptables[pi][1])["on_pre"]["vector"])
+                    arrs = []
+                    p = paths[pi]
+                    for ct, nm, ptr in lds:
+                        if ptr == p["post_ptr"]:
+                            arrs.append((f"I.p[{pi}].post", 4))
+                        elif ptr == p["pre_ptr"]:
+                            arrs.append((f"I.p[{pi}].pre", 4))
+                        else:
+                            k = next(k for k, v in enumerate(p.get("vars", [])) if v["ptr"] == ptr)
+                            arrs.append((f"(const char*)I.p[{pi}].var[{k}]", SIZE[ct]))
+                    w(sp + f"    if (q == {q}) {{")
+                    for a, sz in arrs:
+                        w(sp + f"      for (int ob = 0; ob < ln * {sz}; ob += 128) b200_prefetch_l2((const char*)({a}) + sg0 * {sz} + ob);")
+                    w(sp + "    }")
+                w(sp + "  }")
             w(sp + f"  B200_PHASE({5 + NP});")
             w(sp + "  if (!b200_inst_wait(I, gen, limit_ns, cluster, rank, bar_old)) ok = false;")
             w(sp + "  pend = false;")
@@ -1445,7 +1469,7 @@ def render_model(spec: dict) -> str:
                 w("                }")
             w("              }")
             w("            }")
-            emit_wait(12)
+            emit_wait(12, prefetch=not any(paths[q].get("alias", -1) >= 0 for q in pis))
             w("#pragma unroll")
             w("            for (int qq = 0; qq < B200_EVENT_BATCH; ++qq) {")
             w("              if (_q4[qq] >= 0) {")

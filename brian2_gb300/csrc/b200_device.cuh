@@ -342,6 +342,10 @@ __device__ __forceinline__ int b200_block_compact(bool flag, int* wsum, int* tot
 
 // Block-cooperative copy of `bytes`: 4-byte words when both ends are 4-byte
 // aligned, single bytes otherwise (a 1-byte variable from a tile boundary).
+__device__ __forceinline__ void b200_prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" :: "l"(p));
+}
+
 __device__ __forceinline__ void b200_copy_bytes(void* dst, const void* src, size_t bytes) {
   if ((((uintptr_t)dst) | ((uintptr_t)src)) & 3) {
     unsigned char* db = (unsigned char*)dst;
