@@ -567,7 +567,7 @@ def render_model(spec: dict) -> str:
         if bd["threshold"] is not None and re.search(r"_ptr_array_\w+\[", thr_rest):
             return False
         nbytes = sum(QUADV[own[p_]["ctype"]][1] for p_ in pf)  # bytes per neuron prefetched
-        pfq_big = max(1, min(8, PF_WORDS // max(nbytes, 1)))  # quads in flight per thread
+        pfq_big = max(1, min(8, (2 * PF_WORDS) // max(nbytes, 1)))  # quads in flight per thread
         pfi = {ptr: j for j, ptr in enumerate(sorted(pf))}
         sti = {ptr: j for j, ptr in enumerate(sorted(upd_st))}
         vt = lambda ptr: QUADV[own[ptr]["ctype"]][0]
