@@ -3,8 +3,8 @@
 # SYMLINK tree under oracle/_ref/pyenv: no reference source is copied, only
 # linked, and the two Cython extensions the package needs are compiled next to
 # the links.  `pyparsing` is provided by a one-line shim that re-exports the copy
-# vendored inside pip.  Only this container has the reference; the tree is
-# git-ignored and gpurun-ignored.
+# vendored inside pip.  Only a host with the reference sources can build it; the
+# tree is ignored by git and left out of copies of the repository to other hosts.
 #
 # usage: bash oracle/make_ref_env.sh [/path/to/reference]
 set -euo pipefail
