@@ -266,17 +266,29 @@ class Network:
                                                _ptr(vs, _i32p), vs.size))
         self.__dict__.setdefault("_statemon_shape", {})[(inst, m)] = (vs.size, idx.size)
 
-    def spikes(self, inst=0, mon=0):
-        """(i, timestep, per-neuron count) recorded by a spike monitor."""
+    def spikes(self, inst=0, mon=0, counts=True, out=None):
+        """(i, timestep, per-neuron count) recorded by a spike monitor.
+        `counts=False` skips the per-neuron counts (None is returned for them);
+        `out=(i, ts)` reads into caller-provided int32 arrays (for instance in
+        pinned host memory) of at least the recorded length, and returns views
+        of them."""
         m = mon if isinstance(mon, int) else self.model.spkmon_index[mon]
         n = C.c_int64()
         self._check(self.lib.b200_spikemon_size(self._h, int(inst), m, C.byref(n)))
-        i = np.empty(n.value, np.int32)
-        ts = np.empty(n.value, np.int32)
-        g = self.model.spec["spike_monitors"][m]["group"]
-        cnt = np.empty(int(self.sizes[inst, g]), np.int32)
+        if out is not None:
+            i, ts = out[0][:n.value], out[1][:n.value]
+            if i.dtype != np.int32 or ts.dtype != np.int32 or i.size < n.value or ts.size < n.value or \
+                    not (i.flags.c_contiguous and ts.flags.c_contiguous):
+                raise ValueError("spikes(out=...): contiguous int32 arrays of the recorded length needed")
+        else:
+            i = np.empty(n.value, np.int32)
+            ts = np.empty(n.value, np.int32)
+        cnt = None
+        if counts:
+            g = self.model.spec["spike_monitors"][m]["group"]
+            cnt = np.empty(int(self.sizes[inst, g]), np.int32)
         self._check(self.lib.b200_spikemon_get(self._h, int(inst), m, _ptr(i, _i32p), _ptr(ts, _i32p),
-                                               _ptr(cnt, _i32p), n.value))
+                                               _ptr(cnt, _i32p) if cnt is not None else None, n.value))
         return i, ts, cnt
 
     def rate_counts(self, inst=0, mon=0):
