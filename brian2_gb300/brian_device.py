@@ -45,6 +45,7 @@ from brian2.devices.cpp_standalone.device import CPPStandaloneDevice
 from brian2.devices.device import all_devices
 from brian2.groups.neurongroup import NeuronGroup
 from brian2.groups.subgroup import Subgroup
+from brian2.input.poissongroup import PoissonGroup
 from brian2.input.spikegeneratorgroup import SpikeGeneratorGroup
 from brian2.monitors.ratemonitor import PopulationRateMonitor
 from brian2.monitors.spikemonitor import SpikeMonitor
@@ -174,7 +175,14 @@ class B200Device(CPPStandaloneDevice):
         meta = getattr(CPPStandaloneCodeObject.templater, template_name)
         for vname, var in variables.items():
             if isinstance(var, Function) and vname in ("rand", "randn", "poisson") and vname in str(abstract_code):
-                raise NotImplementedError("b200: random numbers inside the step loop are not supported")
+                # rand() in threshold code (PoissonGroup): the device continues the
+                # reference's generator stream; other random numbers are not supported
+                if not (vname == "rand" and template_name == "threshold"):
+                    raise NotImplementedError(f"b200: {vname}() inside the step loop is only supported in thresholds "
+                                              "(rand())")
+                if prefs.devices.cpp_standalone.openmp_threads:
+                    raise NotImplementedError("b200: rand() in the step loop needs openmp_threads = 0 "
+                                              "(one generator stream)")
         gen = B200CodeGenerator(variables=variables, variable_indices=variable_indices, owner=owner,
                                 iterate_all=meta.iterate_all, codeobj_class=B200CodeObject,
                                 override_conditional_write=override_conditional_write,
@@ -211,6 +219,11 @@ class B200Device(CPPStandaloneDevice):
         n_steps = int(clock._i_end - clock.variables["timestep"].get_value().item()) \
             if False else int(round(float(duration) / float(clock.dt_)))
         spec, objects = self._make_spec(net, all_objects, clock)
+        if spec.get("rng_groups") and not self.b200_runs:
+            # the generator state where the step loop starts drawing (the C++
+            # library's text form: 624 words and the position)
+            self.main_queue.append(("insert_code", '{ std::ofstream _b200_rng(brian::results_dir + "b200_rng_state"); '
+                                                   '_b200_rng << brian::_random_generators[0]; }'))
         self.b200_runs.append(dict(net=net, n_steps=n_steps, spec=spec, objects=objects, clock=clock,
                                    queue_len=len(self.main_queue)))
         self.main_queue.append(("insert_code", f"// b200 network run {len(self.b200_runs) - 1} ({n_steps} steps)"))
@@ -236,7 +249,7 @@ class B200Device(CPPStandaloneDevice):
 
         def group_of(g):
             base = g.source if isinstance(g, Subgroup) else g
-            if not isinstance(base, (NeuronGroup, SpikeGeneratorGroup)):
+            if not isinstance(base, (NeuronGroup, SpikeGeneratorGroup, PoissonGroup)):
                 raise NotImplementedError(f"b200: unsupported source/target {g!r}")
             if base.name not in group_index:
                 gv = []
@@ -292,6 +305,7 @@ class B200Device(CPPStandaloneDevice):
 
         pathways, spkmons, ratemons, statemons = [], [], [], []
         summed_frags = []
+        rng_groups = []  # groups drawing rand() in their thresholds, in schedule order
         b200_objects = []
         for obj in objects:
             if not obj.active:
@@ -312,6 +326,12 @@ class B200Device(CPPStandaloneDevice):
                         b["extra_ptrs"] = {k: list(v) for k, v in ex.items()}
                     if t == "threshold":
                         b["refractory"] = bool(frag["template_kwds"].get("_uses_refractory", False))
+                        n_rand = b["vector"].count("_rand(")
+                        if n_rand:
+                            if n_rand != 1 or "?" in b["vector"] or "&&" in b["vector"] or "||" in b["vector"]:
+                                raise NotImplementedError("b200: a threshold must draw rand() once per neuron")
+                            b["rng"] = True
+                            rng_groups.append(gi)
                         if frag["template_kwds"].get("eventspace_variable") is not None and \
                                 frag["template_kwds"]["eventspace_variable"].name != "_spikespace":
                             raise NotImplementedError("b200: custom events are not supported")
@@ -456,6 +476,8 @@ class B200Device(CPPStandaloneDevice):
                     state_monitors=statemons, clock_ptrs=clock_ptrs)
         if summed:
             spec["summed"] = summed
+        if rng_groups:
+            spec["rng_groups"] = rng_groups
         return spec, b200_objects
 
     PRIVATE_KEYS = {"_obj", "_range", "_src_range", "_tgt_range", "_vars", "_syn"}
@@ -556,6 +578,13 @@ class B200Device(CPPStandaloneDevice):
             init[f"stm{mi}_idx"] = idx + m["_range"][0]
             init[f"stm{mi}_vars"] = np.asarray(m["_vars"])
         init["ts0"] = np.int64(int(self._load(clock.variables["timestep"])[0]))
+        if spec0.get("rng_groups"):
+            with open(os.path.join(self.results_dir, "b200_rng_state")) as f:
+                st = [int(x) for x in f.read().split()]
+            if len(st) != 625:
+                raise RuntimeError("b200: unexpected generator state format")
+            init["rng_words"] = np.asarray(st[:624], np.uint32)
+            init["rng_position"] = np.int64(st[624])
         write_job(directory, pub, init, [r["n_steps"] for r in self.b200_runs], dt, self.b200_run_options)
         self.b200_job_dir = directory
         return directory

@@ -266,6 +266,7 @@ def render_model(spec: dict) -> str:
                   ("reset", _block(g.get("reset")))]
         gtables.append((_Tables(consts, blocks, (clock["t"], clock["timestep"])), blocks))
     SUMMED = spec.get("summed", [])
+    RNG = spec.get("rng_groups", [])  # groups drawing rand() in their thresholds, in draw order
     for pi, p in enumerate(paths):
         blocks = [("on_pre", _block(p.get("on_pre")))]
         blocks += [(f"summed{si}", _block(sm["code"])) for si, sm in enumerate(SUMMED) if sm["pathway"] == pi]
@@ -794,6 +795,12 @@ def render_model(spec: dict) -> str:
                 w(f"        int32_t* const scr = s_scr[{gi}]; int32_t* const tcnt = s_tc[{gi}];")
                 w(f"        int32_t* const oscr = s_oscr[{gi}]; int32_t* const otc = s_otc[{gi}];")
             w(f"        const int* const tst = s_tst + {gi} * max_tiles1;")
+            rng = bool(g.get("threshold") and g["threshold"].get("rng"))
+            if rng:
+                # rand() in the threshold: the step's words of this group, one draw per
+                # neuron in index order (the reference's order)
+                w(f"        const uint32_t* const _b200_rw = I.rng_words + ((ts - I.rng_ts0) * I.rng_per_step + I.rng_off[{gi}]) * 2;")
+                w("#define _rand(i) b200_rand_from(_b200_rw + 2 * (int64_t)(i))")
             if not SUMMED:  # (with summed variables the monitors record before those are summed)
                 emit_statemons(gi)
             # constants and block scalars are loaded once per step, not per neuron
@@ -909,6 +916,8 @@ def render_model(spec: dict) -> str:
             w("        }")
             if quad:
                 w("        }  // scalar path")
+            if rng:
+                w("#undef _rand")
             w("      }")
 
     w("__device__ __forceinline__ int b200_upper_bound(const int* a, int n, int x) {")
@@ -2397,6 +2406,8 @@ def render_model(spec: dict) -> str:
     w("  return n;")
     w("}")
     w("")
+    if RNG:
+        w("static const int b200_rng_groups[] = {" + ", ".join(str(gi) for gi in RNG) + "};")
     if SUMMED:
         w("static const b200_summed_info b200_summed[] = {" + ", ".join(
             f'{{"{sm["name"]}", {sm["pathway"]}, {sm["tgt_group"]}, {sm["tgt_var"]}, {1 if sm["index_post"] else 0}}}'
@@ -2405,7 +2416,7 @@ def render_model(spec: dict) -> str:
     w("  b200_groups, b200_pathways, b200_spkmon, b200_ratemon, b200_statemon,")
     w(f"  {len(consts)}, b200_const_names, b200_const_defaults, b200_eval_scalars, b200_launch, b200_max_active,")
     w(f"  b200_static_smem, b200_max_cluster, {NPH}, {1 if OWNER else 0}, {OWNER_EV_BYTES},")
-    w(f"  {len(SUMMED)}, {'b200_summed' if SUMMED else 'nullptr'}}};")
+    w(f"  {len(SUMMED)}, {'b200_summed' if SUMMED else 'nullptr'}, {len(RNG)}, {'b200_rng_groups' if RNG else 'nullptr'}}};")
     w("")
     w('#include "b200_host.h"')
     w("")

@@ -158,6 +158,13 @@ struct b200_inst_d {
   b200_ratemon_d rm[B200_MAX_RATEMON];
   b200_statemon_d stm[B200_MAX_STATEMON];
   b200_summed_d sum[B200_MAX_SUMMED];
+  // random numbers of the step loop (rand() in threshold code): the reference's
+  // generator stream, two 32-bit words per draw, for the launch's steps
+  const uint32_t* rng_words;  // [steps of the launch][rng_per_step][2], from step rng_ts0
+  int64_t rng_ts0;            // step of rng_words[0]
+  int32_t rng_per_step;       // draws per step (all drawing groups)
+  int32_t rng_off[B200_MAX_GROUPS];  // first draw of each group within a step
+  int32_t _pad_r;
 };
 
 static_assert(sizeof(b200_inst_d) % 8 == 0, "descriptor is copied in 8-byte words");
@@ -241,6 +248,10 @@ struct b200_model_info {
   int owner_event_bytes;  // shared-memory bytes per staged event
   int n_summed;
   const b200_summed_info* summed;
+  // groups whose threshold code draws rand() once per neuron, in the order the
+  // reference's schedule runs their thresholds (the order of the draws)
+  int n_rng_groups;
+  const int* rng_groups;
 };
 // `tcode` bit selecting the owner-mode kernel
 #define B200_TCODE_OWNER (1 << 20)
@@ -466,6 +477,74 @@ __device__ __forceinline__ bool b200_inst_wait(const b200_inst_d& I, unsigned& g
   }
   __syncthreads();
   return ok_w != 0;
+}
+
+// ---------------------------------------------------------------------------
+// The reference's random stream (brian2/devices/cpp_standalone/templates/
+// objects.cpp:426-453): a 32-bit Mersenne Twister (MT19937, Matsumoto and
+// Nishimura 1998) and rand() = (a*2^26 + b) / 2^53 from two outputs
+// a = w0 >> 5, b = w1 >> 6.  b200_mt_fill_kernel continues the generator from
+// its state (the 624 words and the position, as the C++ library stores them)
+// and writes the next `n_words` tempered outputs; one CTA of 640 threads, each
+// regeneration of the 624 words in three parallel sweeps.
+// ---------------------------------------------------------------------------
+#define B200_MT_N 624
+#define B200_MT_M 397
+__device__ __forceinline__ uint32_t b200_mt_mix(uint32_t hi, uint32_t lo, uint32_t far) {
+  const uint32_t y = (hi & 0x80000000u) | (lo & 0x7fffffffu);
+  return far ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+}
+__device__ __forceinline__ uint32_t b200_mt_temper(uint32_t y) {
+  y ^= y >> 11;
+  y ^= (y << 7) & 0x9d2c5680u;
+  y ^= (y << 15) & 0xefc60000u;
+  y ^= y >> 18;
+  return y;
+}
+// state: [624 words, position]; out: n_words outputs.  Launch <<<1, 640>>>.
+__global__ void b200_mt_fill_kernel(uint32_t* state, uint32_t* out, int64_t n_words) {
+  __shared__ uint32_t x[B200_MT_N];
+  __shared__ int s_p;
+  const int t = threadIdx.x;
+  if (t < B200_MT_N) x[t] = state[t];
+  if (t == 0) s_p = (int)state[B200_MT_N];
+  __syncthreads();
+  int p = s_p;
+  int64_t done = 0;
+  while (done < n_words) {
+    if (p >= B200_MT_N) {
+      // sequentially x[i] = x[i+M] ^ mix(x[i], x[i+1]) for i = 0..623, indices
+      // mod 624: each sweep reads the words it needs (x[i+1] before anyone
+      // writes it, the far word after the previous sweep wrote it), then writes
+      uint32_t v = 0;
+      if (t < 227) v = b200_mt_mix(x[t], x[t + 1], x[t + B200_MT_M]);
+      __syncthreads();
+      if (t < 227) x[t] = v;
+      __syncthreads();
+      if (t >= 227 && t < 454) v = b200_mt_mix(x[t], x[t + 1], x[t - 227]);
+      __syncthreads();
+      if (t >= 227 && t < 454) x[t] = v;
+      __syncthreads();
+      if (t >= 454 && t < 623) v = b200_mt_mix(x[t], x[t + 1], x[t - 227]);
+      __syncthreads();
+      if (t >= 454 && t < 623) x[t] = v;
+      __syncthreads();
+      if (t == 0) x[623] = b200_mt_mix(x[623], x[0], x[396]);
+      __syncthreads();
+      p = 0;
+    }
+    const int64_t take = (n_words - done < (int64_t)(B200_MT_N - p)) ? n_words - done : (int64_t)(B200_MT_N - p);
+    for (int k = t; k < (int)take; k += blockDim.x) out[done + k] = b200_mt_temper(x[p + k]);
+    done += take;
+    p += (int)take;
+    __syncthreads();
+  }
+  if (t < B200_MT_N) state[t] = x[t];
+  if (t == 0) state[B200_MT_N] = (uint32_t)p;
+}
+__device__ __forceinline__ double b200_rand_from(const uint32_t* w) {
+  const long long a = (long long)(w[0] >> 5), b = (long long)(w[1] >> 6);
+  return ((double)a * 67108864.0 + (double)b) / 9007199254740992.0;
 }
 
 // ---------------------------------------------------------------------------

@@ -91,6 +91,13 @@ struct b200_inst_h {
   int64_t ts = 0;
   b200_dbuf bar, status, ts_done, pending, bar64;
   int32_t ran_owner = -1;  // mode of the runs so far with spikes in flight: -1 none, 0 classic, 1 owner
+  // random stream of the step loop: generator state on the device (624 words +
+  // position), and two buffers of generated words; rng_buf[rng_cur] holds the
+  // words of steps [rng_from, rng_to), and the state is at rng_to
+  b200_dbuf rng_state, rng_buf[2];
+  int rng_cur = 0;
+  int64_t rng_from = 0, rng_to = 0;
+  bool rng_set = false;
 };
 
 struct b200_net {
@@ -255,6 +262,7 @@ int b200_destroy(b200_net* n) {
     for (auto& S : I.rm) b200_free(n, S.cnt);
     for (auto& S : I.stm) { b200_free(n, S.d_idx); b200_free(n, S.n); b200_free(n, S.data); }
     for (auto& S : I.sum) { b200_free(n, S.seg); b200_free(n, S.syn); }
+    b200_free(n, I.rng_state); b200_free(n, I.rng_buf[0]); b200_free(n, I.rng_buf[1]);
     b200_free(n, I.bar); b200_free(n, I.status); b200_free(n, I.ts_done); b200_free(n, I.pending);
     b200_free(n, I.bar64);
   }
@@ -1282,6 +1290,46 @@ int b200_run(b200_net* n, int64_t n_steps) {
       }
     }
     if (!any) break;
+    int64_t steps = n->chunk_steps;
+    if (M->n_rng_groups > 0) {
+      // the random words of the launch's steps, continuing the generator
+      int64_t per_step = 0;
+      for (int q = 0; q < M->n_rng_groups; ++q) per_step += n->inst[0].g[M->rng_groups[q]].N;
+      const int64_t wps = std::max<int64_t>(2 * per_step, 1);  // words per step
+      steps = std::max<int64_t>(1, std::min<int64_t>(steps, ((int64_t)128 << 20) / 4 / wps));
+      for (int k = 0; k < n->n_inst; ++k) {
+        b200_inst_h& I = n->inst[k];
+        b200_inst_d& D = n->h_insts[k];
+        if (!I.rng_set) return b200_fail(n, B200_ERR_ARG, "instance %d: the model draws random numbers; set the generator (b200_set_rng)", k);
+        int64_t pk = 0;
+        for (int q = 0; q < M->n_rng_groups; ++q) {
+          D.rng_off[M->rng_groups[q]] = (int32_t)pk;
+          pk += I.g[M->rng_groups[q]].N;
+        }
+        D.rng_per_step = (int32_t)pk;
+        const int64_t w_k = std::max<int64_t>(2 * pk, 1);
+        const int64_t end = std::min<int64_t>(target[k], I.ts + steps);
+        if (I.rng_from > I.ts || I.rng_to < I.ts)
+          return b200_fail(n, B200_ERR_ARG, "instance %d: random stream position lost", k);
+        if (end > I.rng_to) {
+          // move the words still unused to the other buffer, generate the rest after them
+          const int nb = 1 - I.rng_cur;
+          const int64_t keep = I.rng_to - I.ts;
+          if ((r = b200_alloc(n, I.rng_buf[nb], (size_t)std::max<int64_t>(end - I.ts, 1) * w_k * 4, false))) return r;
+          if (keep > 0)
+            B200_CU(n, cudaMemcpyAsync(I.rng_buf[nb].p, (uint32_t*)I.rng_buf[I.rng_cur].p + (I.ts - I.rng_from) * w_k,
+                                       (size_t)keep * w_k * 4, cudaMemcpyDeviceToDevice, n->stream));
+          b200_mt_fill_kernel<<<1, 640, 0, n->stream>>>((uint32_t*)I.rng_state.p,
+                                                       (uint32_t*)I.rng_buf[nb].p + keep * w_k, (end - I.rng_to) * 2 * pk);
+          B200_CU(n, cudaGetLastError());
+          I.rng_cur = nb;
+          I.rng_from = I.ts;
+          I.rng_to = end;
+        }
+        D.rng_words = (const uint32_t*)I.rng_buf[I.rng_cur].p + (I.ts - I.rng_from) * w_k;
+        D.rng_ts0 = I.ts;
+      }
+    }
     if (n->owner) {  // the split barrier counts the arrivals of this launch from 0
       for (int k = 0; k < n->n_inst; ++k) {
         n->h_insts[k].ts_base = n->inst[k].ts;
@@ -1291,7 +1339,6 @@ int b200_run(b200_net* n, int64_t n_steps) {
     B200_CU(n, cudaMemcpyAsync(n->d_insts.p, n->h_insts.data(), sizeof(b200_inst_d) * n->n_inst,
                                cudaMemcpyHostToDevice, n->stream));
     B200_CU(n, cudaMemsetAsync(n->d_work.p, 0, 16, n->stream));
-    const int64_t steps = n->chunk_steps;
 
     B200_CU(n, cudaEventRecord(k0, n->stream));
     cudaError_t le = cudaSuccess;
@@ -1480,6 +1527,36 @@ int b200_set_generator(b200_net* n, int32_t inst, int32_t group, const int32_t* 
   return 0;
 }
 
+// The random generator of the step loop (the reference's MT19937 state as the
+// C++ library stores it: 624 words and the position), continuing at the
+// current step.  Replaces the standalone program's brian::_random_generators[0]
+// (brian2/devices/cpp_standalone/templates/objects.cpp:426-453).
+int b200_set_rng(b200_net* n, int32_t inst, const uint32_t* words, int32_t position) {
+  if (!n || inst < 0 || inst >= n->n_inst || !words || position < 0 || position > 624)
+    return b200_fail(n, B200_ERR_ARG, "bad generator state");
+  b200_inst_h& I = n->inst[inst];
+  int r;
+  if ((r = b200_alloc(n, I.rng_state, 625 * 4, false))) return r;
+  std::vector<uint32_t> st(words, words + 624);
+  st.push_back((uint32_t)position);
+  B200_CU(n, cudaMemcpy(I.rng_state.p, st.data(), 625 * 4, cudaMemcpyHostToDevice));
+  I.rng_from = I.rng_to = I.ts;
+  I.rng_set = true;
+  return 0;
+}
+
+// The generator's state after the words generated so far (words the step loop
+// has not consumed yet are included: `unused` reports how many steps of them).
+int b200_get_rng(b200_net* n, int32_t inst, uint32_t* words, int32_t* position, int64_t* unused_steps) {
+  if (!n || inst < 0 || inst >= n->n_inst || !n->inst[inst].rng_set) return b200_fail(n, B200_ERR_ARG, "no generator");
+  std::vector<uint32_t> st(625);
+  B200_CU(n, cudaMemcpy(st.data(), n->inst[inst].rng_state.p, 625 * 4, cudaMemcpyDeviceToHost));
+  if (words) memcpy(words, st.data(), 624 * 4);
+  if (position) *position = (int32_t)st[624];
+  if (unused_steps) *unused_steps = n->inst[inst].rng_to - n->inst[inst].ts;
+  return 0;
+}
+
 // The generator's cursor after a run (the `_lastindex` the reference keeps).
 int b200_get_generator(b200_net* n, int32_t inst, int32_t group, int32_t* last) {
   if (!n || inst < 0 || inst >= n->n_inst || group < 0 || group >= n->M->n_groups || !last ||
@@ -1537,6 +1614,7 @@ int b200_get_step(b200_net* n, int32_t inst, int64_t* ts) {
 int b200_set_step(b200_net* n, int32_t inst, int64_t ts) {
   if (!n || inst < 0 || inst >= n->n_inst || ts < 0) return B200_ERR_ARG;
   n->inst[inst].ts = ts;
+  n->inst[inst].rng_from = n->inst[inst].rng_to = ts;  // (the random stream continues from the generator)
   return 0;
 }
 

@@ -73,6 +73,8 @@ def _declare(lib):
         "b200_owner_active": [h, _i32p],
         "b200_set_event_capacity": [h, C.c_double],
         "b200_set_generator": [h, C.c_int32, C.c_int32, _i32p, _i32p, C.c_int64, C.c_int32, C.c_int32],
+        "b200_set_rng": [h, C.c_int32, C.POINTER(C.c_uint32), C.c_int32],
+        "b200_get_rng": [h, C.c_int32, C.POINTER(C.c_uint32), _i32p, _i64p],
         "b200_get_generator": [h, C.c_int32, C.c_int32, _i32p],
         "b200_launch_plan": [h, _i32p, _i32p, _i32p],
         "b200_profile_phases": [h, _i32p],
@@ -241,6 +243,21 @@ class Network:
             raise ValueError("timebins and indices differ in length")
         self._check(self.lib.b200_set_generator(self._h, int(inst), g, _ptr(b, _i32p), _ptr(i, _i32p), b.size,
                                                 int(period_bins), int(last)))
+
+    def set_rng(self, inst, words, position):
+        """The random generator of the step loop: the reference's MT19937 state
+        (624 words and the position, as the C++ library stores them)."""
+        w = np.ascontiguousarray(words, dtype=np.uint32)
+        if w.size != 624:
+            raise ValueError("624 state words expected")
+        self._check(self.lib.b200_set_rng(self._h, int(inst), _ptr(w, C.POINTER(C.c_uint32)), int(position)))
+
+    def rng_state(self, inst=0):
+        """(words, position, steps generated ahead and not yet consumed)."""
+        w = np.zeros(624, np.uint32)
+        p, u = C.c_int32(), C.c_int64()
+        self._check(self.lib.b200_get_rng(self._h, int(inst), _ptr(w, C.POINTER(C.c_uint32)), C.byref(p), C.byref(u)))
+        return w, int(p.value), int(u.value)
 
     def generator_cursor(self, inst, group):
         """The generator's cursor (the reference's `_lastindex`)."""

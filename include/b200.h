@@ -79,6 +79,17 @@ int b200_set_event_capacity(b200_net* net, double factor);
 int b200_set_generator(b200_net* net, int32_t inst, int32_t group, const int32_t* bins, const int32_t* index,
                        int64_t count, int32_t period_bins, int32_t last);
 int b200_get_generator(b200_net* net, int32_t inst, int32_t group, int32_t* last);
+/* The random generator of the step loop, for models whose threshold code draws
+ * rand() once per neuron (PoissonGroup, brian2/input/poissongroup.py): the
+ * reference's MT19937 state as the C++ library stores it (624 words, then the
+ * position), taken where the standalone program starts the run
+ * (brian::_random_generators[0], templates/objects.cpp:426-453).  The device
+ * continues that stream in the reference's order of draws (groups in schedule
+ * order, neurons in index order, rand() = (a*2^26 + b)/2^53 of two outputs).
+ * b200_get_rng returns the generator state and the steps of words generated
+ * ahead of the current step. */
+int b200_set_rng(b200_net* net, int32_t inst, const uint32_t* words, int32_t position);
+int b200_get_rng(b200_net* net, int32_t inst, uint32_t* words, int32_t* position, int64_t* unused_steps);
 /* Per-instance values of the model's namespace constants (the %CONSTANTS% of the
  * generated code objects, device.py:936-940); scalar blocks are re-evaluated. */
 int b200_set_consts(b200_net* net, int32_t inst, const double* values, int32_t count);

@@ -376,6 +376,34 @@ def explicit_methods(N=300, duration_ms=150.0, seed_value=91):
     return dict(P=Q, G=P, spikes=s_mon, rate=r_mon, other_spikes=p_mon)
 
 
+def poisson_input(N_in=300, N=200, duration_ms=200.0, seed_value=101):
+    """A PoissonGroup (rates 5-45 Hz, a draw of the reference's generator per
+    neuron and step) driving a CUBA population through synapses with delays;
+    a second PoissonGroup at a uniform rate draws after it."""
+    import numpy as np
+    from brian2 import (NeuronGroup, PoissonGroup, Synapses, SpikeMonitor, PopulationRateMonitor,
+                        ms, mV, Hz, seed, run)
+    seed(seed_value)
+    G = PoissonGroup(N_in, rates=(5 + 40 * np.arange(N_in) / N_in) * Hz)
+    H = PoissonGroup(50, rates=30 * Hz)
+    ns = dict(taum=20 * ms, taue=5 * ms, Vt=-50 * mV, Vr=-60 * mV, El=-60 * mV, w_in=1.5 * mV, w_h=2 * mV)
+    P = NeuronGroup(N, '''dv/dt  = (ge-(v-El))/taum : volt
+                          dge/dt = -ge/taue : volt''',
+                    threshold='v>Vt', reset='v = Vr', method='exact', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    S = Synapses(G, P, on_pre='ge += w_in', namespace=ns)
+    S.connect(p=0.1)
+    S.delay = 'rand() * 2*ms'
+    T = Synapses(H, P, on_pre='ge += w_h', namespace=ns)
+    T.connect(p=0.2)
+    # monitors must be locals of the frame that calls run() (Brian collects them there)
+    s_mon = SpikeMonitor(P)
+    r_mon = PopulationRateMonitor(P)
+    g_mon = SpikeMonitor(G)
+    run(duration_ms * ms)
+    return dict(P=P, spikes=s_mon, rate=r_mon, other_spikes=g_mon)
+
+
 SCENARIOS = {
     "lif_refractory": lif_refractory,
     "hetero_delays": hetero_delays,
@@ -386,4 +414,5 @@ SCENARIOS = {
     "stdp": stdp,
     "gap_junctions": gap_junctions,
     "explicit_methods": explicit_methods,
+    "poisson_input": poisson_input,
 }

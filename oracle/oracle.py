@@ -22,6 +22,10 @@ code objects, and executes the spec's *plain* C++ snippets (Brian's own
   (templates/synapses_push_spikes.cpp:24-28, synapses/spikequeue.h:146-205,
   templates/synapses.cpp:20-49);
 * reset for each spike (templates/reset.cpp:16-22);
+* rand() in thresholds (PoissonGroup): the reference's generator,
+  std::mt19937 continued from the state the standalone program had at the
+  run, rand() = (a*2^26 + b)/2^53 of two outputs (templates/objects.cpp:
+  426-453), drawing groups in schedule order and neurons in index order;
 * summed variables: the target range zeroed, then the expression of every
   synapse in creation order added to its target (templates/summed_variable.cpp:
   11-25), after the state monitors and before the state updates;
@@ -85,8 +89,19 @@ def render_oracle(spec: dict) -> str:
     w("template <typename T> static inline int int_(T v) { return (int)v; }")
     w("static inline int64_t _timestep(double t, double dt) { return (int64_t)((t + 1e-3 * dt) / dt); }")
     w("#define _brian_abs fabs")
+    RNG = spec.get("rng_groups", [])
+    if RNG:
+        w("#include <random>\n#include <sstream>\n#include <string>")
+        w("static std::mt19937* _b200_gen = nullptr;")
+        w("static inline double _rand(int64_t) {")
+        w("  const long a = (long)((*_b200_gen)() >> 5);")
+        w("  const long b = (long)((*_b200_gen)() >> 6);")
+        w("  return (a * 67108864.0 + b) / 9007199254740992.0;")
+        w("}")
     w("struct Net {")
     w("  double dt; int64_t ts = 0;")
+    if RNG:
+        w("  std::mt19937 gen;")
     w("  std::vector<double> c;")
     for gi, g in enumerate(groups):
         w(f"  int32_t N{gi} = 0;")
@@ -171,6 +186,13 @@ def render_oracle(spec: dict) -> str:
     w("  return -1;")
     w("}")
     w("void oracle_set_step(Net* n, int64_t ts) { n->ts = ts; }")
+    w("void oracle_set_rng(Net* n, const uint32_t* words, int32_t pos) {")
+    if RNG:  # (the C++ library's text form of the state: the 624 words, then the position)
+        w("  std::ostringstream o; for (int k = 0; k < 624; ++k) o << words[k] << ' '; o << pos;")
+        w("  std::istringstream in(o.str()); in >> n->gen;")
+    else:
+        w("  (void)n; (void)words; (void)pos;")
+    w("}")
     w("void oracle_set_range(Net* n, int32_t kind, int32_t mon, int32_t lo, int32_t hi) {")
     for mi, m in enumerate(spkmons):
         w(f"  if (kind == 0 && mon == {mi}) {{ n->sm{mi}_lo = lo; n->sm{mi}_hi = hi; n->sm{mi}_count.assign(hi - lo, 0); }}")
@@ -184,6 +206,8 @@ def render_oracle(spec: dict) -> str:
 
     # ---- the step loop
     w("void oracle_run(Net* n, int64_t n_steps) {")
+    if RNG:
+        w("  _b200_gen = &n->gen;")
     for k, cst in enumerate(consts):
         w(f"  const {cst['ctype']} {cst['name']} = ({cst['ctype']})n->c[{k}]; (void){cst['name']};")
     w("  const double _dt_v = n->dt;")
@@ -261,8 +285,9 @@ def render_oracle(spec: dict) -> str:
         w("        }")
         w("      }")
         w("    }")
-    # thresholders
-    for gi, g in enumerate(groups):
+    # thresholders (those drawing random numbers last, in the schedule's order)
+    for gi in [k for k in range(len(groups)) if k not in RNG] + list(RNG):
+        g = groups[gi]
         w("    {")
         w(gptrs(gi, 6))
         w(f"      const int32_t N = n->N{gi}; (void)N;")
@@ -421,6 +446,7 @@ class OracleNet:
             lib.oracle_get_generator.argtypes = [C.c_void_p, C.c_int32]
             lib.oracle_get_generator.restype = C.c_int32
             lib.oracle_set_step.argtypes = [C.c_void_p, C.c_int64]
+            lib.oracle_set_rng.argtypes = [C.c_void_p, C.POINTER(C.c_uint32), C.c_int32]
         self.lib = lib
         self.sizes = np.ascontiguousarray(sizes, dtype=np.int32).reshape(-1)
         self.h = lib.oracle_create(self.sizes.ctypes.data_as(_i32p), float(dt))
@@ -520,6 +546,10 @@ class OracleNet:
     def set_step(self, ts):
         self.lib.oracle_set_step(self.h, int(ts))
 
+    def set_rng(self, words, position):
+        w = np.ascontiguousarray(words, np.uint32)
+        self.lib.oracle_set_rng(self.h, w.ctypes.data_as(C.POINTER(C.c_uint32)), int(position))
+
     def run(self, n_steps):
         self.lib.oracle_run(self.h, int(n_steps))
 
@@ -606,6 +636,8 @@ def run_job_on_oracle(directory):
     for mi in range(len(spec.get("state_monitors", []))):
         o.set_statemon(mi, init[f"stm{mi}_idx"], list(init[f"stm{mi}_vars"]))
     o.set_step(int(init["ts0"]))
+    if spec.get("rng_groups"):
+        o.set_rng(init["rng_words"], int(init["rng_position"]))
     for n in job["runs"]:
         o.run(int(n))
     out = {}

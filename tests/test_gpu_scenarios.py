@@ -21,7 +21,7 @@ pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 EXACT = {"lif_refractory": True, "hetero_delays": False, "subgroup_monitors": True, "input_group": True,
          "presynaptic_read": False, "spike_generator": True, "stdp": False,
-         "gap_junctions": True, "explicit_methods": True}
+         "gap_junctions": True, "explicit_methods": True, "poisson_input": False}
 
 
 @pytest.mark.parametrize("name", sorted(EXACT))

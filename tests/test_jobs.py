@@ -34,7 +34,7 @@ def test_job_carries_the_reference_network(case, golden):
 
 
 SCENARIOS = ["lif_refractory", "hetero_delays", "subgroup_monitors", "input_group", "presynaptic_read",
-             "spike_generator", "stdp", "gap_junctions", "explicit_methods"]
+             "spike_generator", "stdp", "gap_junctions", "explicit_methods", "poisson_input"]
 
 
 @pytest.mark.parametrize("name", SCENARIOS)
@@ -51,6 +51,11 @@ def test_scenario_jobs_describe_their_features(name):
         assert list(init["stm0_idx"]) == [0, 10, 250, 499]
     if name == "input_group":
         assert len(spec["groups"]) == 2 and {p["src"] for p in spec["pathways"]} == {0, 1}
+    if name == "poisson_input":  # rand() in two PoissonGroups' thresholds: the generator state travels
+        assert len(spec["rng_groups"]) == 2 and init["rng_words"].dtype == np.uint32
+        assert init["rng_words"].size == 624 and 0 <= int(init["rng_position"]) <= 624
+        for gi in spec["rng_groups"]:
+            assert spec["groups"][gi]["threshold"]["rng"] and "_rand(" in spec["groups"][gi]["threshold"]["vector"]
     if name == "gap_junctions":  # a summed variable over a Synapses object without on_pre
         (sm,) = spec["summed"]
         pw = spec["pathways"][sm["pathway"]]
