@@ -194,3 +194,27 @@ def test_owner_equals_classic_on_device_built_network():
     np.testing.assert_array_equal(t0, t1)
     np.testing.assert_array_equal(v0, v1)
     np.testing.assert_array_equal(g0, g1)
+
+
+@pytest.mark.parametrize("shape", [dict(threads=256, ctas_per_inst=1), dict(threads=256, ctas_per_inst=20, owner=False),
+                                   dict(threads=128, ctas_per_inst=4, owner=False),
+                                   dict(threads=256, ctas_per_inst=8, owner=True)])
+def test_long_delays_match_oracle(shape):
+    """Delays up to 25 ms (251 ring slots): more slots than a CTA keeps the
+    spike bounds of in shared memory, so the delivery windows read the slot
+    bounds from global memory; split runs carry the spikes in flight across
+    launches."""
+    spec = W.load_spec("delays_f64")
+    b = W.build_delays(spec, N=2000, K=100, seed=9, dmin_ms=0.1, dmax_ms=25.0)
+    o = oracle_from_built(spec, b)
+    o.run(1500)
+    net = make_net(spec, b, shape)
+    for chunk in (1, 300, 1199):
+        net.run(chunk)
+    i, ts, _ = net.spikes(0, 0)
+    oi, ots, _ = o.spikes(0)
+    assert len(oi) > 100
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(ts, ots)
+    for var in ("v", "ge", "gi"):
+        np.testing.assert_array_equal(net.download(0, "neurongroup", var), o.download(0, var), err_msg=var)
