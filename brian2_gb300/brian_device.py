@@ -23,14 +23,17 @@ How the work is split with Brian's own machinery (the device subclasses
 
 Limits (raise ``NotImplementedError``, which Brian's test runner treats as
 "not supported by this device"): one clock for all step-loop objects; no host
-code between two ``run()`` calls; random numbers inside the step loop; on_pre
-statements that write a postsynaptic/presynaptic variable other than by
-``+=``/``-=``; on_post pathways; monitors with ``when`` other than the default
-slots; summed variables.
+code between two ``run()`` calls; random numbers inside the step loop other
+than one ``rand()`` per neuron in threshold code (PoissonGroup) and the
+binomial draws of ``PoissonInput`` without its normal approximation (both need
+``openmp_threads = 0``); synaptic statements that write a neuron variable
+other than by ``+=``/``-=``; state monitors outside the ``start`` slot; custom
+events.
 """
 from __future__ import annotations
 
 import os
+import re
 import time
 
 import numpy as np
@@ -45,7 +48,9 @@ from brian2.devices.cpp_standalone.device import CPPStandaloneDevice
 from brian2.devices.device import all_devices
 from brian2.groups.neurongroup import NeuronGroup
 from brian2.groups.subgroup import Subgroup
+from brian2.input.binomial import BinomialFunction
 from brian2.input.poissongroup import PoissonGroup
+from brian2.input.poissoninput import PoissonInput
 from brian2.input.spikegeneratorgroup import SpikeGeneratorGroup
 from brian2.monitors.ratemonitor import PopulationRateMonitor
 from brian2.monitors.spikemonitor import SpikeMonitor
@@ -58,6 +63,18 @@ logger = get_logger(__name__)
 
 STEP_TEMPLATES = {"stateupdate", "threshold", "reset", "synapses", "synapses_push_spikes",
                   "spikemonitor", "ratemonitor", "statemonitor", "spikegenerator", "summed_variable"}
+
+# the constants of Brian's C++ binomial sampler by inversion, as it prints them
+# (brian2/input/binomial.py:93-141): qn, bound, n, P, Q and the returned count
+_NUM = r"([-+0-9.eE]+)"
+_BINOM_RE = re.compile(r"double px = " + _NUM + r";.*?if \(X > " + _NUM + r"\).*?"
+                       r"px = \(\((\d+)-X\+1\) \* " + _NUM + r" \* px\)/\(X\*" + _NUM + r"\);.*?"
+                       r"return ([^;]+);", re.S)
+
+
+def draws_random(spec):
+    """Whether the step loop of a spec draws from the reference's generator."""
+    return bool(spec.get("rng_groups") or spec.get("inputs"))
 
 
 class B200CodeGenerator(CPPCodeGenerator):
@@ -174,6 +191,14 @@ class B200Device(CPPStandaloneDevice):
         name = find_name(name)
         meta = getattr(CPPStandaloneCodeObject.templater, template_name)
         for vname, var in variables.items():
+            if isinstance(var, BinomialFunction):
+                # a PoissonInput's binomial draws (a state update of its target group):
+                # the device continues the reference's stream
+                if template_name != "stateupdate":
+                    raise NotImplementedError("b200: binomial functions in the step loop are only supported "
+                                              "in PoissonInput")
+                if prefs.devices.cpp_standalone.openmp_threads:
+                    raise NotImplementedError("b200: PoissonInput needs openmp_threads = 0 (one generator stream)")
             if isinstance(var, Function) and vname in ("rand", "randn", "poisson") and vname in str(abstract_code):
                 # rand() in threshold code (PoissonGroup): the device continues the
                 # reference's generator stream; other random numbers are not supported
@@ -219,7 +244,7 @@ class B200Device(CPPStandaloneDevice):
         n_steps = int(clock._i_end - clock.variables["timestep"].get_value().item()) \
             if False else int(round(float(duration) / float(clock.dt_)))
         spec, objects = self._make_spec(net, all_objects, clock)
-        if spec.get("rng_groups") and not self.b200_runs:
+        if draws_random(spec) and not self.b200_runs:
             # the generator state where the step loop starts drawing (the C++
             # library's text form: 624 words and the position)
             self.main_queue.append(("insert_code", '{ std::ofstream _b200_rng(brian::results_dir + "b200_rng_state"); '
@@ -305,6 +330,7 @@ class B200Device(CPPStandaloneDevice):
 
         pathways, spkmons, ratemons, statemons = [], [], [], []
         summed_frags = []
+        input_frags = []  # PoissonInputs, in schedule order
         rng_groups = []  # groups drawing rand() in their thresholds, in schedule order
         b200_objects = []
         for obj in objects:
@@ -316,7 +342,9 @@ class B200Device(CPPStandaloneDevice):
                 frag = co.fragment
                 t = frag["template"]
                 b200_objects.append((obj, co))
-                if t in ("stateupdate", "threshold", "reset"):
+                if isinstance(obj, PoissonInput):
+                    input_frags.append((obj, frag))
+                elif t in ("stateupdate", "threshold", "reset"):
                     gi, _ = group_of(obj.group)
                     g = groups[gi]
                     key = {"stateupdate": "update"}.get(t, t)
@@ -447,6 +475,58 @@ class B200Device(CPPStandaloneDevice):
                                tgt_var=tnames.index(tkw["_target_var"].name),
                                index_post=tkw["_index_var"].name == "_synaptic_post",
                                group_ptrs=neuron_ptrs(frag), code=block(frag)))
+        # Poisson inputs (brian2/input/poissoninput.py:20-141): a state update in the
+        # synapses slot, after the on_pre pathways (order -1) and before the
+        # on_post pathways (order +1), drawing one binomial count per neuron
+        inputs = []
+        for obj, frag in input_frags:
+            if obj.when != "synapses" or obj.order != 0:
+                raise NotImplementedError("b200: PoissonInput runs in the synapses slot with order 0")
+            fns = [v for v in frag["variables"].values() if isinstance(v, BinomialFunction)]
+            if len(fns) != 1:
+                raise NotImplementedError("b200: unsupported PoissonInput code")
+            fn = fns[0]
+            support = fn.implementations[CPPCodeGenerator].get_code(None)["support_code"]
+            m = _BINOM_RE.search(support)
+            if m is None:
+                raise NotImplementedError("b200: PoissonInput with N*rate*dt > 5 and N*(1-rate*dt) > 5 (Brian "
+                                          "samples a normal approximation with randn())")
+            qn, bound, n_str, P, Q, ret = m.groups()
+            ret = ret.strip().replace(" ", "")
+            if ret not in ("X", f"{n_str}-X"):
+                raise NotImplementedError("b200: unsupported binomial sampler")
+            gi, (lo, hi) = group_of(obj.group)
+            g = groups[gi]
+            b = block(frag)
+            k = len(inputs)
+            vec = b["vector"]
+            if vec.count(fn.name + "(") != 1 or b.get("vector_device"):
+                raise NotImplementedError("b200: unsupported PoissonInput code")
+            vec = re.sub(r"\b%s\(" % re.escape(fn.name), f"_b200_binomial_{k}(", vec)
+            whole = not isinstance(obj.group, Subgroup)
+            if not whole:  # the subgroup's index array is the contiguous range itself
+                sub = gen_name(obj.group.variables["_sub_idx"])
+                vec = re.sub(re.escape(sub) + r"\s*\[\s*_idx\s*\]", "_b200_abs_idx", vec)
+            names = {v["ptr"] for v in g["vars"]}
+            for ptr in set(re.findall(r"_ptr_array_\w+", vec + b["scalar"])):
+                if ptr not in names and ptr not in clock_ptrs.values():
+                    raise NotImplementedError(f"b200: PoissonInput code reads {ptr} (not a state variable "
+                                              "of its target group)")
+            if collect(frag, {g["name"]}):
+                raise NotImplementedError("b200: PoissonInput reads another group's variables")
+            tv = g["vars"][[v["name"] for v in g["vars"]].index(obj.target_var)]["ptr"] \
+                if obj.target_var in [v["name"] for v in g["vars"]] else None
+            for p in pathways:
+                if p.get("prepost") == "post" and tv in p.get("group_ptrs", {}):
+                    raise NotImplementedError("b200: PoissonInput into a variable an on_post pathway writes")
+            for sm in summed:
+                if sm["tgt_group"] == gi and g["vars"][sm["tgt_var"]]["ptr"] == tv:
+                    raise NotImplementedError("b200: PoissonInput into a summed variable")
+            inputs.append(dict(name=obj.name, group=gi, lo=int(lo), hi=-1 if whole else int(hi),
+                               code=dict(scalar=b["scalar"], vector=vec),
+                               binom=dict(qn=qn, bound=bound, n=int(n_str), p=P, q=Q, reverse=ret != "X")))
+        if len(inputs) > 4:
+            raise NotImplementedError("b200: more than 4 PoissonInputs")
         # pathways of one Synapses object (on_pre and on_post) share its synapses and
         # synaptic variables: the first one in schedule order owns them, the others
         # alias it; all carry the union of the variables their code uses
@@ -478,6 +558,8 @@ class B200Device(CPPStandaloneDevice):
             spec["summed"] = summed
         if rng_groups:
             spec["rng_groups"] = rng_groups
+        if inputs:
+            spec["inputs"] = inputs
         return spec, b200_objects
 
     PRIVATE_KEYS = {"_obj", "_range", "_src_range", "_tgt_range", "_vars", "_syn"}
@@ -578,7 +660,7 @@ class B200Device(CPPStandaloneDevice):
             init[f"stm{mi}_idx"] = idx + m["_range"][0]
             init[f"stm{mi}_vars"] = np.asarray(m["_vars"])
         init["ts0"] = np.int64(int(self._load(clock.variables["timestep"])[0]))
-        if spec0.get("rng_groups"):
+        if draws_random(spec0):
             with open(os.path.join(self.results_dir, "b200_rng_state")) as f:
                 st = [int(x) for x in f.read().split()]
             if len(st) != 625:

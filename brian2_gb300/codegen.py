@@ -259,11 +259,37 @@ def render_model(spec: dict) -> str:
     w("static const char* const b200_const_names[] = {" + ", ".join(f'"{c["name"]}"' for c in consts) + ("" if consts else '""') + "};")
     w("static const double b200_const_defaults[] = {" + ", ".join(c_literal(c["value"], "double") for c in consts) + ("" if consts else "0.0") + "};")
     w("")
+    for k, inp in enumerate(spec.get("inputs", [])):
+        bn = inp["binom"]
+        w(f"// Poisson input {k} '{inp['name']}': the reference's binomial sampler by inversion")
+        w("// (brian2/input/binomial.py:93-141) with its constants as the reference prints them;")
+        w("// one draw (two words of the stream).  The reference draws again when the count")
+        w("// passes the bound (probability < 1e-15): flagged, since the stream's layout gives")
+        w("// one draw per neuron and step.")
+        w(f"__device__ __forceinline__ long long b200_binomial_{k}(const uint32_t* _w, bool& _rej) {{")
+        w("  long long X = 0;")
+        w(f"  double px = {bn['qn']};")
+        w("  double U = b200_rand_from(_w);")
+        w("  while (U > px) {")
+        w("    X++;")
+        w(f"    if (X > {bn['bound']}) {{ _rej = true; X = 0; break; }}")
+        w("    U -= px;")
+        w(f"    px = (({bn['n']} - X + 1) * {bn['p']} * px) / (X * {bn['q']});")
+        w("  }")
+        w(f"  return {str(bn['n']) + ' - X' if bn['reverse'] else 'X'};")
+        w("}")
+        w("")
 
+    # Poisson inputs (PoissonInput), in schedule order: their scalar code sits in
+    # their target group's table, their vector code runs over the group's neurons
+    INPUTS = [dict(inp, code=dict(inp["code"], vector=_device(inp["code"]["vector"])))
+              for inp in spec.get("inputs", [])]
+    assert len(INPUTS) <= 4
     gtables, ptables = [], []
-    for g in groups:
+    for gi, g in enumerate(groups):
         blocks = [("update", _block(g.get("update"))), ("threshold", _block(g.get("threshold"))),
                   ("reset", _block(g.get("reset")))]
+        blocks += [(f"input{k}", _block(inp["code"])) for k, inp in enumerate(INPUTS) if inp["group"] == gi]
         gtables.append((_Tables(consts, blocks, (clock["t"], clock["timestep"])), blocks))
     SUMMED = spec.get("summed", [])
     RNG = spec.get("rng_groups", [])  # groups drawing rand() in their thresholds, in draw order
@@ -281,6 +307,9 @@ def render_model(spec: dict) -> str:
         for blk in ("update", "threshold", "reset"):
             if g.get(blk):
                 text += g[blk].get("vector", "") + "\n" + json.dumps(g[blk].get("extra_ptrs", {}))
+        for inp in INPUTS:
+            if inp["group"] == gi:
+                text += inp["code"]["vector"] + "\n"
         for p in paths:
             text += (p["on_pre"].get("vector_device") or p["on_pre"].get("vector", "")) + json.dumps(p.get("group_ptrs", {}))
         for sm in SUMMED:
@@ -482,6 +511,54 @@ def render_model(spec: dict) -> str:
              "  }",
              "}"]
         return _indent("\n".join(L), indent)
+
+    def input_block(gi, indent, tsexpr):
+        """The Poisson inputs into group gi of step `tsexpr`, over this CTA's
+        neurons: the reference runs them in the synapses slot, after every
+        on_pre delivery of the step and before the resets
+        (brian2/input/poissoninput.py:126-135, templates/stateupdate.cpp:5-21)."""
+        ins = [(k, inp) for k, inp in enumerate(INPUTS) if inp["group"] == gi]
+        if not ins:
+            return ""
+        tab, _ = gtables[gi]
+        L = ["{",
+             f"  const double _b200_t = (double)({tsexpr}) * _b200_dt; (void)_b200_t;  // the step of the inputs",
+             f"  const int64_t _b200_ts = {tsexpr}; (void)_b200_ts;",
+             f"  const int32_t N = I.g[{gi}].N; (void)N;",
+             f"  const double* const _b200_S = s_Sg{gi}; const float* const _b200_Sf = s_Sg{gi}f; const long long* const _b200_Si = s_Sg{gi}i;",
+             gptr_decls(gi, 2, False),
+             f"  const int _own0 = s_tst[{gi} * max_tiles1 + s_ut[{gi}][0]], _own1 = s_tst[{gi} * max_tiles1 + s_ut[{gi}][1]];",
+             "  bool _b200_rej = false;"]
+        for q, (k, inp) in enumerate(ins):
+            hi = str(inp["hi"]) if inp["hi"] >= 0 else "N"
+            if q:
+                L.append("  __syncthreads();  // (inputs into one variable add in schedule order)")
+            L += [f"  {{  // Poisson input {k} '{inp['name']}'",
+                  f"    const int _lo = {inp['lo']}, _hi = {hi};",
+                  f"    const uint32_t* const _b200_rw = I.rng_words + ((({tsexpr}) - I.rng_ts0) * I.rng_per_step + I.rng_in_off[{k}]) * 2;",
+                  f"#define _b200_binomial_{k}(i) b200_binomial_{k}(_b200_rw + 2 * (int64_t)(i), _b200_rej)",
+                  _indent(tab.device_loads(f"input{k}", f32), 4),
+                  _indent(_device(tab.time_code(f"input{k}")), 4),
+                  "    const int _a = _own0 > _lo ? _own0 : _lo, _b = _own1 < _hi ? _own1 : _hi;",
+                  "    for (int _b200_abs_idx = _a + (int)threadIdx.x; _b200_abs_idx < _b; _b200_abs_idx += (int)blockDim.x) {",
+                  "      const int32_t _idx = _b200_abs_idx - _lo;",
+                  "      const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;",
+                  "      {",
+                  _indent(inp["code"]["vector"], 8),
+                  "      }",
+                  "    }",
+                  f"#undef _b200_binomial_{k}",
+                  "  }"]
+        L += ["  if (_b200_rej) atomicCAS(I.status, 0, B200_ERR_RANDOM);", "}"]
+        return _indent("\n".join(L), indent)
+
+    def deferred_block(gi, indent, tsexpr, owner=False):
+        """What the reference runs after the deliveries of step `tsexpr`: the
+        Poisson inputs, then the reset (this CTA's neurons)."""
+        a, b = input_block(gi, indent, tsexpr), reset_block(gi, indent, tsexpr, owner)
+        if a and b:
+            return a + "\n" + " " * indent + "__syncthreads();\n" + b
+        return a or b
 
     def emit_generator(gi, owner):
         """A spike generator group's step (templates/spikegenerator.cpp:5-31):
@@ -724,6 +801,9 @@ def render_model(spec: dict) -> str:
             w("          }")
             w(f"          if (threadIdx.x == 0) s_stm_n[{mi}] = ts + 1 - SM.step0;")
             w("        }")
+        if any(m["group"] == gi for m in statemons):
+            # (the update that follows overwrites what other threads recorded here)
+            w("        __syncthreads();")
 
     def emit_summed(si):
         """Summed variable si (templates/summed_variable.cpp:11-25): each of
@@ -779,9 +859,10 @@ def render_model(spec: dict) -> str:
                 emit_generator(gi, owner)
                 continue
             w(f"      // ---- group {gi} '{g['name']}': phase A (reset of step ts-1, monitors, update + threshold)")
-            if bd["reset"] is not None and not SUMMED:  # (with summed variables: before the sums)
+            dfr = deferred_block(gi, 8, "ts - 1", owner)
+            if dfr and not SUMMED:  # (with summed variables: before the sums)
                 w("      if (ts > ts0) {")
-                w(reset_block(gi, 8, "ts - 1", owner))
+                w(dfr)
                 w("        __syncthreads();")
                 w("      }")
             w("      {")
@@ -1131,9 +1212,10 @@ def render_model(spec: dict) -> str:
         # every CTA has applied its resets before any sums, and finishes its sums
         # before any update
         for gi in range(NG):
-            if dict(gtables[gi][1])["reset"] is not None:
+            dfr = deferred_block(gi, 8, "ts - 1")
+            if dfr:
                 w("      if (ts > ts0) {")
-                w(reset_block(gi, 8, "ts - 1"))
+                w(dfr)
                 w("      }")
         w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster, rank)) { ok = false; break; }")
         for gi in range(NG):
@@ -1591,7 +1673,7 @@ def render_model(spec: dict) -> str:
     w("      const double _b200_t = (double)(ts - 1) * _b200_dt; (void)_b200_t;")
     w("      const int64_t _b200_ts = ts - 1;")
     for gi in range(NG):
-        rb = reset_block(gi, 6, "ts - 1")
+        rb = deferred_block(gi, 6, "ts - 1")
         if rb:
             w(rb)
     w("    }")
@@ -2280,7 +2362,7 @@ def render_model(spec: dict) -> str:
         w("      const double _b200_t = (double)(ts - 1) * _b200_dt; (void)_b200_t;")
         w("      const int64_t _b200_ts = ts - 1;")
         for gi in range(NG):
-            rb = reset_block(gi, 6, "ts - 1", True)
+            rb = deferred_block(gi, 6, "ts - 1", True)
             if rb:
                 w(rb)
         w("    }")
@@ -2408,6 +2490,9 @@ def render_model(spec: dict) -> str:
     w("")
     if RNG:
         w("static const int b200_rng_groups[] = {" + ", ".join(str(gi) for gi in RNG) + "};")
+    if INPUTS:
+        w("static const b200_input_info b200_inputs[] = {" + ", ".join(
+            f'{{"{inp["name"]}", {inp["group"]}, {inp["lo"]}, {inp["hi"]}}}' for inp in INPUTS) + "};")
     if SUMMED:
         w("static const b200_summed_info b200_summed[] = {" + ", ".join(
             f'{{"{sm["name"]}", {sm["pathway"]}, {sm["tgt_group"]}, {sm["tgt_var"]}, {1 if sm["index_post"] else 0}}}'
@@ -2416,7 +2501,8 @@ def render_model(spec: dict) -> str:
     w("  b200_groups, b200_pathways, b200_spkmon, b200_ratemon, b200_statemon,")
     w(f"  {len(consts)}, b200_const_names, b200_const_defaults, b200_eval_scalars, b200_launch, b200_max_active,")
     w(f"  b200_static_smem, b200_max_cluster, {NPH}, {1 if OWNER else 0}, {OWNER_EV_BYTES},")
-    w(f"  {len(SUMMED)}, {'b200_summed' if SUMMED else 'nullptr'}, {len(RNG)}, {'b200_rng_groups' if RNG else 'nullptr'}}};")
+    w(f"  {len(SUMMED)}, {'b200_summed' if SUMMED else 'nullptr'}, {len(RNG)}, {'b200_rng_groups' if RNG else 'nullptr'},")
+    w(f"  {len(INPUTS)}, {'b200_inputs' if INPUTS else 'nullptr'}}};")
     w("")
     w('#include "b200_host.h"')
     w("")

@@ -18,6 +18,7 @@
 #define B200_MAX_RATEMON 4
 #define B200_MAX_STATEMON 4
 #define B200_MAX_SUMMED 4
+#define B200_MAX_INPUTS 4
 #define B200_MAX_THREADS 1024
 #define B200_MAX_WARPS (B200_MAX_THREADS / 32)
 
@@ -26,6 +27,7 @@
 #define B200_ERR_BARRIER_TIMEOUT 4
 #define B200_ERR_INDEX 5
 #define B200_ERR_EVENT_OVERFLOW 6
+#define B200_ERR_RANDOM 7         // a binomial draw needed a second random number
 #define B200_MAX_PAYLOAD 4
 #define B200_OWNER_RING 4   // spike-list slots in owner mode (see the kernel's ordering argument)
 
@@ -162,9 +164,10 @@ struct b200_inst_d {
   // generator stream, two 32-bit words per draw, for the launch's steps
   const uint32_t* rng_words;  // [steps of the launch][rng_per_step][2], from step rng_ts0
   int64_t rng_ts0;            // step of rng_words[0]
-  int32_t rng_per_step;       // draws per step (all drawing groups)
+  int32_t rng_per_step;       // draws per step (all drawing groups and inputs)
   int32_t rng_off[B200_MAX_GROUPS];  // first draw of each group within a step
   int32_t _pad_r;
+  int32_t rng_in_off[B200_MAX_INPUTS];  // first draw of each Poisson input within a step
 };
 
 static_assert(sizeof(b200_inst_d) % 8 == 0, "descriptor is copied in 8-byte words");
@@ -209,6 +212,14 @@ struct b200_pathway_info {
   // synapses and synaptic variables of that pathway (its on_pre pathway)
   int alias;
 };
+// A Poisson input (PoissonInput, brian2/input/poissoninput.py:20-141): every
+// neuron of [lo, hi) of the group (hi < 0: the whole group) adds a binomial
+// count times a weight to a state variable, one draw per neuron and step.
+struct b200_input_info {
+  const char* name;
+  int group;
+  int lo, hi;
+};
 struct b200_summed_info {
   const char* name;
   int pathway;     // the pathway holding the Synapses object's synapses and variables
@@ -252,6 +263,9 @@ struct b200_model_info {
   // reference's schedule runs their thresholds (the order of the draws)
   int n_rng_groups;
   const int* rng_groups;
+  // Poisson inputs (PoissonInput), in schedule order; they draw after the groups
+  int n_inputs;
+  const b200_input_info* inputs;
 };
 // `tcode` bit selecting the owner-mode kernel
 #define B200_TCODE_OWNER (1 << 20)

@@ -20,6 +20,7 @@
 #define B200_ERR_CUDA 1
 #define B200_ERR_ARG 2
 #define B200_ERR_CAPACITY 3
+#define B200_STATUS_RANDOM_H 6  // B200_STATUS_RANDOM of include/b200.h
 
 // ---------------------------------------------------------------------------
 struct b200_dbuf {  // a device buffer owned by the handle
@@ -1291,10 +1292,16 @@ int b200_run(b200_net* n, int64_t n_steps) {
     }
     if (!any) break;
     int64_t steps = n->chunk_steps;
-    if (M->n_rng_groups > 0) {
-      // the random words of the launch's steps, continuing the generator
+    if (M->n_rng_groups > 0 || M->n_inputs > 0) {
+      // the random words of the launch's steps, continuing the generator: per
+      // step the drawing groups' thresholds, then the Poisson inputs
+      auto in_size = [&](const b200_inst_h& I, int q) -> int64_t {
+        const b200_input_info& In = M->inputs[q];
+        return (In.hi < 0 ? I.g[In.group].N : In.hi) - In.lo;
+      };
       int64_t per_step = 0;
       for (int q = 0; q < M->n_rng_groups; ++q) per_step += n->inst[0].g[M->rng_groups[q]].N;
+      for (int q = 0; q < M->n_inputs; ++q) per_step += in_size(n->inst[0], q);
       const int64_t wps = std::max<int64_t>(2 * per_step, 1);  // words per step
       steps = std::max<int64_t>(1, std::min<int64_t>(steps, ((int64_t)128 << 20) / 4 / wps));
       for (int k = 0; k < n->n_inst; ++k) {
@@ -1305,6 +1312,13 @@ int b200_run(b200_net* n, int64_t n_steps) {
         for (int q = 0; q < M->n_rng_groups; ++q) {
           D.rng_off[M->rng_groups[q]] = (int32_t)pk;
           pk += I.g[M->rng_groups[q]].N;
+        }
+        for (int q = 0; q < M->n_inputs; ++q) {
+          const b200_input_info& In = M->inputs[q];
+          if (In.lo < 0 || in_size(I, q) < 0 || In.lo + in_size(I, q) > I.g[In.group].N)
+            return b200_fail(n, B200_ERR_ARG, "instance %d: Poisson input '%s' targets neurons outside its group", k, In.name);
+          D.rng_in_off[q] = (int32_t)pk;
+          pk += in_size(I, q);
         }
         D.rng_per_step = (int32_t)pk;
         const int64_t w_k = std::max<int64_t>(2 * pk, 1);
@@ -1401,6 +1415,13 @@ int b200_run(b200_net* n, int64_t n_steps) {
         // leave the handle usable: clear the status and the barrier state
         cudaMemset(I.status.p, 0, 4);
         cudaMemset(I.bar.p, 0, 16);
+        if (st == B200_ERR_RANDOM) {
+          I.ts = done;
+          return b200_fail(n, B200_STATUS_RANDOM_H,
+                           "instance %d: a Poisson input's binomial draw before step %lld was rejected and needs a "
+                           "second random number (the reference redraws; the device's layout of the stream "
+                           "gives one per neuron and step)", k, (long long)done);
+        }
         if (st == B200_ERR_EVENT_OVERFLOW) {
           I.ts = done;
           return b200_fail(n, B200_ERR_CAPACITY,

@@ -20,7 +20,8 @@ _i32p = C.POINTER(C.c_int32)
 _i64p = C.POINTER(C.c_int64)
 _f64p = C.POINTER(C.c_double)
 
-STATUS = {1: "CUDA error", 2: "invalid argument", 3: "capacity", 4: "device wait timed out", 5: "index out of range"}
+STATUS = {1: "CUDA error", 2: "invalid argument", 3: "capacity", 4: "device wait timed out", 5: "index out of range",
+          6: "random stream"}
 
 
 class B200Error(RuntimeError):

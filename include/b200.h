@@ -29,6 +29,8 @@ typedef struct b200_net b200_net;
 #define B200_STATUS_CAPACITY 3 /* a buffer limit was exceeded */
 #define B200_STATUS_TIMEOUT 4  /* a bounded device-side wait gave up */
 #define B200_STATUS_INDEX 5    /* an index (synapse, neuron) out of range */
+#define B200_STATUS_RANDOM 6   /* a draw needed more random numbers than the stream's layout gives
+                                  (a rejected binomial draw of a Poisson input, probability < 1e-15) */
 
 /* Kinds of variables addressed by b200_upload / b200_download. */
 #define B200_VAR_GROUP 0   /* neuron-group state variable */
@@ -80,12 +82,15 @@ int b200_set_generator(b200_net* net, int32_t inst, int32_t group, const int32_t
                        int64_t count, int32_t period_bins, int32_t last);
 int b200_get_generator(b200_net* net, int32_t inst, int32_t group, int32_t* last);
 /* The random generator of the step loop, for models whose threshold code draws
- * rand() once per neuron (PoissonGroup, brian2/input/poissongroup.py): the
+ * rand() once per neuron (PoissonGroup, brian2/input/poissongroup.py) or that
+ * have Poisson inputs (PoissonInput, brian2/input/poissoninput.py, one binomial
+ * draw per target neuron and step, brian2/input/binomial.py:93-141): the
  * reference's MT19937 state as the C++ library stores it (624 words, then the
  * position), taken where the standalone program starts the run
  * (brian::_random_generators[0], templates/objects.cpp:426-453).  The device
- * continues that stream in the reference's order of draws (groups in schedule
- * order, neurons in index order, rand() = (a*2^26 + b)/2^53 of two outputs).
+ * continues that stream in the reference's order of draws (threshold groups,
+ * then Poisson inputs, in schedule order; neurons in index order; rand() =
+ * (a*2^26 + b)/2^53 of two outputs).
  * b200_get_rng returns the generator state and the steps of words generated
  * ahead of the current step. */
 int b200_set_rng(b200_net* net, int32_t inst, const uint32_t* words, int32_t position);

@@ -404,6 +404,41 @@ def poisson_input(N_in=300, N=200, duration_ms=200.0, seed_value=101):
     return dict(P=P, spikes=s_mon, rate=r_mon, other_spikes=g_mon)
 
 
+def poisson_drive(N=400, duration_ms=200.0, seed_value=202):
+    """Poisson inputs (binomial counts drawn from the reference's generator)
+    into a recurrent CUBA population with delays: one into ge over the whole
+    group, one into v of a subgroup with a weight read from a state variable
+    (the reset follows it), one with rate*dt > 0.5 (the sampler's reversed
+    form) into gi, after a pathway into gi; a PoissonGroup draws before them
+    in every step."""
+    from brian2 import (NeuronGroup, PoissonGroup, PoissonInput, Synapses, SpikeMonitor, PopulationRateMonitor,
+                        StateMonitor, ms, mV, Hz, seed, run)
+    seed(seed_value)
+    ns = dict(taum=20 * ms, taue=5 * ms, taui=10 * ms, Vt=-50 * mV, Vr=-60 * mV, El=-60 * mV, we=0.8 * mV,
+              wi=-2 * mV)
+    P = NeuronGroup(N, '''dv/dt = (ge+gi-(v-El))/taum : volt
+                          dge/dt = -ge/taue : volt
+                          dgi/dt = -gi/taui : volt
+                          scale : 1''',
+                    threshold='v>Vt', reset='v = Vr', method='exact', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    P.scale = 'rand()'
+    H = PoissonGroup(60, rates=25 * Hz)
+    S = Synapses(P, P, on_pre='ge += we', namespace=ns)
+    S.connect(p=0.05)
+    S.delay = 'rand() * 3*ms'
+    T = Synapses(H, P, on_pre='gi += wi', namespace=ns)
+    T.connect(p=0.1)
+    in_ge = PoissonInput(P, 'ge', 200, 5 * Hz, weight=1 * mV)                               # N*p = 0.1
+    in_v = PoissonInput(P[50:250], 'v', 20, 50 * Hz, weight='0.4*mV*(1 + scale)')           # N*p = 0.1
+    in_gi = PoissonInput(P[300:400], 'gi', 5, 8000 * Hz, weight=-0.01 * mV)                 # p = 0.8
+    s_mon = SpikeMonitor(P)
+    r_mon = PopulationRateMonitor(P)
+    st = StateMonitor(P, 'v', record=[0, 60, 320])
+    run(duration_ms * ms)
+    return dict(P=P, spikes=s_mon, rate=r_mon, state=st)
+
+
 SCENARIOS = {
     "lif_refractory": lif_refractory,
     "hetero_delays": hetero_delays,
@@ -415,4 +450,5 @@ SCENARIOS = {
     "gap_junctions": gap_junctions,
     "explicit_methods": explicit_methods,
     "poisson_input": poisson_input,
+    "poisson_drive": poisson_drive,
 }

@@ -26,6 +26,10 @@ code objects, and executes the spec's *plain* C++ snippets (Brian's own
   std::mt19937 continued from the state the standalone program had at the
   run, rand() = (a*2^26 + b)/2^53 of two outputs (templates/objects.cpp:
   426-453), drawing groups in schedule order and neurons in index order;
+* Poisson inputs (PoissonInput, input/poissoninput.py:20-141): after the
+  on_pre pathways and before the on_post ones, every target neuron adds a
+  binomial count drawn by inversion (input/binomial.py:93-141, including the
+  redraw past the bound) from the same generator;
 * summed variables: the target range zeroed, then the expression of every
   synapse in creation order added to its target (templates/summed_variable.cpp:
   11-25), after the state monitors and before the state updates;
@@ -90,7 +94,9 @@ def render_oracle(spec: dict) -> str:
     w("static inline int64_t _timestep(double t, double dt) { return (int64_t)((t + 1e-3 * dt) / dt); }")
     w("#define _brian_abs fabs")
     RNG = spec.get("rng_groups", [])
-    if RNG:
+    INPUTS = spec.get("inputs", [])
+    DRAWS = bool(RNG or INPUTS)
+    if DRAWS:
         w("#include <random>\n#include <sstream>\n#include <string>")
         w("static std::mt19937* _b200_gen = nullptr;")
         w("static inline double _rand(int64_t) {")
@@ -98,9 +104,20 @@ def render_oracle(spec: dict) -> str:
         w("  const long b = (long)((*_b200_gen)() >> 6);")
         w("  return (a * 67108864.0 + b) / 9007199254740992.0;")
         w("}")
+    for k, inp in enumerate(INPUTS):
+        bn = inp["binom"]
+        w(f"static inline long _b200_binomial_{k}(int64_t _vidx) {{  // inversion, with the reference's constants")
+        w(f"  long X = 0; double px = {bn['qn']}; double U = _rand(_vidx);")
+        w("  while (U > px) {")
+        w("    X++;")
+        w(f"    if (X > {bn['bound']}) {{ X = 0; px = {bn['qn']}; U = _rand(_vidx); }}  // start over with a new draw")
+        w(f"    else {{ U -= px; px = (({bn['n']} - X + 1) * {bn['p']} * px) / (X * {bn['q']}); }}")
+        w("  }")
+        w(f"  return {str(bn['n']) + ' - X' if bn['reverse'] else 'X'};")
+        w("}")
     w("struct Net {")
     w("  double dt; int64_t ts = 0;")
-    if RNG:
+    if DRAWS:
         w("  std::mt19937 gen;")
     w("  std::vector<double> c;")
     for gi, g in enumerate(groups):
@@ -187,7 +204,7 @@ def render_oracle(spec: dict) -> str:
     w("}")
     w("void oracle_set_step(Net* n, int64_t ts) { n->ts = ts; }")
     w("void oracle_set_rng(Net* n, const uint32_t* words, int32_t pos) {")
-    if RNG:  # (the C++ library's text form of the state: the 624 words, then the position)
+    if DRAWS:  # (the C++ library's text form of the state: the 624 words, then the position)
         w("  std::ostringstream o; for (int k = 0; k < 624; ++k) o << words[k] << ' '; o << pos;")
         w("  std::istringstream in(o.str()); in >> n->gen;")
     else:
@@ -206,7 +223,7 @@ def render_oracle(spec: dict) -> str:
 
     # ---- the step loop
     w("void oracle_run(Net* n, int64_t n_steps) {")
-    if RNG:
+    if DRAWS:
         w("  _b200_gen = &n->gen;")
     for k, cst in enumerate(consts):
         w(f"  const {cst['ctype']} {cst['name']} = ({cst['ctype']})n->c[{k}]; (void){cst['name']};")
@@ -328,9 +345,31 @@ def render_oracle(spec: dict) -> str:
         w(f"      for (int32_t idx : sp) if (idx >= n->sm{mi}_lo && idx < n->sm{mi}_hi) {{")
         w(f"        n->sm{mi}_i.push_back(idx - n->sm{mi}_lo); n->sm{mi}_ts.push_back((int32_t)n->ts); n->sm{mi}_count[idx - n->sm{mi}_lo]++; }}")
         w("    }")
-    # pathways: advance, push, peek, on_pre
+    def emit_inputs():
+        for k, inp in enumerate(INPUTS):
+            gi = inp["group"]
+            w(f"    {{  // Poisson input {k} '{inp['name']}'")
+            w(gptrs(gi, 6))
+            w(f"      const int32_t N = n->N{gi}; (void)N;")
+            w("      {")
+            w(_ind(inp["code"]["scalar"], 8))
+            w(f"        const int32_t _lo = {inp['lo']}, _hi = {inp['hi'] if inp['hi'] >= 0 else 'N'};")
+            w("        for (int32_t _b200_abs_idx = _lo; _b200_abs_idx < _hi; ++_b200_abs_idx) {")
+            w("          const int32_t _idx = _b200_abs_idx - _lo;")
+            w("          const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+            w(_ind(inp["code"]["vector"], 10))
+            w("        }")
+            w("      }")
+            w("    }")
+
+    # pathways: advance, push, peek, on_pre; the Poisson inputs between the
+    # on_pre (order -1) and on_post (order +1) pathways
+    inputs_done = False
     for pi, p in enumerate(paths):
         sg = p["src"]
+        if p.get("prepost") == "post" and not inputs_done:
+            emit_inputs()
+            inputs_done = True
         w("    {")
         w(f"      std::vector<std::vector<int32_t>>& Q = n->p{pi}_queue; int& off = n->p{pi}_offset;")
         w("      Q[off].clear(); off = (off + 1) % (int)Q.size();")
@@ -363,6 +402,8 @@ def render_oracle(spec: dict) -> str:
         w("        }")
         w("      }")
         w("    }")
+    if not inputs_done:
+        emit_inputs()
     # resets
     for gi, g in enumerate(groups):
         if not g.get("reset"):
@@ -636,7 +677,7 @@ def run_job_on_oracle(directory):
     for mi in range(len(spec.get("state_monitors", []))):
         o.set_statemon(mi, init[f"stm{mi}_idx"], list(init[f"stm{mi}_vars"]))
     o.set_step(int(init["ts0"]))
-    if spec.get("rng_groups"):
+    if spec.get("rng_groups") or spec.get("inputs"):
         o.set_rng(init["rng_words"], int(init["rng_position"]))
     for n in job["runs"]:
         o.run(int(n))

@@ -5,7 +5,8 @@ same script (tests/golden/make_scenarios.py).
 
 Bit-exact where every per-target increment of a pathway is equal (timed
 refractoriness, subgroup monitors and a state monitor, a separate input
-group, a spike generator); where increments differ (random weights, a
+group, a spike generator, Poisson inputs -- which add after every delivery of
+the step, as in the reference); where increments differ (random weights, a
 presynaptic factor, plastic weights) the order of the float64 sums into a
 target differs from the reference's queue order, so the raster must match and
 the state (and the plastic synapses' variables) agree to 1e-12 relative."""
@@ -21,7 +22,7 @@ pytestmark = pytest.mark.gpu
 HERE = os.path.dirname(os.path.abspath(__file__))
 EXACT = {"lif_refractory": True, "hetero_delays": False, "subgroup_monitors": True, "input_group": True,
          "presynaptic_read": False, "spike_generator": True, "stdp": False,
-         "gap_junctions": True, "explicit_methods": True, "poisson_input": False}
+         "gap_junctions": True, "explicit_methods": True, "poisson_input": False, "poisson_drive": True}
 
 
 @pytest.mark.parametrize("name", sorted(EXACT))
