@@ -72,9 +72,24 @@ _BINOM_RE = re.compile(r"double px = " + _NUM + r";.*?if \(X > " + _NUM + r"\).*
                        r"return ([^;]+);", re.S)
 
 
+_NORMAL_RE = re.compile(r"return _randn\(vectorisation_idx\) \* " + _NUM + r" \+ " + _NUM + r";")
+
+
 def draws_random(spec):
     """Whether the step loop of a spec draws from the reference's generator."""
-    return bool(spec.get("rng_groups") or spec.get("inputs"))
+    return bool(spec.get("draws"))
+
+
+def _draw_calls(code, kind):
+    """Rewrites the calls of rand()/randn() in vector code for a draw site (one
+    macro per call, in code order); returns (code, number of calls).  Each call
+    must run once per neuron: none in a conditional expression."""
+    name = {"rand": "_rand(", "randn": "_randn("}[kind]
+    lines = code.split("\n")
+    for ln in lines:
+        if name in ln and ("?" in ln or "&&" in ln or "||" in ln):
+            raise NotImplementedError(f"b200: {kind}() in a conditional expression")
+    return code, code.count(name)
 
 
 class B200CodeGenerator(CPPCodeGenerator):
@@ -200,11 +215,12 @@ class B200Device(CPPStandaloneDevice):
                 if prefs.devices.cpp_standalone.openmp_threads:
                     raise NotImplementedError("b200: PoissonInput needs openmp_threads = 0 (one generator stream)")
             if isinstance(var, Function) and vname in ("rand", "randn", "poisson") and vname in str(abstract_code):
-                # rand() in threshold code (PoissonGroup): the device continues the
-                # reference's generator stream; other random numbers are not supported
-                if not (vname == "rand" and template_name == "threshold"):
-                    raise NotImplementedError(f"b200: {vname}() inside the step loop is only supported in thresholds "
-                                              "(rand())")
+                # rand()/randn() drawn once per neuron and step (PoissonGroup thresholds,
+                # stochastic state updates): the device continues the reference's
+                # stream; draws per spike or per synapse are not supported
+                if not (vname in ("rand", "randn") and template_name in ("threshold", "stateupdate")):
+                    raise NotImplementedError(f"b200: {vname}() in {template_name} code is not supported "
+                                              "(random numbers in state updates and thresholds only)")
                 if prefs.devices.cpp_standalone.openmp_threads:
                     raise NotImplementedError("b200: rand() in the step loop needs openmp_threads = 0 "
                                               "(one generator stream)")
@@ -246,9 +262,17 @@ class B200Device(CPPStandaloneDevice):
         spec, objects = self._make_spec(net, all_objects, clock)
         if draws_random(spec) and not self.b200_runs:
             # the generator state where the step loop starts drawing (the C++
-            # library's text form: 624 words and the position)
-            self.main_queue.append(("insert_code", '{ std::ofstream _b200_rng(brian::results_dir + "b200_rng_state"); '
-                                                   '_b200_rng << brian::_random_generators[0]; }'))
+            # library's text form: 624 words and the position), then whether
+            # randn() keeps a value and the value (a copy's randn() returns the
+            # kept value without advancing its generator)
+            self.main_queue.append(("insert_code",
+                                    '{ std::ofstream _b200_rng(brian::results_dir + "b200_rng_state"); '
+                                    '_b200_rng << brian::_random_generators[0]; '
+                                    'brian::RandomGenerator _b200_c = brian::_random_generators[0], '
+                                    '_b200_d = brian::_random_generators[0]; '
+                                    'const double _b200_g = _b200_c.randn(); '
+                                    'const int _b200_kept = _b200_c.rand() == _b200_d.rand() ? 1 : 0; '
+                                    '_b200_rng << " " << _b200_kept << " " << std::hexfloat << _b200_g; }'))
         self.b200_runs.append(dict(net=net, n_steps=n_steps, spec=spec, objects=objects, clock=clock,
                                    queue_len=len(self.main_queue)))
         self.main_queue.append(("insert_code", f"// b200 network run {len(self.b200_runs) - 1} ({n_steps} steps)"))
@@ -331,9 +355,9 @@ class B200Device(CPPStandaloneDevice):
         pathways, spkmons, ratemons, statemons = [], [], [], []
         summed_frags = []
         input_frags = []  # PoissonInputs, in schedule order
-        rng_groups = []  # groups drawing rand() in their thresholds, in schedule order
+        draw_sites = []  # (position in the schedule, site, the block or input whose code draws)
         b200_objects = []
-        for obj in objects:
+        for pos, obj in enumerate(objects):
             if not obj.active:
                 continue
             for co in obj._code_objects:
@@ -343,7 +367,7 @@ class B200Device(CPPStandaloneDevice):
                 t = frag["template"]
                 b200_objects.append((obj, co))
                 if isinstance(obj, PoissonInput):
-                    input_frags.append((obj, frag))
+                    input_frags.append((obj, frag, pos))
                 elif t in ("stateupdate", "threshold", "reset"):
                     gi, _ = group_of(obj.group)
                     g = groups[gi]
@@ -352,14 +376,19 @@ class B200Device(CPPStandaloneDevice):
                     ex = collect(frag, {g["name"]})
                     if ex:
                         b["extra_ptrs"] = {k: list(v) for k, v in ex.items()}
+                    if t in ("threshold", "stateupdate"):
+                        kinds = [k for k in ("rand", "randn") if f"_{k}(" in b["vector"]]
+                        if len(kinds) > 1:
+                            raise NotImplementedError("b200: rand() and randn() in one code object")
+                        if kinds:
+                            if prefs.devices.cpp_standalone.openmp_threads:
+                                raise NotImplementedError("b200: random numbers in the step loop need "
+                                                          "openmp_threads = 0 (one generator stream)")
+                            _, calls = _draw_calls(b["vector"], kinds[0])
+                            draw_sites.append((pos, dict(name=obj.name, kind=kinds[0], group=gi, lo=0, hi=-1,
+                                                         calls=calls), b))
                     if t == "threshold":
                         b["refractory"] = bool(frag["template_kwds"].get("_uses_refractory", False))
-                        n_rand = b["vector"].count("_rand(")
-                        if n_rand:
-                            if n_rand != 1 or "?" in b["vector"] or "&&" in b["vector"] or "||" in b["vector"]:
-                                raise NotImplementedError("b200: a threshold must draw rand() once per neuron")
-                            b["rng"] = True
-                            rng_groups.append(gi)
                         if frag["template_kwds"].get("eventspace_variable") is not None and \
                                 frag["template_kwds"]["eventspace_variable"].name != "_spikespace":
                             raise NotImplementedError("b200: custom events are not supported")
@@ -479,7 +508,7 @@ class B200Device(CPPStandaloneDevice):
         # synapses slot, after the on_pre pathways (order -1) and before the
         # on_post pathways (order +1), drawing one binomial count per neuron
         inputs = []
-        for obj, frag in input_frags:
+        for obj, frag, pos in input_frags:
             if obj.when != "synapses" or obj.order != 0:
                 raise NotImplementedError("b200: PoissonInput runs in the synapses slot with order 0")
             fns = [v for v in frag["variables"].values() if isinstance(v, BinomialFunction)]
@@ -487,13 +516,18 @@ class B200Device(CPPStandaloneDevice):
                 raise NotImplementedError("b200: unsupported PoissonInput code")
             fn = fns[0]
             support = fn.implementations[CPPCodeGenerator].get_code(None)["support_code"]
-            m = _BINOM_RE.search(support)
-            if m is None:
-                raise NotImplementedError("b200: PoissonInput with N*rate*dt > 5 and N*(1-rate*dt) > 5 (Brian "
-                                          "samples a normal approximation with randn())")
-            qn, bound, n_str, P, Q, ret = m.groups()
-            ret = ret.strip().replace(" ", "")
-            if ret not in ("X", f"{n_str}-X"):
+            m, mn = _BINOM_RE.search(support), _NORMAL_RE.search(support)
+            if m is not None:     # inversion (N*p <= 5 or N*(1-p) <= 5)
+                qn, bound, n_str, P, Q, ret = m.groups()
+                ret = ret.strip().replace(" ", "")
+                if ret not in ("X", f"{n_str}-X"):
+                    raise NotImplementedError("b200: unsupported binomial sampler")
+                site = dict(name=obj.name, kind="binomial", lo=0, hi=-1, calls=1,
+                            binom=dict(qn=qn, bound=bound, n=int(n_str), p=P, q=Q, reverse=ret != "X"))
+            elif mn is not None:  # normal approximation: (float)(randn()*scale + loc)
+                site = dict(name=obj.name, kind="binormal", lo=0, hi=-1, calls=1,
+                            binom=dict(scale=mn.group(1), loc=mn.group(2)))
+            else:
                 raise NotImplementedError("b200: unsupported binomial sampler")
             gi, (lo, hi) = group_of(obj.group)
             g = groups[gi]
@@ -502,7 +536,7 @@ class B200Device(CPPStandaloneDevice):
             vec = b["vector"]
             if vec.count(fn.name + "(") != 1 or b.get("vector_device"):
                 raise NotImplementedError("b200: unsupported PoissonInput code")
-            vec = re.sub(r"\b%s\(" % re.escape(fn.name), f"_b200_binomial_{k}(", vec)
+            vec = re.sub(r"\b%s\(" % re.escape(fn.name), "_b200_binomial(", vec)
             whole = not isinstance(obj.group, Subgroup)
             if not whole:  # the subgroup's index array is the contiguous range itself
                 sub = gen_name(obj.group.variables["_sub_idx"])
@@ -523,10 +557,32 @@ class B200Device(CPPStandaloneDevice):
                 if sm["tgt_group"] == gi and g["vars"][sm["tgt_var"]]["ptr"] == tv:
                     raise NotImplementedError("b200: PoissonInput into a summed variable")
             inputs.append(dict(name=obj.name, group=gi, lo=int(lo), hi=-1 if whole else int(hi),
-                               code=dict(scalar=b["scalar"], vector=vec),
-                               binom=dict(qn=qn, bound=bound, n=int(n_str), p=P, q=Q, reverse=ret != "X")))
+                               code=dict(scalar=b["scalar"], vector=vec)))
+            site.update(group=gi, lo=int(lo), hi=-1 if whole else int(hi))
+            draw_sites.append((pos, site, inputs[-1]))
         if len(inputs) > 4:
             raise NotImplementedError("b200: more than 4 PoissonInputs")
+        # draw sites in the order of the schedule (the order of the draws); each
+        # call of the site's code becomes _b200_draw_<site>_<call>(index)
+        draws = []
+        for _, site, holder in sorted(draw_sites, key=lambda x: x[0]):
+            si = len(draws)
+            code = holder["code"]["vector"] if "code" in holder else holder["vector"]
+            if site["kind"] in ("rand", "randn"):
+                name = "_" + site["kind"] + "("
+                parts = code.split(name)
+                code = parts[0] + "".join(f"_b200_draw_{si}_{c}(" + rest for c, rest in enumerate(parts[1:]))
+            else:
+                code = code.replace("_b200_binomial(", f"_b200_draw_{si}_0(")
+                holder["draw"] = si
+            if "code" in holder:
+                holder["code"]["vector"] = code
+            else:
+                holder["vector"] = code
+                holder["draw"] = si
+            draws.append(site)
+        if len(draws) > 8:
+            raise NotImplementedError("b200: more than 8 code objects drawing random numbers")
         # pathways of one Synapses object (on_pre and on_post) share its synapses and
         # synaptic variables: the first one in schedule order owns them, the others
         # alias it; all carry the union of the variables their code uses
@@ -556,8 +612,8 @@ class B200Device(CPPStandaloneDevice):
                     state_monitors=statemons, clock_ptrs=clock_ptrs)
         if summed:
             spec["summed"] = summed
-        if rng_groups:
-            spec["rng_groups"] = rng_groups
+        if draws:
+            spec["draws"] = draws
         if inputs:
             spec["inputs"] = inputs
         return spec, b200_objects
@@ -662,11 +718,13 @@ class B200Device(CPPStandaloneDevice):
         init["ts0"] = np.int64(int(self._load(clock.variables["timestep"])[0]))
         if draws_random(spec0):
             with open(os.path.join(self.results_dir, "b200_rng_state")) as f:
-                st = [int(x) for x in f.read().split()]
-            if len(st) != 625:
+                tok = f.read().split()
+            if len(tok) != 627:
                 raise RuntimeError("b200: unexpected generator state format")
+            st = [int(x) for x in tok[:625]]
             init["rng_words"] = np.asarray(st[:624], np.uint32)
             init["rng_position"] = np.int64(st[624])
+            init["rng_gauss"] = np.asarray([float(int(tok[625])), float.fromhex(tok[626])], np.float64)
         write_job(directory, pub, init, [r["n_steps"] for r in self.b200_runs], dt, self.b200_run_options)
         self.b200_job_dir = directory
         return directory

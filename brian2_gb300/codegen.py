@@ -259,27 +259,6 @@ def render_model(spec: dict) -> str:
     w("static const char* const b200_const_names[] = {" + ", ".join(f'"{c["name"]}"' for c in consts) + ("" if consts else '""') + "};")
     w("static const double b200_const_defaults[] = {" + ", ".join(c_literal(c["value"], "double") for c in consts) + ("" if consts else "0.0") + "};")
     w("")
-    for k, inp in enumerate(spec.get("inputs", [])):
-        bn = inp["binom"]
-        w(f"// Poisson input {k} '{inp['name']}': the reference's binomial sampler by inversion")
-        w("// (brian2/input/binomial.py:93-141) with its constants as the reference prints them;")
-        w("// one draw (two words of the stream).  The reference draws again when the count")
-        w("// passes the bound (probability < 1e-15): flagged, since the stream's layout gives")
-        w("// one draw per neuron and step.")
-        w(f"__device__ __forceinline__ long long b200_binomial_{k}(const uint32_t* _w, bool& _rej) {{")
-        w("  long long X = 0;")
-        w(f"  double px = {bn['qn']};")
-        w("  double U = b200_rand_from(_w);")
-        w("  while (U > px) {")
-        w("    X++;")
-        w(f"    if (X > {bn['bound']}) {{ _rej = true; X = 0; break; }}")
-        w("    U -= px;")
-        w(f"    px = (({bn['n']} - X + 1) * {bn['p']} * px) / (X * {bn['q']});")
-        w("  }")
-        w(f"  return {str(bn['n']) + ' - X' if bn['reverse'] else 'X'};")
-        w("}")
-        w("")
-
     # Poisson inputs (PoissonInput), in schedule order: their scalar code sits in
     # their target group's table, their vector code runs over the group's neurons
     INPUTS = [dict(inp, code=dict(inp["code"], vector=_device(inp["code"]["vector"])))
@@ -292,7 +271,23 @@ def render_model(spec: dict) -> str:
         blocks += [(f"input{k}", _block(inp["code"])) for k, inp in enumerate(INPUTS) if inp["group"] == gi]
         gtables.append((_Tables(consts, blocks, (clock["t"], clock["timestep"])), blocks))
     SUMMED = spec.get("summed", [])
-    RNG = spec.get("rng_groups", [])  # groups drawing rand() in their thresholds, in draw order
+    # code objects drawing from the reference's generator, in the order of the draws
+    DRAWS = spec.get("draws", [])
+    assert len(DRAWS) <= 8
+
+    def draw_macros(si, tsexpr):
+        """Declarations reading draw site si's values of step `tsexpr` (drawn
+        ahead by b200_variates_kernel): the c-th call of the site's code for
+        neuron i is _b200_draw_<si>_<c>(i).  Returns (lines, undef lines)."""
+        d = DRAWS[si]
+        calls = d["calls"]
+        cast = {"binomial": "(long long)", "binormal": "(float)"}.get(d["kind"], "")
+        lines = [f"const double* const _b200_rv{si} = I.rng_vals + (({tsexpr}) - I.rng_ts0) * I.rng_per_step + I.draw_off[{si}];"]
+        undef = []
+        for c in range(calls):
+            lines.append(f"#define _b200_draw_{si}_{c}(i) ({cast}_b200_rv{si}[(int64_t)(i) * {calls} + {c}])")
+            undef.append(f"#undef _b200_draw_{si}_{c}")
+        return lines, undef
     for pi, p in enumerate(paths):
         blocks = [("on_pre", _block(p.get("on_pre")))]
         blocks += [(f"summed{si}", _block(sm["code"])) for si, sm in enumerate(SUMMED) if sm["pathway"] == pi]
@@ -527,16 +522,15 @@ def render_model(spec: dict) -> str:
              f"  const int32_t N = I.g[{gi}].N; (void)N;",
              f"  const double* const _b200_S = s_Sg{gi}; const float* const _b200_Sf = s_Sg{gi}f; const long long* const _b200_Si = s_Sg{gi}i;",
              gptr_decls(gi, 2, False),
-             f"  const int _own0 = s_tst[{gi} * max_tiles1 + s_ut[{gi}][0]], _own1 = s_tst[{gi} * max_tiles1 + s_ut[{gi}][1]];",
-             "  bool _b200_rej = false;"]
+             f"  const int _own0 = s_tst[{gi} * max_tiles1 + s_ut[{gi}][0]], _own1 = s_tst[{gi} * max_tiles1 + s_ut[{gi}][1]];"]
         for q, (k, inp) in enumerate(ins):
             hi = str(inp["hi"]) if inp["hi"] >= 0 else "N"
             if q:
                 L.append("  __syncthreads();  // (inputs into one variable add in schedule order)")
+            dl, du = draw_macros(inp["draw"], tsexpr)
             L += [f"  {{  // Poisson input {k} '{inp['name']}'",
                   f"    const int _lo = {inp['lo']}, _hi = {hi};",
-                  f"    const uint32_t* const _b200_rw = I.rng_words + ((({tsexpr}) - I.rng_ts0) * I.rng_per_step + I.rng_in_off[{k}]) * 2;",
-                  f"#define _b200_binomial_{k}(i) b200_binomial_{k}(_b200_rw + 2 * (int64_t)(i), _b200_rej)",
+                  _indent("\n".join(dl), 4),
                   _indent(tab.device_loads(f"input{k}", f32), 4),
                   _indent(_device(tab.time_code(f"input{k}")), 4),
                   "    const int _a = _own0 > _lo ? _own0 : _lo, _b = _own1 < _hi ? _own1 : _hi;",
@@ -547,9 +541,9 @@ def render_model(spec: dict) -> str:
                   _indent(inp["code"]["vector"], 8),
                   "      }",
                   "    }",
-                  f"#undef _b200_binomial_{k}",
+                  "\n".join(du),
                   "  }"]
-        L += ["  if (_b200_rej) atomicCAS(I.status, 0, B200_ERR_RANDOM);", "}"]
+        L += ["}"]
         return _indent("\n".join(L), indent)
 
     def deferred_block(gi, indent, tsexpr, owner=False):
@@ -876,12 +870,15 @@ def render_model(spec: dict) -> str:
                 w(f"        int32_t* const scr = s_scr[{gi}]; int32_t* const tcnt = s_tc[{gi}];")
                 w(f"        int32_t* const oscr = s_oscr[{gi}]; int32_t* const otc = s_otc[{gi}];")
             w(f"        const int* const tst = s_tst + {gi} * max_tiles1;")
-            rng = bool(g.get("threshold") and g["threshold"].get("rng"))
-            if rng:
-                # rand() in the threshold: the step's words of this group, one draw per
-                # neuron in index order (the reference's order)
-                w(f"        const uint32_t* const _b200_rw = I.rng_words + ((ts - I.rng_ts0) * I.rng_per_step + I.rng_off[{gi}]) * 2;")
-                w("#define _rand(i) b200_rand_from(_b200_rw + 2 * (int64_t)(i))")
+            # rand() / randn() in the update or threshold: the step's draws of the
+            # site, `calls` per neuron in index order (the reference's order)
+            rng_undef = []
+            for blk_name in ("update", "threshold"):
+                if g.get(blk_name) and g[blk_name].get("draw") is not None:
+                    dl, du = draw_macros(g[blk_name]["draw"], "ts")
+                    w(_indent("\n".join(dl), 8))
+                    rng_undef += du
+            rng = bool(rng_undef)
             if not SUMMED:  # (with summed variables the monitors record before those are summed)
                 emit_statemons(gi)
             # constants and block scalars are loaded once per step, not per neuron
@@ -894,7 +891,7 @@ def render_model(spec: dict) -> str:
                     if bd[blk_name] is not None:
                         w(_indent(tab.scalar_loads(blk_name, f32), 8))
                         w(_indent(_device(tab.time_code(blk_name)), 8))
-            quad = (not owner) and emit_quad(gi, g, bd, tab, hoist_sc)
+            quad = (not owner) and not rng and emit_quad(gi, g, bd, tab, hoist_sc)
             w(f"        for (int u = s_ut[{gi}][0]; u < s_ut[{gi}][1]; ++u) {{")
             w("          const int start = tst[u], end = tst[u + 1];")
             w("          int cnt = 0;")
@@ -998,7 +995,7 @@ def render_model(spec: dict) -> str:
             if quad:
                 w("        }  // scalar path")
             if rng:
-                w("#undef _rand")
+                w("\n".join(rng_undef))
             w("      }")
 
     w("__device__ __forceinline__ int b200_upper_bound(const int* a, int n, int x) {")
@@ -2488,11 +2485,16 @@ def render_model(spec: dict) -> str:
     w("  return n;")
     w("}")
     w("")
-    if RNG:
-        w("static const int b200_rng_groups[] = {" + ", ".join(str(gi) for gi in RNG) + "};")
-    if INPUTS:
-        w("static const b200_input_info b200_inputs[] = {" + ", ".join(
-            f'{{"{inp["name"]}", {inp["group"]}, {inp["lo"]}, {inp["hi"]}}}' for inp in INPUTS) + "};")
+    if DRAWS:
+        kinds = {"rand": "B200_DRAW_UNIFORM", "randn": "B200_DRAW_NORMAL", "binomial": "B200_DRAW_BINOMIAL",
+                 "binormal": "B200_DRAW_BINORMAL"}
+        rows = []
+        for d in DRAWS:
+            bn = d.get("binom") or {}
+            rows.append(f'{{"{d["name"]}", {kinds[d["kind"]]}, {d["group"]}, {d["lo"]}, {d["hi"]}, {d["calls"]}, '
+                        f'{bn.get("n", 0)}, {1 if bn.get("reverse") else 0}, {bn.get("qn", "0.0")}, {bn.get("bound", "0.0")}, '
+                        f'{bn.get("p", "0.0")}, {bn.get("q", "0.0")}, {bn.get("scale", "0.0")}, {bn.get("loc", "0.0")}}}')
+        w("static const b200_draw_info b200_draws[] = {" + ", ".join(rows) + "};")
     if SUMMED:
         w("static const b200_summed_info b200_summed[] = {" + ", ".join(
             f'{{"{sm["name"]}", {sm["pathway"]}, {sm["tgt_group"]}, {sm["tgt_var"]}, {1 if sm["index_post"] else 0}}}'
@@ -2501,8 +2503,7 @@ def render_model(spec: dict) -> str:
     w("  b200_groups, b200_pathways, b200_spkmon, b200_ratemon, b200_statemon,")
     w(f"  {len(consts)}, b200_const_names, b200_const_defaults, b200_eval_scalars, b200_launch, b200_max_active,")
     w(f"  b200_static_smem, b200_max_cluster, {NPH}, {1 if OWNER else 0}, {OWNER_EV_BYTES},")
-    w(f"  {len(SUMMED)}, {'b200_summed' if SUMMED else 'nullptr'}, {len(RNG)}, {'b200_rng_groups' if RNG else 'nullptr'},")
-    w(f"  {len(INPUTS)}, {'b200_inputs' if INPUTS else 'nullptr'}}};")
+    w(f"  {len(SUMMED)}, {'b200_summed' if SUMMED else 'nullptr'}, {len(DRAWS)}, {'b200_draws' if DRAWS else 'nullptr'}}};")
     w("")
     w('#include "b200_host.h"')
     w("")

@@ -18,7 +18,7 @@
 #define B200_MAX_RATEMON 4
 #define B200_MAX_STATEMON 4
 #define B200_MAX_SUMMED 4
-#define B200_MAX_INPUTS 4
+#define B200_MAX_DRAWS 8
 #define B200_MAX_THREADS 1024
 #define B200_MAX_WARPS (B200_MAX_THREADS / 32)
 
@@ -160,14 +160,13 @@ struct b200_inst_d {
   b200_ratemon_d rm[B200_MAX_RATEMON];
   b200_statemon_d stm[B200_MAX_STATEMON];
   b200_summed_d sum[B200_MAX_SUMMED];
-  // random numbers of the step loop (rand() in threshold code): the reference's
-  // generator stream, two 32-bit words per draw, for the launch's steps
-  const uint32_t* rng_words;  // [steps of the launch][rng_per_step][2], from step rng_ts0
-  int64_t rng_ts0;            // step of rng_words[0]
-  int32_t rng_per_step;       // draws per step (all drawing groups and inputs)
-  int32_t rng_off[B200_MAX_GROUPS];  // first draw of each group within a step
+  // random numbers of the step loop: the reference's stream, drawn ahead of the
+  // launch in its order by b200_variates_kernel, one double per draw
+  const double* rng_vals;     // [steps of the launch][rng_per_step], from step rng_ts0
+  int64_t rng_ts0;            // step of rng_vals[0]
+  int32_t rng_per_step;       // draws per step (all draw sites)
+  int32_t draw_off[B200_MAX_DRAWS];  // first draw of each site within a step
   int32_t _pad_r;
-  int32_t rng_in_off[B200_MAX_INPUTS];  // first draw of each Poisson input within a step
 };
 
 static_assert(sizeof(b200_inst_d) % 8 == 0, "descriptor is copied in 8-byte words");
@@ -212,13 +211,18 @@ struct b200_pathway_info {
   // synapses and synaptic variables of that pathway (its on_pre pathway)
   int alias;
 };
-// A Poisson input (PoissonInput, brian2/input/poissoninput.py:20-141): every
-// neuron of [lo, hi) of the group (hi < 0: the whole group) adds a binomial
-// count times a weight to a state variable, one draw per neuron and step.
-struct b200_input_info {
+// A draw site: a code object of the step loop that draws from the reference's
+// generator, `calls` draws per neuron of [lo, hi) of a group (hi < 0: to the
+// group's end) and step -- rand() in threshold code (PoissonGroup), randn() in
+// a state update (stochastic equations), the binomial counts of a PoissonInput
+// (brian2/input/poissoninput.py:20-141, brian2/input/binomial.py:93-141).
+struct b200_draw_info {
   const char* name;
-  int group;
-  int lo, hi;
+  int kind;                   // B200_DRAW_*
+  int group, lo, hi, calls;
+  int n, reverse;             // binomial: trials, sampler counts failures
+  double qn, bound, p, q;     // binomial by inversion (the reference's printed constants)
+  double scale, loc;          // binomial, normal approximation
 };
 struct b200_summed_info {
   const char* name;
@@ -259,13 +263,10 @@ struct b200_model_info {
   int owner_event_bytes;  // shared-memory bytes per staged event
   int n_summed;
   const b200_summed_info* summed;
-  // groups whose threshold code draws rand() once per neuron, in the order the
-  // reference's schedule runs their thresholds (the order of the draws)
-  int n_rng_groups;
-  const int* rng_groups;
-  // Poisson inputs (PoissonInput), in schedule order; they draw after the groups
-  int n_inputs;
-  const b200_input_info* inputs;
+  // the code objects that draw random numbers, in the order the reference's
+  // schedule runs them in a step (the order of the draws)
+  int n_draws;
+  const b200_draw_info* draws;
 };
 // `tcode` bit selecting the owner-mode kernel
 #define B200_TCODE_OWNER (1 << 20)
@@ -495,15 +496,22 @@ __device__ __forceinline__ bool b200_inst_wait(const b200_inst_d& I, unsigned& g
 
 // ---------------------------------------------------------------------------
 // The reference's random stream (brian2/devices/cpp_standalone/templates/
-// objects.cpp:426-453): a 32-bit Mersenne Twister (MT19937, Matsumoto and
-// Nishimura 1998) and rand() = (a*2^26 + b) / 2^53 from two outputs
-// a = w0 >> 5, b = w1 >> 6.  b200_mt_fill_kernel continues the generator from
-// its state (the 624 words and the position, as the C++ library stores them)
-// and writes the next `n_words` tempered outputs; one CTA of 640 threads, each
-// regeneration of the 624 words in three parallel sweeps.
+// objects.cpp:426-478): a 32-bit Mersenne Twister (MT19937, Matsumoto and
+// Nishimura 1998); rand() = (a*2^26 + b) / 2^53 from two outputs a = w0 >> 5,
+// b = w1 >> 6; randn() by the polar method (Marsaglia), which draws pairs
+// until one falls inside the unit circle, returns f*x2 and keeps f*x1 for the
+// next call.  How many outputs a step uses depends only on the stream, never on
+// the network, so b200_variates_kernel walks the stream ahead of a launch, in
+// the reference's order of draws, and writes one double per draw.
 // ---------------------------------------------------------------------------
 #define B200_MT_N 624
 #define B200_MT_M 397
+// kinds of draw sites (one per code object that draws, in schedule order)
+#define B200_DRAW_UNIFORM 0    // rand()
+#define B200_DRAW_NORMAL 1     // randn()
+#define B200_DRAW_BINOMIAL 2   // binomial by inversion (brian2/input/binomial.py:93-141)
+#define B200_DRAW_BINORMAL 3   // binomial, normal approximation: (float)(randn()*scale + loc)
+
 __device__ __forceinline__ uint32_t b200_mt_mix(uint32_t hi, uint32_t lo, uint32_t far) {
   const uint32_t y = (hi & 0x80000000u) | (lo & 0x7fffffffu);
   return far ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
@@ -515,50 +523,198 @@ __device__ __forceinline__ uint32_t b200_mt_temper(uint32_t y) {
   y ^= y >> 18;
   return y;
 }
-// state: [624 words, position]; out: n_words outputs.  Launch <<<1, 640>>>.
-__global__ void b200_mt_fill_kernel(uint32_t* state, uint32_t* out, int64_t n_words) {
-  __shared__ uint32_t x[B200_MT_N];
-  __shared__ int s_p;
+// The next 624 words of the state x (in shared memory), in place.  Sequentially
+// x[i] = x[i+M] ^ mix(x[i], x[i+1]) for i = 0..623, indices mod 624: each of
+// three sweeps reads the words it needs (x[i+1] before anyone writes it, the far
+// word after the previous sweep wrote it), then writes.  All threads of a block
+// of at least 624 threads call it.
+__device__ __forceinline__ void b200_mt_regen(uint32_t* x) {
   const int t = threadIdx.x;
-  if (t < B200_MT_N) x[t] = state[t];
-  if (t == 0) s_p = (int)state[B200_MT_N];
+  uint32_t v = 0;
+  if (t < 227) v = b200_mt_mix(x[t], x[t + 1], x[t + B200_MT_M]);
   __syncthreads();
-  int p = s_p;
-  int64_t done = 0;
-  while (done < n_words) {
-    if (p >= B200_MT_N) {
-      // sequentially x[i] = x[i+M] ^ mix(x[i], x[i+1]) for i = 0..623, indices
-      // mod 624: each sweep reads the words it needs (x[i+1] before anyone
-      // writes it, the far word after the previous sweep wrote it), then writes
-      uint32_t v = 0;
-      if (t < 227) v = b200_mt_mix(x[t], x[t + 1], x[t + B200_MT_M]);
-      __syncthreads();
-      if (t < 227) x[t] = v;
-      __syncthreads();
-      if (t >= 227 && t < 454) v = b200_mt_mix(x[t], x[t + 1], x[t - 227]);
-      __syncthreads();
-      if (t >= 227 && t < 454) x[t] = v;
-      __syncthreads();
-      if (t >= 454 && t < 623) v = b200_mt_mix(x[t], x[t + 1], x[t - 227]);
-      __syncthreads();
-      if (t >= 454 && t < 623) x[t] = v;
-      __syncthreads();
-      if (t == 0) x[623] = b200_mt_mix(x[623], x[0], x[396]);
-      __syncthreads();
-      p = 0;
-    }
-    const int64_t take = (n_words - done < (int64_t)(B200_MT_N - p)) ? n_words - done : (int64_t)(B200_MT_N - p);
-    for (int k = t; k < (int)take; k += blockDim.x) out[done + k] = b200_mt_temper(x[p + k]);
-    done += take;
-    p += (int)take;
-    __syncthreads();
-  }
-  if (t < B200_MT_N) state[t] = x[t];
-  if (t == 0) state[B200_MT_N] = (uint32_t)p;
+  if (t < 227) x[t] = v;
+  __syncthreads();
+  if (t >= 227 && t < 454) v = b200_mt_mix(x[t], x[t + 1], x[t - 227]);
+  __syncthreads();
+  if (t >= 227 && t < 454) x[t] = v;
+  __syncthreads();
+  if (t >= 454 && t < 623) v = b200_mt_mix(x[t], x[t + 1], x[t - 227]);
+  __syncthreads();
+  if (t >= 454 && t < 623) x[t] = v;
+  __syncthreads();
+  if (t == 0) x[623] = b200_mt_mix(x[623], x[0], x[396]);
+  __syncthreads();
 }
-__device__ __forceinline__ double b200_rand_from(const uint32_t* w) {
-  const long long a = (long long)(w[0] >> 5), b = (long long)(w[1] >> 6);
+__device__ __forceinline__ double b200_rand2(uint32_t w0, uint32_t w1) {
+  const long long a = (long long)(w0 >> 5), b = (long long)(w1 >> 6);
   return ((double)a * 67108864.0 + (double)b) / 9007199254740992.0;
+}
+
+// One draw site per step: `count` values (neurons x calls per neuron).
+struct b200_site_d {
+  int32_t kind, count;
+  int32_t n, reverse;           // binomial: trials; 1 = the sampler counts failures
+  double qn, bound, p, q;       // binomial by inversion, the reference's printed constants
+  double scale, loc;            // normal approximation
+};
+struct b200_sites_d {
+  int32_t n_sites, _pad;
+  b200_site_d s[B200_MAX_DRAWS];
+};
+
+// The draws of `steps` steps, continuing the generator: state = [624 words,
+// position] (the C++ library's form), gauss = [has a kept value (0/1), value]
+// (randn()'s cache); out[step][per_step] in site order.  Launch <<<1, 1024>>>.
+// A binomial draw past the bound starts over with a new number, as in the
+// reference; status gets B200_ERR_RANDOM if that needed more numbers than the
+// two blocks of outputs in shared memory hold (never at the probabilities the
+// bound allows).
+__global__ void __launch_bounds__(1024) b200_variates_kernel(uint32_t* state, double* gauss, b200_sites_d S,
+                                                           double* out, int64_t per_step, int64_t steps,
+                                                           int32_t* status) {
+  __shared__ uint32_t xc[B200_MT_N], xn[B200_MT_N];  // the current and the next block of the state
+  __shared__ int s_wsum[B200_MAX_WARPS + 1];
+  __shared__ int s_first, s_cend, s_has, s_used;
+  __shared__ double s_keep;
+  const int t = threadIdx.x;
+  if (t < B200_MT_N) { xc[t] = state[t]; xn[t] = state[t]; }
+  int p = (int)state[B200_MT_N];  // next output: xc[p] (p == 624: xn[0])
+  __syncthreads();
+  b200_mt_regen(xn);
+  bool has = gauss[0] != 0.0;
+  double kept = gauss[1];
+  // output o after the read position (o < 1248 - p)
+  auto word = [&](int o) -> uint32_t {
+    return b200_mt_temper(o < B200_MT_N - p ? xc[p + o] : xn[o - (B200_MT_N - p)]);
+  };
+  auto advance = [&](int k) {  // all threads, same k
+    __syncthreads();
+    p += k;
+    while (p >= B200_MT_N) {
+      if (t < B200_MT_N) xc[t] = xn[t];
+      __syncthreads();
+      b200_mt_regen(xn);
+      p -= B200_MT_N;
+    }
+  };
+  for (int64_t st = 0; st < steps; ++st) {
+    double* o_step = out + st * per_step;
+    for (int si = 0; si < S.n_sites; ++si) {
+      const b200_site_d& D = S.s[si];
+      double* const o = o_step;
+      o_step += D.count;
+      const int64_t K = D.count;
+      if (D.kind == B200_DRAW_UNIFORM) {
+        for (int64_t i = 0; i < K;) {
+          const int C = (int)(K - i < 312 ? K - i : 312);
+          if (t < C) o[i + t] = b200_rand2(word(2 * t), word(2 * t + 1));
+          advance(2 * C);
+          i += C;
+        }
+      } else if (D.kind == B200_DRAW_NORMAL || D.kind == B200_DRAW_BINORMAL) {
+        const bool tr = D.kind == B200_DRAW_BINORMAL;
+        auto value = [&](double v) -> double {
+          return tr ? (double)__double2float_rn(__dadd_rn(__dmul_rn(v, D.scale), D.loc)) : v;
+        };
+        int64_t i = 0;
+        if (K > 0 && has) {  // the value kept by the previous call
+          if (t == 0) o[0] = value(kept);
+          has = false;
+          i = 1;
+        }
+        while (i < K) {
+          const int64_t need = (K - i + 1) / 2;  // pairs still to accept
+          const int C = 156;                     // candidates (4 outputs each) looked at together
+          double x1 = 0.0, x2 = 0.0, r2 = 0.0;
+          bool acc = false;
+          if (t < C) {
+            x1 = __dsub_rn(__dmul_rn(2.0, b200_rand2(word(4 * t), word(4 * t + 1))), 1.0);
+            x2 = __dsub_rn(__dmul_rn(2.0, b200_rand2(word(4 * t + 2), word(4 * t + 3))), 1.0);
+            r2 = __dadd_rn(__dmul_rn(x1, x1), __dmul_rn(x2, x2));
+            acc = !(r2 >= 1.0 || r2 == 0.0);
+          }
+          if (t == 0) { s_cend = C; s_has = 0; }
+          int tot;
+          const int r = b200_block_compact(acc, s_wsum, &tot);
+          const int64_t use = tot < need ? tot : need;
+          if (acc && r < use) {
+            const double f = __dsqrt_rn(__ddiv_rn(__dmul_rn(-2.0, log(r2)), r2));
+            const int64_t j = i + 2 * (int64_t)r;
+            o[j] = value(__dmul_rn(f, x2));
+            if (j + 1 < K) o[j + 1] = value(__dmul_rn(f, x1));
+            else { s_has = 1; s_keep = __dmul_rn(f, x1); }
+            if (r == use - 1 && tot >= need) s_cend = t + 1;
+          }
+          __syncthreads();
+          const int used = s_cend;
+          if (s_has) { has = true; kept = s_keep; }
+          advance(4 * used);
+          i += 2 * use;
+        }
+      } else {  // B200_DRAW_BINOMIAL
+        const double nn = (double)D.n;
+        for (int64_t i = 0; i < K;) {
+          const int C = (int)(K - i < 312 ? K - i : 312);
+          if (t == 0) s_first = C;
+          __syncthreads();
+          if (t < C) {
+            double U = b200_rand2(word(2 * t), word(2 * t + 1)), px = D.qn;
+            long long X = 0;
+            bool redraw = false;
+            while (U > px) {
+              X++;
+              if ((double)X > D.bound) { redraw = true; break; }
+              U = __dsub_rn(U, px);
+              px = __ddiv_rn(__dmul_rn(__dmul_rn((double)(D.n - X + 1), D.p), px), __dmul_rn((double)X, D.q));
+            }
+            if (redraw) atomicMin(&s_first, t);
+            else o[i + t] = D.reverse ? nn - (double)X : (double)X;
+          }
+          __syncthreads();
+          const int first = s_first;
+          if (first == C) {
+            advance(2 * C);
+            i += C;
+            continue;
+          }
+          // the draws before `first` stand; `first` starts over with new numbers
+          advance(2 * first);
+          if (t == 0) {
+            const int win = 2 * B200_MT_N - p;
+            int used = 2;
+            double U = b200_rand2(word(0), word(1)), px = D.qn;
+            long long X = 0;
+            while (U > px) {
+              X++;
+              if ((double)X > D.bound) {
+                X = 0;
+                px = D.qn;
+                if (used + 2 > win) { atomicCAS(status, 0, B200_ERR_RANDOM); break; }
+                U = b200_rand2(word(used), word(used + 1));
+                used += 2;
+              } else {
+                U = __dsub_rn(U, px);
+                px = __ddiv_rn(__dmul_rn(__dmul_rn((double)(D.n - X + 1), D.p), px), __dmul_rn((double)X, D.q));
+              }
+            }
+            o[i + first] = D.reverse ? nn - (double)X : (double)X;
+            s_used = used;
+          }
+          __syncthreads();
+          advance(s_used);
+          i += first + 1;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (t < B200_MT_N) state[t] = xc[t];
+  if (t == 0) {
+    state[B200_MT_N] = (uint32_t)p;
+    gauss[0] = has ? 1.0 : 0.0;
+    gauss[1] = kept;
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -93,9 +93,9 @@ struct b200_inst_h {
   b200_dbuf bar, status, ts_done, pending, bar64;
   int32_t ran_owner = -1;  // mode of the runs so far with spikes in flight: -1 none, 0 classic, 1 owner
   // random stream of the step loop: generator state on the device (624 words +
-  // position), and two buffers of generated words; rng_buf[rng_cur] holds the
-  // words of steps [rng_from, rng_to), and the state is at rng_to
-  b200_dbuf rng_state, rng_buf[2];
+  // position; randn()'s kept value), and two buffers of draws; rng_buf[rng_cur]
+  // holds the draws of steps [rng_from, rng_to), and the state is at rng_to
+  b200_dbuf rng_state, rng_gauss, rng_buf[2];
   int rng_cur = 0;
   int64_t rng_from = 0, rng_to = 0;
   bool rng_set = false;
@@ -263,7 +263,7 @@ int b200_destroy(b200_net* n) {
     for (auto& S : I.rm) b200_free(n, S.cnt);
     for (auto& S : I.stm) { b200_free(n, S.d_idx); b200_free(n, S.n); b200_free(n, S.data); }
     for (auto& S : I.sum) { b200_free(n, S.seg); b200_free(n, S.syn); }
-    b200_free(n, I.rng_state); b200_free(n, I.rng_buf[0]); b200_free(n, I.rng_buf[1]);
+    b200_free(n, I.rng_state); b200_free(n, I.rng_gauss); b200_free(n, I.rng_buf[0]); b200_free(n, I.rng_buf[1]);
     b200_free(n, I.bar); b200_free(n, I.status); b200_free(n, I.ts_done); b200_free(n, I.pending);
     b200_free(n, I.bar64);
   }
@@ -1292,56 +1292,58 @@ int b200_run(b200_net* n, int64_t n_steps) {
     }
     if (!any) break;
     int64_t steps = n->chunk_steps;
-    if (M->n_rng_groups > 0 || M->n_inputs > 0) {
-      // the random words of the launch's steps, continuing the generator: per
-      // step the drawing groups' thresholds, then the Poisson inputs
-      auto in_size = [&](const b200_inst_h& I, int q) -> int64_t {
-        const b200_input_info& In = M->inputs[q];
-        return (In.hi < 0 ? I.g[In.group].N : In.hi) - In.lo;
+    if (M->n_draws > 0) {
+      // the draws of the launch's steps, continuing the generator, in the order
+      // of the draw sites (the reference's schedule)
+      auto site_count = [&](const b200_inst_h& I, int q) -> int64_t {
+        const b200_draw_info& D = M->draws[q];
+        return ((D.hi < 0 ? (int64_t)I.g[D.group].N : (int64_t)D.hi) - D.lo) * D.calls;
       };
       int64_t per_step = 0;
-      for (int q = 0; q < M->n_rng_groups; ++q) per_step += n->inst[0].g[M->rng_groups[q]].N;
-      for (int q = 0; q < M->n_inputs; ++q) per_step += in_size(n->inst[0], q);
-      const int64_t wps = std::max<int64_t>(2 * per_step, 1);  // words per step
-      steps = std::max<int64_t>(1, std::min<int64_t>(steps, ((int64_t)128 << 20) / 4 / wps));
+      for (int q = 0; q < M->n_draws; ++q) per_step += site_count(n->inst[0], q);
+      steps = std::max<int64_t>(1, std::min<int64_t>(steps, ((int64_t)128 << 20) / 8 / std::max<int64_t>(per_step, 1)));
       for (int k = 0; k < n->n_inst; ++k) {
         b200_inst_h& I = n->inst[k];
-        b200_inst_d& D = n->h_insts[k];
+        b200_inst_d& Dd = n->h_insts[k];
         if (!I.rng_set) return b200_fail(n, B200_ERR_ARG, "instance %d: the model draws random numbers; set the generator (b200_set_rng)", k);
+        b200_sites_d sites = {};
+        sites.n_sites = M->n_draws;
         int64_t pk = 0;
-        for (int q = 0; q < M->n_rng_groups; ++q) {
-          D.rng_off[M->rng_groups[q]] = (int32_t)pk;
-          pk += I.g[M->rng_groups[q]].N;
+        for (int q = 0; q < M->n_draws; ++q) {
+          const b200_draw_info& D = M->draws[q];
+          const int64_t c = site_count(I, q);
+          if (D.lo < 0 || c < 0 || D.lo + c / std::max(D.calls, 1) > I.g[D.group].N)
+            return b200_fail(n, B200_ERR_ARG, "instance %d: draw site '%s' covers neurons outside its group", k, D.name);
+          Dd.draw_off[q] = (int32_t)pk;
+          b200_site_d& S = sites.s[q];
+          S.kind = D.kind; S.count = (int32_t)c; S.n = D.n; S.reverse = D.reverse;
+          S.qn = D.qn; S.bound = D.bound; S.p = D.p; S.q = D.q; S.scale = D.scale; S.loc = D.loc;
+          pk += c;
         }
-        for (int q = 0; q < M->n_inputs; ++q) {
-          const b200_input_info& In = M->inputs[q];
-          if (In.lo < 0 || in_size(I, q) < 0 || In.lo + in_size(I, q) > I.g[In.group].N)
-            return b200_fail(n, B200_ERR_ARG, "instance %d: Poisson input '%s' targets neurons outside its group", k, In.name);
-          D.rng_in_off[q] = (int32_t)pk;
-          pk += in_size(I, q);
-        }
-        D.rng_per_step = (int32_t)pk;
-        const int64_t w_k = std::max<int64_t>(2 * pk, 1);
+        if (pk > INT32_MAX) return b200_fail(n, B200_ERR_ARG, "instance %d: too many draws per step", k);
+        Dd.rng_per_step = (int32_t)pk;
+        const int64_t w_k = std::max<int64_t>(pk, 1);
         const int64_t end = std::min<int64_t>(target[k], I.ts + steps);
         if (I.rng_from > I.ts || I.rng_to < I.ts)
           return b200_fail(n, B200_ERR_ARG, "instance %d: random stream position lost", k);
         if (end > I.rng_to) {
-          // move the words still unused to the other buffer, generate the rest after them
+          // move the draws still unused to the other buffer, draw the rest after them
           const int nb = 1 - I.rng_cur;
           const int64_t keep = I.rng_to - I.ts;
-          if ((r = b200_alloc(n, I.rng_buf[nb], (size_t)std::max<int64_t>(end - I.ts, 1) * w_k * 4, false))) return r;
+          if ((r = b200_alloc(n, I.rng_buf[nb], (size_t)std::max<int64_t>(end - I.ts, 1) * w_k * 8, false))) return r;
           if (keep > 0)
-            B200_CU(n, cudaMemcpyAsync(I.rng_buf[nb].p, (uint32_t*)I.rng_buf[I.rng_cur].p + (I.ts - I.rng_from) * w_k,
-                                       (size_t)keep * w_k * 4, cudaMemcpyDeviceToDevice, n->stream));
-          b200_mt_fill_kernel<<<1, 640, 0, n->stream>>>((uint32_t*)I.rng_state.p,
-                                                       (uint32_t*)I.rng_buf[nb].p + keep * w_k, (end - I.rng_to) * 2 * pk);
+            B200_CU(n, cudaMemcpyAsync(I.rng_buf[nb].p, (double*)I.rng_buf[I.rng_cur].p + (I.ts - I.rng_from) * w_k,
+                                       (size_t)keep * w_k * 8, cudaMemcpyDeviceToDevice, n->stream));
+          b200_variates_kernel<<<1, 1024, 0, n->stream>>>((uint32_t*)I.rng_state.p, (double*)I.rng_gauss.p, sites,
+                                                          (double*)I.rng_buf[nb].p + keep * w_k, pk, end - I.rng_to,
+                                                          (int32_t*)I.status.p);
           B200_CU(n, cudaGetLastError());
           I.rng_cur = nb;
           I.rng_from = I.ts;
           I.rng_to = end;
         }
-        D.rng_words = (const uint32_t*)I.rng_buf[I.rng_cur].p + (I.ts - I.rng_from) * w_k;
-        D.rng_ts0 = I.ts;
+        Dd.rng_vals = (const double*)I.rng_buf[I.rng_cur].p + (I.ts - I.rng_from) * w_k;
+        Dd.rng_ts0 = I.ts;
       }
     }
     if (n->owner) {  // the split barrier counts the arrivals of this launch from 0
@@ -1418,9 +1420,8 @@ int b200_run(b200_net* n, int64_t n_steps) {
         if (st == B200_ERR_RANDOM) {
           I.ts = done;
           return b200_fail(n, B200_STATUS_RANDOM_H,
-                           "instance %d: a Poisson input's binomial draw before step %lld was rejected and needs a "
-                           "second random number (the reference redraws; the device's layout of the stream "
-                           "gives one per neuron and step)", k, (long long)done);
+                           "instance %d: a binomial draw before step %lld started over more often than the "
+                           "stream's window holds numbers", k, (long long)done);
         }
         if (st == B200_ERR_EVENT_OVERFLOW) {
           I.ts = done;
@@ -1558,16 +1559,39 @@ int b200_set_rng(b200_net* n, int32_t inst, const uint32_t* words, int32_t posit
   b200_inst_h& I = n->inst[inst];
   int r;
   if ((r = b200_alloc(n, I.rng_state, 625 * 4, false))) return r;
+  if ((r = b200_alloc(n, I.rng_gauss, 16, false))) return r;
   std::vector<uint32_t> st(words, words + 624);
   st.push_back((uint32_t)position);
   B200_CU(n, cudaMemcpy(I.rng_state.p, st.data(), 625 * 4, cudaMemcpyHostToDevice));
+  const double g[2] = {0.0, 0.0};  // no value kept by randn()
+  B200_CU(n, cudaMemcpy(I.rng_gauss.p, g, 16, cudaMemcpyHostToDevice));
   I.rng_from = I.rng_to = I.ts;
   I.rng_set = true;
   return 0;
 }
 
-// The generator's state after the words generated so far (words the step loop
-// has not consumed yet are included: `unused` reports how many steps of them).
+// randn()'s kept value (the second value of its last pair, returned by the
+// next call; RandomGenerator::randn, objects.cpp:455-477).
+int b200_set_rng_gauss(b200_net* n, int32_t inst, int32_t has, double value) {
+  if (!n || inst < 0 || inst >= n->n_inst || !n->inst[inst].rng_set)
+    return b200_fail(n, B200_ERR_ARG, "set the generator (b200_set_rng) first");
+  b200_inst_h& I = n->inst[inst];
+  if (I.rng_to != I.ts) return b200_fail(n, B200_ERR_ARG, "the generator has draws ahead of the step");
+  const double g[2] = {has ? 1.0 : 0.0, value};
+  B200_CU(n, cudaMemcpy(I.rng_gauss.p, g, 16, cudaMemcpyHostToDevice));
+  return 0;
+}
+int b200_get_rng_gauss(b200_net* n, int32_t inst, int32_t* has, double* value) {
+  if (!n || inst < 0 || inst >= n->n_inst || !n->inst[inst].rng_set) return b200_fail(n, B200_ERR_ARG, "no generator");
+  double g[2];
+  B200_CU(n, cudaMemcpy(g, n->inst[inst].rng_gauss.p, 16, cudaMemcpyDeviceToHost));
+  if (has) *has = g[0] != 0.0;
+  if (value) *value = g[1];
+  return 0;
+}
+
+// The generator's state after the draws made so far (draws the step loop has
+// not consumed yet are included: `unused` reports how many steps of them).
 int b200_get_rng(b200_net* n, int32_t inst, uint32_t* words, int32_t* position, int64_t* unused_steps) {
   if (!n || inst < 0 || inst >= n->n_inst || !n->inst[inst].rng_set) return b200_fail(n, B200_ERR_ARG, "no generator");
   std::vector<uint32_t> st(625);

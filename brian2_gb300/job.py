@@ -86,8 +86,8 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None)
         net.set_statemon(0, mi, init[f"stm{mi}_idx"], list(init[f"stm{mi}_vars"]))
     ts0 = int(init["ts0"])
     net.set_step(0, ts0)
-    if spec.get("rng_groups") or spec.get("inputs"):  # the reference's generator, where the step loop starts drawing
-        net.set_rng(0, init["rng_words"], int(init["rng_position"]))
+    if spec.get("draws"):  # the reference's generator, where the step loop starts drawing
+        net.set_rng(0, init["rng_words"], int(init["rng_position"]), init.get("rng_gauss"))
     net.reset_monitors(0)
     total_ms, t0 = 0.0, time.time()
     for n in job["runs"]:

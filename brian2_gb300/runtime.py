@@ -76,6 +76,8 @@ def _declare(lib):
         "b200_set_generator": [h, C.c_int32, C.c_int32, _i32p, _i32p, C.c_int64, C.c_int32, C.c_int32],
         "b200_set_rng": [h, C.c_int32, C.POINTER(C.c_uint32), C.c_int32],
         "b200_get_rng": [h, C.c_int32, C.POINTER(C.c_uint32), _i32p, _i64p],
+        "b200_set_rng_gauss": [h, C.c_int32, C.c_int32, C.c_double],
+        "b200_get_rng_gauss": [h, C.c_int32, _i32p, C.POINTER(C.c_double)],
         "b200_get_generator": [h, C.c_int32, C.c_int32, _i32p],
         "b200_launch_plan": [h, _i32p, _i32p, _i32p],
         "b200_profile_phases": [h, _i32p],
@@ -245,13 +247,22 @@ class Network:
         self._check(self.lib.b200_set_generator(self._h, int(inst), g, _ptr(b, _i32p), _ptr(i, _i32p), b.size,
                                                 int(period_bins), int(last)))
 
-    def set_rng(self, inst, words, position):
+    def set_rng(self, inst, words, position, gauss=None):
         """The random generator of the step loop: the reference's MT19937 state
-        (624 words and the position, as the C++ library stores them)."""
+        (624 words and the position, as the C++ library stores them) and, if
+        given, randn()'s kept value as (has, value)."""
         w = np.ascontiguousarray(words, dtype=np.uint32)
         if w.size != 624:
             raise ValueError("624 state words expected")
         self._check(self.lib.b200_set_rng(self._h, int(inst), _ptr(w, C.POINTER(C.c_uint32)), int(position)))
+        if gauss is not None and int(gauss[0]):
+            self._check(self.lib.b200_set_rng_gauss(self._h, int(inst), 1, float(gauss[1])))
+
+    def rng_gauss(self, inst=0):
+        """randn()'s kept value: (has, value)."""
+        has, val = C.c_int32(), C.c_double()
+        self._check(self.lib.b200_get_rng_gauss(self._h, int(inst), C.byref(has), C.byref(val)))
+        return bool(has.value), float(val.value)
 
     def rng_state(self, inst=0):
         """(words, position, steps generated ahead and not yet consumed)."""

@@ -81,20 +81,25 @@ int b200_set_event_capacity(b200_net* net, double factor);
 int b200_set_generator(b200_net* net, int32_t inst, int32_t group, const int32_t* bins, const int32_t* index,
                        int64_t count, int32_t period_bins, int32_t last);
 int b200_get_generator(b200_net* net, int32_t inst, int32_t group, int32_t* last);
-/* The random generator of the step loop, for models whose threshold code draws
- * rand() once per neuron (PoissonGroup, brian2/input/poissongroup.py) or that
- * have Poisson inputs (PoissonInput, brian2/input/poissoninput.py, one binomial
- * draw per target neuron and step, brian2/input/binomial.py:93-141): the
- * reference's MT19937 state as the C++ library stores it (624 words, then the
- * position), taken where the standalone program starts the run
- * (brian::_random_generators[0], templates/objects.cpp:426-453).  The device
- * continues that stream in the reference's order of draws (threshold groups,
- * then Poisson inputs, in schedule order; neurons in index order; rand() =
- * (a*2^26 + b)/2^53 of two outputs).
+/* The random generator of the step loop, for models that draw in it: rand() in
+ * threshold code (PoissonGroup, brian2/input/poissongroup.py), randn() in state
+ * updates (stochastic equations, brian2/stateupdaters/explicit.py), the binomial
+ * counts of Poisson inputs (brian2/input/poissoninput.py, binomial.py:93-141):
+ * the reference's MT19937 state as the C++ library stores it (624 words, then
+ * the position), taken where the standalone program starts the run
+ * (brian::_random_generators[0], templates/objects.cpp:426-478).  The device
+ * continues that stream in the reference's order of draws (code objects in
+ * schedule order, neurons in index order; rand() = (a*2^26 + b)/2^53 of two
+ * outputs; randn() by the polar method).
  * b200_get_rng returns the generator state and the steps of words generated
  * ahead of the current step. */
 int b200_set_rng(b200_net* net, int32_t inst, const uint32_t* words, int32_t position);
 int b200_get_rng(b200_net* net, int32_t inst, uint32_t* words, int32_t* position, int64_t* unused_steps);
+/* randn()'s kept value (objects.cpp:455-477: the polar method returns one value
+ * of each accepted pair and keeps the other for the next call): set after
+ * b200_set_rng when the program had one kept where the run starts. */
+int b200_set_rng_gauss(b200_net* net, int32_t inst, int32_t has, double value);
+int b200_get_rng_gauss(b200_net* net, int32_t inst, int32_t* has, double* value);
 /* Per-instance values of the model's namespace constants (the %CONSTANTS% of the
  * generated code objects, device.py:936-940); scalar blocks are re-evaluated. */
 int b200_set_consts(b200_net* net, int32_t inst, const double* values, int32_t count);

@@ -439,6 +439,40 @@ def poisson_drive(N=400, duration_ms=200.0, seed_value=202):
     return dict(P=P, spikes=s_mon, rate=r_mon, state=st)
 
 
+def noise_inputs(N=300, duration_ms=200.0, seed_value=303):
+    """randn() in the step loop: a stochastic population (two noise terms per
+    neuron, Euler-Maruyama) and a second noisy group of odd size, so randn()'s
+    kept value passes from site to site and from step to step (one is kept
+    already where the run starts: the second group's initial values draw an
+    odd number); a PoissonInput large enough for Brian's normal approximation
+    ((float)(randn()*scale + loc)) and one small enough for inversion."""
+    from brian2 import (NeuronGroup, PoissonInput, Synapses, SpikeMonitor, PopulationRateMonitor, StateMonitor,
+                        ms, mV, Hz, seed, run)
+    seed(seed_value)
+    ns = dict(taum=20 * ms, taue=5 * ms, Vt=-50 * mV, Vr=-60 * mV, El=-60 * mV, sigma=3 * mV, sig_e=0.5 * mV,
+              we=0.5 * mV, wq=1 * mV)
+    P = NeuronGroup(N, '''dv/dt = (ge - (v - El))/taum + sigma*xi*taum**-0.5 : volt
+                          dge/dt = -ge/taue + sig_e*xi_e*taue**-0.5 : volt''',
+                    threshold='v>Vt', reset='v = Vr', method='euler', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    Q = NeuronGroup(51, 'dx/dt = -x/(10*ms) + 0.5*xi/sqrt(ms) : 1', threshold='x > 0.8', reset='x = 0',
+                    method='euler', namespace=ns)
+    Q.x = 'randn() * 0.1'
+    S = Synapses(P, P, on_pre='ge += we', namespace=ns)
+    S.connect(p=0.05)
+    S.delay = 'rand() * 2*ms'
+    T = Synapses(Q, P, on_pre='ge += wq', namespace=ns)
+    T.connect(p=0.1)
+    in_big = PoissonInput(P, 'ge', 5000, 20 * Hz, weight=0.05 * mV)         # N*p = 10: normal approximation
+    in_small = PoissonInput(P[0:100], 'v', 50, 40 * Hz, weight=0.3 * mV)    # N*p = 0.2: inversion
+    s_mon = SpikeMonitor(P)
+    r_mon = PopulationRateMonitor(P)
+    q_mon = SpikeMonitor(Q)
+    st = StateMonitor(P, 'v', record=[0, 150, 299])
+    run(duration_ms * ms)
+    return dict(P=P, spikes=s_mon, rate=r_mon, state=st, other_spikes=q_mon)
+
+
 SCENARIOS = {
     "lif_refractory": lif_refractory,
     "hetero_delays": hetero_delays,
@@ -451,4 +485,5 @@ SCENARIOS = {
     "explicit_methods": explicit_methods,
     "poisson_input": poisson_input,
     "poisson_drive": poisson_drive,
+    "noise_inputs": noise_inputs,
 }

@@ -93,32 +93,59 @@ def render_oracle(spec: dict) -> str:
     w("template <typename T> static inline int int_(T v) { return (int)v; }")
     w("static inline int64_t _timestep(double t, double dt) { return (int64_t)((t + 1e-3 * dt) / dt); }")
     w("#define _brian_abs fabs")
-    RNG = spec.get("rng_groups", [])
     INPUTS = spec.get("inputs", [])
-    DRAWS = bool(RNG or INPUTS)
+    SITES = spec.get("draws", [])
+    DRAWS = bool(SITES)
     if DRAWS:
         w("#include <random>\n#include <sstream>\n#include <string>")
         w("static std::mt19937* _b200_gen = nullptr;")
+        w("static bool* _b200_has = nullptr; static double* _b200_kept = nullptr;")
         w("static inline double _rand(int64_t) {")
         w("  const long a = (long)((*_b200_gen)() >> 5);")
         w("  const long b = (long)((*_b200_gen)() >> 6);")
         w("  return (a * 67108864.0 + b) / 9007199254740992.0;")
         w("}")
-    for k, inp in enumerate(INPUTS):
-        bn = inp["binom"]
-        w(f"static inline long _b200_binomial_{k}(int64_t _vidx) {{  // inversion, with the reference's constants")
-        w(f"  long X = 0; double px = {bn['qn']}; double U = _rand(_vidx);")
-        w("  while (U > px) {")
-        w("    X++;")
-        w(f"    if (X > {bn['bound']}) {{ X = 0; px = {bn['qn']}; U = _rand(_vidx); }}  // start over with a new draw")
-        w(f"    else {{ U -= px; px = (({bn['n']} - X + 1) * {bn['p']} * px) / (X * {bn['q']}); }}")
-        w("  }")
-        w(f"  return {str(bn['n']) + ' - X' if bn['reverse'] else 'X'};")
+        # the polar method, keeping the second value for the next call
+        w("static inline double _randn(int64_t i) {")
+        w("  if (*_b200_has) { *_b200_has = false; return *_b200_kept; }")
+        w("  double x1, x2, r2;")
+        w("  do { x1 = 2.0 * _rand(i) - 1.0; x2 = 2.0 * _rand(i) - 1.0; r2 = x1 * x1 + x2 * x2; } while (r2 >= 1.0 || r2 == 0.0);")
+        w("  const double f = sqrt(-2.0 * log(r2) / r2);")
+        w("  *_b200_kept = f * x1; *_b200_has = true;")
+        w("  return f * x2;")
         w("}")
+    for si, d in enumerate(SITES):
+        bn = d.get("binom") or {}
+        if d["kind"] in ("rand", "randn"):
+            for c in range(d["calls"]):
+                w(f"#define _b200_draw_{si}_{c}(i) _{d['kind']}(i)")
+        elif d["kind"] == "binomial":
+            w(f"static inline long _b200_draw_{si}_0(int64_t _vidx) {{  // inversion, with the reference's constants")
+            w(f"  long X = 0; double px = {bn['qn']}; double U = _rand(_vidx);")
+            w("  while (U > px) {")
+            w("    X++;")
+            w(f"    if (X > {bn['bound']}) {{ X = 0; px = {bn['qn']}; U = _rand(_vidx); }}  // start over with a new draw")
+            w(f"    else {{ U -= px; px = (({bn['n']} - X + 1) * {bn['p']} * px) / (X * {bn['q']}); }}")
+            w("  }")
+            w(f"  return {str(bn['n']) + ' - X' if bn['reverse'] else 'X'};")
+            w("}")
+        else:  # normal approximation
+            w(f"static inline float _b200_draw_{si}_0(int64_t _vidx) {{ return _randn(_vidx) * {bn['scale']} + {bn['loc']}; }}")
+    # blocks that draw run in the order of their sites (the schedule's order)
+    site_of = {}
+    for si, d in enumerate(SITES):
+        if d["kind"] in ("rand", "randn"):
+            blk = next(b for b in ("update", "threshold") if (groups[d["group"]].get(b) or {}).get("draw") == si)
+            site_of[(d["group"], blk)] = si
+
+    def block_order(blk):
+        plain = [gi for gi in range(len(groups)) if (gi, blk) not in site_of]
+        return plain + sorted((gi for gi in range(len(groups)) if (gi, blk) in site_of),
+                              key=lambda gi: site_of[(gi, blk)])
     w("struct Net {")
     w("  double dt; int64_t ts = 0;")
     if DRAWS:
-        w("  std::mt19937 gen;")
+        w("  std::mt19937 gen; bool has = false; double kept = 0.0;")
     w("  std::vector<double> c;")
     for gi, g in enumerate(groups):
         w(f"  int32_t N{gi} = 0;")
@@ -207,8 +234,12 @@ def render_oracle(spec: dict) -> str:
     if DRAWS:  # (the C++ library's text form of the state: the 624 words, then the position)
         w("  std::ostringstream o; for (int k = 0; k < 624; ++k) o << words[k] << ' '; o << pos;")
         w("  std::istringstream in(o.str()); in >> n->gen;")
+        w("  n->has = false;")
     else:
         w("  (void)n; (void)words; (void)pos;")
+    w("}")
+    w("void oracle_set_gauss(Net* n, int32_t has, double value) {")
+    w("  n->has = has != 0; n->kept = value;" if DRAWS else "  (void)n; (void)has; (void)value;")
     w("}")
     w("void oracle_set_range(Net* n, int32_t kind, int32_t mon, int32_t lo, int32_t hi) {")
     for mi, m in enumerate(spkmons):
@@ -224,7 +255,7 @@ def render_oracle(spec: dict) -> str:
     # ---- the step loop
     w("void oracle_run(Net* n, int64_t n_steps) {")
     if DRAWS:
-        w("  _b200_gen = &n->gen;")
+        w("  _b200_gen = &n->gen; _b200_has = &n->has; _b200_kept = &n->kept;")
     for k, cst in enumerate(consts):
         w(f"  const {cst['ctype']} {cst['name']} = ({cst['ctype']})n->c[{k}]; (void){cst['name']};")
     w("  const double _dt_v = n->dt;")
@@ -286,8 +317,10 @@ def render_oracle(spec: dict) -> str:
         w("        }")
         w("      }")
         w("    }")
-    # state updaters of all groups
-    for gi, g in enumerate(groups):
+    # state updaters of all groups (those drawing random numbers last, in the
+    # schedule's order)
+    for gi in block_order("update"):
+        g = groups[gi]
         if not g.get("update"):
             continue
         w("    {")
@@ -303,7 +336,7 @@ def render_oracle(spec: dict) -> str:
         w("      }")
         w("    }")
     # thresholders (those drawing random numbers last, in the schedule's order)
-    for gi in [k for k in range(len(groups)) if k not in RNG] + list(RNG):
+    for gi in block_order("threshold"):
         g = groups[gi]
         w("    {")
         w(gptrs(gi, 6))
@@ -488,6 +521,7 @@ class OracleNet:
             lib.oracle_get_generator.restype = C.c_int32
             lib.oracle_set_step.argtypes = [C.c_void_p, C.c_int64]
             lib.oracle_set_rng.argtypes = [C.c_void_p, C.POINTER(C.c_uint32), C.c_int32]
+            lib.oracle_set_gauss.argtypes = [C.c_void_p, C.c_int32, C.c_double]
         self.lib = lib
         self.sizes = np.ascontiguousarray(sizes, dtype=np.int32).reshape(-1)
         self.h = lib.oracle_create(self.sizes.ctypes.data_as(_i32p), float(dt))
@@ -587,9 +621,11 @@ class OracleNet:
     def set_step(self, ts):
         self.lib.oracle_set_step(self.h, int(ts))
 
-    def set_rng(self, words, position):
+    def set_rng(self, words, position, gauss=None):
         w = np.ascontiguousarray(words, np.uint32)
         self.lib.oracle_set_rng(self.h, w.ctypes.data_as(C.POINTER(C.c_uint32)), int(position))
+        if gauss is not None:  # randn()'s kept value: (has, value)
+            self.lib.oracle_set_gauss(self.h, int(gauss[0]), float(gauss[1]))
 
     def run(self, n_steps):
         self.lib.oracle_run(self.h, int(n_steps))
@@ -677,8 +713,8 @@ def run_job_on_oracle(directory):
     for mi in range(len(spec.get("state_monitors", []))):
         o.set_statemon(mi, init[f"stm{mi}_idx"], list(init[f"stm{mi}_vars"]))
     o.set_step(int(init["ts0"]))
-    if spec.get("rng_groups") or spec.get("inputs"):
-        o.set_rng(init["rng_words"], int(init["rng_position"]))
+    if spec.get("draws"):
+        o.set_rng(init["rng_words"], int(init["rng_position"]), init.get("rng_gauss"))
     for n in job["runs"]:
         o.run(int(n))
     out = {}

@@ -34,7 +34,8 @@ def test_job_carries_the_reference_network(case, golden):
 
 
 SCENARIOS = ["lif_refractory", "hetero_delays", "subgroup_monitors", "input_group", "presynaptic_read",
-             "spike_generator", "stdp", "gap_junctions", "explicit_methods", "poisson_input"]
+             "spike_generator", "stdp", "gap_junctions", "explicit_methods", "poisson_input", "poisson_drive",
+             "noise_inputs"]
 
 
 @pytest.mark.parametrize("name", SCENARIOS)
@@ -51,11 +52,26 @@ def test_scenario_jobs_describe_their_features(name):
         assert list(init["stm0_idx"]) == [0, 10, 250, 499]
     if name == "input_group":
         assert len(spec["groups"]) == 2 and {p["src"] for p in spec["pathways"]} == {0, 1}
-    if name == "poisson_input":  # rand() in two PoissonGroups' thresholds: the generator state travels
-        assert len(spec["rng_groups"]) == 2 and init["rng_words"].dtype == np.uint32
-        assert init["rng_words"].size == 624 and 0 <= int(init["rng_position"]) <= 624
-        for gi in spec["rng_groups"]:
-            assert spec["groups"][gi]["threshold"]["rng"] and "_rand(" in spec["groups"][gi]["threshold"]["vector"]
+    if name in ("poisson_input", "poisson_drive", "noise_inputs"):  # the generator state travels
+        assert init["rng_words"].dtype == np.uint32 and init["rng_words"].size == 624
+        assert 0 <= int(init["rng_position"]) <= 624 and init["rng_gauss"].shape == (2,)
+        for si, d in enumerate(spec["draws"]):  # every draw site's calls are its macros
+            if d["kind"] in ("rand", "randn"):
+                blk = next(b for b in ("update", "threshold") if (spec["groups"][d["group"]].get(b) or {}).get("draw") == si)
+                code = spec["groups"][d["group"]][blk]["vector"]
+            else:
+                code = next(inp for inp in spec["inputs"] if inp["draw"] == si)["code"]["vector"]
+            assert code.count(f"_b200_draw_{si}_") == d["calls"] and "_rand(" not in code and "_randn(" not in code
+    if name == "poisson_input":  # rand() in two PoissonGroups' thresholds
+        assert [d["kind"] for d in spec["draws"]] == ["rand", "rand"]
+    if name == "poisson_drive":  # a PoissonGroup, then three inputs by inversion (one reversed)
+        assert [d["kind"] for d in spec["draws"]] == ["rand", "binomial", "binomial", "binomial"]
+        assert [d["binom"]["reverse"] for d in spec["draws"][1:]] == [False, False, True]
+        assert [(d["lo"], d["hi"]) for d in spec["draws"][1:]] == [(0, -1), (50, 250), (300, 400)]
+    if name == "noise_inputs":  # randn() in two updates (schedule order: by name), both samplers
+        assert [(d["kind"], d["calls"]) for d in spec["draws"]] == [("randn", 1), ("randn", 2), ("binormal", 1),
+                                                                    ("binomial", 1)]
+        assert int(init["rng_gauss"][0]) == 1  # the initial values left one kept
     if name == "gap_junctions":  # a summed variable over a Synapses object without on_pre
         (sm,) = spec["summed"]
         pw = spec["pathways"][sm["pathway"]]
