@@ -22,7 +22,9 @@ How the work is split with Brian's own machinery (the device subclasses
   unchanged (``device.py:544-585``).
 
 Limits (raise ``NotImplementedError``, which Brian's test runner treats as
-"not supported by this device"): one clock for all step-loop objects; no host
+"not supported by this device"): one clock for all step-loop objects (but
+``run_regularly`` operations in the start and end slots may run every k-th
+step); no host
 code between two ``run()`` calls; random numbers inside the step loop other
 than one ``rand()`` per neuron in threshold code (PoissonGroup) and the
 binomial draws of ``PoissonInput`` without its normal approximation (both need
@@ -43,6 +45,7 @@ from brian2.core.clocks import Clock
 from brian2.core.functions import Function
 from brian2.core.preferences import prefs
 from brian2.core.variables import ArrayVariable, Constant, DynamicArrayVariable
+from brian2.groups.group import CodeRunner
 from brian2.devices.cpp_standalone.codeobject import CPPStandaloneCodeObject
 from brian2.devices.cpp_standalone.device import CPPStandaloneDevice
 from brian2.devices.device import all_devices
@@ -254,9 +257,18 @@ class B200Device(CPPStandaloneDevice):
         net.before_run(namespace)
         self.synapses |= {s for s in net.objects if isinstance(s, Synapses)}
         self.clocks.update(net._clocks)
-        if len(net._clocks) != 1:
-            raise NotImplementedError("b200: all objects of a network must share one clock")
-        clock = next(iter(net._clocks))
+        # one clock for the step loop; operations (run_regularly) may run on a
+        # clock whose dt is a whole multiple of it
+        main = {obj.clock for obj in all_objects if type(obj) is not CodeRunner}
+        if len(main) != 1:
+            raise NotImplementedError("b200: all objects of a network must share one clock "
+                                      "(run_regularly operations may use a multiple of its dt)")
+        clock = next(iter(main))
+        for obj in all_objects:
+            if type(obj) is CodeRunner and obj.clock is not clock:
+                k = float(obj.clock.dt_) / float(clock.dt_)
+                if round(k) < 1 or abs(k - round(k)) > 1e-9 * k:
+                    raise NotImplementedError(f"b200: {obj.name} runs every {k} steps (not a whole number)")
         n_steps = int(clock._i_end - clock.variables["timestep"].get_value().item()) \
             if False else int(round(float(duration) / float(clock.dt_)))
         spec, objects = self._make_spec(net, all_objects, clock)
@@ -355,6 +367,8 @@ class B200Device(CPPStandaloneDevice):
         pathways, spkmons, ratemons, statemons = [], [], [], []
         summed_frags = []
         input_frags = []  # PoissonInputs, in schedule order
+        op_frags = []  # operations (run_regularly), in schedule order
+        statemon_pos = []  # positions of the state monitors in the schedule
         draw_sites = []  # (position in the schedule, site, the block or input whose code draws)
         b200_objects = []
         for pos, obj in enumerate(objects):
@@ -368,6 +382,8 @@ class B200Device(CPPStandaloneDevice):
                 b200_objects.append((obj, co))
                 if isinstance(obj, PoissonInput):
                     input_frags.append((obj, frag, pos))
+                elif type(obj) is CodeRunner and t == "stateupdate":
+                    op_frags.append((obj, frag, pos))
                 elif t in ("stateupdate", "threshold", "reset"):
                     gi, _ = group_of(obj.group)
                     g = groups[gi]
@@ -440,6 +456,7 @@ class B200Device(CPPStandaloneDevice):
                     gi, rng = group_of(obj.source)
                     ratemons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng))
                 elif t == "statemonitor":
+                    statemon_pos.append(pos)
                     if obj.when != "start":
                         raise NotImplementedError("b200: state monitors record at the start of the step")
                     gi, rng = group_of(obj.source)
@@ -562,6 +579,36 @@ class B200Device(CPPStandaloneDevice):
             draw_sites.append((pos, site, inputs[-1]))
         if len(inputs) > 4:
             raise NotImplementedError("b200: more than 4 PoissonInputs")
+        # operations (Group.run_regularly, brian2/groups/group.py CodeRunner with
+        # the stateupdate template): in the start slot before the state monitors,
+        # or in the end slot after the resets; every k-th step of the network
+        # clock (their code reads the group's clock: t and dt of the step)
+        for obj, frag, pos in op_frags:
+            if obj.when not in ("start", "end"):
+                raise NotImplementedError(f"b200: run_regularly in the '{obj.when}' slot (start and end only)")
+            if obj.when == "start" and any(p_ < pos for p_ in statemon_pos):
+                raise NotImplementedError("b200: run_regularly after a state monitor in the start slot")
+            gi, (lo, hi) = group_of(obj.group)
+            g = groups[gi]
+            b = block(frag)
+            if "_rand(" in b["vector"] or "_randn(" in b["vector"] or b.get("vector_device"):
+                raise NotImplementedError("b200: random numbers in run_regularly code")
+            vec = b["vector"]
+            whole = not isinstance(obj.group, Subgroup)
+            if not whole:
+                sub = gen_name(obj.group.variables["_sub_idx"])
+                vec = re.sub(re.escape(sub) + r"\s*\[\s*_idx\s*\]", "_b200_abs_idx", vec)
+            names = {v["ptr"] for v in g["vars"]}
+            for ptr in set(re.findall(r"_ptr_array_\w+", vec + b["scalar"])):
+                if ptr not in names and ptr not in clock_ptrs.values():
+                    raise NotImplementedError(f"b200: run_regularly code reads {ptr} (not a state variable of "
+                                              "its group)")
+            if collect(frag, {g["name"]}):
+                raise NotImplementedError("b200: run_regularly code reads another group's variables")
+            every = int(round(float(obj.clock.dt_) / float(clock.dt_)))
+            g.setdefault("ops", []).append(dict(name=obj.name, when=obj.when, every=every, lo=int(lo),
+                                                hi=-1 if whole else int(hi),
+                                                code=dict(scalar=b["scalar"], vector=vec)))
         # draw sites in the order of the schedule (the order of the draws); each
         # call of the site's code becomes _b200_draw_<site>_<call>(index)
         draws = []

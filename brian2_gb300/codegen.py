@@ -245,6 +245,7 @@ def render_model(spec: dict) -> str:
         for blk in ("update", "threshold", "reset"):
             if g.get(blk):
                 g[blk] = dict(g[blk], vector=_device(g[blk].get("vector")))
+        g["ops"] = [dict(op, code=dict(op["code"], vector=_device(op["code"]["vector"]))) for op in g.get("ops", [])]
     paths = [dict(p, on_pre=dict(p["on_pre"], vector=_device(p["on_pre"].get("vector")),
                                  vector_device=_device(p["on_pre"].get("vector_device"))))
              for p in paths]
@@ -269,6 +270,7 @@ def render_model(spec: dict) -> str:
         blocks = [("update", _block(g.get("update"))), ("threshold", _block(g.get("threshold"))),
                   ("reset", _block(g.get("reset")))]
         blocks += [(f"input{k}", _block(inp["code"])) for k, inp in enumerate(INPUTS) if inp["group"] == gi]
+        blocks += [(f"op{j}", _block(op["code"])) for j, op in enumerate(g["ops"])]
         gtables.append((_Tables(consts, blocks, (clock["t"], clock["timestep"])), blocks))
     SUMMED = spec.get("summed", [])
     # code objects drawing from the reference's generator, in the order of the draws
@@ -305,6 +307,8 @@ def render_model(spec: dict) -> str:
         for inp in INPUTS:
             if inp["group"] == gi:
                 text += inp["code"]["vector"] + "\n"
+        for op in g.get("ops", []):
+            text += op["code"]["vector"] + "\n"
         for p in paths:
             text += (p["on_pre"].get("vector_device") or p["on_pre"].get("vector", "")) + json.dumps(p.get("group_ptrs", {}))
         for sm in SUMMED:
@@ -546,13 +550,46 @@ def render_model(spec: dict) -> str:
         L += ["}"]
         return _indent("\n".join(L), indent)
 
+    def op_block(gi, indent, tsexpr, when):
+        """The operations (run_regularly) of group gi in slot `when` of step
+        `tsexpr`, over this CTA's neurons, each on the steps of its clock."""
+        ops = [(j, op) for j, op in enumerate(groups[gi].get("ops", [])) if op["when"] == when]
+        if not ops:
+            return ""
+        tab, _ = gtables[gi]
+        L = ["{",
+             f"  const double _b200_t = (double)({tsexpr}) * _b200_dt; (void)_b200_t;  // the step of the operations",
+             f"  const int64_t _b200_ts = {tsexpr}; (void)_b200_ts;",
+             f"  const int32_t N = I.g[{gi}].N; (void)N;",
+             f"  const double* const _b200_S = s_Sg{gi}; const float* const _b200_Sf = s_Sg{gi}f; const long long* const _b200_Si = s_Sg{gi}i;",
+             gptr_decls(gi, 2, False),
+             f"  const int _own0 = s_tst[{gi} * max_tiles1 + s_ut[{gi}][0]], _own1 = s_tst[{gi} * max_tiles1 + s_ut[{gi}][1]];"]
+        for q, (j, op) in enumerate(ops):
+            hi = str(op["hi"]) if op["hi"] >= 0 else "N"
+            if q:
+                L.append("  __syncthreads();  // (operations on one variable run in schedule order)")
+            L += [f"  if (_b200_ts % {op['every']} == 0) {{  // operation '{op['name']}'",
+                  f"    const int _lo = {op['lo']}, _hi = {hi};",
+                  _indent(tab.device_loads(f"op{j}", f32), 4),
+                  _indent(_device(tab.time_code(f"op{j}")), 4),
+                  "    const int _a = _own0 > _lo ? _own0 : _lo, _b = _own1 < _hi ? _own1 : _hi;",
+                  "    for (int _b200_abs_idx = _a + (int)threadIdx.x; _b200_abs_idx < _b; _b200_abs_idx += (int)blockDim.x) {",
+                  "      const int32_t _idx = _b200_abs_idx - _lo;",
+                  "      const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;",
+                  "      {",
+                  _indent(op["code"]["vector"], 8),
+                  "      }",
+                  "    }",
+                  "  }"]
+        L.append("}")
+        return _indent("\n".join(L), indent)
+
     def deferred_block(gi, indent, tsexpr, owner=False):
         """What the reference runs after the deliveries of step `tsexpr`: the
-        Poisson inputs, then the reset (this CTA's neurons)."""
-        a, b = input_block(gi, indent, tsexpr), reset_block(gi, indent, tsexpr, owner)
-        if a and b:
-            return a + "\n" + " " * indent + "__syncthreads();\n" + b
-        return a or b
+        Poisson inputs, the reset, the end-slot operations (this CTA's neurons)."""
+        parts = [x for x in (input_block(gi, indent, tsexpr), reset_block(gi, indent, tsexpr, owner),
+                             op_block(gi, indent, tsexpr, "end")) if x]
+        return ("\n" + " " * indent + "__syncthreads();\n").join(parts)
 
     def emit_generator(gi, owner):
         """A spike generator group's step (templates/spikegenerator.cpp:5-31):
@@ -859,6 +896,10 @@ def render_model(spec: dict) -> str:
                 w(dfr)
                 w("        __syncthreads();")
                 w("      }")
+            sop = op_block(gi, 6, "ts", "start")
+            if sop and not SUMMED:  # the start-slot operations of this step
+                w(sop)
+                w("      __syncthreads();")
             w("      {")
             w(f"        const int32_t N = I.g[{gi}].N; (void)N;")
             w(f"        const double* const _b200_S = s_Sg{gi}; const float* const _b200_Sf = s_Sg{gi}f; const long long* const _b200_Si = s_Sg{gi}i;")
@@ -1214,6 +1255,10 @@ def render_model(spec: dict) -> str:
                 w("      if (ts > ts0) {")
                 w(dfr)
                 w("      }")
+            sop = op_block(gi, 6, "ts", "start")
+            if sop:
+                w("      __syncthreads();")
+                w(sop)
         w("      if (!b200_inst_barrier(I, gen, limit_ns, cluster, rank)) { ok = false; break; }")
         for gi in range(NG):
             emit_statemons(gi)

@@ -473,6 +473,33 @@ def noise_inputs(N=300, duration_ms=200.0, seed_value=303):
     return dict(P=P, spikes=s_mon, rate=r_mon, state=st, other_spikes=q_mon)
 
 
+def regular_ops(N=200, duration_ms=200.0, seed_value=404):
+    """Operations (run_regularly): a drive current rewritten every 10 steps
+    from t and the neuron index (start slot, before the state monitor), a kick
+    to a subgroup every 20 steps, and a decay of ge in the end slot of every
+    step (after the reset); recurrent synapses with delays."""
+    from brian2 import (NeuronGroup, Synapses, SpikeMonitor, PopulationRateMonitor, StateMonitor, ms, mV, seed,
+                        run)
+    seed(seed_value)
+    ns = dict(taum=20 * ms, taue=5 * ms, Vt=-50 * mV, Vr=-60 * mV, El=-60 * mV, we=0.6 * mV, I0=8 * mV)
+    P = NeuronGroup(N, '''dv/dt = (I + ge - (v - El))/taum : volt
+                          dge/dt = -ge/taue : volt
+                          I : volt''',
+                    threshold='v>Vt', reset='v = Vr', method='exact', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    P.run_regularly('I = I0 * (1 + (t/ms % 20)/20) * (1 + 0.002*i)', dt=1 * ms)
+    P[50:150].run_regularly('v = v + 0.5*mV', dt=2 * ms)
+    P.run_regularly('ge = ge * 0.9', when='end')
+    S = Synapses(P, P, on_pre='ge += we', namespace=ns)
+    S.connect(p=0.05)
+    S.delay = 'rand() * 2*ms'
+    s_mon = SpikeMonitor(P)
+    r_mon = PopulationRateMonitor(P)
+    st = StateMonitor(P, 'v', record=[0, 60, 199])
+    run(duration_ms * ms)
+    return dict(P=P, spikes=s_mon, rate=r_mon, state=st)
+
+
 SCENARIOS = {
     "lif_refractory": lif_refractory,
     "hetero_delays": hetero_delays,
@@ -486,4 +513,5 @@ SCENARIOS = {
     "poisson_input": poisson_input,
     "poisson_drive": poisson_drive,
     "noise_inputs": noise_inputs,
+    "regular_ops": regular_ops,
 }

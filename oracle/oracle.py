@@ -34,7 +34,9 @@ code objects, and executes the spec's *plain* C++ snippets (Brian's own
   synapse in creation order added to its target (templates/summed_variable.cpp:
   11-25), after the state monitors and before the state updates;
 * rate monitor count per step (templates/ratemonitor.cpp:7-35);
-* state monitor record at the start of the step (templates/statemonitor.cpp).
+* state monitor record at the start of the step (templates/statemonitor.cpp);
+* operations (Group.run_regularly): the start slot's before the state
+  monitors, the end slot's after the resets, on the steps of their clock.
 
 Scalar blocks are evaluated every step, as the reference does.  The library is
 built with ``g++ -O2 -ffp-contract=off -fno-fast-math`` (the reference's strict
@@ -278,7 +280,28 @@ def render_oracle(spec: dict) -> str:
             lines.append(f"{v['ctype']}* const {ptr} = n->g{obj}_{v['name']}.data(); (void){ptr};")
         return _ind("\n".join(lines), indent)
 
-    # state monitors record at the start of the step
+    def emit_ops(when):
+        """Operations (run_regularly) of the slot, on the steps of their clock."""
+        for gi, g in enumerate(groups):
+            for op in g.get("ops", []):
+                if op["when"] != when:
+                    continue
+                w(f"    if (n->ts % {op['every']} == 0) {{  // operation '{op['name']}'")
+                w(gptrs(gi, 6))
+                w(f"      const int32_t N = n->N{gi}; (void)N;")
+                w("      {")
+                w(_ind(op["code"]["scalar"], 8))
+                w(f"        const int32_t _lo = {op['lo']}, _hi = {op['hi'] if op['hi'] >= 0 else 'N'};")
+                w("        for (int32_t _b200_abs_idx = _lo; _b200_abs_idx < _hi; ++_b200_abs_idx) {")
+                w("          const int32_t _idx = _b200_abs_idx - _lo;")
+                w("          const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+                w(_ind(op["code"]["vector"], 10))
+                w("        }")
+                w("      }")
+                w("    }")
+
+    # operations of the start slot, then the state monitors (start of the step)
+    emit_ops("start")
     for mi, m in enumerate(statemons):
         gi = m["group"]
         w("    {")
@@ -456,6 +479,7 @@ def render_oracle(spec: dict) -> str:
     for mi, m in enumerate(ratemons):
         gi = m["group"]
         w(f"    {{ int c = 0; for (int32_t idx : n->spk{gi}) if (idx >= n->rm{mi}_lo && idx < n->rm{mi}_hi) ++c; n->rm{mi}_cnt.push_back(c); }}")
+    emit_ops("end")  # (the rate monitors count spikes, which the operations do not change)
     w("    n->ts += 1;")
     w("  }")
     w("}")

@@ -35,7 +35,7 @@ def test_job_carries_the_reference_network(case, golden):
 
 SCENARIOS = ["lif_refractory", "hetero_delays", "subgroup_monitors", "input_group", "presynaptic_read",
              "spike_generator", "stdp", "gap_junctions", "explicit_methods", "poisson_input", "poisson_drive",
-             "noise_inputs"]
+             "noise_inputs", "regular_ops"]
 
 
 @pytest.mark.parametrize("name", SCENARIOS)
@@ -72,6 +72,11 @@ def test_scenario_jobs_describe_their_features(name):
         assert [(d["kind"], d["calls"]) for d in spec["draws"]] == [("randn", 1), ("randn", 2), ("binormal", 1),
                                                                     ("binomial", 1)]
         assert int(init["rng_gauss"][0]) == 1  # the initial values left one kept
+    if name == "regular_ops":  # run_regularly: slots, clock multiples, a subgroup range
+        ops = spec["groups"][0]["ops"]
+        assert [(o["when"], o["every"], o["lo"], o["hi"]) for o in ops] == [("start", 10, 0, -1), ("start", 20, 50, 150),
+                                                                            ("end", 1, 0, -1)]
+        assert "_sub_idx = _b200_abs_idx;" in ops[1]["code"]["vector"] and "__sub_idx[" not in ops[1]["code"]["vector"]
     if name == "gap_junctions":  # a summed variable over a Synapses object without on_pre
         (sm,) = spec["summed"]
         pw = spec["pathways"][sm["pathway"]]
