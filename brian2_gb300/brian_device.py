@@ -259,13 +259,14 @@ class B200Device(CPPStandaloneDevice):
         self.clocks.update(net._clocks)
         # one clock for the step loop; operations (run_regularly) may run on a
         # clock whose dt is a whole multiple of it
-        main = {obj.clock for obj in all_objects if type(obj) is not CodeRunner}
+        slower = lambda obj: type(obj) is CodeRunner or isinstance(obj, StateMonitor)
+        main = {obj.clock for obj in all_objects if not slower(obj)}
         if len(main) != 1:
             raise NotImplementedError("b200: all objects of a network must share one clock "
-                                      "(run_regularly operations may use a multiple of its dt)")
+                                      "(run_regularly operations and state monitors may use a multiple of its dt)")
         clock = next(iter(main))
         for obj in all_objects:
-            if type(obj) is CodeRunner and obj.clock is not clock:
+            if slower(obj) and obj.clock is not clock:
                 k = float(obj.clock.dt_) / float(clock.dt_)
                 if round(k) < 1 or abs(k - round(k)) > 1e-9 * k:
                     raise NotImplementedError(f"b200: {obj.name} runs every {k} steps (not a whole number)")
@@ -465,6 +466,7 @@ class B200Device(CPPStandaloneDevice):
                         if v not in names:
                             raise NotImplementedError(f"b200: recording '{v}' (not a state variable)")
                     statemons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng,
+                                          every=int(round(float(obj.clock.dt_) / float(clock.dt_))),
                                           _vars=list(obj.record_variables)))
                 elif t == "summed_variable":
                     summed_frags.append((obj, frag))
@@ -711,6 +713,9 @@ class B200Device(CPPStandaloneDevice):
     def _store(self, var, values):
         fname = os.path.join(self.results_dir, self.get_array_filename(var))
         np.ascontiguousarray(values, dtype=var.dtype).tofile(fname)
+        # the results file is now the value (get_value answers from the cache
+        # first, e.g. the zeros a monitor's counts were created with)
+        self.array_cache.pop(var, None)
 
     def b200_export_job(self, directory):
         """Writes the recorded runs as a job directory (:mod:`brian2_gb300.job`):
@@ -818,7 +823,9 @@ class B200Device(CPPStandaloneDevice):
         for mi, m in enumerate(spec0["state_monitors"]):
             tr = out[f"stm{mi}_trace"]
             mon = m["_obj"]
-            self._store(mon.variables["t"], (ts0 + np.arange(tr.shape[0])).astype(np.float64) * dt)
+            ev = int(m.get("every", 1))  # the monitor's clock: t = its time step * its dt
+            first = -(-ts0 // ev)
+            self._store(mon.variables["t"], (first + np.arange(tr.shape[0])).astype(np.float64) * float(mon.clock.dt_))
             for k, v in enumerate(m["_vars"]):
                 self._store(mon.variables[v], tr[:, k, :])
                 mon.variables[v].size = tr[:, k, :].shape

@@ -429,7 +429,7 @@ def render_model(spec: dict) -> str:
         w("static const b200_pathway_info* const b200_pathways = nullptr;")
     for nm, mons in (("spkmon", spkmons), ("ratemon", ratemons), ("statemon", statemons)):
         if mons:
-            w(f"static const b200_mon_info b200_{nm}[] = {{" + ", ".join(f'{{"{m["name"]}", {m["group"]}}}' for m in mons) + "};")
+            w(f"static const b200_mon_info b200_{nm}[] = {{" + ", ".join(f'{{"{m["name"]}", {m["group"]}, {m.get("every", 1)}}}' for m in mons) + "};")
         else:
             w(f"static const b200_mon_info* const b200_{nm} = nullptr;")
     w("")
@@ -814,10 +814,17 @@ def render_model(spec: dict) -> str:
         for mi, m in enumerate(statemons):
             if m["group"] != gi:
                 continue
-            w(f"        {{  // state monitor {mi}: values at the start of the step")
-            w(f"          const b200_statemon_d& SM = I.stm[{mi}];")
+            every = int(m.get("every", 1))
+            if every == 1:
+                w(f"        {{  // state monitor {mi}: values at the start of the step")
+                w(f"          const b200_statemon_d& SM = I.stm[{mi}];")
+                w("          const int64_t rec = ts - SM.step0;  // row of this step")
+            else:  # a slower clock: the steps that are multiples of its dt
+                w(f"        if (ts % {every} == 0) {{  // state monitor {mi}: values at the start of every {every}th step")
+                w(f"          const b200_statemon_d& SM = I.stm[{mi}];")
+                w(f"          const int64_t rec = ts / {every} - (SM.step0 + {every - 1}) / {every};  // row of this step")
             w(f"          const int lo = s_tst[{gi} * max_tiles1 + s_ut[{gi}][0]], hi = s_tst[{gi} * max_tiles1 + s_ut[{gi}][1]];")
-            w("          double* const row = SM.data + (size_t)(ts - SM.step0) * SM.n_vars * SM.n_rec;")
+            w("          double* const row = SM.data + (size_t)rec * SM.n_vars * SM.n_rec;")
             w("          for (int k = threadIdx.x; k < SM.n_rec * SM.n_vars; k += blockDim.x) {")
             w("            const int r = k % SM.n_rec, v = k / SM.n_rec;")
             w("            const int idx = SM.idx[r];")
@@ -830,7 +837,7 @@ def render_model(spec: dict) -> str:
             w("              row[k] = val;")
             w("            }")
             w("          }")
-            w(f"          if (threadIdx.x == 0) s_stm_n[{mi}] = ts + 1 - SM.step0;")
+            w(f"          if (threadIdx.x == 0) s_stm_n[{mi}] = rec + 1;")
             w("        }")
         if any(m["group"] == gi for m in statemons):
             # (the update that follows overwrites what other threads recorded here)

@@ -118,9 +118,9 @@ struct b200_statemon_d {
   const int32_t* idx;     // [n_rec] recorded neuron indices
   int32_t var_id[8];      // which state variables
   int32_t var_dbl[8];     // 1 if the variable is double, 0 if float
-  int64_t step0, cap;     // steps available
-  int64_t* n;             // [1] number of recorded steps
-  double* data;           // [cap][n_vars][n_rec] values (as double)
+  int64_t step0, cap;     // recording starts at step0; rows available
+  int64_t* n;             // [1] number of recorded rows
+  double* data;           // [cap][n_vars][n_rec] values (as double), one row per recorded step
 };
 
 // A summed variable (SummedVariableUpdater, brian2/synapses/synapses.py:116-175;
@@ -234,6 +234,7 @@ struct b200_summed_info {
 struct b200_mon_info {
   const char* name;
   int group;
+  int every;  // records on every k-th step (a state monitor on a slower clock); 1 otherwise
 };
 struct b200_model_info {
   const char* name;

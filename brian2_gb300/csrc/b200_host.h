@@ -1241,7 +1241,10 @@ int b200_run(b200_net* n, int64_t n_steps) {
     }
     for (int s = 0; s < M->n_statemon; ++s) {
       b200_statemon_h& S = I.stm[s];
-      const int64_t need = I.ts + n_steps - S.step0;
+      // rows through the last step of this run: one per step whose index is a
+      // multiple of the monitor's period, from step0 on
+      const int64_t ev = std::max(M->statemon[s].every, 1);
+      const int64_t need = std::max<int64_t>((I.ts + n_steps - 1) / ev - (S.step0 + ev - 1) / ev + 1, 0);
       const size_t row = (size_t)std::max(S.n_rec * S.n_vars, 1) * 8;
       if (S.cap < need) {
         b200_dbuf nb;

@@ -477,7 +477,8 @@ def regular_ops(N=200, duration_ms=200.0, seed_value=404):
     """Operations (run_regularly): a drive current rewritten every 10 steps
     from t and the neuron index (start slot, before the state monitor), a kick
     to a subgroup every 20 steps, and a decay of ge in the end slot of every
-    step (after the reset); recurrent synapses with delays."""
+    step (after the reset); recurrent synapses with delays; a state monitor on
+    a clock of 5 steps."""
     from brian2 import (NeuronGroup, Synapses, SpikeMonitor, PopulationRateMonitor, StateMonitor, ms, mV, seed,
                         run)
     seed(seed_value)
@@ -495,7 +496,7 @@ def regular_ops(N=200, duration_ms=200.0, seed_value=404):
     S.delay = 'rand() * 2*ms'
     s_mon = SpikeMonitor(P)
     r_mon = PopulationRateMonitor(P)
-    st = StateMonitor(P, 'v', record=[0, 60, 199])
+    st = StateMonitor(P, 'v', record=[0, 60, 199], dt=0.5 * ms)
     run(duration_ms * ms)
     return dict(P=P, spikes=s_mon, rate=r_mon, state=st)
 

@@ -304,7 +304,7 @@ def render_oracle(spec: dict) -> str:
     emit_ops("start")
     for mi, m in enumerate(statemons):
         gi = m["group"]
-        w("    {")
+        w(f"    if (n->ts % {int(m.get('every', 1))} == 0) {{  // (a monitor on a slower clock: its steps)")
         w(gptrs(gi, 6))
         w(f"      for (size_t v = 0; v < n->st{mi}_vars.size(); ++v) for (size_t r = 0; r < n->st{mi}_idx.size(); ++r) {{")
         w("        double val = 0;")

@@ -115,6 +115,10 @@ if __name__ == "__main__":
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import brian_configs as bc
     os.makedirs(os.path.join(HERE, "scenarios"), exist_ok=True)
+    # Brian orders the noise terms of a stochastic equation by iterating a set of
+    # names, so the order of randn() calls in its generated code follows Python's
+    # string hashing: both runs of a script use the same hash seed
+    env = dict(os.environ, PYTHONHASHSEED="0")
     for n in sys.argv[1:] or list(bc.SCENARIOS):
         for phase in ("--ref", "--job"):
-            subprocess.run([sys.executable, os.path.abspath(__file__), phase, n], check=True)
+            subprocess.run([sys.executable, os.path.abspath(__file__), phase, n], check=True, env=env)
