@@ -29,11 +29,12 @@ code between two ``run()`` calls; random numbers inside the step loop other
 than one ``rand()`` per neuron in threshold code (PoissonGroup) and the
 binomial draws of ``PoissonInput`` without its normal approximation (both need
 ``openmp_threads = 0``); synaptic statements that write a neuron variable
-other than by ``+=``/``-=``; state monitors outside the ``start`` slot; custom
-events.
+other than by ``+=``/``-=``; state monitors outside the ``start`` and ``end``
+slots; custom events.
 """
 from __future__ import annotations
 
+import json
 import os
 import re
 import time
@@ -42,7 +43,7 @@ import numpy as np
 
 from brian2.codegen.generators.cpp_generator import CPPCodeGenerator, c_data_type
 from brian2.core.clocks import Clock
-from brian2.core.functions import Function
+from brian2.core.functions import DEFAULT_FUNCTIONS, Function
 from brian2.core.preferences import prefs
 from brian2.core.variables import ArrayVariable, Constant, DynamicArrayVariable
 from brian2.groups.group import CodeRunner
@@ -168,7 +169,10 @@ class B200CodeObject(CPPStandaloneCodeObject):
         pass
 
     def run_block(self, block):
-        pass  # executed inside the device step kernel
+        # executed inside the device step kernel; run on its own (outside a
+        # network run, e.g. StateMonitor.record_single_timestep) it has no place
+        if block == "run":
+            raise NotImplementedError(f"b200: running the code object {self.name} outside run() is not supported")
 
 
 class B200Device(CPPStandaloneDevice):
@@ -209,6 +213,11 @@ class B200Device(CPPStandaloneDevice):
         name = find_name(name)
         meta = getattr(CPPStandaloneCodeObject.templater, template_name)
         for vname, var in variables.items():
+            if (isinstance(var, Function) and not isinstance(var, BinomialFunction)
+                    and vname not in DEFAULT_FUNCTIONS and vname in str(abstract_code)):
+                # (a TimedArray, a user function: no device implementation)
+                raise NotImplementedError(f"b200: function '{vname}' in the step loop (Brian's default "
+                                          "functions only)")
             if isinstance(var, BinomialFunction):
                 # a PoissonInput's binomial draws (a state update of its target group):
                 # the device continues the reference's stream
@@ -259,6 +268,8 @@ class B200Device(CPPStandaloneDevice):
         self.clocks.update(net._clocks)
         # one clock for the step loop; operations (run_regularly) may run on a
         # clock whose dt is a whole multiple of it
+        if any(not hasattr(obj.clock, "dt_") for obj in all_objects):
+            raise NotImplementedError("b200: event clocks are not supported")
         slower = lambda obj: type(obj) is CodeRunner or isinstance(obj, StateMonitor)
         main = {obj.clock for obj in all_objects if not slower(obj)}
         if len(main) != 1:
@@ -457,15 +468,15 @@ class B200Device(CPPStandaloneDevice):
                     gi, rng = group_of(obj.source)
                     ratemons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng))
                 elif t == "statemonitor":
-                    statemon_pos.append(pos)
-                    if obj.when != "start":
-                        raise NotImplementedError("b200: state monitors record at the start of the step")
+                    statemon_pos.append((pos, obj.when))
+                    if obj.when not in ("start", "end"):
+                        raise NotImplementedError("b200: state monitors record in the start or end slot")
                     gi, rng = group_of(obj.source)
                     names = [v["name"] for v in groups[gi]["vars"]]
                     for v in obj.record_variables:
                         if v not in names:
                             raise NotImplementedError(f"b200: recording '{v}' (not a state variable)")
-                    statemons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng,
+                    statemons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng, when=obj.when,
                                           every=int(round(float(obj.clock.dt_) / float(clock.dt_))),
                                           _vars=list(obj.record_variables)))
                 elif t == "summed_variable":
@@ -588,8 +599,8 @@ class B200Device(CPPStandaloneDevice):
         for obj, frag, pos in op_frags:
             if obj.when not in ("start", "end"):
                 raise NotImplementedError(f"b200: run_regularly in the '{obj.when}' slot (start and end only)")
-            if obj.when == "start" and any(p_ < pos for p_ in statemon_pos):
-                raise NotImplementedError("b200: run_regularly after a state monitor in the start slot")
+            if any(p_ < pos and w_ == obj.when for p_, w_ in statemon_pos):
+                raise NotImplementedError(f"b200: run_regularly after a state monitor in the {obj.when} slot")
             gi, (lo, hi) = group_of(obj.group)
             g = groups[gi]
             b = block(frag)
@@ -663,6 +674,20 @@ class B200Device(CPPStandaloneDevice):
             spec["summed"] = summed
         if draws:
             spec["draws"] = draws
+        # every array the code of the step loop names must be one the device
+        # holds (a shared variable, e.g. `s : 1 (shared)`, is not carried)
+        known = set(clock_ptrs.values())
+        for g in groups:
+            known |= {v["ptr"] for v in g["vars"]}
+        for p in pathways:
+            known |= {v["ptr"] for v in p["vars"]} | {p["pre_ptr"], p["post_ptr"]}
+        texts = [json.dumps({k: v for k, v in g.items() if k != "_obj"}) for g in groups]
+        texts += [json.dumps(p["on_pre"]) for p in pathways] + [json.dumps(sm["code"]) for sm in summed]
+        texts += [json.dumps(inp["code"]) for inp in inputs]
+        for ptr in set(re.findall(r"_ptr_array_\w+", "\n".join(texts))):
+            if ptr not in known:
+                raise NotImplementedError(f"b200: the step loop reads {ptr}, which the device does not hold "
+                                          "(a shared or another object's variable)")
         if inputs:
             spec["inputs"] = inputs
         return spec, b200_objects

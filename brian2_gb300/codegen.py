@@ -586,9 +586,10 @@ def render_model(spec: dict) -> str:
 
     def deferred_block(gi, indent, tsexpr, owner=False):
         """What the reference runs after the deliveries of step `tsexpr`: the
-        Poisson inputs, the reset, the end-slot operations (this CTA's neurons)."""
+        Poisson inputs, the reset, the end-slot operations and state monitors
+        (this CTA's neurons)."""
         parts = [x for x in (input_block(gi, indent, tsexpr), reset_block(gi, indent, tsexpr, owner),
-                             op_block(gi, indent, tsexpr, "end")) if x]
+                             op_block(gi, indent, tsexpr, "end"), statemon_text(gi, indent, tsexpr, "end")) if x]
         return ("\n" + " " * indent + "__syncthreads();\n").join(parts)
 
     def emit_generator(gi, owner):
@@ -807,41 +808,53 @@ def render_model(spec: dict) -> str:
         w("        } else {")
         return True
 
-    def emit_statemons(gi):
-        """State monitors of group gi: this CTA's recorded neurons, values at
-        the start of the step (templates/statemonitor.cpp)."""
+    def statemon_text(gi, indent, tsexpr, when):
+        """State monitors of group gi in slot `when` (start: values at the start
+        of step `tsexpr`; end: after its resets), this CTA's recorded neurons
+        (templates/statemonitor.cpp).  Ends with a barrier of the CTA: the code
+        that follows overwrites what other threads record."""
         g = groups[gi]
-        for mi, m in enumerate(statemons):
-            if m["group"] != gi:
-                continue
+        mons = [(mi, m) for mi, m in enumerate(statemons) if m["group"] == gi and m.get("when", "start") == when]
+        if not mons:
+            return ""
+        L = []
+        for mi, m in mons:
             every = int(m.get("every", 1))
+            L.append("{")
+            L.append(f"  const int64_t _b200_sts = {tsexpr};  // the step recorded")
             if every == 1:
-                w(f"        {{  // state monitor {mi}: values at the start of the step")
-                w(f"          const b200_statemon_d& SM = I.stm[{mi}];")
-                w("          const int64_t rec = ts - SM.step0;  // row of this step")
+                L.append(f"  {{  // state monitor {mi}")
+                L.append(f"    const b200_statemon_d& SM = I.stm[{mi}];")
+                L.append("    const int64_t rec = _b200_sts - SM.step0;  // row of this step")
             else:  # a slower clock: the steps that are multiples of its dt
-                w(f"        if (ts % {every} == 0) {{  // state monitor {mi}: values at the start of every {every}th step")
-                w(f"          const b200_statemon_d& SM = I.stm[{mi}];")
-                w(f"          const int64_t rec = ts / {every} - (SM.step0 + {every - 1}) / {every};  // row of this step")
-            w(f"          const int lo = s_tst[{gi} * max_tiles1 + s_ut[{gi}][0]], hi = s_tst[{gi} * max_tiles1 + s_ut[{gi}][1]];")
-            w("          double* const row = SM.data + (size_t)rec * SM.n_vars * SM.n_rec;")
-            w("          for (int k = threadIdx.x; k < SM.n_rec * SM.n_vars; k += blockDim.x) {")
-            w("            const int r = k % SM.n_rec, v = k / SM.n_rec;")
-            w("            const int idx = SM.idx[r];")
-            w("            if (idx >= lo && idx < hi) {")
-            w("              double val = 0.0;")
-            w("              switch (SM.var_id[v]) {")
+                L.append(f"  if (_b200_sts % {every} == 0) {{  // state monitor {mi}: every {every}th step")
+                L.append(f"    const b200_statemon_d& SM = I.stm[{mi}];")
+                L.append(f"    const int64_t rec = _b200_sts / {every} - (SM.step0 + {every - 1}) / {every};  // row of this step")
+            L.append(f"    const int lo = s_tst[{gi} * max_tiles1 + s_ut[{gi}][0]], hi = s_tst[{gi} * max_tiles1 + s_ut[{gi}][1]];")
+            L.append("    double* const row = SM.data + (size_t)rec * SM.n_vars * SM.n_rec;")
+            L.append("    for (int k = threadIdx.x; k < SM.n_rec * SM.n_vars; k += blockDim.x) {")
+            L.append("      const int r = k % SM.n_rec, v = k / SM.n_rec;")
+            L.append("      const int idx = SM.idx[r];")
+            L.append("      if (idx >= lo && idx < hi) {")
+            L.append("        double val = 0.0;")
+            L.append("        switch (SM.var_id[v]) {")
             for k, v in enumerate(g["vars"]):
-                w(f"                case {k}: val = (double)(({v['ctype']}*)s_gv[{gi}][{k}])[idx]; break;")
-            w("              }")
-            w("              row[k] = val;")
-            w("            }")
-            w("          }")
-            w(f"          if (threadIdx.x == 0) s_stm_n[{mi}] = rec + 1;")
-            w("        }")
-        if any(m["group"] == gi for m in statemons):
-            # (the update that follows overwrites what other threads recorded here)
-            w("        __syncthreads();")
+                L.append(f"          case {k}: val = (double)(({v['ctype']}*)s_gv[{gi}][{k}])[idx]; break;")
+            L.append("        }")
+            L.append("        row[k] = val;")
+            L.append("      }")
+            L.append("    }")
+            L.append(f"    if (threadIdx.x == 0) s_stm_n[{mi}] = rec + 1;")
+            L.append("  }")
+            L.append("}")
+        L.append("__syncthreads();")
+        return _indent("\n".join(L), indent)
+
+    def emit_statemons(gi):
+        """The start-slot state monitors of group gi at step ts."""
+        txt = statemon_text(gi, 8, "ts", "start")
+        if txt:
+            w(txt)
 
     def emit_summed(si):
         """Summed variable si (templates/summed_variable.cpp:11-25): each of

@@ -501,6 +501,29 @@ def regular_ops(N=200, duration_ms=200.0, seed_value=404):
     return dict(P=P, spikes=s_mon, rate=r_mon, state=st)
 
 
+def end_monitor(N=300, duration_ms=150.0, seed_value=505):
+    """A state monitor in the end slot (after the resets and an end-slot
+    operation): refractory LIF neurons with an adaptation current, recurrent
+    synapses with delays."""
+    from brian2 import (NeuronGroup, Synapses, SpikeMonitor, PopulationRateMonitor, StateMonitor, ms, mV, seed,
+                        run)
+    seed(seed_value)
+    ns = dict(taum=20 * ms, tauw=50 * ms, Vt=-50 * mV, Vr=-60 * mV, El=-49 * mV, we=0.4 * mV, b=1 * mV)
+    P = NeuronGroup(N, '''dv/dt = (El - v - w)/taum : volt (unless refractory)
+                          dw/dt = -w/tauw : volt''',
+                    threshold='v>Vt', reset='v = Vr; w += b', refractory=3 * ms, method='exact', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    P.run_regularly('w = w * 0.999', when='end')
+    S = Synapses(P, P, on_pre='v += we', namespace=ns)
+    S.connect(p=0.05)
+    S.delay = 'rand() * 2*ms'
+    s_mon = SpikeMonitor(P)
+    r_mon = PopulationRateMonitor(P)
+    st = StateMonitor(P, 'v', record=[0, 100, 299], when='end')
+    run(duration_ms * ms)
+    return dict(P=P, spikes=s_mon, rate=r_mon, state=st)
+
+
 SCENARIOS = {
     "lif_refractory": lif_refractory,
     "hetero_delays": hetero_delays,
@@ -515,4 +538,5 @@ SCENARIOS = {
     "poisson_drive": poisson_drive,
     "noise_inputs": noise_inputs,
     "regular_ops": regular_ops,
+    "end_monitor": end_monitor,
 }

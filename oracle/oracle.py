@@ -300,9 +300,13 @@ def render_oracle(spec: dict) -> str:
                 w("      }")
                 w("    }")
 
-    # operations of the start slot, then the state monitors (start of the step)
-    emit_ops("start")
-    for mi, m in enumerate(statemons):
+    def emit_statemons(when):
+        for mi, m in enumerate(statemons):
+            if m.get("when", "start") != when:
+                continue
+            emit_statemon(mi, m)
+
+    def emit_statemon(mi, m):
         gi = m["group"]
         w(f"    if (n->ts % {int(m.get('every', 1))} == 0) {{  // (a monitor on a slower clock: its steps)")
         w(gptrs(gi, 6))
@@ -314,6 +318,10 @@ def render_oracle(spec: dict) -> str:
         w("      }")
         w(f"      n->st{mi}_n++;")
         w("    }")
+
+    # operations of the start slot, then the state monitors (start of the step)
+    emit_ops("start")
+    emit_statemons("start")
     # summed variables (groups slot, before the groups' updates)
     for si, sm in enumerate(spec.get("summed", [])):
         pi, gi = sm["pathway"], sm["tgt_group"]
@@ -480,6 +488,7 @@ def render_oracle(spec: dict) -> str:
         gi = m["group"]
         w(f"    {{ int c = 0; for (int32_t idx : n->spk{gi}) if (idx >= n->rm{mi}_lo && idx < n->rm{mi}_hi) ++c; n->rm{mi}_cnt.push_back(c); }}")
     emit_ops("end")  # (the rate monitors count spikes, which the operations do not change)
+    emit_statemons("end")
     w("    n->ts += 1;")
     w("  }")
     w("}")

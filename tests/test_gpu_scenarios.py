@@ -23,7 +23,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 EXACT = {"lif_refractory": True, "hetero_delays": False, "subgroup_monitors": True, "input_group": True,
          "presynaptic_read": False, "spike_generator": True, "stdp": False,
          "gap_junctions": True, "explicit_methods": True, "poisson_input": False, "poisson_drive": True,
-         "noise_inputs": False, "regular_ops": True}
+         "noise_inputs": False, "regular_ops": True,
+         "end_monitor": True}
 
 
 @pytest.mark.parametrize("name", sorted(EXACT))
