@@ -213,11 +213,6 @@ class B200Device(CPPStandaloneDevice):
         name = find_name(name)
         meta = getattr(CPPStandaloneCodeObject.templater, template_name)
         for vname, var in variables.items():
-            if (isinstance(var, Function) and not isinstance(var, BinomialFunction)
-                    and vname not in DEFAULT_FUNCTIONS and vname in str(abstract_code)):
-                # (a TimedArray, a user function: no device implementation)
-                raise NotImplementedError(f"b200: function '{vname}' in the step loop (Brian's default "
-                                          "functions only)")
             if isinstance(var, BinomialFunction):
                 # a PoissonInput's binomial draws (a state update of its target group):
                 # the device continues the reference's stream
@@ -242,6 +237,20 @@ class B200Device(CPPStandaloneDevice):
                                 allows_scalar_write=meta.allows_scalar_write, name=name,
                                 template_name=template_name)
         scalar_code, vector_code, kwds = gen.translate(abstract_code, dtype=prefs["core.default_float_dtype"])
+        # functions other than Brian's default table (a TimedArray, a user
+        # function) have no device implementation; they may come in through a
+        # subexpression, so look for their calls in the generated code
+        code_text = str(scalar_code) + str(vector_code)
+        for vname, var in variables.items():
+            if not isinstance(var, Function) or isinstance(var, BinomialFunction) or vname in DEFAULT_FUNCTIONS:
+                continue
+            try:
+                impl = var.implementations[CPPCodeGenerator].name or vname
+            except Exception:  # (no C++ implementation registered under this generator)
+                impl = vname
+            if re.search(r"\b(%s|%s)\s*\(" % (re.escape(vname), re.escape(impl)), code_text):
+                raise NotImplementedError(f"b200: function '{vname}' in the step loop (Brian's default "
+                                          "functions only)")
         fragment = dict(template=template_name, scalar=scalar_code, vector=vector_code,
                         vector_device=kwds.get("vector_code_device"), template_kwds=dict(template_kwds or {}),
                         variables=variables, variable_indices=variable_indices, generator=gen)
