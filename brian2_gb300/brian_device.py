@@ -25,7 +25,8 @@ Limits (raise ``NotImplementedError``, which Brian's test runner treats as
 "not supported by this device"): one clock for all step-loop objects (but
 ``run_regularly`` operations in the start and end slots may run every k-th
 step); no host
-code between two ``run()`` calls; random numbers inside the step loop other
+code between two ``run()`` calls other than assignments of values to neuron-group
+state variables (applied between the device runs); random numbers inside the step loop other
 than one ``rand()`` per neuron in threshold code (PoissonGroup) and the
 binomial draws of ``PoissonInput`` without its normal approximation (both need
 ``openmp_threads = 0``); synaptic statements that write a neuron variable
@@ -725,14 +726,12 @@ class B200Device(CPPStandaloneDevice):
                 self.b200_run_options[k] = kwds.pop(k)
         if "b200_defer" in kwds:
             self.b200_run_options["defer"] = bool(kwds.pop("b200_defer"))
-        # host code after the first GPU run cannot be executed before it
+        # host code after the first GPU run cannot run in `main` (before the GPU
+        # runs); assignments of values to state and synaptic variables become
+        # actions of the job, applied after the run they follow
+        self.b200_actions = []
         if self.b200_runs:
-            first = self.b200_runs[0]["queue_len"]
-            for func, args in self.main_queue[first:]:
-                if func == "insert_code" and str(args).startswith("// b200 network run"):
-                    continue
-                raise NotImplementedError("b200: host code between or after run() calls is not supported "
-                                          f"(found '{func}')")
+            self.b200_actions = self._b200_take_actions()
         super().build(directory=directory, results_directory=results_directory, compile=compile, run=run,
                       debug=debug, clean=clean, with_output=with_output,
                       additional_source_files=additional_source_files, run_args=run_args,
@@ -743,6 +742,50 @@ class B200Device(CPPStandaloneDevice):
     def _load(self, var):
         fname = os.path.join(self.results_dir, self.get_array_filename(var))
         return np.fromfile(fname, dtype=var.dtype)
+
+    def _b200_take_actions(self):
+        """Takes the assignments of values to neuron-group state variables
+        queued after the first run out of `main`'s queue (the reference's forms:
+        device.py:440-545) and returns them as job actions: (after run k, kind,
+        object, variable, indices or None, values).  Any other host code there
+        is refused."""
+        spec0 = self.b200_runs[0]["spec"]
+        arrays = {}
+        for gi, g in enumerate(spec0["groups"]):
+            for v in g["vars"]:
+                arrays[v["ptr"][len("_ptr"):]] = ("group", gi, v["name"])
+        # (synaptic variables are not among them: an owner-mode event carries its
+        # synapse's values from the step it was pushed)
+        clock_arrays = {p_[len("_ptr"):] for p_ in spec0["clock_ptrs"].values()}
+        actions, run = [], -1
+        for q in range(self.b200_runs[0]["queue_len"], len(self.main_queue)):
+            func, args = self.main_queue[q]
+            if func == "insert_code" and str(args).startswith("// b200 network run"):
+                run = int(str(args).split()[4])
+                continue
+            if func == "set_by_single_value" and args[0] in clock_arrays:
+                # (Network.run sets the clock where the next run starts: the
+                # device's runs follow each other step by step)
+                self.main_queue[q] = ("insert_code", f"// b200: {args[0]} = {args[2]} (the next run's start)")
+                continue
+            target = arrays.get(args[0]) if func in ("set_by_constant", "set_by_array", "set_by_single_value",
+                                                     "set_array_by_array") else None
+            if target is None:
+                raise NotImplementedError("b200: host code between or after run() calls is not supported "
+                                          f"(found '{func}')")
+            if func == "set_by_constant":
+                index, values = None, np.asarray(args[1])
+            elif func == "set_by_array":
+                index, values = None, np.asarray(self.static_arrays[args[1]])
+            elif func == "set_by_single_value":
+                txt = str(args[2]).strip()
+                val = {"true": 1.0, "false": 0.0}.get(txt.lower(), None)
+                index, values = np.asarray([int(args[1])]), np.asarray([float(txt) if val is None else val])
+            else:
+                index, values = np.asarray(self.static_arrays[args[1]]), np.asarray(self.static_arrays[args[2]])
+            actions.append((run, *target, index, values))
+            self.main_queue[q] = ("insert_code", f"// b200: {func} {args[0]} applied after run {run} on the device")
+        return actions
 
     def _store(self, var, values):
         fname = os.path.join(self.results_dir, self.get_array_filename(var))
@@ -811,7 +854,14 @@ class B200Device(CPPStandaloneDevice):
             init["rng_words"] = np.asarray(st[:624], np.uint32)
             init["rng_position"] = np.int64(st[624])
             init["rng_gauss"] = np.asarray([float(int(tok[625])), float.fromhex(tok[626])], np.float64)
-        write_job(directory, pub, init, [r["n_steps"] for r in self.b200_runs], dt, self.b200_run_options)
+        actions = []
+        for j, (after, kind, obj, var, index, values) in enumerate(getattr(self, "b200_actions", [])):
+            init[f"act{j}_values"] = values
+            if index is not None:
+                init[f"act{j}_index"] = index.astype(np.int64)
+            actions.append(dict(after=int(after), kind=kind, obj=int(obj), var=var, indexed=index is not None))
+        write_job(directory, pub, init, [r["n_steps"] for r in self.b200_runs], dt, self.b200_run_options,
+                  actions=actions)
         self.b200_job_dir = directory
         return directory
 

@@ -31,13 +31,32 @@ import time
 import numpy as np
 
 
-def write_job(directory, spec, init, runs, dt, options=None):
+def write_job(directory, spec, init, runs, dt, options=None, actions=None):
     os.makedirs(directory, exist_ok=True)
     with open(os.path.join(directory, "spec.json"), "w") as f:
         json.dump(spec, f, indent=1, sort_keys=True)
     np.savez_compressed(os.path.join(directory, "init.npz"), **init)
+    job = dict(dt=float(dt), runs=[int(r) for r in runs], options=dict(options or {}))
+    if actions:
+        job["actions"] = list(actions)
     with open(os.path.join(directory, "job.json"), "w") as f:
-        json.dump(dict(dt=float(dt), runs=[int(r) for r in runs], options=dict(options or {})), f, indent=1)
+        json.dump(job, f, indent=1)
+
+
+def apply_actions(job, init, after, download, upload):
+    """The script's assignments after run `after` (job["actions"]: a group's
+    state variable or a pathway's synaptic variable, all of it or at indices):
+    download(kind, obj, var) -> array, upload(kind, obj, var, array)."""
+    for j, a in enumerate(job.get("actions", [])):
+        if a["after"] != after:
+            continue
+        cur = download(a["kind"], a["obj"], a["var"])
+        vals = np.asarray(init[f"act{j}_values"])
+        if a["indexed"]:
+            cur[np.asarray(init[f"act{j}_index"], np.int64)] = vals.astype(cur.dtype)
+        else:
+            cur[...] = np.broadcast_to(vals.astype(cur.dtype), cur.shape)
+        upload(a["kind"], a["obj"], a["var"], cur)
 
 
 def load_job(directory):
@@ -90,9 +109,16 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None)
         net.set_rng(0, init["rng_words"], int(init["rng_position"]), init.get("rng_gauss"))
     net.reset_monitors(0)
     total_ms, t0 = 0.0, time.time()
-    for n in job["runs"]:
+    def download(kind, obj, var):
+        return net.download(0, obj, var) if kind == "group" else net.download_synapse_var(0, obj, var)
+
+    def upload(kind, obj, var, arr):
+        (net.upload if kind == "group" else net.upload_synapse_var)(0, obj, var, arr)
+
+    for k, n in enumerate(job["runs"]):
         net.run(int(n))
         total_ms += net.last_run_ms()
+        apply_actions(job, init, k, download, upload)  # the script's assignments after this run
     out = dict(device_ms=np.float64(total_ms), wall_s=np.float64(time.time() - t0), ts_end=np.int64(net.step(0)),
                ts0=np.int64(ts0), owner=np.int64(net.owner_active()))
     for gi, g in enumerate(spec["groups"]):

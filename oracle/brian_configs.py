@@ -524,6 +524,40 @@ def end_monitor(N=300, duration_ms=150.0, seed_value=505):
     return dict(P=P, spikes=s_mon, rate=r_mon, state=st)
 
 
+def host_sets(N=200, seed_value=606):
+    """Three runs with assignments between them and after the last: a drive
+    current set for the whole group, a slice of membrane potentials, one
+    neuron's current (the reference's set_by_constant, set_array_by_array,
+    set_by_single_value); recurrent synapses with delays (spikes in flight
+    across the runs).  Runs with build_on_run=False and an explicit build."""
+    from brian2 import (NeuronGroup, Synapses, SpikeMonitor, PopulationRateMonitor, StateMonitor, ms, mV, seed,
+                        run)
+    seed(seed_value)
+    ns = dict(taum=20 * ms, taue=5 * ms, Vt=-50 * mV, Vr=-60 * mV, El=-60 * mV, we=0.5 * mV)
+    P = NeuronGroup(N, '''dv/dt = (I + ge - (v - El))/taum : volt
+                          dge/dt = -ge/taue : volt
+                          I : volt''',
+                    threshold='v>Vt', reset='v = Vr', method='exact', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    P.I = 8 * mV
+    S = Synapses(P, P, on_pre='ge += we', namespace=ns)
+    S.connect(p=0.05)
+    S.delay = 'rand() * 2*ms'
+    s_mon = SpikeMonitor(P)
+    r_mon = PopulationRateMonitor(P)
+    st = StateMonitor(P, 'v', record=[0, 5, 150])
+    run(50 * ms)
+    P.I = 12 * mV
+    P.v[:10] = -55 * mV
+    run(50 * ms)
+    P.I[5] = 0 * mV
+    run(50 * ms)
+    P.I = 3 * mV
+    return dict(P=P, spikes=s_mon, rate=r_mon, state=st)
+
+
+host_sets.multiple_runs = True
+
 SCENARIOS = {
     "lif_refractory": lif_refractory,
     "hetero_delays": hetero_delays,
@@ -539,4 +573,5 @@ SCENARIOS = {
     "noise_inputs": noise_inputs,
     "regular_ops": regular_ops,
     "end_monitor": end_monitor,
+    "host_sets": host_sets,
 }

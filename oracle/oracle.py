@@ -748,8 +748,17 @@ def run_job_on_oracle(directory):
     o.set_step(int(init["ts0"]))
     if spec.get("draws"):
         o.set_rng(init["rng_words"], int(init["rng_position"]), init.get("rng_gauss"))
-    for n in job["runs"]:
+    from brian2_gb300.job import apply_actions  # (the job format's own helper)
+
+    def download(kind, obj, var):
+        return o.download(obj, var) if kind == "group" else o.download_synapse_var(obj, var)
+
+    def upload(kind, obj, var, arr):
+        (o.upload if kind == "group" else o.upload_synapse_var)(obj, var, arr)
+
+    for k, n in enumerate(job["runs"]):
         o.run(int(n))
+        apply_actions(job, init, k, download, upload)
     out = {}
     for gi, g in enumerate(spec["groups"]):
         for v in g["vars"]:

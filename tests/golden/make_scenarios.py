@@ -30,10 +30,10 @@ BUILD = os.path.join(ROOT, "oracle", "_ref", "scenario_build")
 STRICT = ['-w', '-O3', '-std=c++17', '-ffp-contract=off', '-fno-fast-math']
 
 
-def setup(device_name, directory, **kw):
+def setup(device_name, directory, build_on_run=True, **kw):
     import numpy as np
     from brian2 import set_device, prefs, defaultclock, ms
-    set_device(device_name, directory=directory, build_on_run=True, **kw)
+    set_device(device_name, directory=directory, build_on_run=build_on_run, **kw)
     prefs.devices.cpp_standalone.openmp_threads = 0
     prefs.codegen.cpp.extra_compile_args_gcc = STRICT
     prefs.core.default_float_dtype = np.float64
@@ -46,8 +46,12 @@ def run_ref(name):
     import brian_configs as bc
     d = os.path.join(BUILD, name + "_ref")
     shutil.rmtree(d, ignore_errors=True)
-    setup("cpp_standalone", d)
+    multi = getattr(bc.SCENARIOS[name], "multiple_runs", False)
+    setup("cpp_standalone", d, build_on_run=not multi)
     r = bc.SCENARIOS[name]()
+    if multi:  # several run() calls: one explicit build
+        from brian2 import device
+        device.build(directory=d)
     P, spk, rate = r["P"], r["spikes"], r["rate"]
     out = {}
     t = np.asarray(spk.t_[:])
@@ -97,8 +101,11 @@ def run_job(name):
     import brian_configs as bc
     d = os.path.join(BUILD, name + "_job")
     shutil.rmtree(d, ignore_errors=True)
-    setup("b200", d, b200_defer=True)
+    multi = getattr(bc.SCENARIOS[name], "multiple_runs", False)
+    setup("b200", d, build_on_run=not multi, b200_defer=True)
     bc.SCENARIOS[name]()
+    if multi:
+        device.build(directory=d, b200_defer=True)
     out = os.path.join(HERE, "jobs", name)
     shutil.rmtree(out, ignore_errors=True)
     shutil.copytree(device.b200_job_dir, out)

@@ -35,7 +35,7 @@ def test_job_carries_the_reference_network(case, golden):
 
 SCENARIOS = ["lif_refractory", "hetero_delays", "subgroup_monitors", "input_group", "presynaptic_read",
              "spike_generator", "stdp", "gap_junctions", "explicit_methods", "poisson_input", "poisson_drive",
-             "noise_inputs", "regular_ops"]
+             "noise_inputs", "regular_ops", "host_sets"]
 
 
 @pytest.mark.parametrize("name", SCENARIOS)
@@ -77,6 +77,12 @@ def test_scenario_jobs_describe_their_features(name):
         assert [(o["when"], o["every"], o["lo"], o["hi"]) for o in ops] == [("start", 10, 0, -1), ("start", 20, 50, 150),
                                                                             ("end", 1, 0, -1)]
         assert "_sub_idx = _b200_abs_idx;" in ops[1]["code"]["vector"] and "__sub_idx[" not in ops[1]["code"]["vector"]
+    if name == "host_sets":  # assignments between and after the runs, in the reference's three forms
+        assert job["runs"] == [500, 500, 500]
+        assert [(a["after"], a["var"], a["indexed"]) for a in job["actions"]] == [
+            (0, "I", False), (0, "v", True), (1, "I", True), (2, "I", False)]
+        np.testing.assert_array_equal(init["act1_index"], np.arange(10))
+        assert init["act2_index"].tolist() == [5] and float(init["act2_values"][0]) == 0.0
     if name == "gap_junctions":  # a summed variable over a Synapses object without on_pre
         (sm,) = spec["summed"]
         pw = spec["pathways"][sm["pathway"]]

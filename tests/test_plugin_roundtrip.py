@@ -26,12 +26,15 @@ import brian2_gb300.brian_device  # noqa: F401  (registers the device)
 from brian2 import set_device, prefs, defaultclock, device, ms
 import brian_configs as bc
 from oracle import run_job_on_oracle
-set_device("b200", directory=DIR, build_on_run=True, b200_defer=True)
+multi = getattr(bc.SCENARIOS[NAME], "multiple_runs", False)
+set_device("b200", directory=DIR, build_on_run=not multi, b200_defer=True)
 prefs.devices.cpp_standalone.openmp_threads = 0
 prefs.codegen.cpp.extra_compile_args_gcc = ['-w', '-O3', '-std=c++17', '-ffp-contract=off', '-fno-fast-math']
 prefs.core.default_float_dtype = np.float64
 defaultclock.dt = 0.1 * ms
 r = bc.SCENARIOS[NAME]()
+if multi:  # several run() calls: one explicit build
+    device.build(directory=DIR, b200_defer=True)
 jobdir = device.b200_job_dir
 out = run_job_on_oracle(jobdir)
 with open(os.path.join(jobdir, "job.json")) as f:
@@ -45,6 +48,8 @@ device.b200_import_results(jobdir)
 spk = r["spikes"]
 res = dict(spk_i=np.asarray(spk.i[:]), spk_t=np.asarray(spk.t_[:]), v=np.asarray(r["P"].v_[:]),
            count=np.asarray(spk.count[:]), rate=np.asarray(r["rate"].rate_[:]))
+if "I" in r["P"].variables:
+    res["I"] = np.asarray(r["P"].I_[:])
 if "state" in r:
     res.update(state_t=np.asarray(r["state"].t_[:]), state_v=np.asarray(r["state"].v_[:]))
 if "G" in r and hasattr(r["G"], "_lastindex"):   # a spike generator's cursor
@@ -56,7 +61,7 @@ np.savez(OUT, **res)
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(PYENV, "brian2")), reason="the reference is not importable here")
-@pytest.mark.parametrize("name", ["regular_ops", "spike_generator", "stdp", "noise_inputs"])
+@pytest.mark.parametrize("name", ["regular_ops", "spike_generator", "stdp", "noise_inputs", "host_sets"])
 def test_plugin_imports_results_into_brian_monitors(tmp_path, name):
     out = tmp_path / "got.npz"
     env = dict(os.environ, PYTHONPATH=PYENV, PYTHONHASHSEED="0")  # (the fixtures' hash seed: the order of noise terms)
@@ -84,3 +89,5 @@ def test_plugin_imports_results_into_brian_monitors(tmp_path, name):
         assert int(got["gen_last"].reshape(-1)[0]) == meta["gen_lastindex"]
     for var in meta.get("syn_vars", []):
         np.testing.assert_array_equal(got["syn_" + var], ref["syn_" + var], err_msg=var)
+    if name == "host_sets":  # the assignment after the last run reaches the results
+        np.testing.assert_array_equal(got["I"], np.full(len(got["I"]), 0.003))
