@@ -286,6 +286,8 @@ class B200Device(CPPStandaloneDevice):
             raise NotImplementedError("b200: all objects of a network must share one clock "
                                       "(run_regularly operations and state monitors may use a multiple of its dt)")
         clock = next(iter(main))
+        if self.b200_runs and self.b200_runs[0].get("dt", float(clock.dt_)) != float(clock.dt_):
+            raise NotImplementedError("b200: the time step changed between runs")
         for obj in all_objects:
             if slower(obj) and obj.clock is not clock:
                 k = float(obj.clock.dt_) / float(clock.dt_)
@@ -308,6 +310,7 @@ class B200Device(CPPStandaloneDevice):
                                     'const int _b200_kept = _b200_c.rand() == _b200_d.rand() ? 1 : 0; '
                                     '_b200_rng << " " << _b200_kept << " " << std::hexfloat << _b200_g; }'))
         self.b200_runs.append(dict(net=net, n_steps=n_steps, spec=spec, objects=objects, clock=clock,
+                                   dt=float(clock.dt_),
                                    queue_len=len(self.main_queue)))
         self.main_queue.append(("insert_code", f"// b200 network run {len(self.b200_runs) - 1} ({n_steps} steps)"))
         net.t_ = float(t_end)
@@ -323,7 +326,12 @@ class B200Device(CPPStandaloneDevice):
             self.build(direct_call=False, **self.build_options)
 
     def network_get_profiling_info(self, net):
-        return [(name, ms * 1e-3) for name, ms in self.b200_timings]
+        # (device.py:1991-2002: no information without profile=True; times as
+        # quantities in seconds; one entry for the device's step loop)
+        from brian2.units import second
+        if not self.enable_profiling:
+            raise ValueError("No profiling info collected (did you run with 'profile=True'?)")
+        return [(name, ms * 1e-3 * second) for name, ms in self.b200_timings]
 
     # ------------------------------------------------------------- spec
     def _make_spec(self, net, objects, clock):
@@ -402,6 +410,9 @@ class B200Device(CPPStandaloneDevice):
                 frag = co.fragment
                 t = frag["template"]
                 b200_objects.append((obj, co))
+                if not isinstance(obj, PoissonInput) and any(
+                        isinstance(v, BinomialFunction) for v in frag["variables"].values()):
+                    raise NotImplementedError("b200: binomial functions outside PoissonInput")
                 if isinstance(obj, PoissonInput):
                     input_frags.append((obj, frag, pos))
                 elif type(obj) is CodeRunner and t == "stateupdate":
