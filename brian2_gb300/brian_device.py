@@ -611,8 +611,8 @@ class B200Device(CPPStandaloneDevice):
                                code=dict(scalar=b["scalar"], vector=vec)))
             site.update(group=gi, lo=int(lo), hi=-1 if whole else int(hi))
             draw_sites.append((pos, site, inputs[-1]))
-        if len(inputs) > 4:
-            raise NotImplementedError("b200: more than 4 PoissonInputs")
+        if len(inputs) > 8:
+            raise NotImplementedError("b200: more than 8 PoissonInputs")
         # operations (Group.run_regularly, brian2/groups/group.py CodeRunner with
         # the stateupdate template): in the start slot before the state monitors,
         # or in the end slot after the resets; every k-th step of the network

@@ -264,7 +264,7 @@ def render_model(spec: dict) -> str:
     # their target group's table, their vector code runs over the group's neurons
     INPUTS = [dict(inp, code=dict(inp["code"], vector=_device(inp["code"]["vector"])))
               for inp in spec.get("inputs", [])]
-    assert len(INPUTS) <= 4
+    assert len(INPUTS) <= 8
     gtables, ptables = [], []
     for gi, g in enumerate(groups):
         blocks = [("update", _block(g.get("update"))), ("threshold", _block(g.get("threshold"))),
