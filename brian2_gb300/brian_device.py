@@ -293,8 +293,7 @@ class B200Device(CPPStandaloneDevice):
                 k = float(obj.clock.dt_) / float(clock.dt_)
                 if round(k) < 1 or abs(k - round(k)) > 1e-9 * k:
                     raise NotImplementedError(f"b200: {obj.name} runs every {k} steps (not a whole number)")
-        n_steps = int(clock._i_end - clock.variables["timestep"].get_value().item()) \
-            if False else int(round(float(duration) / float(clock.dt_)))
+        n_steps = int(round(float(duration) / float(clock.dt_)))
         spec, objects = self._make_spec(net, all_objects, clock)
         if draws_random(spec) and not self.b200_runs:
             # the generator state where the step loop starts drawing (the C++

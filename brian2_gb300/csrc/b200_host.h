@@ -92,6 +92,10 @@ struct b200_inst_h {
   int64_t ts = 0;
   b200_dbuf bar, status, ts_done, pending, bar64;
   int32_t ran_owner = -1;  // mode of the runs so far with spikes in flight: -1 none, 0 classic, 1 owner
+  // a launch failed part-way (timeout, index error, dropped events): the CTAs
+  // stopped at different steps, so the state no longer belongs to one time
+  // step; runs are refused until b200_set_step declares the step of the state
+  bool stale = false;
   // random stream of the step loop: generator state on the device (624 words +
   // position; randn()'s kept value), and two buffers of draws; rng_buf[rng_cur]
   // holds the draws of steps [rng_from, rng_to), and the state is at rng_to
@@ -1216,6 +1220,11 @@ extern "C" {
 int b200_run(b200_net* n, int64_t n_steps) {
   if (!n) return B200_ERR_ARG;
   if (n_steps < 0) return b200_fail(n, B200_ERR_ARG, "negative step count");
+  for (int k = 0; k < n->n_inst; ++k)
+    if (n->inst[k].stale)
+      return b200_fail(n, B200_ERR_ARG,
+                       "instance %d: an earlier run failed part-way, so its state belongs to no single time "
+                       "step; upload the state and call b200_set_step before running it again", k);
   int r;
   if (!n->prepared && (r = b200_prepare(n))) return r;
   const b200_model_info* M = n->M;
@@ -1410,6 +1419,12 @@ int b200_run(b200_net* n, int64_t n_steps) {
       cudaEventElapsedTime(&kms, k0, k1);
       kernel_ms += kms;
     }
+    // read every instance's status first and clear the failed ones' status and
+    // barrier words, so that one failure leaves no other instance with a
+    // half-counted barrier; then report the first failure
+    int first_bad = -1;
+    int32_t bad_st = 0;
+    int64_t bad_done = 0;
     for (int k = 0; k < n->n_inst; ++k) {
       b200_inst_h& I = n->inst[k];
       int32_t st = 0;
@@ -1417,30 +1432,34 @@ int b200_run(b200_net* n, int64_t n_steps) {
       B200_CU(n, cudaMemcpy(&st, I.status.p, 4, cudaMemcpyDeviceToHost));
       B200_CU(n, cudaMemcpy(&done, I.ts_done.p, 8, cudaMemcpyDeviceToHost));
       if (st != 0) {
-        // leave the handle usable: clear the status and the barrier state
-        cudaMemset(I.status.p, 0, 4);
-        cudaMemset(I.bar.p, 0, 16);
-        if (st == B200_ERR_RANDOM) {
-          I.ts = done;
-          return b200_fail(n, B200_STATUS_RANDOM_H,
-                           "instance %d: a binomial draw before step %lld started over more often than the "
-                           "stream's window holds numbers", k, (long long)done);
-        }
-        if (st == B200_ERR_EVENT_OVERFLOW) {
-          I.ts = done;
-          return b200_fail(n, B200_ERR_CAPACITY,
-                           "instance %d: an owner-mode event FIFO overflowed before step %lld (events were dropped; "
-                           "raise its size with b200_set_event_capacity and run again from the start)",
-                           k, (long long)done);
-        }
-        return b200_fail(n, st == B200_ERR_BARRIER_TIMEOUT ? B200_ERR_BARRIER_TIMEOUT : B200_ERR_INDEX,
-                         "instance %d: device status %d at step %lld (%s)", k, st, (long long)done,
-                         st == B200_ERR_BARRIER_TIMEOUT ? "instance barrier timed out" : "index out of range");
+        B200_CU(n, cudaMemset(I.status.p, 0, 4));
+        B200_CU(n, cudaMemset(I.bar.p, 0, 16));
+        I.ts = done;
+        // a binomial restart stops every CTA at the same step boundary; the
+        // other failures leave CTAs at different steps
+        if (st != B200_ERR_RANDOM) I.stale = true;
+        if (first_bad < 0) { first_bad = k; bad_st = st; bad_done = done; }
+        continue;
       }
       if (done < I.ts || done > target[k])
         return b200_fail(n, B200_ERR_CUDA, "instance %d: bad progress %lld", k, (long long)done);
       if (done > I.ts) I.ran_owner = n->owner;
       I.ts = done;
+    }
+    if (first_bad >= 0) {
+      const int k = first_bad;
+      if (bad_st == B200_ERR_RANDOM)
+        return b200_fail(n, B200_STATUS_RANDOM_H,
+                         "instance %d: a binomial draw before step %lld started over more often than the "
+                         "stream's window holds numbers", k, (long long)bad_done);
+      if (bad_st == B200_ERR_EVENT_OVERFLOW)
+        return b200_fail(n, B200_ERR_CAPACITY,
+                         "instance %d: an owner-mode event FIFO overflowed before step %lld (events were dropped; "
+                         "raise its size with b200_set_event_capacity and run again from the start)",
+                         k, (long long)bad_done);
+      return b200_fail(n, bad_st == B200_ERR_BARRIER_TIMEOUT ? B200_ERR_BARRIER_TIMEOUT : B200_ERR_INDEX,
+                       "instance %d: device status %d at step %lld (%s)", k, bad_st, (long long)bad_done,
+                       bad_st == B200_ERR_BARRIER_TIMEOUT ? "instance barrier timed out" : "index out of range");
     }
   }
   B200_CU(n, cudaEventRecord(e1, n->stream));
@@ -1662,6 +1681,7 @@ int b200_get_step(b200_net* n, int32_t inst, int64_t* ts) {
 int b200_set_step(b200_net* n, int32_t inst, int64_t ts) {
   if (!n || inst < 0 || inst >= n->n_inst || ts < 0) return B200_ERR_ARG;
   n->inst[inst].ts = ts;
+  n->inst[inst].stale = false;
   n->inst[inst].rng_from = n->inst[inst].rng_to = ts;  // (the random stream continues from the generator)
   return 0;
 }

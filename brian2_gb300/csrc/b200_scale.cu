@@ -26,6 +26,8 @@
 #include <mutex>
 #include <cuda_runtime.h>
 
+#include "b200_scale.h"  // the C ABI this file implements (include/)
+
 namespace {
 
 struct u4 { uint32_t x, y, z, w; };
@@ -271,12 +273,12 @@ int b200s_fixed_indegree_csr(uint64_t seed, int32_t path_id, int32_t n_src, int3
   g_err[0] = 0;
   if (K < 0 || K > 1024 || K > n_src || n_post < 0 || n_src <= 0) {
     snprintf(g_err, sizeof(g_err), "invalid sizes (K=%d, n_src=%d)", K, n_src);
-    return 2;
+    return B200S_STATUS_ARG;
   }
   const int s0 = (int)(dmin / dt + 0.5), s1 = (int)((dmin + dspan) / dt + 0.5);
   if (s0 < 0 || s1 > 255) {
     snprintf(g_err, sizeof(g_err), "delays out of the 0..255 step range");
-    return 2;
+    return B200S_STATUS_ARG;
   }
   const int W = s1 - s0 + 1;
   const int64_t n = (int64_t)n_post * K;
@@ -301,7 +303,7 @@ int b200s_fixed_indegree_csr(uint64_t seed, int32_t path_id, int32_t n_src, int3
     cudaFree(slot);
     cudaFree(err);
     snprintf(g_err, sizeof(g_err), "sampling did not converge");
-    return 3;
+    return B200S_STATUS_NOT_CONVERGED;
   }
   S_CU(cudaMalloc(&cnt, (size_t)nb * 4 + 16));
   S_CU(cudaMemset(cnt, 0, (size_t)nb * 4 + 16));
@@ -311,7 +313,7 @@ int b200s_fixed_indegree_csr(uint64_t seed, int32_t path_id, int32_t n_src, int3
   if (h_err) {
     cudaFree(pre); cudaFree(slot); cudaFree(err); cudaFree(cnt);
     snprintf(g_err, sizeof(g_err), "construction produced an out-of-range index");
-    return 5;
+    return B200S_STATUS_INDEX;
   }
   const int64_t nblk = (nb + 1023) / 1024;
   S_CU(cudaMalloc(&seg, (size_t)(nb + 1) * 8));
@@ -339,7 +341,7 @@ int b200s_fixed_indegree_csr(uint64_t seed, int32_t path_id, int32_t n_src, int3
     cudaFree(post_csr);
     cudaFree(pre_csr);
     snprintf(g_err, sizeof(g_err), "sampling did not converge");
-    return 3;
+    return B200S_STATUS_NOT_CONVERGED;
   }
   *slot_min = s0;
   *slot_max = s1;
@@ -414,7 +416,7 @@ int scratch_on_current_device(unsigned char** out) {
   S_CU(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 256) {
     snprintf(g_err, sizeof(g_err), "device ordinal %d out of range", dev);
-    return 2;
+    return B200S_STATUS_ARG;
   }
   std::lock_guard<std::mutex> lock(g_scratch_mu);
   if (!g_scratch_addr[dev]) {
@@ -461,13 +463,13 @@ int b200s_fixed_indegree_csr_noalloc(uint64_t seed, int32_t path_id, int32_t n_s
   const int64_t need = b200s_noalloc_scratch_bytes(n_src, n_post, K, dmin, dspan, dt);
   if (need == 0) {
     snprintf(g_err, sizeof(g_err), "invalid sizes (K=%d, n_src=%d, n_post=%d) or delays", K, n_src, n_post);
-    return 2;
+    return B200S_STATUS_ARG;
   }
   if ((size_t)need > B200S_NOALLOC_SCRATCH_BYTES) {
     snprintf(g_err, sizeof(g_err),
              "network too large for the allocation-free path: needs %lld scratch bytes, the limit is %zu "
              "(use b200s_fixed_indegree_csr)", (long long)need, B200S_NOALLOC_SCRATCH_BYTES);
-    return 3;
+    return B200S_STATUS_SCRATCH_LIMIT;
   }
   const int s0 = (int)(dmin / dt + 0.5), s1 = (int)((dmin + dspan) / dt + 0.5);
   const int W = s1 - s0 + 1;
@@ -475,7 +477,7 @@ int b200s_fixed_indegree_csr_noalloc(uint64_t seed, int32_t path_id, int32_t n_s
   if (cap_seg < nb + 1 || cap_syn < n || !d_segptr || (n > 0 && (!d_post || !d_pre))) {
     snprintf(g_err, sizeof(g_err), "output buffers too small: need %lld segment and %lld synapse entries",
              (long long)(nb + 1), (long long)n);
-    return 2;
+    return B200S_STATUS_ARG;
   }
   unsigned char* base = nullptr;
   int r = scratch_on_current_device(&base);
@@ -499,7 +501,7 @@ int b200s_fixed_indegree_csr_noalloc(uint64_t seed, int32_t path_id, int32_t n_s
   S_CU(cudaMemcpy(&h_err, err, 4, cudaMemcpyDeviceToHost));
   if (h_err) {
     snprintf(g_err, sizeof(g_err), "sampling did not converge");
-    return 3;
+    return B200S_STATUS_NOT_CONVERGED;
   }
   S_CU(cudaMemset(cnt, 0, (size_t)nb * 4 + 16));
   b200s_count_kernel<<<4096, 256>>>(pre, slot, n, W, s0, n_src, cnt, err);
@@ -507,7 +509,7 @@ int b200s_fixed_indegree_csr_noalloc(uint64_t seed, int32_t path_id, int32_t n_s
   S_CU(cudaMemcpy(&h_err, err, 4, cudaMemcpyDeviceToHost));
   if (h_err) {
     snprintf(g_err, sizeof(g_err), "construction produced an out-of-range index");
-    return 5;
+    return B200S_STATUS_INDEX;
   }
   b200s_scan_block<<<(unsigned)nblk, 1024>>>(cnt, nb, d_segptr, bsum);
   b200s_scan_sums<<<1, 32>>>(bsum, nblk);
@@ -519,7 +521,7 @@ int b200s_fixed_indegree_csr_noalloc(uint64_t seed, int32_t path_id, int32_t n_s
   S_CU(cudaGetLastError());
   b200s_sort_segments<<<4096, 256>>>(d_segptr, nb, W, src_off, d_post, d_pre);
   S_CU(cudaGetLastError());
-  S_CU(cudaDeviceSynchronize());
+  S_CU(cudaStreamSynchronize(0));  // the legacy default stream, which every launch above used
   *slot_min = s0;
   *slot_max = s1;
   return 0;

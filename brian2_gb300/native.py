@@ -21,6 +21,7 @@ import threading
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -110,9 +111,10 @@ def build_construct() -> str:
 
 def build_scale() -> str:
     src = os.path.join(CSRC, "b200_scale.cu")
-    out = os.path.join(BUILD, f"libb200_scale_{_sources_digest([src, os.path.join(CSRC, 'b200_device.cuh')])}.so")
+    hdr = os.path.join(INCLUDE, "b200_scale.h")
+    out = os.path.join(BUILD, f"libb200_scale_{_sources_digest([src, hdr, os.path.join(CSRC, 'b200_device.cuh')])}.so")
     return _locked_build(out, lambda tmp: _run(
-        [nvcc_path()] + nvcc_flags(True) + [src, "-o", tmp], "libb200_scale"))
+        [nvcc_path()] + nvcc_flags(True) + [f"-I{INCLUDE}", src, "-o", tmp], "libb200_scale"))
 
 
 def build_adjoint() -> str:

@@ -144,6 +144,10 @@ int b200_set_statemon(b200_net* net, int32_t inst, int32_t mon, const int32_t* i
 int b200_run(b200_net* net, int64_t n_steps);
 /* Current clock step of an instance (Clock::timestep, brianlib/clocks.h:34-38). */
 int b200_get_step(b200_net* net, int32_t inst, int64_t* ts);
+/* Sets an instance's clock step.  After a run that failed part-way (timeout,
+ * index error, dropped events) the instance's CTAs stopped at different steps
+ * and b200_run refuses it (B200_STATUS_ARG) until the caller has uploaded a
+ * consistent state and declared its step here. */
 int b200_set_step(b200_net* net, int32_t inst, int64_t ts);
 /* Device time of the last b200_run in ms (CUDA events); the reference's
  * _last_run_time (device.py:1326-1332). */
@@ -166,7 +170,9 @@ int b200_reset_monitors(b200_net* net, int32_t inst);
 /* Bounded device-side waits: limit in ns for the instance barrier, and a test
  * hook (fault_rank >= 0) that makes that CTA leave before its first barrier of
  * the next launch, so the others time out and b200_run returns
- * B200_STATUS_TIMEOUT with the handle still usable.  The reference's analogue
+ * B200_STATUS_TIMEOUT with the handle still usable (every instance's status and
+ * barrier words are cleared; a failed instance runs again after
+ * b200_set_step).  The reference's analogue
  * is the wall-clock limit of Network::run (templates/network.cpp:59-82). */
 int b200_set_wait_limit(b200_net* net, int64_t limit_ns, int32_t fault_rank);
 

@@ -6,9 +6,9 @@
 # vendored inside pip.  Only a host with the reference sources can build it; the
 # tree is ignored by git and left out of copies of the repository to other hosts.
 #
-# usage: bash oracle/make_ref_env.sh [/path/to/reference]
+# usage: bash oracle/make_ref_env.sh /path/to/reference
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:?usage: make_ref_env.sh /path/to/reference (the directory holding brian2/)}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref/pyenv"
 [ -d "$REF/brian2" ] || { echo "reference not found at $REF" >&2; exit 1; }

@@ -8,7 +8,7 @@ code generator for its OpenMP standalone path
 so what runs on the host cores is the reference's generated step loop
 unchanged.  Generation needs the reference importable, so it runs here::
 
-    bash oracle/make_ref_env.sh
+    bash oracle/make_ref_env.sh <reference checkout>
     PYTHONPATH=oracle/_ref/pyenv python oracle/make_ref_standalone.py [threads ...]
 
 Output (git-ignored, compiled where it runs by ``ref_standalone.build``): one

@@ -13,7 +13,7 @@ compile flags so the results are the reference's exact arithmetic.  It stores:
 
 Run where the reference is importable (it is not needed afterwards)::
 
-    bash oracle/make_ref_env.sh
+    bash oracle/make_ref_env.sh <reference checkout>
     PYTHONPATH=oracle/_ref/pyenv python tests/golden/make_golden.py [case ...]
 """
 import hashlib

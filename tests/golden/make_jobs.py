@@ -12,7 +12,7 @@ the result with the reference's fixture of the same case.
 Run where the reference is importable (single-threaded, strict flags, as the
 golden fixtures)::
 
-    bash oracle/make_ref_env.sh
+    bash oracle/make_ref_env.sh <reference checkout>
     PYTHONPATH=oracle/_ref/pyenv python tests/golden/make_jobs.py
 """
 import os

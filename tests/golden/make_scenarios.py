@@ -15,7 +15,7 @@ per process):
 
 Run where the reference is importable::
 
-    bash oracle/make_ref_env.sh
+    bash oracle/make_ref_env.sh <reference checkout>
     PYTHONPATH=oracle/_ref/pyenv python tests/golden/make_scenarios.py [name ...]
 """
 import json

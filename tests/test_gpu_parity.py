@@ -136,21 +136,33 @@ def test_batched_instances_equal_separate_oracles():
 
 @pytest.mark.parametrize("owner", [True, False])
 def test_barrier_timeout_reports_status_and_handle_stays_usable(owner):
+    """CTA 1 of every instance skips its first barrier: the run fails with the
+    timeout status; both instances are cleared (status and barrier words), are
+    refused until their state and step are declared again, and then run on the
+    same handle identically to the oracle."""
     from brian2_gb300.runtime import B200Error
     spec = W.load_spec("cuba_f64")
-    b = W.build_cuba(spec, N=2000, seed=3)
-    net = W.instantiate(spec, [b], threads=128, ctas_per_inst=4)
+    builts = [W.build_cuba(spec, N=2000, seed=3), W.build_cuba(spec, N=1500, seed=4)]
+    net = W.instantiate(spec, builts, threads=128, ctas_per_inst=4)
     net.set_owner(owner)
-    net.set_wait_limit(50_000_000, fault_rank=1)   # 50 ms; CTA 1 skips its first barrier
+    net.set_wait_limit(50_000_000, fault_rank=1)   # 50 ms; CTA 1 of each instance skips its first barrier
     with pytest.raises(B200Error) as e:
         net.run(10)
     assert e.value.status == 4
-    # the context is intact: a new network on the same device runs normally
-    net2 = W.instantiate(spec, [b], threads=128, ctas_per_inst=4)
-    net2.run(100)
-    o = oracle_from_built(spec, b)
-    o.run(100)
-    np.testing.assert_array_equal(net2.spikes(0, 0)[0], o.spikes(0)[0])
+    with pytest.raises(B200Error) as e:
+        net.run(10)
+    assert e.value.status == 2 and "set_step" in str(e.value)
+    for k, b in enumerate(builts):
+        for (g, v), arr in b.group_init.items():
+            net.upload(k, g, v, arr)
+        net.set_step(k, 0)
+        net.reset_monitors(k)
+    net.run(100)
+    for k, b in enumerate(builts):
+        o = oracle_from_built(spec, b)
+        o.run(100)
+        np.testing.assert_array_equal(net.spikes(k, 0)[0], o.spikes(0)[0])
+        np.testing.assert_array_equal(net.download(k, "neurongroup", "v"), o.download(0, "v"))
 
 
 def test_owner_fifo_overflow_is_reported():
