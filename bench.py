@@ -11,15 +11,19 @@ Printed (rank 0, one JSON line): synaptic events/s over the timed steps
 (events = sum over emitted spikes of the source's out-degree), simulated
 seconds per wall second, an end-to-end figure through the public API with host
 buffers (state uploaded from pinned memory and the step's spikes read back every
-step), the step kernel's roofline, and the reference's own CPU step loop timed
-on the host cores as a CPU baseline: the cpp_standalone project the reference
-generates for the 10,000-neuron subnetwork of identical construction, OpenMP
-(oracle/ref_standalone.py); where that project was not generated, the oracle
-(single-threaded C++ restatement) instead.  On one GPU the line also carries
-the other workloads, each measured in this run: CUBA 4000 (float64), COBAHH
-4000 (float64 and float32), the 256-network batched sweep against the same
-networks run one after another, and the adjoint's forward+adjoint / forward
-cost ratio.
+step), the step kernel's roofline, and a CPU baseline: the reference's own
+generated cpp_standalone project (OpenMP) of the 10,000-neuron subnetwork of
+identical construction, a bounded sample that fits the default run (where that
+project was not generated, the oracle instead).  On one GPU the line also
+carries the other workloads, each measured in this run: CUBA 4000 (float64),
+COBAHH 4000 (float64 and float32), the 256-network batched sweep against the
+same networks run one after another, and the adjoint's forward+adjoint /
+forward cost ratio.
+
+--impl reference runs the reference's own step loop on the headline network
+itself (1e6 neurons, 1e9 synapses, float32, its generated cpp_standalone
+project with OpenMP on all host cores) and prints the same metric and config;
+each of its steps is one progress-report interval of that run.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -283,26 +287,79 @@ def extras():
     return out
 
 
+def workload_config(N, K):
+    """The workload both arms of the benchmark run (the reference arm prints
+    the same dictionary)."""
+    return {"workload": WORKLOAD if (N, K) == (N_NEURONS, K_IN) else f"cuba_delays_n{N}_k{K}_f32",
+            "neurons": N, "in_degree": K, "synapses": N * K, "delays_ms": [0.1, 5.0], "dt_ms": 0.1,
+            "state": "float32", "l2": "inputs larger than L2 (synapse arrays 8 GB per GPU)"}
+
+
+def reference_headline(steps, warmup):
+    """The reference's own step loop on the headline network itself: its
+    generated cpp_standalone project of the 1,000,000-neuron network (float32,
+    OpenMP on all host cores) runs once -- construction, a 50 ms run, then a
+    100 ms run whose progress reports (about every 0.5 s of wall time) are the
+    samples; the first `warmup` samples are discarded, the next `steps` timed.
+    None when the project was not generated."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_standalone
+    if not ref_standalone.available("delays1e6"):
+        return None
+    T = ref_standalone.all_threads("delays1e6")
+    ref_standalone.build(T, workload="delays1e6")
+    t0 = time.perf_counter()
+    r = ref_standalone.run(T, workload="delays1e6", timeout=1500)
+    wall = time.perf_counter() - t0
+    smp = r["samples"]
+    use = smp[warmup:warmup + steps] if len(smp) > warmup else smp
+    if not use:
+        return None
+    ev = sum(x["events"] for x in use)
+    sec = sum(x["run_time_s"] for x in use)
+    st = sum(x["steps"] for x in use)
+    return {"value": ev / sec, "unit": UNIT, "cores": r["threads"], "kind": "reference",
+            "sample": f"reference cpp_standalone project of this network (generated by the reference, "
+                      f"g++ -O3 -ffast-math -fopenmp, {r['threads']} OpenMP threads, float32): one execution "
+                      f"(construction, 50 ms run, 100 ms reported run; {wall:.0f} s wall in all), "
+                      f"{len(use)} progress-report intervals after {min(warmup, len(smp))} discarded: "
+                      f"{st} clock steps, {sum(x['spikes'] for x in use)} spikes, {ev} events, "
+                      f"step loop {sec:.2f} s",
+            "sim_s_per_wall_s": st * 1e-4 / sec, "samples_used": len(use), "samples_available": len(smp),
+            "per_sample": [round(x["events"] / x["run_time_s"], 1) for x in use]}
+
+
 def run_reference(args, rank, world):
-    """--impl reference: the reference's CPU path for this workload (its
-    generated cpp_standalone project with OpenMP, else the oracle port) on the
-    same metric and config; every step is one bounded sample."""
+    """--impl reference: the reference's CPU path for this workload -- its
+    generated cpp_standalone project of the same network with OpenMP -- on the
+    same metric and config; every step is one progress-report interval of the
+    reference's own run.  Where that project was not generated: the
+    10,000-neuron subnetwork project, else the oracle port, each stated."""
     if rank != 0:
         return
-    vals = []
-    for _ in range(min(args.warmup, 1)):
-        cpu_baseline(max_seconds=5.0)
-    for _ in range(args.steps):
-        vals.append(cpu_baseline(max_seconds=10.0))
-    v = float(np.median([x["value"] for x in vals]))
-    base = vals[0]
+    r = reference_headline(args.steps, args.warmup)
+    if r is not None:
+        config = workload_config(N_NEURONS, K_IN)
+        dtype = "f32"
+    else:
+        vals = []
+        for _ in range(min(args.warmup, 1)):
+            cpu_baseline(max_seconds=5.0)
+        for _ in range(args.steps):
+            vals.append(cpu_baseline(max_seconds=10.0))
+        r = dict(vals[0], value=float(np.median([x["value"] for x in vals])))
+        config = dict(workload_config(N_NEURONS, K_IN), sample="10,000-neuron subnetwork, same construction, float64")
+        dtype = "f64"
+    v = r["value"]
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded construction)",
-            "config": {"workload": WORKLOAD, "sample": "10,000-neuron subnetwork, same construction"},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": base["cores"], "kind": base["kind"],
-                             "sample": base["sample"]},
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic (seeded construction)",
+            "config": config,
+            "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample") if k in r},
+            "sim_s_per_wall_s": r.get("sim_s_per_wall_s"),
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if "per_sample" in r:
+        line["per_sample"] = r["per_sample"]
     print(json.dumps(line), flush=True)
 
 
@@ -442,12 +499,9 @@ def main():
             "warmup": args.warmup, "ms_per_step": device_s / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: network constructed on the device from a seed",
-            "config": {"workload": WORKLOAD if (N, K) == (N_NEURONS, K_IN) else f"cuba_delays_n{N}_k{K}_f32",
-                       "neurons": N, "in_degree": K, "synapses": N * K,
-                       "delays_ms": [0.1, 5.0], "dt_ms": 0.1, "clock_steps_per_step": STEPS_PER_BENCH_STEP,
-                       "l2": "inputs larger than L2 (synapse arrays 8 GB per GPU)",
-                       "threads": threads, "ctas": ctas, "launch_plan": plan, "build_s": round(t_build, 2),
-                       "owner_mode": net_owner},
+            "config": workload_config(N, K),
+            "launch": {"clock_steps_per_step": STEPS_PER_BENCH_STEP, "threads": threads, "ctas": ctas,
+                       "launch_plan": plan, "build_s": round(t_build, 2), "owner_mode": net_owner},
             "sim_s_per_wall_s": sim_s / device_s,
             "wall_ms_per_step": wall / args.steps * 1e3,
             "spikes_per_step": float(len(i)) / args.steps,

@@ -36,11 +36,19 @@ def nvcc_path() -> str:
     return p
 
 
-def nvcc_flags(exact: bool = True) -> list[str]:
+def nvcc_flags(exact: bool = True, single: bool = False) -> list[str]:
+    """exact: IEEE division and square root, no contraction into FMAs (the
+    float64 models' bit-exactness with the reference needs all three).
+    single (float32 models): no contraction either -- Brian's float32
+    expressions keep their rounding order -- but the fast division and square
+    root; float32 results are held to a stated error against the float64
+    reference, not to bit-exactness."""
     flags = [ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xptxas", "-dlcm=cg",
              "-diag-suppress", "177,550,2361", "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math",
              "-shared", f"-I{CSRC}"]
-    if exact:
+    if exact and single:
+        flags += ["--fmad=false", "-prec-div=false", "-prec-sqrt=false"]
+    elif exact:
         flags += ["--fmad=false", "-prec-div=true", "-prec-sqrt=true"]
     return flags
 
@@ -81,7 +89,7 @@ def _locked_build(out: str, build_fn):
 def model_library_path(spec: dict) -> str:
     from .codegen import spec_hash
     deps = [os.path.join(CSRC, f) for f in ("b200_device.cuh", "b200_host.h")]
-    tag = spec_hash(spec) + _sources_digest(deps + [os.path.join(HERE, "codegen.py")])
+    tag = spec_hash(spec) + _sources_digest(deps + [os.path.join(HERE, "codegen.py"), os.path.abspath(__file__)])
     return os.path.join(BUILD, "models", f"{spec['name']}_{tag}.so")
 
 
@@ -95,7 +103,8 @@ def build_model(spec: dict) -> str:
         with open(src, "w") as f:
             f.write(render_model(spec))
         exact = not spec.get("fast_math", False)
-        _run([nvcc_path()] + nvcc_flags(exact) + [src, "-o", tmp], f"model {spec['name']}")
+        single = spec.get("float", "double") == "float"
+        _run([nvcc_path()] + nvcc_flags(exact, single) + [src, "-o", tmp], f"model {spec['name']}")
 
     return _locked_build(out, _build)
 

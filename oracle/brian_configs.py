@@ -84,13 +84,17 @@ def cobahh(N=4000, duration_ms=1000.0, seed_value=1234, ne_frac=0.8):
 
 
 def cuba_delays(N=10000, K=1000, duration_ms=1000.0, seed_value=1234, ne_frac=0.8,
-                wscale=1.0 / 50, dmin_ms=0.1, dmax_ms=5.0):
+                wscale=1.0 / 50, dmin_ms=0.1, dmax_ms=5.0, warmup_ms=0.0, report=None, report_period_s=10.0):
     """Large CUBA: fixed in-degree K split 80/20 between E and I sources.
 
     Every neuron receives exactly ``ne_frac*K`` synapses from distinct sources
     drawn uniformly from the excitatory population and ``K - ne_frac*K`` from the
     inhibitory one (``sample(N_pre, size=...)`` per target).  Weights are a
     per-synapse variable ``w`` and delays are drawn uniformly per synapse.
+    With ``warmup_ms`` a first ``run(warmup_ms)`` precedes the run of
+    ``duration_ms``; ``report`` and ``report_period_s`` are passed to that run
+    (Brian's progress report: for the standalone device, C++ code of the
+    report function, ``device.py:1889-1907``).
     """
     from brian2 import (NeuronGroup, Synapses, SpikeMonitor, PopulationRateMonitor,
                         ms, mV, seed, run)
@@ -120,7 +124,13 @@ def cuba_delays(N=10000, K=1000, duration_ms=1000.0, seed_value=1234, ne_frac=0.
     Ci.delay = 'dmin + rand()*dspan'
     s_mon = SpikeMonitor(P)
     r_mon = PopulationRateMonitor(P)
-    run(duration_ms * ms)
+    from brian2 import second
+    if warmup_ms > 0:
+        run(warmup_ms * ms)
+    if report is None:
+        run(duration_ms * ms)
+    else:
+        run(duration_ms * ms, report=report, report_period=report_period_s * second)
     return dict(P=P, Ce=Ce, Ci=Ci, spikes=s_mon, rate=r_mon)
 
 

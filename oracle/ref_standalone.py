@@ -1,18 +1,22 @@
-"""Compiles and times the reference's generated ``cpp_standalone`` project.
+"""Compiles and times the reference's generated ``cpp_standalone`` projects.
 
 Test infrastructure only: the timed CPU baseline beside the GPU numbers (the
 reference's own OpenMP step loop on the host cores).  The projects under
-``oracle/_ref/standalone_delays_t<threads>/`` are written by
-``make_ref_standalone.py`` from the reference's code generator, one per OpenMP
-thread count; this module compiles them with the
+``oracle/_ref/standalone_<workload>_t<threads>/`` are written by
+``make_ref_standalone.py`` from the reference's code generator, one per
+workload and OpenMP thread count; this module compiles them with the
 reference's default GCC options for this architecture
 (``brian2/codegen/cpp_prefs.py:109-116``) minus ``-march=native`` (kept
-portable), plus ``-fopenmp``, and runs it.  The run time is the reference's own
-measurement of its step loop (``Network::_last_run_time``, written to
-``results/last_run_info.txt`` by ``templates/objects.cpp:364-371``), so
-construction and file output are outside it.  Synaptic events are counted from
-the run's own results: the out-degree of every spiking source, from the
-synapses' presynaptic index arrays.
+portable), plus ``-fopenmp``, and runs them.  The run time is the reference's
+own measurement of its step loop: ``Network::_last_run_time`` (written to
+``results/last_run_info.txt`` by ``templates/objects.cpp:364-371``) for the
+whole run, and for a run that reports its progress the elapsed times its report
+function prints (the same ``elapsed_realtime``,
+``templates/network.cpp:59-121``); construction and file output are outside
+it.  Synaptic events are counted from the run's own results: the out-degree of
+every spiking source, from the synapses' presynaptic index arrays, and for a
+run that reports its progress the spikes of each interval between reports from
+the monitor's spike times.
 """
 from __future__ import annotations
 
@@ -30,53 +34,65 @@ REF = os.path.join(HERE, "_ref")
 FLAGS = ["-w", "-O3", "-ffast-math", "-fno-finite-math-only", "-std=c++17", "-fopenmp"]
 
 
-def project(threads: int) -> str:
-    return os.path.join(REF, f"standalone_delays_t{threads}")
+def project(threads: int, workload: str = "delays") -> str:
+    return os.path.join(REF, f"standalone_{workload}_t{threads}")
 
 
-def variants() -> list[int]:
-    """OpenMP thread counts of the generated projects present here."""
+def variants(workload: str = "delays") -> list[int]:
+    """OpenMP thread counts of the generated projects of a workload present here."""
     out = []
+    pre = f"standalone_{workload}_t"
     if os.path.isdir(REF):
         for d in os.listdir(REF):
-            if d.startswith("standalone_delays_t") and os.path.exists(os.path.join(REF, d, "manifest.json")):
-                out.append(int(d.rsplit("_t", 1)[1]))
+            if d.startswith(pre) and d[len(pre):].isdigit() and os.path.exists(os.path.join(REF, d, "manifest.json")):
+                out.append(int(d[len(pre):]))
     return sorted(out)
 
 
-def available() -> bool:
-    return bool(variants())
+def workloads() -> list[tuple[str, int]]:
+    """(workload, threads) of every generated project present here."""
+    out = []
+    if os.path.isdir(REF):
+        for d in sorted(os.listdir(REF)):
+            if d.startswith("standalone_") and os.path.exists(os.path.join(REF, d, "manifest.json")):
+                w, t = d[len("standalone_"):].rsplit("_t", 1)
+                out.append((w, int(t)))
+    return out
 
 
-def all_threads() -> int:
+def available(workload: str = "delays") -> bool:
+    return bool(variants(workload))
+
+
+def all_threads(workload: str = "delays") -> int:
     """The largest generated thread count this host has cores for (the
     smallest one when it has fewer cores than any)."""
-    v = variants()
+    v = variants(workload)
     fit = [t for t in v if t <= (os.cpu_count() or 1)]
     return max(fit) if fit else min(v)
 
 
-def manifest(threads: int) -> dict:
-    with open(os.path.join(project(threads), "manifest.json")) as f:
+def manifest(threads: int, workload: str = "delays") -> dict:
+    with open(os.path.join(project(threads, workload), "manifest.json")) as f:
         return json.load(f)
 
 
-def binary_path(threads: int) -> str:
-    return os.path.join(project(threads), f"main_{platform.machine()}")
+def binary_path(threads: int, workload: str = "delays") -> str:
+    return os.path.join(project(threads, workload), f"main_{platform.machine()}")
 
 
 def build_all() -> list[str]:
-    return [build(t) for t in variants()]
+    return [build(t, workload=w) for w, t in workloads()]
 
 
-def build(threads: int, jobs: int = 0) -> str:
+def build(threads: int, jobs: int = 0, workload: str = "delays") -> str:
     """Compiles one project (one g++ per source file, in parallel); returns the
     binary's path.  Rebuilds only when the binary is missing."""
-    out = binary_path(threads)
+    out = binary_path(threads, workload)
     if os.path.exists(out):
         return out
-    PROJECT = project(threads)
-    man = manifest(threads)
+    PROJECT = project(threads, workload)
+    man = manifest(threads, workload)
     cxx = shutil.which("g++") or "g++"
     objdir = os.path.join(PROJECT, f"_obj_{platform.machine()}")
     os.makedirs(objdir, exist_ok=True)
@@ -100,25 +116,54 @@ def build(threads: int, jobs: int = 0) -> str:
     return out
 
 
-def run(threads: int, timeout: float = 600.0) -> dict:
+def run(threads: int, timeout: float = 1200.0, workload: str = "delays") -> dict:
     """Runs one compiled project once; returns its step-loop time, simulated
-    steps, spikes and synaptic events."""
-    man = manifest(threads)
-    PROJECT = project(threads)
+    steps, spikes and synaptic events -- over its (last) run, and, for a
+    project whose run reports its progress, per interval between consecutive
+    reports (``samples``; the report function is called with the run's
+    elapsed time and completed fraction, ``templates/network.cpp:59-121``)."""
+    man = manifest(threads, workload)
+    PROJECT = project(threads, workload)
     res = os.path.join(PROJECT, "results")
     os.makedirs(res, exist_ok=True)
-    r = subprocess.run([binary_path(threads)], cwd=PROJECT, capture_output=True, text=True, timeout=timeout)
-    if r.returncode:
-        raise RuntimeError(f"reference project exited with {r.returncode}:\n{r.stdout[-1000:]}{r.stderr[-1000:]}")
-    with open(os.path.join(res, "last_run_info.txt")) as f:
-        run_time, frac = (float(x) for x in f.read().split())
-    spk = np.fromfile(os.path.join(res, man["spike_i"]), dtype=np.int32)
-    N = man["N"]
-    outdeg = np.zeros(N, np.int64)
-    for k, fname in man["pre"].items():
-        pre = np.fromfile(os.path.join(res, fname), dtype=np.int32)
-        outdeg += np.bincount(pre, minlength=N)
-    steps = int(round(man["duration_ms"] * 1e-3 / man["dt"] * frac))
-    shutil.rmtree(res, ignore_errors=True)  # every array of the run: hundreds of MB
-    return dict(run_time_s=run_time, steps=steps, spikes=int(spk.size), events=int(outdeg[spk].sum()),
-                threads=man["threads"], sim_s=steps * man["dt"])
+    try:
+        r = subprocess.run([binary_path(threads, workload)], cwd=PROJECT, capture_output=True, text=True,
+                           timeout=timeout)
+        if r.returncode:
+            raise RuntimeError(f"reference project exited with {r.returncode}:\n{r.stdout[-1000:]}{r.stderr[-1000:]}")
+        with open(os.path.join(res, "last_run_info.txt")) as f:
+            last_time, frac = (float(x) for x in f.read().split())
+        N, dt = man["N"], man["dt"]
+        spk = np.fromfile(os.path.join(res, man["spike_i"]), dtype=np.int32)
+        outdeg = np.zeros(N, np.int64)
+        for k, fname in man["pre"].items():
+            pre = np.fromfile(os.path.join(res, fname), dtype=np.int32)
+            outdeg += np.bincount(pre, minlength=N)
+            del pre
+        ev = outdeg[spk]
+        n_run = int(round(man["duration_ms"] * 1e-3 / dt))
+        done = int(round(n_run * frac))
+        samples = []
+        if man.get("spike_t"):
+            step = np.rint(np.fromfile(os.path.join(res, man["spike_t"]), dtype=np.float64) / dt).astype(np.int64)
+        else:  # (a project of one run from its start)
+            step = None
+        s0 = int(round(man.get("warmup_ms", 0.0) * 1e-3 / dt))  # first step of the reported run
+        if step is not None:
+            in_run = (step >= s0) & (step < s0 + done)
+            total = dict(run_time_s=last_time, steps=done, spikes=int(in_run.sum()), events=int(ev[in_run].sum()))
+        else:
+            total = dict(run_time_s=last_time, steps=done, spikes=int(spk.size), events=int(ev.sum()))
+        if man.get("run_mark") and step is not None:
+            rep = [(float(a), float(b)) for ln in r.stdout.splitlines() if ln.startswith(man["run_mark"] + " ")
+                   for a, b in [ln.split()[1:3]]]
+            for (e0, c0), (e1, c1) in zip(rep, rep[1:]):
+                a, b = s0 + int(round(c0 * n_run)), s0 + int(round(c1 * n_run))
+                if b > a and e1 > e0:
+                    m = (step >= a) & (step < b)
+                    samples.append(dict(run_time_s=e1 - e0, steps=b - a, spikes=int(m.sum()),
+                                        events=int(ev[m].sum())))
+    finally:
+        shutil.rmtree(res, ignore_errors=True)  # every array of the run: up to many GB
+    return dict(total, threads=man["threads"], sim_s=total["steps"] * dt, samples=samples, N=man["N"],
+                K=man["K"], float_dtype=man.get("float_dtype", "float64"))

@@ -46,6 +46,9 @@ CASES = {
     "cobahh_small_f64": ("cobahh", dict(N=400, duration_ms=100.0, seed_value=3), "float64", True),
     "delays_f64": ("cuba_delays", dict(N=10000, K=1000, duration_ms=200.0, seed_value=1234), "float64", False),
     "delays_small_f64": ("cuba_delays", dict(N=2000, K=100, duration_ms=300.0, seed_value=5), "float64", True),
+    # the full simulated second of the benchmark configurations
+    "cobahh_1s_f64": ("cobahh", dict(N=4000, duration_ms=1000.0, seed_value=1234), "float64", False),
+    "delays_1s_f64": ("cuba_delays", dict(N=10000, K=1000, duration_ms=1000.0, seed_value=1234), "float64", False),
 }
 
 
