@@ -337,7 +337,7 @@ def run_reference(args, rank, world):
     10,000-neuron subnetwork project, else the oracle port, each stated."""
     if rank != 0:
         return
-    r = reference_headline(args.steps, args.warmup)
+    r = reference_headline(args.steps, args.warmup) if args.reference_sample == "headline" else None
     if r is not None:
         config = workload_config(N_NEURONS, K_IN)
         dtype = "f32"
@@ -375,6 +375,9 @@ def main():
     ap.add_argument("--threads", type=int, default=0)
     ap.add_argument("--ctas", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--reference-sample", default="headline", choices=["headline", "subnetwork"],
+                    help="--impl reference: the headline network itself (default) or its 10,000-neuron "
+                         "subnetwork (a quick check)")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--chunk-steps", type=int, default=0,
                     help="clock steps per kernel launch (default: one launch per bench step)")
