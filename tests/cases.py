@@ -11,6 +11,9 @@ CASES = {
     "cobahh_f32": ("cobahh_f32", lambda s: W.build_cobahh(s, N=4000, seed=1234), 1000),
     "delays_small_f64": ("delays_f64", lambda s: W.build_delays(s, N=2000, K=100, seed=5), 3000),
     "delays_f64": ("delays_f64", lambda s: W.build_delays(s, N=10000, K=1000, seed=1234), 2000),
+    # the full simulated second of the benchmark configurations
+    "cobahh_1s_f64": ("cobahh_f64", lambda s: W.build_cobahh(s, N=4000, seed=1234), 10000),
+    "delays_1s_f64": ("delays_f64", lambda s: W.build_delays(s, N=10000, K=1000, seed=1234), 10000),
 }
 
 SYN_KEYS = (("synapses_pre", "Ce"), ("synapses_1_pre", "Ci"))

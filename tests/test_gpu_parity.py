@@ -44,7 +44,7 @@ def first_divergence(i1, t1, i2, t2):
     return None
 
 
-@pytest.mark.parametrize("case", ["cuba_small_f64", "cuba_f64", "delays_small_f64", "delays_f64"])
+@pytest.mark.parametrize("case", ["cuba_small_f64", "cuba_f64", "delays_small_f64", "delays_f64", "delays_1s_f64"])
 @pytest.mark.parametrize("shape", range(len(SHAPES)))
 def test_bit_exact_with_reference(case, shape, golden):
     spec_name, build, steps = CASES[case]
@@ -79,21 +79,93 @@ def test_split_runs_equal_one_run(golden, owner):
     np.testing.assert_array_equal(net.download(0, "neurongroup", "v"), z["v"])
 
 
-@pytest.mark.parametrize("case", ["cobahh_small_f64", "cobahh_f64", "cobahh_f32"])
-def test_cobahh_until_first_divergence(case, golden):
+COBAHH_REL = 1e-9       # float64 state against the reference while the rasters agree
+COBAHH_VT = -20e-3      # threshold (and refractory condition) v > -20 mV
+
+
+def state_rel_err(net, ref, names):
+    """Largest relative difference per state variable (conductances relative
+    to their largest value: they decay to zero between spikes)."""
+    out = {}
+    for var in names:
+        a = net.download(0, "neurongroup", var).astype(np.float64)
+        b = np.asarray(ref(var), np.float64)
+        scale = np.maximum(np.abs(b), 1e-3 * np.max(np.abs(b))) if var in ("ge", "gi") else np.abs(b)
+        out[var] = float(np.max(np.abs(a - b) / np.maximum(scale, 1e-300)))
+    return out
+
+
+def trace_divergence(spec, built, step, ishape=None):
+    """The first raster difference of a float64 COBAHH run, traced: the state
+    just before the divergent step (GPU vs the oracle, which is bit-exact
+    with the reference), and, for each neuron that spikes in one raster but
+    not the other at that step, its membrane potential on both sides after
+    the step's update, its distance to threshold and the ulps between them."""
+    o = oracle_from_built(spec, built)
+    net = W.instantiate(spec, [built], threads=256)
+    net.run(step)
+    o.run(step)
+    before = state_rel_err(net, lambda v: o.download(0, v), ("v", "m", "n", "h", "ge", "gi"))
+    net.run(1)
+    o.run(1)
+    i, ts, _ = net.spikes(0, 0)
+    oi, ots, _ = o.spikes(0)
+    a, b = set(i[ts == step].tolist()), set(oi[ots == step].tolist())
+    v, ov = net.download(0, "neurongroup", "v"), o.download(0, "v")
+    rows = []
+    for n in sorted(a ^ b):
+        rows.append(dict(neuron=n, spikes_on="gpu" if n in a else "reference", v_gpu=float(v[n]), v_ref=float(ov[n]),
+                         ref_minus_threshold=float(ov[n] - COBAHH_VT),
+                         ulps=float(abs(v[n] - ov[n]) / np.spacing(abs(ov[n])))))
+    net.close()
+    return before, rows
+
+
+@pytest.mark.parametrize("case", ["cobahh_small_f64", "cobahh_f64", "cobahh_1s_f64"])
+def test_cobahh_float64_against_reference(case, golden):
+    """float64 Hodgkin-Huxley: device exp/expm1/pow differ from glibc in the
+    last ulp, so bit-identity is not guaranteed.  Bar: the raster identical to
+    the reference's over the whole fixture (up to 1 s) with the state within
+    1e-9 relative; a divergence, if one occurs, must be a near-threshold ulp
+    difference: the states agree to 1e-9 just before it and the neuron's
+    reference potential lies within 1e-9 (relative) of the threshold."""
     spec_name, build, steps = CASES[case]
     spec = W.load_spec(spec_name)
     meta, z = golden(case)
+    b = build(spec)
+    net = W.instantiate(spec, [b], threads=256)
+    net.run(steps)
+    i, ts, _ = net.spikes(0, 0)
+    div = first_divergence(i, ts, z["spk_i"], z["spk_ts"])
+    err = state_rel_err(net, lambda v: z[v], ("v", "m", "n", "h", "ge", "gi"))
+    net.close()
+    print(f"\n{case}: {steps} steps, spikes gpu={len(i)} ref={len(z['spk_i'])}, first divergent step={div}, "
+          f"final state max rel err " + ", ".join(f"{k}={e:.2e}" for k, e in err.items()))
+    if div is None:
+        assert max(err.values()) < COBAHH_REL, err
+        return
+    before, rows = trace_divergence(spec, b, div)
+    print(f"  divergence traced at step {div}: state before it " +
+          ", ".join(f"{k}={e:.2e}" for k, e in before.items()))
+    for r in rows:
+        print("  ", r)
+    assert max(before.values()) < COBAHH_REL, before
+    assert rows and all(abs(r["ref_minus_threshold"]) <= COBAHH_REL * abs(COBAHH_VT) for r in rows), rows
+
+
+def test_cobahh_float32_until_first_divergence(golden):
+    """float32 against the float64 reference: counts within 5 %, no raster
+    divergence in the first 20 ms (the per-configuration error figures are in
+    test_gpu_fp32.py)."""
+    spec_name, build, steps = CASES["cobahh_f32"]
+    spec = W.load_spec(spec_name)
+    meta, z = golden("cobahh_f32")
     net = W.instantiate(spec, [build(spec)], threads=256)
     net.run(steps)
     i, ts, _ = net.spikes(0, 0)
     div = first_divergence(i, ts, z["spk_i"], z["spk_ts"])
-    v = net.download(0, "neurongroup", "v").astype(np.float64)
-    rel = np.abs(v - z["v"]) / np.maximum(np.abs(z["v"]), 1e-12)
-    print(f"\n{case}: spikes gpu={len(i)} ref={len(z['spk_i'])} first divergent step={div} "
-          f"v max rel err={rel.max():.3e} median={np.median(rel):.3e}")
+    print(f"\ncobahh_f32: spikes gpu={len(i)} ref={len(z['spk_i'])} first divergent step={div}")
     assert abs(len(i) - len(z["spk_i"])) <= 0.05 * len(z["spk_i"]) + 5
-    # no divergence in the first 20 ms (200 steps) of the run
     assert div is None or div >= 200
 
 
