@@ -330,7 +330,7 @@ class B200Device(CPPStandaloneDevice):
         from brian2.units import second
         if not self.enable_profiling:
             raise ValueError("No profiling info collected (did you run with 'profile=True'?)")
-        return [(name, ms * 1e-3 * second) for name, ms in self.b200_timings]
+        return sorted(((name, ms * 1e-3 * second) for name, ms in self.b200_timings), key=lambda x: -x[1])
 
     # ------------------------------------------------------------- spec
     def _make_spec(self, net, objects, clock):
@@ -400,6 +400,7 @@ class B200Device(CPPStandaloneDevice):
         statemon_pos = []  # positions of the state monitors in the schedule
         draw_sites = []  # (position in the schedule, site, the block or input whose code draws)
         b200_objects = []
+        push_names = {}  # pathway -> its push code object (for the profile)
         for pos, obj in enumerate(objects):
             if not obj.active:
                 continue
@@ -442,6 +443,7 @@ class B200Device(CPPStandaloneDevice):
                             raise NotImplementedError("b200: custom events are not supported")
                     if key in g:
                         raise NotImplementedError(f"b200: several {t} code objects for one group")
+                    b["_co"] = co.name  # (for the profile: the time of each code object)
                     g[key] = b
                 elif t == "synapses":
                     pw = obj
@@ -472,21 +474,22 @@ class B200Device(CPPStandaloneDevice):
                                          pre_ptr=gen_name(syn.variables["_synaptic_pre"]),
                                          post_ptr=gen_name(syn.variables["_synaptic_post"]),
                                          group_ptrs=gptrs, on_pre=block(frag),
-                                         _obj=pw, _src_range=srange, _tgt_range=trange, _syn=syn.name))
+                                         _obj=pw, _src_range=srange, _tgt_range=trange, _syn=syn.name,
+                                         _co=co.name))
                     if pw.prepost == "post":  # spiking side = the postsynaptic neurons
                         pathways[-1]["prepost"] = "post"
                 elif t == "synapses_push_spikes":
-                    pass
+                    push_names[id(obj)] = co.name
                 elif t == "spikegenerator":
                     group_of(obj)
                 elif t == "spikemonitor":
                     if not isinstance(obj, SpikeMonitor) or set(obj.record_variables) - {"i", "t"}:
                         raise NotImplementedError("b200: spike monitors record i and t only")
                     gi, rng = group_of(obj.source)
-                    spkmons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng))
+                    spkmons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng, _co=co.name))
                 elif t == "ratemonitor":
                     gi, rng = group_of(obj.source)
-                    ratemons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng))
+                    ratemons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng, _co=co.name))
                 elif t == "statemonitor":
                     statemon_pos.append((pos, obj.when))
                     if obj.when not in ("start", "end"):
@@ -687,6 +690,9 @@ class B200Device(CPPStandaloneDevice):
         # every array pointer used by a group block must be declared: add the
         # clock and constant names used in snippets as they are
         fdt = prefs["core.default_float_dtype"]
+        for p in pathways:
+            if p.get("events", True) and id(p["_obj"]) in push_names:
+                p["_push_co"] = push_names[id(p["_obj"])]
         spec = dict(name=f"{net.name}", float=c_data_type(fdt), consts=sorted(consts.values(), key=lambda c: c["name"]),
                     groups=groups, pathways=pathways, spike_monitors=spkmons, rate_monitors=ratemons,
                     state_monitors=statemons, clock_ptrs=clock_ptrs)
@@ -712,7 +718,7 @@ class B200Device(CPPStandaloneDevice):
             spec["inputs"] = inputs
         return spec, b200_objects
 
-    PRIVATE_KEYS = {"_obj", "_range", "_src_range", "_tgt_range", "_vars", "_syn"}
+    PRIVATE_KEYS = {"_obj", "_range", "_src_range", "_tgt_range", "_vars", "_syn", "_co", "_push_co"}
 
     @staticmethod
     def public_spec(spec):
@@ -870,7 +876,10 @@ class B200Device(CPPStandaloneDevice):
             if index is not None:
                 init[f"act{j}_index"] = index.astype(np.int64)
             actions.append(dict(after=int(after), kind=kind, obj=int(obj), var=var, indexed=index is not None))
-        write_job(directory, pub, init, [r["n_steps"] for r in self.b200_runs], dt, self.b200_run_options,
+        opts = dict(self.b200_run_options)
+        if self.enable_profiling:  # run(profile=True): the device profile, per code object
+            opts["profile"] = True
+        write_job(directory, pub, init, [r["n_steps"] for r in self.b200_runs], dt, opts,
                   actions=actions)
         self.b200_job_dir = directory
         return directory
@@ -885,7 +894,8 @@ class B200Device(CPPStandaloneDevice):
         with np.load(os.path.join(directory, "out.npz")) as z:
             out = {k: z[k] for k in z.files}
         ts0 = int(out["ts0"])
-        self.b200_timings = [("b200_step_kernel", float(out["device_ms"]))]
+        self.b200_timings = self._b200_profile(spec0, out) if "prof_names" in out else \
+            [("b200_step_kernel", float(out["device_ms"]))]
         self._last_run_time = float(out["device_ms"]) * 1e-3
         self._last_run_completed_fraction = 1.0
         for gi, g in enumerate(spec0["groups"]):
@@ -929,6 +939,55 @@ class B200Device(CPPStandaloneDevice):
         self._store(clock.variables["t"], np.array([ts_end * dt]))
         logger.debug(f"b200: {sum(r['n_steps'] for r in self.b200_runs)} steps in "
                      f"{float(out['device_ms']):.2f} ms (device)")
+
+    @staticmethod
+    def _b200_profile(spec, out):
+        """(code object name, ms) from the device profile of a job run: the
+        kernels' launch time split in proportion to the SM cycles of each
+        profile slot (b200_get_profile), the slots mapped to the code objects
+        they run -- a group's state updater, thresholder (its spike list) and
+        resetter, a pathway's push (delay ring, delivery windows and items,
+        shared equally by the pathways from one group) and its on_pre code, the
+        monitors.  Time spent waiting at the instance barriers belongs to no
+        code object and is left out, as the reference's profile covers code
+        objects only (templates/common_group.cpp:72-90)."""
+        names = [str(x) for x in out["prof_names"]]
+        cyc = dict(zip(names, (float(x) for x in out["prof_cycles"])))
+        total = sum(cyc.values())
+        if total <= 0:
+            return []
+        ms_per = float(out["kernel_ms"]) / total
+        t = {}
+
+        def add(co, c):
+            if co and c > 0:
+                t[co] = t.get(co, 0.0) + c * ms_per
+        owner = bool(int(out.get("owner", 0)))
+        groups, paths = spec["groups"], spec["pathways"]
+        deliv = [p for p in paths if p.get("events", True)]
+        if owner:  # (the owner-mode kernel's coarser phases)
+            for g in groups:
+                add((g.get("update") or {}).get("_co"), cyc.get("update_threshold_reset", 0) / len(groups))
+                add((g.get("threshold") or {}).get("_co"), cyc.get("spike_lists_monitors", 0) / len(groups))
+            for p in deliv:
+                add(p.get("_push_co"), (cyc.get("push_count", 0) + cyc.get("push_fifo", 0)) / len(deliv))
+                add(p.get("_co"), cyc.get("deliver", 0) / len(deliv))
+        else:
+            for g in groups:
+                for blk, slot in (("update", "update"), ("threshold", "threshold"), ("reset", "reset")):
+                    add((g.get(blk) or {}).get("_co"), cyc.get(f"{slot}:{g['name']}", 0))
+            for gi, g in enumerate(groups):
+                out_p = [p for p in deliv if p["src"] == gi]
+                for p in out_p:
+                    add(p.get("_push_co"), cyc.get(f"ring:{g['name']}", 0) / len(out_p))
+            for p in deliv:
+                add(p.get("_push_co"), (cyc.get("delay_windows", 0) + cyc.get("items", 0)) / len(deliv))
+                add(p.get("_co"), cyc.get(f"events:{p['name']}", 0))
+            for m in spec["spike_monitors"]:
+                add(m.get("_co"), cyc.get(f"spikemon:{m['name']}", 0))
+            for m in spec["rate_monitors"]:
+                add(m.get("_co"), cyc.get(f"ratemon:{m['name']}", 0))
+        return sorted(t.items(), key=lambda x: -x[1])
 
     def _run_on_gpu(self):
         """Export the runs as a job, run it on this host's GPU, import the

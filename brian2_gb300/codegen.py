@@ -400,7 +400,17 @@ def render_model(spec: dict) -> str:
     # device profile slots: classic kernel A, barrier A, lists, one per pathway,
     # barrier B; owner kernel update, barrier, lists, push pass 1, batch table +
     # pass 2, delivery
-    NPH = 6 + NP  # classic: A, barrier, lists, NP propagation, barrier, windows, items; owner: 6
+    # classic kernel, after those: per group update, threshold, reset; per group
+    # the copy of its spikes into the delay ring; per spike / rate monitor its
+    # recording (the code objects of profile_slots())
+    NSM, NRM = len(spkmons), len(ratemons)
+    PH_UPD = lambda gi: 6 + NP + 3 * gi
+    PH_THR = lambda gi: 7 + NP + 3 * gi
+    PH_RST = lambda gi: 8 + NP + 3 * gi
+    PH_RING = lambda gi: 6 + NP + 3 * NG + gi
+    PH_SPKMON = lambda m: 6 + NP + 4 * NG + m
+    PH_RATEMON = lambda m: 6 + NP + 4 * NG + NSM + m
+    NPH = 6 + NP + 4 * NG + NSM + NRM
     MAXV = max(len(g["vars"]) for g in groups)
 
     # ------------------------------------------------------------- model tables
@@ -773,6 +783,7 @@ def render_model(spec: dict) -> str:
         w("                  }")
         w("                }")
         w("              }")
+        w(f"              B200_PHASE({PH_UPD(gi)});  // update + threshold condition")
         w("              // order-preserving compaction: ascending = slice, warp, lane, element")
         w("              for (int k = 0; k < E; ++k) {")
         w("                int c = 0;")
@@ -802,6 +813,7 @@ def render_model(spec: dict) -> str:
         w("              }")
         w("              cnt += tot;")
         w("              __syncthreads();")
+        w(f"              B200_PHASE({PH_THR(gi)});  // spike list (threshold)")
         w("            }")
         w("            if (threadIdx.x == 0) { tcnt[u] = cnt; otc[u] = cnt; }")
         w("          }")
@@ -911,11 +923,15 @@ def render_model(spec: dict) -> str:
                 continue
             w(f"      // ---- group {gi} '{g['name']}': phase A (reset of step ts-1, monitors, update + threshold)")
             dfr = deferred_block(gi, 8, "ts - 1", owner)
+            if not owner:
+                w("      B200_PHASE(0);")
             if dfr and not SUMMED:  # (with summed variables: before the sums)
                 w("      if (ts > ts0) {")
                 w(dfr)
                 w("        __syncthreads();")
                 w("      }")
+                if not owner:
+                    w(f"      B200_PHASE({PH_RST(gi)});  // reset of the previous step")
             sop = op_block(gi, 6, "ts", "start")
             if sop and not SUMMED:  # the start-slot operations of this step
                 w(sop)
@@ -1025,6 +1041,8 @@ def render_model(spec: dict) -> str:
             w("              }")
             w("              }")
             w("            }")
+            if not owner:
+                w(f"            B200_PHASE({PH_UPD(gi)});  // update + threshold condition")
             w("            // order-preserving compaction: counts per (slice k, warp), one block scan")
             w("            for (int k = 0; k < E; ++k) {")
             w("              const unsigned m = __ballot_sync(0xffffffffu, (flags >> k) & 1u);")
@@ -1050,6 +1068,8 @@ def render_model(spec: dict) -> str:
             w("            }")
             w("            cnt += tot;")
             w("            __syncthreads();")
+            if not owner:
+                w(f"            B200_PHASE({PH_THR(gi)});  // spike list (threshold)")
             w("          }")
             w("          if (threadIdx.x == 0) tcnt[u] = cnt;" if owner else "          if (threadIdx.x == 0) { tcnt[u] = cnt; otc[u] = cnt; }")
             w("        }")
@@ -1344,6 +1364,7 @@ def render_model(spec: dict) -> str:
             w("          if (threadIdx.x == 0) pref[nt] = tot;")
             w("        }")
             w("        __syncthreads();")
+            w(f"        B200_PHASE({PH_THR(gi)});  // the step's spike list (threshold)")
             w(f"        const int u0 = s_ut[{gi}][0], u1 = s_ut[{gi}][1];")
             src_of = [pi for pi, p in enumerate(paths) if p["src"] == gi]
             if src_of:
@@ -1365,6 +1386,7 @@ def render_model(spec: dict) -> str:
             w("            if (threadIdx.x == 0) GD.ring_total[slot] = pref[nt];")
             w("          }")
             w("        }")
+            w(f"        B200_PHASE({PH_RING(gi)});  // spikes into the delay ring (push)")
             for mi, m in enumerate(spkmons):
                 if m["group"] != gi:
                     continue
@@ -1385,6 +1407,7 @@ def render_model(spec: dict) -> str:
                 w("          __syncthreads();")
                 w(f"          if (threadIdx.x == 0) s_mon_n[{mi}] += pref[SM.tile_hi] - pref[SM.tile_lo];")
                 w("        }")
+                w(f"        B200_PHASE({PH_SPKMON(mi)});  // spike monitor")
             for mi, m in enumerate(ratemons):
                 if m["group"] != gi:
                     continue
@@ -1392,6 +1415,7 @@ def render_model(spec: dict) -> str:
                 w(f"          const b200_ratemon_d& RM = I.rm[{mi}];")
                 w("          RM.cnt[ts - RM.step0] = pref[RM.tile_hi] - pref[RM.tile_lo];")
                 w("        }")
+                w(f"        B200_PHASE({PH_RATEMON(mi)});  // rate monitor")
             w("      }")
 
         if NP:
@@ -2573,6 +2597,33 @@ def render_model(spec: dict) -> str:
     w('#include "b200_host.h"')
     w("")
     return "\n".join(o) + "\n"
+
+
+def profile_slots(spec: dict, owner: bool = False) -> list[str]:
+    """Names of the device profile's slots (b200_get_profile), in order.
+    Owner-mode kernel: update (update, threshold and reset of every group),
+    barrier, spike lists, push counts, push into the event FIFOs, delivery.
+    Classic kernel: the rest of the update phase, barrier A, the rest of the
+    spike-list phase, one slot per pathway for its events, barrier B,
+    delivery windows, delivery items; per group its update (with the threshold
+    condition), its spike list (threshold), its reset; per group the copy of
+    its spikes into the delay ring; one slot per spike and per rate monitor."""
+    groups = spec["groups"]
+    paths = spec.get("pathways", [])
+    if owner:
+        names = ["update_threshold_reset", "barrier", "spike_lists_monitors", "push_count", "push_fifo", "deliver"]
+    else:
+        names = ["other", "barrier_a", "lists_other"] + [f"events:{p['name']}" for p in paths] + \
+                ["barrier_b", "delay_windows", "items"]
+    n = 6 + len(paths) + 4 * len(groups) + len(spec.get("spike_monitors", [])) + len(spec.get("rate_monitors", []))
+    if not owner:
+        for g in groups:
+            names += [f"update:{g['name']}", f"threshold:{g['name']}", f"reset:{g['name']}"]
+        names += [f"ring:{g['name']}" for g in groups]
+        names += [f"spikemon:{m['name']}" for m in spec.get("spike_monitors", [])]
+        names += [f"ratemon:{m['name']}" for m in spec.get("rate_monitors", [])]
+    names += [f"unused{k}" for k in range(len(names), n)]
+    return names
 
 
 def spec_tables(spec: dict) -> dict:

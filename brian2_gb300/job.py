@@ -69,9 +69,11 @@ def load_job(directory):
     return spec, init, job
 
 
-def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None):
+def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None, profile=None):
     """Runs a job on the GPU; returns (and writes as out.npz) its outputs.
-    `owner`: delivery mode (True, False, "auto"; None keeps the default)."""
+    `owner`: delivery mode (True, False, "auto"; None keeps the default);
+    `profile`: record the device profile (None: as the job's options say, set
+    by run(profile=True)) -- its slots' SM cycles in prof_names/prof_cycles."""
     from .runtime import Model, Network
     spec, init, job = load_job(directory)
     opts = dict(job.get("options", {}))
@@ -108,7 +110,10 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None)
     if spec.get("draws"):  # the reference's generator, where the step loop starts drawing
         net.set_rng(0, init["rng_words"], int(init["rng_position"]), init.get("rng_gauss"))
     net.reset_monitors(0)
-    total_ms, t0 = 0.0, time.time()
+    profile = bool(opts.get("profile")) if profile is None else bool(profile)
+    if profile:  # per-phase SM cycles of the step kernel (run(profile=True))
+        net.set_profiling(True)
+    total_ms, kernel_ms, t0 = 0.0, 0.0, time.time()
     def download(kind, obj, var):
         return net.download(0, obj, var) if kind == "group" else net.download_synapse_var(0, obj, var)
 
@@ -118,9 +123,14 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None)
     for k, n in enumerate(job["runs"]):
         net.run(int(n))
         total_ms += net.last_run_ms()
+        kernel_ms += net.last_kernel_ms()
         apply_actions(job, init, k, download, upload)  # the script's assignments after this run
     out = dict(device_ms=np.float64(total_ms), wall_s=np.float64(time.time() - t0), ts_end=np.int64(net.step(0)),
-               ts0=np.int64(ts0), owner=np.int64(net.owner_active()))
+               ts0=np.int64(ts0), owner=np.int64(net.owner_active()), kernel_ms=np.float64(kernel_ms))
+    if profile:
+        prof = net.profile(0)
+        out["prof_names"] = np.array(list(prof), dtype=str)
+        out["prof_cycles"] = np.array(list(prof.values()), dtype=np.float64)
     for gi, g in enumerate(spec["groups"]):
         for v in g["vars"]:
             out[f"g{gi}_{v['name']}"] = net.download(0, gi, v["name"])

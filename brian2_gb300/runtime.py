@@ -398,14 +398,9 @@ class Network:
         self._check(self.lib.b200_profile_phases(self._h, C.byref(n)))
         a = np.zeros(n.value, np.uint64)
         self._check(self.lib.b200_get_profile(self._h, int(inst), a.ctypes.data_as(C.POINTER(C.c_uint64)), n.value))
-        if self.owner_active():
-            names = ["update_threshold_reset", "barrier", "spike_lists_monitors", "push_count",
-                     "push_fifo", "deliver"]
-        else:
-            names = ["update_threshold_reset", "barrier_a", "spike_lists_monitors"] + \
-                    [f"events:{p['name']}" for p in self.model.spec.get("pathways", [])] + \
-                    ["barrier_b", "delay_windows", "items"]
-        return dict(zip(names, (int(x) for x in a)))
+        from .codegen import profile_slots
+        names = profile_slots(self.model.spec, owner=self.owner_active())
+        return {k: int(x) for k, x in zip(names, a) if not k.startswith("unused")}
 
     def set_smem_cache(self, enable=True):
         self._check(self.lib.b200_set_smem_cache(self._h, int(bool(enable))))

@@ -42,6 +42,15 @@ class B200OracleDevice(B200Device):
         out["ts0"] = np.int64(int(init["ts0"]))
         out["ts_end"] = np.int64(int(init["ts0"]) + sum(int(n) for n in job["runs"]))
         out["device_ms"] = np.float64(0.0)
+        if job.get("options", {}).get("profile"):
+            # (the oracle has no device profile: one cycle per slot, so that the
+            # plugin's mapping of the slots to code objects runs; times are 0)
+            from brian2_gb300.codegen import profile_slots
+            with open(os.path.join(directory, "spec.json")) as f:
+                names = [n for n in profile_slots(json.load(f)) if not n.startswith("unused")]
+            out["prof_names"] = np.array(names, dtype=str)
+            out["prof_cycles"] = np.ones(len(names))
+            out["kernel_ms"] = np.float64(0.0)
         np.savez(os.path.join(directory, "out.npz"), **out)
         self.b200_import_results(directory)
 
