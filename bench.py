@@ -231,7 +231,8 @@ def extra_plain(name, builder, steps=10_000):
 def extra_batched(steps=5000):
     """256 CUBA networks of uneven size (float32, 500 ms): one persistent
     graph-replayed launch (autotuned block size) against the same networks run
-    one after another on the plain path (each with its own tuned shape)."""
+    one after another on the plain path, both at one fixed shape (512 threads,
+    one CTA) and each at the autotuned shape of its size class."""
     from brian2_gb300 import autotune, batched, workloads as W
     spec = W.load_spec("cuba_f32")
     t0 = time.perf_counter()
@@ -271,6 +272,24 @@ def extra_adjoint(reps=5):
             "clock_steps": P.cfg.steps, "hidden": P.cfg.n_h, "inputs": P.cfg.n_in, "readout": P.cfg.n_o}
 
 
+def alu_roofline(entry, spec_name, fp64, peaks_cache={}):
+    """ALU roofline of a compute-bound plain run (Hodgkin-Huxley): the update's
+    arithmetic operators per neuron-step counted from its generated code, over
+    the run's device time, against the FMA throughput measured on this device
+    in the same precision (libb200_peaks)."""
+    from brian2_gb300 import roofline, workloads as W
+    ops = roofline.update_ops(W.load_spec(spec_name))
+    if fp64 not in peaks_cache:
+        peaks_cache[fp64] = roofline.fma_peak_gflops(fp64)
+    peak = peaks_cache[fp64]
+    achieved = ops["flops"] * entry["neurons"] * entry["clock_steps"] / (entry["device_ms"] * 1e-3) / 1e9
+    return {"bound": "fp64 alu" if fp64 else "fp32 alu", "achieved": achieved, "peak": peak, "unit": "GFLOP/s",
+            "frac": achieved / peak, "peak_kind": "measured (FMA loop on every SM, libb200_peaks)",
+            "flops_per_neuron_step": ops["flops"], "calls_per_neuron_step": ops["calls"],
+            "note": "counted arithmetic of the generated update; each exp/expm1/pow call is many more "
+                    "instructions, so this is a lower bound of the executed work"}
+
+
 def extras():
     from brian2_gb300 import workloads as W
     out = {}
@@ -284,6 +303,12 @@ def extras():
             out[name] = fn()
         except Exception as e:  # reported, not fatal: the headline line still prints
             out[name] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    for name, spec_name, fp64 in (("cobahh_4000_f64", "cobahh_f64", True), ("cobahh_4000_f32", "cobahh_f32", False)):
+        if "error" not in out.get(name, {"error": 1}):
+            try:
+                out[name]["roofline"] = alu_roofline(out[name], spec_name, fp64)
+            except Exception as e:
+                out[name]["roofline"] = {"error": f"{type(e).__name__}: {e}"[:300]}
     return out
 
 

@@ -6,8 +6,10 @@ own size, its own namespace constants (here ``taum`` and the excitatory weight
 kernel in queue mode: resident CTAs take instances from a work queue (largest
 first, so the long ones start early), each instance on one CTA with its state
 in shared memory, every launch replayed from a captured CUDA graph.  The plain
-path for comparison runs the same networks one after another, each with its
-own best launch shape.
+path for comparison runs the same networks one after another, twice: all at
+one fixed launch shape (512 threads, one CTA), and each at the shape the
+autotuner picks for its size class (the networks binned by size, one tuning
+per bin).
 
 Sweep of the benchmark (configuration "batched parameter sweep"): 256 CUBA
 networks, N uniform in 500..8000 (80/20 E/I), taum uniform in 10..30 ms,
@@ -67,13 +69,14 @@ class Sweep:
         return self.net.spikes(slot, 0)
 
 
-def run_sequential(spec, builts, steps, shape=None):
-    """The plain GPU path: every network alone, one after another; returns the
-    summed device time (ms) and the per-network spike counts."""
+def run_sequential(spec, builts, steps, shape=None, shapes=None):
+    """The plain GPU path: every network alone, one after another (at `shape`,
+    or at its own entry of `shapes`); returns the summed device time (ms) and
+    the per-network spike counts."""
     total_ms = 0.0
     counts = []
-    for b in builts:
-        s = shape or dict(threads=512, ctas_per_inst=1)
+    for k, b in enumerate(builts):
+        s = (shapes[k] if shapes else shape) or dict(threads=512, ctas_per_inst=1)
         net = W.instantiate(spec, [b], threads=s["threads"], ctas_per_inst=s.get("ctas_per_inst", 1))
         net.run(steps)
         total_ms += net.last_kernel_ms()
@@ -82,13 +85,43 @@ def run_sequential(spec, builts, steps, shape=None):
     return total_ms, counts
 
 
-def compare(spec, builts, steps, threads=512, seq_shape=None):
-    """Batched vs sequential: device ms of each and the speed-up."""
+def tuned_shapes(spec, builts, bins=8):
+    """The autotuner's launch shape for every network: the networks are binned
+    by size (equal counts per bin), the median network of each bin is tuned,
+    and its shape serves the bin.  Returns (shape per network, tuned shapes)."""
+    from . import autotune
+    order = sorted(range(len(builts)), key=lambda k: sum(builts[k].sizes))
+    groups = [order[i * len(order) // bins:(i + 1) * len(order) // bins] for i in range(bins)]
+    shapes = [None] * len(builts)
+    tuned = []
+    for g in groups:
+        if not g:
+            continue
+        rep_ = builts[g[len(g) // 2]]
+        sh = autotune.tune(spec, [rep_])
+        tuned.append(dict(neurons=int(sum(rep_.sizes)), threads=sh["threads"], ctas_per_inst=sh["ctas_per_inst"]))
+        for k in g:
+            shapes[k] = dict(threads=sh["threads"], ctas_per_inst=sh["ctas_per_inst"])
+    return shapes, tuned
+
+
+def compare(spec, builts, steps, threads=512, seq_shape=None, tuned=True):
+    """Batched vs sequential: device ms of each and the speed-ups, against the
+    sequential networks at one fixed shape and (tuned) each at its size
+    class's tuned shape."""
     t0 = time.perf_counter()
     sw = Sweep(spec, builts, threads=threads)
     batched_ms = sw.run(steps)
     b_counts = [len(sw.spikes(k)[0]) for k in range(len(builts))]
     sw.net.close()
     seq_ms, s_counts = run_sequential(spec, builts, steps, seq_shape)
-    return dict(batched_ms=batched_ms, sequential_ms=seq_ms, speedup=seq_ms / batched_ms,
-                same_spike_counts=b_counts == s_counts, wall_s=time.perf_counter() - t0)
+    out = dict(batched_ms=batched_ms, sequential_ms=seq_ms, speedup=seq_ms / batched_ms,
+               sequential_shape=seq_shape or dict(threads=512, ctas_per_inst=1),
+               same_spike_counts=b_counts == s_counts)
+    if tuned:
+        shapes, tuned_list = tuned_shapes(spec, builts)
+        t_ms, t_counts = run_sequential(spec, builts, steps, shapes=shapes)
+        out.update(sequential_tuned_ms=t_ms, speedup_vs_tuned=t_ms / batched_ms, tuned_shapes=tuned_list,
+                   same_spike_counts_tuned=b_counts == t_counts)
+    out["wall_s"] = time.perf_counter() - t0
+    return out

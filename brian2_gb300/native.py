@@ -126,6 +126,16 @@ def build_scale() -> str:
         [nvcc_path()] + nvcc_flags(True) + [f"-I{INCLUDE}", src, "-o", tmp], "libb200_scale"))
 
 
+def build_peaks() -> str:
+    """libb200_peaks: the measured FMA throughput (the ALU roofline's peaks)."""
+    src = os.path.join(CSRC, "b200_peaks.cu")
+    hdr = os.path.join(INCLUDE, "b200_peaks.h")
+    out = os.path.join(BUILD, f"libb200_peaks_{_sources_digest([src, hdr])}.so")
+    return _locked_build(out, lambda tmp: _run(
+        [nvcc_path(), ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", f"-I{INCLUDE}", src, "-o", tmp],
+        "libb200_peaks"))
+
+
 def build_adjoint() -> str:
     src = os.path.join(CSRC, "b200_adjoint.cu")
     out = os.path.join(BUILD, f"libb200_adjoint_{_sources_digest([src])}.so")

@@ -14,7 +14,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared(header):
     text = open(os.path.join(ROOT, "include", header)).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(b200[sa]?_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(b200[sap]?_\w+)\s*\(", text)))
 
 
 def exported(path):
@@ -56,3 +56,11 @@ def test_model_name_without_device():
     buf = ctypes.create_string_buffer(64)
     assert lib.b200_model_name(buf, 64) == 0
     assert buf.value == b"cuba_f64"
+
+
+def test_peaks_library_exports_abi():
+    lib = exported(native.build_peaks())
+    names = declared("b200_peaks.h")
+    assert names == ["b200p_fma_peak", "b200p_last_error"]
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
