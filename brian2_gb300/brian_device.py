@@ -982,7 +982,11 @@ class B200Device(CPPStandaloneDevice):
                     add(p.get("_push_co"), cyc.get(f"ring:{g['name']}", 0) / len(out_p))
             for p in deliv:
                 add(p.get("_push_co"), (cyc.get("delay_windows", 0) + cyc.get("items", 0)) / len(deliv))
-                add(p.get("_co"), cyc.get(f"events:{p['name']}", 0))
+            from .codegen import delivery_passes
+            for _, pis, _ in delivery_passes(paths):  # a shared pass: its events split equally
+                c = cyc.get(f"events:{paths[pis[0]]['name']}", 0)
+                for q in pis:
+                    add(paths[q].get("_co"), c / len(pis))
             for m in spec["spike_monitors"]:
                 add(m.get("_co"), cyc.get(f"spikemon:{m['name']}", 0))
             for m in spec["rate_monitors"]:

@@ -1441,19 +1441,7 @@ def render_model(spec: dict) -> str:
     # consecutive pathways from the same source whose on_pre code touches
     # disjoint neuron variables: running them interleaved cannot change what
     # any of them reads, so the reference's pathway-by-pathway order is kept
-    merged = []
-    for pi, p in enumerate(paths):
-        if not p.get("events", True):
-            continue  # the synapses of a Synapses object without a delivering pathway
-        # neuron variables and synaptic variables (shared by the pathways of one
-        # Synapses object): pathways touching the same ones are not interleaved
-        touched = set(p.get("group_ptrs", {})) | {v["ptr"] for v in p.get("vars", [])}
-        last = merged[-1] if merged else None
-        if last and last[0] == p["src"] and not (last[2] & touched):
-            last[1].append(pi)
-            last[2].update(touched)
-        else:
-            merged.append((p["src"], [pi], set(touched)))
+    merged = delivery_passes(paths)
     seen_svars = set()
     for sg, pis, _ in merged:
         L = len(pis)
@@ -2597,6 +2585,28 @@ def render_model(spec: dict) -> str:
     w('#include "b200_host.h"')
     w("")
     return "\n".join(o) + "\n"
+
+
+def delivery_passes(paths) -> list:
+    """The classic kernel's delivery passes: (source group, [pathway indices],
+    touched pointers).  Consecutive pathways from one source whose on_pre code
+    touches disjoint neuron and synaptic variables share a pass (running them
+    interleaved cannot change what any of them reads); a pass's events are
+    profiled in the slot of its first pathway."""
+    merged = []
+    for pi, p in enumerate(paths):
+        if not p.get("events", True):
+            continue  # the synapses of a Synapses object without a delivering pathway
+        # neuron variables and synaptic variables (shared by the pathways of one
+        # Synapses object): pathways touching the same ones are not interleaved
+        touched = set(p.get("group_ptrs", {})) | {v["ptr"] for v in p.get("vars", [])}
+        last = merged[-1] if merged else None
+        if last and last[0] == p["src"] and not (last[2] & touched):
+            last[1].append(pi)
+            last[2].update(touched)
+        else:
+            merged.append((p["src"], [pi], set(touched)))
+    return merged
 
 
 def profile_slots(spec: dict, owner: bool = False) -> list[str]:

@@ -31,13 +31,17 @@ def test_plugin_job_reproduces_reference(case, ctas, golden):
 @pytest.mark.parametrize("case", ["delays_small_f64", "cuba_small_f64"])
 def test_profiled_job_reports_every_code_object(case, golden):
     """run(profile=True) through the plugin: the device profile has cycles in
-    the slots of the group's update, threshold and reset, of every pathway's
-    events and of the monitors; profiling does not change the results."""
+    the slots of the group's update, threshold and reset, of every delivery
+    pass's events and of the monitors; profiling does not change the results."""
+    from brian2_gb300.codegen import delivery_passes
+    from brian2_gb300.job import load_job
     meta, z = golden(case)
     out = run_job(os.path.join(HERE, "golden", "jobs", case), write=False, profile=True)
     np.testing.assert_array_equal(out["sm0_i"], z["spk_i"])
     prof = dict(zip((str(x) for x in out["prof_names"]), out["prof_cycles"]))
-    for slot in ("update:neurongroup", "threshold:neurongroup", "reset:neurongroup", "ring:neurongroup",
-                 "events:synapses_pre", "events:synapses_1_pre", "spikemon:spikemonitor", "ratemon:ratemonitor"):
+    spec, _, _ = load_job(os.path.join(HERE, "golden", "jobs", case))
+    passes = [f"events:{spec['pathways'][pis[0]]['name']}" for _, pis, _ in delivery_passes(spec["pathways"])]
+    for slot in ["update:neurongroup", "threshold:neurongroup", "reset:neurongroup", "ring:neurongroup",
+                 "spikemon:spikemonitor", "ratemon:ratemonitor"] + passes:
         assert prof.get(slot, 0) > 0, (slot, prof)
     assert float(out["kernel_ms"]) > 0
