@@ -31,7 +31,7 @@ def lib():
     global _lib
     if _lib is None:
         L = native.load(native.build_adjoint())
-        for name in ("b200a_forward_f32", "b200a_forward_f64"):
+        for name in ("b200a_forward_f32", "b200a_forward_f64", "b200a_forward_grid_f32", "b200a_forward_grid_f64"):
             getattr(L, name).argtypes = [C.c_void_p] * 11 + [C.c_void_p]
             getattr(L, name).restype = C.c_int
         for name in ("b200a_backward_f32", "b200a_backward_f64"):
@@ -114,12 +114,15 @@ def _suffix(dtype):
     return "f64" if dtype == torch.float64 else "f32"
 
 
-def forward_trace(ctx: _Ctx, W, W_out, taum, ckpt=None, spike_count=None, io=None):
+def forward_trace(ctx: _Ctx, W, W_out, taum, ckpt=None, spike_count=None, io=None, grid=False):
+    """Readout trace vo[steps, n_o] (the state after each step).  grid: the
+    readout receives hidden spikes at the end of their step (the reference's
+    on_pre timing) instead of at the interpolated crossing time."""
     import torch
     cfg = ctx.cfg
     vo = torch.empty((cfg.steps, cfg.n_o), dtype=ctx.dtype, device="cuda")
     fp = cfg.fparams(taum)
-    f = getattr(lib(), "b200a_forward_" + _suffix(ctx.dtype))
+    f = getattr(lib(), ("b200a_forward_grid_" if grid else "b200a_forward_") + _suffix(ctx.dtype))
     r = f(ctx.ip.numpy().ctypes.data, fp.ctypes.data, _ptr(W), _ptr(W_out), _ptr(ctx.in_ptr), _ptr(ctx.in_ids),
           _ptr(ctx.state0), _ptr(vo), _ptr(spike_count), _ptr(ckpt), _ptr(io), _stream())
     if r:

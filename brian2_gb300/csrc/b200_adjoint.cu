@@ -33,6 +33,10 @@ template <typename T>
 struct AdjP {
   int steps, K, n_in, n_h, n_o;
   T dt, El, Vt, Vr, taus, taum;
+  // 1: the readout receives a hidden spike at the end of its step (the
+  // reference's on_pre timing, templates/synapses.cpp) instead of at the
+  // interpolated crossing time -- the forward pass only
+  int grid;
 };
 
 template <typename T> __device__ __forceinline__ T ex(T x);
@@ -83,7 +87,7 @@ __device__ void step_forward(const AdjP<T>& P, const Coef<T>& C, int n, T* s_v, 
         const int k = atomicAdd(s_nspk, 1);
         if (k < MAXSPK) {
           s_spk[k] = h;
-          s_r[k] = (T)1 - (P.Vt - v) / (vm - v);
+          s_r[k] = P.grid ? (T)0 : (T)1 - (P.Vt - v) / (vm - v);  // (r = 0: f = 0, e = 1)
         }
       }
       s_v[h] = P.Vr;
@@ -440,6 +444,27 @@ int b200a_forward_f64(const int32_t* ip, const double* fp, const double* W, cons
 // segbuf: K*(2 n_h + 2 n_o) entries; dW (n_in*n_h), dWout (n_h*n_o) are
 // accumulated into (zero them first); dtaum: one entry, written; vo_trace and
 // io_trace are the forward pass's traces, state0 its initial state.
+// The forward pass with the readout driven at the step grid (each hidden spike
+// adds W_out to Io at the end of its step, the reference's on_pre timing):
+// the network as a Brian script with on_pre delivery computes it, so it pins
+// the forward to the reference.  The loss is then piecewise constant in the
+// spike times (no gradient through them), which is why the adjoint uses the
+// interpolated delivery.
+int b200a_forward_grid_f32(const int32_t* ip, const double* fp, const float* W, const float* Wout,
+                           const int32_t* in_ptr, const int32_t* in_ids, const float* state0, float* vo_trace,
+                           int32_t* spike_count, float* ckpt, float* io_trace, void* stream) {
+  AdjP<float> P{ip[0], ip[1], ip[2], ip[3], ip[4], (float)fp[0], (float)fp[1], (float)fp[2], (float)fp[3],
+                (float)fp[4], (float)fp[5], 1};
+  return run_forward(P, W, Wout, in_ptr, in_ids, state0, vo_trace, spike_count, ckpt, io_trace,
+                     (cudaStream_t)stream);
+}
+int b200a_forward_grid_f64(const int32_t* ip, const double* fp, const double* W, const double* Wout,
+                           const int32_t* in_ptr, const int32_t* in_ids, const double* state0, double* vo_trace,
+                           int32_t* spike_count, double* ckpt, double* io_trace, void* stream) {
+  AdjP<double> P{ip[0], ip[1], ip[2], ip[3], ip[4], fp[0], fp[1], fp[2], fp[3], fp[4], fp[5], 1};
+  return run_forward(P, W, Wout, in_ptr, in_ids, state0, vo_trace, spike_count, ckpt, io_trace,
+                     (cudaStream_t)stream);
+}
 int b200a_backward_f32(const int32_t* ip, const double* fp, const float* W, const float* Wout, const int32_t* in_ptr,
                        const int32_t* in_ids, const float* ckpt, const float* grad_vo, float* segbuf, float* dW,
                        float* dWout, float* dtaum, const float* vo_trace, const float* io_trace, const float* state0,

@@ -41,6 +41,20 @@ int b200a_forward_f64(const int32_t* ip, const double* fp, const double* W, cons
                       const int32_t* in_ptr, const int32_t* in_ids, const double* state0, double* vo_trace,
                       int32_t* spike_count, double* ckpt, double* io_trace, void* stream);
 
+/* The forward pass with the readout driven at the step grid: each hidden
+ * spike adds W_out to Io at the end of its step, as the reference's on_pre
+ * delivery does (templates/synapses.cpp:20-49; the same network written as a
+ * Brian script with a SpikeGeneratorGroup input computes it).  It pins the
+ * forward pass to the reference; the loss is then piecewise constant in the
+ * spike times, so the adjoint pass differentiates the interpolated delivery
+ * above instead.  Same arguments as b200a_forward_*. */
+int b200a_forward_grid_f32(const int32_t* ip, const double* fp, const float* W, const float* W_out,
+                           const int32_t* in_ptr, const int32_t* in_ids, const float* state0, float* vo_trace,
+                           int32_t* spike_count, float* ckpt, float* io_trace, void* stream);
+int b200a_forward_grid_f64(const int32_t* ip, const double* fp, const double* W, const double* W_out,
+                           const int32_t* in_ptr, const int32_t* in_ids, const double* state0, double* vo_trace,
+                           int32_t* spike_count, double* ckpt, double* io_trace, void* stream);
+
 /* Adjoint pass: grad_vo[steps][n_o] = dL/dvo_trace.  Accumulates dL/dW into dW
  * and dL/dW_out into dW_out (zero them first); writes dL/dtaum to *dtaum.
  * segbuf: K * (2 n_h + 2 n_o) entries of scratch (the recomputed segment). */

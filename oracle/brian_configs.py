@@ -585,3 +585,48 @@ SCENARIOS = {
     "end_monitor": end_monitor,
     "host_sets": host_sets,
 }
+
+
+# ---------------------------------------------------------------------------
+# The adjoint benchmark's network ("adjoint gradients" configuration) as a
+# Brian script: the forward pass the reference computes for it (on_pre
+# delivery at the step grid).  Inputs, weights, initial state come from
+# brian2_gb300.adjoint.make_problem (seeded numpy).
+# ---------------------------------------------------------------------------
+def adjoint_network(seed=42, steps=5000, n_in=200, n_h=1000, n_o=10):
+    """200 input trains (SpikeGeneratorGroup) -> 1000 exact-linear LIF neurons
+    with an exponential current (taum 20 ms, taus 5 ms, CUBA threshold and
+    reset) through the dense W, -> 10 non-spiking readout neurons of the same
+    dynamics through the dense W_out.  Records the hidden spikes and the
+    readout potentials at the end of every step (after the deliveries)."""
+    import numpy as np
+    from brian2 import (NeuronGroup, Synapses, SpikeGeneratorGroup, SpikeMonitor, StateMonitor,
+                        volt, second, run)
+    from brian2_gb300.adjoint import AdjointConfig, make_problem
+    cfg = AdjointConfig(n_in=n_in, n_h=n_h, n_o=n_o, steps=steps, seed=seed)
+    prob = make_problem(cfg)
+    ptr, ids = prob["in_ptr"], prob["in_ids"]
+    in_steps = np.repeat(np.arange(cfg.steps), np.diff(ptr))
+    ns = dict(El=cfg.El * volt, Vt=cfg.Vt * volt, Vr=cfg.Vr * volt, taum=cfg.taum * second, taus=cfg.taus * second)
+    eqs = '''
+    dv/dt = (El - v + I)/taum : volt
+    dI/dt = -I/taus : volt
+    '''
+    inp = SpikeGeneratorGroup(cfg.n_in, ids, in_steps * cfg.dt * second)
+    H = NeuronGroup(cfg.n_h, eqs, threshold='v > Vt', reset='v = Vr', method='exact', namespace=ns)
+    O = NeuronGroup(cfg.n_o, eqs, method='exact', namespace=ns)
+    s0 = prob["state0"]
+    H.v = s0[:cfg.n_h] * volt
+    O.v = s0[2 * cfg.n_h:2 * cfg.n_h + cfg.n_o] * volt
+    Sin = Synapses(inp, H, 'w : volt', on_pre='I_post += w')
+    ii, jj = np.meshgrid(np.arange(cfg.n_in), np.arange(cfg.n_h), indexing="ij")
+    Sin.connect(i=ii.ravel(), j=jj.ravel())
+    Sin.w = prob["W"].ravel() * volt
+    Sout = Synapses(H, O, 'w : volt', on_pre='I_post += w')
+    hh, oo = np.meshgrid(np.arange(cfg.n_h), np.arange(cfg.n_o), indexing="ij")
+    Sout.connect(i=hh.ravel(), j=oo.ravel())
+    Sout.w = prob["W_out"].ravel() * volt
+    spikes = SpikeMonitor(H)
+    readout = StateMonitor(O, 'v', record=True, when='end')
+    run(cfg.steps * cfg.dt * second)
+    return dict(P=H, O=O, Sin=Sin, Sout=Sout, spikes=spikes, readout=readout)

@@ -46,7 +46,7 @@ def test_scale_library_exports_abi():
 def test_adjoint_library_exports_abi():
     lib = exported(native.build_adjoint())
     names = declared("b200_adjoint.h")
-    assert len(names) == 5
+    assert len(names) == 7
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
 
