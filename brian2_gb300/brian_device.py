@@ -186,6 +186,7 @@ class B200Device(CPPStandaloneDevice):
         self.b200_last_network = None
         self.b200_timings = []
         self.b200_job_dir = None
+        self.b200_report_kind = None   # the runs' progress report (one kind per device, as the reference)
 
     def reinit(self):
         opts = self.b200_run_options
@@ -194,6 +195,7 @@ class B200Device(CPPStandaloneDevice):
         self.b200_run_options = opts
         self.b200_last_network = None
         self.b200_timings = []
+        self.b200_report_kind = None
 
     def activate(self, build_on_run=True, **kwargs):
         for k in ("threads", "ctas_per_inst"):
@@ -264,6 +266,19 @@ class B200Device(CPPStandaloneDevice):
         from brian2.core.namespace import get_local_namespace
         if duration < 0:
             raise ValueError(f"Function 'run' expected a non-negative duration but got '{duration}'")
+        # progress report (device.py:1842-1917): the standard reports are printed
+        # by the job runner at the start and end of the run on the device
+        if report is not None:
+            if not isinstance(report, str):
+                raise TypeError("report argument has to be either 'text', 'stdout', 'stderr', or the code for a "
+                                "report function")
+            if report not in ("text", "stdout", "stderr"):
+                raise NotImplementedError("b200: report functions given as C++ code are not supported")
+            kind = "stderr" if report == "stderr" else "stdout"
+            if getattr(self, "b200_report_kind", None) not in (None, kind):
+                raise NotImplementedError("The b200 device does not support multiple report functions, each run "
+                                          "has to use the same (or none).")
+            self.b200_report_kind = kind
         self.networks.add(net)
         self.enable_profiling = bool(profile)
         all_objects = net.sorted_objects
@@ -310,6 +325,8 @@ class B200Device(CPPStandaloneDevice):
                                     '_b200_rng << " " << _b200_kept << " " << std::hexfloat << _b200_g; }'))
         self.b200_runs.append(dict(net=net, n_steps=n_steps, spec=spec, objects=objects, clock=clock,
                                    dt=float(clock.dt_),
+                                   report=None if report is None else ("stderr" if report == "stderr" else "stdout"),
+                                   report_period=float(report_period) if report_period is not None else 10.0,
                                    queue_len=len(self.main_queue)))
         self.main_queue.append(("insert_code", f"// b200 network run {len(self.b200_runs) - 1} ({n_steps} steps)"))
         net.t_ = float(t_end)
@@ -879,6 +896,9 @@ class B200Device(CPPStandaloneDevice):
         opts = dict(self.b200_run_options)
         if self.enable_profiling:  # run(profile=True): the device profile, per code object
             opts["profile"] = True
+        if any(r.get("report") for r in self.b200_runs):  # run(report=...): printed by the job runner
+            opts["reports"] = [r.get("report") for r in self.b200_runs]
+            opts["report_periods"] = [r.get("report_period", 10.0) for r in self.b200_runs]
         write_job(directory, pub, init, [r["n_steps"] for r in self.b200_runs], dt, opts,
                   actions=actions)
         self.b200_job_dir = directory

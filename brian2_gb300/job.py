@@ -59,6 +59,30 @@ def apply_actions(job, init, after, download, upload):
         upload(a["kind"], a["obj"], a["var"], cur)
 
 
+def _format_time(seconds):
+    """The reference's progress-report time format (d h m s, or "< 1s")."""
+    remaining, parts = float(seconds), []
+    for div, letter in ((86400, "d"), (3600, "h"), (60, "m"), (1, "s")):
+        k = int(remaining / div)
+        remaining -= k * div
+        if k > 0 or parts:
+            parts.append(f"{k}{letter}")
+    return " ".join(parts) if parts else "< 1s"
+
+
+def _report(stream, elapsed, completed, start, duration):
+    """A progress line as the reference's standard report function prints it
+    (brian2/devices/cpp_standalone/device.py:1843-1887), to stdout or stderr."""
+    out = sys.stderr if stream == "stderr" else sys.stdout
+    if completed == 0.0:
+        print(f"Starting simulation at t={start:g} s for duration {duration:g} s", file=out, flush=True)
+        return
+    line = f"{completed * duration:g} s ({int(completed * 100.0)}%) simulated in {_format_time(elapsed)}"
+    if completed < 1.0:
+        line += f", estimated {_format_time(int((1 - completed) / completed * elapsed + 0.5))} remaining."
+    print(line, file=out, flush=True)
+
+
 def load_job(directory):
     with open(os.path.join(directory, "spec.json")) as f:
         spec = json.load(f)
@@ -120,10 +144,25 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None,
     def upload(kind, obj, var, arr):
         (net.upload if kind == "group" else net.upload_synapse_var)(0, obj, var, arr)
 
+    reports = opts.get("reports") or [None] * len(job["runs"])
+    periods = opts.get("report_periods") or [10.0] * len(job["runs"])
     for k, n in enumerate(job["runs"]):
-        net.run(int(n))
-        total_ms += net.last_run_ms()
-        kernel_ms += net.last_kernel_ms()
+        if reports[k]:
+            _report(reports[k], 0.0, 0.0, net.step(0) * dt, int(n) * dt)
+        t_run = time.time()
+        done = 0
+        while done < int(n):  # (a run reporting its progress: pieces of about one report period)
+            piece = int(n) - done
+            if reports[k]:
+                piece = min(piece, 1000)
+            net.run(piece)
+            done += piece
+            total_ms += net.last_run_ms()
+            kernel_ms += net.last_kernel_ms()
+            if reports[k] and done < int(n) and time.time() - t_run > periods[k]:
+                _report(reports[k], time.time() - t_run, done / int(n), (net.step(0) - done) * dt, int(n) * dt)
+        if reports[k]:
+            _report(reports[k], time.time() - t_run, 1.0, (net.step(0) - int(n)) * dt, int(n) * dt)
         apply_actions(job, init, k, download, upload)  # the script's assignments after this run
     out = dict(device_ms=np.float64(total_ms), wall_s=np.float64(time.time() - t0), ts_end=np.int64(net.step(0)),
                ts0=np.int64(ts0), owner=np.int64(net.owner_active()), kernel_ms=np.float64(kernel_ms))

@@ -105,3 +105,17 @@ def test_scenario_jobs_describe_their_features(name):
     if name == "presynaptic_read":
         assert any("_presynaptic_idx" in (p["on_pre"].get("vector_device") or p["on_pre"]["vector"])
                    for p in spec["pathways"])
+
+
+def test_progress_report_lines(capsys):
+    """run(report='text'/'stderr'): the job runner prints the reference's
+    standard report lines (device.py:1843-1887) to the chosen stream."""
+    from brian2_gb300.job import _format_time, _report
+    assert _format_time(0.2) == "< 1s" and _format_time(61) == "1m 1s" and _format_time(3600) == "1h 0m 0s"
+    _report("stdout", 0.0, 0.0, 0.0, 0.5)
+    _report("stdout", 2.0, 0.5, 0.0, 0.5)
+    _report("stderr", 4.0, 1.0, 0.0, 0.5)
+    out, err = capsys.readouterr()
+    assert out.splitlines() == ["Starting simulation at t=0 s for duration 0.5 s",
+                                "0.25 s (50%) simulated in 2s, estimated 2s remaining."]
+    assert err.splitlines() == ["0.5 s (100%) simulated in 4s"]
