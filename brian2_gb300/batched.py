@@ -125,3 +125,48 @@ def compare(spec, builts, steps, threads=512, seq_shape=None, tuned=True):
                    same_spike_counts_tuned=b_counts == t_counts)
     out["wall_s"] = time.perf_counter() - t0
     return out
+
+
+# ---------------------------------------------------------------------------
+# A sweep over several GPUs: the instances are independent, so they are split
+# over the ranks (one process per GPU) with no exchange during the run; only
+# the per-instance results are gathered at the end.
+# ---------------------------------------------------------------------------
+def shard(sizes, world):
+    """Instance indices per rank: largest first, each to the rank with the
+    fewest neurons so far (a greedy longest-processing-time split, so every
+    rank's queue-mode launch has about the same work)."""
+    load = [0] * world
+    out = [[] for _ in range(world)]
+    for k in sorted(range(len(sizes)), key=lambda k: (-sizes[k], k)):
+        r = min(range(world), key=lambda r: (load[r], r))
+        out[r].append(k)
+        load[r] += sizes[k]
+    return [sorted(x) for x in out]
+
+
+def _device_runner(spec, builts, steps, threads=512):
+    """This rank's instances in one queue-mode launch on its GPU."""
+    sw = Sweep(spec, builts, threads=threads)
+    ms = sw.run(steps)
+    res = [sw.spikes(k) for k in range(len(builts))]
+    sw.net.close()
+    return ms, [(np.asarray(i), np.asarray(t)) for i, t, _ in res]
+
+
+def run_sharded(spec, params, steps, rank=0, world=1, dist=None, runner=None, threads=512):
+    """Runs this rank's share of a sweep and gathers every instance's raster
+    on every rank (torch.distributed object all-gather; none with one rank).
+    Returns (device ms of this rank, {sweep index: (i, ts)})."""
+    mine = shard([p["N"] for p in params], world)[rank]
+    builts = build_sweep(spec, [params[k] for k in mine])
+    ms, res = (runner or _device_runner)(spec, builts, steps, threads) if builts else (0.0, [])
+    local = {k: r for k, r in zip(mine, res)}
+    if dist is None or world == 1:
+        return ms, local
+    gathered = [None] * world
+    dist.all_gather_object(gathered, local)
+    allres = {}
+    for part in gathered:
+        allres.update(part)
+    return ms, allres
