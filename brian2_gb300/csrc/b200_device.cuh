@@ -750,6 +750,13 @@ __host__ __device__ __forceinline__ auto _brian_pow(T1 a, T2 b) -> decltype(pow(
   using std::pow;
   return pow(a, b);
 }
+#ifdef __CUDA_ARCH__
+// a float base with an integer exponent (Brian writes n**4 as _brian_pow(n, 4)):
+// std::pow would promote it to double; on the device a float model stays in
+// float (the FP64 pipe runs at a small fraction of the FP32 rate)
+__device__ __forceinline__ float _brian_pow(float a, int b) { return powf(a, (float)b); }
+__device__ __forceinline__ float _brian_pow(float a, long long b) { return powf(a, (float)b); }
+#endif
 template <typename T1, typename T2>
 __host__ __device__ __forceinline__ double _brian_floordiv(T1 x, T2 y) { return floor(1.0 * x / y); }
 __host__ __device__ __forceinline__ int32_t _brian_floordiv(int32_t a, int32_t b) {
