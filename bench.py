@@ -18,7 +18,9 @@ project was not generated, the oracle instead).  On one GPU the line also
 carries the other workloads, each measured in this run: CUBA 4000 (float64),
 COBAHH 4000 (float64 and float32), the 256-network batched sweep against the
 same networks run one after another, and the adjoint's forward+adjoint /
-forward cost ratio.
+forward cost ratio; beside each, the reference's own generated project of the
+same network timed on the host cores at 1 thread and at all cores
+(``cpu_reference``).
 
 --impl reference runs the reference's own step loop on the headline network
 itself (1e6 neurons, 1e9 synapses, float32, its generated cpp_standalone
@@ -315,6 +317,65 @@ def extras():
     return out
 
 
+# other workloads -> the reference's generated project of the same network
+REFERENCE_OF = {"cuba_4000_f64": "cuba", "cobahh_4000_f64": "cobahh", "cobahh_4000_f32": "cobahh32",
+                "batched_sweep_256_f32": "sweep8", "adjoint_f32": "adjoint"}
+
+
+def reference_of_others(other):
+    """The reference's CPU step loop beside each other workload: its generated
+    cpp_standalone project of the same network (same script, seed and
+    precision), at 1 OpenMP thread and at the largest generated count the host
+    has cores for, timed by its own step-loop clock.  The sweep is sampled: 8
+    of the 256 networks, the middle one of each size stratum of 32, run one
+    after another; the 256-network time is the stratified estimate (32 x the
+    sample).  Adds ``cpu_reference`` to each entry of ``other`` (in place)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_standalone
+    for name, wl in REFERENCE_OF.items():
+        if name not in other or "error" in other[name] or not ref_standalone.available(wl):
+            continue
+        entry = {"kind": "reference", "host_cpus": os.cpu_count()}
+        try:
+            for T in sorted({1, ref_standalone.all_threads(wl)}):
+                if T not in ref_standalone.variants(wl):
+                    continue
+                ref_standalone.build(T, workload=wl)
+                r = ref_standalone.run(T, workload=wl)
+                d = {"threads": T, "step_loop_s": r["run_time_s"], "spikes": r["spikes"], "events": r["events"]}
+                if r.get("networks"):
+                    per = len(r["networks"])
+                    scale = r["sweep_networks"] / per
+                    d.update(sample_networks=[n["N"] for n in r["networks"]],
+                             projected_all_s=r["run_time_s"] * scale,
+                             events_per_s=r["events"] / r["run_time_s"])
+                elif wl == "adjoint":  # forward time is the figure; its event count would miss the inputs'
+                    del d["events"]
+                    d.update(sim_s_per_wall_s=r["sim_s"] / r["run_time_s"])
+                else:
+                    d.update(sim_s_per_wall_s=r["sim_s"] / r["run_time_s"], events_per_s=r["events"] / r["run_time_s"])
+                entry[f"threads_{T}"] = d
+            runs = [v for k, v in entry.items() if k.startswith("threads_")]
+            if not runs:
+                continue
+            best = min(runs, key=lambda v: v.get("projected_all_s", v["step_loop_s"]))
+            o = other[name]
+            if name == "batched_sweep_256_f32":
+                entry["sample"] = ("8 of the 256 networks (sizes sorted, the middle one of each stratum of 32), "
+                                   "500 ms each, run one after another; projected_all_s = 32 x the sample")
+                entry["speedup_batched_vs_best"] = best["projected_all_s"] / (o["batched_ms"] * 1e-3)
+            elif name == "adjoint_f32":
+                entry["sample"] = "forward pass only (the reference has no gradient code), 5000 steps"
+                entry["speedup_forward_vs_best"] = best["step_loop_s"] / (o["forward_ms"] * 1e-3)
+            else:
+                entry["sample"] = "the whole run: 1 s simulated, 10000 clock steps"
+                entry["speedup_vs_best"] = best["step_loop_s"] / (o["device_ms"] * 1e-3)
+            o["cpu_reference"] = entry
+        except Exception as e:  # reported, not fatal
+            other[name]["cpu_reference"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    return other
+
+
 def workload_config(N, K):
     """The workload both arms of the benchmark run (the reference arm prints
     the same dictionary)."""
@@ -528,6 +589,8 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline()
+        if other:
+            reference_of_others(other)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

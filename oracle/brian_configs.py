@@ -134,6 +134,45 @@ def cuba_delays(N=10000, K=1000, duration_ms=1000.0, seed_value=1234, ne_frac=0.
     return dict(P=P, Ce=Ce, Ci=Ci, spikes=s_mon, rate=r_mon)
 
 
+def cuba_sweep(params, duration_ms=500.0, ne_frac=0.8, report=None):
+    """Networks of a parameter sweep, one after another in one script: for each
+    parameter set (``N``, ``seed``, ``taum`` in s, excitatory weight scale
+    ``wscale``) the construction of ``cuba`` with that size, seed, membrane time
+    constant and excitatory weight, built and run by its own ``Network``.  In
+    the standalone device every ``seed``, construction and run is executed by
+    ``main`` in script order, so each network is what ``cuba`` alone builds.
+    ``report`` (standalone: C++ code of the report function) goes to every run;
+    its end-of-run call gives each network's own run time
+    (``templates/network.cpp:114-121``)."""
+    from brian2 import NeuronGroup, Synapses, SpikeMonitor, Network, ms, mV, second, seed
+    out = []
+    for p in params:
+        seed(p["seed"])
+        Vt = -50 * mV; Vr = -60 * mV; El = -49 * mV
+        eqs = '''
+        dv/dt  = (ge+gi-(v-El))/taum : volt
+        dge/dt = -ge/taue : volt
+        dgi/dt = -gi/taui : volt
+        '''
+        N = p["N"]
+        Ne = int(N * ne_frac)
+        P = NeuronGroup(N, eqs, threshold='v>Vt', reset='v = Vr', method='exact',
+                        namespace=dict(taum=p["taum"] * second, taue=5 * ms, taui=10 * ms, Vt=Vt, Vr=Vr, El=El))
+        P.v = 'Vr + rand() * (Vt - Vr)'
+        Ce = Synapses(P, P, on_pre='ge += we', namespace=dict(we=(60 * 0.27 / 10) * mV * p["wscale"]))
+        Ci = Synapses(P, P, on_pre='gi += wi', namespace=dict(wi=(-20 * 4.5 / 10) * mV))
+        Ce.connect(f'i<{Ne} and i!=j', p=0.02)
+        Ci.connect(f'i>={Ne} and i!=j', p=0.02)
+        s_mon = SpikeMonitor(P)
+        net = Network(P, Ce, Ci, s_mon)
+        if report is None:
+            net.run(duration_ms * ms)
+        else:
+            net.run(duration_ms * ms, report=report, report_period=1e6 * second)
+        out.append(dict(P=P, Ce=Ce, Ci=Ci, spikes=s_mon))
+    return out
+
+
 # ---------------------------------------------------------------------------
 # Scenarios beyond the benchmark networks (parity of less common step-loop
 # features: timed refractoriness, heterogeneous weights and delays, monitors

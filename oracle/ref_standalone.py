@@ -81,8 +81,38 @@ def binary_path(threads: int, workload: str = "delays") -> str:
     return os.path.join(project(threads, workload), f"main_{platform.machine()}")
 
 
-def build_all() -> list[str]:
-    return [build(t, workload=w) for w, t in workloads()]
+def build_all(jobs: int = 0) -> list[str]:
+    """Compiles every generated project present here, all source files of all
+    projects in one pool of g++ processes; returns the binaries' paths."""
+    todo = [(w, t) for w, t in workloads() if not os.path.exists(binary_path(t, w))]
+    units = [(w, t, src) for w, t in todo for src in manifest(t, w)["sources"]]
+    with ThreadPoolExecutor(max_workers=jobs or min(16, os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(lambda u: _compile(project(u[1], u[0]), u[2]), units))
+    for w, t in todo:
+        _link(binary_path(t, w), [o for (w2, t2, _), o in zip(units, objs) if (w2, t2) == (w, t)])
+    return [binary_path(t, w) for w, t in workloads()]
+
+
+def _compile(PROJECT, src):
+    cxx = shutil.which("g++") or "g++"
+    objdir = os.path.join(PROJECT, f"_obj_{platform.machine()}")
+    os.makedirs(objdir, exist_ok=True)
+    obj = os.path.join(objdir, src.replace("/", "__") + ".o")
+    lang = ["-x", "c++"] if src.endswith(".c") else []
+    r = subprocess.run([cxx] + FLAGS + ["-I", PROJECT, "-c"] + lang + [os.path.join(PROJECT, src), "-o", obj],
+                       capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError(f"compiling {src} failed:\n{r.stderr[-2000:]}")
+    return obj
+
+
+def _link(out, objs):
+    cxx = shutil.which("g++") or "g++"
+    tmp = out + f".tmp{os.getpid()}"
+    r = subprocess.run([cxx] + objs + ["-fopenmp", "-o", tmp], capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError(f"linking the reference project failed:\n{r.stderr[-2000:]}")
+    os.replace(tmp, out)
 
 
 def build(threads: int, jobs: int = 0, workload: str = "delays") -> str:
@@ -92,27 +122,10 @@ def build(threads: int, jobs: int = 0, workload: str = "delays") -> str:
     if os.path.exists(out):
         return out
     PROJECT = project(threads, workload)
-    man = manifest(threads, workload)
-    cxx = shutil.which("g++") or "g++"
-    objdir = os.path.join(PROJECT, f"_obj_{platform.machine()}")
-    os.makedirs(objdir, exist_ok=True)
-
-    def one(src):
-        obj = os.path.join(objdir, src.replace("/", "__") + ".o")
-        lang = ["-x", "c++"] if src.endswith(".c") else []
-        r = subprocess.run([cxx] + FLAGS + ["-I", PROJECT, "-c"] + lang + [os.path.join(PROJECT, src), "-o", obj],
-                           capture_output=True, text=True)
-        if r.returncode:
-            raise RuntimeError(f"compiling {src} failed:\n{r.stderr[-2000:]}")
-        return obj
-
+    srcs = manifest(threads, workload)["sources"]
     with ThreadPoolExecutor(max_workers=jobs or min(16, os.cpu_count() or 4)) as ex:
-        objs = list(ex.map(one, man["sources"]))
-    tmp = out + f".tmp{os.getpid()}"
-    r = subprocess.run([cxx] + objs + ["-fopenmp", "-o", tmp], capture_output=True, text=True)
-    if r.returncode:
-        raise RuntimeError(f"linking the reference project failed:\n{r.stderr[-2000:]}")
-    os.replace(tmp, out)
+        objs = list(ex.map(lambda src: _compile(PROJECT, src), srcs))
+    _link(out, objs)
     return out
 
 
@@ -131,6 +144,8 @@ def run(threads: int, timeout: float = 1200.0, workload: str = "delays") -> dict
                            timeout=timeout)
         if r.returncode:
             raise RuntimeError(f"reference project exited with {r.returncode}:\n{r.stdout[-1000:]}{r.stderr[-1000:]}")
+        if man.get("networks"):
+            return _run_networks(man, res, r.stdout)
         with open(os.path.join(res, "last_run_info.txt")) as f:
             last_time, frac = (float(x) for x in f.read().split())
         N, dt = man["N"], man["dt"]
@@ -166,4 +181,28 @@ def run(threads: int, timeout: float = 1200.0, workload: str = "delays") -> dict
     finally:
         shutil.rmtree(res, ignore_errors=True)  # every array of the run: up to many GB
     return dict(total, threads=man["threads"], sim_s=total["steps"] * dt, samples=samples, N=man["N"],
-                K=man["K"], float_dtype=man.get("float_dtype", "float64"))
+                K=man.get("K"), float_dtype=man.get("float_dtype", "float64"))
+
+
+def _run_networks(man, res, stdout):
+    """A project of several networks run one after another: each run's own
+    time is the elapsed time its report function got at the end of the run
+    (completed fraction 1; the call at its start has fraction 0,
+    ``templates/network.cpp:51-52, 119-120``)."""
+    ends = [float(ln.split()[1]) for ln in stdout.splitlines()
+            if ln.startswith(man["run_mark"] + " ") and float(ln.split()[2]) >= 1.0]
+    nets = man["networks"]
+    if len(ends) != len(nets):
+        raise RuntimeError(f"expected {len(nets)} end-of-run reports, found {len(ends)}")
+    steps = int(round(man["duration_ms"] * 1e-3 / man["dt"]))
+    per = []
+    for n, t in zip(nets, ends):
+        spk = np.fromfile(os.path.join(res, n["spike_i"]), dtype=np.int32)
+        outdeg = np.zeros(n["N"], np.int64)
+        for fname in n["pre"].values():
+            outdeg += np.bincount(np.fromfile(os.path.join(res, fname), dtype=np.int32), minlength=n["N"])
+        per.append(dict(N=n["N"], run_time_s=t, steps=steps, spikes=int(spk.size), events=int(outdeg[spk].sum())))
+    return dict(run_time_s=float(sum(p["run_time_s"] for p in per)), steps=steps * len(per),
+                spikes=sum(p["spikes"] for p in per), events=sum(p["events"] for p in per),
+                threads=man["threads"], networks=per, sweep_networks=man.get("sweep_networks"),
+                sweep_indices=man.get("sweep_indices"), float_dtype=man.get("float_dtype", "float64"))
