@@ -500,10 +500,37 @@ class B200Device(CPPStandaloneDevice):
                 elif t == "spikegenerator":
                     group_of(obj)
                 elif t == "spikemonitor":
-                    if not isinstance(obj, SpikeMonitor) or set(obj.record_variables) - {"i", "t"}:
-                        raise NotImplementedError("b200: spike monitors record i and t only")
+                    if not isinstance(obj, SpikeMonitor):
+                        raise NotImplementedError("b200: unsupported spike monitor")
                     gi, rng = group_of(obj.source)
-                    spkmons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng, _co=co.name))
+                    # the monitor's slot in the schedule (core/network.py:42-50):
+                    # after its group's thresholder; recorded variables only
+                    # before the step's deliveries, where they are the values
+                    # the thresholder saw
+                    base = obj.source.source if isinstance(obj.source, Subgroup) else obj.source
+                    thr = getattr(base, "thresholder", {}).get("spike") if hasattr(base, "thresholder") else None
+                    late = ("synapses", "after_synapses", "before_resets", "resets", "after_resets",
+                            "before_end", "end")
+                    if not (obj.when in ("after_thresholds", "before_synapses") + late or
+                            (obj.when == "thresholds" and (thr is None or obj.order > thr.order))):
+                        raise NotImplementedError(f"b200: a spike monitor in the '{obj.when}' slot before its "
+                                                  "group's thresholder")
+                    # recorded variables (monitors/spikemonitor.py:62-67): state
+                    # variables of the monitored group, their values at the spike
+                    extra = [v for v in obj.record_variables if v not in ("i", "t")]
+                    if extra and obj.when in late:
+                        raise NotImplementedError(f"b200: a spike monitor recording variables in the '{obj.when}' "
+                                                  "slot (after the step's deliveries)")
+                    names = [v["name"] for v in groups[gi]["vars"]]
+                    if extra and groups[gi].get("generator"):
+                        raise NotImplementedError("b200: a spike generator's monitor records i and t only")
+                    for v in extra:
+                        if v not in names:
+                            raise NotImplementedError(f"b200: spike monitor recording '{v}' (not a state variable)")
+                    if len(extra) > 8:
+                        raise NotImplementedError("b200: a spike monitor recording more than 8 variables")
+                    spkmons.append(dict(name=obj.name, group=gi, vars=[names.index(v) for v in extra], _obj=obj,
+                                        _range=rng, _co=co.name, _vars=extra))
                 elif t == "ratemonitor":
                     gi, rng = group_of(obj.source)
                     ratemons.append(dict(name=obj.name, group=gi, _obj=obj, _range=rng, _co=co.name))
@@ -935,6 +962,8 @@ class B200Device(CPPStandaloneDevice):
             lo, hi = m["_range"]
             self._store(mon.variables["count"], cnt[: hi - lo])
             self._store(mon.variables["N"], np.array([len(i)]))
+            for k, v in enumerate(m.get("_vars", [])):  # recorded variables, in the variable's type
+                self._store(mon.variables[v], out[f"sm{mi}_vals"][:, k].astype(mon.variables[v].dtype))
         for mi, m in enumerate(spec0["rate_monitors"]):
             c = out[f"rm{mi}_counts"]
             mon = m["_obj"]

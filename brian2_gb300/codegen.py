@@ -439,7 +439,8 @@ def render_model(spec: dict) -> str:
         w("static const b200_pathway_info* const b200_pathways = nullptr;")
     for nm, mons in (("spkmon", spkmons), ("ratemon", ratemons), ("statemon", statemons)):
         if mons:
-            w(f"static const b200_mon_info b200_{nm}[] = {{" + ", ".join(f'{{"{m["name"]}", {m["group"]}, {m.get("every", 1)}}}' for m in mons) + "};")
+            w(f"static const b200_mon_info b200_{nm}[] = {{" + ", ".join(
+                f'{{"{m["name"]}", {m["group"]}, {m.get("every", 1)}, {len(m.get("vars", []))}}}' for m in mons) + "};")
         else:
             w(f"static const b200_mon_info* const b200_{nm} = nullptr;")
     w("")
@@ -475,6 +476,25 @@ def render_model(spec: dict) -> str:
         lines = [f"{v['ctype']}*{r} const {v['ptr']} = ({v['ctype']}*)s_gv[{gi}][{k}]; (void){v['ptr']};"
                  for k, v in enumerate(g["vars"])]
         return _indent("\n".join(lines), indent)
+
+    def snap_code(gi, idx):
+        """The recorded variables of the spike monitors of group gi for the
+        spiking neuron `idx`, taken when the thresholder runs (after the
+        update, before the step's deliveries and its reset)."""
+        out = []
+        for mi, m in enumerate(spkmons):
+            if m["group"] == gi:
+                for v, k in enumerate(m.get("vars", [])):
+                    ptr = groups[gi]["vars"][k]["ptr"]
+                    out.append(f"I.sm[{mi}].snap[(size_t){v} * I.g[{gi}].N + ({idx})] = (double){ptr}[{idx}];")
+        return " ".join(out)
+
+    def value_rows(mi, gi, pos, idx):
+        """The recorded variables of spike monitor mi into its row `pos`."""
+        m = spkmons[mi]
+        nv = len(m.get("vars", []))
+        return " ".join(f"SM.vals[({pos}) * {nv} + {v}] = SM.snap[(size_t){v} * I.g[{gi}].N + ({idx})];"
+                        for v in range(nv))
 
     def extra_ptrs(block_spec, indent):
         lines = []
@@ -808,7 +828,7 @@ def render_model(spec: dict) -> str:
         w("                  const int nb = 4 * (qb + k * (int)blockDim.x + (int)threadIdx.x);")
         w("#pragma unroll")
         w("                  for (int e = 0; e < 4; ++e)")
-        w("                    if ((mine >> e) & 1u) { scr[p] = nb + e; oscr[p] = nb + e; ++p; }")
+        w("                    if ((mine >> e) & 1u) { scr[p] = nb + e; oscr[p] = nb + e; " + snap_code(gi, "nb + e") + " ++p; }")
         w("                }")
         w("              }")
         w("              cnt += tot;")
@@ -1057,14 +1077,16 @@ def render_model(spec: dict) -> str:
             w("            for (int k = 0; k < E; ++k) {")
             w("              const unsigned m = __ballot_sync(0xffffffffu, (flags >> k) & 1u);")
             w("              if ((flags >> k) & 1u)")
-            if owner:
-                w("                scr[start + cnt + s_cnt[k * NW + wid] + __popc(m & b200_lanemask_lt())] = pb + k * (int)blockDim.x + threadIdx.x;")
-            else:
-                w("                {")
-                w("                  const int _p = start + cnt + s_cnt[k * NW + wid] + __popc(m & b200_lanemask_lt());")
-                w("                  scr[_p] = pb + k * (int)blockDim.x + threadIdx.x;")
-                w("                  oscr[_p] = pb + k * (int)blockDim.x + threadIdx.x;  // this CTA's copy")
-                w("                }")
+            w("                {")
+            w("                  const int _p = start + cnt + s_cnt[k * NW + wid] + __popc(m & b200_lanemask_lt());")
+            w("                  const int _sn = pb + k * (int)blockDim.x + threadIdx.x;  // the spiking neuron")
+            w("                  scr[_p] = _sn;")
+            if not owner:
+                w("                  oscr[_p] = _sn;  // this CTA's copy")
+            sc = snap_code(gi, "_sn")
+            if sc:
+                w("                  " + sc)
+            w("                }")
             w("            }")
             w("            cnt += tot;")
             w("            __syncthreads();")
@@ -1401,6 +1423,8 @@ def render_model(spec: dict) -> str:
                 w("              const long long pos = mbase + pref[u] + j;")
                 w("              SM.i[pos] = idx - SM.lo;")
                 w("              SM.ts[pos] = (int32_t)ts;")
+                if m.get("vars"):
+                    w("              " + value_rows(mi, gi, "pos", "idx"))
                 w("              atomicAdd(&SM.count[idx - SM.lo], 1);  // no read round trip (own neurons: uncontended)")
                 w("            }")
                 w("          }")
@@ -2026,6 +2050,8 @@ def render_model(spec: dict) -> str:
                     w(sp + "        const long long pos = mbase + pref[u] + j;")
                     w(sp + "        SM.i[pos] = idx - SM.lo;")
                     w(sp + f"        SM.ts[pos] = (int32_t)({tsexpr});")
+                    if m.get("vars"):
+                        w(sp + "        " + value_rows(mi, gi, "pos", "idx"))
                     w(sp + "        SM.count[idx - SM.lo] += 1;")
                     w(sp + "      }")
                     w(sp + "    }")

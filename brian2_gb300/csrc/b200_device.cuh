@@ -98,12 +98,16 @@ struct b200_pathway_d {
 };
 
 struct b200_spkmon_d {
-  int32_t group, lo, hi, tile_lo, tile_hi, _pad;
+  int32_t group, lo, hi, tile_lo, tile_hi, n_vars;
   int64_t cap;            // capacity of i/ts
   int64_t* n;             // [1] number of recorded spikes
   int32_t* i;             // [cap] neuron index - lo
   int32_t* ts;            // [cap] time step of the spike
   int32_t* count;         // [hi-lo] spikes per neuron
+  // recorded variables (SpikeMonitor(..., variables=...)): their values when the
+  // step's thresholder ran, as double
+  double* snap;           // [n_vars][group N] the values of the step's spiking neurons
+  double* vals;           // [cap][n_vars] one row per recorded spike
 };
 
 struct b200_ratemon_d {
@@ -234,7 +238,8 @@ struct b200_summed_info {
 struct b200_mon_info {
   const char* name;
   int group;
-  int every;  // records on every k-th step (a state monitor on a slower clock); 1 otherwise
+  int every;   // records on every k-th step (a state monitor on a slower clock); 1 otherwise
+  int n_vars;  // a spike monitor's recorded variables besides i and t
 };
 struct b200_model_info {
   const char* name;

@@ -68,6 +68,7 @@ struct b200_spkmon_h {
   int32_t lo = 0, hi = 0;
   int64_t cap = 0;
   b200_dbuf n, i, ts, count;
+  b200_dbuf snap, vals;  // recorded variables: per-neuron values of the step, per-spike rows
 };
 struct b200_ratemon_h {
   int32_t lo = 0, hi = 0;
@@ -263,7 +264,10 @@ int b200_destroy(b200_net* n) {
       b200_free(n, P.ev_tgt); b200_free(n, P.ev_state); b200_free(n, P.ev_base); b200_free(n, P.ev_tag);
       b200_free(n, P.ev_off);
     }
-    for (auto& S : I.sm) { b200_free(n, S.n); b200_free(n, S.i); b200_free(n, S.ts); b200_free(n, S.count); }
+    for (auto& S : I.sm) {
+      b200_free(n, S.n); b200_free(n, S.i); b200_free(n, S.ts); b200_free(n, S.count);
+      b200_free(n, S.snap); b200_free(n, S.vals);
+    }
     for (auto& S : I.rm) b200_free(n, S.cnt);
     for (auto& S : I.stm) { b200_free(n, S.d_idx); b200_free(n, S.n); b200_free(n, S.data); }
     for (auto& S : I.sum) { b200_free(n, S.seg); b200_free(n, S.syn); }
@@ -938,13 +942,18 @@ static int b200_prepare(b200_net* n) {
         if ((r = b200_alloc(n, S.n, 16))) return r;
         if ((r = b200_alloc(n, S.count, (size_t)std::max(S.hi - S.lo, 1) * 4))) return r;
       }
+      const int nv = M->spkmon[s].n_vars;
       if (!S.i.p) {
         S.cap = std::max<int64_t>(1 << 16, 8 * (int64_t)(S.hi - S.lo));
         if ((r = b200_alloc(n, S.i, (size_t)S.cap * 4, false))) return r;
         if ((r = b200_alloc(n, S.ts, (size_t)S.cap * 4, false))) return r;
+        if (nv > 0 && (r = b200_alloc(n, S.vals, (size_t)S.cap * nv * 8, false))) return r;
       }
+      if (nv > 0 && (r = b200_alloc(n, S.snap, (size_t)nv * std::max(G.N, 1) * 8))) return r;
       b200_spkmon_d& SD = D.sm[s];
       SD.group = M->spkmon[s].group; SD.lo = S.lo; SD.hi = S.hi;
+      SD.n_vars = nv;
+      SD.snap = (double*)S.snap.p; SD.vals = (double*)S.vals.p;
       SD.tile_lo = (int)(std::lower_bound(G.tile_start.begin(), G.tile_start.end(), S.lo) - G.tile_start.begin());
       SD.tile_hi = (int)(std::lower_bound(G.tile_start.begin(), G.tile_start.end(), S.hi) - G.tile_start.begin());
       SD.cap = S.cap;
@@ -1189,24 +1198,31 @@ static int b200_prepare(b200_net* n) {
   return 0;
 }
 
-// Grow a spike monitor so that at least `need` more spikes fit.
-static int b200_grow_spkmon(b200_net* n, b200_spkmon_h& S, int64_t used, int64_t need) {
+// Grow a spike monitor (nv recorded variables) so that at least `need` more spikes fit.
+static int b200_grow_spkmon(b200_net* n, b200_spkmon_h& S, int nv, int64_t used, int64_t need) {
   int64_t cap = S.cap;
   while (cap - used < need) cap *= 2;
   if (cap == S.cap) return 0;
-  b200_dbuf ni, nt;
+  b200_dbuf ni, nt, nvl;
   int r;
   if ((r = b200_alloc(n, ni, (size_t)cap * 4, false))) return r;
   if ((r = b200_alloc(n, nt, (size_t)cap * 4, false))) return r;
+  if (nv > 0 && (r = b200_alloc(n, nvl, (size_t)cap * nv * 8, false))) return r;
   if (used) {
     B200_CU(n, cudaMemcpyAsync(ni.p, S.i.p, (size_t)used * 4, cudaMemcpyDeviceToDevice, n->stream));
     B200_CU(n, cudaMemcpyAsync(nt.p, S.ts.p, (size_t)used * 4, cudaMemcpyDeviceToDevice, n->stream));
+    if (nv > 0)
+      B200_CU(n, cudaMemcpyAsync(nvl.p, S.vals.p, (size_t)used * nv * 8, cudaMemcpyDeviceToDevice, n->stream));
   }
   B200_CU(n, cudaStreamSynchronize(n->stream));
   b200_free(n, S.i);
   b200_free(n, S.ts);
   S.i = ni;
   S.ts = nt;
+  if (nv > 0) {
+    b200_free(n, S.vals);
+    S.vals = nvl;
+  }
   S.cap = cap;
   return 0;
 }
@@ -1296,10 +1312,11 @@ int b200_run(b200_net* n, int64_t n_steps) {
         // room for at least 64 steps of all neurons spiking
         // (owner mode records a step's spikes one step later: one more step of room)
         const int64_t need = (std::min<int64_t>(target[k] - I.ts, 64) + (n->owner ? 1 : 0)) * (int64_t)(S.hi - S.lo);
-        if ((r = b200_grow_spkmon(n, S, used, need))) return r;
+        if ((r = b200_grow_spkmon(n, S, M->spkmon[s].n_vars, used, need))) return r;
         D.sm[s].cap = S.cap;
         D.sm[s].i = (int32_t*)S.i.p;
         D.sm[s].ts = (int32_t*)S.ts.p;
+        D.sm[s].vals = (double*)S.vals.p;
       }
     }
     if (!any) break;
@@ -1721,6 +1738,18 @@ int b200_spikemon_get(b200_net* n, int32_t inst, int32_t mon, int32_t* i, int32_
   }
   if (per_neuron && S.count.p && S.hi > S.lo)
     B200_CU(n, cudaMemcpy(per_neuron, S.count.p, (size_t)(S.hi - S.lo) * 4, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+int b200_spikemon_values(b200_net* n, int32_t inst, int32_t mon, double* vals, int64_t count) {
+  int64_t have = 0;
+  int r = b200_spikemon_size(n, inst, mon, &have);
+  if (r) return r;
+  if (count != have) return b200_fail(n, B200_ERR_ARG, "spike monitor size mismatch");
+  const int nv = n->M->spkmon[mon].n_vars;
+  if (nv == 0 || count == 0) return 0;
+  if (!vals) return B200_ERR_ARG;
+  B200_CU(n, cudaMemcpy(vals, n->inst[inst].sm[mon].vals.p, (size_t)count * nv * 8, cudaMemcpyDeviceToHost));
   return 0;
 }
 

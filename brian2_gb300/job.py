@@ -178,9 +178,11 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None,
     for pi, p in enumerate(spec.get("pathways", [])):
         for v in p.get("vars", []) if p.get("alias", -1) < 0 else []:
             out[f"p{pi}_{v['name']}"] = net.download_synapse_var(0, pi, v["name"])
-    for mi in range(len(spec.get("spike_monitors", []))):
+    for mi, m in enumerate(spec.get("spike_monitors", [])):
         i, ts, cnt = net.spikes(0, mi)
         out[f"sm{mi}_i"], out[f"sm{mi}_ts"], out[f"sm{mi}_count"] = i, ts, cnt
+        if m.get("vars"):
+            out[f"sm{mi}_vals"] = net.spike_values(0, mi)
     for mi in range(len(spec.get("rate_monitors", []))):
         out[f"rm{mi}_counts"] = net.rate_counts(0, mi)
     for mi in range(len(spec.get("state_monitors", []))):

@@ -58,6 +58,7 @@ def _declare(lib):
         "b200_last_kernel_ms": [h, _f64p],
         "b200_spikemon_size": [h, C.c_int32, C.c_int32, _i64p],
         "b200_spikemon_get": [h, C.c_int32, C.c_int32, _i32p, _i32p, _i32p, C.c_int64],
+        "b200_spikemon_values": [h, C.c_int32, C.c_int32, C.POINTER(C.c_double), C.c_int64],
         "b200_ratemon_size": [h, C.c_int32, C.c_int32, _i64p],
         "b200_ratemon_get": [h, C.c_int32, C.c_int32, _i32p, C.c_int64],
         "b200_statemon_size": [h, C.c_int32, C.c_int32, _i64p],
@@ -319,6 +320,20 @@ class Network:
         self._check(self.lib.b200_spikemon_get(self._h, int(inst), m, _ptr(i, _i32p), _ptr(ts, _i32p),
                                                _ptr(cnt, _i32p) if cnt is not None else None, n.value))
         return i, ts, cnt
+
+    def spike_values(self, inst=0, mon=0):
+        """[spikes, n_vars] float64: the values of the monitor's recorded
+        variables (``SpikeMonitor(..., variables=...)``) at each spike, in the
+        order of spikes()."""
+        m = mon if isinstance(mon, int) else self.model.spkmon_index[mon]
+        nv = len(self.model.spec["spike_monitors"][m].get("vars", []))
+        n = C.c_int64()
+        self._check(self.lib.b200_spikemon_size(self._h, int(inst), m, C.byref(n)))
+        a = np.empty((n.value, nv), np.float64)
+        if nv:
+            self._check(self.lib.b200_spikemon_values(self._h, int(inst), m,
+                                                      a.ctypes.data_as(C.POINTER(C.c_double)), n.value))
+        return a
 
     def rate_counts(self, inst=0, mon=0):
         m = mon if isinstance(mon, int) else self.model.ratemon_index[mon]

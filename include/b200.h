@@ -161,6 +161,13 @@ int b200_last_kernel_ms(b200_net* net, double* ms);
 int b200_spikemon_size(b200_net* net, int32_t inst, int32_t mon, int64_t* count);
 int b200_spikemon_get(b200_net* net, int32_t inst, int32_t mon, int32_t* i, int32_t* ts,
                       int32_t* per_neuron, int64_t count);
+/* The values of a spike monitor's recorded variables (SpikeMonitor(G, variables=...),
+ * monitors/spikemonitor.py:62-67; appended with i and t by spikemonitor.cpp:37-47):
+ * vals[count][n_vars] as double, in the order of the spikes, each the
+ * variable's value when the step's thresholder ran (after the state update,
+ * before that step's deliveries and reset).  n_vars is the model's count for
+ * that monitor; count as from b200_spikemon_size. */
+int b200_spikemon_values(b200_net* net, int32_t inst, int32_t mon, double* vals, int64_t count);
 int b200_ratemon_size(b200_net* net, int32_t inst, int32_t mon, int64_t* steps);
 int b200_ratemon_get(b200_net* net, int32_t inst, int32_t mon, int32_t* counts, int64_t steps);
 int b200_statemon_size(b200_net* net, int32_t inst, int32_t mon, int64_t* steps);

@@ -607,6 +607,35 @@ def host_sets(N=200, seed_value=606):
 
 host_sets.multiple_runs = True
 
+
+def spike_vars(N=400, duration_ms=200.0, seed_value=707):
+    """Spike monitors recording variables (``monitors/spikemonitor.py:62-67``):
+    the whole group with v and ge, a subgroup with gi and lastspike.  Every
+    pathway has a delay, and one of them writes v itself, so the values must
+    be those the thresholder saw (after the update, before the step's
+    deliveries and its reset; lastspike already set to the spike's time)."""
+    from brian2 import NeuronGroup, Synapses, SpikeMonitor, PopulationRateMonitor, ms, mV, seed, run
+    seed(seed_value)
+    ns = dict(taum=20 * ms, taue=5 * ms, taui=10 * ms, Vt=-50 * mV, Vr=-60 * mV, El=-49 * mV,
+              we=1.62 * mV, wi=-9 * mV, wv=0.5 * mV)
+    P = NeuronGroup(N, '''dv/dt  = (ge+gi-(v-El))/taum : volt (unless refractory)
+                          dge/dt = -ge/taue : volt
+                          dgi/dt = -gi/taui : volt''',
+                    threshold='v>Vt', reset='v = Vr', refractory=2 * ms, method='exact', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    Ne = int(0.8 * N)
+    Ce = Synapses(P[:Ne], P, on_pre='ge += we', delay=0.1 * ms, namespace=ns)
+    Ci = Synapses(P[Ne:], P, on_pre='gi += wi', delay=0.1 * ms, namespace=ns)
+    Cv = Synapses(P, P, on_pre='v += wv', delay=0.3 * ms, namespace=ns)
+    Ce.connect(p=0.02)
+    Ci.connect(p=0.02)
+    Cv.connect(p=0.02)
+    s_mon = SpikeMonitor(P, variables=['v', 'ge'])
+    sub_mon = SpikeMonitor(P[100:300], variables=['gi', 'lastspike'])
+    r_mon = PopulationRateMonitor(P)
+    run(duration_ms * ms)
+    return dict(P=P, spikes=s_mon, rate=r_mon, other_spikes=sub_mon, spike_var_monitors=[s_mon, sub_mon])
+
 SCENARIOS = {
     "lif_refractory": lif_refractory,
     "hetero_delays": hetero_delays,
@@ -623,6 +652,7 @@ SCENARIOS = {
     "regular_ops": regular_ops,
     "end_monitor": end_monitor,
     "host_sets": host_sets,
+    "spike_vars": spike_vars,
 }
 
 

@@ -164,6 +164,7 @@ def render_oracle(spec: dict) -> str:
         w(f"  std::vector<std::vector<int32_t>> p{pi}_syn;")
     for mi, m in enumerate(spkmons):
         w(f"  int32_t sm{mi}_lo = 0, sm{mi}_hi = 0; std::vector<int32_t> sm{mi}_i, sm{mi}_ts, sm{mi}_count;")
+        w(f"  std::vector<double> sm{mi}_vals;  // recorded variables, one row per spike")
     for mi, m in enumerate(ratemons):
         w(f"  int32_t rm{mi}_lo = 0, rm{mi}_hi = 0; std::vector<int32_t> rm{mi}_cnt;")
     for mi, m in enumerate(statemons):
@@ -407,7 +408,10 @@ def render_oracle(spec: dict) -> str:
         w("    {")
         w(f"      const std::vector<int32_t>& sp = n->spk{gi};")
         w(f"      for (int32_t idx : sp) if (idx >= n->sm{mi}_lo && idx < n->sm{mi}_hi) {{")
-        w(f"        n->sm{mi}_i.push_back(idx - n->sm{mi}_lo); n->sm{mi}_ts.push_back((int32_t)n->ts); n->sm{mi}_count[idx - n->sm{mi}_lo]++; }}")
+        w(f"        n->sm{mi}_i.push_back(idx - n->sm{mi}_lo); n->sm{mi}_ts.push_back((int32_t)n->ts); n->sm{mi}_count[idx - n->sm{mi}_lo]++;")
+        for k in m.get("vars", []):  # (spikemonitor.cpp:37-47: _source_<var>[idx] after the thresholder)
+            w(f"        n->sm{mi}_vals.push_back((double)n->g{gi}_{groups[gi]['vars'][k]['name']}[idx]);")
+        w("      }")
         w("    }")
     def emit_inputs():
         for k, inp in enumerate(INPUTS):
@@ -497,6 +501,7 @@ def render_oracle(spec: dict) -> str:
         w(f"void oracle_spikemon_get_{mi}(Net* n, int32_t* i, int32_t* ts, int32_t* cnt) {{")
         w(f"  std::copy(n->sm{mi}_i.begin(), n->sm{mi}_i.end(), i); std::copy(n->sm{mi}_ts.begin(), n->sm{mi}_ts.end(), ts);")
         w(f"  std::copy(n->sm{mi}_count.begin(), n->sm{mi}_count.end(), cnt); }}")
+        w(f"void oracle_spikemon_values_{mi}(Net* n, double* vals) {{ std::copy(n->sm{mi}_vals.begin(), n->sm{mi}_vals.end(), vals); }}")
     for mi, _ in enumerate(ratemons):
         w(f"int64_t oracle_ratemon_size_{mi}(Net* n) {{ return (int64_t)n->rm{mi}_cnt.size(); }}")
         w(f"void oracle_ratemon_get_{mi}(Net* n, int32_t* c) {{ std::copy(n->rm{mi}_cnt.begin(), n->rm{mi}_cnt.end(), c); }}")
@@ -676,6 +681,18 @@ class OracleNet:
                                                          ts.ctypes.data_as(_i32p), cnt.ctypes.data_as(_i32p))
         return i, ts, cnt
 
+    def spike_values(self, mon=0):
+        """[spikes, n_vars] values of the monitor's recorded variables."""
+        nv = len(self.spec["spike_monitors"][mon].get("vars", []))
+        f = getattr(self.lib, f"oracle_spikemon_size_{mon}")
+        f.restype = C.c_int64
+        f.argtypes = [C.c_void_p]
+        n = f(self.h)
+        a = np.empty((n, nv), np.float64)
+        if nv and n:
+            getattr(self.lib, f"oracle_spikemon_values_{mon}")(C.c_void_p(self.h), a.ctypes.data_as(C.POINTER(C.c_double)))
+        return a
+
     def rate_counts(self, mon=0):
         f = getattr(self.lib, f"oracle_ratemon_size_{mon}")
         f.restype = C.c_int64
@@ -768,8 +785,10 @@ def run_job_on_oracle(directory):
     for pi, p in enumerate(spec.get("pathways", [])):
         for v in p.get("vars", []) if p.get("alias", -1) < 0 else []:
             out[f"p{pi}_{v['name']}"] = o.download_synapse_var(pi, v["name"])
-    for mi in range(len(spec.get("spike_monitors", []))):
+    for mi, m in enumerate(spec.get("spike_monitors", [])):
         out[f"sm{mi}_i"], out[f"sm{mi}_ts"], out[f"sm{mi}_count"] = o.spikes(mi)
+        if m.get("vars"):
+            out[f"sm{mi}_vals"] = o.spike_values(mi)
     for mi in range(len(spec.get("rate_monitors", []))):
         out[f"rm{mi}_counts"] = o.rate_counts(mi)
     for mi in range(len(spec.get("state_monitors", []))):

@@ -82,6 +82,13 @@ def run_ref(name):
         out["other_i"] = np.asarray(o.i[:], dtype=np.int32)
         out["other_ts"] = np.round(np.asarray(o.t_[:]) / 1e-4).astype(np.int32)
         meta["other_monitor"] = o.name
+    if "spike_var_monitors" in r:              # spike monitors' recorded variables
+        meta["spike_var_monitors"] = {}
+        for mon in r["spike_var_monitors"]:
+            names = [v for v in mon.record_variables if v not in ("i", "t")]
+            for var in names:
+                out[f"smv_{mon.name}_{var}"] = np.asarray(getattr(mon, var + "_")[:]).copy()
+            meta["spike_var_monitors"][mon.name] = names
     if "syn_vars" in r:                        # synaptic variables (creation order)
         for var in r["syn_vars"]:
             out["syn_" + var] = np.asarray(getattr(r["S"], var + "_")[:]).copy()

@@ -24,7 +24,7 @@ EXACT = {"lif_refractory": True, "hetero_delays": False, "subgroup_monitors": Tr
          "presynaptic_read": False, "spike_generator": True, "stdp": False,
          "gap_junctions": True, "explicit_methods": True, "poisson_input": False, "poisson_drive": True,
          "noise_inputs": False, "regular_ops": True,
-         "end_monitor": True, "host_sets": True}
+         "end_monitor": True, "host_sets": True, "spike_vars": True}
 
 
 @pytest.mark.parametrize("name", sorted(EXACT))
@@ -52,6 +52,14 @@ def test_scenario_matches_reference(name, ctas, owner):
         np.testing.assert_array_equal(out[f"sm{gm}_ts"], ref["gen_ts"])
         gg = [g["name"] for g in spec["groups"]].index(meta["gen_group"])
         assert int(out[f"g{gg}_gen_last"]) == meta["gen_lastindex"]
+    for mname, names in meta.get("spike_var_monitors", {}).items():  # recorded variables at each spike
+        mi = mons.index(mname)
+        m = spec["spike_monitors"][mi]
+        gvars = [v["name"] for v in spec["groups"][m["group"]]["vars"]]
+        for col, k in enumerate(m["vars"]):
+            np.testing.assert_array_equal(out[f"sm{mi}_vals"][:, col], ref[f"smv_{mname}_{gvars[k]}"],
+                                          err_msg=f"{mname}.{gvars[k]}")
+        assert sorted(gvars[k] for k in m["vars"]) == sorted(names)
     np.testing.assert_array_equal(out["rm0_counts"], ref["rate_counts"])
     gi = [g["name"] for g in spec["groups"]].index(meta["group"])
     for var in ("v", "ge", "gi", "a", "Igap", "u"):

@@ -41,6 +41,14 @@ def test_oracle_reproduces_reference_scenario(name):
         np.testing.assert_array_equal(out[f"sm{gm}_ts"], ref["gen_ts"])
         gg = [g["name"] for g in spec["groups"]].index(meta["gen_group"])
         assert int(out[f"g{gg}_gen_last"]) == meta["gen_lastindex"]
+    for mname, names in meta.get("spike_var_monitors", {}).items():  # recorded variables at each spike
+        mi = mons.index(mname)
+        m = spec["spike_monitors"][mi]
+        gvars = [v["name"] for v in spec["groups"][m["group"]]["vars"]]
+        assert sorted(gvars[k] for k in m["vars"]) == sorted(names)
+        for col, k in enumerate(m["vars"]):
+            np.testing.assert_array_equal(out[f"sm{mi}_vals"][:, col], ref[f"smv_{mname}_{gvars[k]}"],
+                                          err_msg=f"{mname}.{gvars[k]}")
     gi = [g["name"] for g in spec["groups"]].index(meta["group"])
     for var in ("v", "ge", "gi", "a", "Igap", "u"):
         if var in ref:
