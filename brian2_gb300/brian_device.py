@@ -58,7 +58,7 @@ from brian2.input.poissongroup import PoissonGroup
 from brian2.input.poissoninput import PoissonInput
 from brian2.input.spikegeneratorgroup import SpikeGeneratorGroup
 from brian2.monitors.ratemonitor import PopulationRateMonitor
-from brian2.monitors.spikemonitor import SpikeMonitor
+from brian2.monitors.spikemonitor import EventMonitor, SpikeMonitor
 from brian2.monitors.statemonitor import StateMonitor
 from brian2.synapses.synapses import Synapses, SynapticPathway
 from brian2.utils.logger import get_logger
@@ -375,6 +375,24 @@ class B200Device(CPPStandaloneDevice):
             hi = g.stop if isinstance(g, Subgroup) else len(base)
             return group_index[base.name], (int(lo), int(hi))
 
+        def event_group_of(g, event):
+            """The group whose spike list is the event's list: the group itself
+            for 'spike'; for a custom event (NeuronGroup(events=...),
+            groups/neurongroup.py:522-560) a shadow group on the same state
+            arrays (alias_of), with the event's condition as its threshold and
+            its run_on_event code as its reset, and no state update."""
+            gi, rng = group_of(g)
+            if event == "spike":
+                return gi, rng
+            if groups[gi].get("generator"):
+                raise NotImplementedError("b200: custom events of a spike generator")
+            key = groups[gi]["name"] + "\x00" + event
+            if key not in group_index:
+                group_index[key] = len(groups)
+                groups.append(dict(name=f"{groups[gi]['name']}__{event}", vars=[dict(v) for v in groups[gi]["vars"]],
+                                   alias_of=gi, event=event, _obj=groups[gi]["_obj"]))
+            return group_index[key], rng
+
         clock_ptrs = dict(dt=gen_name(clock.variables["dt"]), t=gen_name(clock.variables["t"]),
                           timestep=gen_name(clock.variables["timestep"]))
         consts = {}
@@ -435,7 +453,7 @@ class B200Device(CPPStandaloneDevice):
                 elif type(obj) is CodeRunner and t == "stateupdate":
                     op_frags.append((obj, frag, pos))
                 elif t in ("stateupdate", "threshold", "reset"):
-                    gi, _ = group_of(obj.group)
+                    gi, _ = event_group_of(obj.group, getattr(obj, "event", "spike") if t != "stateupdate" else "spike")
                     g = groups[gi]
                     key = {"stateupdate": "update"}.get(t, t)
                     b = block(frag)
@@ -455,9 +473,8 @@ class B200Device(CPPStandaloneDevice):
                                                          calls=calls), b))
                     if t == "threshold":
                         b["refractory"] = bool(frag["template_kwds"].get("_uses_refractory", False))
-                        if frag["template_kwds"].get("eventspace_variable") is not None and \
-                                frag["template_kwds"]["eventspace_variable"].name != "_spikespace":
-                            raise NotImplementedError("b200: custom events are not supported")
+                    if t == "reset":
+                        g["_reset_pos"] = pos  # (the resets of a group and its events run in schedule order)
                     if key in g:
                         raise NotImplementedError(f"b200: several {t} code objects for one group")
                     b["_co"] = co.name  # (for the profile: the time of each code object)
@@ -467,7 +484,7 @@ class B200Device(CPPStandaloneDevice):
                     if not isinstance(pw, SynapticPathway) or pw.prepost not in ("pre", "post"):
                         raise NotImplementedError("b200: unsupported synaptic pathway")
                     syn = pw.synapses
-                    sgi, srange = group_of(pw.source)
+                    sgi, srange = event_group_of(pw.source, pw.event)
                     tgi, trange = group_of(pw.target)
                     sv, seen = [], set()
                     used = {id(v) for v in frag["variables"].values()}
@@ -500,15 +517,15 @@ class B200Device(CPPStandaloneDevice):
                 elif t == "spikegenerator":
                     group_of(obj)
                 elif t == "spikemonitor":
-                    if not isinstance(obj, SpikeMonitor):
+                    if not isinstance(obj, EventMonitor):
                         raise NotImplementedError("b200: unsupported spike monitor")
-                    gi, rng = group_of(obj.source)
+                    gi, rng = event_group_of(obj.source, obj.event)
                     # the monitor's slot in the schedule (core/network.py:42-50):
                     # after its group's thresholder; recorded variables only
                     # before the step's deliveries, where they are the values
                     # the thresholder saw
                     base = obj.source.source if isinstance(obj.source, Subgroup) else obj.source
-                    thr = getattr(base, "thresholder", {}).get("spike") if hasattr(base, "thresholder") else None
+                    thr = getattr(base, "thresholder", {}).get(obj.event) if hasattr(base, "thresholder") else None
                     late = ("synapses", "after_synapses", "before_resets", "resets", "after_resets",
                             "before_end", "end")
                     if not (obj.when in ("after_thresholds", "before_synapses") + late or
@@ -731,6 +748,13 @@ class B200Device(CPPStandaloneDevice):
         for g in groups:
             for k in ("update", "threshold", "reset"):
                 g.setdefault(k, None)
+        # a group's resets and its custom events' resets (run_on_event) change the
+        # same state: they run one after another in the schedule's order
+        for gi, g in enumerate(groups):
+            members = [gi] + [k for k, h in enumerate(groups) if h.get("alias_of") == gi]
+            if len(members) > 1:
+                with_reset = [k for k in members if groups[k]["reset"] is not None]
+                g["reset_order"] = sorted(with_reset, key=lambda k: groups[k]["_reset_pos"])
         # every array pointer used by a group block must be declared: add the
         # clock and constant names used in snippets as they are
         fdt = prefs["core.default_float_dtype"]
@@ -868,7 +892,7 @@ class B200Device(CPPStandaloneDevice):
         init = {}
         for gi, g in enumerate(spec0["groups"]):
             init[f"g{gi}_N"] = np.int64(len(g["_obj"]))
-            for v in g["vars"]:
+            for v in g["vars"] if g.get("alias_of") is None else []:  # (a custom event's group shares them)
                 init[f"g{gi}_{v['name']}"] = self._load(g["_obj"].variables[v["name"]])
             if g.get("generator"):
                 gv = g["_obj"].variables
@@ -946,7 +970,7 @@ class B200Device(CPPStandaloneDevice):
         self._last_run_time = float(out["device_ms"]) * 1e-3
         self._last_run_completed_fraction = 1.0
         for gi, g in enumerate(spec0["groups"]):
-            for v in g["vars"]:
+            for v in g["vars"] if g.get("alias_of") is None else []:
                 self._store(g["_obj"].variables[v["name"]], out[f"g{gi}_{v['name']}"])
             if g.get("generator"):
                 self._store(g["_obj"].variables["_lastindex"], np.array([int(out[f"g{gi}_gen_last"])]))
@@ -957,11 +981,12 @@ class B200Device(CPPStandaloneDevice):
         for mi, m in enumerate(spec0["spike_monitors"]):
             i, ts, cnt = out[f"sm{mi}_i"], out[f"sm{mi}_ts"], out[f"sm{mi}_count"]
             mon = m["_obj"]
-            self._store(mon.variables["i"], i)
-            self._store(mon.variables["t"], ts.astype(np.float64) * dt)
             lo, hi = m["_range"]
             self._store(mon.variables["count"], cnt[: hi - lo])
             self._store(mon.variables["N"], np.array([len(i)]))
+            if mon.record:  # (record=False: no i and t, monitors/spikemonitor.py:127-128)
+                self._store(mon.variables["i"], i)
+                self._store(mon.variables["t"], ts.astype(np.float64) * dt)
             for k, v in enumerate(m.get("_vars", [])):  # recorded variables, in the variable's type
                 self._store(mon.variables[v], out[f"sm{mi}_vals"][:, k].astype(mon.variables[v].dtype))
         for mi, m in enumerate(spec0["rate_monitors"]):

@@ -328,7 +328,10 @@ def render_model(spec: dict) -> str:
         # pack 8-byte variables first so every cached array stays aligned
         return sorted(used, key=lambda k: -SIZE[g["vars"][k]["ctype"]])
 
-    USED = [used_vars(gi) for gi in range(NG)]
+    # a custom event's group (alias_of: the group whose events they are) has no
+    # state of its own: its pointers are its parent's, cached with the parent's
+    ALIAS = [g.get("alias_of") for g in groups]
+    USED = [used_vars(gi) if ALIAS[gi] is None else [] for gi in range(NG)]
 
     def private_vars(gi):
         """Used variables of group gi that only the CTA owning a neuron touches:
@@ -348,7 +351,7 @@ def render_model(spec: dict) -> str:
                     text += json.dumps(gg[blk].get("extra_ptrs", {}))
         return [k for k in USED[gi] if not re.search(r"\b%s\b" % re.escape(g["vars"][k]["ptr"]), text)]
 
-    PRIV = [private_vars(gi) for gi in range(NG)]
+    PRIV = [private_vars(gi) if ALIAS[gi] is None else [] for gi in range(NG)]
 
     def syn_arr(pi, which):
         """Device array holding Brian's _synaptic_pre ('pre') or _synaptic_post
@@ -425,7 +428,7 @@ def render_model(spec: dict) -> str:
         w(f"static const int b200_p{pi}_kinds[] = {{" + ", ".join(str(CTYPE_KIND[v["ctype"]]) for v in pv) + ('' if pv else '0') + "};")
     w("static const b200_group_info b200_groups[] = {" + ", ".join(
         f'{{"{g["name"]}", {len(g["vars"])}, b200_g{gi}_vars, b200_g{gi}_kinds, {gtables[gi][0].size}, b200_g{gi}_used, '
-        f'{1 if g.get("generator") else 0}, b200_g{gi}_priv}}'
+        f'{1 if g.get("generator") else 0}, b200_g{gi}_priv, {-1 if ALIAS[gi] is None else ALIAS[gi]}}}'
         for gi, g in enumerate(groups)) + "};")
     for pi, p in enumerate(paths):
         pay = PAYLOAD[pi] if OWNER else []
@@ -618,8 +621,11 @@ def render_model(spec: dict) -> str:
         """What the reference runs after the deliveries of step `tsexpr`: the
         Poisson inputs, the reset, the end-slot operations and state monitors
         (this CTA's neurons)."""
-        parts = [x for x in (input_block(gi, indent, tsexpr), reset_block(gi, indent, tsexpr, owner),
-                             op_block(gi, indent, tsexpr, "end"), statemon_text(gi, indent, tsexpr, "end")) if x]
+        if ALIAS[gi] is not None:
+            return ""  # (its reset runs in its parent's block)
+        resets = [reset_block(k, indent, tsexpr, owner) for k in (groups[gi].get("reset_order") or [gi])]
+        parts = [x for x in [input_block(gi, indent, tsexpr)] + resets +
+                 [op_block(gi, indent, tsexpr, "end"), statemon_text(gi, indent, tsexpr, "end")] if x]
         return ("\n" + " " * indent + "__syncthreads();\n").join(parts)
 
     def emit_generator(gi, owner):
@@ -1229,6 +1235,10 @@ def render_model(spec: dict) -> str:
     # quad accesses need every state pointer aligned to 4 elements (shared
     # memory copies are offset by the CTA's first neuron)
     w("    if (threadIdx.x == 0) {")
+    for gi, g in enumerate(groups):
+        if ALIAS[gi] is not None:
+            for k in range(len(g["vars"])):
+                w(f"      s_gv[{gi}][{k}] = s_gv[{ALIAS[gi]}][{k}];  // a custom event of group {ALIAS[gi]}")
     for gi, g in enumerate(groups):
         conds = []
         for k, v in enumerate(g["vars"]):
@@ -1972,6 +1982,10 @@ def render_model(spec: dict) -> str:
             w(f"          s_ttag[{pi}] = (long long*)F.tag + (size_t)rank * F.RB;")
             w("        }")
             w("      }")
+        for gi, g in enumerate(groups):
+            if ALIAS[gi] is not None:
+                for k in range(len(g["vars"])):
+                    w(f"      s_gv[{gi}][{k}] = s_gv[{ALIAS[gi]}][{k}];  // a custom event of group {ALIAS[gi]}")
         w("    }")
         w("    __syncthreads();")
         w("    if (I.tab_smem) {  // this CTA's batch tables live in shared memory for the launch")

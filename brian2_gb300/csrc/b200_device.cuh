@@ -200,6 +200,8 @@ struct b200_group_info {
   int generator;  // 1: a spike generator group (spikes from b200_set_generator lists)
   const int* var_private;  // 1: used, and touched only by the CTA that owns the neuron (no
                            // pathway or other group reads or writes it)
+  int alias;  // a custom event's group: the group whose state it shares (its events' lists
+              // are this group's spike lists); -1 otherwise
 };
 struct b200_pathway_info {
   const char* name;

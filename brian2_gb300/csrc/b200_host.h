@@ -221,6 +221,13 @@ int b200_create(b200_net** out, int32_t n_inst, const int32_t* group_sizes, doub
         return b200_fail(n, B200_ERR_ARG, "negative group size");
       }
       G.var.resize(M->groups[g].n_vars);
+      if (M->groups[g].alias >= 0) {  // a custom event's group: the state of the group it belongs to
+        if (G.N != I.g[M->groups[g].alias].N) {
+          *out = n;
+          return b200_fail(n, B200_ERR_ARG, "group %d (events of group %d) has another size", g, M->groups[g].alias);
+        }
+        continue;
+      }
       for (int v = 0; v < M->groups[g].n_vars; ++v) {
         // rounded up to 16 bytes: the update reads and writes whole groups of four neurons
         int r = b200_alloc(n, G.var[v], ((size_t)G.N * b200_kind_size(M->groups[g].var_kind[v]) + 15) & ~(size_t)15);
@@ -327,6 +334,7 @@ static int b200_var_buf(b200_net* n, int32_t inst, int32_t kind, int32_t obj, in
   if (kind == 0) {
     if (obj < 0 || obj >= n->M->n_groups || var < 0 || var >= n->M->groups[obj].n_vars)
       return b200_fail(n, B200_ERR_ARG, "bad group variable %d/%d", obj, var);
+    if (n->M->groups[obj].alias >= 0) obj = n->M->groups[obj].alias;  // a custom event's group: shared state
     *buf = &I.g[obj].var[var];
     *vkind = n->M->groups[obj].var_kind[var];
     *count = I.g[obj].N;
@@ -872,7 +880,8 @@ static int b200_prepare(b200_net* n) {
       GD.ring = (int32_t*)G.ring.p;
       GD.ring_total = (int32_t*)G.ring_total.p;
       GD.ring_prefix = (int32_t*)G.ring_prefix.p;
-      for (int v = 0; v < M->groups[g].n_vars; ++v) GD.var[v] = G.var[v].p;
+      const b200_group_h& GS = M->groups[g].alias >= 0 ? I.g[M->groups[g].alias] : G;  // (state owner)
+      for (int v = 0; v < M->groups[g].n_vars; ++v) GD.var[v] = GS.var[v].p;
       GD.S = (const double*)G.S.p;
       if (M->groups[g].generator) {
         if (!G.gen_last.p) {  // no lists set: a generator without spikes

@@ -111,7 +111,7 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None,
     if owner is not None:
         net.set_owner(owner)
     for gi, g in enumerate(spec["groups"]):
-        for v in g["vars"]:
+        for v in g["vars"] if g.get("alias_of") is None else []:  # (a custom event's group shares them)
             net.upload(0, gi, v["name"], init[f"g{gi}_{v['name']}"])
         if g.get("generator"):
             net.set_generator(0, gi, init[f"g{gi}_gen_bins"], init[f"g{gi}_gen_index"],
@@ -171,7 +171,7 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None,
         out["prof_names"] = np.array(list(prof), dtype=str)
         out["prof_cycles"] = np.array(list(prof.values()), dtype=np.float64)
     for gi, g in enumerate(spec["groups"]):
-        for v in g["vars"]:
+        for v in g["vars"] if g.get("alias_of") is None else []:
             out[f"g{gi}_{v['name']}"] = net.download(0, gi, v["name"])
         if g.get("generator"):
             out[f"g{gi}_gen_last"] = np.int64(net.generator_cursor(0, gi))

@@ -636,6 +636,35 @@ def spike_vars(N=400, duration_ms=200.0, seed_value=707):
     run(duration_ms * ms)
     return dict(P=P, spikes=s_mon, rate=r_mon, other_spikes=sub_mon, spike_var_monitors=[s_mon, sub_mon])
 
+
+def custom_events(N=300, duration_ms=200.0, seed_value=808):
+    """A custom event (``NeuronGroup(events=...)``, ``groups/neurongroup.py:522-560``):
+    'high' while the potential is above -52 mV.  Its ``run_on_event`` code
+    changes v as the spike reset does (the two resets run in the schedule's
+    order, before the next update) and drives an adaptation current; a pathway
+    ``on_event='high'`` with a delay, and an ``EventMonitor`` recording v."""
+    from brian2 import (NeuronGroup, Synapses, SpikeMonitor, EventMonitor, PopulationRateMonitor, ms, mV, seed,
+                        run)
+    seed(seed_value)
+    ns = dict(taum=20 * ms, taue=5 * ms, taua=50 * ms, Vt=-50 * mV, Vr=-60 * mV, El=-49 * mV, Vh=-52 * mV,
+              we=0.8 * mV, wh=0.3 * mV, da=0.001 * mV, dvh=0.0005 * mV)
+    P = NeuronGroup(N, '''dv/dt = (ge - gh - a - (v - El))/taum : volt
+                          dge/dt = -ge/taue : volt
+                          dgh/dt = -gh/taue : volt
+                          da/dt = -a/taua : volt''',
+                    threshold='v>Vt', reset='v = Vr', events={'high': 'v > Vh'}, method='exact', namespace=ns)
+    P.run_on_event('high', 'a += da; v -= dvh')
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    S = Synapses(P, P, on_pre='ge += we', delay=0.2 * ms, namespace=ns)
+    S.connect(p=0.05)
+    Sh = Synapses(P, P, on_pre='gh += wh', on_event='high', delay=0.5 * ms, namespace=ns)
+    Sh.connect(p=0.02)
+    s_mon = SpikeMonitor(P)
+    e_mon = EventMonitor(P, 'high', variables=['v'])
+    r_mon = PopulationRateMonitor(P)
+    run(duration_ms * ms)
+    return dict(P=P, spikes=s_mon, rate=r_mon, other_spikes=e_mon, spike_var_monitors=[e_mon])
+
 SCENARIOS = {
     "lif_refractory": lif_refractory,
     "hetero_delays": hetero_delays,
@@ -653,6 +682,7 @@ SCENARIOS = {
     "end_monitor": end_monitor,
     "host_sets": host_sets,
     "spike_vars": spike_vars,
+    "custom_events": custom_events,
 }
 
 

@@ -191,8 +191,9 @@ def render_oracle(spec: dict) -> str:
     # uploads / downloads through a switch over (group, var)
     w("void* oracle_var(Net* n, int32_t kind, int32_t obj, int32_t var) {")
     for gi, g in enumerate(groups):
+        src = gi if g.get("alias_of") is None else g["alias_of"]
         for vi, v in enumerate(g["vars"]):
-            w(f"  if (kind == 0 && obj == {gi} && var == {vi}) return n->g{gi}_{v['name']}.data();")
+            w(f"  if (kind == 0 && obj == {gi} && var == {vi}) return n->g{src}_{v['name']}.data();")
     for pi, p in enumerate(paths):
         for vi, v in enumerate(p.get("vars", [])):
             w(f"  if (kind == 1 && obj == {pi} && var == {vi}) return n->p{pi}_{v['name']}.data();")
@@ -271,7 +272,8 @@ def render_oracle(spec: dict) -> str:
 
     def gptrs(gi, indent):
         g = groups[gi]
-        return _ind("\n".join(f"{v['ctype']}* const {v['ptr']} = n->g{gi}_{v['name']}.data(); (void){v['ptr']};"
+        src = gi if g.get("alias_of") is None else g["alias_of"]  # (a custom event's group: its parent's state)
+        return _ind("\n".join(f"{v['ctype']}* const {v['ptr']} = n->g{src}_{v['name']}.data(); (void){v['ptr']};"
                               for v in g["vars"]), indent)
 
     def extra(block, indent):
@@ -409,8 +411,9 @@ def render_oracle(spec: dict) -> str:
         w(f"      const std::vector<int32_t>& sp = n->spk{gi};")
         w(f"      for (int32_t idx : sp) if (idx >= n->sm{mi}_lo && idx < n->sm{mi}_hi) {{")
         w(f"        n->sm{mi}_i.push_back(idx - n->sm{mi}_lo); n->sm{mi}_ts.push_back((int32_t)n->ts); n->sm{mi}_count[idx - n->sm{mi}_lo]++;")
+        src = gi if groups[gi].get("alias_of") is None else groups[gi]["alias_of"]  # (an event monitor: the group's state)
         for k in m.get("vars", []):  # (spikemonitor.cpp:37-47: _source_<var>[idx] after the thresholder)
-            w(f"        n->sm{mi}_vals.push_back((double)n->g{gi}_{groups[gi]['vars'][k]['name']}[idx]);")
+            w(f"        n->sm{mi}_vals.push_back((double)n->g{src}_{groups[gi]['vars'][k]['name']}[idx]);")
         w("      }")
         w("    }")
     def emit_inputs():
@@ -472,8 +475,13 @@ def render_oracle(spec: dict) -> str:
         w("    }")
     if not inputs_done:
         emit_inputs()
-    # resets
+    # resets (a group's and its custom events' in the schedule's order)
+    reset_seq = []
     for gi, g in enumerate(groups):
+        if g.get("alias_of") is None:
+            reset_seq += g.get("reset_order") or [gi]
+    for gi in reset_seq:
+        g = groups[gi]
         if not g.get("reset"):
             continue
         w("    {")
@@ -745,7 +753,7 @@ def run_job_on_oracle(directory):
     sizes = [int(init[f"g{gi}_N"]) for gi in range(len(spec["groups"]))]
     o = OracleNet(spec, sizes, job["dt"])
     for gi, g in enumerate(spec["groups"]):
-        for v in g["vars"]:
+        for v in g["vars"] if g.get("alias_of") is None else []:  # (a custom event's group shares them)
             o.upload(gi, v["name"], init[f"g{gi}_{v['name']}"])
         if g.get("generator"):
             o.set_generator(gi, init[f"g{gi}_gen_bins"], init[f"g{gi}_gen_index"], int(init[f"g{gi}_gen_period"]),
@@ -778,7 +786,7 @@ def run_job_on_oracle(directory):
         apply_actions(job, init, k, download, upload)
     out = {}
     for gi, g in enumerate(spec["groups"]):
-        for v in g["vars"]:
+        for v in g["vars"] if g.get("alias_of") is None else []:
             out[f"g{gi}_{v['name']}"] = o.download(gi, v["name"])
         if g.get("generator"):
             out[f"g{gi}_gen_last"] = np.int64(o.generator_cursor(gi))

@@ -24,7 +24,8 @@ EXACT = {"lif_refractory": True, "hetero_delays": False, "subgroup_monitors": Tr
          "presynaptic_read": False, "spike_generator": True, "stdp": False,
          "gap_junctions": True, "explicit_methods": True, "poisson_input": False, "poisson_drive": True,
          "noise_inputs": False, "regular_ops": True,
-         "end_monitor": True, "host_sets": True, "spike_vars": True}
+         "end_monitor": True, "host_sets": True, "spike_vars": True,
+         "custom_events": True}
 
 
 @pytest.mark.parametrize("name", sorted(EXACT))
