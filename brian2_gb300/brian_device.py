@@ -436,6 +436,7 @@ class B200Device(CPPStandaloneDevice):
         draw_sites = []  # (position in the schedule, site, the block or input whose code draws)
         b200_objects = []
         push_names = {}  # pathway -> its push code object (for the profile)
+        syn_frags = []  # per-synapse code (clock-driven equations, run_regularly) and monitors of Synapses
         for pos, obj in enumerate(objects):
             if not obj.active:
                 continue
@@ -450,6 +451,9 @@ class B200Device(CPPStandaloneDevice):
                     raise NotImplementedError("b200: binomial functions outside PoissonInput")
                 if isinstance(obj, PoissonInput):
                     input_frags.append((obj, frag, pos))
+                elif t in ("stateupdate", "statemonitor") and isinstance(
+                        getattr(obj, "source" if t == "statemonitor" else "group", None), Synapses):
+                    syn_frags.append((obj, frag, pos, t, co.name))
                 elif type(obj) is CodeRunner and t == "stateupdate":
                     op_frags.append((obj, frag, pos))
                 elif t in ("stateupdate", "threshold", "reset"):
@@ -618,6 +622,55 @@ class B200Device(CPPStandaloneDevice):
                                tgt_var=tnames.index(tkw["_target_var"].name),
                                index_post=tkw["_index_var"].name == "_synaptic_post",
                                group_ptrs=neuron_ptrs(frag), code=block(frag)))
+        # per-synapse code of a Synapses object (its clock-driven equations,
+        # synapses.py:779-794, and run_regularly operations) and state monitors
+        # recording its variables: over its synapses, held by its first pathway or
+        # by a pathway that delivers no events
+        def syn_pathway(syn):
+            pi = next((k for k, p in enumerate(pathways) if p["_syn"] == syn.name), None)
+            if pi is None:
+                sgi, srange = group_of(syn.source)
+                tg2, trange = group_of(syn.target)
+                pathways.append(dict(name=syn.name + "_synapses", src=sgi, tgt=tg2, vars=[],
+                                     pre_ptr=gen_name(syn.variables["_synaptic_pre"]),
+                                     post_ptr=gen_name(syn.variables["_synaptic_post"]),
+                                     group_ptrs={}, on_pre=dict(scalar="", vector=""), events=False,
+                                     _obj=syn, _src_range=srange, _tgt_range=trange, _syn=syn.name))
+                pi = len(pathways) - 1
+            return pi
+
+        synops = []
+        for obj, frag, pos, t, co_name in syn_frags:
+            syn = obj.source if t == "statemonitor" else obj.group
+            pi = syn_pathway(syn)
+            every = int(round(float(obj.clock.dt_) / float(clock.dt_)))
+            if abs(every * float(clock.dt_) - float(obj.clock.dt_)) > 1e-9 * float(clock.dt_):
+                raise NotImplementedError(f"b200: {obj.name} runs every {float(obj.clock.dt_)} s (not a whole "
+                                          "number of steps)")
+            if obj.when not in ("start", "groups", "end") or (t == "statemonitor" and obj.when == "groups"):
+                raise NotImplementedError(f"b200: {obj.name} in the '{obj.when}' slot (synaptic code and monitors "
+                                          "run in the start, groups (code) and end slots)")
+            if t == "statemonitor":
+                names = list(obj.record_variables)
+                own = {v["name"] for v in synaptic_vars(syn, {"variables": {k: syn.variables[k] for k in names
+                                                                            if k in syn.variables}})}
+                for v in names:
+                    if v not in own:
+                        raise NotImplementedError(f"b200: recording '{v}' of {syn.name} (not a synaptic variable)")
+                have = {v["name"] for v in pathways[pi]["vars"]}
+                pathways[pi]["vars"] += [dict(name=v, ctype=c_data_type(syn.variables[v].dtype),
+                                              ptr=gen_name(syn.variables[v])) for v in sorted(own - have)]
+                statemons.append(dict(name=obj.name, group=-1, syn=pi, _obj=obj, _range=(0, 0), when=obj.when,
+                                      every=every, _vars=names, pos=pos))
+                continue
+            b = block(frag)
+            if "_rand(" in b["vector"] or "_randn(" in b["vector"] or b.get("vector_device"):
+                raise NotImplementedError(f"b200: random numbers in the per-synapse code of {syn.name}")
+            if neuron_ptrs(frag) or collect(frag, {syn.name}):
+                raise NotImplementedError(f"b200: per-synapse code of {syn.name} reading neuron variables")
+            have = {v["name"] for v in pathways[pi]["vars"]}
+            pathways[pi]["vars"] += [v for v in synaptic_vars(syn, frag) if v["name"] not in have]
+            synops.append(dict(name=obj.name, pathway=pi, when=obj.when, every=every, code=b, _co=co_name, pos=pos))
         # Poisson inputs (brian2/input/poissoninput.py:20-141): a state update in the
         # synapses slot, after the on_pre pathways (order -1) and before the
         # on_post pathways (order +1), drawing one binomial count per neuron
@@ -766,6 +819,10 @@ class B200Device(CPPStandaloneDevice):
                     state_monitors=statemons, clock_ptrs=clock_ptrs)
         if summed:
             spec["summed"] = summed
+        if synops:
+            if summed:
+                raise NotImplementedError("b200: per-synapse code together with summed variables")
+            spec["syn_ops"] = synops
         if draws:
             spec["draws"] = draws
         # every array the code of the step loop names must be one the device

@@ -290,9 +290,14 @@ def render_model(spec: dict) -> str:
             lines.append(f"#define _b200_draw_{si}_{c}(i) ({cast}_b200_rv{si}[(int64_t)(i) * {calls} + {c}])")
             undef.append(f"#undef _b200_draw_{si}_{c}")
         return lines, undef
+    # per-synapse code of a Synapses object (clock-driven equations, run_regularly)
+    # and state monitors of its variables, over its synapses in CSR order
+    SYNOPS = spec.get("syn_ops", [])
+    SYNMONS = [(mi, m) for mi, m in enumerate(statemons) if m.get("syn", -1) >= 0]
     for pi, p in enumerate(paths):
         blocks = [("on_pre", _block(p.get("on_pre")))]
         blocks += [(f"summed{si}", _block(sm["code"])) for si, sm in enumerate(SUMMED) if sm["pathway"] == pi]
+        blocks += [(f"synop{j}", _block(op["code"])) for j, op in enumerate(SYNOPS) if op["pathway"] == pi]
         ptables.append((_Tables(consts, blocks, (clock["t"], clock["timestep"])), blocks))
 
     SIZE = {"double": 8, "int64_t": 8, "float": 4, "int32_t": 4, "char": 1, "int8_t": 1}
@@ -366,7 +371,8 @@ def render_model(spec: dict) -> str:
         target neuron, values computed from synaptic variables and constants.
         Returns, per pathway, the synaptic variables an event carries (indices
         into the pathway's variables), or None for the whole model."""
-        if not paths or SUMMED or any(p.get("alias", -1) >= 0 or not p.get("events", True) for p in paths):
+        if not paths or SUMMED or SYNOPS or SYNMONS or \
+                any(p.get("alias", -1) >= 0 or not p.get("events", True) for p in paths):
             return None
         for g in groups:
             for blk in ("update", "threshold", "reset"):
@@ -443,7 +449,8 @@ def render_model(spec: dict) -> str:
     for nm, mons in (("spkmon", spkmons), ("ratemon", ratemons), ("statemon", statemons)):
         if mons:
             w(f"static const b200_mon_info b200_{nm}[] = {{" + ", ".join(
-                f'{{"{m["name"]}", {m["group"]}, {m.get("every", 1)}, {len(m.get("vars", []))}}}' for m in mons) + "};")
+                f'{{"{m["name"]}", {m["group"]}, {m.get("every", 1)}, {len(m.get("vars", [])) if nm == "spkmon" else 0}, '
+                f'{m.get("syn", -1)}}}' for m in mons) + "};")
         else:
             w(f"static const b200_mon_info* const b200_{nm} = nullptr;")
     w("")
@@ -614,6 +621,66 @@ def render_model(spec: dict) -> str:
                   "      }",
                   "    }",
                   "  }"]
+        L.append("}")
+        return _indent("\n".join(L), indent)
+
+    def syn_text(indent, tsexpr, when):
+        """The per-synapse code and the synaptic state monitors of slot `when`
+        of step `tsexpr`, in schedule order, over this CTA's share of each
+        Synapses object's synapses (a contiguous range of CSR positions); each
+        on the steps of its clock.  Ends with a barrier of the CTA."""
+        items = [("op", j, op) for j, op in enumerate(SYNOPS) if op["when"] == when] + \
+                [("mon", mi, m) for mi, m in SYNMONS if m.get("when", "start") == when]
+        if not items:
+            return ""
+        items.sort(key=lambda x: x[2].get("pos", 0))
+        L = ["{",
+             f"  const double _b200_t = (double)({tsexpr}) * _b200_dt; (void)_b200_t;",
+             f"  const int64_t _b200_ts = {tsexpr}; (void)_b200_ts;"]
+        for kind, j, it in items:
+            pi = it["pathway"] if kind == "op" else it["syn"]
+            p = paths[pi]
+            every = int(it.get("every", 1))
+            L += [f"  if (_b200_ts % {every} == 0) {{  // {'code' if kind == 'op' else 'state monitor'} '{it['name']}'",
+                  f"    const b200_pathway_d& PQ = I.p[{pi}];",
+                  "    const int64_t _q0 = PQ.n_syn * rank / I.n_cta, _q1 = PQ.n_syn * (rank + 1) / I.n_cta;"]
+            if kind == "op":
+                tab = ptables[pi][0]
+                L += [f"    const double* const _b200_S = s_Sp{pi}; const float* const _b200_Sf = s_Sp{pi}f; "
+                      f"const long long* const _b200_Si = s_Sp{pi}i;",
+                      "    (void)_b200_S; (void)_b200_Sf; (void)_b200_Si;"]
+                for k, v in enumerate(p.get("vars", [])):
+                    L.append(f"    {v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)PQ.var[{k}]; (void){v['ptr']};")
+                L += [f"    const int32_t* __restrict__ const {p['pre_ptr']} = PQ.pre; (void){p['pre_ptr']};",
+                      f"    const int32_t* __restrict__ const {p['post_ptr']} = PQ.post; (void){p['post_ptr']};",
+                      _indent(tab.device_loads(f"synop{j}", f32), 4),
+                      _indent(_device(tab.time_code(f"synop{j}")), 4),
+                      "    for (int64_t _idx = _q0 + threadIdx.x; _idx < _q1; _idx += blockDim.x) {",
+                      "      const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;",
+                      "      {",
+                      _indent(it["code"]["vector"], 8),
+                      "      }",
+                      "    }"]
+            else:
+                rec = ("_b200_ts - SM.step0" if every == 1 else
+                       f"_b200_ts / {every} - (SM.step0 + {every - 1}) / {every}")
+                L += [f"    const b200_statemon_d& SM = I.stm[{j}];",
+                      f"    const int64_t rec = {rec};  // row of this step",
+                      "    double* const row = SM.data + (size_t)rec * SM.n_vars * SM.n_rec;",
+                      "    for (int k = threadIdx.x; k < SM.n_rec * SM.n_vars; k += blockDim.x) {",
+                      "      const int r = k % SM.n_rec, v = k / SM.n_rec;",
+                      "      const int64_t pos = SM.idx[r];  // the synapse's CSR position",
+                      "      if (pos >= _q0 && pos < _q1) {",
+                      "        double val = 0.0;",
+                      "        switch (SM.var_id[v]) {"]
+                for k, v in enumerate(p.get("vars", [])):
+                    L.append(f"          case {k}: val = (double)(({v['ctype']}*)PQ.var[{k}])[pos]; break;")
+                L += ["        }",
+                      "        row[k] = val;",
+                      "      }",
+                      "    }",
+                      f"    if (threadIdx.x == 0) s_stm_n[{j}] = rec + 1;"]
+            L += ["  }", "  __syncthreads();"]
         L.append("}")
         return _indent("\n".join(L), indent)
 
@@ -941,6 +1008,19 @@ def render_model(spec: dict) -> str:
         """Reset of the previous step, state monitors, update + threshold with
         ordered compaction of this CTA's tiles."""
         # ---- Phase A
+        if not owner and (SYNOPS or SYNMONS):
+            # per-synapse code and synaptic monitors: after the previous step's
+            # deliveries (its end slot), then this step's start and groups slots;
+            # the step's deliveries follow the barrier
+            end = syn_text(8, "ts - 1", "end")
+            if end:
+                w("      if (ts > ts0) {")
+                w(end)
+                w("      }")
+            for when in ("start", "groups"):
+                txt = syn_text(6, "ts", when)
+                if txt:
+                    w(txt)
         for gi, g in enumerate(groups):
             tab, blocks = gtables[gi]
             bd = dict(blocks)
@@ -1295,7 +1375,7 @@ def render_model(spec: dict) -> str:
     w("    bool ok = true;")
     # deliveries read no spikes of their own step; not in the variants capped at
     # 64 registers (their code would spill; they serve single-CTA instances)
-    w("    const bool lagm = (MAXT * MINB < 1024) && I.lag && I.n_cta > 1;")
+    w(f"    const bool lagm = (MAXT * MINB < 1024) && I.lag && I.n_cta > 1{' && false' if SYNOPS else ''};")
     w("    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, NW = blockDim.x >> 5;")
     w(f"    // per-phase device profile (thread 0 of each CTA; phases: A, barrier A, spike lists,")
     w(f"    // {NP} pathway(s), barrier B)")
@@ -1784,6 +1864,9 @@ def render_model(spec: dict) -> str:
         rb = deferred_block(gi, 6, "ts - 1")
         if rb:
             w(rb)
+    end = syn_text(6, "ts - 1", "end")
+    if end:
+        w(end)
     w("    }")
     w("    __syncthreads();")
     w("    if (s_cache) {")

@@ -242,6 +242,7 @@ struct b200_mon_info {
   int group;
   int every;   // records on every k-th step (a state monitor on a slower clock); 1 otherwise
   int n_vars;  // a spike monitor's recorded variables besides i and t
+  int syn;     // a state monitor of a Synapses object: the pathway holding its synapses; -1 otherwise
 };
 struct b200_model_info {
   const char* name;

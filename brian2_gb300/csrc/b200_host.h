@@ -580,11 +580,15 @@ int b200_set_statemon(b200_net* n, int32_t inst, int32_t mon, const int32_t* idx
   if (!n || inst < 0 || inst >= n->n_inst || mon < 0 || mon >= n->M->n_statemon) return B200_ERR_ARG;
   if (n_vars > 8 || n_vars < 0 || n_rec < 0) return b200_fail(n, B200_ERR_ARG, "bad state monitor");
   b200_statemon_h& S = n->inst[inst].stm[mon];
-  const int g = n->M->statemon[mon].group;
+  const int g = n->M->statemon[mon].group, sp = n->M->statemon[mon].syn;
+  // a neuron group's monitor: neuron indices; a Synapses object's: synapse indices (creation
+  // order, checked against the synapses when the run is prepared)
   for (int k = 0; k < n_rec; ++k)
-    if (idx[k] < 0 || idx[k] >= n->inst[inst].g[g].N) return b200_fail(n, B200_ERR_INDEX, "bad record index");
+    if (idx[k] < 0 || (sp < 0 && idx[k] >= n->inst[inst].g[g].N))
+      return b200_fail(n, B200_ERR_INDEX, "bad record index");
+  const int nv = sp < 0 ? n->M->groups[g].n_vars : n->M->pathways[sp].n_vars;
   for (int k = 0; k < n_vars; ++k)
-    if (vars[k] < 0 || vars[k] >= n->M->groups[g].n_vars) return b200_fail(n, B200_ERR_ARG, "bad var");
+    if (vars[k] < 0 || vars[k] >= nv) return b200_fail(n, B200_ERR_ARG, "bad var");
   S.idx.assign(idx, idx + n_rec);
   S.vars.assign(vars, vars + n_vars);
   S.n_rec = n_rec;
@@ -984,13 +988,27 @@ static int b200_prepare(b200_net* n) {
       SD.n_rec = S.n_rec;
       SD.n_vars = S.n_vars;
       if ((r = b200_alloc(n, S.d_idx, (size_t)std::max(S.n_rec, 1) * 4, false))) return r;
+      const int sp = M->statemon[s].syn;
+      std::vector<int32_t> rec(S.idx);
+      if (sp >= 0 && S.n_rec) {  // synapse index -> its position in the synapses' CSR order
+        const b200_pathway_h& P = I.p[sp];
+        if (P.n_syn > INT32_MAX) return b200_fail(n, B200_ERR_ARG, "state monitor of more than 2^31 synapses");
+        std::vector<int32_t> inv((size_t)P.n_syn);
+        for (int64_t q = 0; q < P.n_syn; ++q) inv[(size_t)P.perm[q]] = (int32_t)q;
+        for (auto& x : rec) {
+          if (x < 0 || x >= P.n_syn) return b200_fail(n, B200_ERR_INDEX, "state monitor %d: no synapse %d", s, x);
+          x = inv[(size_t)x];
+        }
+      }
       if (S.n_rec)
-        B200_CU(n, cudaMemcpyAsync(S.d_idx.p, S.idx.data(), (size_t)S.n_rec * 4, cudaMemcpyHostToDevice, n->stream));
+        B200_CU(n, cudaMemcpyAsync(S.d_idx.p, rec.data(), (size_t)S.n_rec * 4, cudaMemcpyHostToDevice, n->stream));
+      B200_CU(n, cudaStreamSynchronize(n->stream));
       if (!S.n.p && (r = b200_alloc(n, S.n, 16))) return r;
       SD.idx = (const int32_t*)S.d_idx.p;
       for (int v = 0; v < S.n_vars; ++v) {
         SD.var_id[v] = S.vars[v];
-        SD.var_dbl[v] = M->groups[SD.group].var_kind[S.vars[v]] == B200_F64;
+        SD.var_dbl[v] = (sp >= 0 ? M->pathways[sp].var_kind[S.vars[v]] : M->groups[SD.group].var_kind[S.vars[v]]) ==
+                        B200_F64;
       }
       SD.n = (int64_t*)S.n.p;
     }

@@ -288,10 +288,12 @@ class Network:
 
     def set_statemon(self, inst, mon, indices, variables):
         m = mon if isinstance(mon, int) else self.model.statemon_index[mon]
-        g = self.model.spec["state_monitors"][m]["group"]
+        sm = self.model.spec["state_monitors"][m]
+        # a Synapses object's monitor: synapse indices and that pathway's variables
+        names = (self.model.tables["pathways"][sm["syn"]] if sm.get("syn", -1) >= 0
+                 else self.model.tables["groups"][sm["group"]])
         idx = np.ascontiguousarray(indices, dtype=np.int32)
-        vs = np.ascontiguousarray([v if isinstance(v, int) else self.model.tables["groups"][g].index(v)
-                                   for v in variables], dtype=np.int32)
+        vs = np.ascontiguousarray([v if isinstance(v, int) else names.index(v) for v in variables], dtype=np.int32)
         self._check(self.lib.b200_set_statemon(self._h, int(inst), m, _ptr(idx, _i32p), idx.size,
                                                _ptr(vs, _i32p), vs.size))
         self.__dict__.setdefault("_statemon_shape", {})[(inst, m)] = (vs.size, idx.size)

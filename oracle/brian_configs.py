@@ -665,6 +665,35 @@ def custom_events(N=300, duration_ms=200.0, seed_value=808):
     run(duration_ms * ms)
     return dict(P=P, spikes=s_mon, rate=r_mon, other_spikes=e_mon, spike_var_monitors=[e_mon])
 
+
+def synaptic_state(N=300, duration_ms=150.0, seed_value=909):
+    """Per-synapse state of a Synapses object: a clock-driven trace x
+    (``synapses/synapses.py:779-794``, the groups slot) that on_pre also
+    raises, ``run_regularly`` code on the synapses every 1 ms changing the
+    weights from the trace, and state monitors of synaptic variables (start
+    slot, several synapses; end slot, one)."""
+    from brian2 import (NeuronGroup, Synapses, SpikeMonitor, PopulationRateMonitor, StateMonitor, ms, mV, seed,
+                        run)
+    seed(seed_value)
+    ns = dict(taum=20 * ms, taue=5 * ms, taux=15 * ms, Vt=-50 * mV, Vr=-60 * mV, El=-49 * mV, we=0.6 * mV,
+              dw=0.02 * mV, wmax=1.5 * mV)
+    P = NeuronGroup(N, '''dv/dt = (ge - (v - El))/taum : volt
+                          dge/dt = -ge/taue : volt''',
+                    threshold='v>Vt', reset='v = Vr', method='exact', namespace=ns)
+    P.v = 'Vr + rand() * (Vt - Vr)'
+    S = Synapses(P, P, '''w : volt
+                          dx/dt = -x/taux : 1 (clock-driven)''',
+                 on_pre='ge += w; x += 1', delay=0.2 * ms, namespace=ns)
+    S.connect(p=0.05)
+    S.w = 'we * (0.5 + rand())'
+    S.run_regularly('w = clip(w + dw * (x - 0.5), 0*mV, wmax)', dt=1 * ms)
+    st = StateMonitor(S, ['w', 'x'], record=[0, 7, 42, 100])
+    st_end = StateMonitor(S, 'w', record=[3], when='end')
+    s_mon = SpikeMonitor(P)
+    r_mon = PopulationRateMonitor(P)
+    run(duration_ms * ms)
+    return dict(P=P, spikes=s_mon, rate=r_mon, S=S, syn_vars=['w', 'x'], syn_state=[st, st_end])
+
 SCENARIOS = {
     "lif_refractory": lif_refractory,
     "hetero_delays": hetero_delays,
@@ -683,6 +712,7 @@ SCENARIOS = {
     "host_sets": host_sets,
     "spike_vars": spike_vars,
     "custom_events": custom_events,
+    "synaptic_state": synaptic_state,
 }
 
 

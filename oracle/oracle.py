@@ -305,9 +305,48 @@ def render_oracle(spec: dict) -> str:
 
     def emit_statemons(when):
         for mi, m in enumerate(statemons):
-            if m.get("when", "start") != when:
+            if m.get("when", "start") != when or m.get("syn", -1) >= 0:
                 continue
             emit_statemon(mi, m)
+
+    def emit_syn(when):
+        """Per-synapse code (clock-driven synaptic equations, run_regularly of a
+        Synapses object; templates/stateupdate.cpp over the synapses) and state
+        monitors of synaptic variables in the slot, in schedule order, over the
+        synapses in creation order."""
+        items = [("op", op) for op in spec.get("syn_ops", []) if op["when"] == when] + \
+                [("mon", (mi, m)) for mi, m in enumerate(statemons) if m.get("syn", -1) >= 0 and
+                 m.get("when", "start") == when]
+        items.sort(key=lambda x: (x[1] if x[0] == "op" else x[1][1]).get("pos", 0))
+        for kind, it in items:
+            if kind == "mon":
+                mi, m = it
+                pi = m["syn"]
+                w(f"    if (n->ts % {int(m.get('every', 1))} == 0) {{  // synaptic state monitor '{m['name']}'")
+                w(f"      for (size_t v = 0; v < n->st{mi}_vars.size(); ++v) for (size_t r = 0; r < n->st{mi}_idx.size(); ++r) {{")
+                w("        double val = 0;")
+                for vi, v in enumerate(paths[pi].get("vars", [])):
+                    w(f"        if (n->st{mi}_vars[v] == {vi}) val = (double)n->p{pi}_{v['name']}[n->st{mi}_idx[r]];")
+                w(f"        n->st{mi}_data.push_back(val);")
+                w("      }")
+                w(f"      n->st{mi}_n++;")
+                w("    }")
+                continue
+            pi = it["pathway"]
+            p = paths[pi]
+            w(f"    if (n->ts % {it['every']} == 0) {{  // per-synapse code '{it['name']}'")
+            for v in p.get("vars", []):
+                w(f"      {v['ctype']}* const {v['ptr']} = n->p{pi}_{v['name']}.data(); (void){v['ptr']};")
+            w(f"      int32_t* const {p['pre_ptr']} = n->p{pi}_pre.data(); (void){p['pre_ptr']};")
+            w(f"      int32_t* const {p['post_ptr']} = n->p{pi}_post.data(); (void){p['post_ptr']};")
+            w("      {")
+            w(_ind(it["code"]["scalar"], 8))
+            w(f"        for (int64_t _idx = 0; _idx < (int64_t)n->p{pi}_pre.size(); ++_idx) {{")
+            w("          const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+            w(_ind(it["code"]["vector"], 10))
+            w("        }")
+            w("      }")
+            w("    }")
 
     def emit_statemon(mi, m):
         gi = m["group"]
@@ -325,6 +364,8 @@ def render_oracle(spec: dict) -> str:
     # operations of the start slot, then the state monitors (start of the step)
     emit_ops("start")
     emit_statemons("start")
+    emit_syn("start")
+    emit_syn("groups")
     # summed variables (groups slot, before the groups' updates)
     for si, sm in enumerate(spec.get("summed", [])):
         pi, gi = sm["pathway"], sm["tgt_group"]
@@ -501,6 +542,7 @@ def render_oracle(spec: dict) -> str:
         w(f"    {{ int c = 0; for (int32_t idx : n->spk{gi}) if (idx >= n->rm{mi}_lo && idx < n->rm{mi}_hi) ++c; n->rm{mi}_cnt.push_back(c); }}")
     emit_ops("end")  # (the rate monitors count spikes, which the operations do not change)
     emit_statemons("end")
+    emit_syn("end")
     w("    n->ts += 1;")
     w("  }")
     w("}")
@@ -647,8 +689,11 @@ class OracleNet:
         self.lib.oracle_set_range(self.h, 1, int(mon), int(lo), int(hi))
 
     def set_statemon(self, mon, indices, variables):
-        g = self.spec["state_monitors"][mon]["group"]
-        names = [v["name"] for v in self.spec["groups"][g]["vars"]]
+        sm = self.spec["state_monitors"][mon]
+        if sm.get("syn", -1) >= 0:  # a Synapses object's monitor: its pathway's variables
+            names = [v["name"] for v in self.spec["pathways"][sm["syn"]]["vars"]]
+        else:
+            names = [v["name"] for v in self.spec["groups"][sm["group"]]["vars"]]
         idx = np.ascontiguousarray(indices, np.int32)
         vs = np.ascontiguousarray([v if isinstance(v, int) else names.index(v) for v in variables], np.int32)
         self.lib.oracle_set_statemon(self.h, int(mon), idx.ctypes.data_as(_i32p), idx.size,

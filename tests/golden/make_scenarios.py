@@ -89,6 +89,12 @@ def run_ref(name):
             for var in names:
                 out[f"smv_{mon.name}_{var}"] = np.asarray(getattr(mon, var + "_")[:]).copy()
             meta["spike_var_monitors"][mon.name] = names
+    if "syn_state" in r:                       # state monitors of synaptic variables: [n_rec, steps]
+        meta["syn_state_monitors"] = {}
+        for mon in r["syn_state"]:
+            for var in mon.record_variables:
+                out[f"sst_{mon.name}_{var}"] = np.asarray(getattr(mon, var + "_")[:]).copy()
+            meta["syn_state_monitors"][mon.name] = list(mon.record_variables)
     if "syn_vars" in r:                        # synaptic variables (creation order)
         for var in r["syn_vars"]:
             out["syn_" + var] = np.asarray(getattr(r["S"], var + "_")[:]).copy()

@@ -25,14 +25,14 @@ EXACT = {"lif_refractory": True, "hetero_delays": False, "subgroup_monitors": Tr
          "gap_junctions": True, "explicit_methods": True, "poisson_input": False, "poisson_drive": True,
          "noise_inputs": False, "regular_ops": True,
          "end_monitor": True, "host_sets": True, "spike_vars": True,
-         "custom_events": True}
+         "custom_events": True, "synaptic_state": False}
 
 
 @pytest.mark.parametrize("name", sorted(EXACT))
 @pytest.mark.parametrize("ctas,owner", [(1, "auto"), (4, True), (4, False), (20, "auto")])
 def test_scenario_matches_reference(name, ctas, owner):
     jobdir = os.path.join(HERE, "golden", "jobs", name)
-    spec, _, job = load_job(jobdir)
+    spec, init, job = load_job(jobdir)
     with np.load(os.path.join(HERE, "golden", "scenarios", name + ".npz")) as z:
         ref = {k: z[k] for k in z.files}
     with open(os.path.join(HERE, "golden", "scenarios", name + ".json")) as f:
@@ -74,6 +74,12 @@ def test_scenario_matches_reference(name, ctas, owner):
         np.testing.assert_array_equal(tr, ref["state_v"])
     if "state_Igap" in ref:                        # a second recorded variable (a summed one)
         np.testing.assert_array_equal(out["stm0_trace"][:, 1, :].T, ref["state_Igap"])
+    for mname, names in meta.get("syn_state_monitors", {}).items():  # synaptic variables over time
+        mi = [m["name"] for m in spec["state_monitors"]].index(mname)
+        cols = [str(x) for x in init[f"stm{mi}_vars"]]
+        for var in names:
+            np.testing.assert_array_equal(out[f"stm{mi}_trace"][:, cols.index(var), :].T, ref[f"sst_{mname}_{var}"],
+                                          err_msg=f"{mname}.{var}")
     for var in meta.get("syn_vars", []):           # plastic synapses (on_pre and on_post share them)
         pi = next(k for k, p in enumerate(spec["pathways"])
                   if p["name"].startswith(meta["synapses"] + "_") and p.get("alias", -1) < 0)

@@ -26,6 +26,7 @@ def test_oracle_reproduces_reference_scenario(name):
     with open(os.path.join(HERE, "golden", "scenarios", name + ".json")) as f:
         meta = json.load(f)
     out = run_job_on_oracle(jobdir)
+    init = np.load(os.path.join(jobdir, "init.npz"))
     mons = [m["name"] for m in spec["spike_monitors"]]
     sm = mons.index(meta.get("spike_monitor", mons[0]))
     np.testing.assert_array_equal(out[f"sm{sm}_i"], ref["spk_i"])
@@ -57,6 +58,12 @@ def test_oracle_reproduces_reference_scenario(name):
         np.testing.assert_array_equal(out["stm0_trace"][:, 0, :].T, ref["state_v"])
     if "state_Igap" in ref:                      # a second recorded variable (a summed one)
         np.testing.assert_array_equal(out["stm0_trace"][:, 1, :].T, ref["state_Igap"])
+    for mname, names in meta.get("syn_state_monitors", {}).items():  # synaptic variables over time
+        mi = [m["name"] for m in spec["state_monitors"]].index(mname)
+        cols = [str(x) for x in init[f"stm{mi}_vars"]]
+        for var in names:
+            np.testing.assert_array_equal(out[f"stm{mi}_trace"][:, cols.index(var), :].T, ref[f"sst_{mname}_{var}"],
+                                          err_msg=f"{mname}.{var}")
     for var in meta.get("syn_vars", []):        # plastic synapses: final synaptic variables
         pi = next(k for k, p in enumerate(spec["pathways"])
                   if p["name"].startswith(meta["synapses"] + "_") and p.get("alias", -1) < 0)
