@@ -470,6 +470,8 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--chunk-steps", type=int, default=0,
                     help="clock steps per kernel launch (default: one launch per bench step)")
+    ap.add_argument("--push", default="auto", choices=["auto", "on", "off"],
+                    help="push-mode delivery (auto: the library's choice)")
     ap.add_argument("--owner", default="auto", choices=["auto", "on", "off"],
                     help="owner-mode delivery (auto: the library's choice)")
     args = ap.parse_args()
@@ -503,10 +505,12 @@ def main():
         net.configure(threads=threads, ctas_per_inst=ctas, queue_mode=False, chunk_steps=args.chunk_steps,
                       use_graph=False)
     net.set_owner({"auto": "auto", "on": True, "off": False}[args.owner])
+    net.set_push({"auto": "auto", "on": True, "off": False}[args.push])
     t_build = time.perf_counter() - t_build
     outdeg = net.outdegree
     plan = net.launch_plan()
     net_owner = net.owner_active()
+    net_mode = net.delivery_mode()
 
     def bench_step():
         net.run(STEPS_PER_BENCH_STEP)
@@ -599,7 +603,8 @@ def main():
             "data": "synthetic: network constructed on the device from a seed",
             "config": workload_config(N, K),
             "launch": {"clock_steps_per_step": STEPS_PER_BENCH_STEP, "threads": threads, "ctas": ctas,
-                       "launch_plan": plan, "build_s": round(t_build, 2), "owner_mode": net_owner},
+                       "launch_plan": plan, "build_s": round(t_build, 2), "owner_mode": net_owner,
+                       "delivery": net_mode},
             "sim_s_per_wall_s": sim_s / device_s,
             "wall_ms_per_step": wall / args.steps * 1e3,
             "spikes_per_step": float(len(i)) / args.steps,

@@ -187,6 +187,7 @@ class _Tables:
 # state words (4-byte) a thread keeps in flight in phase A's prefetch, in the
 # kernel variants with more than 64 registers
 PF_WORDS = 12
+PF_WORDS_PUSH = 12
 # events per thread whose loads are issued before any is applied (variants
 # with more than 64 registers)
 EVENT_BATCH = 4
@@ -406,6 +407,36 @@ def render_model(spec: dict) -> str:
 
     PAYLOAD = owner_payloads()
     OWNER = PAYLOAD is not None
+    # push mode: owner mode's condition, and every group keeps its own spike lists
+    # (no spike generator, no custom-event group), so that each CTA can deliver
+    # its own neurons' spikes; ACC: the neuron variables that receive deliveries
+    PUSH = OWNER and NP > 0 and not any(g.get("generator") or g.get("alias_of") is not None for g in groups)
+    ACC = sorted({(gi, vi) for p in paths for _, (gi, vi) in p.get("group_ptrs", {}).items() if gi == p["tgt"]})
+    if len(ACC) > 8:
+        PUSH = False
+    ACCI_ = {gv: k for k, gv in enumerate(ACC)}
+
+    def _fusable(gi, vi):
+        """A delivered variable whose deliveries can be added as the update
+        loads it: the update reads it, and nothing that runs between the
+        deliveries and the update (inputs, resets, operations, state monitors)
+        names it, so adding them later changes no value that anything reads."""
+        g = groups[gi]
+        ptr = g["vars"][vi]["ptr"]
+        if not g.get("update") or g["update"].get("vector") is None:
+            return False
+        if ptr not in {p_ for _, _, p_ in split_loads(g["update"]["vector"])[0]}:
+            return False
+        text = json.dumps(g.get("reset") or {}) + json.dumps(g.get("ops", []))
+        text += json.dumps([inp for inp in INPUTS if inp["group"] == gi])
+        if re.search(r"\b%s\b" % re.escape(ptr), text):
+            return False
+        if any(m["group"] == gi for m in statemons):
+            return False  # (its recorded variables are chosen at run time)
+        return True
+
+    FUSED = {gv for gv in ACC if PUSH and _fusable(*gv)}
+
     # device profile slots: classic kernel A, barrier A, lists, one per pathway,
     # barrier B; owner kernel update, barrier, lists, push pass 1, batch table +
     # pass 2, delivery
@@ -519,13 +550,36 @@ def render_model(spec: dict) -> str:
         return (f"I.g[{gi}].ring + (int64_t)(({tsexpr}) % B200_OWNER_RING) * I.g[{gi}].N",
                 f"I.g[{gi}].ring_prefix + (int64_t)(({tsexpr}) % B200_OWNER_RING) * (I.g[{gi}].n_tiles + 1)")
 
-    def reset_block(gi, indent, tsexpr, owner=False):
-        """Reset of the spikes of step `tsexpr` in this CTA's tiles."""
+    def reset_block(gi, indent, tsexpr, owner=False, push=False):
+        """Reset of the spikes of step `tsexpr` in this CTA's tiles (push: from
+        the CTA's compact spike history)."""
         tab, blocks = gtables[gi]
         bd = dict(blocks)
         if bd["reset"] is None:
             return ""
         g = groups[gi]
+        if push:
+            L = ["{",
+                 f"  const double _b200_t = (double)({tsexpr}) * _b200_dt; (void)_b200_t;  // the step of the reset",
+                 f"  const int64_t _b200_ts = {tsexpr}; (void)_b200_ts;",
+                 f"  const int _rsl = (int)(({tsexpr}) % I.g[{gi}].RH), _rcnt = s_hcnt[{gi}][_rsl], _rhc = I.g[{gi}].HCAP;",
+                 f"  const int32_t* const _rhs = s_hist[{gi}] + _rsl * _rhc;",
+                 f"  const int32_t* const _rhg = I.g[{gi}].hist + (int64_t)_rsl * I.g[{gi}].N + s_own[{gi}][0];",
+                 f"  const int32_t N = I.g[{gi}].N; (void)N;",
+                 f"  const double* const _b200_S = s_Sg{gi}; const float* const _b200_Sf = s_Sg{gi}f; const long long* const _b200_Si = s_Sg{gi}i;",
+                 gptr_decls(gi, 2, False),
+                 "  for (int j = threadIdx.x; j < _rcnt; j += blockDim.x) {",
+                 "    const int32_t _idx = j < _rhc ? _rhs[j] : _rhg[j];",
+                 "    const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;",
+                 "    {",
+                 _indent(tab.device_loads("reset", f32), 6),
+                 _indent(_device(tab.time_code("reset")), 6),
+                 extra_ptrs(g.get("reset"), 6),
+                 _indent(bd["reset"]["vector"], 6),
+                 "    }",
+                 "  }",
+                 "}"]
+            return _indent("\n".join(L), indent)
         scr_e, tc_e = owner_list(gi, tsexpr) if owner else (f"s_oscr[{gi}]", f"s_otc[{gi}]")
         L = ["{",
              f"  const double _b200_t = (double)({tsexpr}) * _b200_dt; (void)_b200_t;  // the step of the reset",
@@ -684,13 +738,13 @@ def render_model(spec: dict) -> str:
         L.append("}")
         return _indent("\n".join(L), indent)
 
-    def deferred_block(gi, indent, tsexpr, owner=False):
+    def deferred_block(gi, indent, tsexpr, owner=False, push=False):
         """What the reference runs after the deliveries of step `tsexpr`: the
         Poisson inputs, the reset, the end-slot operations and state monitors
         (this CTA's neurons)."""
         if ALIAS[gi] is not None:
             return ""  # (its reset runs in its parent's block)
-        resets = [reset_block(k, indent, tsexpr, owner) for k in (groups[gi].get("reset_order") or [gi])]
+        resets = [reset_block(k, indent, tsexpr, owner, push) for k in (groups[gi].get("reset_order") or [gi])]
         parts = [x for x in [input_block(gi, indent, tsexpr)] + resets +
                  [op_block(gi, indent, tsexpr, "end"), statemon_text(gi, indent, tsexpr, "end")] if x]
         return ("\n" + " " * indent + "__syncthreads();\n").join(parts)
@@ -1004,9 +1058,11 @@ def render_model(spec: dict) -> str:
         w("        }")
         w("      }")
 
-    def emit_phase_a(owner):
+    def emit_phase_a(owner, push=False, only=None):
         """Reset of the previous step, state monitors, update + threshold with
-        ordered compaction of this CTA's tiles."""
+        ordered compaction of this CTA's tiles.  `push`: the step's spikes are
+        also appended to the CTA's compact spike history (shared memory for the
+        first HCAP of the slot, global memory for all)."""
         # ---- Phase A
         if not owner and (SYNOPS or SYNMONS):
             # per-synapse code and synaptic monitors: after the previous step's
@@ -1022,13 +1078,15 @@ def render_model(spec: dict) -> str:
                 if txt:
                     w(txt)
         for gi, g in enumerate(groups):
+            if only is not None and gi not in only:
+                continue
             tab, blocks = gtables[gi]
             bd = dict(blocks)
             if g.get("generator"):
                 emit_generator(gi, owner)
                 continue
             w(f"      // ---- group {gi} '{g['name']}': phase A (reset of step ts-1, monitors, update + threshold)")
-            dfr = deferred_block(gi, 8, "ts - 1", owner)
+            dfr = deferred_block(gi, 8, "ts - 1", owner, push)
             if not owner:
                 w("      B200_PHASE(0);")
             if dfr and not SUMMED:  # (with summed variables: before the sums)
@@ -1036,7 +1094,7 @@ def render_model(spec: dict) -> str:
                 w(dfr)
                 w("        __syncthreads();")
                 w("      }")
-                if not owner:
+                if not owner or push:
                     w(f"      B200_PHASE({PH_RST(gi)});  // reset of the previous step")
             sop = op_block(gi, 6, "ts", "start")
             if sop and not SUMMED:  # the start-slot operations of this step
@@ -1046,7 +1104,9 @@ def render_model(spec: dict) -> str:
             w(f"        const int32_t N = I.g[{gi}].N; (void)N;")
             w(f"        const double* const _b200_S = s_Sg{gi}; const float* const _b200_Sf = s_Sg{gi}f; const long long* const _b200_Si = s_Sg{gi}i;")
             w(gptr_decls(gi, 8, True))
-            if owner:
+            if push:
+                pass  # (the step's list goes to the compact history only)
+            elif owner:
                 scr_e, tc_e = owner_list(gi, "ts")
                 w(f"        int32_t* const scr = {scr_e}; int32_t* const tcnt = {tc_e};")
             else:
@@ -1075,6 +1135,11 @@ def render_model(spec: dict) -> str:
                         w(_indent(tab.scalar_loads(blk_name, f32), 8))
                         w(_indent(_device(tab.time_code(blk_name)), 8))
             quad = (not owner) and not rng and emit_quad(gi, g, bd, tab, hoist_sc)
+            if push:
+                w("        int _hrun = 0;  // spikes of this CTA's earlier tiles this step")
+                w(f"        const int _hslot = _hs{gi}, _hcap = I.g[{gi}].HCAP;")
+                w(f"        int32_t* const _hsh = s_hist[{gi}] + _hslot * _hcap;")
+                w(f"        int32_t* const _hgl = I.g[{gi}].hist + (int64_t)_hslot * I.g[{gi}].N + s_own[{gi}][0];")
             w(f"        for (int u = s_ut[{gi}][0]; u < s_ut[{gi}][1]; ++u) {{")
             w("          const int start = tst[u], end = tst[u + 1];")
             w("          int cnt = 0;")
@@ -1092,11 +1157,21 @@ def render_model(spec: dict) -> str:
             for ct, nm, ptr in upd_loads + [x for x in thr_loads if x[2] not in upd_st]:
                 pf.setdefault(ptr, ct)
             pfi = {ptr: j for j, ptr in enumerate(pf)}
+            # push mode: the deliveries due at ts-1 of a fused variable are added as
+            # the update loads it (buffer (ts-1) % 3; cleared in the compute loop,
+            # since a store right behind the load of the same word would wait for it)
+            fz = {v["ptr"]: ACCI_[(gi, k)] for k, v in enumerate(g["vars"])
+                  if v["ptr"] in pf and (gi, k) in FUSED} if push else {}
+            for ptr, a in fz.items():
+                w(f"            {pf[ptr]}* const _facc{pfi[ptr]} = ({pf[ptr]}*)I.acc[{a}] + (size_t)((ts + 2) % B200_PUSH_BUFS) * I.g[{gi}].N;")
+
             words = sum(max(1, SIZE.get(ct, 8) // 4) for ct in pf.values())
             # 16 words of loads in flight per thread in the variants capped at 64
             # registers, PF_WORDS in the others
             pf_small = max(1, min(4, 16 // max(words, 1)))
-            pf_big = max(1, min(32, PF_WORDS // max(words, 1)))
+            # (push mode with folded deliveries: the loads of more slices at once, the
+            # deliveries' loads going to L2)
+            pf_big = max(1, min(32, (PF_WORDS_PUSH if fz else PF_WORDS) // max(words, 1)))
             w(f"            constexpr int PF = (MAXT * MINB < 1024) ? {pf_big} : {pf_small};")
             w("            unsigned flags = 0u;")
             w("            for (int k0 = 0; k0 < E; k0 += PF) {")
@@ -1107,7 +1182,10 @@ def render_model(spec: dict) -> str:
             w("                const int32_t _idx = pb + (k0 + kq) * (int)blockDim.x + threadIdx.x;")
             w("                if (k0 + kq < E && _idx < pe) {")
             for ptr, j in pfi.items():
-                w(f"                  _pf{j}[kq] = {ptr}[_idx];")
+                if ptr in fz:
+                    w(f"                  _pf{j}[kq] = {ptr}[_idx] + __ldcg(_facc{j} + _idx);")
+                else:
+                    w(f"                  _pf{j}[kq] = {ptr}[_idx];")
             w("                }")
             w("              }")
             w("#pragma unroll")
@@ -1116,6 +1194,8 @@ def render_model(spec: dict) -> str:
             w("              const int32_t _idx = pb + k * (int)blockDim.x + threadIdx.x;")
             w("              if (k < E && _idx < pe) {")
             w("                const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+            for ptr in fz:
+                w(f"                __stcg(_facc{pfi[ptr]} + _idx, ({pf[ptr]})0);")
             if bd["update"] is not None:
                 w("                {")
                 if not hoist_sc:
@@ -1147,7 +1227,7 @@ def render_model(spec: dict) -> str:
             w("              }")
             w("              }")
             w("            }")
-            if not owner:
+            if not owner or push:
                 w(f"            B200_PHASE({PH_UPD(gi)});  // update + threshold condition")
             w("            // order-preserving compaction: counts per (slice k, warp), one block scan")
             w("            for (int k = 0; k < E; ++k) {")
@@ -1166,9 +1246,14 @@ def render_model(spec: dict) -> str:
             w("                {")
             w("                  const int _p = start + cnt + s_cnt[k * NW + wid] + __popc(m & b200_lanemask_lt());")
             w("                  const int _sn = pb + k * (int)blockDim.x + threadIdx.x;  // the spiking neuron")
-            w("                  scr[_p] = _sn;")
+            if not push:
+                w("                  scr[_p] = _sn;")
             if not owner:
                 w("                  oscr[_p] = _sn;  // this CTA's copy")
+            if push:
+                w("                  const int _h = _hrun + _p - start;  // position in the CTA's compact list")
+                w("                  if (_h < _hcap) _hsh[_h] = _sn;")
+                w("                  _hgl[_h] = _sn;")
             sc = snap_code(gi, "_sn")
             if sc:
                 w("                  " + sc)
@@ -1176,11 +1261,19 @@ def render_model(spec: dict) -> str:
             w("            }")
             w("            cnt += tot;")
             w("            __syncthreads();")
-            if not owner:
+            if not owner or push:
                 w(f"            B200_PHASE({PH_THR(gi)});  // spike list (threshold)")
             w("          }")
-            w("          if (threadIdx.x == 0) tcnt[u] = cnt;" if owner else "          if (threadIdx.x == 0) { tcnt[u] = cnt; otc[u] = cnt; }")
+            if not push:
+                w("          if (threadIdx.x == 0) tcnt[u] = cnt;" if owner else "          if (threadIdx.x == 0) { tcnt[u] = cnt; otc[u] = cnt; }")
+            if push:
+                w("          _hrun += cnt;")
             w("        }")
+            if push:
+                w("        if (threadIdx.x == 0) {")
+                w(f"          s_hcnt[{gi}][_hslot] = _hrun;")
+                w(f"          I.g[{gi}].hcnt[(int64_t)_hslot * I.n_cta + rank] = _hrun;")
+                w("        }")
             if quad:
                 w("        }  // scalar path")
             if rng:
@@ -2599,9 +2692,784 @@ def render_model(spec: dict) -> str:
         w("}")
         w("")
 
+
+    def lean_ok(gi):
+        """Push mode's lean phase A applies to group gi: no random draws in its
+        update or threshold, no start-slot state monitors (the generic phase A
+        handles those)."""
+        g = groups[gi]
+        if g.get("generator") or ALIAS[gi] is not None or not g.get("update") or not g.get("threshold"):
+            return False
+        for blk in ("update", "threshold"):
+            if g[blk].get("draw") is not None:
+                return False
+        return not any(m["group"] == gi and m.get("when", "start") == "start" for m in statemons)
+
+    def emit_lean_phase_a(gi):
+        """Push mode, group gi: the reset of step ts-1 and the start-slot
+        operations as in the generic phase A, then the update and threshold of
+        this CTA's neurons with each warp on a contiguous run of them (32 per
+        iteration, PFL iterations' loads issued at once), the deliveries of a
+        folded variable added as it is loaded, the spikes appended to a per-warp
+        list in neuron order, and one block scan placing the lists into the
+        CTA's spike history.  Cached state is addressed through pointers derived
+        from the dynamic shared memory, so its accesses are shared-memory ones."""
+        g = groups[gi]
+        tab, blocks = gtables[gi]
+        bd = dict(blocks)
+        w(f"      // ---- group {gi} '{g['name']}': push phase A")
+        dfr = deferred_block(gi, 8, "ts - 1", True, True)
+        if dfr:
+            w("      if (ts > ts0) {")
+            w(dfr)
+            w("        __syncthreads();")
+            w("      }")
+            w(f"      B200_PHASE({PH_RST(gi)});  // reset of the previous step")
+        sop = op_block(gi, 6, "ts", "start")
+        if sop:
+            w(sop)
+            w("      __syncthreads();")
+        upd_v = bd["update"]["vector"]
+        thr_v = bd["threshold"]["vector"]
+        upd_loads, upd_rest = split_loads(upd_v)
+        thr_loads, thr_rest = split_loads(thr_v)
+        upd_st = stored_ptrs(upd_v)
+        pf = {}
+        for ct, nm, ptr in upd_loads + [x for x in thr_loads if x[2] not in upd_st]:
+            pf.setdefault(ptr, ct)
+        pfi = {ptr: j for j, ptr in enumerate(pf)}
+        words = sum(max(1, SIZE.get(ct, 8) // 4) for ct in pf.values())
+        fz = {v["ptr"]: ACCI_[(gi, k)] for k, v in enumerate(g["vars"]) if v["ptr"] in pf and (gi, k) in FUSED}
+        upd_sc = {nm for _, nm in scalar_outputs(bd["update"]["scalar"])}
+        thr_sc = {nm for _, nm in scalar_outputs(bd["threshold"]["scalar"])}
+        hoist_sc = not (upd_sc & thr_sc)
+
+        def body(cached):
+            """Slices of 32 consecutive neurons per warp (conflict-free shared
+            memory, coalesced global memory); the deliveries of NS slices are
+            loaded before any slice is computed (one L2 round trip per chunk)."""
+            L = []
+            if cached:
+                # the cache's pointers as offsets from the dynamic shared memory base
+                for k, v in enumerate(g["vars"]):
+                    if k in USED[gi]:
+                        L.append(f"{v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)(b200_dyn + ((const unsigned char*)s_gv[{gi}][{k}] - b200_dyn)); (void){v['ptr']};")
+                    else:
+                        L.append(f"{v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)s_gv[{gi}][{k}]; (void){v['ptr']};")
+            else:
+                L.append(gptr_decls(gi, 0, True))
+            for ptr, a in fz.items():
+                L.append(f"{pf[ptr]}* const _facc{pfi[ptr]} = ({pf[ptr]}*)I.acc[{a}] + (size_t)((ts + 2) % B200_PUSH_BUFS) * I.g[{gi}].N;")
+            L.append("constexpr int NS = (MAXT * MINB < 1024) ? 16 : 4;  // slices per chunk")
+            L.append("for (int _c0 = _a; _c0 < _b; _c0 += 32 * NS) {")
+            for ptr in fz:
+                L.append(f"  {pf[ptr]} _d{pfi[ptr]}[NS];")
+            if fz:
+                L.append("#pragma unroll")
+                L.append("  for (int _s = 0; _s < NS; ++_s) {")
+                L.append("    const int32_t _idx = _c0 + _s * 32 + lane;")
+                for ptr in fz:
+                    j = pfi[ptr]
+                    L.append(f"    _d{j}[_s] = _idx < _b ? __ldcg(_facc{j} + _idx) : ({pf[ptr]})0;")
+                L.append("  }")
+            L.append("#pragma unroll")
+            L.append("  for (int _s = 0; _s < NS; ++_s) {")
+            L.append("    const int32_t _idx = _c0 + _s * 32 + lane;")
+            L.append("    bool _sp = false;")
+            L.append("    if (_idx < _b) {")
+            L.append("      const int32_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+            for ptr, j in pfi.items():
+                if ptr in fz:
+                    L.append(f"      const {pf[ptr]} _pf{j} = {ptr}[_idx] + _d{j}[_s];")
+                else:
+                    L.append(f"      const {pf[ptr]} _pf{j} = {ptr}[_idx];")
+            L.append("      {")
+            if not hoist_sc:
+                L.append(_indent(tab.scalar_loads("update", f32), 8))
+                L.append(_indent(_device(tab.time_code("update")), 8))
+            L.append(extra_ptrs(g.get("update"), 8))
+            for ct, nm, ptr in upd_loads:
+                L.append(f"        {ct} {nm} = _pf{pfi[ptr]};")
+            L.append(_indent(upd_rest, 8))
+            L.append("      }")
+            L.append("      {")
+            if not hoist_sc:
+                L.append(_indent(tab.scalar_loads("threshold", f32), 8))
+                L.append(_indent(_device(tab.time_code("threshold")), 8))
+            L.append(extra_ptrs(g.get("threshold"), 8))
+            for ct, nm, ptr in thr_loads:
+                L.append(f"        {ct} {nm} = " + (f"_pf{pfi[ptr]};" if ptr not in upd_st else f"{ptr}[_idx];"))
+            L.append(_indent(thr_rest, 8))
+            L.append("        _sp = _cond;")
+            if bd["threshold"].get("refractory"):
+                nr = next(v["ptr"] for v in g["vars"] if v["name"] == "not_refractory")
+                ls = next(v["ptr"] for v in g["vars"] if v["name"] == "lastspike")
+                L.append("        if (_cond) {")
+                L.append(f"          {nr}[_idx] = false;")
+                L.append(f"          {ls}[_idx] = _b200_t;")
+                L.append("        }")
+            sc = snap_code(gi, "_idx")
+            if sc:
+                L.append("        if (_cond) { " + sc + " }")
+            L.append("      }")
+            L.append("    }")
+            L.append("    const unsigned _m = __ballot_sync(0xffffffffu, _sp);")
+            L.append("    if (_sp) _wl[_wcnt + __popc(_m & b200_lanemask_lt())] = _idx;")
+            L.append("    _wcnt += __popc(_m);")
+            L.append("  }")
+            if fz:
+                L.append("  {  // the chunk's folded deliveries cleared (16-byte stores where aligned)")
+                L.append("    const int _z0 = _c0, _z1 = (_c0 + 32 * NS < _b) ? _c0 + 32 * NS : _b;")
+                for ptr in fz:
+                    j = pfi[ptr]
+                    ct = pf[ptr]
+                    L.append("    {")
+                    L.append(f"      {ct}* const _z = _facc{j};")
+                    if SIZE[ct] == 4:
+                        L.append("      const int _n4 = ((((uintptr_t)(_z + _z0)) & 15) == 0) ? (_z1 - _z0) >> 2 : 0;")
+                        L.append("      for (int _q = lane; _q < _n4; _q += 32) __stcg((float4*)(_z + _z0) + _q, make_float4(0.f, 0.f, 0.f, 0.f));")
+                        L.append(f"      for (int _i = _z0 + 4 * _n4 + lane; _i < _z1; _i += 32) __stcg(_z + _i, ({ct})0);")
+                    else:
+                        L.append(f"      for (int _i = _z0 + lane; _i < _z1; _i += 32) __stcg(_z + _i, ({ct})0);")
+                    L.append("    }")
+                L.append("  }")
+            L.append("}")
+            return _indent("\n".join(L), 10)
+
+        w("      {")
+        w(f"        const int32_t N = I.g[{gi}].N; (void)N;")
+        w(f"        const double* const _b200_S = s_Sg{gi}; const float* const _b200_Sf = s_Sg{gi}f; const long long* const _b200_Si = s_Sg{gi}i;")
+        w("        (void)_b200_S; (void)_b200_Sf; (void)_b200_Si;")
+        w(_indent(tab.const_loads(f32), 8))
+        if hoist_sc:
+            for blk_name in ("update", "threshold"):
+                w(_indent(tab.scalar_loads(blk_name, f32), 8))
+                w(_indent(_device(tab.time_code(blk_name)), 8))
+        w(f"        const int _o0 = s_own[{gi}][0], _o1 = s_own[{gi}][1], _on = _o1 - _o0;")
+        w("        const int _pw = (((_on + NW - 1) / NW) + 31) & ~31;  // neurons per warp")
+        w("        const int _a = _o0 + wid * _pw, _b = (_a + _pw < _o1) ? _a + _pw : _o1;")
+        w(f"        int32_t* const _wl = (int32_t*)(b200_dyn + I.g[{gi}].own_off) + wid * _pw;  // this warp's spikes")
+        w("        int _wcnt = 0;")
+        w("        if (s_cache) {")
+        w(body(True))
+        w("        } else {")
+        w(body(False))
+        w("        }")
+        w(f"        B200_PHASE({PH_UPD(gi)});  // update + threshold condition")
+        w("        int _tot;")
+        w("        const int _wb = b200_block_exscan(lane == 0 ? _wcnt : 0, s_wsum, &_tot);")
+        w("        const int _base = __shfl_sync(0xffffffffu, _wb, 0);")
+        w(f"        const int _hslot = _hs{gi}, _hcap = I.g[{gi}].HCAP;")
+        w(f"        int32_t* const _hsh = s_hist[{gi}] + _hslot * _hcap;")
+        w(f"        int32_t* const _hgl = I.g[{gi}].hist + (int64_t)_hslot * I.g[{gi}].N + _o0;")
+        w("        for (int j = lane; j < _wcnt; j += 32) {")
+        w("          const int _h = _base + j;")
+        w("          const int32_t _sn = _wl[j];")
+        w("          if (_h < _hcap) _hsh[_h] = _sn;")
+        w("          _hgl[_h] = _sn;")
+        w("        }")
+        w("        if (threadIdx.x == 0) {")
+        w(f"          s_hcnt[{gi}][_hslot] = _tot;")
+        w(f"          I.g[{gi}].hcnt[(int64_t)_hslot * I.n_cta + rank] = _tot;")
+        w("        }")
+        w(f"        B200_PHASE({PH_THR(gi)});  // spike list (threshold)")
+        w("      }")
+
+    def emit_push_kernel():
+        """Push mode: each CTA owns the neurons of its tiles (their state lives in
+        its shared memory for the launch) and delivers its own neurons' spikes.
+        Every delay is >= 1 step, so the events due at step ts+1 come from spikes
+        of steps <= ts: after arriving at step ts's barrier a CTA gathers them and
+        adds them into accumulator buffer (ts+1) % 3 of each delivered variable;
+        after the barrier of step ts+1 each owner adds buffer (ts+1) % 3 of its
+        neurons to their state and clears it.  Three buffers, because a CTA
+        starts the deliveries due at ts+2 before the slowest CTA has cleared the
+        buffer of the deliveries due at ts.  A step is: wait for step ts-1 ->
+        fold -> monitors of step ts-1 -> phase A (as the owner kernel: deferred
+        reset, operations, state monitors, update, threshold) -> spike bounds and
+        monitor counts of step ts -> arrive -> deliveries due at ts+1.  The
+        only change against the reference's order is the order of the additions
+        into a variable (the deliveries of a step are summed before they reach it)."""
+        ACCI = {gv: k for k, gv in enumerate(ACC)}
+        NSM_, NRM_ = len(spkmons), len(ratemons)
+        # monitors of step ts-1 written after the deliveries of step ts (in the
+        # barrier's slack) unless a spike monitor records variables: their
+        # per-neuron snapshot of step ts-1 is overwritten by step ts's thresholder
+        LATE = not any(m.get("vars") for m in spkmons)
+
+        def pathway_window(kexpr, ind):
+            """q (pathway index) and kk (delay index) of delivery window k."""
+            out = [f"int q = 0, kk = {kexpr};"]
+            for q in range(1, NP):
+                out.append(f"if (q == {q - 1} && kk >= W{q - 1}) {{ kk -= W{q - 1}; q = {q}; }}")
+            return _indent("\n".join(out), ind)
+
+        def qsel(qexpr, attr):
+            """I.p[q].attr for a runtime pathway index (small if-chain)."""
+            e = f"I.p[{NP - 1}].{attr}"
+            for q in reversed(range(NP - 1)):
+                e = f"(({qexpr}) == {q} ? I.p[{q}].{attr} : {e})"
+            return e
+
+        def list_elem(gexpr, slot, k):
+            return (f"(({k}) < I.g[{gexpr}].HCAP ? s_hist[{gexpr}][({slot}) * I.g[{gexpr}].HCAP + ({k})] : "
+                    f"I.g[{gexpr}].hist[(int64_t)({slot}) * I.g[{gexpr}].N + s_own[{gexpr}][0] + ({k})])")
+
+        # the pathways' source groups, as a runtime expression of q
+        def src_of(qexpr):
+            e = f"{paths[NP - 1]['src']}"
+            for q in reversed(range(NP - 1)):
+                e = f"(({qexpr}) == {q} ? {paths[q]['src']} : {e})"
+            return e
+
+        w("static size_t b200_dyn_smem_push(int threads, int max_tiles1, int max_w, int state_bytes) {")
+        w("  (void)threads;")
+        w("  return (size_t)state_bytes + (size_t)B200_NG * max_tiles1 * 8 + (size_t)(2 * max_w + 2) * 4 + 16;")
+        w("}")
+        w("")
+        # a lower bound over a CTA's list of one slot (shared memory head, global tail)
+        w("__device__ __forceinline__ int b200_push_lb(const int32_t* sh, const int32_t* gl, int hcap, int n, int x) {")
+        w("  int lo = 0, hi = n;")
+        w("  while (lo < hi) {")
+        w("    const int m = (lo + hi) >> 1;")
+        w("    const int v = m < hcap ? sh[m] : gl[m];")
+        w("    if (v < x) lo = m + 1; else hi = m;")
+        w("  }")
+        w("  return lo;")
+        w("}")
+        w("")
+        w("template <int MAXT, int MINB>")
+        w("__global__ void __launch_bounds__(MAXT, MINB) b200_push_kernel(")
+        w("    const b200_inst_d* __restrict__ insts, const int2* __restrict__ cta_map, int n_inst,")
+        w("    int queue_mode, int* work, int64_t max_steps, uint64_t limit_ns, int max_tiles1, int max_w,")
+        w("    int fault_rank, int state_bytes, unsigned long long* __restrict__ prof, int cluster) {")
+        w("  (void)queue_mode; (void)work;")
+        w("  extern __shared__ __align__(16) unsigned char b200_dyn[];")
+        w("  unsigned char* const s_state = b200_dyn;")
+        w("  int* const s_pref_all = (int*)(b200_dyn + state_bytes);              // [NG * max_tiles1]")
+        w("  int* const s_tst = s_pref_all + B200_NG * max_tiles1;               // [NG * max_tiles1]")
+        w("  int* const s_nd = s_tst + B200_NG * max_tiles1;                     // [max_w] events per window")
+        w("  int* const s_ndoff = s_nd + max_w + 1;                              // [max_w + 1] window offsets")
+        w("  (void)s_pref_all;")
+        w("  __shared__ __align__(16) b200_inst_d I;")
+        w("  __shared__ int s_wsum[B200_MAX_WARPS + 1];")
+        w("  __shared__ int s_cnt[B200_MAX_THREADS];")
+        w("  __shared__ int s_unit, s_rank, s_flag, s_cache;")
+        w("  __shared__ long long s_mon_n[B200_MAX_SPKMON];")
+        w("  __shared__ long long s_stm_n[B200_MAX_STATEMON];")
+        w("  __shared__ void* s_gv[B200_NG][B200_MAXV];")
+        w("  __shared__ int s_ut[B200_NG][2];")
+        w("  __shared__ int s_own[B200_NG][2];")
+        w("  __shared__ int s_glast[B200_NG], s_gen_lo, s_gen_hi;")
+        w("  (void)s_glast; (void)s_gen_lo; (void)s_gen_hi;")
+        w("  __shared__ int32_t* s_hist[B200_NG];   // this CTA's spike history (first HCAP of each slot)")
+        w("  __shared__ int32_t* s_hcnt[B200_NG];   // its spikes per slot")
+        w(f"  __shared__ int2* s_pb[{max(NP, 1)}];   // per slot, the bounds of the spikes in a pathway's source range")
+        w(f"  __shared__ int s_mb[{max(NSM_, 1)}][2][2];   // per step parity: the recorded spikes not yet written")
+        w(f"  __shared__ int s_red[{2 * max(NSM_ + NRM_, 1)}];")
+        for gi in range(NG):
+            n_ = max(gtables[gi][0].size, 1)
+            w(f"  __shared__ double s_Sg{gi}[{n_}]; __shared__ float s_Sg{gi}f[{n_}]; __shared__ long long s_Sg{gi}i[{n_}];")
+        for pi in range(NP):
+            n_ = max(ptables[pi][0].size, 1)
+            w(f"  __shared__ double s_Sp{pi}[{n_}]; __shared__ float s_Sp{pi}f[{n_}]; __shared__ long long s_Sp{pi}i[{n_}];")
+        w("  (void)s_state; (void)s_red; (void)s_mb;")
+        w("  for (int pass = 0;; ++pass) {")
+        w("    if (threadIdx.x == 0) {")
+        w("      if (pass == 0) { const int2 m = cta_map[blockIdx.x]; s_unit = m.x; s_rank = m.y; }")
+        w("      else s_unit = n_inst;")
+        w("    }")
+        w("    __syncthreads();")
+        w("    const int unit = s_unit, rank = s_rank;")
+        w("    if (unit >= n_inst) break;")
+        w("    {")
+        w("      const long long* src = (const long long*)&insts[unit];")
+        w("      long long* dst = (long long*)&I;")
+        w("      for (int k = threadIdx.x; k < (int)(sizeof(b200_inst_d) / 8); k += blockDim.x) dst[k] = src[k];")
+        w("    }")
+        w("    __syncthreads();")
+        w("    if (threadIdx.x == 0) {")
+        for m in range(len(spkmons)):
+            w(f"      s_mon_n[{m}] = *((volatile long long*)I.sm[{m}].n);")
+        for m in range(len(statemons)):
+            w(f"      s_stm_n[{m}] = *((volatile long long*)I.stm[{m}].n);")
+        w("      const int cache = (I.cache_bytes > 0 && I.cache_bytes <= state_bytes) ? 1 : 0;")
+        w("      s_cache = cache;")
+        w("      size_t off = 0;")
+        for gi, g in enumerate(groups):
+            w(f"      s_ut[{gi}][0] = I.g[{gi}].cta_tile[rank]; s_ut[{gi}][1] = I.g[{gi}].cta_tile[rank + 1];")
+            w(f"      s_own[{gi}][0] = I.g[{gi}].tile_start[s_ut[{gi}][0]]; s_own[{gi}][1] = I.g[{gi}].tile_start[s_ut[{gi}][1]];")
+            for k in range(len(g["vars"])):
+                w(f"      s_gv[{gi}][{k}] = I.g[{gi}].var[{k}];")
+            w("      if (cache) {  // own neurons only: pointers offset so that global indices address them")
+            for k in USED[gi]:
+                sz = SIZE[g["vars"][k]["ctype"]]
+                w(f"        s_gv[{gi}][{k}] = (void*)(s_state + off - (size_t)s_own[{gi}][0] * {sz});")
+                w(f"        off += ((size_t)(s_own[{gi}][1] - s_own[{gi}][0]) * {sz} + 15) & ~(size_t)15;")
+            w("      }")
+            w(f"      s_hist[{gi}] = (int32_t*)(s_state + I.g[{gi}].hist_off);")
+            w(f"      s_hcnt[{gi}] = (int32_t*)(s_state + I.g[{gi}].hcnt_off);")
+        for pi in range(NP):
+            w(f"      s_pb[{pi}] = (int2*)(s_state + I.p[{pi}].pb_off);")
+        w("    }")
+        w("    __syncthreads();")
+        for gi in range(NG):
+            w(f"    for (int u = threadIdx.x; u <= I.g[{gi}].n_tiles; u += blockDim.x) s_tst[{gi} * max_tiles1 + u] = I.g[{gi}].tile_start[u];")
+        for gi in range(NG):
+            w(f"    for (int k = threadIdx.x; k < {gtables[gi][0].size}; k += blockDim.x) {{")
+            w(f"      const double x = I.g[{gi}].S[k]; s_Sg{gi}[k] = x; s_Sg{gi}f[k] = (float)x; s_Sg{gi}i[k] = (long long)x;")
+            w("    }")
+        for pi in range(NP):
+            w(f"    for (int k = threadIdx.x; k < {ptables[pi][0].size}; k += blockDim.x) {{")
+            w(f"      const double x = I.p[{pi}].S[k]; s_Sp{pi}[k] = x; s_Sp{pi}f[k] = (float)x; s_Sp{pi}i[k] = (long long)x;")
+            w("    }")
+        w("    if (s_cache) {  // the owned neurons' state lives in shared memory for the launch")
+        for gi, g in enumerate(groups):
+            for k in USED[gi]:
+                sz = SIZE[g["vars"][k]["ctype"]]
+                w(f"      b200_copy_bytes((char*)s_gv[{gi}][{k}] + (size_t)s_own[{gi}][0] * {sz}, (const char*)I.g[{gi}].var[{k}] + (size_t)s_own[{gi}][0] * {sz},")
+                w(f"                      (size_t)(s_own[{gi}][1] - s_own[{gi}][0]) * {sz});")
+        w("    }")
+        w("    // the spike history of the last RH steps: counts, then the head of each list")
+        for gi in range(NG):
+            w(f"    for (int sl = threadIdx.x; sl < I.g[{gi}].RH; sl += blockDim.x) s_hcnt[{gi}][sl] = I.g[{gi}].hcnt[(int64_t)sl * I.n_cta + rank];")
+        w("    __syncthreads();")
+        for gi in range(NG):
+            w("    {")
+            w(f"      const int hc = I.g[{gi}].HCAP, rh = I.g[{gi}].RH;")
+            w("      for (int x = threadIdx.x; x < rh * hc; x += blockDim.x) {")
+            w("        const int sl = x / hc, k = x - sl * hc;")
+            w(f"        if (k < s_hcnt[{gi}][sl]) s_hist[{gi}][x] = I.g[{gi}].hist[(int64_t)sl * I.g[{gi}].N + s_own[{gi}][0] + k];")
+            w("      }")
+            w("    }")
+        w("    __syncthreads();")
+        for pi in range(NP):
+            gi = paths[pi]["src"]
+            w(f"    for (int sl = threadIdx.x; sl < I.g[{gi}].RH; sl += blockDim.x) {{  // pathway {pi}: bounds per slot")
+            w(f"      const int nn = s_hcnt[{gi}][sl], hc = I.g[{gi}].HCAP;")
+            w(f"      const int32_t* sh = s_hist[{gi}] + sl * hc;")
+            w(f"      const int32_t* gl = I.g[{gi}].hist + (int64_t)sl * I.g[{gi}].N + s_own[{gi}][0];")
+            w(f"      const int b = b200_push_lb(sh, gl, hc, nn, I.p[{pi}].src_lo), e = b200_push_lb(sh, gl, hc, nn, I.p[{pi}].src_hi);")
+            w(f"      s_pb[{pi}][sl] = make_int2(b, e);")
+            w("    }")
+        w("    __syncthreads();")
+        w("    const int64_t ts0 = I.ts;")
+        w("    const int64_t ts_stop = (I.ts_end < ts0 + max_steps) ? I.ts_end : ts0 + max_steps;")
+        w("    const double _b200_dt = I.dt;")
+        w("    int64_t ts = ts0;")
+        w("    bool ok = true;")
+        w("    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, NW = blockDim.x >> 5;")
+        w("    (void)lane; (void)wid; (void)NW;")
+        w(f"    __shared__ unsigned long long _pt, _pacc[{NPH}];")
+        w(f"    if (threadIdx.x == 0) {{ _pt = 0; for (int q = 0; q < {NPH}; ++q) _pacc[q] = 0; }}")
+        w("#define B200_PHASE(q) do { if (prof && threadIdx.x == 0) { const unsigned long long _c = clock64(); _pacc[q] += _c - _pt; _pt = _c; } } while (0)")
+
+        def emit_fold(sexpr, ind, all_vars=True):
+            """Adds accumulator buffer (sexpr) % 3 of the own neurons to their
+            state and clears it (the deliveries due at step sexpr).  The loads of
+            every variable are issued before any is added (one L2 round trip):
+            4-byte variables as float4/int4 groups of 4 neurons where aligned."""
+            sp = " " * ind
+            todo = [(kk, gv) for kk, gv in enumerate(ACC) if all_vars or gv not in FUSED]
+            if not todo:
+                return
+            w(sp + "{")
+            w(sp + f"  const int par = (int)(({sexpr}) % B200_PUSH_BUFS);")
+            vec = [(kk, gi, vi) for kk, (gi, vi) in todo if SIZE[groups[gi]["vars"][vi]["ctype"]] == 4]
+            sca = [(kk, gi, vi) for kk, (gi, vi) in todo if SIZE[groups[gi]["vars"][vi]["ctype"]] != 4]
+            for kk, gi, vi in vec + sca:
+                ct = groups[gi]["vars"][vi]["ctype"]
+                w(sp + f"  {ct}* const _fa{kk} = ({ct}*)I.acc[{kk}] + (size_t)par * I.g[{gi}].N;")
+                w(sp + f"  {ct}* const _fx{kk} = ({ct}*)s_gv[{gi}][{vi}];")
+            if vec:
+                # groups of 4 neurons from the (4-aligned) start of the CTA's range
+                w(sp + "  bool _fv = true;")
+                for kk, gi, vi in vec:
+                    w(sp + f"  _fv = _fv && (((uintptr_t)(_fa{kk} + s_own[{gi}][0]) | (uintptr_t)(_fx{kk} + s_own[{gi}][0])) & 15) == 0;")
+                gis = sorted({gi for _, gi, _ in vec})
+                for gi in gis:
+                    vs = [(kk, vi) for kk, g_, vi in vec if g_ == gi]
+                    w(sp + "  {")
+                    w(sp + f"    const int i0 = s_own[{gi}][0], i1 = s_own[{gi}][1];")
+                    w(sp + "    const int n4 = _fv ? (i1 - i0) >> 2 : 0;  // whole groups of 4")
+                    w(sp + "    for (int gb = (int)threadIdx.x; gb < n4; gb += 4 * (int)blockDim.x) {")
+                    for kk, vi in vs:
+                        w(sp + f"      float4 _d{kk}[4];")
+                    w("#pragma unroll")
+                    w(sp + "      for (int u = 0; u < 4; ++u) {")
+                    w(sp + "        const int g4 = gb + u * (int)blockDim.x;")
+                    w(sp + "        if (g4 < n4) {")
+                    for kk, vi in vs:
+                        w(sp + f"          _d{kk}[u] = __ldcg((const float4*)(_fa{kk} + i0) + g4);")
+                    w(sp + "        }")
+                    w(sp + "      }")
+                    w("#pragma unroll")
+                    w(sp + "      for (int u = 0; u < 4; ++u) {")
+                    w(sp + "        const int g4 = gb + u * (int)blockDim.x;")
+                    w(sp + "        if (g4 < n4) {")
+                    for kk, vi in vs:
+                        ct = groups[gi]["vars"][vi]["ctype"]
+                        w(sp + f"          {{ {ct}* const xs = _fx{kk} + i0 + 4 * g4; const {ct}* const ds = ({ct}*)&_d{kk}[u];")
+                        w(sp + "            xs[0] += ds[0]; xs[1] += ds[1]; xs[2] += ds[2]; xs[3] += ds[3]; }")
+                        w(sp + f"          __stcg((float4*)(_fa{kk} + i0) + g4, make_float4(0.f, 0.f, 0.f, 0.f));")
+                    w(sp + "        }")
+                    w(sp + "      }")
+                    w(sp + "    }")
+                    w(sp + "    for (int i = i0 + 4 * n4 + (int)threadIdx.x; i < i1; i += (int)blockDim.x) {  // the rest, one by one")
+                    for kk, vi in vs:
+                        w(sp + f"      {{ const auto dd = __ldcg(_fa{kk} + i); _fx{kk}[i] += dd; _fa{kk}[i] = 0; }}")
+                    w(sp + "    }")
+                    w(sp + "  }")
+            for kk, gi, vi in sca:
+                ct = groups[gi]["vars"][vi]["ctype"]
+                w(sp + "  {")
+                w(sp + f"    const int i0 = s_own[{gi}][0], i1 = s_own[{gi}][1];")
+                w(sp + "    for (int ib = i0 + (int)threadIdx.x; ib < i1; ib += 8 * (int)blockDim.x) {")
+                w(sp + f"      {ct} d[8];")
+                w("#pragma unroll")
+                w(sp + f"      for (int u = 0; u < 8; ++u) {{ const int i = ib + u * (int)blockDim.x; d[u] = i < i1 ? __ldcg(_fa{kk} + i) : ({ct})0; }}")
+                w("#pragma unroll")
+                w(sp + "      for (int u = 0; u < 8; ++u) {")
+                w(sp + "        const int i = ib + u * (int)blockDim.x;")
+                w(sp + f"        if (i < i1) {{ _fx{kk}[i] += d[u]; __stcg(_fa{kk} + i, ({ct})0); }}")
+                w(sp + "      }")
+                w(sp + "    }")
+                w(sp + "  }")
+            w(sp + "}")
+            w(sp + "__syncthreads();")
+
+        NMON = NSM_ + NRM_
+
+        def emit_monitor_counts(sexpr, ind):
+            """Each thread's share of all CTAs' counts of step sexpr (written
+            before that step's barrier): into bf (CTAs before this one) and tt
+            (all), declared by the caller."""
+            sp = " " * ind
+            if not NMON:
+                return
+            w(sp + "{")
+            w(sp + f"  const int xb = (int)(({sexpr}) % 3) * I.n_cta;")
+            w(sp + f"  for (int m = 0; m < {NMON}; ++m) {{ bf[m] = 0; tt[m] = 0; }}")
+            w(sp + "  for (int c = threadIdx.x; c < I.n_cta; c += blockDim.x) {")
+            for mi in range(NSM_):
+                w(sp + f"    {{ const int x = I.sm[{mi}].xcnt[xb + c]; tt[{mi}] += x; if (c < rank) bf[{mi}] += x; }}")
+            for ri in range(NRM_):
+                w(sp + f"    {{ const int x = I.rm[{ri}].xcnt[xb + c]; tt[{NSM_ + ri}] += x; }}")
+            w(sp + "  }")
+            w(sp + "}")
+
+        def emit_monitors(sexpr, ind, counts=True):
+            """The spike and rate monitors of step sexpr: every CTA writes its own
+            spikes after those of the CTAs before it (counts: load the counts
+            here; otherwise emit_monitor_counts filled bf/tt earlier)."""
+            sp = " " * ind
+            if not NMON:
+                return
+            nmon = NMON
+            if counts:
+                emit_monitor_counts(sexpr, ind)
+            w(sp + "{")
+            w(sp + f"  for (int m = 0; m < {nmon}; ++m) {{")
+            w(sp + "#pragma unroll")
+            w(sp + "    for (int o = 16; o >= 1; o >>= 1) { bf[m] += __shfl_down_sync(0xffffffffu, bf[m], o); tt[m] += __shfl_down_sync(0xffffffffu, tt[m], o); }")
+            w(sp + "  }")
+            w(sp + f"  if (threadIdx.x < {2 * nmon}) s_red[threadIdx.x] = 0;")
+            w(sp + "  __syncthreads();")
+            w(sp + f"  if (lane == 0) for (int m = 0; m < {nmon}; ++m) {{ atomicAdd(&s_red[2 * m], bf[m]); atomicAdd(&s_red[2 * m + 1], tt[m]); }}")
+            w(sp + "  __syncthreads();")
+            for mi, m in enumerate(spkmons):
+                gi = m["group"]
+                w(sp + f"  {{  // spike monitor {mi}")
+                w(sp + f"    const b200_spkmon_d& SM = I.sm[{mi}];")
+                w(sp + f"    const int sl = (int)(({sexpr}) % I.g[{gi}].RH);")
+                w(sp + f"    const long long mbase = s_mon_n[{mi}] + s_red[{2 * mi}];")
+                w(sp + f"    const int mpar = (int)(({sexpr}) & 1);")
+                w(sp + f"    for (int j = threadIdx.x; j < s_mb[{mi}][mpar][1]; j += blockDim.x) {{")
+                w(sp + f"      const int idx = {list_elem(gi, 'sl', f's_mb[{mi}][mpar][0] + j')};")
+                w(sp + "      const long long pos = mbase + j;")
+                w(sp + "      SM.i[pos] = idx - SM.lo;")
+                w(sp + f"      SM.ts[pos] = (int32_t)({sexpr});")
+                if m.get("vars"):
+                    w(sp + "      " + value_rows(mi, gi, "pos", "idx"))
+                w(sp + "      SM.count[idx - SM.lo] += 1;")
+                w(sp + "    }")
+                w(sp + "  }")
+            for ri, m in enumerate(ratemons):
+                w(sp + f"  if (rank == 0 && threadIdx.x == 0) I.rm[{ri}].cnt[({sexpr}) - I.rm[{ri}].step0] = s_red[{2 * (NSM_ + ri) + 1}];")
+            w(sp + "  __syncthreads();")
+            w(sp + "  if (threadIdx.x == 0) {")
+            for mi in range(NSM_):
+                w(sp + f"    s_mon_n[{mi}] += s_red[{2 * mi + 1}];")
+            w(sp + "  }")
+            w(sp + "  __syncthreads();")
+            w(sp + "}")
+
+        w(f"    int bf[{max(NMON, 1)}], tt[{max(NMON, 1)}];  // monitors: this thread's share of the CTAs' counts")
+        w("    (void)bf; (void)tt;")
+        w("    for (; ts < ts_stop; ++ts) {")
+        w("      if (threadIdx.x == 0) {")
+        w("        int st = 0;")
+        for m in range(len(spkmons)):
+            w(f"        if (s_mon_n[{m}] + 2 * (long long)(I.sm[{m}].hi - I.sm[{m}].lo) > I.sm[{m}].cap) st = 1;")
+        w("        s_flag = st;")
+        w("      }")
+        w("      __syncthreads();")
+        w("      if (s_flag) break;")
+        w("      if (prof && threadIdx.x == 0) _pt = clock64();")
+        w("      if (ts > ts0) {")
+        w("        if (!b200_owner_wait(I, ts - 1, limit_ns, cluster)) { ok = false; break; }")
+        w("        B200_PHASE(1);")
+        if LATE:
+            emit_monitor_counts("ts - 1", 8)  # (their round trip overlaps the fold and the step)
+        emit_fold("ts - 1", 8, all_vars=False)
+        if not LATE:
+            emit_monitors("ts - 1", 8)
+        w("        B200_PHASE(3);")
+        w("      }")
+        w("      const double _b200_t = (double)ts * _b200_dt;")
+        w("      const int64_t _b200_ts = ts;")
+        for gi in range(NG):
+            w(f"      const int _hs{gi} = (int)(ts % I.g[{gi}].RH);  // this step's history slot")
+        w("      const int _x3 = (int)(ts % 3);")
+        for gi in range(NG):
+            if lean_ok(gi):
+                emit_lean_phase_a(gi)
+            else:
+                emit_phase_a(True, push=True, only=[gi])
+        w("      __syncthreads();")
+        w("      B200_PHASE(0);")
+        w("      // the step's spike bounds per pathway source range, and the monitors' counts")
+        w("      {")
+        w("        // job j (a pathway or monitor) on lane j / NW of warp j % NW: one per warp first")
+        w("        const int t_ = lane < 16 ? lane * NW + wid : -1;")
+        for pi in range(NP):
+            gi = paths[pi]["src"]
+            w(f"        if (t_ == {pi}) {{")
+            w(f"          const int sl = _hs{gi}, nn = s_hcnt[{gi}][sl], hc = I.g[{gi}].HCAP;")
+            w(f"          const int32_t* sh = s_hist[{gi}] + sl * hc;")
+            w(f"          const int32_t* gl = I.g[{gi}].hist + (int64_t)sl * I.g[{gi}].N + s_own[{gi}][0];")
+            w(f"          const bool all = I.p[{pi}].src_lo <= s_own[{gi}][0] && I.p[{pi}].src_hi >= s_own[{gi}][1];")
+            w(f"          s_pb[{pi}][sl] = all ? make_int2(0, nn) : make_int2(b200_push_lb(sh, gl, hc, nn, I.p[{pi}].src_lo), b200_push_lb(sh, gl, hc, nn, I.p[{pi}].src_hi));")
+            w("        }")
+        for mi, m in enumerate(spkmons):
+            gi = m["group"]
+            w(f"        if (t_ == {NP + mi}) {{")
+            w(f"          const int sl = _hs{gi}, nn = s_hcnt[{gi}][sl], hc = I.g[{gi}].HCAP;")
+            w(f"          const int32_t* sh = s_hist[{gi}] + sl * hc;")
+            w(f"          const int32_t* gl = I.g[{gi}].hist + (int64_t)sl * I.g[{gi}].N + s_own[{gi}][0];")
+            w(f"          const bool all = I.sm[{mi}].lo <= s_own[{gi}][0] && I.sm[{mi}].hi >= s_own[{gi}][1];")
+            w(f"          const int b = all ? 0 : b200_push_lb(sh, gl, hc, nn, I.sm[{mi}].lo), e = all ? nn : b200_push_lb(sh, gl, hc, nn, I.sm[{mi}].hi);")
+            w(f"          s_mb[{mi}][ts & 1][0] = b; s_mb[{mi}][ts & 1][1] = e - b;")
+            w(f"          I.sm[{mi}].xcnt[_x3 * I.n_cta + rank] = e - b;")
+            w("        }")
+        for ri, m in enumerate(ratemons):
+            gi = m["group"]
+            w(f"        if (t_ == {NP + NSM_ + ri}) {{")
+            w(f"          const int sl = _hs{gi}, nn = s_hcnt[{gi}][sl], hc = I.g[{gi}].HCAP;")
+            w(f"          const int32_t* sh = s_hist[{gi}] + sl * hc;")
+            w(f"          const int32_t* gl = I.g[{gi}].hist + (int64_t)sl * I.g[{gi}].N + s_own[{gi}][0];")
+            w(f"          const bool all = I.rm[{ri}].lo <= s_own[{gi}][0] && I.rm[{ri}].hi >= s_own[{gi}][1];")
+            w(f"          I.rm[{ri}].xcnt[_x3 * I.n_cta + rank] = all ? nn : b200_push_lb(sh, gl, hc, nn, I.rm[{ri}].hi) - b200_push_lb(sh, gl, hc, nn, I.rm[{ri}].lo);")
+            w("        }")
+        w("      }")
+        w("      B200_PHASE(6);")
+        w("      // test hook: CTA `fault_rank` leaves without arriving, the others must time out")
+        w("      if (rank == fault_rank && ts == ts0) { ok = false; break; }")
+        w("      b200_owner_arrive(I, cluster);  // (its __syncthreads orders the bounds above)")
+        w("      B200_PHASE(2);")
+        # ---------------------------------------------- deliveries due at ts + 1
+        w("      {  // deliveries due at ts+1: this CTA's spikes of steps ts+1-d, d = dmin..D")
+        w("        const int64_t tn = ts + 1;")
+        w("        const double _b200_t = (double)tn * _b200_dt; (void)_b200_t;  // (on_pre runs at the due step)")
+        w("        const int64_t _b200_ts = tn; (void)_b200_ts;")
+        w("        const int _b200_apar = (int)(tn % B200_PUSH_BUFS);")
+        for q in range(NP):
+            w(f"        const int W{q} = I.p[{q}].D > 0 ? I.p[{q}].D - I.p[{q}].dmin + 1 : 0;")
+        w(f"        const int WT = {' + '.join(f'W{q}' for q in range(NP))};")
+        w("        for (int k = threadIdx.x; k < WT; k += blockDim.x) {")
+        w(pathway_window("k", 10))
+        w("          int n = 0;")
+        for q in range(NP):
+            gi = paths[q]["src"]
+            w(("          if" if q == 0 else "          else if") + f" (q == {q}) {{")
+            w(f"            const int dd = I.p[{q}].dmin + kk;  // spikes of step tn - dd, slot _hs + 1 - dd (mod RH)")
+            w(f"            int sl = _hs{gi} + 1 - dd; if (sl < 0) sl += I.g[{gi}].RH;")
+            w(f"            if (tn - dd >= 0) {{ const int2 bb = s_pb[{q}][sl]; n = bb.y - bb.x; }}")
+            w("          }")
+        w("          s_nd[k] = n;")
+        w("        }")
+        w("        __syncthreads();")
+        w("        {")
+        w("          int carry = 0;")
+        w("          for (int c0 = 0; c0 < WT; c0 += blockDim.x) {")
+        w("            const int k = c0 + threadIdx.x;")
+        w("            const int x = k < WT ? s_nd[k] : 0;")
+        w("            int tot;")
+        w("            const int ex = b200_block_exscan(x, s_wsum, &tot);")
+        w("            if (k < WT) s_ndoff[k] = carry + ex;")
+        w("            carry += tot;")
+        w("          }")
+        w("          if (threadIdx.x == 0) s_ndoff[WT] = carry;")
+        w("          __syncthreads();")
+        w("        }")
+        w("        const int NI = s_ndoff[WT];")
+        w("        // items (one spike at one delay) split evenly over the warps, at most 32")
+        w("        // per warp and round; a warp's events are numbered across its items, each")
+        w("        // lane finds its event's item by a binary search over the lanes")
+        w("        const int per = NI < 32 * NW ? (NI + NW - 1) / NW : 32;")
+        w("        for (int r0 = wid * per; r0 < NI; r0 += NW * per) {")
+        w("          const int it = r0 + lane;")
+        w("          int64_t ilo = 0; int len = 0, iq = 0;")
+        w("          if (lane < per && it < NI) {")
+        w("            const int k = b200_upper_bound(s_ndoff, WT + 1, it) - 1;")
+        w(pathway_window("k", 12))
+        for q in range(NP):
+            gi = paths[q]["src"]
+            w(("            if" if q == 0 else "            else if") + f" (q == {q}) {{")
+            w(f"              const b200_pathway_d& PD = I.p[{q}];")
+            w(f"              int sl = _hs{gi} + 1 - (PD.dmin + kk); if (sl < 0) sl += I.g[{gi}].RH;")
+            w(f"              const int r = it - s_ndoff[k] + s_pb[{q}][sl].x;")
+            w(f"              const int32_t src = {list_elem(gi, 'sl', 'r')};")
+            w("              const int64_t sg = (int64_t)(src - PD.src_lo) * W" + str(q) + " + kk;")
+            w("              ilo = PD.segptr[sg];")
+            w("              len = (int)(PD.segptr[sg + 1] - ilo);")
+            w("            }")
+        w("            iq = q;")
+        w("          }")
+        w("          int inc = len;")
+        w("#pragma unroll")
+        w("          for (int o = 1; o < 32; o <<= 1) { const int y = __shfl_up_sync(0xffffffffu, inc, o); if (lane >= o) inc += y; }")
+        w("          const int Ew = __shfl_sync(0xffffffffu, inc, 31);")
+        w("          const int ioff = (lane < per && it < NI) ? inc - len : 0x7fffffff;")
+        # event loop: two-phase loads when every pathway's on_pre starts with the same load types
+        sigs = []
+        for pi in range(NP):
+            lds, _ = split_loads(dict(ptables[pi][1])["on_pre"]["vector_device"] or dict(ptables[pi][1])["on_pre"]["vector"])
+            sigs.append([ct for ct, _, _ in lds])
+        two = NP > 0 and all(sg_ == sigs[0] for sg_ in sigs)
+        KB = "KBP"
+        w("          constexpr int KBP = (MAXT * MINB <= 512) ? 8 : 2;  // events whose loads a lane issues at once")
+        w(f"          for (int e0 = 0; e0 < Ew; e0 += 32 * {KB}) {{  // warp-uniform: every lane shuffles")
+        w(f"            int _q[{KB}]; int64_t _ix[{KB}];")
+        if two:
+            for li, ct in enumerate(sigs[0]):
+                w(f"            {ct} _ld{li}[{KB}];")
+        w("#pragma unroll")
+        w(f"            for (int _b200_kq = 0; _b200_kq < {KB}; ++_b200_kq) {{")
+        w("              const int e = e0 + _b200_kq * 32 + lane;")
+        w("              int j = 0;")
+        w("#pragma unroll")
+        w("              for (int st = 16; st >= 1; st >>= 1) { const int oj = __shfl_sync(0xffffffffu, ioff, j + st); if (oj <= e) j += st; }")
+        w("              const int64_t lj = __shfl_sync(0xffffffffu, ilo, j);")
+        w("              const int oj = __shfl_sync(0xffffffffu, ioff, j);")
+        w("              const int qj = __shfl_sync(0xffffffffu, iq, j);")
+        w("              _q[_b200_kq] = -1;")
+        w("              if (e < Ew) {")
+        w("                const int64_t _idx = lj + (e - oj);")
+        w("                _q[_b200_kq] = qj; _ix[_b200_kq] = _idx;")
+        if two:
+            for q in range(NP):
+                lds, _ = split_loads(dict(ptables[q][1])["on_pre"]["vector_device"] or dict(ptables[q][1])["on_pre"]["vector"])
+                p = paths[q]
+                w(("                if" if q == 0 else "                else if") + f" (qj == {q}) {{")
+                for li, (ct, nm, ptr) in enumerate(lds):
+                    if ptr == p["post_ptr"]:
+                        ex = f"I.p[{q}].post[_idx]"
+                    else:
+                        kv = next(kk_ for kk_, v in enumerate(p.get("vars", [])) if v["ptr"] == ptr)
+                        ex = f"(({ct}*)I.p[{q}].var[{kv}])[_idx]"
+                    w(f"                  _ld{li}[_b200_kq] = {ex};")
+                w("                }")
+        w("              }")
+        w("            }")
+        w("#pragma unroll")
+        w(f"            for (int _b200_kq = 0; _b200_kq < {KB}; ++_b200_kq) {{")
+        w("              if (_q[_b200_kq] >= 0) {")
+        w("                const int64_t _idx = _ix[_b200_kq]; (void)_idx;")
+        w("                const int64_t _vectorisation_idx = _idx; (void)_vectorisation_idx;")
+        for q in range(NP):
+            p = paths[q]
+            tab, blocks = ptables[q]
+            blk = dict(blocks)["on_pre"]
+            code = blk["vector_device"] if blk.get("vector_device") else blk["vector"]
+            lds, rest = split_loads(code)
+            w(("                if" if q == 0 else "                else if") + f" (_q[_b200_kq] == {q}) {{  // {p['name']}")
+            w(f"                  const b200_pathway_d& PQ = I.p[{q}]; (void)PQ;")
+            w(f"                  const double* const _b200_S = s_Sp{q}; const float* const _b200_Sf = s_Sp{q}f; const long long* const _b200_Si = s_Sp{q}i;")
+            w("                  (void)_b200_S; (void)_b200_Sf; (void)_b200_Si;")
+            w(_indent(tab.const_loads(f32), 18))
+            for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
+                v = groups[gidx]["vars"][vidx]
+                w(f"                  {v['ctype']}* __restrict__ const {ptr} = ({v['ctype']}*)I.acc[{ACCI[(gidx, vidx)]}] + (size_t)_b200_apar * I.g[{gidx}].N; (void){ptr};")
+            for kv, v in enumerate(p.get("vars", [])):
+                w(f"                  {v['ctype']}* __restrict__ const {v['ptr']} = ({v['ctype']}*)PQ.var[{kv}]; (void){v['ptr']};")
+            w(f"                  const int32_t* __restrict__ const {p['post_ptr']} = PQ.post; (void){p['post_ptr']};")
+            w(_indent(tab.scalar_loads("on_pre", f32), 18))
+            w(_indent(_device(tab.time_code("on_pre")), 18))
+            w("                  {  // (Brian's vector code may redeclare the clock's names)")
+            if two:
+                for li, (ct, nm, ptr) in enumerate(lds):
+                    w(f"                  {ct} {nm} = _ld{li}[_b200_kq];")
+                w(_indent(rest, 18))
+            else:
+                w(_indent(code, 18))
+            w("                  }")
+            w("                }")
+        w("              }")
+        w("            }")
+        w("          }")
+        w("        }")
+        w("      }")
+        w("      B200_PHASE(4);")
+        if LATE:
+            w("      if (ts > ts0) {  // the monitors of step ts-1, in the slack before the barrier")
+            emit_monitors("ts - 1", 8, counts=False)
+            w("      }")
+            w("      B200_PHASE(5);")
+        w("    }  // steps")
+        w(f"    if (prof && threadIdx.x == 0)")
+        w(f"      for (int q = 0; q < {NPH}; ++q) atomicAdd(&prof[(size_t)unit * {NPH} + q], _pacc[q]);")
+        w("#undef B200_PHASE")
+        w("    // the last step: wait for its arrivals, add its deliveries, record its spikes,")
+        w("    // apply its reset; the deliveries due at the next step stay in their buffer")
+        w("    if (ok && ts > ts0) {")
+        w("      if (!b200_owner_wait(I, ts - 1, limit_ns, cluster)) ok = false;")
+        w("      if (ok) {")
+        emit_fold("ts - 1", 8)
+        emit_monitors("ts - 1", 8)
+        w("        const double _b200_t = (double)(ts - 1) * _b200_dt; (void)_b200_t;")
+        w("        const int64_t _b200_ts = ts - 1;")
+        for gi in range(NG):
+            rb = deferred_block(gi, 8, "ts - 1", True, push=True)
+            if rb:
+                w(rb)
+        w("      }")
+        w("    }")
+        w("    __syncthreads();")
+        w("    if (s_cache) {")
+        for gi, g in enumerate(groups):
+            for k in USED[gi]:
+                sz = SIZE[g["vars"][k]["ctype"]]
+                w(f"      b200_copy_bytes((char*)I.g[{gi}].var[{k}] + (size_t)s_own[{gi}][0] * {sz}, (const char*)s_gv[{gi}][{k}] + (size_t)s_own[{gi}][0] * {sz},")
+                w(f"                      (size_t)(s_own[{gi}][1] - s_own[{gi}][0]) * {sz});")
+        w("    }")
+        w("    if (threadIdx.x == 0 && rank == 0) {")
+        w("      *I.ts_done = ts;")
+        for m in range(len(spkmons)):
+            w(f"      *I.sm[{m}].n = s_mon_n[{m}];")
+        for m in range(len(statemons)):
+            w(f"      *I.stm[{m}].n = s_stm_n[{m}];")
+        w("    }")
+        w("    __syncthreads();")
+        w("  }")
+        w("}")
+        w("")
+
     group_ev_bytes = []
     if OWNER:
         emit_owner_kernel()
+    if PUSH:
+        emit_push_kernel()
     OWNER_EV_BYTES = max(group_ev_bytes) if group_ev_bytes else 8
 
     # ------------------------------------------------------------- launch glue
@@ -2609,6 +3477,12 @@ def render_model(spec: dict) -> str:
     w("// registers so that two CTAs fit on an SM (sweeps with more instances than SMs)")
     w("static const void* b200_kernel_for(int tcode) {")
     w("  const int threads = tcode & 0xffff, minb = ((tcode >> 16) & 0xf) + 1;")
+    if PUSH:
+        w("  if (tcode & B200_TCODE_PUSH) {  // push mode")
+        w("    if (threads <= 256) return minb >= 2 ? (const void*)b200_push_kernel<256, 2> : (const void*)b200_push_kernel<256, 1>;")
+        w("    if (threads <= 512) return (const void*)b200_push_kernel<512, 1>;")
+        w("    return (const void*)b200_push_kernel<1024, 1>;")
+        w("  }")
     if OWNER:
         w("  if (tcode & B200_TCODE_OWNER) {  // owner mode: one CTA per SM")
         w("    if (threads <= 256) return (const void*)b200_owner_kernel<256, 1>;")
@@ -2621,6 +3495,8 @@ def render_model(spec: dict) -> str:
     w("}")
     w("static size_t b200_smem_for(int tcode, int max_tiles1, int max_w, int state_bytes) {")
     w("  const int threads = tcode & 0xffff;")
+    if PUSH:
+        w("  if (tcode & B200_TCODE_PUSH) return b200_dyn_smem_push(threads, max_tiles1, max_w, state_bytes);")
     if OWNER:
         w("  if (tcode & B200_TCODE_OWNER) return b200_dyn_smem_owner(threads, max_tiles1, max_w, state_bytes);")
     w("  return b200_dyn_smem(threads, max_tiles1, max_w, state_bytes);")
@@ -2699,11 +3575,13 @@ def render_model(spec: dict) -> str:
         w("static const b200_summed_info b200_summed[] = {" + ", ".join(
             f'{{"{sm["name"]}", {sm["pathway"]}, {sm["tgt_group"]}, {sm["tgt_var"]}, {1 if sm["index_post"] else 0}}}'
             for sm in SUMMED) + "};")
+    w("static const int b200_acc_vars[] = {" + (", ".join(f"{gi}, {vi}" for gi, vi in ACC) if ACC else "0") + "};")
     w(f'static const b200_model_info B200_MODEL = {{"{spec["name"]}", {NG}, {NP}, {len(spkmons)}, {len(ratemons)}, {len(statemons)},')
     w("  b200_groups, b200_pathways, b200_spkmon, b200_ratemon, b200_statemon,")
     w(f"  {len(consts)}, b200_const_names, b200_const_defaults, b200_eval_scalars, b200_launch, b200_max_active,")
     w(f"  b200_static_smem, b200_max_cluster, {NPH}, {1 if OWNER else 0}, {OWNER_EV_BYTES},")
-    w(f"  {len(SUMMED)}, {'b200_summed' if SUMMED else 'nullptr'}, {len(DRAWS)}, {'b200_draws' if DRAWS else 'nullptr'}}};")
+    w(f"  {len(SUMMED)}, {'b200_summed' if SUMMED else 'nullptr'}, {len(DRAWS)}, {'b200_draws' if DRAWS else 'nullptr'},")
+    w(f"  {1 if PUSH else 0}, {len(ACC)}, b200_acc_vars}};")
     w("")
     w('#include "b200_host.h"')
     w("")
@@ -2732,7 +3610,7 @@ def delivery_passes(paths) -> list:
     return merged
 
 
-def profile_slots(spec: dict, owner: bool = False) -> list[str]:
+def profile_slots(spec: dict, owner: bool = False, push: bool = False) -> list[str]:
     """Names of the device profile's slots (b200_get_profile), in order.
     Owner-mode kernel: update (update, threshold and reset of every group),
     barrier, spike lists, push counts, push into the event FIFOs, delivery.
@@ -2740,10 +3618,19 @@ def profile_slots(spec: dict, owner: bool = False) -> list[str]:
     spike-list phase, one slot per pathway for its events, barrier B,
     delivery windows, delivery items; per group its update (with the threshold
     condition), its spike list (threshold), its reset; per group the copy of
-    its spikes into the delay ring; one slot per spike and per rate monitor."""
+    its spikes into the delay ring; one slot per spike and per rate monitor.
+    Push-mode kernel: update (update, threshold and reset of every group),
+    barrier, spike bounds and arrival, accumulators added and monitors, delivery."""
     groups = spec["groups"]
     paths = spec.get("pathways", [])
-    if owner:
+    if push:
+        # (phase A's per-group slots as in the classic layout)
+        names = ["other", "barrier", "arrive", "fold", "deliver", "monitors", "bounds"]
+        names += [f"unused{k}" for k in range(len(names), 6 + len(paths))]
+        for g in groups:
+            names += [f"update:{g['name']}", f"threshold:{g['name']}", f"reset:{g['name']}"]
+        owner = True  # (no ring or monitor slots)
+    elif owner:
         names = ["update_threshold_reset", "barrier", "spike_lists_monitors", "push_count", "push_fifo", "deliver"]
     else:
         names = ["other", "barrier_a", "lists_other"] + [f"events:{p['name']}" for p in paths] + \

@@ -30,6 +30,8 @@
 #define B200_ERR_RANDOM 7         // a binomial draw needed a second random number
 #define B200_MAX_PAYLOAD 4
 #define B200_OWNER_RING 4   // spike-list slots in owner mode (see the kernel's ordering argument)
+#define B200_MAX_ACC 8      // push mode: neuron variables that receive deliveries
+#define B200_PUSH_BUFS 3    // push mode: accumulator buffers per variable (deliveries of 3 steps)
 
 // ---------------------------------------------------------------------------
 // Descriptors (plain data, filled by the host runtime, read by the kernel).
@@ -56,7 +58,13 @@ struct b200_group_d {
   int64_t gen_n;
   int32_t* gen_last;         // [1] next spike to emit (persists across launches)
   int32_t gen_period;        // period in steps (0: no repetition)
-  int32_t _pad_g;
+  // push mode: each CTA's spike list of the last RH steps, compact and ascending,
+  // at hist[(ts % RH) * N + first own neuron + k]; the first HCAP entries of each
+  // slot also in shared memory at byte offset hist_off, the slot counts at hcnt_off
+  int32_t RH, HCAP;
+  int32_t hist_off, hcnt_off;
+  int32_t* hist;             // [RH * N]
+  int32_t* hcnt;             // [RH * n_cta] spikes of each CTA per slot
 };
 
 // Owner mode: per (pathway, CTA) FIFO of delivery events.  Every step the CTA
@@ -95,6 +103,9 @@ struct b200_pathway_d {
   // source, post/var are in that order, odelay is each synapse's delay slot
   const uint16_t* odelay;
   b200_fifo_d ev;
+  // push mode: byte offset in shared memory of the per-slot bounds (int2, RH of the
+  // source group) of the CTA's spikes in [src_lo, src_hi)
+  int32_t pb_off, _pad_p;
 };
 
 struct b200_spkmon_d {
@@ -108,6 +119,7 @@ struct b200_spkmon_d {
   // step's thresholder ran, as double
   double* snap;           // [n_vars][group N] the values of the step's spiking neurons
   double* vals;           // [cap][n_vars] one row per recorded spike
+  int32_t* xcnt;          // push mode: [3][n_cta] each CTA's recorded spikes of a step (by step % 3)
 };
 
 struct b200_ratemon_d {
@@ -115,6 +127,7 @@ struct b200_ratemon_d {
   int64_t step0;          // time step of cnt[0]
   int64_t cap;            // steps available in cnt
   int32_t* cnt;           // [cap] spikes in [lo,hi) per step
+  int32_t* xcnt;          // push mode: [3][n_cta] each CTA's spikes in [lo,hi) of a step (by step % 3)
 };
 
 struct b200_statemon_d {
@@ -158,6 +171,11 @@ struct b200_inst_d {
   int32_t stage_cap;      // events it holds (0: none; pushes take two passes over global memory)
   int32_t priv_bytes;     // classic multi-CTA instance: bytes of each CTA's shared-memory copy of
                           // its own neurons' private variables (0: none)
+  // push mode (b200_push_kernel): each CTA delivers its own neurons' spikes, one step
+  // ahead, into accumulators that the target's owner adds to its state after the
+  // step's barrier; acc[k] is [B200_PUSH_BUFS][N] of the model's k-th delivered variable
+  int32_t push, _pad_push;
+  void* acc[B200_MAX_ACC];
   b200_group_d g[B200_MAX_GROUPS];
   b200_pathway_d p[B200_MAX_PATHWAYS];
   b200_spkmon_d sm[B200_MAX_SPKMON];
@@ -276,9 +294,16 @@ struct b200_model_info {
   // schedule runs them in a step (the order of the draws)
   int n_draws;
   const b200_draw_info* draws;
+  // 1: push-mode delivery applies (owner_ok, and no spike generator or custom event
+  // is the source of a pathway); the delivered variables as (group, variable) pairs
+  int push_ok;
+  int n_acc;
+  const int* acc_vars;  // [2 * n_acc]
 };
 // `tcode` bit selecting the owner-mode kernel
 #define B200_TCODE_OWNER (1 << 20)
+// `tcode` bit selecting the push-mode kernel
+#define B200_TCODE_PUSH (1 << 21)
 
 
 // ---------------------------------------------------------------------------
@@ -308,6 +333,10 @@ __device__ __forceinline__ unsigned long long b200_ld_acquire64(const unsigned l
 
 __device__ __forceinline__ void b200_red_release_add64(unsigned long long* p, unsigned long long v) {
   asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+__device__ __forceinline__ void b200_red_relaxed_add64(unsigned long long* p, unsigned long long v) {
+  asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 __device__ __forceinline__ uint64_t b200_globaltimer() {
@@ -819,8 +848,8 @@ __device__ __forceinline__ void b200_owner_arrive(const b200_inst_d& I, int clus
     return;
   }
   if (threadIdx.x == 0) {
-    __threadfence();
-    b200_red_release_add64(I.bar64, 1ull);
+    __threadfence();  // (the fence releases the CTA's writes; the add itself can be relaxed)
+    b200_red_relaxed_add64(I.bar64, 1ull);
   }
 }
 

@@ -38,6 +38,9 @@ struct b200_group_h {
   b200_dbuf d_tile_start, d_cta_tile, scratch, tile_cnt, ring, ring_total, ring_prefix;
   b200_dbuf S;
   int32_t R = 1;
+  // push mode: each CTA's compact spike lists of the last RH steps, counts per slot and CTA
+  b200_dbuf hist, hcnt;
+  int32_t RH = 0, hist_ncta = 0;
 };
 struct b200_pathway_h {
   int32_t src_lo = 0, src_hi = 0, tgt_lo = 0, tgt_hi = 0;
@@ -69,11 +72,13 @@ struct b200_spkmon_h {
   int64_t cap = 0;
   b200_dbuf n, i, ts, count;
   b200_dbuf snap, vals;  // recorded variables: per-neuron values of the step, per-spike rows
+  b200_dbuf xcnt;        // push mode: each CTA's recorded spikes of the last three steps
 };
 struct b200_ratemon_h {
   int32_t lo = 0, hi = 0;
   int64_t step0 = 0, cap = 0, n = 0;
   b200_dbuf cnt;
+  b200_dbuf xcnt;        // push mode: each CTA's spikes of the last three steps
 };
 struct b200_statemon_h {
   int32_t n_rec = 0, n_vars = 0;
@@ -92,7 +97,8 @@ struct b200_inst_h {
   int32_t n_cta = 1;
   int64_t ts = 0;
   b200_dbuf bar, status, ts_done, pending, bar64;
-  int32_t ran_owner = -1;  // mode of the runs so far with spikes in flight: -1 none, 0 classic, 1 owner
+  int32_t ran_owner = -1;  // mode of the runs so far with spikes in flight: -1 none, 0 classic, 1 owner, 2 push
+  b200_dbuf acc[B200_MAX_ACC];  // push mode: deliveries not yet added, B200_PUSH_BUFS steps per variable
   // a launch failed part-way (timeout, index error, dropped events): the CTAs
   // stopped at different steps, so the state no longer belongs to one time
   // step; runs are refused until b200_set_step declares the step of the state
@@ -123,6 +129,8 @@ struct b200_net {
   bool use_clusters = true;       // instances of 2..16 CTAs run as thread-block clusters
   int allow_owner = 2;            // owner-mode delivery: 0 off, 1 on where possible, 2 auto
   int owner = 0;                  // 1: the current plan runs b200_owner_kernel
+  int allow_push = 2;             // push-mode delivery: 0 off, 1 on where possible, 2 auto
+  int push = 0;                   // 1: the current plan runs b200_push_kernel
   double ev_factor = 0.0;         // event FIFO records per CTA, in units of its incoming synapses (0: worst case)
   int cluster = 0;                // cluster size of the current launch plan (0: none)
   b200_dbuf prof;
@@ -140,7 +148,10 @@ struct b200_net {
   double last_kernel_ms = 0.0;  // kernel launches only (CUDA events around them)
   std::string err;
   size_t device_bytes = 0;
-  int tcode() const { return threads | ((min_blocks - 1) << 16) | (owner ? B200_TCODE_OWNER : 0); }
+  int tcode() const {
+    return threads | ((min_blocks - 1) << 16) | (owner ? B200_TCODE_OWNER : 0) | (push ? B200_TCODE_PUSH : 0);
+  }
+  int mode() const { return push ? 2 : (owner ? 1 : 0); }
 };
 
 static int b200_fail(b200_net* n, int code, const char* fmt, ...) {
@@ -261,6 +272,7 @@ int b200_destroy(b200_net* n) {
       b200_free(n, G.d_tile_start); b200_free(n, G.d_cta_tile); b200_free(n, G.scratch);
       b200_free(n, G.tile_cnt); b200_free(n, G.ring); b200_free(n, G.ring_total);
       b200_free(n, G.ring_prefix); b200_free(n, G.S);
+      b200_free(n, G.hist); b200_free(n, G.hcnt);
     }
     for (auto& P : I.p) {
       for (auto& b : P.var) b200_free(n, b);
@@ -273,9 +285,10 @@ int b200_destroy(b200_net* n) {
     }
     for (auto& S : I.sm) {
       b200_free(n, S.n); b200_free(n, S.i); b200_free(n, S.ts); b200_free(n, S.count);
-      b200_free(n, S.snap); b200_free(n, S.vals);
+      b200_free(n, S.snap); b200_free(n, S.vals); b200_free(n, S.xcnt);
     }
-    for (auto& S : I.rm) b200_free(n, S.cnt);
+    for (auto& S : I.rm) { b200_free(n, S.cnt); b200_free(n, S.xcnt); }
+    for (auto& b : I.acc) b200_free(n, b);
     for (auto& S : I.stm) { b200_free(n, S.d_idx); b200_free(n, S.n); b200_free(n, S.data); }
     for (auto& S : I.sum) { b200_free(n, S.seg); b200_free(n, S.syn); }
     b200_free(n, I.rng_state); b200_free(n, I.rng_gauss); b200_free(n, I.rng_buf[0]); b200_free(n, I.rng_buf[1]);
@@ -779,16 +792,41 @@ static int b200_prepare(b200_net* n) {
     for (int k = 0; k < n->n_inst && want && n->allow_owner == 2; ++k)
       for (int p = 0; p < M->n_pathways; ++p)
         if (n->inst[k].p[p].n_syn > 0 && n->inst[k].p[p].dmax > 0) want = false;
-    n->owner = want ? 1 : 0;
+    // push mode: a model whose on_pre allows it, every synaptic delay >= 1 step;
+    // auto: float32 models (the deliveries of a step are summed before they reach
+    // their variable, which changes float64 results in the last bits) on 2+ CTAs
+    bool push = n->allow_push != 0 && M->push_ok && !n->queue_mode;
+    bool any_delay = false;
+    for (int k = 0; k < n->n_inst && push; ++k)
+      for (int p = 0; p < M->n_pathways; ++p) {
+        if (n->inst[k].p[p].n_syn > 0 && n->inst[k].p[p].dmin == 0) push = false;
+        if (n->inst[k].p[p].n_syn > 0 && n->inst[k].p[p].dmax > 0) any_delay = true;
+      }
+    if (push && n->allow_push == 2) {
+      bool f32 = M->n_acc > 0;
+      for (int a = 0; a < M->n_acc; ++a)
+        f32 = f32 && M->groups[M->acc_vars[2 * a]].var_kind[M->acc_vars[2 * a + 1]] == B200_F32;
+      push = f32 && any_delay;
+      for (int k = 0; k < n->n_inst && push; ++k) push = n->inst[k].n_cta >= 2;
+    }
+    n->push = push ? 1 : 0;
+    n->owner = (want && !push) ? 1 : 0;
     for (int k = 0; k < n->n_inst; ++k) {
       const b200_inst_h& I = n->inst[k];
       bool inflight = false;
       for (int p = 0; p < M->n_pathways; ++p) inflight = inflight || (I.p[p].dmax >= 1 && I.p[p].n_syn > 0);
-      if (I.ts > 0 && inflight && I.ran_owner >= 0 && I.ran_owner != n->owner)
+      if (I.ts > 0 && inflight && I.ran_owner >= 0 && I.ran_owner != n->mode())
         return b200_fail(n, B200_ERR_ARG,
-                         "instance %d: switching between owner and classic delivery after the first run of a "
-                         "network with delays would lose the spikes in flight; choose the mode (b200_set_owner) "
-                         "and the CTA count before the first run", k);
+                         "instance %d: switching between the classic, owner and push delivery modes after the "
+                         "first run of a network with delays would lose the spikes in flight; choose the mode "
+                         "(b200_set_owner, b200_set_push) and the CTA count before the first run", k);
+      if (n->push && I.ts > 0 && inflight && I.ran_owner == 2) {
+        for (int g = 0; g < M->n_groups; ++g)
+          if (I.g[g].hist_ncta != 0 && I.g[g].hist_ncta != I.n_cta)
+            return b200_fail(n, B200_ERR_ARG,
+                             "instance %d: the CTA count of a push-mode network with spikes in flight cannot "
+                             "change between runs", k);
+      }
     }
   }
   n->h_insts.assign(n->n_inst, b200_inst_d());
@@ -827,7 +865,7 @@ static int b200_prepare(b200_net* n) {
         if (M->spkmon[s].group == g) { cuts.push_back(I.sm[s].lo); cuts.push_back(I.sm[s].hi); }
       for (int s = 0; s < M->n_ratemon; ++s)
         if (M->ratemon[s].group == g) { cuts.push_back(I.rm[s].lo); cuts.push_back(I.rm[s].hi); }
-      if (n->owner) R = B200_OWNER_RING;  // lists of the last steps only: events wait in the FIFOs
+      if (n->owner || n->push) R = B200_OWNER_RING;  // lists of the last steps only (FIFOs / history)
       const std::vector<int32_t> old_tiles = G.tile_start;
       if (M->groups[g].generator) {
         // a spike generator emits in array order (not by neuron): all its tiles
@@ -841,7 +879,7 @@ static int b200_prepare(b200_net* n) {
       }
       const int n_tiles = (int)G.tile_start.size() - 1;
       const bool ring_changed = (R != G.R) || !G.ring.p;
-      const bool retile = !n->owner && !ring_changed && old_tiles != G.tile_start && I.ts > 0 && R > 1;
+      const bool retile = !n->owner && !n->push && !ring_changed && old_tiles != G.tile_start && I.ts > 0 && R > 1;
       G.R = R;
       if ((r = b200_alloc(n, G.d_tile_start, G.tile_start.size() * 4, false))) return r;
       if ((r = b200_alloc(n, G.d_cta_tile, G.cta_tile.size() * 4, false))) return r;
@@ -884,6 +922,22 @@ static int b200_prepare(b200_net* n) {
       GD.ring = (int32_t*)G.ring.p;
       GD.ring_total = (int32_t*)G.ring_total.p;
       GD.ring_prefix = (int32_t*)G.ring_prefix.p;
+      GD.RH = 0; GD.HCAP = 0; GD.hist_off = 0; GD.hcnt_off = 0; GD.hist = nullptr; GD.hcnt = nullptr;
+      if (n->push) {
+        // each CTA's spike lists of the steps whose deliveries are still due
+        int32_t RH = 2;
+        for (int p = 0; p < M->n_pathways; ++p)
+          if (M->pathways[p].src_group == g) RH = std::max(RH, I.p[p].dmax + 1);
+        if (RH != G.RH || G.hist_ncta != I.n_cta || !G.hist.p || !G.hcnt.p) {
+          if ((r = b200_alloc(n, G.hist, (size_t)RH * std::max(G.N, 1) * 4, false))) return r;
+          if ((r = b200_alloc(n, G.hcnt, (size_t)RH * I.n_cta * 4))) return r;
+          G.RH = RH;
+          G.hist_ncta = I.n_cta;
+        }
+        GD.RH = RH;
+        GD.hist = (int32_t*)G.hist.p;
+        GD.hcnt = (int32_t*)G.hcnt.p;
+      }
       const b200_group_h& GS = M->groups[g].alias >= 0 ? I.g[M->groups[g].alias] : G;  // (state owner)
       for (int v = 0; v < M->groups[g].n_vars; ++v) GD.var[v] = GS.var[v].p;
       GD.S = (const double*)G.S.p;
@@ -948,6 +1002,20 @@ static int b200_prepare(b200_net* n) {
       if ((r = b200_alloc(n, I.bar64, 16))) return r;
       D.bar64 = (unsigned long long*)I.bar64.p;
     }
+    if (n->push) {
+      D.push = 1;
+      if ((r = b200_alloc(n, I.bar64, 16))) return r;
+      D.bar64 = (unsigned long long*)I.bar64.p;
+      // the accumulators keep the deliveries due at the next steps across runs:
+      // (re)allocated, zeroed, only when missing or too small
+      for (int a = 0; a < M->n_acc; ++a) {
+        const int ag = M->acc_vars[2 * a], av = M->acc_vars[2 * a + 1];
+        const size_t bytes = (size_t)B200_PUSH_BUFS * std::max(I.g[ag].N, 1) * b200_kind_size(M->groups[ag].var_kind[av]);
+        if (!I.acc[a].p || I.acc[a].bytes < bytes)
+          if ((r = b200_alloc(n, I.acc[a], bytes))) return r;
+        D.acc[a] = I.acc[a].p;
+      }
+    }
     for (int s = 0; s < M->n_spkmon; ++s) {
       b200_spkmon_h& S = I.sm[s];
       const b200_group_h& G = I.g[M->spkmon[s].group];
@@ -972,6 +1040,11 @@ static int b200_prepare(b200_net* n) {
       SD.cap = S.cap;
       SD.n = (int64_t*)S.n.p; SD.i = (int32_t*)S.i.p; SD.ts = (int32_t*)S.ts.p;
       SD.count = (int32_t*)S.count.p;
+      SD.xcnt = nullptr;
+      if (n->push) {
+        if ((r = b200_alloc(n, S.xcnt, (size_t)3 * I.n_cta * 4))) return r;
+        SD.xcnt = (int32_t*)S.xcnt.p;
+      }
     }
     for (int s = 0; s < M->n_ratemon; ++s) {
       b200_ratemon_h& S = I.rm[s];
@@ -980,6 +1053,11 @@ static int b200_prepare(b200_net* n) {
       RD.group = M->ratemon[s].group; RD.lo = S.lo; RD.hi = S.hi;
       RD.tile_lo = (int)(std::lower_bound(G.tile_start.begin(), G.tile_start.end(), S.lo) - G.tile_start.begin());
       RD.tile_hi = (int)(std::lower_bound(G.tile_start.begin(), G.tile_start.end(), S.hi) - G.tile_start.begin());
+      RD.xcnt = nullptr;
+      if (n->push) {
+        if ((r = b200_alloc(n, S.xcnt, (size_t)3 * I.n_cta * 4))) return r;
+        RD.xcnt = (int32_t*)S.xcnt.p;
+      }
     }
     for (int s = 0; s < M->n_statemon; ++s) {
       b200_statemon_h& S = I.stm[s];
@@ -1043,7 +1121,7 @@ static int b200_prepare(b200_net* n) {
     // the other's work) use it too
     int max_cta = 0;
     for (int k = 0; k < n->n_inst; ++k) max_cta = std::max(max_cta, n->inst[k].n_cta);
-    n->min_blocks = (!n->owner && ((n->threads == 512 && n->queue_mode && n->n_inst > n_sm_) ||
+    n->min_blocks = (!n->owner && ((n->threads == 512 && n->queue_mode && n->n_inst > n_sm_ && !n->push) ||
                                    ((n->threads == 512 || n->threads == 256) && !n->queue_mode && max_cta > n_sm_)))
                         ? 2 : 1;
     const long other = (long)M->static_smem(n->tcode()) +
@@ -1055,7 +1133,7 @@ static int b200_prepare(b200_net* n) {
     auto cache_bytes = [&](int k, bool lists) -> long {
       b200_inst_h& I = n->inst[k];
       if (!n->smem_cache) return 0;
-      if (n->owner) {  // each CTA caches the neurons it owns
+      if (n->owner || n->push) {  // each CTA caches the neurons it owns
         long worst = 0;
         for (int c = 0; c < I.n_cta; ++c) {
           long bytes = 0;
@@ -1101,7 +1179,7 @@ static int b200_prepare(b200_net* n) {
       n->h_insts[k].cache_lists = lists ? 1 : 0;
       n->state_bytes = std::max<long>(n->state_bytes, bytes);
     }
-    if (!n->owner && !n->queue_mode) {
+    if (!n->owner && !n->push && !n->queue_mode) {
       // classic multi-CTA instances: each CTA keeps its own neurons' private
       // variables (touched by no pathway) in shared memory for the launch, then
       // a copy of its own spike lists and tile counts (the reset and the ring
@@ -1180,6 +1258,42 @@ static int b200_prepare(b200_net* n) {
         D.stage_off = (int32_t)off;
         D.stage_cap = (int32_t)cap;
         off += cap * ev;
+        n->state_bytes = std::max<long>(n->state_bytes, off);
+      }
+    }
+    if (n->push) {
+      // after the state cache: per group the slot counts of the spike history and
+      // its first HCAP entries per slot, per pathway the bounds of its source
+      // range per slot (HCAP as large as the room allows, at most 64)
+      const long room = n->min_blocks == 2 ? std::min(budget, (long)optin / 2 - other - 1024) : budget;
+      for (int k = 0; k < n->n_inst; ++k) {
+        b200_inst_d& D = n->h_insts[k];
+        long off = ((long)D.cache_bytes + 15) & ~15L;
+        long hist_words = 0;
+        const b200_inst_h& IH = n->inst[k];
+        for (int g = 0; g < M->n_groups; ++g) {
+          D.g[g].hcnt_off = (int32_t)off;
+          off += ((long)D.g[g].RH * 4 + 15) & ~15L;
+          hist_words += D.g[g].RH;
+          // each warp's spikes of the step, in neuron order, before they enter the history
+          int cap = 0;
+          const b200_group_h& G = IH.g[g];
+          for (int c = 0; c < IH.n_cta; ++c) cap = std::max(cap, G.tile_start[G.cta_tile[c + 1]] - G.tile_start[G.cta_tile[c]]);
+          D.g[g].own_cap = cap + 128 * (n->threads / 32);
+          D.g[g].own_off = (int32_t)off;
+          off += ((long)D.g[g].own_cap * 4 + 15) & ~15L;
+        }
+        for (int p = 0; p < M->n_pathways; ++p) {
+          D.p[p].pb_off = (int32_t)off;
+          off += (long)D.g[M->pathways[p].src_group].RH * 8;
+        }
+        long hcap = hist_words > 0 ? std::min<long>(64, std::max<long>(0, room - off - 16 * M->n_groups) / (hist_words * 4)) : 0;
+        if (hcap < 0) hcap = 0;
+        for (int g = 0; g < M->n_groups; ++g) {
+          D.g[g].HCAP = (int32_t)hcap;
+          D.g[g].hist_off = (int32_t)off;
+          off += ((long)D.g[g].RH * hcap * 4 + 15) & ~15L;
+        }
         n->state_bytes = std::max<long>(n->state_bytes, off);
       }
     }
@@ -1338,7 +1452,7 @@ int b200_run(b200_net* n, int64_t n_steps) {
         B200_CU(n, cudaMemcpy(&used, S.n.p, 8, cudaMemcpyDeviceToHost));
         // room for at least 64 steps of all neurons spiking
         // (owner mode records a step's spikes one step later: one more step of room)
-        const int64_t need = (std::min<int64_t>(target[k] - I.ts, 64) + (n->owner ? 1 : 0)) * (int64_t)(S.hi - S.lo);
+        const int64_t need = (std::min<int64_t>(target[k] - I.ts, 64) + ((n->owner || n->push) ? 1 : 0)) * (int64_t)(S.hi - S.lo);
         if ((r = b200_grow_spkmon(n, S, M->spkmon[s].n_vars, used, need))) return r;
         D.sm[s].cap = S.cap;
         D.sm[s].i = (int32_t*)S.i.p;
@@ -1402,7 +1516,7 @@ int b200_run(b200_net* n, int64_t n_steps) {
         Dd.rng_ts0 = I.ts;
       }
     }
-    if (n->owner) {  // the split barrier counts the arrivals of this launch from 0
+    if (n->owner || n->push) {  // the split barrier counts the arrivals of this launch from 0
       for (int k = 0; k < n->n_inst; ++k) {
         n->h_insts[k].ts_base = n->inst[k].ts;
         B200_CU(n, cudaMemsetAsync(n->inst[k].bar64.p, 0, 8, n->stream));
@@ -1487,7 +1601,7 @@ int b200_run(b200_net* n, int64_t n_steps) {
       }
       if (done < I.ts || done > target[k])
         return b200_fail(n, B200_ERR_CUDA, "instance %d: bad progress %lld", k, (long long)done);
-      if (done > I.ts) I.ran_owner = n->owner;
+      if (done > I.ts) I.ran_owner = n->mode();
       I.ts = done;
     }
     if (first_bad >= 0) {
@@ -1562,6 +1676,32 @@ int b200_set_owner(b200_net* n, int32_t enable) {
   if (!n || enable < 0 || enable > 2) return B200_ERR_ARG;
   n->allow_owner = enable;
   n->prepared = false;
+  return 0;
+}
+
+// Push-mode delivery: 0 off, 1 on where the model allows it, 2 auto (default:
+// float32 models with synaptic delays on instances of 2+ CTAs).  In push mode
+// each CTA delivers the spikes of the neurons it owns: every delay is at least
+// one step, so right after arriving at the barrier of step ts it gathers the
+// synapses of its spikes due at step ts+1 and adds their values into an
+// accumulator buffer of each delivered variable; after the barrier of step
+// ts+1 each owner adds the buffer into its neurons' state.  One barrier per
+// step and no global spike list; the order of the additions into a variable
+// is the only change against the reference's CSpikeQueue delivery
+// (brian2/synapses/spikequeue.h:14-206, templates/synapses.cpp:20-49).
+int b200_set_push(b200_net* n, int32_t enable) {
+  if (!n || enable < 0 || enable > 2) return B200_ERR_ARG;
+  n->allow_push = enable;
+  n->prepared = false;
+  return 0;
+}
+
+// 1 if the current launch plan uses push-mode delivery.
+int b200_push_active(b200_net* n, int32_t* active) {
+  if (!n || !active) return B200_ERR_ARG;
+  int r;
+  if (!n->prepared && (r = b200_prepare(n))) return r;
+  *active = n->push;
   return 0;
 }
 

@@ -73,6 +73,8 @@ def _declare(lib):
         "b200_set_clusters": [h, C.c_int32],
         "b200_set_owner": [h, C.c_int32],
         "b200_owner_active": [h, _i32p],
+        "b200_set_push": [h, C.c_int32],
+        "b200_push_active": [h, _i32p],
         "b200_set_event_capacity": [h, C.c_double],
         "b200_set_generator": [h, C.c_int32, C.c_int32, _i32p, _i32p, C.c_int64, C.c_int32, C.c_int32],
         "b200_set_rng": [h, C.c_int32, C.POINTER(C.c_uint32), C.c_int32],
@@ -398,6 +400,21 @@ class Network:
         self._check(self.lib.b200_owner_active(self._h, C.byref(a)))
         return bool(a.value)
 
+    def set_push(self, enable=True):
+        """Push-mode delivery: True (where the model allows it), False, or
+        "auto" (the default: on for float32 models with synaptic delays on
+        instances of 2+ CTAs)."""
+        self._check(self.lib.b200_set_push(self._h, 2 if enable == "auto" else int(bool(enable))))
+
+    def push_active(self):
+        a = C.c_int32()
+        self._check(self.lib.b200_push_active(self._h, C.byref(a)))
+        return bool(a.value)
+
+    def delivery_mode(self):
+        """'push', 'owner' or 'classic': the delivery of the current launch plan."""
+        return "push" if self.push_active() else ("owner" if self.owner_active() else "classic")
+
     def set_event_capacity(self, factor):
         self._check(self.lib.b200_set_event_capacity(self._h, float(factor)))
 
@@ -416,7 +433,7 @@ class Network:
         a = np.zeros(n.value, np.uint64)
         self._check(self.lib.b200_get_profile(self._h, int(inst), a.ctypes.data_as(C.POINTER(C.c_uint64)), n.value))
         from .codegen import profile_slots
-        names = profile_slots(self.model.spec, owner=self.owner_active())
+        names = profile_slots(self.model.spec, owner=self.owner_active(), push=self.push_active())
         return {k: int(x) for k, x in zip(names, a) if not k.startswith("unused")}
 
     def set_smem_cache(self, enable=True):

@@ -72,6 +72,19 @@ int b200_launch_plan(b200_net* net, int32_t* grid, int32_t* cluster, int32_t* st
 int b200_set_owner(b200_net* net, int32_t enable);
 int b200_owner_active(b200_net* net, int32_t* active);
 int b200_set_event_capacity(b200_net* net, double factor);
+/* Push-mode delivery (0 off, 1 on where it applies, 2 auto = default: on for
+ * float32 models with synaptic delays on instances of 2+ CTAs).  A third
+ * implementation of CSpikeQueue + on_pre (brian2/synapses/spikequeue.h:14-206,
+ * templates/synapses.cpp:20-49) for models whose on_pre only adds into target
+ * variables and whose delays are all >= 1 step: each CTA delivers the spikes of
+ * the neurons it owns one step ahead into accumulator buffers that the target's
+ * owner adds to its state after the next barrier -- one barrier per step, no
+ * global spike list.  The deliveries of a step are summed before they reach
+ * their variable, so float64 results may differ from the reference in the last
+ * bits (float64 models use it only when asked: 1).  b200_push_active reports
+ * whether the current launch plan uses it; it takes precedence over owner mode. */
+int b200_set_push(b200_net* net, int32_t enable);
+int b200_push_active(b200_net* net, int32_t* active);
 /* Spike generator groups (input/spikegeneratorgroup.py:37-372, stepped by
  * templates/spikegenerator.cpp:5-31): the entries' time bins (sorted, the
  * group's `_timebins`), their neuron indices (`neuron_index`), the period in
