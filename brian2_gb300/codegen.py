@@ -427,9 +427,12 @@ def render_model(spec: dict) -> str:
             return False
         if ptr not in {p_ for _, _, p_ in split_loads(g["update"]["vector"])[0]}:
             return False
-        text = json.dumps(g.get("reset") or {}) + json.dumps(g.get("ops", []))
-        text += json.dumps([inp for inp in INPUTS if inp["group"] == gi])
-        if re.search(r"\b%s\b" % re.escape(ptr), text):
+        # (the code itself, not its JSON form: there a line break is the two
+        # characters \\n, and a pointer starting a line would have no word boundary)
+        codes = [(g.get("reset") or {}).get(k) or "" for k in ("scalar", "vector")]
+        codes += [op["code"].get(k) or "" for op in g.get("ops", []) for k in ("scalar", "vector")]
+        codes += [inp["code"].get(k) or "" for inp in INPUTS if inp["group"] == gi for k in ("scalar", "vector")]
+        if any(re.search(r"(?<![A-Za-z0-9_])%s(?![A-Za-z0-9_])" % re.escape(ptr), c) for c in codes):
             return False
         if any(m["group"] == gi for m in statemons):
             return False  # (its recorded variables are chosen at run time)

@@ -93,9 +93,9 @@ def load_job(directory):
     return spec, init, job
 
 
-def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None, profile=None):
+def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None, profile=None, push=None):
     """Runs a job on the GPU; returns (and writes as out.npz) its outputs.
-    `owner`: delivery mode (True, False, "auto"; None keeps the default);
+    `owner`, `push`: delivery modes (True, False, "auto"; None keeps the default);
     `profile`: record the device profile (None: as the job's options say, set
     by run(profile=True)) -- its slots' SM cycles in prof_names/prof_cycles."""
     from .runtime import Model, Network
@@ -110,6 +110,8 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None,
     net.configure(threads=threads, ctas_per_inst=ctas)
     if owner is not None:
         net.set_owner(owner)
+    if push is not None:
+        net.set_push(push)
     for gi, g in enumerate(spec["groups"]):
         for v in g["vars"] if g.get("alias_of") is None else []:  # (a custom event's group shares them)
             net.upload(0, gi, v["name"], init[f"g{gi}_{v['name']}"])
@@ -165,7 +167,8 @@ def run_job(directory, threads=None, ctas_per_inst=None, write=True, owner=None,
             _report(reports[k], time.time() - t_run, 1.0, (net.step(0) - int(n)) * dt, int(n) * dt)
         apply_actions(job, init, k, download, upload)  # the script's assignments after this run
     out = dict(device_ms=np.float64(total_ms), wall_s=np.float64(time.time() - t0), ts_end=np.int64(net.step(0)),
-               ts0=np.int64(ts0), owner=np.int64(net.owner_active()), kernel_ms=np.float64(kernel_ms))
+               ts0=np.int64(ts0), owner=np.int64(net.owner_active()), kernel_ms=np.float64(kernel_ms),
+               push=np.int64(net.push_active()))
     if profile:
         prof = net.profile(0)
         out["prof_names"] = np.array(list(prof), dtype=str)

@@ -38,6 +38,14 @@ code objects, and executes the spec's *plain* C++ snippets (Brian's own
 * operations (Group.run_regularly): the start slot's before the state
   monitors, the end slot's after the resets, on the steps of their clock.
 
+A spec with ``"push_order": true`` gives the oracle of the device's push-mode
+delivery: every on_pre of a step adds into a per-variable accumulator (zero at
+the start of the step) instead of its target, and after the last pathway each
+target neuron adds its accumulator -- the one change push mode makes to the
+reference's arithmetic (the order of the additions into a target).  For models
+whose increments into one variable are equal within a step, the device's
+push mode reproduces this oracle bit for bit whatever order its atomics take.
+
 Scalar blocks are evaluated every step, as the reference does.  The library is
 built with ``g++ -O2 -ffp-contract=off -fno-fast-math`` (the reference's strict
 build).  It is pinned against fixtures produced by running Brian2 itself
@@ -78,6 +86,10 @@ def render_oracle(spec: dict) -> str:
     consts = spec.get("consts", [])
     clock = spec.get("clock_ptrs", {"dt": "_ptr_array_defaultclock_dt", "t": "_ptr_array_defaultclock_t",
                                      "timestep": "_ptr_array_defaultclock_timestep"})
+    # push order: the variables the pathways deliver into (group, variable)
+    PUSH_ORDER = bool(spec.get("push_order"))
+    ACC = sorted({(gi, vi) for p in paths for _, (gi, vi) in p.get("group_ptrs", {}).items() if gi == p["tgt"]}) \
+        if PUSH_ORDER else []
     o = []
     w = o.append
     w("// oracle for model '%s' (generated; test infrastructure)" % spec["name"])
@@ -169,6 +181,9 @@ def render_oracle(spec: dict) -> str:
         w(f"  int32_t rm{mi}_lo = 0, rm{mi}_hi = 0; std::vector<int32_t> rm{mi}_cnt;")
     for mi, m in enumerate(statemons):
         w(f"  std::vector<int32_t> st{mi}_idx, st{mi}_vars; std::vector<double> st{mi}_data; int64_t st{mi}_n = 0;")
+    for gi, vi in ACC:
+        v = groups[gi]["vars"][vi]
+        w(f"  std::vector<{v['ctype']}> acc_g{gi}_{v['name']};  // push order: the step's deliveries")
     w("};")
     w('extern "C" {')
     w("Net* oracle_create(const int32_t* sizes, double dt) {")
@@ -178,6 +193,8 @@ def render_oracle(spec: dict) -> str:
         w(f"  n->N{gi} = sizes[{gi}];")
         for v in g["vars"]:
             w(f"  n->g{gi}_{v['name']}.assign(sizes[{gi}], 0);")
+    for gi, vi in ACC:
+        w(f"  n->acc_g{gi}_{groups[gi]['vars'][vi]['name']}.assign(sizes[{gi}], 0);")
     for pi, p in enumerate(paths):
         w(f"  n->p{pi}_src_hi = sizes[{p['src']}];")
     for mi, m in enumerate(spkmons):
@@ -503,7 +520,8 @@ def render_oracle(spec: dict) -> str:
             w(f"      {v['ctype']}* const {v['ptr']} = n->p{own}_{v['name']}.data(); (void){v['ptr']};")
         for ptr, (gidx, vidx) in sorted(p.get("group_ptrs", {}).items()):
             v = groups[gidx]["vars"][vidx]
-            w(f"      {v['ctype']}* const {ptr} = n->g{gidx}_{v['name']}.data(); (void){ptr};")
+            arr = "acc_g" if (gidx, vidx) in ACC else "g"
+            w(f"      {v['ctype']}* const {ptr} = n->{arr}{gidx}_{v['name']}.data(); (void){ptr};")
         w("      {")
         w(_ind(p["on_pre"]["scalar"], 8))
         w("        const std::vector<int32_t>& q = Q[off];")
@@ -514,6 +532,9 @@ def render_oracle(spec: dict) -> str:
         w("        }")
         w("      }")
         w("    }")
+    for gi, vi in ACC:  # push order: the step's deliveries reach their targets
+        nm = groups[gi]["vars"][vi]["name"]
+        w(f"    for (int32_t i = 0; i < n->N{gi}; ++i) {{ n->g{gi}_{nm}[i] += n->acc_g{gi}_{nm}[i]; n->acc_g{gi}_{nm}[i] = 0; }}")
     if not inputs_done:
         emit_inputs()
     # resets (a group's and its custom events' in the schedule's order)
@@ -785,12 +806,15 @@ def oracle_from_built(spec, built, dt=1e-4):
     return o
 
 
-def run_job_on_oracle(directory):
+def run_job_on_oracle(directory, push_order=False):
     """Runs a job directory (brian2_gb300/job.py's format) on the oracle; the
-    returned dict has run_job's keys for state, monitors and generator cursors."""
+    returned dict has run_job's keys for state, monitors and generator cursors.
+    push_order: the oracle of the device's push-mode delivery."""
     import json as _json
     with open(os.path.join(directory, "spec.json")) as f:
         spec = _json.load(f)
+    if push_order:
+        spec = dict(spec, push_order=True)
     with open(os.path.join(directory, "job.json")) as f:
         job = _json.load(f)
     with np.load(os.path.join(directory, "init.npz")) as z:
