@@ -132,12 +132,15 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0}, "fallback"
 
 
-def ncu_traffic(K):
+def ncu_traffic(K, kernel="b200_step_kernel"):
     """DRAM bytes per launch (1000 clock steps of the 1e6-neuron network) of the
-    step kernel at in-degree K, from the committed ncu captures at in-degree
-    250 and 500 (profiles/step_kernel_cuba_delays.json; the full-size network
-    is too large for a capture), extrapolated linearly in K; or None."""
-    p = os.path.join(ROOT, "profiles", "step_kernel_cuba_delays.json")
+    step kernel (b200_step_kernel: classic delivery; b200_push_kernel: push
+    mode) at in-degree K, from the committed ncu captures at in-degree 250 and
+    500 (profiles/<kernel>_cuba_delays.json; the full-size network is too large
+    for a capture), extrapolated linearly in K; or None."""
+    name = {"b200_step_kernel": "step_kernel_cuba_delays.json",
+            "b200_push_kernel": "push_kernel_cuba_delays.json"}.get(kernel, "")
+    p = os.path.join(ROOT, "profiles", name)
     try:
         with open(p) as f:
             d = json.load(f)
@@ -547,7 +550,8 @@ def main():
     alg_bytes = 24.0 * N * STEPS_PER_BENCH_STEP + 8.0 * events / args.steps
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     peaks, peak_kind = measured_peaks()
-    traffic = ncu_traffic(K) if N == N_NEURONS else None  # (captured on the 1e6-neuron network)
+    kernel_name = {"push": "b200_push_kernel", "owner": "b200_owner_kernel"}.get(net_mode, "b200_step_kernel")
+    traffic = ncu_traffic(K, kernel_name) if N == N_NEURONS else None  # (captured on the 1e6-neuron network)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "peak_kind": peak_kind,
                 "traffic": traffic,
@@ -555,7 +559,7 @@ def main():
                 "dram_frac": traffic / (launch_ms * 1e-3) / 1e9 / peaks["hbm_gbs"] if traffic else None,
                 "traffic_note": "ncu DRAM bytes at in-degree 250 and 500, extrapolated linearly to this in-degree; "
                                 "the neuron state mostly stays in L2, so DRAM traffic is below the algorithmic bytes",
-                "kernel": "b200_step_kernel", "ms_per_launch": launch_ms,
+                "kernel": kernel_name, "ms_per_launch": launch_ms,
                 "algorithmic_bytes_per_launch": alg_bytes}
 
     # end to end through the public API: every step uploads the state from

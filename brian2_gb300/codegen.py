@@ -3143,6 +3143,28 @@ def render_model(spec: dict) -> str:
 
         NMON = NSM_ + NRM_
 
+        def emit_monitor_raw_loads(sexpr, ind):
+            """Late monitors: the counts of step sexpr loaded into registers (_xr,
+            two per thread and monitor) and summed only when the monitors run, so
+            the round trip overlaps the step; more CTAs than two per thread: summed
+            at once."""
+            sp = " " * ind
+            if not NMON:
+                return
+            w(sp + "if (I.n_cta <= 2 * (int)blockDim.x) {")
+            w(sp + f"  const int xb = (int)(({sexpr}) % 3) * I.n_cta;")
+            w(sp + "#pragma unroll")
+            w(sp + "  for (int u = 0; u < 2; ++u) {")
+            w(sp + "    const int c = (int)threadIdx.x + u * (int)blockDim.x;")
+            for mi in range(NSM_):
+                w(sp + f"    _xr[{mi}][u] = c < I.n_cta ? I.sm[{mi}].xcnt[xb + c] : 0;")
+            for ri in range(NRM_):
+                w(sp + f"    _xr[{NSM_ + ri}][u] = c < I.n_cta ? I.rm[{ri}].xcnt[xb + c] : 0;")
+            w(sp + "  }")
+            w(sp + "} else {")
+            emit_monitor_counts(sexpr, ind + 2)
+            w(sp + "}")
+
         def emit_monitor_counts(sexpr, ind):
             """Each thread's share of all CTAs' counts of step sexpr (written
             before that step's barrier): into bf (CTAs before this one) and tt
@@ -3164,13 +3186,22 @@ def render_model(spec: dict) -> str:
         def emit_monitors(sexpr, ind, counts=True):
             """The spike and rate monitors of step sexpr: every CTA writes its own
             spikes after those of the CTAs before it (counts: load the counts
-            here; otherwise emit_monitor_counts filled bf/tt earlier)."""
+            here; otherwise emit_monitor_raw_loads loaded them earlier)."""
             sp = " " * ind
             if not NMON:
                 return
             nmon = NMON
             if counts:
                 emit_monitor_counts(sexpr, ind)
+            else:
+                w(sp + "if (I.n_cta <= 2 * (int)blockDim.x) {  // the counts loaded after the barrier")
+                w(sp + f"  for (int m = 0; m < {NMON}; ++m) {{ bf[m] = 0; tt[m] = 0; }}")
+                w(sp + "#pragma unroll")
+                w(sp + "  for (int u = 0; u < 2; ++u) {")
+                w(sp + "    const int c = (int)threadIdx.x + u * (int)blockDim.x;")
+                w(sp + f"    for (int m = 0; m < {NMON}; ++m) {{ tt[m] += _xr[m][u]; if (c < rank) bf[m] += (m < {NSM_}) ? _xr[m][u] : 0; }}")
+                w(sp + "  }")
+                w(sp + "}")
             w(sp + "{")
             w(sp + f"  for (int m = 0; m < {nmon}; ++m) {{")
             w(sp + "#pragma unroll")
@@ -3208,7 +3239,8 @@ def render_model(spec: dict) -> str:
             w(sp + "}")
 
         w(f"    int bf[{max(NMON, 1)}], tt[{max(NMON, 1)}];  // monitors: this thread's share of the CTAs' counts")
-        w("    (void)bf; (void)tt;")
+        w(f"    int _xr[{max(NMON, 1)}][2];  // (late monitors: the counts as loaded)")
+        w("    (void)bf; (void)tt; (void)_xr;")
         w("    for (; ts < ts_stop; ++ts) {")
         w("      if (threadIdx.x == 0) {")
         w("        int st = 0;")
@@ -3223,7 +3255,7 @@ def render_model(spec: dict) -> str:
         w("        if (!b200_owner_wait(I, ts - 1, limit_ns, cluster)) { ok = false; break; }")
         w("        B200_PHASE(1);")
         if LATE:
-            emit_monitor_counts("ts - 1", 8)  # (their round trip overlaps the fold and the step)
+            emit_monitor_raw_loads("ts - 1", 8)  # (their round trip overlaps the fold and the step)
         emit_fold("ts - 1", 8, all_vars=False)
         if not LATE:
             emit_monitors("ts - 1", 8)
