@@ -2245,7 +2245,7 @@ def render_model(spec: dict) -> str:
                     w(sp + f"        SM.ts[pos] = (int32_t)({tsexpr});")
                     if m.get("vars"):
                         w(sp + "        " + value_rows(mi, gi, "pos", "idx"))
-                    w(sp + "        SM.count[idx - SM.lo] += 1;")
+                    w(sp + "        atomicAdd(&SM.count[idx - SM.lo], 1);  // (no read round trip)")
                     w(sp + "      }")
                     w(sp + "    }")
                     w(sp + "    __syncthreads();")
@@ -2888,16 +2888,17 @@ def render_model(spec: dict) -> str:
         neurons to their state and clears it.  Three buffers, because a CTA
         starts the deliveries due at ts+2 before the slowest CTA has cleared the
         buffer of the deliveries due at ts.  A step is: wait for step ts-1 ->
-        fold -> monitors of step ts-1 -> phase A (as the owner kernel: deferred
-        reset, operations, state monitors, update, threshold) -> spike bounds and
-        monitor counts of step ts -> arrive -> deliveries due at ts+1.  The
+        fold -> phase A (as the owner kernel: deferred reset, operations, state
+        monitors, update, threshold) -> spike bounds and monitor counts of step
+        ts -> arrive -> monitors of step ts-1 -> deliveries due at ts+1.  The
         only change against the reference's order is the order of the additions
         into a variable (the deliveries of a step are summed before they reach it)."""
         ACCI = {gv: k for k, gv in enumerate(ACC)}
         NSM_, NRM_ = len(spkmons), len(ratemons)
-        # monitors of step ts-1 written after the deliveries of step ts (in the
-        # barrier's slack) unless a spike monitor records variables: their
-        # per-neuron snapshot of step ts-1 is overwritten by step ts's thresholder
+        # monitors of step ts-1 written after step ts's arrival (their counts, loaded
+        # after the barrier, have arrived by then) unless a spike monitor records
+        # variables: their per-neuron snapshot of step ts-1 is overwritten by step
+        # ts's thresholder
         LATE = not any(m.get("vars") for m in spkmons)
 
         def pathway_window(kexpr, ind):
@@ -2969,7 +2970,7 @@ def render_model(spec: dict) -> str:
         w("  __shared__ int32_t* s_hcnt[B200_NG];   // its spikes per slot")
         w(f"  __shared__ int2* s_pb[{max(NP, 1)}];   // per slot, the bounds of the spikes in a pathway's source range")
         w(f"  __shared__ int s_mb[{max(NSM_, 1)}][2][2];   // per step parity: the recorded spikes not yet written")
-        w(f"  __shared__ int s_red[{2 * max(NSM_ + NRM_, 1)}];")
+        w(f"  __shared__ int s_red[2][{2 * max(NSM_ + NRM_, 1)}];  // monitors' block sums, by step parity")
         for gi in range(NG):
             n_ = max(gtables[gi][0].size, 1)
             w(f"  __shared__ double s_Sg{gi}[{n_}]; __shared__ float s_Sg{gi}f[{n_}]; __shared__ long long s_Sg{gi}i[{n_}];")
@@ -3207,16 +3208,17 @@ def render_model(spec: dict) -> str:
             w(sp + "#pragma unroll")
             w(sp + "    for (int o = 16; o >= 1; o >>= 1) { bf[m] += __shfl_down_sync(0xffffffffu, bf[m], o); tt[m] += __shfl_down_sync(0xffffffffu, tt[m], o); }")
             w(sp + "  }")
-            w(sp + f"  if (threadIdx.x < {2 * nmon}) s_red[threadIdx.x] = 0;")
-            w(sp + "  __syncthreads();")
-            w(sp + f"  if (lane == 0) for (int m = 0; m < {nmon}; ++m) {{ atomicAdd(&s_red[2 * m], bf[m]); atomicAdd(&s_red[2 * m + 1], tt[m]); }}")
+            # one block barrier: the sums of step parity p go to s_red[p], which the
+            # previous step cleared (its readers are past a barrier by then)
+            w(sp + f"  const int _rp = (int)(({sexpr}) & 1);")
+            w(sp + f"  if (lane == 0) for (int m = 0; m < {nmon}; ++m) {{ atomicAdd(&s_red[_rp][2 * m], bf[m]); atomicAdd(&s_red[_rp][2 * m + 1], tt[m]); }}")
             w(sp + "  __syncthreads();")
             for mi, m in enumerate(spkmons):
                 gi = m["group"]
                 w(sp + f"  {{  // spike monitor {mi}")
                 w(sp + f"    const b200_spkmon_d& SM = I.sm[{mi}];")
                 w(sp + f"    const int sl = (int)(({sexpr}) % I.g[{gi}].RH);")
-                w(sp + f"    const long long mbase = s_mon_n[{mi}] + s_red[{2 * mi}];")
+                w(sp + f"    const long long mbase = _mn[{mi}] + s_red[_rp][{2 * mi}];")
                 w(sp + f"    const int mpar = (int)(({sexpr}) & 1);")
                 w(sp + f"    for (int j = threadIdx.x; j < s_mb[{mi}][mpar][1]; j += blockDim.x) {{")
                 w(sp + f"      const int idx = {list_elem(gi, 'sl', f's_mb[{mi}][mpar][0] + j')};")
@@ -3225,22 +3227,27 @@ def render_model(spec: dict) -> str:
                 w(sp + f"      SM.ts[pos] = (int32_t)({sexpr});")
                 if m.get("vars"):
                     w(sp + "      " + value_rows(mi, gi, "pos", "idx"))
-                w(sp + "      SM.count[idx - SM.lo] += 1;")
+                w(sp + "      atomicAdd(&SM.count[idx - SM.lo], 1);  // no read round trip (own neurons: uncontended)")
                 w(sp + "    }")
                 w(sp + "  }")
             for ri, m in enumerate(ratemons):
-                w(sp + f"  if (rank == 0 && threadIdx.x == 0) I.rm[{ri}].cnt[({sexpr}) - I.rm[{ri}].step0] = s_red[{2 * (NSM_ + ri) + 1}];")
-            w(sp + "  __syncthreads();")
-            w(sp + "  if (threadIdx.x == 0) {")
+                w(sp + f"  if (rank == 0 && threadIdx.x == 0) I.rm[{ri}].cnt[({sexpr}) - I.rm[{ri}].step0] = s_red[_rp][{2 * (NSM_ + ri) + 1}];")
+            # every thread keeps the spike monitors' running totals; thread 0 also in
+            # shared memory (its capacity check and the write-back at the end)
             for mi in range(NSM_):
-                w(sp + f"    s_mon_n[{mi}] += s_red[{2 * mi + 1}];")
-            w(sp + "  }")
-            w(sp + "  __syncthreads();")
+                w(sp + f"  _mn[{mi}] += s_red[_rp][{2 * mi + 1}];")
+                w(sp + f"  if (threadIdx.x == 0) s_mon_n[{mi}] = _mn[{mi}];")
+            w(sp + f"  if (threadIdx.x < {2 * nmon}) s_red[_rp ^ 1][threadIdx.x] = 0;  // for the next step")
             w(sp + "}")
 
         w(f"    int bf[{max(NMON, 1)}], tt[{max(NMON, 1)}];  // monitors: this thread's share of the CTAs' counts")
         w(f"    int _xr[{max(NMON, 1)}][2];  // (late monitors: the counts as loaded)")
         w("    (void)bf; (void)tt; (void)_xr;")
+        w(f"    long long _mn[{max(NSM_, 1)}];  // the spike monitors' totals (every thread)")
+        for mi in range(NSM_):
+            w(f"    _mn[{mi}] = s_mon_n[{mi}];")
+        w(f"    if (threadIdx.x < {4 * max(NSM_ + NRM_, 1)}) (&s_red[0][0])[threadIdx.x] = 0;")
+        w("    __syncthreads();")
         w("    for (; ts < ts_stop; ++ts) {")
         w("      if (threadIdx.x == 0) {")
         w("        int st = 0;")
@@ -3312,6 +3319,13 @@ def render_model(spec: dict) -> str:
         w("      if (rank == fault_rank && ts == ts0) { ok = false; break; }")
         w("      b200_owner_arrive(I, cluster);  // (its __syncthreads orders the bounds above)")
         w("      B200_PHASE(2);")
+        if LATE:
+            # right after the arrival: no atomics of this CTA are queued yet, so its
+            # stores are not held behind them (after the deliveries they were)
+            w("      if (ts > ts0) {  // the monitors of step ts-1")
+            emit_monitors("ts - 1", 8, counts=False)
+            w("      }")
+            w("      B200_PHASE(5);")
         # ---------------------------------------------- deliveries due at ts + 1
         w("      {  // deliveries due at ts+1: this CTA's spikes of steps ts+1-d, d = dmin..D")
         w("        const int64_t tn = ts + 1;")
@@ -3456,11 +3470,7 @@ def render_model(spec: dict) -> str:
         w("        }")
         w("      }")
         w("      B200_PHASE(4);")
-        if LATE:
-            w("      if (ts > ts0) {  // the monitors of step ts-1, in the slack before the barrier")
-            emit_monitors("ts - 1", 8, counts=False)
-            w("      }")
-            w("      B200_PHASE(5);")
+
         w("    }  // steps")
         w(f"    if (prof && threadIdx.x == 0)")
         w(f"      for (int q = 0; q < {NPH}; ++q) atomicAdd(&prof[(size_t)unit * {NPH} + q], _pacc[q]);")
