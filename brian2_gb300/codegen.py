@@ -2763,7 +2763,9 @@ def render_model(spec: dict) -> str:
                 L.append(gptr_decls(gi, 0, True))
             for ptr, a in fz.items():
                 L.append(f"{pf[ptr]}* const _facc{pfi[ptr]} = ({pf[ptr]}*)I.acc[{a}] + (size_t)((ts + 2) % B200_PUSH_BUFS) * I.g[{gi}].N;")
-            L.append("constexpr int NS = (MAXT * MINB < 1024) ? 16 : 4;  // slices per chunk")
+            # (8: no register spills at 128 registers a thread, whose L1 traffic cost more
+            # than the second round trip of a longer run)
+            L.append("constexpr int NS = (MAXT * MINB < 1024) ? 8 : 4;  // slices per chunk")
             L.append("for (int _c0 = _a; _c0 < _b; _c0 += 32 * NS) {")
             for ptr in fz:
                 L.append(f"  {pf[ptr]} _d{pfi[ptr]}[NS];")
